@@ -1,0 +1,145 @@
+/*
+ * lsdtt_gb300.h -- C ABI of the GB300 (sm_103a) backend for the lsdtt3
+ * landscape-evolution timestep hot path.
+ *
+ * Every entry point takes plain pointers and sizes, returns an int status
+ * (LSDTT_GPU_OK == 0) and never throws. Pointers named *_dev are device
+ * pointers (cudaMalloc'd or from any allocator on the current device);
+ * pointers named *_host are host pointers. `stream` is a cudaStream_t passed
+ * as void* (NULL = the legacy default stream). Calls on one handle are not
+ * thread safe; distinct handles may be used from distinct threads.
+ *
+ * The message of the last failing call on the calling thread is returned by
+ * lsdtt_gpu_last_error(); it is the reference's exception text where the
+ * reference throws (e.g. "lsdtt_flowinfo: could not assign a receiver at row
+ * R, col C. The DEM likely contains an unresolved sink or flat.").
+ *
+ * There is no CPU fallback: with no usable device every call returns
+ * LSDTT_GPU_ENODEV.
+ *
+ * Reference paths are relative to the lsdtt3 checkout.
+ */
+#ifndef LSDTT_GB300_H
+#define LSDTT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes -------------------------------------------------------- */
+enum lsdtt_gpu_status
+{
+    LSDTT_GPU_OK = 0,
+    LSDTT_GPU_ENODEV = 1,      /* no CUDA device / driver                      */
+    LSDTT_GPU_ENOMEM = 2,      /* device allocation failed                     */
+    LSDTT_GPU_EINVAL = 3,      /* bad argument (message names it)              */
+    LSDTT_GPU_EUNRESOLVED = 4, /* unresolved sink: message carries (row, col)  */
+    LSDTT_GPU_ECYCLIC = 5,     /* routing graph cyclic or incomplete           */
+    LSDTT_GPU_ENOCONV = 6,     /* iterative solve did not converge             */
+    LSDTT_GPU_ETIMEOUT = 7,    /* a bounded device wait gave up                */
+    LSDTT_GPU_ECUDA = 8,       /* CUDA runtime error (message has the text)    */
+    LSDTT_GPU_EOVERFLOW = 9,   /* a device work list exceeded its capacity     */
+    LSDTT_GPU_ESTATE = 10      /* handle not built / component not available   */
+};
+
+/* ---- grid ---------------------------------------------------------------- */
+/* lsdtt_raster_meta (src/core/lsdtt_raster_meta.hpp) reduced to what the path
+ * reads, plus the NESW boundary string ('o' open, 'n' no-flux, 'p' periodic,
+ * 'b' base level). */
+typedef struct lsdtt_gpu_grid
+{
+    int32_t n_rows;
+    int32_t n_cols;
+    double cell_size;
+    double no_data_value;
+    char boundary_conditions[4];
+} lsdtt_gpu_grid;
+
+int lsdtt_gpu_device_available(void);
+const char* lsdtt_gpu_last_error(void);
+const char* lsdtt_gpu_version(void);
+
+/* ---- fill ----------------------------------------------------------------
+ * Replaces fill_pits(const lsdtt_raster_cpu&, float min_slope,
+ * const std::string& bc, int n_threads, priority_flood_queue_backend)
+ * (src/cpu/lsdtt_raster_flow_preprocessing_cpu.hpp:191-199,
+ *  .cpp:727-782). Output cells that are masked or nodata hold no_data_value. */
+int lsdtt_gpu_fill_pits(const lsdtt_gpu_grid* grid, const float* z_dev, const uint8_t* mask_dev,
+                        float min_slope, float* filled_dev, void* stream);
+
+/* ---- D8 engine (lsdtt_flowinfo) ------------------------------------------
+ * Replaces lsdtt_flowinfo(dem, mask, meta, options) and the lsdtt_flow_base
+ * queries built on it (src/core/lsdtt_flow_base.hpp:126-491,
+ * src/cpu/lsdtt_flowinfo_cpu.cpp:197-253). The engine owns its device arrays;
+ * build() may be called again with new elevations of the same grid. */
+typedef struct lsdtt_gpu_flow_options
+{
+    int32_t interior_nodata_is_outlet; /* default 1 */
+    int32_t require_acyclic_graph;     /* default 1 */
+    int32_t build_topological_order;   /* default 1 */
+    int32_t build_s_vector;            /* default 1 */
+    int32_t allow_pits_as_outlets;     /* default 0 */
+} lsdtt_gpu_flow_options;
+
+typedef struct lsdtt_gpu_flow lsdtt_gpu_flow;
+
+typedef struct lsdtt_gpu_flow_view
+{
+    const int64_t* receiver;          /* [n]  -1 nodata, -2 outlet              */
+    const uint8_t* direction;         /* [n]  0..7, 255 none                     */
+    const uint8_t* donor_count;       /* [n]                                     */
+    const int64_t* outlets;           /* [n_outlets] row-major                   */
+    const int64_t* topological_order; /* [n_valid] or NULL when not kept         */
+    const int64_t* s_vector;          /* [n_valid] or NULL when not built        */
+    const int64_t* s_vector_start;    /* [n] (-1 for nodata) or NULL             */
+    const uint64_t* s_vector_size;    /* [n] contributing-cell counts or NULL    */
+    int64_t n_cells;
+    int64_t n_valid_cells;
+    int64_t n_outlets;
+    int32_t is_acyclic;
+    int32_t has_topological_order;
+    int32_t has_s_vector;
+    int32_t reserved;
+} lsdtt_gpu_flow_view;
+
+int lsdtt_gpu_flow_create(const lsdtt_gpu_grid* grid, lsdtt_gpu_flow** out);
+int lsdtt_gpu_flow_destroy(lsdtt_gpu_flow* flow);
+int lsdtt_gpu_flow_build(lsdtt_gpu_flow* flow, const float* z_dev, const uint8_t* mask_dev,
+                         const lsdtt_gpu_flow_options* options, const int64_t* forced_outlets_dev,
+                         int64_t n_forced, void* stream);
+int lsdtt_gpu_flow_get_view(const lsdtt_gpu_flow* flow, lsdtt_gpu_flow_view* view);
+
+/* lsdtt_flowinfo::accumulate(cell_weights) (src/cpu/lsdtt_flowinfo_cpu.cpp:
+ * 1979-2046): weights_dev NULL = cell_size^2 on every valid cell. Bitwise the
+ * reference's forward push in topological order. */
+int lsdtt_gpu_flow_accumulate(lsdtt_gpu_flow* flow, const double* weights_dev, double* out_dev,
+                              void* stream);
+
+/* ---- stream power ---------------------------------------------------------
+ * compute_d8_stream_power_incision (src/cpu/lsdtt_stream_power_cpu.hpp:74-89,
+ * .cpp:159-326) on a built engine, moving-average kernel 1 and no width
+ * correction. k_field_dev may be NULL (scalar K). */
+int lsdtt_gpu_stream_power_d8(lsdtt_gpu_flow* flow, const float* z_dev, const float* k_field_dev,
+                              float K, float m, float n, float dt, float incision_threshold_area,
+                              int32_t divide_area_by_dx, float slope_clamp, float* z_out_dev,
+                              void* stream);
+
+/* ---- whole routing pass with host buffers ---------------------------------
+ * fill_pits(z, min_slope, bc) then lsdtt_flowinfo on the filled surface, then
+ * the results copied back: filled elevations, int64 receivers, topological
+ * order and contributing-cell counts (s_vector_size). Any output pointer may
+ * be NULL to skip that copy. This is the call a host-side caller (CLI,
+ * Python binding) makes; it keeps one engine per grid shape internally. */
+int lsdtt_gpu_route_host(const lsdtt_gpu_grid* grid, const float* z_host, const uint8_t* mask_host,
+                         float min_slope, const lsdtt_gpu_flow_options* options, float* filled_host,
+                         int64_t* receiver_host, int64_t* topo_host, uint64_t* counts_host,
+                         void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LSDTT_GB300_H */

@@ -1,0 +1,267 @@
+"""lsdtt_gb300 -- GB300 (sm_103a) backend for the lsdtt3 landscape-evolution
+timestep hot path.
+
+This module is the Python face of the C ABI in include/lsdtt_gb300.h. It
+mirrors the reference's own Python surface for the path (lsdtt3.FlowInfo,
+lsdtt3.fill_pits, LandscapeModel.step; python_bindings/bindings/flow_info.cpp,
+raster_pit_processing.cpp, landscape_model.cpp) with the same argument
+meaning and the same error messages, and keeps every array in device memory.
+PyTorch supplies device allocation and streams; all computation happens in
+liblsdtt_gb300.so. There is no CPU fallback: importing works anywhere, but
+every call fails loudly when the library or a CUDA device is missing.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import Optional, Sequence
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liblsdtt_gb300.so")
+
+# status codes (include/lsdtt_gb300.h)
+OK, ENODEV, ENOMEM, EINVAL, EUNRESOLVED, ECYCLIC, ENOCONV, ETIMEOUT, ECUDA, EOVERFLOW, ESTATE = range(11)
+
+
+class GpuError(RuntimeError):
+    """A non-zero status from the library. `status` is the C status code and
+    the message is the reference's exception text where the reference throws."""
+
+    def __init__(self, status: int, message: str):
+        super().__init__(message)
+        self.status = status
+
+
+class Grid(ctypes.Structure):
+    _fields_ = [("n_rows", ctypes.c_int32), ("n_cols", ctypes.c_int32), ("cell_size", ctypes.c_double),
+                ("no_data_value", ctypes.c_double), ("boundary_conditions", ctypes.c_char * 4)]
+
+
+class FlowOptions(ctypes.Structure):
+    _fields_ = [("interior_nodata_is_outlet", ctypes.c_int32), ("require_acyclic_graph", ctypes.c_int32),
+                ("build_topological_order", ctypes.c_int32), ("build_s_vector", ctypes.c_int32),
+                ("allow_pits_as_outlets", ctypes.c_int32)]
+
+
+class FlowView(ctypes.Structure):
+    _fields_ = [("receiver", ctypes.c_void_p), ("direction", ctypes.c_void_p), ("donor_count", ctypes.c_void_p),
+                ("outlets", ctypes.c_void_p), ("topological_order", ctypes.c_void_p), ("s_vector", ctypes.c_void_p),
+                ("s_vector_start", ctypes.c_void_p), ("s_vector_size", ctypes.c_void_p), ("n_cells", ctypes.c_int64),
+                ("n_valid_cells", ctypes.c_int64), ("n_outlets", ctypes.c_int64), ("is_acyclic", ctypes.c_int32),
+                ("has_topological_order", ctypes.c_int32), ("has_s_vector", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
+
+
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    """The loaded liblsdtt_gb300.so; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with `python -m lsdtt_gb300.build`")
+        L = ctypes.CDLL(LIB_PATH)
+        vp, i32, i64, f32 = ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, ctypes.c_float
+        L.lsdtt_gpu_last_error.restype = ctypes.c_char_p
+        L.lsdtt_gpu_version.restype = ctypes.c_char_p
+        L.lsdtt_gpu_device_available.restype = ctypes.c_int
+        for name, args in {
+            "lsdtt_gpu_fill_pits": [ctypes.POINTER(Grid), vp, vp, f32, vp, vp],
+            "lsdtt_gpu_flow_create": [ctypes.POINTER(Grid), ctypes.POINTER(vp)],
+            "lsdtt_gpu_flow_destroy": [vp],
+            "lsdtt_gpu_flow_build": [vp, vp, vp, ctypes.POINTER(FlowOptions), vp, i64, vp],
+            "lsdtt_gpu_flow_get_view": [vp, ctypes.POINTER(FlowView)],
+            "lsdtt_gpu_flow_accumulate": [vp, vp, vp, vp],
+            "lsdtt_gpu_stream_power_d8": [vp, vp, vp, f32, f32, f32, f32, f32, i32, f32, vp, vp],
+            "lsdtt_gpu_route_host": [ctypes.POINTER(Grid), vp, vp, f32, ctypes.POINTER(FlowOptions), vp, vp, vp, vp,
+                                     vp],
+        }.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = ctypes.c_int
+        _lib = L
+    return _lib
+
+
+def _check(status: int):
+    if status != OK:
+        raise GpuError(status, lib().lsdtt_gpu_last_error().decode())
+
+
+def _torch():
+    import torch
+    if not torch.cuda.is_available():
+        raise GpuError(ENODEV, "lsdtt_gb300: no CUDA device")
+    return torch
+
+
+def _dev(a, dtype):
+    """Device tensor view/copy of a numpy array or tensor, contiguous."""
+    torch = _torch()
+    if isinstance(a, torch.Tensor):
+        t = a.to(device="cuda", dtype=dtype)
+    else:
+        t = torch.from_numpy(np.ascontiguousarray(a)).to(device="cuda", dtype=dtype)
+    return t.contiguous()
+
+
+def _stream(stream):
+    torch = _torch()
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+def make_grid(n_rows: int, n_cols: int, cell_size: float, boundary_conditions: str = "oooo",
+              no_data_value: float = -9999.0) -> Grid:
+    bc = (boundary_conditions or "")
+    if len(bc) != 4:
+        raise GpuError(EINVAL, "lsdtt_flowinfo: boundary_conditions must have length 4 (north, east, south, west)")
+    return Grid(int(n_rows), int(n_cols), float(cell_size), float(no_data_value), bc.encode())
+
+
+def fill_pits(z, mask, cell_size: float, boundary_conditions: str = "oooo", min_slope: float = 1e-4,
+              no_data_value: float = -9999.0, out=None, stream=None):
+    """fill_pits(raster, min_slope, bc) on the GPU. Returns a float32 CUDA
+    tensor; masked/nodata cells hold no_data_value."""
+    torch = _torch()
+    zt = _dev(z, torch.float32)
+    mt = _dev(mask, torch.uint8)
+    nr, nc = zt.shape
+    g = make_grid(nr, nc, cell_size, boundary_conditions, no_data_value)
+    if out is None:
+        out = torch.empty_like(zt)
+    _check(lib().lsdtt_gpu_fill_pits(ctypes.byref(g), ctypes.c_void_p(zt.data_ptr()), ctypes.c_void_p(mt.data_ptr()),
+                                     ctypes.c_float(min_slope), ctypes.c_void_p(out.data_ptr()), _stream(stream)))
+    return out
+
+
+class FlowInfo:
+    """The D8 engine (lsdtt_flowinfo) on the GPU.
+
+    Same constructor options as lsdtt_flowinfo_options
+    (src/core/lsdtt_flow_base.hpp:79-111). Array accessors return CUDA
+    tensors that stay valid until the next build() or close()."""
+
+    def __init__(self, z, mask, cell_size: float, boundary_conditions: str = "oooo", *,
+                 interior_nodata_is_outlet: bool = True, require_acyclic_graph: bool = True,
+                 build_topological_order: bool = True, build_s_vector: bool = True,
+                 allow_pits_as_outlets: bool = False, forced_outlet_flats: Sequence[int] = (),
+                 no_data_value: float = -9999.0, stream=None):
+        torch = _torch()
+        zt = _dev(z, torch.float32)
+        nr, nc = zt.shape
+        self.shape = (nr, nc)
+        self.cell_size = float(cell_size)
+        self.grid = make_grid(nr, nc, cell_size, boundary_conditions, no_data_value)
+        h = ctypes.c_void_p()
+        _check(lib().lsdtt_gpu_flow_create(ctypes.byref(self.grid), ctypes.byref(h)))
+        self._h = h
+        self.options = FlowOptions(int(interior_nodata_is_outlet), int(require_acyclic_graph),
+                                   int(build_topological_order), int(build_s_vector), int(allow_pits_as_outlets))
+        self._forced = forced_outlet_flats
+        self.build(zt, mask, stream=stream)
+
+    def build(self, z, mask, stream=None):
+        torch = _torch()
+        zt = _dev(z, torch.float32)
+        mt = _dev(mask, torch.uint8)
+        forced = None
+        nf = 0
+        if self._forced is not None and len(self._forced):
+            forced = _dev(np.asarray(self._forced, np.int64), torch.int64)
+            nf = forced.numel()
+        self._keep = (zt, mt, forced)
+        _check(lib().lsdtt_gpu_flow_build(self._h, ctypes.c_void_p(zt.data_ptr()), ctypes.c_void_p(mt.data_ptr()),
+                                          ctypes.byref(self.options),
+                                          ctypes.c_void_p(forced.data_ptr() if forced is not None else 0),
+                                          ctypes.c_int64(nf), _stream(stream)))
+        v = FlowView()
+        _check(lib().lsdtt_gpu_flow_get_view(self._h, ctypes.byref(v)))
+        self.view = v
+        return self
+
+    # -- array views ----------------------------------------------------
+    def _wrap(self, ptr, count, dtype):
+        """Zero-copy CUDA tensor over an engine-owned device array."""
+        torch = _torch()
+        if not ptr:
+            return None
+        return torch.as_tensor(_DeviceArray(ptr, int(count), dtype), device="cuda")
+
+    def receiver(self):
+        return self._wrap(self.view.receiver, self.view.n_cells, _torch().int64)
+
+    def direction(self):
+        return self._wrap(self.view.direction, self.view.n_cells, _torch().uint8)
+
+    def donor_count(self):
+        return self._wrap(self.view.donor_count, self.view.n_cells, _torch().uint8)
+
+    def outlets(self):
+        return self._wrap(self.view.outlets, self.view.n_outlets, _torch().int64)
+
+    def topological_order(self):
+        if not self.view.has_topological_order:
+            raise GpuError(ESTATE, "topological_order not built - set build_topological_order = true in "
+                                   "lsdtt_flowinfo_options")
+        return self._wrap(self.view.topological_order, self.view.n_valid_cells, _torch().int64)
+
+    def s_vector(self):
+        self._need_sv()
+        return self._wrap(self.view.s_vector, self.view.n_valid_cells, _torch().int64)
+
+    def s_vector_start(self):
+        self._need_sv()
+        return self._wrap(self.view.s_vector_start, self.view.n_cells, _torch().int64)
+
+    def s_vector_size(self):
+        self._need_sv()
+        t = self._wrap(self.view.s_vector_size, self.view.n_cells, _torch().int64)
+        return t  # uint64 counts (never above 2^63)
+
+    def _need_sv(self):
+        if not self.view.has_s_vector:
+            raise GpuError(ESTATE, "s_vector not built - set build_s_vector = true in lsdtt_flowinfo_options")
+
+    def has_topological_order(self):
+        return bool(self.view.has_topological_order)
+
+    def has_s_vector(self):
+        return bool(self.view.has_s_vector)
+
+    def n_valid_cells(self):
+        return int(self.view.n_valid_cells)
+
+    def accumulate(self, weights=None, stream=None):
+        """lsdtt_flowinfo::accumulate(cell_weights): float64 CUDA tensor."""
+        torch = _torch()
+        out = torch.empty(self.view.n_cells, dtype=torch.float64, device="cuda")
+        w = None if weights is None else _dev(weights, torch.float64).reshape(-1)
+        _check(lib().lsdtt_gpu_flow_accumulate(self._h, ctypes.c_void_p(w.data_ptr() if w is not None else 0),
+                                               ctypes.c_void_p(out.data_ptr()), _stream(stream)))
+        return out
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().lsdtt_gpu_flow_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class _DeviceArray:
+    """__cuda_array_interface__ holder for a raw device pointer."""
+
+    _TYPESTR = {"torch.int64": "<i8", "torch.uint8": "|u1", "torch.float32": "<f4", "torch.float64": "<f8",
+                "torch.int32": "<i4"}
+
+    def __init__(self, ptr, count, dtype):
+        self.__cuda_array_interface__ = {"shape": (count,), "typestr": self._TYPESTR[str(dtype)],
+                                         "data": (int(ptr), False), "version": 3, "strides": None}

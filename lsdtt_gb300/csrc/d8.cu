@@ -1,0 +1,275 @@
+// d8.cu -- D8 steepest-descent receivers, donor counts and the outlet list.
+//
+// Receivers restate build_receiver_graph_d8 (src/cpu/lsdtt_flowinfo_cpu.cpp:
+// 1077-1329): for each valid cell the steepest downhill neighbour, slope
+// (double)z - (double)z_nb over dx or dx*sqrt(2) in double, strict '>' so the
+// first of equal slopes in direction order 0..7 wins.
+//
+// GB300 note: this part has very little FP64 throughput, and a double
+// division per neighbour would make the kernel compute-bound by ~50x. The
+// kernel therefore ranks neighbours with float slopes (relative error below
+// 2^-21 against the exact quotient) and only falls back to the reference's
+// double division when the two best float slopes are within 2^-18 of each
+// other, i.e. when rounding could decide the winner. Outside that band the
+// float ranking provably equals the double ranking, so the result is the
+// reference's bit for bit; inside it the double path IS the reference.
+//
+// Donor counts restate build_donor_counts_and_outlets_d8 (:1359-1408) as a
+// gather: cell c counts the neighbours d whose direction code points back
+// at c. The outlet list is the row-major compaction of valid cells with no
+// receiver.
+
+#include "engine.cuh"
+
+namespace lsdtt_gb300
+{
+namespace
+{
+
+constexpr unsigned kErrUnresolved = 4;
+
+struct Cand
+{
+    float best;
+    float second;
+    int dir;
+    std::int64_t rec;
+};
+
+// Exact reference evaluation for one cell (used for near-ties and for the
+// cells whose float ranking is ambiguous).
+__device__ void exact_receiver(const Grid& g, const float* __restrict__ z, const std::uint8_t* __restrict__ mask,
+                               int row, int col, int& out_dir, std::int64_t& out_rec, bool& allowed_outlet,
+                               int interior_nodata_is_outlet)
+{
+    const std::int64_t flat = static_cast<std::int64_t>(row) * g.nc + col;
+    const double card = g.cell;
+    const double diag = g.cell * 1.4142135623730950488;
+    const float zc = z[flat];
+    double best = 0.0;
+    out_dir = kNoDir;
+    out_rec = kOutletReceiver;
+    allowed_outlet = false;
+    for (int d = 0; d < 8; ++d)
+    {
+        const Step s = resolve_step(g, row, col, d);
+        if (s.kind == 2) { allowed_outlet = true; continue; }
+        if (s.kind == 0) continue;
+        const std::int64_t nf = static_cast<std::int64_t>(s.r) * g.nc + s.c;
+        if (mask[nf] == 0)
+        {
+            if (interior_nodata_is_outlet) allowed_outlet = true;
+            continue;
+        }
+        if (nf == flat) continue;
+        const double dz = static_cast<double>(zc) - static_cast<double>(z[nf]);
+        if (dz <= 0.0) continue;
+        const double slope = __ddiv_rn(dz, (d & 1) ? diag : card);
+        if (slope > best)
+        {
+            best = slope;
+            out_rec = nf;
+            out_dir = d;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) receivers_kernel(Grid g, const float* __restrict__ z,
+                                                        const std::uint8_t* __restrict__ mask,
+                                                        const std::uint8_t* __restrict__ forced,
+                                                        int interior_nodata_is_outlet, int allow_pits,
+                                                        std::int64_t* __restrict__ receiver,
+                                                        std::uint8_t* __restrict__ dir,
+                                                        unsigned long long* __restrict__ err)
+{
+    const int col = blockIdx.x * blockDim.x + threadIdx.x;
+    const int row = blockIdx.y * blockDim.y + threadIdx.y;
+    if (row >= g.nr || col >= g.nc) return;
+    const std::int64_t flat = static_cast<std::int64_t>(row) * g.nc + col;
+    if (mask[flat] == 0)
+    {
+        receiver[flat] = kNodataReceiver;
+        dir[flat] = kNoDir;
+        return;
+    }
+    const bool forced_edge = (row == 0 && g.bc[0] == 'b') || (col == g.nc - 1 && g.bc[1] == 'b') ||
+                             (row == g.nr - 1 && g.bc[2] == 'b') || (col == 0 && g.bc[3] == 'b');
+    if (forced_edge || (forced != nullptr && forced[flat] != 0))
+    {
+        receiver[flat] = kOutletReceiver;
+        dir[flat] = kNoDir;
+        return;
+    }
+    const float zc = z[flat];
+    // Float ranking: weights are 1/dx and 1/(dx*sqrt2) rounded to float.
+    const float inv_card = static_cast<float>(1.0 / g.cell);
+    const float inv_diag = static_cast<float>(1.0 / (g.cell * 1.4142135623730950488));
+    float best = 0.0f, second = 0.0f;
+    int bdir = kNoDir;
+    std::int64_t brec = kOutletReceiver;
+    bool allowed_outlet = false;
+    if (is_interior(g, row, col))
+    {
+#pragma unroll
+        for (int d = 0; d < 8; ++d)
+        {
+            const std::int64_t nf = flat + static_cast<std::int64_t>(d8_dr(d)) * g.nc + d8_dc(d);
+            if (mask[nf] == 0)
+            {
+                if (interior_nodata_is_outlet) allowed_outlet = true;
+                continue;
+            }
+            const float zn = z[nf];
+            if (!(zc > zn)) continue;  // (double)zc - (double)zn <= 0
+            const float s = (zc - zn) * ((d & 1) ? inv_diag : inv_card);
+            if (s > best)
+            {
+                second = best;
+                best = s;
+                bdir = d;
+                brec = nf;
+            }
+            else if (s > second)
+                second = s;
+        }
+    }
+    else
+    {
+        for (int d = 0; d < 8; ++d)
+        {
+            const Step st = resolve_step(g, row, col, d);
+            if (st.kind == 2) { allowed_outlet = true; continue; }
+            if (st.kind == 0) continue;
+            const std::int64_t nf = static_cast<std::int64_t>(st.r) * g.nc + st.c;
+            if (mask[nf] == 0)
+            {
+                if (interior_nodata_is_outlet) allowed_outlet = true;
+                continue;
+            }
+            if (nf == flat) continue;
+            const float zn = z[nf];
+            if (!(zc > zn)) continue;
+            const float s = (zc - zn) * ((d & 1) ? inv_diag : inv_card);
+            if (s > best)
+            {
+                second = best;
+                best = s;
+                bdir = d;
+                brec = nf;
+            }
+            else if (s > second)
+                second = s;
+        }
+    }
+    // Ambiguous when the runner-up is within 2^-18 (relative) of the winner,
+    // or when float arithmetic lost the plot (non-finite, underflow to 0).
+    const bool ambiguous = (bdir != kNoDir) &&
+                           (!(best < 3.0e38f) || !(best > 1.0e-30f) || second * (1.0f + 3.814697265625e-06f) >= best);
+    if (ambiguous)
+        exact_receiver(g, z, mask, row, col, bdir, brec, allowed_outlet, interior_nodata_is_outlet);
+    if (bdir != kNoDir)
+    {
+        receiver[flat] = brec;
+        dir[flat] = static_cast<std::uint8_t>(bdir);
+        return;
+    }
+    receiver[flat] = kOutletReceiver;
+    dir[flat] = kNoDir;
+    if (!allowed_outlet && !allow_pits)
+    {
+        // Lexicographically first unresolved cell, as the reference reports.
+        atomicMin(err + 1, static_cast<unsigned long long>(flat));
+        raise_error(err, kErrUnresolved, 0);
+    }
+}
+
+// Donor counts by gather (cell c counts neighbours d with dir(d) pointing to
+// c; each donor matches exactly one direction, so no de-duplication is
+// needed even when periodic wrap makes two directions reach one cell) and
+// outlet flags for the ordered compaction.
+__global__ void __launch_bounds__(256) donors_kernel(Grid g, const std::uint8_t* __restrict__ mask,
+                                                     const std::uint8_t* __restrict__ dir,
+                                                     std::uint8_t* __restrict__ donors,
+                                                     std::uint8_t* __restrict__ outlet_flag)
+{
+    const std::int64_t flat = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (flat >= g.n) return;
+    const int row = static_cast<int>(flat / g.nc), col = static_cast<int>(flat % g.nc);
+    std::uint8_t cnt = 0;
+    const bool valid = mask[flat] != 0;
+    if (valid)
+    {
+        if (is_interior(g, row, col))
+        {
+#pragma unroll
+            for (int d = 0; d < 8; ++d)
+            {
+                const std::int64_t nf = flat + static_cast<std::int64_t>(d8_dr(d)) * g.nc + d8_dc(d);
+                if (mask[nf] && dir[nf] == ((d + 4) & 7)) ++cnt;
+            }
+        }
+        else
+        {
+            for (int d = 0; d < 8; ++d)
+            {
+                const Step s = resolve_step(g, row, col, d);
+                if (s.kind != 1) continue;
+                const std::int64_t nf = static_cast<std::int64_t>(s.r) * g.nc + s.c;
+                if (nf == flat) continue;
+                if (mask[nf] && dir[nf] == ((d + 4) & 7)) ++cnt;
+            }
+        }
+    }
+    donors[flat] = cnt;
+    outlet_flag[flat] = (valid && dir[flat] == kNoDir) ? 1 : 0;
+}
+
+__global__ void scatter_flagged(const std::uint8_t* __restrict__ flag, const std::int64_t* __restrict__ pos,
+                                std::int64_t n, std::int64_t* __restrict__ out)
+{
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < n && flag[i]) out[pos[i]] = i;
+}
+
+__global__ void count_valid(const std::uint8_t* __restrict__ mask, std::int64_t n, unsigned long long* acc)
+{
+    std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const std::int64_t stride = static_cast<std::int64_t>(gridDim.x) * blockDim.x;
+    unsigned long long c = 0;
+    for (; i < n; i += stride) c += mask[i] ? 1 : 0;
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(acc, c);
+}
+
+}  // namespace
+
+cudaError_t launch_receivers(lsdtt_gpu_flow* f, const float* z, const std::uint8_t* mask,
+                             const std::uint8_t* forced_plane, int interior_nodata_is_outlet,
+                             int allow_pits_as_outlets, cudaStream_t st)
+{
+    const dim3 block(32, 8);
+    const dim3 grid((f->g.nc + 31) / 32, (f->g.nr + 7) / 8);
+    receivers_kernel<<<grid, block, 0, st>>>(f->g, z, mask, forced_plane, interior_nodata_is_outlet,
+                                             allow_pits_as_outlets, f->receiver, f->dir, f->derr);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_donors_outlets(lsdtt_gpu_flow* f, cudaStream_t st)
+{
+    const std::int64_t n = f->g.n;
+    Scratch& ws = f->ws;
+    const std::size_t mark = ws.used;
+    std::uint8_t* flag = ws.take<std::uint8_t>(static_cast<std::size_t>(n));
+    std::int64_t* pos = ws.take<std::int64_t>(static_cast<std::size_t>(n));
+    if (!flag || !pos) return cudaErrorMemoryAllocation;
+    donors_kernel<<<grid_blocks(n, 256), 256, 0, st>>>(f->g, f->mask, f->dir, f->donors, flag);
+    cudaError_t e = exclusive_scan<std::uint8_t, std::int64_t>(flag, n, pos, f->dscal + 1, ws, st);
+    if (e != cudaSuccess) return e;
+    scatter_flagged<<<grid_blocks(n, 256), 256, 0, st>>>(flag, pos, n, f->outlets);
+    cudaMemsetAsync(f->dscal, 0, sizeof(std::int64_t), st);
+    count_valid<<<152 * 4, 256, 0, st>>>(f->mask, n, reinterpret_cast<unsigned long long*>(f->dscal));
+    ws.used = mark;
+    return cudaGetLastError();
+}
+
+}  // namespace lsdtt_gb300

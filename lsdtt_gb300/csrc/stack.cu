@@ -1,0 +1,685 @@
+// stack.cu -- s-vector, contributing-cell counts, depths, heights and the
+// Kahn topological order of the D8 receiver forest, all without a
+// level-by-level sweep.
+//
+// 1. Euler tour. The reference's s-vector (src/cpu/lsdtt_flowinfo_cpu.cpp:
+//    1544-1731) is a DFS preorder from each outlet in row-major order with
+//    donors visited in ascending flat index. That preorder is the order of
+//    "enter" events on the Euler tour of the forest whose children lists are
+//    sorted ascending and whose trees are chained in outlet order. Each valid
+//    cell c owns two tour nodes, enter(c) = 2c and exit(c) = 2c+1, and the
+//    successor of every node follows from first child / next sibling /
+//    parent / next outlet.
+// 2. List ranking by a sparse ruling set: every 64th node (plus the head)
+//    starts a walk to the next ruler, the rulers' list is ranked
+//    recursively, then every node adds its ruler's rank. With weights
+//    (enter: +1, exit: 0) the prefix is the preorder index; with (+1, -1)
+//    it is the depth. s_vector_start = prefix at enter, s_vector_size =
+//    prefix at exit - prefix at enter, depth = signed prefix at enter.
+// 3. Kahn order (build_topological_order, :1428-1522). The FIFO processes
+//    level L_k (cells whose longest path from a headwater is k) before
+//    L_{k+1}, and L_{k+1} is the list of receivers pushed by L_k in L_k
+//    order, each pushed by its last-processed donor. By induction the order
+//    inside every level is the order of the flat index of a single
+//    headwater per cell: the deepest headwater of its subtree, the largest
+//    flat index among equally deep ones. Both the height and that headwater
+//    are one range-max over the cell's s-vector interval of the key
+//    (depth << 32 | flat). The order is then a stable radix sort by
+//    (height, headwater).
+
+#include <cmath>
+#include <cstdlib>
+
+#include "engine.cuh"
+
+namespace lsdtt_gb300
+{
+namespace
+{
+
+constexpr std::uint32_t kEnd = 0xffffffffu;
+constexpr std::uint32_t kNone = 0xffffffffu;
+constexpr unsigned kErrCycle = 5;
+constexpr int kRuler = 64;        // mean sublist length of the ruling set
+constexpr int kSerialLimit = 96;  // rank lists this short with one thread
+
+__device__ __forceinline__ bool is_ruler(std::uint32_t v)
+{
+    // Spread rulers pseudo-randomly so sublists stay short on any layout.
+    std::uint32_t h = v * 0x9E3779B1u;
+    h ^= h >> 15;
+    return (h & (kRuler - 1)) == 0;
+}
+
+// Sorted donor list of a valid cell: ascending flat index, de-duplicated
+// (a donor matches exactly one direction, see donors_kernel).
+__device__ int donor_list(const Grid& g, const std::uint8_t* __restrict__ mask, const std::uint8_t* __restrict__ dir,
+                          std::int64_t flat, std::int64_t out[8])
+{
+    const int row = static_cast<int>(flat / g.nc), col = static_cast<int>(flat % g.nc);
+    int k = 0;
+    if (is_interior(g, row, col))
+    {
+        // NW, N, NE, W, E, SW, S, SE: ascending flat order; code of each and
+        // the code that points back (opposite).
+        const int order[8] = {7, 0, 1, 6, 2, 5, 4, 3};
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+        {
+            const int d = order[i];
+            const std::int64_t nf = flat + static_cast<std::int64_t>(d8_dr(d)) * g.nc + d8_dc(d);
+            if (mask[nf] && dir[nf] == ((d + 4) & 7)) out[k++] = nf;
+        }
+        return k;
+    }
+    for (int d = 0; d < 8; ++d)
+    {
+        const Step s = resolve_step(g, row, col, d);
+        if (s.kind != 1) continue;
+        const std::int64_t nf = static_cast<std::int64_t>(s.r) * g.nc + s.c;
+        if (nf == flat || !mask[nf] || dir[nf] != ((d + 4) & 7)) continue;
+        bool dup = false;
+        for (int i = 0; i < k; ++i) dup |= (out[i] == nf);
+        if (!dup) out[k++] = nf;
+    }
+    for (int i = 1; i < k; ++i)
+    {
+        const std::int64_t key = out[i];
+        int j = i;
+        while (j > 0 && out[j - 1] > key) { out[j] = out[j - 1]; --j; }
+        out[j] = key;
+    }
+    return k;
+}
+
+// first child / next sibling links. next_sibling of each donor is written
+// by its (unique) receiver.
+__global__ void links_kernel(Grid g, const std::uint8_t* __restrict__ mask, const std::uint8_t* __restrict__ dir,
+                             std::uint32_t* __restrict__ first_child, std::uint32_t* __restrict__ next_sib)
+{
+    const std::int64_t flat = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (flat >= g.n || !mask[flat]) return;
+    std::int64_t d[8];
+    const int k = donor_list(g, mask, dir, flat, d);
+    first_child[flat] = k ? static_cast<std::uint32_t>(d[0]) : kNone;
+    for (int i = 0; i < k; ++i)
+        next_sib[d[i]] = (i + 1 < k) ? static_cast<std::uint32_t>(d[i + 1]) : kNone;
+}
+
+__global__ void root_links_kernel(const std::int64_t* __restrict__ outlets, const std::int64_t* __restrict__ n_out,
+                                  std::uint32_t* __restrict__ next_sib, std::uint32_t* __restrict__ head)
+{
+    const std::int64_t n = *n_out;
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i == 0) *head = n > 0 ? static_cast<std::uint32_t>(2 * outlets[0]) : kEnd;
+    if (i < n) next_sib[outlets[i]] = (i + 1 < n) ? static_cast<std::uint32_t>(outlets[i + 1]) : kNone;
+}
+
+// Successor of every tour node. For a root the "next sibling" link holds the
+// next outlet, and a root's exit with no next outlet ends the list.
+__global__ void succ_kernel(Grid g, const std::uint8_t* __restrict__ mask, const std::int64_t* __restrict__ receiver,
+                            const std::uint32_t* __restrict__ first_child, const std::uint32_t* __restrict__ next_sib,
+                            std::uint32_t* __restrict__ succ)
+{
+    const std::int64_t flat = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (flat >= g.n) return;
+    if (!mask[flat])
+    {
+        succ[2 * flat] = kEnd;
+        succ[2 * flat + 1] = kEnd;
+        return;
+    }
+    const std::uint32_t fc = first_child[flat];
+    const std::uint32_t ns = next_sib[flat];
+    const std::int64_t p = receiver[flat];
+    succ[2 * flat] = (fc != kNone) ? 2u * fc : static_cast<std::uint32_t>(2 * flat + 1);
+    if (ns != kNone) succ[2 * flat + 1] = 2u * ns;
+    else if (p >= 0) succ[2 * flat + 1] = static_cast<std::uint32_t>(2 * p + 1);
+    else succ[2 * flat + 1] = kEnd;
+}
+
+struct RankLevel
+{
+    std::uint32_t n;                 // node capacity of this level
+    const std::uint32_t* succ;       // [n]
+    const std::int32_t* w0;          // [n] or null: parity weights
+    const std::int32_t* w1;          // [n] or null
+    const std::uint8_t* cell_mask;   // level 0: node v valid iff cell_mask[v>>1]
+    const std::uint32_t* head;       // device scalar
+    const std::uint32_t* count;      // device scalar: valid nodes at this level (null: n)
+};
+
+__device__ __forceinline__ void weights(const RankLevel& L, std::uint32_t v, int& a, int& b)
+{
+    if (L.w0) { a = L.w0[v]; b = L.w1[v]; }
+    else { a = (v & 1u) ? 0 : 1; b = (v & 1u) ? -1 : 1; }
+}
+
+__device__ __forceinline__ bool node_valid(const RankLevel& L, std::uint32_t v)
+{
+    if (L.cell_mask) return L.cell_mask[v >> 1] != 0;
+    return v < *L.count;
+}
+
+__global__ void ruler_flags(RankLevel L, std::uint8_t* __restrict__ flag)
+{
+    const std::uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= L.n) return;
+    flag[v] = (node_valid(L, v) && (is_ruler(v) || v == *L.head)) ? 1 : 0;
+}
+
+__global__ void ruler_scatter(const std::uint8_t* __restrict__ flag, const std::uint32_t* __restrict__ pos,
+                              std::uint32_t n, std::uint32_t cap, std::uint32_t* __restrict__ rulers,
+                              std::uint32_t* __restrict__ owner)
+{
+    const std::uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= n || !flag[v] || pos[v] >= cap) return;  // overflow is reported by ruler_cap_check
+    rulers[pos[v]] = v;
+    owner[v] = pos[v];
+}
+
+__global__ void ruler_walk(RankLevel L, const std::uint8_t* __restrict__ flag, const std::uint32_t* __restrict__ rulers,
+                           const std::uint32_t* __restrict__ n_rulers, std::uint32_t* __restrict__ owner,
+                           std::int32_t* __restrict__ loc0, std::int32_t* __restrict__ loc1,
+                           std::int32_t* __restrict__ sub0, std::int32_t* __restrict__ sub1,
+                           std::uint32_t* __restrict__ nxt, std::uint32_t* __restrict__ next_head,
+                           std::uint32_t cap, unsigned long long* __restrict__ err)
+{
+    const std::uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const std::uint32_t nr = *n_rulers;
+    if (i >= nr || i >= cap) return;
+    std::uint32_t v = rulers[i];
+    if (v == *L.head) *next_head = i;
+    int a0 = 0, a1 = 0;
+    std::uint32_t steps = 0;
+    do
+    {
+        owner[v] = i;
+        loc0[v] = a0;
+        loc1[v] = a1;
+        int w0, w1;
+        weights(L, v, w0, w1);
+        a0 += w0;
+        a1 += w1;
+        v = L.succ[v];
+        ++steps;
+    } while (v != kEnd && !flag[v] && steps <= L.n);
+    if (steps > L.n) raise_error(err, kErrCycle, 0);
+    sub0[i] = a0;
+    sub1[i] = a1;
+    nxt[i] = (v == kEnd) ? kEnd : owner[v];
+}
+
+__global__ void serial_rank(RankLevel L, std::int32_t* __restrict__ p0, std::int32_t* __restrict__ p1,
+                            unsigned long long* __restrict__ err)
+{
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    std::uint32_t v = *L.head;
+    int a0 = 0, a1 = 0;
+    std::uint32_t steps = 0;
+    while (v != kEnd && steps <= L.n)
+    {
+        p0[v] = a0;
+        p1[v] = a1;
+        int w0, w1;
+        weights(L, v, w0, w1);
+        a0 += w0;
+        a1 += w1;
+        v = L.succ[v];
+        ++steps;
+    }
+    if (steps > L.n) raise_error(err, kErrCycle, 1);
+}
+
+__global__ void rank_finish(RankLevel L, const std::uint32_t* __restrict__ owner, const std::int32_t* __restrict__ loc0,
+                            const std::int32_t* __restrict__ loc1, const std::int32_t* __restrict__ P0,
+                            const std::int32_t* __restrict__ P1, std::uint32_t cap, std::int32_t* __restrict__ p0,
+                            std::int32_t* __restrict__ p1, unsigned long long* __restrict__ err)
+{
+    const std::uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= L.n || !node_valid(L, v)) return;
+    const std::uint32_t o = owner[v];
+    if (o >= cap)
+    {
+        // Not reached by any walk: the tour does not cover every valid node.
+        raise_error(err, kErrCycle, 2);
+        p0[v] = -1;
+        p1[v] = 0;
+        return;
+    }
+    p0[v] = P0[o] + loc0[v];
+    p1[v] = P1[o] + loc1[v];
+}
+
+__global__ void fill_u32(std::uint32_t* __restrict__ a, std::uint32_t n, std::uint32_t v)
+{
+    const std::uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) a[i] = v;
+}
+
+__global__ void ruler_cap_check(const std::uint32_t* cnt, std::uint32_t cap, unsigned long long* err)
+{
+    if (*cnt > cap) raise_error(err, 9, *cnt);
+}
+
+// Recursive list ranking. p0/p1 receive the exclusive prefix sums of the two
+// weights along the list starting at *L.head.
+cudaError_t rank_list(const RankLevel& L, std::int32_t* p0, std::int32_t* p1, Scratch& ws,
+                      unsigned long long* err, cudaStream_t st)
+{
+    if (L.n <= static_cast<std::uint32_t>(kSerialLimit))
+    {
+        serial_rank<<<1, 32, 0, st>>>(L, p0, p1, err);
+        return cudaGetLastError();
+    }
+    const std::size_t mark = ws.used;
+    const std::uint32_t cap = L.n / (kRuler / 4) + 64;  // generous bound on the ruler count
+    std::uint8_t* flag = ws.take<std::uint8_t>(L.n);
+    std::uint32_t* pos = ws.take<std::uint32_t>(L.n);
+    std::uint32_t* cnt = ws.take<std::uint32_t>(2);
+    std::uint32_t* owner = ws.take<std::uint32_t>(L.n);
+    std::int32_t* loc0 = ws.take<std::int32_t>(L.n);
+    std::int32_t* loc1 = ws.take<std::int32_t>(L.n);
+    if (!flag || !pos || !cnt || !owner || !loc0 || !loc1) return cudaErrorMemoryAllocation;
+    const unsigned nb = grid_blocks(L.n, 256);
+    fill_u32<<<nb, 256, 0, st>>>(owner, L.n, kNone);
+    ruler_flags<<<nb, 256, 0, st>>>(L, flag);
+    cudaError_t e = exclusive_scan<std::uint8_t, std::uint32_t>(flag, L.n, pos, cnt, ws, st);
+    if (e != cudaSuccess) return e;
+    // The ruler count is data dependent; size everything by `cap` and let the
+    // kernels read the true count. A count above `cap` is reported.
+    std::uint32_t* rulers = ws.take<std::uint32_t>(cap);
+    std::uint32_t* nxt = ws.take<std::uint32_t>(cap);
+    std::int32_t* sub0 = ws.take<std::int32_t>(cap);
+    std::int32_t* sub1 = ws.take<std::int32_t>(cap);
+    std::int32_t* P0 = ws.take<std::int32_t>(cap);
+    std::int32_t* P1 = ws.take<std::int32_t>(cap);
+    std::uint32_t* nhead = cnt + 1;
+    if (!rulers || !nxt || !sub0 || !sub1 || !P0 || !P1) return cudaErrorMemoryAllocation;
+    ruler_scatter<<<nb, 256, 0, st>>>(flag, pos, L.n, cap, rulers, owner);
+    ruler_cap_check<<<1, 1, 0, st>>>(cnt, cap, err);
+    ruler_walk<<<grid_blocks(cap, 128), 128, 0, st>>>(L, flag, rulers, cnt, owner, loc0, loc1, sub0, sub1, nxt,
+                                                      nhead, cap, err);
+    RankLevel up{cap, nxt, sub0, sub1, nullptr, nhead, cnt};
+    e = rank_list(up, P0, P1, ws, err, st);
+    if (e != cudaSuccess) return e;
+    rank_finish<<<nb, 256, 0, st>>>(L, owner, loc0, loc1, P0, P1, cap, p0, p1, err);
+    ws.used = mark;
+    return cudaGetLastError();
+}
+
+
+
+// Per-cell s-vector outputs from the two prefix sums.
+__global__ void sv_outputs(Grid g, const std::uint8_t* __restrict__ mask, const std::int32_t* __restrict__ p0,
+                           const std::int32_t* __restrict__ p1, std::int64_t n_valid, std::int64_t* __restrict__ start,
+                           std::uint64_t* __restrict__ size, std::int32_t* __restrict__ depth,
+                           std::int64_t* __restrict__ svec, unsigned long long* __restrict__ err)
+{
+    const std::int64_t c = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (c >= g.n) return;
+    if (!mask[c])
+    {
+        start[c] = kNodataReceiver;
+        size[c] = 0;
+        depth[c] = -1;
+        return;
+    }
+    const std::int32_t s = p0[2 * c];
+    const std::int32_t e = p0[2 * c + 1];
+    if (s < 0 || e <= s || static_cast<std::int64_t>(e) > n_valid)
+    {
+        raise_error(err, kErrCycle, 3);
+        start[c] = kNodataReceiver;
+        size[c] = 0;
+        depth[c] = 0;
+        return;
+    }
+    start[c] = s;
+    size[c] = static_cast<std::uint64_t>(e - s);
+    depth[c] = p1[2 * c];
+    svec[s] = c;
+}
+
+// ---- range max over the s-vector: blocks of 32, sparse table over blocks ----
+__global__ void rmq_base(const std::int64_t* __restrict__ svec, const std::int32_t* __restrict__ depth,
+                         std::int64_t n, std::uint64_t* __restrict__ A, std::uint64_t* __restrict__ pre,
+                         std::uint64_t* __restrict__ suf, std::uint64_t* __restrict__ blk)
+{
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    std::uint64_t a = 0;
+    if (i < n)
+    {
+        const std::int64_t c = svec[i];
+        a = (static_cast<std::uint64_t>(static_cast<std::uint32_t>(depth[c])) << 32) | static_cast<std::uint32_t>(c);
+        A[i] = a;
+    }
+    std::uint64_t p = a;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1)
+    {
+        const std::uint64_t y = __shfl_up_sync(0xffffffffu, p, o);
+        if (lane >= o && y > p) p = y;
+    }
+    std::uint64_t s = a;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1)
+    {
+        const std::uint64_t y = __shfl_down_sync(0xffffffffu, s, o);
+        if (lane + o < 32 && y > s) s = y;
+    }
+    if (i < n)
+    {
+        pre[i] = p;
+        suf[i] = s;
+    }
+    if (lane == 31 && (i - 31) < n) blk[i >> 5] = p;
+}
+
+__global__ void rmq_level(const std::uint64_t* __restrict__ prev, std::int64_t nb, std::int64_t half,
+                          std::uint64_t* __restrict__ next)
+{
+    const std::int64_t b = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (b >= nb) return;
+    std::uint64_t v = prev[b];
+    if (b + half < nb && prev[b + half] > v) v = prev[b + half];
+    next[b] = v;
+}
+
+struct Rmq
+{
+    const std::uint64_t* A;
+    const std::uint64_t* pre;
+    const std::uint64_t* suf;
+    const std::uint64_t* const* table;  // device array of level pointers
+    int levels;
+};
+
+__device__ std::uint64_t rmq_query(const Rmq& R, std::int64_t a, std::int64_t b)  // inclusive
+{
+    const std::int64_t ba = a >> 5, bb = b >> 5;
+    if (ba == bb)
+    {
+        std::uint64_t m = 0;
+        for (std::int64_t i = a; i <= b; ++i)
+            if (R.A[i] > m) m = R.A[i];
+        return m;
+    }
+    std::uint64_t m = R.suf[a];
+    if (R.pre[b] > m) m = R.pre[b];
+    const std::int64_t lo = ba + 1, hi = bb - 1;
+    if (lo <= hi)
+    {
+        const std::int64_t len = hi - lo + 1;
+        const int k = 63 - __clzll(static_cast<unsigned long long>(len));
+        const std::uint64_t* T = R.table[k];
+        std::uint64_t x = T[lo];
+        const std::uint64_t y = T[hi - (std::int64_t(1) << k) + 1];
+        if (y > x) x = y;
+        if (x > m) m = x;
+    }
+    return m;
+}
+
+__global__ void topo_heights(Grid g, const std::uint8_t* __restrict__ mask, const std::int64_t* __restrict__ start,
+                             const std::uint64_t* __restrict__ size, const std::int32_t* __restrict__ depth, Rmq R,
+                             std::int32_t* __restrict__ height, std::uint32_t* __restrict__ leaf,
+                             unsigned long long* __restrict__ maxh)
+{
+    const std::int64_t c = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (c >= g.n) return;
+    if (!mask[c])
+    {
+        height[c] = -1;
+        return;
+    }
+    const std::int64_t a = start[c];
+    const std::int64_t b = a + static_cast<std::int64_t>(size[c]) - 1;
+    std::int32_t h = 0;
+    if (a < 0 || b < a)
+    {
+        height[c] = 0;  // already reported by sv_outputs
+        leaf[c] = static_cast<std::uint32_t>(c);
+    }
+    else
+    {
+        const std::uint64_t m = rmq_query(R, a, b);
+        h = static_cast<std::int32_t>(m >> 32) - depth[c];
+        height[c] = h;
+        leaf[c] = static_cast<std::uint32_t>(m & 0xffffffffull);
+    }
+    // Warp-aggregated max keeps the atomic traffic low.
+    unsigned long long v = static_cast<unsigned long long>(h);
+    for (int o = 16; o > 0; o >>= 1)
+    {
+        const unsigned long long y = __shfl_down_sync(__activemask(), v, o);
+        if (y > v) v = y;
+    }
+    if ((threadIdx.x & 31) == 0) atomicMax(maxh, v);
+}
+
+// Sort keys (height, headwater); invalid cells get height maxh+1 so they
+// sort after every valid cell and are dropped.
+__global__ void topo_keys(Grid g, const std::uint8_t* __restrict__ mask, const std::int32_t* __restrict__ height,
+                          const std::uint32_t* __restrict__ leaf, int leaf_bits, std::uint64_t maxh,
+                          std::uint64_t* __restrict__ keys, std::uint32_t* __restrict__ vals)
+{
+    const std::int64_t c = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (c >= g.n) return;
+    const std::uint64_t h = mask[c] ? static_cast<std::uint64_t>(height[c]) : maxh + 1;
+    const std::uint64_t l = mask[c] ? leaf[c] : 0u;
+    keys[c] = (h << leaf_bits) | l;
+    vals[c] = static_cast<std::uint32_t>(c);
+}
+
+__global__ void topo_store(const std::uint32_t* __restrict__ vals, std::int64_t n_valid, std::int64_t* __restrict__ topo,
+                           std::uint32_t* __restrict__ topo_pos)
+{
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n_valid) return;
+    const std::uint32_t c = vals[i];
+    topo[i] = c;
+    topo_pos[c] = static_cast<std::uint32_t>(i);
+}
+
+int bits_for(std::uint64_t v)
+{
+    int b = 0;
+    while (v) { ++b; v >>= 1; }
+    return b;
+}
+
+}  // namespace
+
+cudaError_t build_stack(lsdtt_gpu_flow* f, bool want_topo, cudaStream_t st)
+{
+    const Grid& g = f->g;
+    const std::int64_t n = g.n;
+    Scratch& ws = f->ws;
+    const std::size_t mark = ws.used;
+    const unsigned nb = grid_blocks(n, 256);
+
+    std::uint32_t* first_child = ws.take<std::uint32_t>(n);
+    std::uint32_t* next_sib = ws.take<std::uint32_t>(n);
+    std::uint32_t* succ = ws.take<std::uint32_t>(2 * n);
+    std::uint32_t* head = ws.take<std::uint32_t>(1);
+    std::int32_t* p0 = ws.take<std::int32_t>(2 * n);
+    std::int32_t* p1 = ws.take<std::int32_t>(2 * n);
+    if (!first_child || !next_sib || !succ || !head || !p0 || !p1) return cudaErrorMemoryAllocation;
+
+    links_kernel<<<nb, 256, 0, st>>>(g, f->mask, f->dir, first_child, next_sib);
+    root_links_kernel<<<grid_blocks(n, 256), 256, 0, st>>>(f->outlets, f->dscal + 1, next_sib, head);
+    succ_kernel<<<nb, 256, 0, st>>>(g, f->mask, f->receiver, first_child, next_sib, succ);
+
+    RankLevel L0{static_cast<std::uint32_t>(2 * n), succ, nullptr, nullptr, f->mask, head, nullptr};
+    cudaError_t e = rank_list(L0, p0, p1, ws, f->derr, st);
+    if (e != cudaSuccess) return e;
+    sv_outputs<<<nb, 256, 0, st>>>(g, f->mask, p0, p1, f->n_valid, f->sv_start, f->sv_size, f->depth, f->svec,
+                                   f->derr);
+    ws.used = mark;  // tour buffers are no longer needed
+    if (!want_topo) return cudaGetLastError();
+
+    // Range-max structure over the s-vector.
+    const std::int64_t nv = f->n_valid;
+    if (nv == 0) return cudaGetLastError();
+    const std::int64_t nblk = (nv + 31) / 32;
+    std::uint64_t* A = ws.take<std::uint64_t>(nv);
+    std::uint64_t* pre = ws.take<std::uint64_t>(nv);
+    std::uint64_t* suf = ws.take<std::uint64_t>(nv);
+    int levels = 1;
+    while ((std::int64_t(1) << levels) <= nblk) ++levels;
+    std::uint64_t* tab[40] = {};
+    for (int k = 0; k < levels; ++k) tab[k] = ws.take<std::uint64_t>(nblk);
+    std::uint64_t** dtab = ws.take<std::uint64_t*>(40);
+    if (!A || !pre || !suf || !dtab || !tab[levels - 1]) return cudaErrorMemoryAllocation;
+    rmq_base<<<grid_blocks(nblk * 32, 256), 256, 0, st>>>(f->svec, f->depth, nv, A, pre, suf, tab[0]);
+    for (int k = 1; k < levels; ++k)
+        rmq_level<<<grid_blocks(nblk, 256), 256, 0, st>>>(tab[k - 1], nblk, std::int64_t(1) << (k - 1), tab[k]);
+    cudaMemcpyAsync(dtab, tab, sizeof(tab), cudaMemcpyHostToDevice, st);
+
+    std::uint64_t* k0 = ws.take<std::uint64_t>(n);
+    std::uint32_t* v0 = ws.take<std::uint32_t>(n);
+    std::uint64_t* k1 = ws.take<std::uint64_t>(n);
+    std::uint32_t* v1 = ws.take<std::uint32_t>(n);
+    std::uint32_t* leaf = ws.take<std::uint32_t>(n);
+    if (!k0 || !v0 || !k1 || !v1 || !leaf) return cudaErrorMemoryAllocation;
+    const int leaf_bits = bits_for(static_cast<std::uint64_t>(n - 1) | 1);
+    Rmq R{A, pre, suf, dtab, levels};
+    cudaMemsetAsync(f->derr + 2, 0, sizeof(unsigned long long), st);
+    topo_heights<<<nb, 256, 0, st>>>(g, f->mask, f->sv_start, f->sv_size, f->depth, R, f->height, leaf, f->derr + 2);
+    // The number of radix passes depends on the tallest level: read it back.
+    cudaMemcpyAsync(&f->herr[2], f->derr + 2, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
+    e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return e;
+    const std::uint64_t maxh = f->herr[2];
+    f->max_height = static_cast<std::int64_t>(maxh);
+    topo_keys<<<nb, 256, 0, st>>>(g, f->mask, f->height, leaf, leaf_bits, maxh, k0, v0);
+    const int bits = leaf_bits + bits_for(maxh + 1);
+    const int cur = radix_sort_pairs(k0, v0, k1, v1, n, bits, ws, st, &e);
+    if (e != cudaSuccess) return e;
+    topo_store<<<grid_blocks(nv, 256), 256, 0, st>>>(cur ? v1 : v0, nv, f->topo, f->topo_pos);
+    ws.used = mark;
+    return cudaGetLastError();
+}
+
+
+// ---------------------------------------------------------------------------
+// accumulate (src/cpu/lsdtt_flowinfo_cpu.cpp:1979-2046)
+//
+// The reference seeds every valid cell with its weight and pushes
+// acc[rec] += acc[flat] in topological order, so a receiver's total is its
+// weight plus its donors' totals added in the donors' topological order.
+// When every partial sum is exactly representable (default weights dx^2 with
+// dx^2 = m*2^e and n_valid*m < 2^53) the order cannot matter and the total is
+// size*dx^2 exactly: one pass. Otherwise the totals are formed level by level
+// (height 0 first) with each cell adding its donors in topological order --
+// the reference's additions in the reference's order.
+// ---------------------------------------------------------------------------
+namespace
+{
+
+__global__ void accum_exact(Grid g, const std::uint8_t* __restrict__ mask, const std::uint64_t* __restrict__ size,
+                            double w, double* __restrict__ out)
+{
+    const std::int64_t c = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (c >= g.n) return;
+    out[c] = mask[c] ? static_cast<double>(size[c]) * w : 0.0;
+}
+
+__global__ void accum_seed(Grid g, const std::uint8_t* __restrict__ mask, const double* __restrict__ w, double dw,
+                           double* __restrict__ out)
+{
+    const std::int64_t c = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (c >= g.n) return;
+    out[c] = mask[c] ? (w ? w[c] : dw) : 0.0;
+}
+
+__global__ void accum_level(Grid g, const std::uint8_t* __restrict__ mask, const std::uint8_t* __restrict__ dir,
+                            const std::int64_t* __restrict__ topo, const std::uint32_t* __restrict__ topo_pos,
+                            std::int64_t lo, std::int64_t hi, double* __restrict__ acc)
+{
+    const std::int64_t i = lo + static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= hi) return;
+    const std::int64_t c = topo[i];
+    std::int64_t d[8];
+    const int k = donor_list(g, mask, dir, c, d);
+    // Order donors by topological position.
+    std::uint32_t p[8];
+    for (int a = 0; a < k; ++a) p[a] = topo_pos[d[a]];
+    for (int a = 1; a < k; ++a)
+    {
+        const std::uint32_t pk = p[a];
+        const std::int64_t dk = d[a];
+        int j = a;
+        while (j > 0 && p[j - 1] > pk) { p[j] = p[j - 1]; d[j] = d[j - 1]; --j; }
+        p[j] = pk;
+        d[j] = dk;
+    }
+    double s = acc[c];
+    for (int a = 0; a < k; ++a) s = __dadd_rn(s, acc[d[a]]);
+    acc[c] = s;
+}
+
+__global__ void level_bounds(const std::int64_t* __restrict__ topo, const std::int32_t* __restrict__ height,
+                             std::int64_t nv, std::int64_t* __restrict__ start)
+{
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= nv) return;
+    const std::int32_t h = height[topo[i]];
+    if (i == 0 || height[topo[i - 1]] != h) start[h] = i;
+    if (i == nv - 1) start[h + 1] = nv;
+}
+
+bool exact_by_count(double dw, std::int64_t nv)
+{
+    // dw = m * 2^e with m odd; exact iff nv * m < 2^53.
+    if (!(dw > 0.0) || !std::isfinite(dw)) return false;
+    int e = 0;
+    double fr = std::frexp(dw, &e);  // dw = fr * 2^e, fr in [0.5, 1)
+    std::uint64_t m = static_cast<std::uint64_t>(std::ldexp(fr, 53));
+    while (m && !(m & 1)) m >>= 1;
+    const long double prod = static_cast<long double>(m) * static_cast<long double>(nv);
+    return prod < 9007199254740992.0L;
+}
+
+}  // namespace
+
+cudaError_t accumulate(lsdtt_gpu_flow* f, const double* w, double* out, cudaStream_t st, bool* exact_path)
+{
+    const Grid& g = f->g;
+    const unsigned nb = grid_blocks(g.n, 256);
+    const double dw = g.cell * g.cell;
+    if (!w && f->has_sv && exact_by_count(dw, f->n_valid))
+    {
+        *exact_path = true;
+        accum_exact<<<nb, 256, 0, st>>>(g, f->mask, f->sv_size, dw, out);
+        return cudaGetLastError();
+    }
+    *exact_path = false;
+    accum_seed<<<nb, 256, 0, st>>>(g, f->mask, w, dw, out);
+    const std::int64_t nv = f->n_valid;
+    if (nv == 0) return cudaGetLastError();
+    const std::int64_t nlev = f->max_height + 1;
+    Scratch& ws = f->ws;
+    const std::size_t mark = ws.used;
+    std::int64_t* start = ws.take<std::int64_t>(static_cast<std::size_t>(nlev) + 1);
+    if (!start) return cudaErrorMemoryAllocation;
+    level_bounds<<<grid_blocks(nv, 256), 256, 0, st>>>(f->topo, f->height, nv, start);
+    std::int64_t* hstart = static_cast<std::int64_t*>(std::malloc(sizeof(std::int64_t) * (nlev + 1)));
+    if (!hstart) return cudaErrorMemoryAllocation;
+    cudaMemcpyAsync(hstart, start, sizeof(std::int64_t) * (nlev + 1), cudaMemcpyDeviceToHost, st);
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess)
+        for (std::int64_t k = 1; k < nlev; ++k)  // level 0 cells have no donors
+        {
+            const std::int64_t lo = hstart[k], hi = hstart[k + 1];
+            if (hi > lo) accum_level<<<grid_blocks(hi - lo, 128), 128, 0, st>>>(g, f->mask, f->dir, f->topo,
+                                                                               f->topo_pos, lo, hi, out);
+        }
+    std::free(hstart);
+    ws.used = mark;
+    return e != cudaSuccess ? e : cudaGetLastError();
+}
+
+}  // namespace lsdtt_gb300

@@ -1,0 +1,897 @@
+// lsdtt_oracle.cpp -- TEST INFRASTRUCTURE ONLY (the CPU oracle).
+//
+// A restatement, in plain C++17, of the reference lsdtt3 algorithms on the
+// landscape-evolution hot path. It is the checker for the GPU kernels (GPU
+// parity tests), the CPU baseline that bench.py times, and it is itself
+// pinned against (a) the reference's golden FNV-1a vectors in
+// tests/cpp/test_flow_d8_identity.cpp and (b) the reference's own sources
+// compiled into oracle/_ref/liblsdtt_ref.so. The product never links it.
+//
+// Reference file paths below are relative to the lsdtt3 checkout.
+//
+// Floating point: build with -ffp-contract=off (oracle/Makefile). Every
+// expression keeps the reference's operand types (float vs double), because the
+// results must be bitwise those of the reference's x86-64 build.
+
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <deque>
+#include <functional>
+#include <limits>
+#include <queue>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace
+{
+
+// D8 clockwise N, NE, E, SE, S, SW, W, NW -- direction codes 0..7
+// (src/utils/lsdtt_grid_neighbours.hpp:50-51).
+constexpr int kDr[8] = {-1, -1, 0, 1, 1, 1, 0, -1};
+constexpr int kDc[8] = {0, 1, 1, 1, 0, -1, -1, -1};
+constexpr double kSqrt2d = 1.4142135623730950488;
+constexpr float kSqrt2f = static_cast<float>(kSqrt2d);
+
+constexpr std::int64_t kNodataReceiver = -1;  // src/core/lsdtt_types.hpp:142
+constexpr std::int64_t kOutletReceiver = -2;  // src/core/lsdtt_types.hpp:143
+constexpr std::uint8_t kNoDirection = 255;    // src/core/lsdtt_types.hpp:144
+
+void put_err(char* err, int errlen, const std::string& what)
+{
+    if (!err || errlen <= 0) return;
+    std::strncpy(err, what.c_str(), static_cast<std::size_t>(errlen - 1));
+    err[errlen - 1] = '\0';
+}
+
+bool is_nodata(double v, double ndv)
+{
+    if (std::isnan(ndv)) return std::isnan(v);
+    return v == ndv;
+}
+
+// ============================================================================
+// Fill: improved priority-flood with epsilon (Barnes et al. 2014)
+// src/cpu/lsdtt_raster_flow_preprocessing_cpu.cpp:416-511 (core),
+// :518-589 (seeding), :350-392 (inputs), :727-782 (dispatch).
+// ============================================================================
+
+struct Node
+{
+    float zeta;
+    int row;
+    int col;
+};
+// Min-heap keyed on zeta only, exactly std::priority_queue<.., greater<>>
+// with a comparator that looks at zeta alone (:55-62): ties fall wherever
+// libstdc++'s push_heap/pop_heap leave them, and the restatement performs the
+// same push/pop sequence, so it leaves them in the same places.
+struct NodeGreater
+{
+    bool operator()(const Node& a, const Node& b) const { return a.zeta > b.zeta; }
+};
+using Heap = std::priority_queue<Node, std::vector<Node>, NodeGreater>;
+
+enum : int { kOpen = 0, kQueued = 1, kClosed = 2, kNoCell = -1 };
+
+struct FillTrace
+{
+    std::int64_t* discoverer = nullptr;  // flat index of the cell that queued it; -1 seed
+    std::int64_t* order = nullptr;       // position in the processing sequence
+    std::uint8_t* via_fifo = nullptr;    // 1 = raised (went through the FIFO)
+};
+
+void priority_flood(std::vector<float>& dem, std::vector<int>& idx, int nr, int nc,
+                    float L, float min_slope, bool per_ns, bool per_ew, FillTrace tr)
+{
+    Heap pq;
+
+    // Seeding (:518-589): every non-nodata cell on a non-periodic raster edge,
+    // plus cells with an in-bounds nodata neighbour when the interior has any
+    // nodata at all. Row-major push order.
+    bool interior_nodata = false;
+    for (int r = 1; r < nr - 1 && !interior_nodata; ++r)
+        for (int c = 1; c < nc - 1; ++c)
+            if (idx[static_cast<std::size_t>(r) * nc + c] == kNoCell) { interior_nodata = true; break; }
+
+    for (int r = 0; r < nr; ++r)
+        for (int c = 0; c < nc; ++c)
+        {
+            const std::size_t k = static_cast<std::size_t>(r) * nc + c;
+            if (idx[k] == kNoCell) continue;
+            bool seed = (!per_ns && (r == 0 || r == nr - 1)) || (!per_ew && (c == 0 || c == nc - 1));
+            if (!seed && interior_nodata)
+                for (int n = 0; n < 8 && !seed; ++n)
+                {
+                    const int rr = r + kDr[n], cc = c + kDc[n];
+                    if (rr >= 0 && rr < nr && cc >= 0 && cc < nc &&
+                        idx[static_cast<std::size_t>(rr) * nc + cc] == kNoCell)
+                        seed = true;
+                }
+            if (seed && idx[k] == kOpen)
+            {
+                pq.push(Node{dem[k], r, c});
+                idx[k] = kQueued;
+                if (tr.discoverer) tr.discoverer[k] = -1;
+            }
+        }
+
+    std::deque<Node> fifo;
+    std::int64_t seq = 0;
+    while (!pq.empty() || !fifo.empty())
+    {
+        Node cur;
+        bool from_fifo = false;
+        if (!fifo.empty() && (pq.empty() || fifo.front().zeta <= pq.top().zeta))
+        {
+            cur = fifo.front();
+            fifo.pop_front();
+            from_fifo = true;
+        }
+        else
+        {
+            cur = pq.top();
+            pq.pop();
+        }
+        const std::size_t ck = static_cast<std::size_t>(cur.row) * nc + cur.col;
+        if (idx[ck] == kClosed) continue;
+        idx[ck] = kClosed;
+        if (tr.order) tr.order[ck] = seq;
+        if (tr.via_fifo) tr.via_fifo[ck] = from_fifo ? 1 : 0;
+        ++seq;
+
+        for (int n = 0; n < 8; ++n)
+        {
+            int rr = cur.row + kDr[n];
+            int cc = cur.col + kDc[n];
+            if (per_ns) { if (rr < 0) rr += nr; else if (rr >= nr) rr -= nr; }
+            if (per_ew) { if (cc < 0) cc += nc; else if (cc >= nc) cc -= nc; }
+            if (rr < 0 || rr >= nr || cc < 0 || cc >= nc) continue;
+            const std::size_t k = static_cast<std::size_t>(rr) * nc + cc;
+            if (idx[k] != kOpen) continue;
+            float nz = dem[k];
+            if (nz <= cur.zeta)
+            {
+                if (min_slope > 0.0f)
+                {
+                    const float d = (n % 2 == 0) ? L : L * kSqrt2f;
+                    const float requested = cur.zeta + min_slope * d;
+                    const float strict = std::nextafter(cur.zeta, std::numeric_limits<float>::infinity());
+                    nz = std::max(requested, strict);
+                }
+                else
+                {
+                    nz = cur.zeta;
+                }
+                dem[k] = nz;
+                fifo.push_back(Node{nz, rr, cc});
+            }
+            else
+            {
+                pq.push(Node{nz, rr, cc});
+            }
+            idx[k] = kQueued;
+            if (tr.discoverer) tr.discoverer[k] = static_cast<std::int64_t>(ck);
+        }
+    }
+}
+
+// ============================================================================
+// D8 engine: lsdtt_flowinfo (src/cpu/lsdtt_flowinfo_cpu.cpp)
+// ============================================================================
+
+struct Bc
+{
+    char c[4];  // N E S W
+};
+
+Bc parse_bc(const char* s)
+{
+    // parse_boundary_conditions (:845-884): length 4, codes o/n/p/b folded to
+    // lower case, periodic flags must match per axis.
+    const std::string b = s ? s : "";
+    if (b.size() != 4)
+        throw std::runtime_error("lsdtt_flowinfo: boundary_conditions must have length 4 (north, east, south, west)");
+    Bc out{};
+    for (int i = 0; i < 4; ++i)
+    {
+        const char ch = static_cast<char>(std::tolower(static_cast<unsigned char>(b[i])));
+        if (ch != 'o' && ch != 'n' && ch != 'p' && ch != 'b')
+            throw std::runtime_error(std::string("lsdtt_flowinfo: invalid boundary code '") + b[i] + "'");
+        out.c[i] = ch;
+    }
+    if ((out.c[0] == 'p') != (out.c[2] == 'p'))
+        throw std::runtime_error("lsdtt_flowinfo: north and south periodic boundary flags must match");
+    if ((out.c[1] == 'p') != (out.c[3] == 'p'))
+        throw std::runtime_error("lsdtt_flowinfo: east and west periodic boundary flags must match");
+    return out;
+}
+
+struct Resolved
+{
+    bool inside = false;
+    bool outlet = false;
+    int r = 0, c = 0;
+};
+
+// resolve_neighbour (:101-158)
+Resolved resolve(int row, int col, int dir, int nr, int nc, const Bc& bc)
+{
+    Resolved res;
+    int r = row + kDr[dir], c = col + kDc[dir];
+    bool out = false;
+    if (r < 0)
+    {
+        if (bc.c[0] == 'p') r = nr - 1;
+        else if (bc.c[0] == 'o' || bc.c[0] == 'b') out = true;
+        else return res;
+    }
+    else if (r >= nr)
+    {
+        if (bc.c[2] == 'p') r = 0;
+        else if (bc.c[2] == 'o' || bc.c[2] == 'b') out = true;
+        else return res;
+    }
+    if (c < 0)
+    {
+        if (bc.c[3] == 'p') c = nc - 1;
+        else if (bc.c[3] == 'o' || bc.c[3] == 'b') out = true;
+        else return res;
+    }
+    else if (c >= nc)
+    {
+        if (bc.c[1] == 'p') c = 0;
+        else if (bc.c[1] == 'o' || bc.c[1] == 'b') out = true;
+        else return res;
+    }
+    if (out) { res.outlet = true; return res; }
+    res.inside = true;
+    res.r = r;
+    res.c = c;
+    return res;
+}
+
+struct FlowOpts
+{
+    Bc bc;
+    bool interior_nodata_is_outlet = true;
+    bool allow_pits_as_outlets = false;
+    bool build_topo = true;
+    bool build_sv = true;
+    bool require_acyclic = true;
+    int n_threads = 0;
+};
+
+struct Flow
+{
+    int nr = 0, nc = 0;
+    double cell = 0.0;
+    std::vector<std::uint8_t> mask;
+    std::vector<std::int64_t> receiver;
+    std::vector<std::uint8_t> dir;
+    std::vector<std::uint8_t> donors;
+    std::vector<std::int64_t> outlets;
+    std::vector<std::int64_t> topo;
+    bool has_topo = false;
+    bool acyclic = false;
+    std::vector<std::int64_t> svec, sv_start;
+    std::vector<std::uint64_t> sv_size;
+    bool has_sv = false;
+    std::int64_t n_valid = 0;
+};
+
+// build_receiver_graph_d8 (:1077-1329). Every cell's receiver is independent of
+// every other's; the strict '>' in direction order 0..7 keeps the first of
+// equal slopes. Slopes are double: (double)z - (double)z_nb over dx or dx*sqrt2.
+void build_receivers(Flow& F, const float* z, const FlowOpts& o,
+                     const std::vector<std::uint8_t>& forced_plane)
+{
+    const int nr = F.nr, nc = F.nc;
+    const double card = F.cell, diag = F.cell * kSqrt2d;
+    bool failed = false;
+    int fail_r = 0, fail_c = 0;
+    int nthreads = o.n_threads;
+#ifdef _OPENMP
+    if (nthreads <= 0) nthreads = omp_get_max_threads();
+#pragma omp parallel for collapse(2) schedule(static) num_threads(nthreads)
+#endif
+    for (int row = 0; row < nr; ++row)
+        for (int col = 0; col < nc; ++col)
+        {
+            const std::int64_t flat = static_cast<std::int64_t>(row) * nc + col;
+            if (F.mask[flat] == 0) { F.receiver[flat] = kNodataReceiver; F.dir[flat] = kNoDirection; continue; }
+            const bool forced_edge = (row == 0 && o.bc.c[0] == 'b') || (col == nc - 1 && o.bc.c[1] == 'b') ||
+                                     (row == nr - 1 && o.bc.c[2] == 'b') || (col == 0 && o.bc.c[3] == 'b');
+            if (forced_edge || (!forced_plane.empty() && forced_plane[flat]))
+            {
+                F.receiver[flat] = kOutletReceiver;
+                F.dir[flat] = kNoDirection;
+                continue;
+            }
+            const float zc = z[flat];
+            double best = 0.0;
+            std::int64_t best_rec = kOutletReceiver;
+            std::uint8_t best_dir = kNoDirection;
+            bool allowed_outlet = false;
+            for (int d = 0; d < 8; ++d)
+            {
+                const Resolved nb = resolve(row, col, d, nr, nc, o.bc);
+                if (nb.outlet) { allowed_outlet = true; continue; }
+                if (!nb.inside) continue;
+                const std::int64_t nf = static_cast<std::int64_t>(nb.r) * nc + nb.c;
+                if (F.mask[nf] == 0)
+                {
+                    if (o.interior_nodata_is_outlet) allowed_outlet = true;
+                    continue;
+                }
+                if (nf == flat) continue;
+                const double dz = static_cast<double>(zc) - static_cast<double>(z[nf]);
+                if (dz <= 0.0) continue;
+                const double slope = dz / ((d % 2 == 0) ? card : diag);
+                if (slope > best) { best = slope; best_rec = nf; best_dir = static_cast<std::uint8_t>(d); }
+            }
+            if (best_dir != kNoDirection) { F.receiver[flat] = best_rec; F.dir[flat] = best_dir; }
+            else
+            {
+                F.receiver[flat] = kOutletReceiver;
+                F.dir[flat] = kNoDirection;
+                if (!allowed_outlet && !o.allow_pits_as_outlets)
+                {
+#ifdef _OPENMP
+#pragma omp critical(oracle_receiver_failure)
+#endif
+                    {
+                        if (!failed || row < fail_r || (row == fail_r && col < fail_c))
+                        {
+                            failed = true;
+                            fail_r = row;
+                            fail_c = col;
+                        }
+                    }
+                }
+            }
+        }
+    if (failed)
+        throw std::runtime_error("lsdtt_flowinfo: could not assign a receiver at row " + std::to_string(fail_r) +
+                                 ", col " + std::to_string(fail_c) +
+                                 ". The DEM likely contains an unresolved sink or flat.");
+}
+
+// build_donor_counts_and_outlets_d8 (:1359-1408)
+void build_donors(Flow& F)
+{
+    const std::int64_t n = static_cast<std::int64_t>(F.nr) * F.nc;
+    F.outlets.clear();
+    for (std::int64_t f = 0; f < n; ++f)
+    {
+        if (!F.mask[f]) continue;
+        const std::int64_t r = F.receiver[f];
+        if (r >= 0)
+        {
+            if (F.donors[r] == 255) throw std::runtime_error("lsdtt_flowinfo: donor count overflow while building donor counts");
+            ++F.donors[r];
+        }
+        else if (r == kOutletReceiver)
+            F.outlets.push_back(f);
+    }
+}
+
+// build_topological_order (:1428-1522): Kahn's FIFO, headwaters seeded in
+// row-major order; a short result means the graph is cyclic.
+void build_topo(Flow& F)
+{
+    const std::int64_t n = static_cast<std::int64_t>(F.nr) * F.nc;
+    F.topo.clear();
+    F.topo.reserve(static_cast<std::size_t>(F.n_valid));
+    if (F.n_valid == 0) { F.has_topo = true; F.acyclic = true; return; }
+    std::vector<std::uint8_t> rem(F.donors);
+    for (std::int64_t f = 0; f < n; ++f)
+        if (F.mask[f] && rem[f] == 0) F.topo.push_back(f);
+    for (std::size_t head = 0; head < F.topo.size(); ++head)
+    {
+        const std::int64_t r = F.receiver[F.topo[head]];
+        if (r >= 0 && --rem[r] == 0) F.topo.push_back(r);
+    }
+    if (static_cast<std::int64_t>(F.topo.size()) != F.n_valid)
+    {
+        F.topo.clear();
+        F.has_topo = false;
+        F.acyclic = false;
+        return;
+    }
+    F.has_topo = true;
+    F.acyclic = true;
+}
+
+// build_s_vector (:1544-1731): iterative DFS preorder from each outlet in
+// row-major order, donors visited in ascending flat index.
+void build_svector(Flow& F, const Bc& bc)
+{
+    if (!F.acyclic) throw std::runtime_error("lsdtt_flowinfo: cannot build s_vector from a cyclic or invalid routing graph");
+    const std::int64_t n = static_cast<std::int64_t>(F.nr) * F.nc;
+    F.sv_start.assign(static_cast<std::size_t>(n), kNodataReceiver);
+    F.sv_size.assign(static_cast<std::size_t>(n), 0);
+    F.svec.clear();
+    F.svec.reserve(static_cast<std::size_t>(F.n_valid));
+    if (F.n_valid == 0) { F.has_sv = true; return; }
+    if (F.outlets.empty()) throw std::runtime_error("lsdtt_flowinfo: cannot build s_vector because no outlets were found");
+
+    struct Frame
+    {
+        std::int64_t flat;
+        std::int64_t donors[8];
+        int nd;
+        int next;
+    };
+    auto make = [&](std::int64_t flat) {
+        Frame fr{};
+        fr.flat = flat;
+        F.sv_start[flat] = static_cast<std::int64_t>(F.svec.size());
+        F.sv_size[flat] = 1;
+        F.svec.push_back(flat);
+        const int row = static_cast<int>(flat / F.nc), col = static_cast<int>(flat % F.nc);
+        for (int d = 0; d < 8; ++d)
+        {
+            const Resolved nb = resolve(row, col, d, F.nr, F.nc, bc);
+            if (!nb.inside) continue;
+            const std::int64_t df = static_cast<std::int64_t>(nb.r) * F.nc + nb.c;
+            if (!F.mask[df] || F.receiver[df] != flat) continue;
+            bool dup = false;
+            for (int i = 0; i < fr.nd; ++i) dup = dup || fr.donors[i] == df;
+            if (!dup) fr.donors[fr.nd++] = df;
+        }
+        std::sort(fr.donors, fr.donors + fr.nd);
+        return fr;
+    };
+    std::vector<Frame> st;
+    for (const std::int64_t o : F.outlets)
+    {
+        if (F.sv_start[o] >= 0) continue;
+        st.clear();
+        st.push_back(make(o));
+        while (!st.empty())
+        {
+            Frame& fr = st.back();
+            if (fr.next < fr.nd)
+            {
+                const std::int64_t child = fr.donors[fr.next++];
+                if (F.sv_start[child] >= 0) throw std::runtime_error("lsdtt_flowinfo: duplicate visit while building s_vector");
+                st.push_back(make(child));
+                continue;
+            }
+            const std::int64_t done = fr.flat;
+            const std::uint64_t sz = F.sv_size[done];
+            st.pop_back();
+            if (!st.empty()) F.sv_size[st.back().flat] += sz;
+        }
+    }
+    if (static_cast<std::int64_t>(F.svec.size()) != F.n_valid)
+        throw std::runtime_error("lsdtt_flowinfo: s_vector does not cover all valid cells");
+    F.has_sv = true;
+}
+
+Flow build_flow(const float* z, const std::uint8_t* mask, int nr, int nc, double cell, double nodata,
+                const FlowOpts& o, const std::int64_t* forced, std::int64_t n_forced)
+{
+    if (!(nr > 0 && nc > 0 && cell > 0.0)) throw std::runtime_error("lsdtt_flowinfo: raster metadata is invalid");
+    Flow F;
+    F.nr = nr;
+    F.nc = nc;
+    F.cell = cell;
+    const std::int64_t n = static_cast<std::int64_t>(nr) * nc;
+    F.mask.assign(mask, mask + n);
+    // validate_inputs (:887-966): valid cells need finite, non-nodata z.
+    const float ndv = static_cast<float>(nodata);
+    for (int r = 0; r < nr; ++r)
+        for (int c = 0; c < nc; ++c)
+        {
+            const std::int64_t f = static_cast<std::int64_t>(r) * nc + c;
+            if (!F.mask[f]) continue;
+            if (!std::isfinite(z[f]) || z[f] == ndv)
+                throw std::runtime_error("lsdtt_flowinfo: valid mask cell has nodata or non-finite DEM value at row " +
+                                         std::to_string(r) + ", col " + std::to_string(c));
+        }
+    // validate_forced_outlet_flats (:969-1009)
+    std::vector<std::uint8_t> plane;
+    if (n_forced > 0)
+    {
+        plane.assign(static_cast<std::size_t>(n), 0);
+        for (std::int64_t i = 0; i < n_forced; ++i)
+        {
+            const std::int64_t f = forced[i];
+            if (f < 0 || f >= n)
+                throw std::invalid_argument("lsdtt_flowinfo: forced outlet flat index " + std::to_string(f) + " (entry " +
+                                            std::to_string(i) + ") is outside the raster, which has " +
+                                            std::to_string(n) + " cells");
+            if (!F.mask[f])
+                throw std::invalid_argument("lsdtt_flowinfo: forced outlet flat index " + std::to_string(f) + " (entry " +
+                                            std::to_string(i) + ", row " + std::to_string(f / nc) + ", col " +
+                                            std::to_string(f % nc) +
+                                            ") lands on a nodata or masked cell, so it cannot act as a flow termination");
+            plane[f] = 1;
+        }
+    }
+    for (std::int64_t f = 0; f < n; ++f) F.n_valid += F.mask[f] ? 1 : 0;
+    F.receiver.assign(static_cast<std::size_t>(n), kNodataReceiver);
+    F.dir.assign(static_cast<std::size_t>(n), kNoDirection);
+    F.donors.assign(static_cast<std::size_t>(n), 0);
+    build_receivers(F, z, o, plane);
+    build_donors(F);
+    if (o.build_topo || o.build_sv || o.require_acyclic)
+    {
+        build_topo(F);
+        if (!F.acyclic && o.require_acyclic)
+            throw std::runtime_error(
+                "lsdtt_flowinfo: routing graph is cyclic or incomplete. This usually means the DEM still contains "
+                "unresolved flats, pits, or incompatible periodic routing.");
+    }
+    if (o.build_sv) build_svector(F, o.bc);
+    return F;
+}
+
+// accumulate (:1979-2046): seed every valid cell with its weight (dx^2 by
+// default), then push acc[rec] += acc[flat] in topological order.
+std::vector<double> accumulate(const Flow& F, const double* w)
+{
+    const std::int64_t n = static_cast<std::int64_t>(F.nr) * F.nc;
+    const double dw = F.cell * F.cell;
+    if (w)
+        for (std::int64_t f = 0; f < n; ++f)
+            if (F.mask[f] && !std::isfinite(w[f]))
+                throw std::invalid_argument("lsdtt_flowinfo::accumulate: cell_weights must be finite for all valid cells");
+    std::vector<double> acc(static_cast<std::size_t>(n), 0.0);
+    for (std::int64_t f = 0; f < n; ++f)
+        if (F.mask[f]) acc[f] = w ? w[f] : dw;
+    for (const std::int64_t f : F.topo)
+    {
+        const std::int64_t r = F.receiver[f];
+        if (r >= 0) acc[r] += acc[f];
+    }
+    return acc;
+}
+
+std::uint64_t splitmix64(std::uint64_t x)
+{
+    // Steele, Lea & Flood (2014) splitmix64 with Vigna's published constants.
+    x += 0x9E3779B97F4A7C15ULL;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBULL;
+    return x ^ (x >> 31);
+}
+
+std::uint64_t mix_in(std::uint64_t h, std::uint64_t v)
+{
+    return splitmix64(h ^ (v + 0x9E3779B97F4A7C15ULL + (h << 6) + (h >> 2)));
+}
+
+}  // namespace
+
+extern "C" {
+
+// ---------------------------------------------------------------------------
+// oracle_fill_pits: fill_pits(raster, min_slope, bc, n_threads, binary_heap)
+// (src/cpu/lsdtt_raster_flow_preprocessing_cpu.cpp:727-782). min_slope <= 0
+// runs the flood with a zero rise, which the reference documents as bitwise
+// equal to its reconstruction backend (docs/design_and_algorithms/
+// flow_routing.md:603-620).
+// ---------------------------------------------------------------------------
+int oracle_fill_pits_traced(const float* z, const std::uint8_t* mask, int nr, int nc, double cell, double nodata,
+                            const char* bc, float min_slope, float* out, std::int64_t* discoverer,
+                            std::int64_t* order, std::uint8_t* via_fifo, char* err, int errlen)
+{
+    try
+    {
+        if (!(nr > 0 && nc > 0 && cell > 0.0)) throw std::runtime_error("lsdtt::fill_pits: invalid raster metadata");
+        const std::string b = bc ? bc : "";
+        auto is_p = [&](std::size_t i) { return b.size() > i && (b[i] == 'p' || b[i] == 'P'); };
+        const bool per_ns = is_p(0), per_ew = is_p(1);
+        if (per_ns != is_p(2))
+            throw std::runtime_error("lsdtt::fill_pits: north and south periodic flags must match (boundary_conditions '" + b + "')");
+        if (per_ew != is_p(3))
+            throw std::runtime_error("lsdtt::fill_pits: east and west periodic flags must match (boundary_conditions '" + b + "')");
+        if (per_ns && per_ew)
+            throw std::runtime_error("lsdtt::fill_pits: boundary_conditions '" + b +
+                                     "' is periodic in BOTH directions, so the grid has no drainage exit at all and every "
+                                     "cell would fill to the global maximum. Leave one pair open.");
+        const std::size_t n = static_cast<std::size_t>(nr) * nc;
+        std::vector<float> dem(n);
+        std::vector<int> idx(n);
+        const float ndv = static_cast<float>(nodata);
+        for (std::size_t k = 0; k < n; ++k)
+        {
+            if (mask[k] != 0 && !is_nodata(z[k], nodata)) { dem[k] = z[k]; idx[k] = kOpen; }
+            else { dem[k] = ndv; idx[k] = kNoCell; }
+        }
+        FillTrace tr{discoverer, order, via_fifo};
+        if (discoverer) std::fill(discoverer, discoverer + n, static_cast<std::int64_t>(-2));
+        if (order) std::fill(order, order + n, static_cast<std::int64_t>(-1));
+        priority_flood(dem, idx, nr, nc, static_cast<float>(cell), min_slope > 0.0f ? min_slope : 0.0f, per_ns, per_ew, tr);
+        std::memcpy(out, dem.data(), sizeof(float) * n);
+        return 0;
+    }
+    catch (const std::exception& e) { put_err(err, errlen, e.what()); return 1; }
+}
+
+int oracle_fill_pits(const float* z, const std::uint8_t* mask, int nr, int nc, double cell, double nodata,
+                     const char* bc, float min_slope, int /*radix_queue*/, float* out, char* err, int errlen)
+{
+    return oracle_fill_pits_traced(z, mask, nr, nc, cell, nodata, bc, min_slope, out, nullptr, nullptr, nullptr, err,
+                                   errlen);
+}
+
+// ---------------------------------------------------------------------------
+// oracle_flowinfo: lsdtt_flowinfo::create (src/cpu/lsdtt_flowinfo_cpu.cpp:
+// 197-253) and every component tests/cpp/test_flow_d8_identity.cpp pins.
+// Same argument layout as ref_flowinfo in oracle/ref_shim.cpp.
+// ---------------------------------------------------------------------------
+int oracle_flowinfo(const float* z, const std::uint8_t* mask, int nr, int nc, double cell, double nodata,
+                    const char* bc, int interior_nodata_is_outlet, int allow_pits_as_outlets, int build_topo,
+                    int build_sv, int require_acyclic, const std::int64_t* forced, std::int64_t n_forced,
+                    int n_threads, std::int64_t* receiver, std::uint8_t* dir, std::uint8_t* donors,
+                    std::int64_t* outlets, std::int64_t* n_outlets, std::int64_t* topo, std::int64_t* n_topo,
+                    std::int64_t* svec, std::int64_t* sv_start, std::uint64_t* sv_size, std::int32_t* flags,
+                    const double* weights, double* accum, char* err, int errlen)
+{
+    try
+    {
+        FlowOpts o;
+        o.bc = parse_bc(bc);
+        o.interior_nodata_is_outlet = interior_nodata_is_outlet != 0;
+        o.allow_pits_as_outlets = allow_pits_as_outlets != 0;
+        o.build_topo = build_topo != 0;
+        o.build_sv = build_sv != 0;
+        o.require_acyclic = require_acyclic != 0;
+        o.n_threads = n_threads;
+        Flow F = build_flow(z, mask, nr, nc, cell, nodata, o, forced, n_forced);
+        const std::size_t n = static_cast<std::size_t>(nr) * nc;
+        std::memcpy(receiver, F.receiver.data(), sizeof(std::int64_t) * n);
+        std::memcpy(dir, F.dir.data(), n);
+        std::memcpy(donors, F.donors.data(), n);
+        *n_outlets = static_cast<std::int64_t>(F.outlets.size());
+        std::memcpy(outlets, F.outlets.data(), sizeof(std::int64_t) * F.outlets.size());
+        // The topological order is kept only when asked for (:240-247).
+        const bool keep_topo = F.has_topo && o.build_topo;
+        flags[0] = keep_topo ? 1 : 0;
+        flags[1] = F.has_sv ? 1 : 0;
+        *n_topo = 0;
+        if (keep_topo)
+        {
+            *n_topo = static_cast<std::int64_t>(F.topo.size());
+            std::memcpy(topo, F.topo.data(), sizeof(std::int64_t) * F.topo.size());
+        }
+        if (F.has_sv)
+        {
+            // The outlets' slices, concatenated in outlet order, ARE the
+            // s-vector: each outlet's DFS appends a contiguous block.
+            std::memcpy(svec, F.svec.data(), sizeof(std::int64_t) * F.svec.size());
+            std::memcpy(sv_start, F.sv_start.data(), sizeof(std::int64_t) * n);
+            std::memcpy(sv_size, F.sv_size.data(), sizeof(std::uint64_t) * n);
+        }
+        if (accum && keep_topo)
+        {
+            const std::vector<double> a = accumulate(F, weights);
+            std::memcpy(accum, a.data(), sizeof(double) * n);
+        }
+        return 0;
+    }
+    catch (const std::exception& e) { put_err(err, errlen, e.what()); return 1; }
+}
+
+// ---------------------------------------------------------------------------
+// oracle_stream_power: compute_d8_stream_power_incision
+// (src/cpu/lsdtt_stream_power_cpu.cpp:159-326) on a flow object built as
+// run_lem_step builds it (src/cpu/lsdtt_lem_cpu.cpp:329-339), moving-average
+// kernel 1 (identity), no width correction.
+// ---------------------------------------------------------------------------
+int oracle_stream_power(const float* z, const std::uint8_t* mask, int nr, int nc, double cell, double nodata,
+                        const char* bc, float K, float m, float n_exp, float dt, float threshold_area,
+                        int divide_area_by_dx, float slope_clamp, const float* k_field, float* out, char* err,
+                        int errlen)
+{
+    try
+    {
+        FlowOpts o;
+        o.bc = parse_bc(bc);
+        o.interior_nodata_is_outlet = true;
+        o.allow_pits_as_outlets = true;
+        const Flow F = build_flow(z, mask, nr, nc, cell, nodata, o, nullptr, 0);
+        const std::int64_t ncell = static_cast<std::int64_t>(nr) * nc;
+        const float dx = static_cast<float>(cell);
+        const float dx_diag = dx * kSqrt2f;
+        std::vector<float> zz(z, z + ncell);
+        const std::vector<double> area_d = accumulate(F, nullptr);
+        const bool n_is_one = std::abs(n_exp - 1.0f) < 1e-6f;
+        const double width_factor = 1.0;
+        for (std::int64_t ti = static_cast<std::int64_t>(F.topo.size()) - 1; ti >= 0; --ti)
+        {
+            const std::int64_t flat = F.topo[static_cast<std::size_t>(ti)];
+            const std::int64_t recv = F.receiver[flat];
+            if (recv == kOutletReceiver || !F.mask[flat]) continue;
+            if (recv < 0 || recv >= ncell) continue;
+            const std::uint8_t d = F.dir[flat];
+            const float dx_eff = (d & 1u) ? dx_diag : dx;
+            double area = area_d[flat];
+            if (divide_area_by_dx) area /= dx;
+            if (threshold_area > 0.0f && area < static_cast<double>(threshold_area)) continue;
+            const float z_old = z[flat];
+            const float z_r = zz[recv];
+            float z_new = z_old;
+            if (z_r >= z_old) continue;
+            const double tol = static_cast<double>(slope_clamp) * dx_eff;
+            const float Ki = k_field ? k_field[flat] : K;
+            const double kam = static_cast<double>(Ki) * width_factor * std::pow(area, static_cast<double>(m));
+            if (n_is_one)
+            {
+                const double spf = kam * (dt / dx_eff);
+                z_new = static_cast<float>((z_old + z_r * spf) / (1.0 + spf));
+                if ((z_new - z_old) > static_cast<float>(tol) || std::isnan(z_new)) z_new = z_old;
+            }
+            else
+            {
+                double eps = tol + 1.0;
+                int it = 0;
+                do
+                {
+                    const double slope = (z_new - z_r) / dx_eff;
+                    if (slope <= 0.0) eps = 0.0;
+                    else
+                    {
+                        const double fz = z_new - z_old + kam * dt * std::pow(slope, n_exp);
+                        const double fdz = 1.0 + kam * dt * (n_exp / dx_eff) * std::pow(slope, n_exp - 1.0);
+                        eps = fz / fdz;
+                    }
+                    z_new -= static_cast<float>(eps);
+                    ++it;
+                    if (it > 100) eps = tol / 2.0;
+                } while (std::abs(eps) > tol);
+                if ((z_new - z_old) > static_cast<float>(tol) || std::isnan(z_new)) z_new = z_old;
+                if (z_new < z_r) z_new = static_cast<float>(z_r + slope_clamp * dx_eff);
+            }
+            zz[flat] = z_new;
+        }
+        std::memcpy(out, zz.data(), sizeof(float) * ncell);
+        return 0;
+    }
+    catch (const std::exception& e) { put_err(err, errlen, e.what()); return 1; }
+}
+
+// ---------------------------------------------------------------------------
+// oracle_boundary_flats: build_boundary_flats (src/cpu/lsdtt_lem_cpu.cpp:735-808)
+// ---------------------------------------------------------------------------
+std::int64_t oracle_boundary_flats(const std::uint8_t* mask, int nr, int nc, const char* bc, std::int64_t* out)
+{
+    const std::string b = bc ? bc : "";
+    auto fixed = [&](std::size_t i) { return b.size() > i && (b[i] == 'o' || b[i] == 'b'); };
+    const bool fn = fixed(0), fe = fixed(1), fs = fixed(2), fw = fixed(3);
+    std::int64_t k = 0;
+    for (int r = 0; r < nr; ++r)
+        for (int c = 0; c < nc; ++c)
+        {
+            const std::int64_t f = static_cast<std::int64_t>(r) * nc + c;
+            if (!mask[f]) continue;
+            bool edge = false;
+            for (int dr = -1; dr <= 1 && !edge; ++dr)
+                for (int dc = -1; dc <= 1; ++dc)
+                {
+                    if (dr == 0 && dc == 0) continue;
+                    const int r2 = r + dr, c2 = c + dc;
+                    if (r2 < 0) { if (fn) edge = true; }
+                    else if (r2 >= nr) { if (fs) edge = true; }
+                    else if (c2 < 0) { if (fw) edge = true; }
+                    else if (c2 >= nc) { if (fe) edge = true; }
+                    else if (!mask[static_cast<std::int64_t>(r2) * nc + c2])
+                    {
+                        if ((dr == -1 && fn) || (dr == 1 && fs) || (dc == -1 && fw) || (dc == 1 && fe)) edge = true;
+                    }
+                }
+            if (edge) out[k++] = f;
+        }
+    return k;
+}
+
+// ---------------------------------------------------------------------------
+// oracle_lem_finish: the end of run_lem_step (src/cpu/lsdtt_lem_cpu.cpp:
+// 611-731) -- uplift on valid cells, restore the boundary flats to their
+// pre-step value minus base-level fall, then the step statistics.
+// z is updated in place; z_before is the step's input surface.
+// stats: delta_max, delta_mean, max_local, p999_local, mean_erosion, max_erosion.
+// ---------------------------------------------------------------------------
+void oracle_lem_finish(float* z, const float* z_before, const std::uint8_t* mask, std::int64_t n, float U, float dt,
+                       float baselevel_fall, const std::int64_t* bflats, std::int64_t n_bf, float* stats)
+{
+    const float uplift_dz = U * dt;
+    for (std::int64_t i = 0; i < n; ++i)
+        if (mask[i]) z[i] += uplift_dz;
+    const float bl = baselevel_fall * dt;
+    for (std::int64_t i = 0; i < n_bf; ++i)
+        if (bflats[i] >= 0 && bflats[i] < n) z[bflats[i]] = z_before[bflats[i]] - bl;
+    double sb = 0.0, sa = 0.0, mb = -1e30, ma = -1e30, ml = 0.0, se = 0.0, me = 0.0;
+    std::vector<float> lc;
+    lc.reserve(static_cast<std::size_t>(n));
+    std::int64_t nv = 0;
+    const double udz = static_cast<double>(U * dt);
+    for (std::int64_t i = 0; i < n; ++i)
+    {
+        if (!mask[i]) continue;
+        ++nv;
+        const double zb = z_before[i], za = z[i];
+        sb += zb;
+        sa += za;
+        mb = std::max(mb, zb);
+        ma = std::max(ma, za);
+        const double d = std::abs(za - zb);
+        ml = std::max(ml, d);
+        lc.push_back(static_cast<float>(d));
+        const double ero = zb - (za - udz);
+        if (ero > 0.0) { se += ero; me = std::max(me, ero); }
+    }
+    const double inv_dt = 1.0 / static_cast<double>(dt);
+    const double inv_n = nv > 0 ? 1.0 / static_cast<double>(nv) : 0.0;
+    stats[0] = static_cast<float>(std::abs(ma - mb));
+    stats[1] = static_cast<float>(std::abs((sa - sb) * inv_n));
+    stats[2] = static_cast<float>(ml);
+    if (!lc.empty())
+    {
+        // compute_quantile_floor_in_place (src/utils/lsdtt_statistics.cpp:420-429):
+        // the order statistic at floor(q*(n-1)).
+        std::size_t k = static_cast<std::size_t>(0.999 * static_cast<double>(lc.size() - 1));
+        k = std::min(k, lc.size() - 1);
+        std::nth_element(lc.begin(), lc.begin() + static_cast<std::ptrdiff_t>(k), lc.end());
+        stats[3] = lc[k];
+    }
+    else
+        stats[3] = 0.0f;
+    stats[4] = static_cast<float>(se * inv_n * inv_dt);
+    stats[5] = static_cast<float>(me * inv_dt);
+}
+
+// ---------------------------------------------------------------------------
+// oracle_noise_tilt_surface: generate_uniform_random_noise_surface followed by
+// superimpose_open_boundary_gradient (src/cpu/lsdtt_raster_synthetic_surfaces_
+// cpu.cpp:118-147, 359-459). The noise is a splitmix64 hash of
+// (seed, tag, row, col, 0, 0) mapped to [0,1) by its top 53 bits.
+// ---------------------------------------------------------------------------
+int oracle_noise_tilt_surface(int nr, int nc, double cell, int seed, double lo, double hi, const char* bc,
+                              float slope, float* out, char* /*err*/, int /*errlen*/)
+{
+    const double span = hi - lo;
+    const std::uint64_t tag = 0x554E49464F524DULL;
+    for (int r = 0; r < nr; ++r)
+        for (int c = 0; c < nc; ++c)
+        {
+            std::uint64_t h = splitmix64(static_cast<std::uint64_t>(static_cast<std::uint32_t>(seed)));
+            h = mix_in(h, tag);
+            h = mix_in(h, static_cast<std::uint64_t>(r));
+            h = mix_in(h, static_cast<std::uint64_t>(c));
+            h = mix_in(h, 0);
+            h = mix_in(h, 0);
+            const std::uint64_t key = splitmix64(h);
+            const double u = static_cast<double>(key >> 11) * (1.0 / 9007199254740992.0);
+            out[static_cast<std::size_t>(r) * nc + c] = static_cast<float>(lo + span * u);
+        }
+    const std::string b = bc ? bc : "";
+    auto open = [&](std::size_t i) { return b.size() > i && (b[i] == 'o' || b[i] == 'b'); };
+    const bool on = open(0), oe = open(1), os = open(2), ow = open(3);
+    if (slope == 0.0f || !(on || oe || os || ow)) return 0;
+    const float dx = static_cast<float>(cell);
+    for (int r = 0; r < nr; ++r)
+        for (int c = 0; c < nc; ++c)
+        {
+            int d = nr + nc;
+            if (on) d = std::min(d, r);
+            if (oe) d = std::min(d, nc - 1 - c);
+            if (os) d = std::min(d, nr - 1 - r);
+            if (ow) d = std::min(d, c);
+            out[static_cast<std::size_t>(r) * nc + c] += slope * dx * static_cast<float>(d);
+        }
+    return 0;
+}
+
+}  // extern "C"

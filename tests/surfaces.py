@@ -1,0 +1,53 @@
+"""Seeded synthetic surfaces for the parity tests and the benchmark.
+
+* noise_tilt: config 1 of the benchmark suite -- seeded uniform noise 0-1 m
+  plus a 0.001 planar tilt toward the open edges (the reference's
+  generate_uniform_random_noise_surface + superimpose_open_boundary_gradient,
+  restated by the oracle).
+* fractal_pits: config 2 -- spectral synthesis with power spectrum ~ k^-2
+  (random phases, amplitude k^-1), rescaled to the given relief, plus seeded
+  paraboloid pits of uniform depth 0-5 m and radius 1-4 cells. The reference
+  has no FFT on this machine (FFTW absent), so the surface is defined here.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def fractal(n_rows: int, n_cols: int, relief: float, seed: int, beta: float = 2.0) -> np.ndarray:
+    rng = np.random.default_rng(seed)
+    ky = np.fft.fftfreq(n_rows)[:, None]
+    kx = np.fft.rfftfreq(n_cols)[None, :]
+    k = np.sqrt(kx * kx + ky * ky)
+    k[0, 0] = 1.0
+    amp = k ** (-beta / 2.0)
+    amp[0, 0] = 0.0
+    phase = rng.uniform(0.0, 2.0 * np.pi, size=amp.shape)
+    z = np.fft.irfft2(amp * np.exp(1j * phase), s=(n_rows, n_cols))
+    z = (z - z.min()) / (z.max() - z.min()) * relief
+    return z.astype(np.float32)
+
+
+def add_pits(z: np.ndarray, n_pits: int, seed: int, rmin: float = 1.0, rmax: float = 4.0,
+             dmax: float = 5.0) -> np.ndarray:
+    rng = np.random.default_rng(seed + 1)
+    nr, nc = z.shape
+    cy = rng.integers(0, nr, n_pits)
+    cx = rng.integers(0, nc, n_pits)
+    rad = rng.uniform(rmin, rmax, n_pits)
+    dep = rng.uniform(0.0, dmax, n_pits)
+    z = z.copy()
+    R = int(np.ceil(rmax))
+    oy, ox = np.mgrid[-R:R + 1, -R:R + 1]
+    dd = np.sqrt(oy * oy + ox * ox)
+    for y, x, r, d in zip(cy, cx, rad, dep):
+        w = np.clip(1.0 - (dd / r) ** 2, 0.0, None) * d
+        y0, y1 = max(0, y - R), min(nr, y + R + 1)
+        x0, x1 = max(0, x - R), min(nc, x + R + 1)
+        z[y0:y1, x0:x1] -= w[y0 - (y - R):y1 - (y - R), x0 - (x - R):x1 - (x - R)].astype(np.float32)
+    return z
+
+
+def fractal_pits(n: int, relief: float = 1000.0, seed: int = 7, pits_per_8192sq: int = 100000) -> np.ndarray:
+    z = fractal(n, n, relief, seed)
+    return add_pits(z, max(1, int(round(pits_per_8192sq * (n / 8192.0) ** 2))), seed)
