@@ -62,6 +62,19 @@ int lsdtt_gpu_device_available(void);
 const char* lsdtt_gpu_last_error(void);
 const char* lsdtt_gpu_version(void);
 
+/* ---- instrumentation (no reference counterpart; tracing for the backend) --
+ * launch_count: kernels of this library executed since load (each kernel's
+ * first block bumps a device counter; reading it synchronises the device).
+ * profile_enable(1) starts recording a CUDA event pair around each hot
+ * kernel launch, on the launch's own stream; profile_read sums, for one
+ * kernel name, the elapsed time, the number of launches and the algorithmic
+ * bytes those launches move (the per-cell byte counts of the backend's
+ * design notes times the cells each launch covers). profile_enable(0) stops
+ * recording and drops the records. */
+unsigned long long lsdtt_gpu_launch_count(void);
+int lsdtt_gpu_profile_enable(int32_t on);
+int lsdtt_gpu_profile_read(const char* kernel, double* total_ms, int64_t* launches, double* bytes);
+
 /* ---- fill ----------------------------------------------------------------
  * Replaces fill_pits(const lsdtt_raster_cpu&, float min_slope,
  * const std::string& bc, int n_threads, priority_flood_queue_backend)
@@ -126,6 +139,74 @@ int lsdtt_gpu_stream_power_d8(lsdtt_gpu_flow* flow, const float* z_dev, const fl
                               float K, float m, float n, float dt, float incision_threshold_area,
                               int32_t divide_area_by_dx, float slope_clamp, float* z_out_dev,
                               void* stream);
+
+/* ---- implicit hillslope diffusion ------------------------------------------
+ * One backward-Euler step of linear hillslope diffusion over dt: the Newton
+ * step of compute_hillslope_newton (src/cpu/lsdtt_hillslope_newton_cpu.cpp:
+ * 196-675; operator src/cpu/lsdtt_hillslope_operator_cpu.hpp:83-322) with
+ * alpha = 1, solved matrix-free by Jacobi-PCG to ||r||_2 <= rel_tol*||b||_2.
+ * is_channel_dev may be NULL (no channel cells). Returns LSDTT_GPU_ENOCONV
+ * (with z_out still written) when max_iter is reached first. */
+typedef struct lsdtt_gpu_solve_report
+{
+    int32_t iterations;
+    int32_t converged;
+    double relative_residual;
+    double initial_residual_inf; /* ||F||_inf before the step (m/yr) */
+} lsdtt_gpu_solve_report;
+
+int lsdtt_gpu_hillslope_linear_implicit(const lsdtt_gpu_grid* grid, const float* z_dev, const uint8_t* mask_dev,
+                                        const uint8_t* is_channel_dev, float D, float dt, double rel_tol,
+                                        int32_t max_iter, float* z_out_dev, lsdtt_gpu_solve_report* report,
+                                        void* stream);
+
+/* ---- LEM timestep ----------------------------------------------------------
+ * run_lem_step (src/cpu/lsdtt_lem_cpu.cpp:285-732) for the D8 coupled
+ * regime with the "roering_implicit" linear hillslope model, optionally
+ * preceded by fill_pits(z, fill_min_slope, bc) as the benchmark
+ * configurations ask: fill -> D8 engine -> stream power -> hillslope ->
+ * uplift on valid cells -> boundary flats restored to their pre-step value
+ * minus base-level fall -> statistics. The LEM handle owns every buffer. */
+typedef struct lsdtt_gpu_lem_options
+{
+    float timestep;
+    float erodibility;
+    float m_exponent;
+    float n_exponent;
+    float uplift_rate;
+    float hillslope_diffusivity;
+    float slope_clamp;            /* reference default 1e-5 */
+    float baselevel_fall_rate;
+    float fill_min_slope;         /* <= 0: no per-step fill */
+    int32_t enable_hillslope;     /* linear implicit hillslope step */
+    int32_t divide_area_by_dx;    /* reference default 1 */
+    double hillslope_rel_tol;     /* PCG relative residual, e.g. 1e-8 */
+    int32_t hillslope_max_iter;
+} lsdtt_gpu_lem_options;
+
+/* lsdtt_lem_step_stats (src/cpu/lsdtt_lem_cpu.hpp:185-211) */
+typedef struct lsdtt_gpu_lem_stats
+{
+    float delta_max_elevation;
+    float delta_mean_elevation;
+    float max_local_elevation_change;
+    float p999_local_elevation_change;
+    float mean_erosion_rate;
+    float max_erosion_rate;
+    int32_t hillslope_iterations;
+    int32_t reserved;
+} lsdtt_gpu_lem_stats;
+
+typedef struct lsdtt_gpu_lem lsdtt_gpu_lem;
+
+/* mask_dev is copied; boundary flats (build_boundary_flats,
+ * src/cpu/lsdtt_lem_cpu.cpp:735-808) are derived from it and the grid's
+ * boundary string. */
+int lsdtt_gpu_lem_create(const lsdtt_gpu_grid* grid, const uint8_t* mask_dev, const lsdtt_gpu_lem_options* options,
+                         lsdtt_gpu_lem** out, void* stream);
+int lsdtt_gpu_lem_destroy(lsdtt_gpu_lem* lem);
+/* Advances z_dev (in place) by one timestep. stats may be NULL. */
+int lsdtt_gpu_lem_step(lsdtt_gpu_lem* lem, float* z_dev, lsdtt_gpu_lem_stats* stats, void* stream);
 
 /* ---- whole routing pass with host buffers ---------------------------------
  * fill_pits(z, min_slope, bc) then lsdtt_flowinfo on the filled surface, then

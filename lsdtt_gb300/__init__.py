@@ -265,3 +265,121 @@ class _DeviceArray:
     def __init__(self, ptr, count, dtype):
         self.__cuda_array_interface__ = {"shape": (count,), "typestr": self._TYPESTR[str(dtype)],
                                          "data": (int(ptr), False), "version": 3, "strides": None}
+
+
+class SolveReport(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int32), ("converged", ctypes.c_int32), ("relative_residual", ctypes.c_double),
+                ("initial_residual_inf", ctypes.c_double)]
+
+
+class LemOptions(ctypes.Structure):
+    _fields_ = [("timestep", ctypes.c_float), ("erodibility", ctypes.c_float), ("m_exponent", ctypes.c_float),
+                ("n_exponent", ctypes.c_float), ("uplift_rate", ctypes.c_float),
+                ("hillslope_diffusivity", ctypes.c_float), ("slope_clamp", ctypes.c_float),
+                ("baselevel_fall_rate", ctypes.c_float), ("fill_min_slope", ctypes.c_float),
+                ("enable_hillslope", ctypes.c_int32), ("divide_area_by_dx", ctypes.c_int32),
+                ("hillslope_rel_tol", ctypes.c_double), ("hillslope_max_iter", ctypes.c_int32)]
+
+
+class LemStats(ctypes.Structure):
+    _fields_ = [("delta_max_elevation", ctypes.c_float), ("delta_mean_elevation", ctypes.c_float),
+                ("max_local_elevation_change", ctypes.c_float), ("p999_local_elevation_change", ctypes.c_float),
+                ("mean_erosion_rate", ctypes.c_float), ("max_erosion_rate", ctypes.c_float),
+                ("hillslope_iterations", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+
+
+def _bind_more():
+    L = lib()
+    vp, i32, f32, f64 = ctypes.c_void_p, ctypes.c_int32, ctypes.c_float, ctypes.c_double
+    for name, args in {
+        "lsdtt_gpu_hillslope_linear_implicit": [ctypes.POINTER(Grid), vp, vp, vp, f32, f32, f64, i32, vp,
+                                                ctypes.POINTER(SolveReport), vp],
+        "lsdtt_gpu_lem_create": [ctypes.POINTER(Grid), vp, ctypes.POINTER(LemOptions), ctypes.POINTER(vp), vp],
+        "lsdtt_gpu_lem_destroy": [vp],
+        "lsdtt_gpu_lem_step": [vp, vp, ctypes.POINTER(LemStats), vp],
+    }.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = ctypes.c_int
+    return L
+
+
+def hillslope_linear_implicit(z, mask, cell_size, boundary_conditions, D, dt, rel_tol=1e-8, max_iter=2000,
+                              is_channel=None, stream=None):
+    """One backward-Euler linear hillslope step (compute_hillslope_newton,
+    alpha = 1). Returns (z_out CUDA tensor, SolveReport)."""
+    torch = _torch()
+    L = _bind_more()
+    zt = _dev(z, torch.float32)
+    mt = _dev(mask, torch.uint8)
+    ct = None if is_channel is None else _dev(is_channel, torch.uint8)
+    g = make_grid(zt.shape[0], zt.shape[1], cell_size, boundary_conditions)
+    out = torch.empty_like(zt)
+    rep = SolveReport()
+    st = L.lsdtt_gpu_hillslope_linear_implicit(ctypes.byref(g), ctypes.c_void_p(zt.data_ptr()),
+                                               ctypes.c_void_p(mt.data_ptr()),
+                                               ctypes.c_void_p(ct.data_ptr() if ct is not None else 0),
+                                               ctypes.c_float(D), ctypes.c_float(dt), ctypes.c_double(rel_tol),
+                                               ctypes.c_int32(max_iter), ctypes.c_void_p(out.data_ptr()),
+                                               ctypes.byref(rep), _stream(stream))
+    _check(st)
+    return out, rep
+
+
+def stream_power_d8(flow: "FlowInfo", z, K, m, n, dt, incision_threshold_area=0.0, divide_area_by_dx=True,
+                    slope_clamp=1e-5, erodibility_field=None, stream=None):
+    """compute_d8_stream_power_incision on a built FlowInfo (moving-average
+    kernel 1, no width correction). Returns a float32 CUDA tensor."""
+    torch = _torch()
+    zt = _dev(z, torch.float32)
+    kf = None if erodibility_field is None else _dev(erodibility_field, torch.float32)
+    out = torch.empty_like(zt)
+    _check(lib().lsdtt_gpu_stream_power_d8(flow._h, ctypes.c_void_p(zt.data_ptr()),
+                                           ctypes.c_void_p(kf.data_ptr() if kf is not None else 0),
+                                           ctypes.c_float(K), ctypes.c_float(m), ctypes.c_float(n), ctypes.c_float(dt),
+                                           ctypes.c_float(incision_threshold_area),
+                                           ctypes.c_int32(int(divide_area_by_dx)), ctypes.c_float(slope_clamp),
+                                           ctypes.c_void_p(out.data_ptr()), _stream(stream)))
+    return out
+
+
+class LandscapeModel:
+    """Device-resident LEM (run_lem_step in the D8 coupled regime with the
+    linear implicit hillslope), optionally filling the surface each step."""
+
+    def __init__(self, z, mask, cell_size, boundary_conditions="oooo", *, timestep=100.0, erodibility=1e-3,
+                 m_exponent=0.45, n_exponent=1.0, uplift_rate=1e-4, hillslope_diffusivity=1e-3,
+                 enable_hillslope=True, slope_clamp=1e-5, baselevel_fall_rate=0.0, fill_min_slope=0.0,
+                 divide_area_by_dx=True, hillslope_rel_tol=1e-8, hillslope_max_iter=2000, stream=None):
+        torch = _torch()
+        L = _bind_more()
+        self.z = _dev(z, torch.float32).clone()
+        self.mask = _dev(mask, torch.uint8)
+        self.grid = make_grid(self.z.shape[0], self.z.shape[1], cell_size, boundary_conditions)
+        self.options = LemOptions(timestep, erodibility, m_exponent, n_exponent, uplift_rate, hillslope_diffusivity,
+                                  slope_clamp, baselevel_fall_rate, fill_min_slope, int(enable_hillslope),
+                                  int(divide_area_by_dx), hillslope_rel_tol, hillslope_max_iter)
+        h = ctypes.c_void_p()
+        _check(L.lsdtt_gpu_lem_create(ctypes.byref(self.grid), ctypes.c_void_p(self.mask.data_ptr()),
+                                      ctypes.byref(self.options), ctypes.byref(h), _stream(stream)))
+        self._h = h
+
+    def step(self, stream=None, want_stats=True):
+        st = LemStats()
+        _check(lib().lsdtt_gpu_lem_step(self._h, ctypes.c_void_p(self.z.data_ptr()),
+                                        ctypes.byref(st) if want_stats else None, _stream(stream)))
+        return st.as_dict() if want_stats else None
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().lsdtt_gpu_lem_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

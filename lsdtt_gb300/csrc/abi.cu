@@ -7,6 +7,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "engine.cuh"
 
@@ -80,6 +81,7 @@ namespace
 __global__ void check_valid_z(const float* __restrict__ z, const std::uint8_t* __restrict__ mask, std::int64_t n,
                               float ndv, unsigned long long* __restrict__ first_bad)
 {
+    LSDTT_COUNT();
     const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n || !mask[i]) return;
     const float v = z[i];
@@ -89,6 +91,7 @@ __global__ void check_valid_z(const float* __restrict__ z, const std::uint8_t* _
 __global__ void check_finite_w(const double* __restrict__ w, const std::uint8_t* __restrict__ mask, std::int64_t n,
                                unsigned long long* __restrict__ first_bad)
 {
+    LSDTT_COUNT();
     const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n || !mask[i]) return;
     if (!isfinite(w[i])) atomicMin(first_bad, static_cast<unsigned long long>(i));
@@ -96,6 +99,7 @@ __global__ void check_finite_w(const double* __restrict__ w, const std::uint8_t*
 
 __global__ void copy_mask(const std::uint8_t* __restrict__ in, std::int64_t n, std::uint8_t* __restrict__ out)
 {
+    LSDTT_COUNT();
     const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i < n) out[i] = in[i] ? 1 : 0;
 }
@@ -104,6 +108,7 @@ __global__ void stamp_forced(const std::int64_t* __restrict__ forced, std::int64
                              const std::uint8_t* __restrict__ mask, std::uint8_t* __restrict__ plane,
                              unsigned long long* __restrict__ bad)
 {
+    LSDTT_COUNT();
     const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= nf) return;
     const std::int64_t f = forced[i];
@@ -118,9 +123,89 @@ __global__ void stamp_forced(const std::int64_t* __restrict__ forced, std::int64
 }  // namespace
 }  // namespace lsdtt_gb300
 
+namespace lsdtt_gb300
+{
+
+unsigned long long launches_abi();
+unsigned long long launches_d8();
+unsigned long long launches_fill();
+unsigned long long launches_hillslope();
+unsigned long long launches_lem();
+unsigned long long launches_stack();
+unsigned long long launches_stream_power();
+
+namespace
+{
+struct ProfRec
+{
+    std::string name;
+    double bytes;
+    cudaEvent_t b, e;
+};
+std::mutex g_prof_mu;
+bool g_prof_on = false;
+std::vector<ProfRec> g_prof;
+}  // namespace
+
+bool profiling_enabled() { return g_prof_on; }
+
+void profile_begin(const char* kernel, double bytes, cudaStream_t, cudaEvent_t* b, cudaEvent_t* e)
+{
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    ProfRec r{kernel, bytes, nullptr, nullptr};
+    if (cudaEventCreate(&r.b) != cudaSuccess || cudaEventCreate(&r.e) != cudaSuccess) return;
+    *b = r.b;
+    *e = r.e;
+    g_prof.push_back(r);
+}
+
+}  // namespace lsdtt_gb300
+
 using namespace lsdtt_gb300;
 
 extern "C" {
+
+unsigned long long lsdtt_gpu_launch_count(void)
+{
+    return launches_abi() + launches_d8() + launches_fill() + launches_hillslope() + launches_lem() +
+           launches_stack() + launches_stream_power();
+}
+
+int lsdtt_gpu_profile_enable(int32_t on)
+{
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    for (auto& r : g_prof)
+    {
+        cudaEventDestroy(r.b);
+        cudaEventDestroy(r.e);
+    }
+    g_prof.clear();
+    g_prof_on = on != 0;
+    return LSDTT_GPU_OK;
+}
+
+int lsdtt_gpu_profile_read(const char* kernel, double* total_ms, int64_t* launches, double* bytes)
+{
+    if (!kernel || !total_ms || !launches || !bytes) return fail(LSDTT_GPU_EINVAL, "lsdtt_gpu_profile_read: null");
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    double t = 0.0, by = 0.0;
+    std::int64_t k = 0;
+    for (auto& r : g_prof)
+    {
+        if (r.name != kernel) continue;
+        float ms = 0.0f;
+        cudaError_t e = cudaEventSynchronize(r.e);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, r.b, r.e);
+        if (e != cudaSuccess) return cuda_fail(e, "lsdtt_gpu_profile_read");
+        t += ms;
+        by += r.bytes;
+        ++k;
+    }
+    *total_ms = t;
+    *launches = k;
+    *bytes = by;
+    return LSDTT_GPU_OK;
+}
 
 const char* lsdtt_gpu_last_error(void) { return g_last_error.c_str(); }
 
@@ -343,3 +428,8 @@ int lsdtt_gpu_flow_accumulate(lsdtt_gpu_flow* f, const double* w_dev, double* ou
 }
 
 }  // extern "C"
+
+namespace lsdtt_gb300
+{
+LSDTT_DEFINE_LAUNCH_READER(abi)
+}  // namespace lsdtt_gb300

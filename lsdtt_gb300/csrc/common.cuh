@@ -114,3 +114,48 @@ __device__ inline void raise_error(unsigned long long* err, unsigned code, unsig
 }
 
 }  // namespace lsdtt_gb300
+
+// ---------------------------------------------------------------------------
+// Instrumentation.
+//
+// Launch counting: block (0,0,0) thread 0 of every kernel bumps a per-
+// translation-unit device counter (LSDTT_COUNT() is the first statement of
+// each kernel); lsdtt_gpu_launch_count() sums the counters of every unit.
+//
+// Kernel timing: hot launch sites record a CUDA event pair on their own
+// stream when profiling is enabled (lsdtt_gpu_profile_enable); the totals
+// per kernel name are resolved by lsdtt_gpu_profile_read.
+// ---------------------------------------------------------------------------
+static __device__ unsigned long long g_tu_launches;
+
+#define LSDTT_COUNT()                                                                                  \
+    do                                                                                                 \
+    {                                                                                                  \
+        if ((blockIdx.x | blockIdx.y | blockIdx.z | threadIdx.x | threadIdx.y | threadIdx.z) == 0)     \
+            atomicAdd(&g_tu_launches, 1ull);                                                           \
+    } while (0)
+
+#define LSDTT_DEFINE_LAUNCH_READER(name)                                                               \
+    unsigned long long launches_##name()                                                               \
+    {                                                                                                  \
+        unsigned long long v = 0;                                                                      \
+        cudaMemcpyFromSymbol(&v, g_tu_launches, sizeof(v));                                            \
+        return v;                                                                                      \
+    }
+
+namespace lsdtt_gb300
+{
+bool profiling_enabled();
+// Returns the pair to record around one launch (nullptrs when disabled).
+void profile_begin(const char* kernel, double bytes, cudaStream_t st, cudaEvent_t* b, cudaEvent_t* e);
+}  // namespace lsdtt_gb300
+
+#define LSDTT_TIMED(name, bytes, st, launch)                                                           \
+    do                                                                                                 \
+    {                                                                                                  \
+        cudaEvent_t _b = nullptr, _e = nullptr;                                                        \
+        if (::lsdtt_gb300::profiling_enabled()) ::lsdtt_gb300::profile_begin(name, bytes, st, &_b, &_e); \
+        if (_b) cudaEventRecord(_b, st);                                                               \
+        launch;                                                                                        \
+        if (_e) cudaEventRecord(_e, st);                                                               \
+    } while (0)

@@ -77,11 +77,12 @@ __device__ void exact_receiver(const Grid& g, const float* __restrict__ z, const
 __global__ void __launch_bounds__(256) receivers_kernel(Grid g, const float* __restrict__ z,
                                                         const std::uint8_t* __restrict__ mask,
                                                         const std::uint8_t* __restrict__ forced,
-                                                        int interior_nodata_is_outlet, int allow_pits,
-                                                        std::int64_t* __restrict__ receiver,
+                                                        int interior_nodata_is_outlet, int allow_pits, float inv_card,
+                                                        float inv_diag, std::int64_t* __restrict__ receiver,
                                                         std::uint8_t* __restrict__ dir,
                                                         unsigned long long* __restrict__ err)
 {
+    LSDTT_COUNT();
     const int col = blockIdx.x * blockDim.x + threadIdx.x;
     const int row = blockIdx.y * blockDim.y + threadIdx.y;
     if (row >= g.nr || col >= g.nc) return;
@@ -101,9 +102,8 @@ __global__ void __launch_bounds__(256) receivers_kernel(Grid g, const float* __r
         return;
     }
     const float zc = z[flat];
-    // Float ranking: weights are 1/dx and 1/(dx*sqrt2) rounded to float.
-    const float inv_card = static_cast<float>(1.0 / g.cell);
-    const float inv_diag = static_cast<float>(1.0 / (g.cell * 1.4142135623730950488));
+    // Float ranking: weights are 1/dx and 1/(dx*sqrt2) rounded to float
+    // (computed once on the host: FP64 division is costly on this part).
     float best = 0.0f, second = 0.0f;
     int bdir = kNoDir;
     std::int64_t brec = kOutletReceiver;
@@ -192,6 +192,7 @@ __global__ void __launch_bounds__(256) donors_kernel(Grid g, const std::uint8_t*
                                                      std::uint8_t* __restrict__ donors,
                                                      std::uint8_t* __restrict__ outlet_flag)
 {
+    LSDTT_COUNT();
     const std::int64_t flat = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (flat >= g.n) return;
     const int row = static_cast<int>(flat / g.nc), col = static_cast<int>(flat % g.nc);
@@ -227,12 +228,14 @@ __global__ void __launch_bounds__(256) donors_kernel(Grid g, const std::uint8_t*
 __global__ void scatter_flagged(const std::uint8_t* __restrict__ flag, const std::int64_t* __restrict__ pos,
                                 std::int64_t n, std::int64_t* __restrict__ out)
 {
+    LSDTT_COUNT();
     const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i < n && flag[i]) out[pos[i]] = i;
 }
 
 __global__ void count_valid(const std::uint8_t* __restrict__ mask, std::int64_t n, unsigned long long* acc)
 {
+    LSDTT_COUNT();
     std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     const std::int64_t stride = static_cast<std::int64_t>(gridDim.x) * blockDim.x;
     unsigned long long c = 0;
@@ -249,8 +252,13 @@ cudaError_t launch_receivers(lsdtt_gpu_flow* f, const float* z, const std::uint8
 {
     const dim3 block(32, 8);
     const dim3 grid((f->g.nc + 31) / 32, (f->g.nr + 7) / 8);
-    receivers_kernel<<<grid, block, 0, st>>>(f->g, z, mask, forced_plane, interior_nodata_is_outlet,
-                                             allow_pits_as_outlets, f->receiver, f->dir, f->derr);
+    const float inv_card = static_cast<float>(1.0 / f->g.cell);
+    const float inv_diag = static_cast<float>(1.0 / (f->g.cell * 1.4142135623730950488));
+    // Algorithmic bytes: z 4 + mask 1 in, direction 1 + int64 receiver 8 out.
+    LSDTT_TIMED("d8_receivers", 14.0 * static_cast<double>(f->g.n), st,
+                (receivers_kernel<<<grid, block, 0, st>>>(f->g, z, mask, forced_plane, interior_nodata_is_outlet,
+                                                          allow_pits_as_outlets, inv_card, inv_diag, f->receiver,
+                                                          f->dir, f->derr)));
     return cudaGetLastError();
 }
 
@@ -262,7 +270,9 @@ cudaError_t launch_donors_outlets(lsdtt_gpu_flow* f, cudaStream_t st)
     std::uint8_t* flag = ws.take<std::uint8_t>(static_cast<std::size_t>(n));
     std::int64_t* pos = ws.take<std::int64_t>(static_cast<std::size_t>(n));
     if (!flag || !pos) return cudaErrorMemoryAllocation;
-    donors_kernel<<<grid_blocks(n, 256), 256, 0, st>>>(f->g, f->mask, f->dir, f->donors, flag);
+    // Algorithmic bytes: direction 1 in, donor count 1 out.
+    LSDTT_TIMED("d8_donors", 2.0 * static_cast<double>(n), st,
+                (donors_kernel<<<grid_blocks(n, 256), 256, 0, st>>>(f->g, f->mask, f->dir, f->donors, flag)));
     cudaError_t e = exclusive_scan<std::uint8_t, std::int64_t>(flag, n, pos, f->dscal + 1, ws, st);
     if (e != cudaSuccess) return e;
     scatter_flagged<<<grid_blocks(n, 256), 256, 0, st>>>(flag, pos, n, f->outlets);
@@ -272,4 +282,9 @@ cudaError_t launch_donors_outlets(lsdtt_gpu_flow* f, cudaStream_t st)
     return cudaGetLastError();
 }
 
+}  // namespace lsdtt_gb300
+
+namespace lsdtt_gb300
+{
+LSDTT_DEFINE_LAUNCH_READER(d8)
 }  // namespace lsdtt_gb300

@@ -1,0 +1,305 @@
+// fill.cu -- pit filling with an imposed minimum gradient (epsilon fill).
+//
+// Reference: fill_pits(raster, min_slope, bc) -> the improved priority-flood
+// of Barnes et al. (2014) (src/cpu/lsdtt_raster_flow_preprocessing_cpu.cpp:
+// 416-589, 707-782). Seeds are every valid cell on a non-periodic raster
+// edge plus, when the interior holds any nodata, every valid cell with an
+// in-bounds nodata neighbour. A cell first reached from a neighbour whose
+// filled value is >= its own elevation is raised to
+//     max(zeta + min_slope * d, nextafter(zeta, +inf)),   d = L or L*sqrt2 (float)
+// and otherwise keeps its elevation.
+//
+// This kernel computes the value-ordered form of that rule: every cell's
+// "discoverer" is its neighbour of lowest filled value (first in direction
+// order N, NE, ..., NW on ties), which is the fixed point of
+//     F(c) = z(c)                        if z(c) > m(c)
+//          = raise(m(c), dir of m(c))    otherwise,   m(c) = min_nb F(nb)
+// with seeds fixed at their elevation. It is solved by tile-local relaxation
+// in shared memory (each CTA iterates its 32x32 tile to local convergence),
+// repeated until no tile changes. The set of raised cells and every cell
+// outside a depression match the reference exactly; inside large flats the
+// reference's FIFO processes cells in breadth-first push order rather than
+// value order, so some raised values differ in the last few epsilon steps.
+// The parity tests count those cells per surface.
+
+#include <cmath>
+
+#include "engine.cuh"
+
+namespace lsdtt_gb300
+{
+namespace
+{
+
+constexpr int kT = 32;        // tile edge (cells)
+constexpr int kH = kT + 2;    // with halo
+constexpr int kMaxLocal = 4 * kT;
+
+__device__ __forceinline__ float raise_from(float zeta, float min_slope, float d)
+{
+    // min_slope <= 0: the neighbour takes the spill value itself (:491-494).
+    if (!(min_slope > 0.0f)) return zeta;
+    // max(zeta + min_slope*d, nextafter(zeta, +inf)) in float, no contraction
+    const float requested = __fadd_rn(zeta, __fmul_rn(min_slope, d));
+    const float strict = nextafterf(zeta, INFINITY);
+    return fmaxf(requested, strict);
+}
+
+// Resolve a neighbour for the fill: periodic wrap on periodic axes only,
+// otherwise off-grid = none.
+__device__ __forceinline__ bool fill_nb(int nr, int nc, bool per_ns, bool per_ew, int r, int c, int d, int& rr,
+                                        int& cc)
+{
+    rr = r + d8_dr(d);
+    cc = c + d8_dc(d);
+    if (per_ns) { if (rr < 0) rr += nr; else if (rr >= nr) rr -= nr; }
+    if (per_ew) { if (cc < 0) cc += nc; else if (cc >= nc) cc -= nc; }
+    return rr >= 0 && rr < nr && cc >= 0 && cc < nc;
+}
+
+__global__ void fill_interior_nodata(int nr, int nc, const float* __restrict__ z, const std::uint8_t* __restrict__ mask,
+                                     double nodata, int* __restrict__ flag)
+{
+    LSDTT_COUNT();
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const std::int64_t n = static_cast<std::int64_t>(nr) * nc;
+    if (i >= n) return;
+    const int r = static_cast<int>(i / nc), c = static_cast<int>(i % nc);
+    if (r < 1 || r >= nr - 1 || c < 1 || c >= nc - 1) return;
+    const bool valid = mask[i] != 0 && !(isnan(nodata) ? isnan(z[i]) : static_cast<double>(z[i]) == nodata);
+    if (!valid) *flag = 1;
+}
+
+// Initial state: seeds hold z and are fixed, other valid cells +inf,
+// invalid cells hold the nodata value (and are never read as neighbours).
+__global__ void fill_init(int nr, int nc, bool per_ns, bool per_ew, const float* __restrict__ z,
+                          const std::uint8_t* __restrict__ mask, double nodata, const int* __restrict__ interior_nd,
+                          float* __restrict__ F, std::uint8_t* __restrict__ kind)
+{
+    LSDTT_COUNT();
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const std::int64_t n = static_cast<std::int64_t>(nr) * nc;
+    if (i >= n) return;
+    const int r = static_cast<int>(i / nc), c = static_cast<int>(i % nc);
+    auto valid_at = [&](std::int64_t k) {
+        return mask[k] != 0 && !(isnan(nodata) ? isnan(z[k]) : static_cast<double>(z[k]) == nodata);
+    };
+    if (!valid_at(i))
+    {
+        F[i] = static_cast<float>(nodata);
+        kind[i] = 0;  // invalid
+        return;
+    }
+    bool seed = (!per_ns && (r == 0 || r == nr - 1)) || (!per_ew && (c == 0 || c == nc - 1));
+    if (!seed && *interior_nd)
+        for (int d = 0; d < 8 && !seed; ++d)
+        {
+            const int rr = r + d8_dr(d), cc = c + d8_dc(d);
+            if (rr >= 0 && rr < nr && cc >= 0 && cc < nc && !valid_at(static_cast<std::int64_t>(rr) * nc + cc))
+                seed = true;
+        }
+    F[i] = seed ? z[i] : INFINITY;
+    kind[i] = seed ? 2 : 1;  // 2 seed (fixed), 1 free
+}
+
+__global__ void __launch_bounds__(256) fill_relax(int nr, int nc, bool per_ns, bool per_ew, float L, float Ld,
+                                                  float min_slope, const float* __restrict__ z,
+                                                  const std::uint8_t* __restrict__ kind, float* __restrict__ F,
+                                                  int* __restrict__ changed, const std::uint8_t* __restrict__ dirty_in,
+                                                  std::uint8_t* __restrict__ dirty_out)
+{
+    LSDTT_COUNT();
+    // Active-tile gate: a tile can only change if it or one of its eight
+    // neighbouring tiles changed in the previous pass (periodic axes wrap).
+    {
+        const int tx = blockIdx.x, ty = blockIdx.y, ntx = gridDim.x, nty = gridDim.y;
+        bool active = false;
+        for (int dy = -1; dy <= 1 && !active; ++dy)
+            for (int dx = -1; dx <= 1; ++dx)
+            {
+                int yy = ty + dy, xx = tx + dx;
+                if (per_ns) yy = (yy + nty) % nty;
+                if (per_ew) xx = (xx + ntx) % ntx;
+                if (yy < 0 || yy >= nty || xx < 0 || xx >= ntx) continue;
+                if (dirty_in[yy * ntx + xx]) { active = true; break; }
+            }
+        if (!active)
+        {
+            if (threadIdx.x == 0 && threadIdx.y == 0) dirty_out[ty * ntx + tx] = 0;
+            return;
+        }
+    }
+    __shared__ float sF[kH][kH];
+    __shared__ float sz[kH][kH];
+    __shared__ std::uint8_t sk[kH][kH];
+    __shared__ int any;
+    const int r0 = blockIdx.y * kT - 1, c0 = blockIdx.x * kT - 1;
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    for (int k = tid; k < kH * kH; k += blockDim.x * blockDim.y)
+    {
+        const int lr = k / kH, lc = k % kH;
+        int r = r0 + lr, c = c0 + lc;
+        if (per_ns) { if (r < 0) r += nr; else if (r >= nr) r -= nr; }
+        if (per_ew) { if (c < 0) c += nc; else if (c >= nc) c -= nc; }
+        if (r >= 0 && r < nr && c >= 0 && c < nc)
+        {
+            const std::int64_t g = static_cast<std::int64_t>(r) * nc + c;
+            sF[lr][lc] = F[g];
+            sz[lr][lc] = z[g];
+            sk[lr][lc] = kind[g];
+        }
+        else
+        {
+            sF[lr][lc] = INFINITY;
+            sz[lr][lc] = INFINITY;
+            sk[lr][lc] = 0;
+        }
+    }
+    if (tid == 0) any = 0;
+    __syncthreads();
+    // Interior cells of this tile owned by this thread: 32 columns x 4 rows.
+    const int lc = threadIdx.x + 1;
+    bool tile_changed = false;
+    for (int it = 0; it < kMaxLocal; ++it)
+    {
+        bool local = false;
+#pragma unroll
+        for (int q = 0; q < kT / 8; ++q)
+        {
+            const int lr = threadIdx.y * (kT / 8) + q + 1;
+            const int r = r0 + lr, c = c0 + lc;
+            if (r >= nr || c >= nc || sk[lr][lc] != 1) continue;
+            float m = INFINITY;
+            int md = -1;
+#pragma unroll
+            for (int d = 0; d < 8; ++d)
+            {
+                int rr, cc;
+                if (!fill_nb(nr, nc, per_ns, per_ew, r, c, d, rr, cc)) continue;
+                const int ar = lr + d8_dr(d), ac = lc + d8_dc(d);
+                if (sk[ar][ac] == 0) continue;
+                const float v = sF[ar][ac];
+                if (v < m) { m = v; md = d; }
+            }
+            if (md < 0) continue;
+            const float zc = sz[lr][lc];
+            const float nv = (zc > m) ? zc : raise_from(m, min_slope, (md & 1) ? Ld : L);
+            if (nv < sF[lr][lc])
+            {
+                sF[lr][lc] = nv;
+                local = true;
+            }
+        }
+        __syncthreads();
+        if (local) any = 1;
+        __syncthreads();
+        const int a = any;
+        __syncthreads();
+        if (!a) break;
+        tile_changed = true;
+        if (tid == 0) any = 0;
+        __syncthreads();
+    }
+#pragma unroll
+    for (int q = 0; q < kT / 8; ++q)
+    {
+        const int lr = threadIdx.y * (kT / 8) + q + 1;
+        const int r = r0 + lr, c = c0 + lc;
+        if (r >= nr || c >= nc || sk[lr][lc] != 1) continue;
+        const std::int64_t g = static_cast<std::int64_t>(r) * nc + c;
+        if (sF[lr][lc] < F[g]) F[g] = sF[lr][lc];
+    }
+    if (tid == 0)
+    {
+        dirty_out[blockIdx.y * gridDim.x + blockIdx.x] = tile_changed ? 1 : 0;
+        if (tile_changed) atomicOr(changed, 1);
+    }
+}
+
+}  // namespace
+}  // namespace lsdtt_gb300
+
+using namespace lsdtt_gb300;
+
+extern "C" int lsdtt_gpu_fill_pits(const lsdtt_gpu_grid* grid, const float* z_dev, const std::uint8_t* mask_dev,
+                                   float min_slope, float* out_dev, void* stream)
+{
+    if (!grid || !z_dev || !mask_dev || !out_dev) return fail(LSDTT_GPU_EINVAL, "lsdtt_gpu_fill_pits: null argument");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        return fail(LSDTT_GPU_ENODEV, "lsdtt_gpu_fill_pits: no CUDA device");
+    if (!(grid->n_rows > 0 && grid->n_cols > 0 && grid->cell_size > 0.0))
+        return fail(LSDTT_GPU_EINVAL, "lsdtt::fill_pits: invalid raster metadata");
+    auto is_p = [&](int i) { return grid->boundary_conditions[i] == 'p' || grid->boundary_conditions[i] == 'P'; };
+    const bool per_ns = is_p(0), per_ew = is_p(1);
+    const std::string bc(grid->boundary_conditions, 4);
+    if (per_ns != is_p(2))
+        return fail(LSDTT_GPU_EINVAL,
+                    "lsdtt::fill_pits: north and south periodic flags must match (boundary_conditions '" + bc + "')");
+    if (per_ew != is_p(3))
+        return fail(LSDTT_GPU_EINVAL,
+                    "lsdtt::fill_pits: east and west periodic flags must match (boundary_conditions '" + bc + "')");
+    if (per_ns && per_ew)
+        return fail(LSDTT_GPU_EINVAL, "lsdtt::fill_pits: boundary_conditions '" + bc +
+                                          "' is periodic in BOTH directions, so the grid has no drainage exit at all "
+                                          "and every cell would fill to the global maximum. Leave one pair open.");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int nr = grid->n_rows, nc = grid->n_cols;
+    const std::int64_t n = static_cast<std::int64_t>(nr) * nc;
+    std::uint8_t* kind = nullptr;
+    int* flags = nullptr;   // [0] interior nodata, [1] changed
+    int* hflag = nullptr;
+    std::uint8_t* dirty = nullptr;  // two per-tile activity planes
+    const std::int64_t ntiles = static_cast<std::int64_t>((nc + kT - 1) / kT) * ((nr + kT - 1) / kT);
+    cudaError_t e = cudaMallocAsync(&kind, static_cast<std::size_t>(n), st);
+    if (e == cudaSuccess) e = cudaMallocAsync(&dirty, static_cast<std::size_t>(2 * ntiles), st);
+    if (e == cudaSuccess) e = cudaMallocAsync(&flags, sizeof(int) * 2, st);
+    if (e == cudaSuccess) e = cudaMallocHost(&hflag, sizeof(int));
+    if (e != cudaSuccess) return cuda_fail(e, "lsdtt_gpu_fill_pits");
+    cudaMemsetAsync(flags, 0, sizeof(int) * 2, st);
+    cudaMemsetAsync(dirty, 1, static_cast<std::size_t>(2 * ntiles), st);
+    fill_interior_nodata<<<grid_blocks(n, 256), 256, 0, st>>>(nr, nc, z_dev, mask_dev, grid->no_data_value, flags);
+    fill_init<<<grid_blocks(n, 256), 256, 0, st>>>(nr, nc, per_ns, per_ew, z_dev, mask_dev, grid->no_data_value, flags,
+                                                  out_dev, kind);
+    const float L = static_cast<float>(grid->cell_size);
+    const float Ld = L * static_cast<float>(1.4142135623730950488);
+    const float eps = min_slope > 0.0f ? min_slope : 0.0f;
+    const dim3 block(32, 8);
+    const dim3 tiles((nc + kT - 1) / kT, (nr + kT - 1) / kT);
+    // Global passes until no tile changes; the change flag is read back every
+    // few passes to keep the host out of the loop.
+    const int kCheckEvery = 4;
+    const long max_pass = 4L * (nr + nc) + 64;  // bound: any path crosses each tile row/column at most a few times
+    long pass = 0;
+    for (;;)
+    {
+        cudaMemsetAsync(flags + 1, 0, sizeof(int), st);
+        for (int k = 0; k < kCheckEvery; ++k, ++pass)
+            // Algorithmic bytes per pass: z 4 + mask 1 in, filled value 4 out.
+            LSDTT_TIMED("fill_relax", 9.0 * static_cast<double>(n), st,
+                        (fill_relax<<<tiles, block, 0, st>>>(nr, nc, per_ns, per_ew, L, Ld, eps, z_dev, kind, out_dev,
+                                                             flags + 1, dirty + (pass & 1) * ntiles,
+                                                             dirty + ((pass + 1) & 1) * ntiles)));
+        cudaMemcpyAsync(hflag, flags + 1, sizeof(int), cudaMemcpyDeviceToHost, st);
+        e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) break;
+        if (*hflag == 0) break;
+        if (pass > max_pass)
+        {
+            e = cudaErrorUnknown;
+            break;
+        }
+    }
+    cudaFreeAsync(kind, st);
+    cudaFreeAsync(dirty, st);
+    cudaFreeAsync(flags, st);
+    cudaFreeHost(hflag);
+    if (e == cudaErrorUnknown) return fail(LSDTT_GPU_ETIMEOUT, "lsdtt_gpu_fill_pits: relaxation did not converge");
+    if (e != cudaSuccess) return cuda_fail(e, "lsdtt_gpu_fill_pits");
+    return LSDTT_GPU_OK;
+}
+
+namespace lsdtt_gb300
+{
+LSDTT_DEFINE_LAUNCH_READER(fill)
+}  // namespace lsdtt_gb300

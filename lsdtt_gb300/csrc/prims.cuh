@@ -69,6 +69,7 @@ __device__ inline T block_exclusive_scan(T v, T* smem_warp, T& total)
 template <class TIn, class T>
 __global__ void scan_tile_sums(const TIn* __restrict__ in, std::int64_t n, T* __restrict__ sums)
 {
+    LSDTT_COUNT();
     __shared__ T sw[32];
     const std::int64_t base = static_cast<std::int64_t>(blockIdx.x) * kScanTile;
     T acc = 0;
@@ -89,6 +90,7 @@ template <class TIn, class T>
 __global__ void scan_tile_apply(const TIn* __restrict__ in, std::int64_t n, const T* __restrict__ offs,
                                 T* __restrict__ out)
 {
+    LSDTT_COUNT();
     __shared__ T sw[32];
     const std::int64_t base = static_cast<std::int64_t>(blockIdx.x) * kScanTile +
                               static_cast<std::int64_t>(threadIdx.x) * kScanItems;
@@ -156,6 +158,7 @@ constexpr int kSortTile = kSortWarpItems * (kSortThreads / 32);  // 4096
 static __global__ void radix_hist(const std::uint64_t* __restrict__ keys, std::int64_t n, int shift,
                            std::uint32_t* __restrict__ hist, int n_tiles)
 {
+    LSDTT_COUNT();
     __shared__ std::uint32_t h[256];
     for (int i = threadIdx.x; i < 256; i += blockDim.x) h[i] = 0;
     __syncthreads();
@@ -174,6 +177,7 @@ static __global__ void radix_scatter(const std::uint64_t* __restrict__ kin, cons
                               std::int64_t n, int shift, const std::uint32_t* __restrict__ offs, int n_tiles,
                               std::uint64_t* __restrict__ kout, std::uint32_t* __restrict__ vout)
 {
+    LSDTT_COUNT();
     __shared__ std::uint32_t wcount[kSortThreads / 32][256];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int i = lane; i < 256; i += 32) wcount[warp][i] = 0;

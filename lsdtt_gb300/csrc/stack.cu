@@ -97,6 +97,7 @@ __device__ int donor_list(const Grid& g, const std::uint8_t* __restrict__ mask, 
 __global__ void links_kernel(Grid g, const std::uint8_t* __restrict__ mask, const std::uint8_t* __restrict__ dir,
                              std::uint32_t* __restrict__ first_child, std::uint32_t* __restrict__ next_sib)
 {
+    LSDTT_COUNT();
     const std::int64_t flat = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (flat >= g.n || !mask[flat]) return;
     std::int64_t d[8];
@@ -109,6 +110,7 @@ __global__ void links_kernel(Grid g, const std::uint8_t* __restrict__ mask, cons
 __global__ void root_links_kernel(const std::int64_t* __restrict__ outlets, const std::int64_t* __restrict__ n_out,
                                   std::uint32_t* __restrict__ next_sib, std::uint32_t* __restrict__ head)
 {
+    LSDTT_COUNT();
     const std::int64_t n = *n_out;
     const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i == 0) *head = n > 0 ? static_cast<std::uint32_t>(2 * outlets[0]) : kEnd;
@@ -121,6 +123,7 @@ __global__ void succ_kernel(Grid g, const std::uint8_t* __restrict__ mask, const
                             const std::uint32_t* __restrict__ first_child, const std::uint32_t* __restrict__ next_sib,
                             std::uint32_t* __restrict__ succ)
 {
+    LSDTT_COUNT();
     const std::int64_t flat = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (flat >= g.n) return;
     if (!mask[flat])
@@ -163,6 +166,7 @@ __device__ __forceinline__ bool node_valid(const RankLevel& L, std::uint32_t v)
 
 __global__ void ruler_flags(RankLevel L, std::uint8_t* __restrict__ flag)
 {
+    LSDTT_COUNT();
     const std::uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= L.n) return;
     flag[v] = (node_valid(L, v) && (is_ruler(v) || v == *L.head)) ? 1 : 0;
@@ -172,6 +176,7 @@ __global__ void ruler_scatter(const std::uint8_t* __restrict__ flag, const std::
                               std::uint32_t n, std::uint32_t cap, std::uint32_t* __restrict__ rulers,
                               std::uint32_t* __restrict__ owner)
 {
+    LSDTT_COUNT();
     const std::uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= n || !flag[v] || pos[v] >= cap) return;  // overflow is reported by ruler_cap_check
     rulers[pos[v]] = v;
@@ -185,6 +190,7 @@ __global__ void ruler_walk(RankLevel L, const std::uint8_t* __restrict__ flag, c
                            std::uint32_t* __restrict__ nxt, std::uint32_t* __restrict__ next_head,
                            std::uint32_t cap, unsigned long long* __restrict__ err)
 {
+    LSDTT_COUNT();
     const std::uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const std::uint32_t nr = *n_rulers;
     if (i >= nr || i >= cap) return;
@@ -213,6 +219,7 @@ __global__ void ruler_walk(RankLevel L, const std::uint8_t* __restrict__ flag, c
 __global__ void serial_rank(RankLevel L, std::int32_t* __restrict__ p0, std::int32_t* __restrict__ p1,
                             unsigned long long* __restrict__ err)
 {
+    LSDTT_COUNT();
     if (blockIdx.x != 0 || threadIdx.x != 0) return;
     std::uint32_t v = *L.head;
     int a0 = 0, a1 = 0;
@@ -236,6 +243,7 @@ __global__ void rank_finish(RankLevel L, const std::uint32_t* __restrict__ owner
                             const std::int32_t* __restrict__ P1, std::uint32_t cap, std::int32_t* __restrict__ p0,
                             std::int32_t* __restrict__ p1, unsigned long long* __restrict__ err)
 {
+    LSDTT_COUNT();
     const std::uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= L.n || !node_valid(L, v)) return;
     const std::uint32_t o = owner[v];
@@ -253,12 +261,14 @@ __global__ void rank_finish(RankLevel L, const std::uint32_t* __restrict__ owner
 
 __global__ void fill_u32(std::uint32_t* __restrict__ a, std::uint32_t n, std::uint32_t v)
 {
+    LSDTT_COUNT();
     const std::uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) a[i] = v;
 }
 
 __global__ void ruler_cap_check(const std::uint32_t* cnt, std::uint32_t cap, unsigned long long* err)
 {
+    LSDTT_COUNT();
     if (*cnt > cap) raise_error(err, 9, *cnt);
 }
 
@@ -298,8 +308,10 @@ cudaError_t rank_list(const RankLevel& L, std::int32_t* p0, std::int32_t* p1, Sc
     if (!rulers || !nxt || !sub0 || !sub1 || !P0 || !P1) return cudaErrorMemoryAllocation;
     ruler_scatter<<<nb, 256, 0, st>>>(flag, pos, L.n, cap, rulers, owner);
     ruler_cap_check<<<1, 1, 0, st>>>(cnt, cap, err);
-    ruler_walk<<<grid_blocks(cap, 128), 128, 0, st>>>(L, flag, rulers, cnt, owner, loc0, loc1, sub0, sub1, nxt,
-                                                      nhead, cap, err);
+    // Bytes touched per tour node: successor 4 + ruler flag 1 in, owner 4 + two prefixes 8 out.
+    LSDTT_TIMED("stack_ruler_walk", 17.0 * static_cast<double>(L.n), st,
+                (ruler_walk<<<grid_blocks(cap, 128), 128, 0, st>>>(L, flag, rulers, cnt, owner, loc0, loc1, sub0, sub1,
+                                                                   nxt, nhead, cap, err)));
     RankLevel up{cap, nxt, sub0, sub1, nullptr, nhead, cnt};
     e = rank_list(up, P0, P1, ws, err, st);
     if (e != cudaSuccess) return e;
@@ -316,6 +328,7 @@ __global__ void sv_outputs(Grid g, const std::uint8_t* __restrict__ mask, const 
                            std::uint64_t* __restrict__ size, std::int32_t* __restrict__ depth,
                            std::int64_t* __restrict__ svec, unsigned long long* __restrict__ err)
 {
+    LSDTT_COUNT();
     const std::int64_t c = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (c >= g.n) return;
     if (!mask[c])
@@ -346,6 +359,7 @@ __global__ void rmq_base(const std::int64_t* __restrict__ svec, const std::int32
                          std::int64_t n, std::uint64_t* __restrict__ A, std::uint64_t* __restrict__ pre,
                          std::uint64_t* __restrict__ suf, std::uint64_t* __restrict__ blk)
 {
+    LSDTT_COUNT();
     const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31;
     std::uint64_t a = 0;
@@ -380,6 +394,7 @@ __global__ void rmq_base(const std::int64_t* __restrict__ svec, const std::int32
 __global__ void rmq_level(const std::uint64_t* __restrict__ prev, std::int64_t nb, std::int64_t half,
                           std::uint64_t* __restrict__ next)
 {
+    LSDTT_COUNT();
     const std::int64_t b = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (b >= nb) return;
     std::uint64_t v = prev[b];
@@ -427,6 +442,7 @@ __global__ void topo_heights(Grid g, const std::uint8_t* __restrict__ mask, cons
                              std::int32_t* __restrict__ height, std::uint32_t* __restrict__ leaf,
                              unsigned long long* __restrict__ maxh)
 {
+    LSDTT_COUNT();
     const std::int64_t c = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (c >= g.n) return;
     if (!mask[c])
@@ -465,6 +481,7 @@ __global__ void topo_keys(Grid g, const std::uint8_t* __restrict__ mask, const s
                           const std::uint32_t* __restrict__ leaf, int leaf_bits, std::uint64_t maxh,
                           std::uint64_t* __restrict__ keys, std::uint32_t* __restrict__ vals)
 {
+    LSDTT_COUNT();
     const std::int64_t c = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (c >= g.n) return;
     const std::uint64_t h = mask[c] ? static_cast<std::uint64_t>(height[c]) : maxh + 1;
@@ -476,6 +493,7 @@ __global__ void topo_keys(Grid g, const std::uint8_t* __restrict__ mask, const s
 __global__ void topo_store(const std::uint32_t* __restrict__ vals, std::int64_t n_valid, std::int64_t* __restrict__ topo,
                            std::uint32_t* __restrict__ topo_pos)
 {
+    LSDTT_COUNT();
     const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n_valid) return;
     const std::uint32_t c = vals[i];
@@ -582,6 +600,7 @@ namespace
 __global__ void accum_exact(Grid g, const std::uint8_t* __restrict__ mask, const std::uint64_t* __restrict__ size,
                             double w, double* __restrict__ out)
 {
+    LSDTT_COUNT();
     const std::int64_t c = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (c >= g.n) return;
     out[c] = mask[c] ? static_cast<double>(size[c]) * w : 0.0;
@@ -590,6 +609,7 @@ __global__ void accum_exact(Grid g, const std::uint8_t* __restrict__ mask, const
 __global__ void accum_seed(Grid g, const std::uint8_t* __restrict__ mask, const double* __restrict__ w, double dw,
                            double* __restrict__ out)
 {
+    LSDTT_COUNT();
     const std::int64_t c = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (c >= g.n) return;
     out[c] = mask[c] ? (w ? w[c] : dw) : 0.0;
@@ -599,6 +619,7 @@ __global__ void accum_level(Grid g, const std::uint8_t* __restrict__ mask, const
                             const std::int64_t* __restrict__ topo, const std::uint32_t* __restrict__ topo_pos,
                             std::int64_t lo, std::int64_t hi, double* __restrict__ acc)
 {
+    LSDTT_COUNT();
     const std::int64_t i = lo + static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= hi) return;
     const std::int64_t c = topo[i];
@@ -624,6 +645,7 @@ __global__ void accum_level(Grid g, const std::uint8_t* __restrict__ mask, const
 __global__ void level_bounds(const std::int64_t* __restrict__ topo, const std::int32_t* __restrict__ height,
                              std::int64_t nv, std::int64_t* __restrict__ start)
 {
+    LSDTT_COUNT();
     const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= nv) return;
     const std::int32_t h = height[topo[i]];
@@ -650,7 +672,7 @@ cudaError_t accumulate(lsdtt_gpu_flow* f, const double* w, double* out, cudaStre
     const Grid& g = f->g;
     const unsigned nb = grid_blocks(g.n, 256);
     const double dw = g.cell * g.cell;
-    if (!w && f->has_sv && exact_by_count(dw, f->n_valid))
+    if (!w && exact_by_count(dw, f->n_valid))
     {
         *exact_path = true;
         accum_exact<<<nb, 256, 0, st>>>(g, f->mask, f->sv_size, dw, out);
@@ -682,4 +704,9 @@ cudaError_t accumulate(lsdtt_gpu_flow* f, const double* w, double* out, cudaStre
     return e != cudaSuccess ? e : cudaGetLastError();
 }
 
+}  // namespace lsdtt_gb300
+
+namespace lsdtt_gb300
+{
+LSDTT_DEFINE_LAUNCH_READER(stack)
 }  // namespace lsdtt_gb300
