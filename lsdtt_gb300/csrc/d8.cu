@@ -6,13 +6,14 @@
 // first of equal slopes in direction order 0..7 wins.
 //
 // GB300 note: this part has very little FP64 throughput, and a double
-// division per neighbour would make the kernel compute-bound by ~50x. The
-// kernel therefore ranks neighbours with float slopes (relative error below
-// 2^-21 against the exact quotient) and only falls back to the reference's
-// double division when the two best float slopes are within 2^-18 of each
-// other, i.e. when rounding could decide the winner. Outside that band the
-// float ranking provably equals the double ranking, so the result is the
-// reference's bit for bit; inside it the double path IS the reference.
+// division per neighbour would make the kernel FP64-bound many times over.
+// The kernel therefore ranks neighbours without dividing: within a direction
+// class (all cardinal or all diagonal) the quotients share a divisor, so the
+// exact float drop orders them; between the two class winners a float screen
+// or, near a tie, two double products decide (see the comment at the
+// comparison). Cells whose drop is not exact in float, and exact cross-class
+// ties, take the reference's own double division. The result is the
+// reference's bit for bit.
 //
 // Donor counts restate build_donor_counts_and_outlets_d8 (:1359-1408) as a
 // gather: cell c counts the neighbours d whose direction code points back
@@ -102,12 +103,26 @@ __global__ void __launch_bounds__(256) receivers_kernel(Grid g, const float* __r
         return;
     }
     const float zc = z[flat];
-    // Float ranking: weights are 1/dx and 1/(dx*sqrt2) rounded to float
-    // (computed once on the host: FP64 division is costly on this part).
-    float best = 0.0f, second = 0.0f;
-    int bdir = kNoDir;
-    std::int64_t brec = kOutletReceiver;
+    // Rank per direction class. Within a class (cardinal or diagonal) every
+    // slope shares one divisor, so the reference's double quotients order
+    // exactly like the elevation drops; a drop z - z_nb computed in float is
+    // exact whenever Sterbenz's lemma applies (z_nb > 0 and z - z_nb <= z_nb,
+    // or the mirrored negative case), and the first of equal drops in
+    // direction order wins, as the reference's strict '>' does.
+    float bdz[2] = {0.0f, 0.0f};
+    int bd[2] = {kNoDir, kNoDir};
+    std::int64_t br[2] = {kOutletReceiver, kOutletReceiver};
     bool allowed_outlet = false;
+    bool inexact = false;
+    auto consider = [&](int d, std::int64_t nf) {
+        const float zn = z[nf];
+        if (!(zc > zn)) return;  // (double)zc - (double)zn <= 0
+        const float dz = __fsub_rn(zc, zn);
+        const bool exact = (zn > 0.0f && dz <= zn) || (zc < 0.0f && dz <= -zc) || zn == 0.0f || zc == 0.0f;
+        inexact |= !exact;
+        const int k = d & 1;
+        if (dz > bdz[k]) { bdz[k] = dz; bd[k] = d; br[k] = nf; }
+    };
     if (is_interior(g, row, col))
     {
 #pragma unroll
@@ -119,18 +134,7 @@ __global__ void __launch_bounds__(256) receivers_kernel(Grid g, const float* __r
                 if (interior_nodata_is_outlet) allowed_outlet = true;
                 continue;
             }
-            const float zn = z[nf];
-            if (!(zc > zn)) continue;  // (double)zc - (double)zn <= 0
-            const float s = (zc - zn) * ((d & 1) ? inv_diag : inv_card);
-            if (s > best)
-            {
-                second = best;
-                best = s;
-                bdir = d;
-                brec = nf;
-            }
-            else if (s > second)
-                second = s;
+            consider(d, nf);
         }
     }
     else
@@ -147,26 +151,47 @@ __global__ void __launch_bounds__(256) receivers_kernel(Grid g, const float* __r
                 continue;
             }
             if (nf == flat) continue;
-            const float zn = z[nf];
-            if (!(zc > zn)) continue;
-            const float s = (zc - zn) * ((d & 1) ? inv_diag : inv_card);
-            if (s > best)
-            {
-                second = best;
-                best = s;
-                bdir = d;
-                brec = nf;
-            }
-            else if (s > second)
-                second = s;
+            consider(d, nf);
         }
     }
-    // Ambiguous when the runner-up is within 2^-18 (relative) of the winner,
-    // or when float arithmetic lost the plot (non-finite, underflow to 0).
-    const bool ambiguous = (bdir != kNoDir) &&
-                           (!(best < 3.0e38f) || !(best > 1.0e-30f) || second * (1.0f + 3.814697265625e-06f) >= best);
-    if (ambiguous)
+    int bdir = kNoDir;
+    std::int64_t brec = kOutletReceiver;
+    if (inexact)
         exact_receiver(g, z, mask, row, col, bdir, brec, allowed_outlet, interior_nodata_is_outlet);
+    else if (bd[0] == kNoDir || bd[1] == kNoDir)
+    {
+        const int k = (bd[0] != kNoDir) ? 0 : 1;
+        bdir = bd[k];
+        brec = br[k];
+    }
+    else
+    {
+        // Cardinal vs diagonal: q_c = dz_c / dx against q_d = dz_d / (dx*sqrt2).
+        // A float screen settles clear cases; otherwise compare dz_c*Ld with
+        // dz_d*dx in double. For 24-bit drops the exact quotients cannot be
+        // closer than ~2^-50 relative (sqrt2 is badly approximable:
+        // |sqrt2 - p/q| > 1/(4 q^2)), so the products decide the reference's
+        // rounded comparison; a residual near-tie takes the division path.
+        const float sc = bdz[0] * inv_card, sd = bdz[1] * inv_diag;
+        int win;
+        if (sc > sd * (1.0f + 3.814697265625e-06f)) win = 0;
+        else if (sd > sc * (1.0f + 3.814697265625e-06f)) win = 1;
+        else
+        {
+            const double A = __dmul_rn(static_cast<double>(bdz[0]), g.cell * 1.4142135623730950488);
+            const double B = __dmul_rn(static_cast<double>(bdz[1]), g.cell);
+            const double gap = fabs(A - B);
+            if (gap > 8.881784197001252e-16 * fmax(A, B)) win = (A > B) ? 0 : 1;  // 2^-50
+            else win = -1;
+        }
+        if (win >= 0)
+        {
+            bdir = bd[win];
+            brec = br[win];
+        }
+        else
+            exact_receiver(g, z, mask, row, col, bdir, brec, allowed_outlet, interior_nodata_is_outlet);
+    }
     if (bdir != kNoDir)
     {
         receiver[flat] = brec;
