@@ -1,0 +1,38 @@
+"""The C++ drop-in for lsdtt3's abstract D8 seam
+(lsdtt_gb300/host/lsdtt_flowinfo_gpu.hpp) compiles against the reference's
+own headers and implements every pure virtual of lsdtt_flow_base (it is not
+abstract). Needs a reference checkout (LSDTT3_SRC or the default location);
+skipped where there is none."""
+import os
+import shutil
+import subprocess
+import tempfile
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+REF = os.environ.get("LSDTT3_SRC", "/root/reference/src")
+
+
+@pytest.mark.skipif(not os.path.isdir(REF), reason="no lsdtt3 checkout")
+def test_seam_compiles_and_is_concrete():
+    gxx = shutil.which("g++")
+    assert gxx
+    src = """
+#include "lsdtt_gb300/host/lsdtt_flowinfo_gpu.hpp"
+#include <type_traits>
+static_assert(!std::is_abstract<lsdtt::lsdtt_flowinfo_gpu>::value, "every pure virtual is implemented");
+static_assert(std::is_base_of<lsdtt::lsdtt_flow_base, lsdtt::lsdtt_flowinfo_gpu>::value, "behind the seam");
+std::unique_ptr<lsdtt::lsdtt_flow_base> make_gpu(const lsdtt::lsdtt_array2d_f& d, const lsdtt::lsdtt_array2d_u8& m,
+                                                 const lsdtt::lsdtt_raster_meta& meta,
+                                                 const lsdtt::lsdtt_flowinfo_options& o)
+{ return std::make_unique<lsdtt::lsdtt_flowinfo_gpu>(d, m, meta, o); }
+"""
+    with tempfile.TemporaryDirectory() as td:
+        f = os.path.join(td, "seam.cpp")
+        open(f, "w").write(src)
+        cmd = [gxx, "-std=c++17", "-c", f, "-o", os.path.join(td, "seam.o"), "-I", ROOT,
+               "-I", os.path.join(ROOT, "include"), "-I", os.path.join(REF, "core"), "-I", os.path.join(REF, "utils"),
+               "-I", os.path.join(REF, "cpu"), "-I", "/usr/local/cuda/include"]
+        p = subprocess.run(cmd, capture_output=True, text=True)
+        assert p.returncode == 0, p.stderr[-3000:]
