@@ -83,6 +83,20 @@ int lsdtt_gpu_profile_read(const char* kernel, double* total_ms, int64_t* launch
 int lsdtt_gpu_fill_pits(const lsdtt_gpu_grid* grid, const float* z_dev, const uint8_t* mask_dev,
                         float min_slope, float* filled_dev, void* stream);
 
+/* Allocation-free variant of lsdtt_gpu_fill_pits (no counterpart in the
+ * reference). For callers that must not have a library allocate device
+ * memory -- a host framework that has reserved the device's memory for its
+ * own allocator, or a latency-critical loop where a growing or failing
+ * stream-ordered allocation is unacceptable. Its working memory is one
+ * fixed array inside the library (16 MiB + 64 KiB, held on every device
+ * that loads the library), so grids are limited to about 4096 x 4096 cells;
+ * larger grids return LSDTT_GPU_EINVAL. Same results as
+ * lsdtt_gpu_fill_pits. The first call on a device looks up the array's
+ * device address: make it before any stream capture. All calls share the
+ * array, so calls that overlap on the GPU race; order them on one stream. */
+int lsdtt_gpu_fill_pits_noalloc(const lsdtt_gpu_grid* grid, const float* z_dev, const uint8_t* mask_dev,
+                                float min_slope, float* filled_dev, void* stream);
+
 /* ---- D8 engine (lsdtt_flowinfo) ------------------------------------------
  * Replaces lsdtt_flowinfo(dem, mask, meta, options) and the lsdtt_flow_base
  * queries built on it (src/core/lsdtt_flow_base.hpp:126-491,

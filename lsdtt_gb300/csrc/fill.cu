@@ -23,6 +23,8 @@
 // The parity tests count those cells per surface.
 
 #include <cmath>
+#include <mutex>
+#include <string>
 
 #include "engine.cuh"
 
@@ -303,3 +305,122 @@ namespace lsdtt_gb300
 {
 LSDTT_DEFINE_LAUNCH_READER(fill)
 }  // namespace lsdtt_gb300
+
+// ---------------------------------------------------------------------------
+// lsdtt_gpu_fill_pits_noalloc -- the same fill with no device allocation.
+//
+// Some callers cannot let a library allocate device memory: a host framework
+// whose caching allocator has already reserved the device's memory and
+// budgets every byte itself, or a latency-critical loop where a
+// cudaMallocAsync that has to grow its pool (or fails when the pool is
+// exhausted) is not acceptable. For them this entry point takes its working
+// memory -- the per-cell state plane, the two per-tile activity planes and
+// the convergence flags -- from one fixed array that lives in this file:
+//
+//   * The array is a file-scope __device__ variable of kFillNoAllocBytes
+//     (16 MiB + 64 KiB), allocated when the library is loaded and held by
+//     every GPU that loads it until the process exits.
+//   * It fits grids of up to about 16.7 million cells (4096 x 4096); larger
+//     grids are rejected with LSDTT_GPU_EINVAL before any work is queued.
+//   * Host code cannot use the array's name as a device address, so the
+//     first call on each device looks the address up with
+//     cudaGetSymbolAddress (with that device current) and caches it. Make
+//     that first call before any stream capture.
+//   * Every call reuses the same array and clears the parts that must start
+//     from a known state. Calls whose work overlaps on the GPU (different
+//     streams, or host threads without ordering) race on the array; keep
+//     them on one stream or otherwise ordered.
+// The caller still provides the input and output buffers.
+// ---------------------------------------------------------------------------
+static constexpr std::size_t kFillNoAllocBytes = (std::size_t(16) << 20) + (std::size_t(64) << 10);
+static __device__ __align__(256) unsigned char g_fill_noalloc_scratch[kFillNoAllocBytes];
+
+static std::mutex g_fill_noalloc_mu;
+static void* g_fill_noalloc_addr[256] = {};  // per-device address of the array, filled on first use
+
+extern "C" int lsdtt_gpu_fill_pits_noalloc(const lsdtt_gpu_grid* grid, const float* z_dev,
+                                           const std::uint8_t* mask_dev, float min_slope, float* out_dev,
+                                           void* stream)
+{
+    if (!grid || !z_dev || !mask_dev || !out_dev)
+        return fail(LSDTT_GPU_EINVAL, "lsdtt_gpu_fill_pits_noalloc: null argument");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        return fail(LSDTT_GPU_ENODEV, "lsdtt_gpu_fill_pits_noalloc: no CUDA device");
+    if (!(grid->n_rows > 0 && grid->n_cols > 0 && grid->cell_size > 0.0))
+        return fail(LSDTT_GPU_EINVAL, "lsdtt::fill_pits: invalid raster metadata");
+    auto is_p = [&](int i) { return grid->boundary_conditions[i] == 'p' || grid->boundary_conditions[i] == 'P'; };
+    const bool per_ns = is_p(0), per_ew = is_p(1);
+    const std::string bc(grid->boundary_conditions, 4);
+    if (per_ns != is_p(2))
+        return fail(LSDTT_GPU_EINVAL,
+                    "lsdtt::fill_pits: north and south periodic flags must match (boundary_conditions '" + bc + "')");
+    if (per_ew != is_p(3))
+        return fail(LSDTT_GPU_EINVAL,
+                    "lsdtt::fill_pits: east and west periodic flags must match (boundary_conditions '" + bc + "')");
+    if (per_ns && per_ew)
+        return fail(LSDTT_GPU_EINVAL, "lsdtt::fill_pits: boundary_conditions '" + bc +
+                                          "' is periodic in BOTH directions, so the grid has no drainage exit at all "
+                                          "and every cell would fill to the global maximum. Leave one pair open.");
+    const int nr = grid->n_rows, nc = grid->n_cols;
+    const std::int64_t n = static_cast<std::int64_t>(nr) * nc;
+    const std::int64_t ntiles = static_cast<std::int64_t>((nc + kT - 1) / kT) * ((nr + kT - 1) / kT);
+    // Layout inside the fixed array: flags (256 B), two activity planes
+    // (rounded to 256 B), then the per-cell state plane.
+    const std::size_t dirty_bytes = (static_cast<std::size_t>(2 * ntiles) + 255) & ~std::size_t(255);
+    const std::size_t need = 256 + dirty_bytes + static_cast<std::size_t>(n);
+    if (need > kFillNoAllocBytes)
+        return fail(LSDTT_GPU_EINVAL, "lsdtt_gpu_fill_pits_noalloc: a " + std::to_string(nr) + " x " +
+                                          std::to_string(nc) + " grid needs " + std::to_string(need) +
+                                          " bytes of scratch but the fixed scratch holds " +
+                                          std::to_string(kFillNoAllocBytes) +
+                                          " (about 4096 x 4096 cells); use lsdtt_gpu_fill_pits");
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_fail(e, "lsdtt_gpu_fill_pits_noalloc");
+    if (dev < 0 || dev >= 256) return fail(LSDTT_GPU_EINVAL, "lsdtt_gpu_fill_pits_noalloc: device index out of range");
+    void* base = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g_fill_noalloc_mu);
+        if (!g_fill_noalloc_addr[dev])
+        {
+            void* p = nullptr;
+            e = cudaGetSymbolAddress(&p, g_fill_noalloc_scratch);
+            if (e != cudaSuccess) return cuda_fail(e, "lsdtt_gpu_fill_pits_noalloc: cudaGetSymbolAddress");
+            g_fill_noalloc_addr[dev] = p;
+        }
+        base = g_fill_noalloc_addr[dev];
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    int* flags = static_cast<int*>(base);  // [0] interior nodata, [1] changed
+    std::uint8_t* dirty = static_cast<std::uint8_t*>(base) + 256;
+    std::uint8_t* kind = static_cast<std::uint8_t*>(base) + 256 + dirty_bytes;
+    // The previous call's contents are stale: reset flags and activity.
+    cudaMemsetAsync(flags, 0, sizeof(int) * 2, st);
+    cudaMemsetAsync(dirty, 1, static_cast<std::size_t>(2 * ntiles), st);
+    fill_interior_nodata<<<grid_blocks(n, 256), 256, 0, st>>>(nr, nc, z_dev, mask_dev, grid->no_data_value, flags);
+    fill_init<<<grid_blocks(n, 256), 256, 0, st>>>(nr, nc, per_ns, per_ew, z_dev, mask_dev, grid->no_data_value, flags,
+                                                  out_dev, kind);
+    const float L = static_cast<float>(grid->cell_size);
+    const float Ld = L * static_cast<float>(1.4142135623730950488);
+    const float eps = min_slope > 0.0f ? min_slope : 0.0f;
+    const dim3 block(32, 8);
+    const dim3 tiles((nc + kT - 1) / kT, (nr + kT - 1) / kT);
+    const int kCheckEvery = 4;
+    const long max_pass = 4L * (nr + nc) + 64;
+    long pass = 0;
+    int changed = 0;  // pageable host word: the read-back allocates nothing
+    for (;;)
+    {
+        cudaMemsetAsync(flags + 1, 0, sizeof(int), st);
+        for (int k = 0; k < kCheckEvery; ++k, ++pass)
+            fill_relax<<<tiles, block, 0, st>>>(nr, nc, per_ns, per_ew, L, Ld, eps, z_dev, kind, out_dev, flags + 1,
+                                                dirty + (pass & 1) * ntiles, dirty + ((pass + 1) & 1) * ntiles);
+        e = cudaMemcpyAsync(&changed, flags + 1, sizeof(int), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return cuda_fail(e, "lsdtt_gpu_fill_pits_noalloc");
+        if (changed == 0) break;
+        if (pass > max_pass) return fail(LSDTT_GPU_ETIMEOUT, "lsdtt_gpu_fill_pits_noalloc: relaxation did not converge");
+    }
+    return LSDTT_GPU_OK;
+}
