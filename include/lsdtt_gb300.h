@@ -174,6 +174,18 @@ int lsdtt_gpu_hillslope_linear_implicit(const lsdtt_gpu_grid* grid, const float*
                                         int32_t max_iter, float* z_out_dev, lsdtt_gpu_solve_report* report,
                                         void* stream);
 
+/* Backward-Euler hillslope diffusion over dt_total, linear or nonlinear
+ * (Roering critical-slope flux): compute_hillslope_newton_transient
+ * (src/cpu/lsdtt_hillslope_newton_cpu.hpp:305-310, .cpp:690-788) with the
+ * reference's sub-step controller, feasibility line search and convergence
+ * test ||F||_inf <= residual_tol (<= 0: 1e-12 m/yr). The inner linear solves
+ * are Jacobi-PCG on the lagged-coefficient operator to rel_tol. report->
+ * iterations is the total number of PCG iterations. */
+int lsdtt_gpu_hillslope_implicit(const lsdtt_gpu_grid* grid, const float* z_dev, const uint8_t* mask_dev,
+                                 const uint8_t* is_channel_dev, float D, float Sc, int32_t nonlinear, float dt_total,
+                                 double rel_tol, int32_t max_pcg_iter, double residual_tol, int32_t max_outer,
+                                 float* z_out_dev, lsdtt_gpu_solve_report* report, void* stream);
+
 /* ---- LEM timestep ----------------------------------------------------------
  * run_lem_step (src/cpu/lsdtt_lem_cpu.cpp:285-732) for the D8 coupled
  * regime with the "roering_implicit" linear hillslope model, optionally

@@ -383,3 +383,28 @@ class LandscapeModel:
             self.close()
         except Exception:
             pass
+
+
+def hillslope_implicit(z, mask, cell_size, boundary_conditions, D, Sc, dt, nonlinear=True, rel_tol=1e-8,
+                       max_pcg_iter=4000, residual_tol=1e-12, max_outer=200, is_channel=None, stream=None):
+    """Backward-Euler hillslope step over dt (linear or Roering), the
+    reference's compute_hillslope_newton_transient. Returns (z CUDA tensor,
+    SolveReport with the total PCG iteration count)."""
+    torch = _torch()
+    L = _bind_more()
+    fn = L.lsdtt_gpu_hillslope_implicit
+    vp = ctypes.c_void_p
+    fn.argtypes = [ctypes.POINTER(Grid), vp, vp, vp, ctypes.c_float, ctypes.c_float, ctypes.c_int32, ctypes.c_float,
+                   ctypes.c_double, ctypes.c_int32, ctypes.c_double, ctypes.c_int32, vp, ctypes.POINTER(SolveReport), vp]
+    fn.restype = ctypes.c_int
+    zt = _dev(z, torch.float32)
+    mt = _dev(mask, torch.uint8)
+    ct = None if is_channel is None else _dev(is_channel, torch.uint8)
+    g = make_grid(zt.shape[0], zt.shape[1], cell_size, boundary_conditions)
+    out = torch.empty_like(zt)
+    rep = SolveReport()
+    _check(fn(ctypes.byref(g), vp(zt.data_ptr()), vp(mt.data_ptr()), vp(ct.data_ptr() if ct is not None else 0),
+              ctypes.c_float(D), ctypes.c_float(Sc), ctypes.c_int32(int(nonlinear)), ctypes.c_float(dt),
+              ctypes.c_double(rel_tol), ctypes.c_int32(max_pcg_iter), ctypes.c_double(residual_tol),
+              ctypes.c_int32(max_outer), vp(out.data_ptr()), ctypes.byref(rep), _stream(stream)))
+    return out, rep

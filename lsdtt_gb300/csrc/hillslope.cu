@@ -339,3 +339,473 @@ namespace lsdtt_gb300
 {
 LSDTT_DEFINE_LAUNCH_READER(hillslope)
 }  // namespace lsdtt_gb300
+
+// ===========================================================================
+// Nonlinear (Roering) implicit step.
+//
+// compute_hillslope_newton_transient with nonlinear = true: the face
+// coefficient alpha_f = 1/(1 - min((S_n^2 + S_t^2)/Sc^2, cap)) with the
+// tangential slope averaged across the face (operator_cpu.hpp:229-321), so
+// alpha is a property of the face and the lagged-coefficient (Picard)
+// operator
+//     (A x)_P = inv_dt x_P + (D/h^2) sum_f alpha_f (x_P - [nb DOF] x_nb)
+// is symmetric positive definite. Each outer iteration evaluates F(z) in
+// FP64 on an FP64 working field, solves A(alpha(z)) dz = -F by Jacobi-PCG
+// (FP32 vectors, FP64 dot products, relative residual rel_tol) and takes the
+// largest step lambda = 1, 1/2, ... that keeps every face sub-critical and
+// lowers ||F||_inf, restoring feasibility first when the iterate starts
+// super-critical (newton_cpu.cpp:553-641). Converged when ||F||_inf <=
+// residual_tol (1e-12 m/yr, the reference's default). Sub-steps follow the
+// reference controller (newton_cpu.cpp:690-788): start with the whole dt,
+// halve on failure, grow x1.7 after an easy step. The outer iteration is a
+// fixed point on the symmetric operator rather than the reference's Newton
+// on the 9-point Jacobian, so iteration counts differ; the converged field
+// is the same root of F.
+// ===========================================================================
+namespace lsdtt_gb300
+{
+namespace
+{
+
+struct HsN
+{
+    Hs H;
+    double Sc2;
+    double cap;
+    double h;
+    int nonlinear;
+};
+
+__device__ __forceinline__ double hs_slope_x(const HsN& P, const std::uint8_t* mask, const double* z, int r, int c)
+{
+    const std::int64_t e = hs_nb(P.H, mask, r, c, 0, 1), w = hs_nb(P.H, mask, r, c, 0, -1);
+    return (z[e] - z[w]) / (2.0 * P.h);
+}
+
+__device__ __forceinline__ double hs_slope_y(const HsN& P, const std::uint8_t* mask, const double* z, int r, int c)
+{
+    const std::int64_t s = hs_nb(P.H, mask, r, c, 1, 0), n = hs_nb(P.H, mask, r, c, -1, 0);
+    return (z[s] - z[n]) / (2.0 * P.h);
+}
+
+// Per DOF: face alphas (float4 N,E,S,W), residual F (double), and the
+// reductions ||F||_inf, ||F||_2^2, max |grad z|/Sc (feasibility).
+__global__ void hsn_eval(HsN P, const std::uint8_t* __restrict__ mask, const std::uint8_t* __restrict__ dof,
+                         const double* __restrict__ z, const double* __restrict__ zn, float4* __restrict__ alpha,
+                         double* __restrict__ F, double* __restrict__ acc)
+{
+    LSDTT_COUNT();
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const std::int64_t n = static_cast<std::int64_t>(P.H.nr) * P.H.nc;
+    double finf = 0.0, f2 = 0.0, ratio = 0.0;
+    if (i < n && dof[i])
+    {
+        const int r = static_cast<int>(i / P.H.nc), c = static_cast<int>(i % P.H.nc);
+        const double zc = z[i];
+        const double sxc = P.nonlinear ? hs_slope_x(P, mask, z, r, c) : 0.0;
+        const double syc = P.nonlinear ? hs_slope_y(P, mask, z, r, c) : 0.0;
+        double a[4];
+        double flux = 0.0;
+#pragma unroll
+        for (int f = 0; f < 4; ++f)
+        {
+            const std::int64_t j = hs_nb(P.H, mask, r, c, kDr[f], kDc[f]);
+            const double sn = (z[j] - zc) / P.h;
+            double al = 1.0;
+            if (P.nonlinear)
+            {
+                const int jr = static_cast<int>(j / P.H.nc), jc = static_cast<int>(j % P.H.nc);
+                const double st = (f == 0 || f == 2) ? 0.5 * (sxc + hs_slope_x(P, mask, z, jr, jc))
+                                                     : 0.5 * (syc + hs_slope_y(P, mask, z, jr, jc));
+                const double s2 = fmin((sn * sn + st * st) / P.Sc2, P.cap);
+                al = 1.0 / (1.0 - s2);
+            }
+            a[f] = al;
+            flux += al * sn * P.h;
+        }
+        alpha[i] = make_float4(static_cast<float>(a[0]), static_cast<float>(a[1]), static_cast<float>(a[2]),
+                               static_cast<float>(a[3]));
+        double Fv = -P.H.U - P.H.DA * flux;
+        if (P.H.inv_dt > 0.0) Fv += P.H.inv_dt * (zc - zn[i]);
+        F[i] = Fv;
+        finf = fabs(Fv);
+        f2 = Fv * Fv;
+        if (P.nonlinear) ratio = sqrt(sxc * sxc + syc * syc) / sqrt(P.Sc2);
+    }
+    else if (i < n)
+    {
+        F[i] = 0.0;
+        alpha[i] = make_float4(1.f, 1.f, 1.f, 1.f);
+    }
+    for (int o = 16; o > 0; o >>= 1)
+    {
+        finf = fmax(finf, __shfl_down_sync(0xffffffffu, finf, o));
+        f2 += __shfl_down_sync(0xffffffffu, f2, o);
+        ratio = fmax(ratio, __shfl_down_sync(0xffffffffu, ratio, o));
+    }
+    if ((threadIdx.x & 31) == 0)
+    {
+        atomicMax(reinterpret_cast<unsigned long long*>(&acc[0]), __double_as_longlong(finf));
+        atomicAdd(&acc[1], f2);
+        atomicMax(reinterpret_cast<unsigned long long*>(&acc[2]), __double_as_longlong(ratio));
+    }
+}
+
+// PCG set-up for A(alpha) x = -F: inverse diagonal, b, x = 0, r = b,
+// p = M^-1 r, acc[0] = r.z, acc[1] = ||b||^2.
+__global__ void hsn_pcg_init(HsN P, const std::uint8_t* __restrict__ mask, const std::uint8_t* __restrict__ dof,
+                             const float4* __restrict__ alpha, const double* __restrict__ F,
+                             float* __restrict__ invd, float* __restrict__ b, float* __restrict__ x,
+                             float* __restrict__ r, float* __restrict__ p, double* __restrict__ acc)
+{
+    LSDTT_COUNT();
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const std::int64_t n = static_cast<std::int64_t>(P.H.nr) * P.H.nc;
+    double rz = 0.0, bb = 0.0;
+    if (i < n)
+    {
+        float id = 0.0f, bi = 0.0f;
+        if (dof[i])
+        {
+            const int rr = static_cast<int>(i / P.H.nc), cc = static_cast<int>(i % P.H.nc);
+            const float4 a = alpha[i];
+            const float av[4] = {a.x, a.y, a.z, a.w};
+            double diag = P.H.inv_dt;
+#pragma unroll
+            for (int f = 0; f < 4; ++f)
+                if (hs_nb(P.H, mask, rr, cc, kDr[f], kDc[f]) != i) diag += P.H.DA * av[f];
+            id = static_cast<float>(1.0 / diag);
+            bi = static_cast<float>(-F[i]);
+        }
+        invd[i] = id;
+        b[i] = bi;
+        x[i] = 0.0f;
+        r[i] = bi;
+        const float zi = bi * id;
+        p[i] = zi;
+        rz = static_cast<double>(bi) * zi;
+        bb = static_cast<double>(bi) * bi;
+    }
+    for (int o = 16; o > 0; o >>= 1)
+    {
+        rz += __shfl_down_sync(0xffffffffu, rz, o);
+        bb += __shfl_down_sync(0xffffffffu, bb, o);
+    }
+    if ((threadIdx.x & 31) == 0)
+    {
+        atomicAdd(&acc[0], rz);
+        atomicAdd(&acc[1], bb);
+    }
+}
+
+__global__ void hsn_apply(HsN P, const std::uint8_t* __restrict__ mask, const std::uint8_t* __restrict__ dof,
+                          const float4* __restrict__ alpha, const float* __restrict__ p, float* __restrict__ Ap,
+                          double* __restrict__ acc_it)
+{
+    LSDTT_COUNT();
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const std::int64_t n = static_cast<std::int64_t>(P.H.nr) * P.H.nc;
+    double pap = 0.0;
+    if (i < n)
+    {
+        float v = 0.0f;
+        if (dof[i])
+        {
+            const int rr = static_cast<int>(i / P.H.nc), cc = static_cast<int>(i % P.H.nc);
+            const float4 a = alpha[i];
+            const float av[4] = {a.x, a.y, a.z, a.w};
+            const float pi = p[i];
+            double diag = P.H.inv_dt, off = 0.0;
+#pragma unroll
+            for (int f = 0; f < 4; ++f)
+            {
+                const std::int64_t j = hs_nb(P.H, mask, rr, cc, kDr[f], kDc[f]);
+                if (j == i) continue;
+                diag += P.H.DA * av[f];
+                if (dof[j]) off += P.H.DA * av[f] * p[j];
+            }
+            v = static_cast<float>(diag * pi - off);
+            pap = static_cast<double>(pi) * v;
+        }
+        Ap[i] = v;
+    }
+    for (int o = 16; o > 0; o >>= 1) pap += __shfl_down_sync(0xffffffffu, pap, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(&acc_it[0], pap);
+}
+
+// z_try = z + lambda * dz on DOFs (double)
+__global__ void hsn_axpy(std::int64_t n, const std::uint8_t* __restrict__ dof, const double* __restrict__ z,
+                         const float* __restrict__ dz, double lambda, double* __restrict__ zt)
+{
+    LSDTT_COUNT();
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    zt[i] = dof[i] ? z[i] + lambda * static_cast<double>(dz[i]) : z[i];
+}
+
+__global__ void hsn_to_double(std::int64_t n, const float* __restrict__ a, double* __restrict__ b)
+{
+    LSDTT_COUNT();
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < n) b[i] = a[i];
+}
+
+__global__ void hsn_to_float(std::int64_t n, const double* __restrict__ a, float* __restrict__ b)
+{
+    LSDTT_COUNT();
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < n) b[i] = static_cast<float>(a[i]);
+}
+
+struct HsnBuf
+{
+    std::uint8_t* dof;
+    double *z, *zn, *zt, *F, *acc;
+    float4* alpha;
+    float *invd, *b, *x, *r, *p, *zz, *Ap;
+    double* hacc;
+};
+
+// One evaluation of alpha, F and the norms at z (device), read back.
+cudaError_t hsn_evaluate(const HsN& P, const std::uint8_t* mask, HsnBuf& B, const double* z, std::int64_t n,
+                         cudaStream_t st, double out[3])
+{
+    cudaMemsetAsync(B.acc, 0, sizeof(double) * 3, st);
+    hsn_eval<<<grid_blocks(n, 256), 256, 0, st>>>(P, mask, B.dof, z, B.zn, B.alpha, B.F, B.acc);
+    cudaMemcpyAsync(B.hacc, B.acc, sizeof(double) * 3, cudaMemcpyDeviceToHost, st);
+    cudaError_t e = cudaStreamSynchronize(st);
+    out[0] = B.hacc[0];
+    out[1] = B.hacc[1];
+    out[2] = B.hacc[2];
+    return e;
+}
+
+// PCG on A(alpha) dz = -F; returns iterations, sets *rel.
+cudaError_t hsn_pcg(const HsN& P, const std::uint8_t* mask, HsnBuf& B, std::int64_t n, double rel_tol, int max_iter,
+                    cudaStream_t st, int* iters, double* rel, double* acc_it_base)
+{
+    const unsigned nb = grid_blocks(n, 256);
+    cudaMemsetAsync(acc_it_base, 0, sizeof(double) * (2 + 3 * (max_iter + 1)), st);
+    hsn_pcg_init<<<nb, 256, 0, st>>>(P, mask, B.dof, B.alpha, B.F, B.invd, B.b, B.x, B.r, B.p, acc_it_base);
+    cudaMemcpyAsync(B.hacc, acc_it_base, sizeof(double) * 2, cudaMemcpyDeviceToHost, st);
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return e;
+    const double bnorm = std::sqrt(B.hacc[1]);
+    int it = 0;
+    *rel = 0.0;
+    if (bnorm == 0.0) { *iters = 0; return cudaSuccess; }
+    const int kCheck = 4;
+    bool done = false;
+    while (!done && it < max_iter)
+    {
+        const int batch = std::min(kCheck, max_iter - it);
+        for (int k = 0; k < batch; ++k, ++it)
+        {
+            double* cur = acc_it_base + 2 + 3 * it;
+            const double* rz_prev = (it == 0) ? acc_it_base : acc_it_base + 2 + 3 * (it - 1) + 1;
+            LSDTT_TIMED("hillslope_apply", 8.0 * static_cast<double>(n), st,
+                        (hsn_apply<<<nb, 256, 0, st>>>(P, mask, B.dof, B.alpha, B.p, B.Ap, cur)));
+            hs_update<<<nb, 256, 0, st>>>(n, rz_prev, cur, B.invd, B.p, B.Ap, B.x, B.r, B.zz, cur);
+            hs_direction<<<nb, 256, 0, st>>>(n, rz_prev, cur + 1, B.zz, B.p);
+        }
+        cudaMemcpyAsync(B.hacc, acc_it_base + 2 + 3 * (it - 1), sizeof(double) * 3, cudaMemcpyDeviceToHost, st);
+        e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return e;
+        *rel = std::sqrt(B.hacc[2]) / bnorm;
+        done = *rel <= rel_tol;
+    }
+    *iters = it;
+    return cudaSuccess;
+}
+
+}  // namespace
+}  // namespace lsdtt_gb300
+
+extern "C" int lsdtt_gpu_hillslope_implicit(const lsdtt_gpu_grid* grid, const float* z_dev, const std::uint8_t* mask_dev,
+                                            const std::uint8_t* is_channel_dev, float D, float Sc, int32_t nonlinear,
+                                            float dt_total, double rel_tol, int32_t max_pcg_iter, double residual_tol,
+                                            int32_t max_outer, float* z_out_dev, lsdtt_gpu_solve_report* report,
+                                            void* stream)
+{
+    using namespace lsdtt_gb300;
+    if (!grid || !z_dev || !mask_dev || !z_out_dev)
+        return fail(LSDTT_GPU_EINVAL, "lsdtt_gpu_hillslope_implicit: null argument");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        return fail(LSDTT_GPU_ENODEV, "lsdtt_gpu_hillslope_implicit: no CUDA device");
+    if (!(grid->n_rows > 0 && grid->n_cols > 0 && grid->cell_size > 0.0))
+        return fail(LSDTT_GPU_EINVAL, "lsdtt_gpu_hillslope_implicit: raster metadata is invalid");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const std::int64_t n = static_cast<std::int64_t>(grid->n_rows) * grid->n_cols;
+    const unsigned nb = grid_blocks(n, 256);
+    HsN P{};
+    P.H.nr = grid->n_rows;
+    P.H.nc = grid->n_cols;
+    const char* bc = grid->boundary_conditions;
+    P.H.bn = bc[0]; P.H.be = bc[1]; P.H.bs = bc[2]; P.H.bw = bc[3];
+    P.h = grid->cell_size;
+    P.H.DA = static_cast<double>(D) / (P.h * P.h);
+    P.H.U = 0.0;
+    P.Sc2 = static_cast<double>(Sc) * static_cast<double>(Sc);
+    P.cap = 0.9999;
+    P.nonlinear = nonlinear ? 1 : 0;
+    const int kPcg = max_pcg_iter > 0 ? max_pcg_iter : 2000;
+    const int kOuter = max_outer > 0 ? max_outer : 200;
+    const double ftol = residual_tol > 0 ? residual_tol : 1e-12;
+    const double rtol = rel_tol > 0 ? rel_tol : 1e-8;
+    if (!(dt_total > 0.0f))
+    {
+        // dt_total <= 0: nothing to integrate (newton_cpu.cpp:700-706).
+        cudaMemcpyAsync(z_out_dev, z_dev, sizeof(float) * n, cudaMemcpyDeviceToDevice, st);
+        const cudaError_t e0 = cudaStreamSynchronize(st);
+        return e0 == cudaSuccess ? LSDTT_GPU_OK : cuda_fail(e0, "lsdtt_gpu_hillslope_implicit");
+    }
+    // Buffers: doubles z, zn, zt, F; float4 alpha; 7 floats; dof; reductions.
+    HsnBuf B{};
+    const std::size_t need = static_cast<std::size_t>(n) * (4 * 8 + 16 + 7 * 4 + 1) + 64 * 256 +
+                             sizeof(double) * (8 + 3 * (kPcg + 1));
+    char* base = nullptr;
+    cudaError_t e = cudaMallocAsync(&base, need, st);
+    if (e == cudaSuccess) e = cudaMallocHost(&B.hacc, sizeof(double) * 8);
+    if (e != cudaSuccess)
+    {
+        if (base) cudaFreeAsync(base, st);
+        return cuda_fail(e, "lsdtt_gpu_hillslope_implicit");
+    }
+    char* cur = base;
+    auto carve = [&](std::size_t bytes) {
+        char* p = cur;
+        cur += (bytes + 255) & ~std::size_t(255);
+        return p;
+    };
+    B.z = reinterpret_cast<double*>(carve(8 * n));
+    B.zn = reinterpret_cast<double*>(carve(8 * n));
+    B.zt = reinterpret_cast<double*>(carve(8 * n));
+    B.F = reinterpret_cast<double*>(carve(8 * n));
+    B.alpha = reinterpret_cast<float4*>(carve(16 * n));
+    B.invd = reinterpret_cast<float*>(carve(4 * n));
+    B.b = reinterpret_cast<float*>(carve(4 * n));
+    B.x = reinterpret_cast<float*>(carve(4 * n));
+    B.r = reinterpret_cast<float*>(carve(4 * n));
+    B.p = reinterpret_cast<float*>(carve(4 * n));
+    B.zz = reinterpret_cast<float*>(carve(4 * n));
+    B.Ap = reinterpret_cast<float*>(carve(4 * n));
+    B.dof = reinterpret_cast<std::uint8_t*>(carve(n));
+    B.acc = reinterpret_cast<double*>(carve(sizeof(double) * 8));
+    double* acc_it = reinterpret_cast<double*>(carve(sizeof(double) * (2 + 3 * (kPcg + 1))));
+    // DOF mask via the linear set-up kernel (it only needs mask, channels, edges).
+    {
+        double* junk = B.F;
+        hs_setup<<<nb, 256, 0, st>>>(P.H, mask_dev, is_channel_dev, z_dev, z_dev, B.dof, B.invd, B.b, junk);
+    }
+    hsn_to_double<<<nb, 256, 0, st>>>(n, z_dev, B.z);
+    cudaMemcpyAsync(B.zn, B.z, 8 * n, cudaMemcpyDeviceToDevice, st);
+
+    const double total = static_cast<double>(dt_total);
+    double dt = total, remaining = total;
+    const double dt_min = total * 1e-9;
+    int n_sub = 0, rejects = 0, total_outer = 0, total_pcg = 0;
+    double last_rel = 0.0, last_finf = 0.0;
+    int status = LSDTT_GPU_OK;
+    const double feasible = std::sqrt(P.cap);
+    while (remaining > 0.0 && status == LSDTT_GPU_OK)
+    {
+        const double step = std::min(dt, remaining);
+        P.H.inv_dt = 1.0 / step;
+        // z starts from the previous accepted field (== zn).
+        cudaMemcpyAsync(B.z, B.zn, 8 * n, cudaMemcpyDeviceToDevice, st);
+        double ev[3];
+        e = hsn_evaluate(P, mask_dev, B, B.z, n, st, ev);
+        if (e != cudaSuccess) break;
+        double fnorm = ev[0];
+        bool converged = false;
+        int it = 0;
+        for (; it < kOuter; ++it)
+        {
+            if (fnorm <= ftol) { converged = true; break; }
+            int pit = 0;
+            double rel = 0.0;
+            e = hsn_pcg(P, mask_dev, B, n, rtol, kPcg, st, &pit, &rel, acc_it);
+            if (e != cudaSuccess) break;
+            total_pcg += pit;
+            last_rel = rel;
+            // Line search on the true residual (alpha/F buffers are reused:
+            // re-evaluate at z before leaving).
+            const double ratio_now = P.nonlinear ? ev[2] : 0.0;
+            const bool restoring = P.nonlinear && ratio_now > feasible;
+            double lambda = 1.0;
+            bool accepted = false;
+            double evt[3] = {0, 0, 0};
+            for (int ls = 0; ls < 30; ++ls)
+            {
+                hsn_axpy<<<nb, 256, 0, st>>>(n, B.dof, B.z, B.x, lambda, B.zt);
+                e = hsn_evaluate(P, mask_dev, B, B.zt, n, st, evt);
+                if (e != cudaSuccess) break;
+                if (P.nonlinear)
+                {
+                    if (restoring)
+                    {
+                        if (evt[2] >= ratio_now) { lambda *= 0.5; continue; }
+                        accepted = true;
+                        break;
+                    }
+                    if (evt[2] > feasible) { lambda *= 0.5; continue; }
+                }
+                if (evt[0] < fnorm) { accepted = true; break; }
+                lambda *= 0.5;
+            }
+            if (e != cudaSuccess) break;
+            if (!accepted)
+            {
+                // restore alpha/F at z for a clean state
+                e = hsn_evaluate(P, mask_dev, B, B.z, n, st, ev);
+                break;
+            }
+            std::swap(B.z, B.zt);
+            ev[0] = evt[0];
+            ev[1] = evt[1];
+            ev[2] = evt[2];
+            fnorm = ev[0];
+            if (fnorm <= ftol) { converged = true; ++it; break; }
+        }
+        if (e != cudaSuccess) break;
+        total_outer += it;
+        last_finf = fnorm;
+        if (!converged)
+        {
+            ++rejects;
+            if (rejects > 40 || step <= dt_min)
+            {
+                status = LSDTT_GPU_ENOCONV;
+                break;
+            }
+            dt = std::max(dt_min, step * 0.5);
+            continue;
+        }
+        cudaMemcpyAsync(B.zn, B.z, 8 * n, cudaMemcpyDeviceToDevice, st);
+        remaining -= step;
+        ++n_sub;
+        if (it <= 4) dt = std::min(total, step * 1.7);
+        else if (it >= 15) dt = std::max(dt_min, step * 0.5);
+    }
+    if (e == cudaSuccess)
+    {
+        hsn_to_float<<<nb, 256, 0, st>>>(n, B.zn, z_out_dev);
+        e = cudaStreamSynchronize(st);
+    }
+    cudaFreeAsync(base, st);
+    cudaFreeHost(B.hacc);
+    if (e != cudaSuccess) return cuda_fail(e, "lsdtt_gpu_hillslope_implicit");
+    if (report)
+    {
+        report->iterations = total_pcg;
+        report->converged = status == LSDTT_GPU_OK ? 1 : 0;
+        report->relative_residual = last_rel;
+        report->initial_residual_inf = last_finf;
+    }
+    if (status != LSDTT_GPU_OK)
+        return fail(status, "lsdtt_gpu_hillslope_implicit: Newton failed at the minimum sub-step");
+    (void)n_sub;
+    (void)total_outer;
+    return LSDTT_GPU_OK;
+}

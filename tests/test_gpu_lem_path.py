@@ -156,3 +156,30 @@ def test_route_host_matches_device_path(port):
     assert np.array_equal(rec, want["receiver"])
     assert np.array_equal(topo, want["topo"])
     assert np.array_equal(cnt, want["sv_size"])
+
+
+@pytest.mark.parametrize("relief,bc", [(5.0, "oooo"), (20.0, "oooo"), (8.0, "popo"), (8.0, "nnon")])
+def test_hillslope_roering_vs_fp64_newton(relief, bc):
+    """Nonlinear (Roering, Sc = 1) backward-Euler step against the FP64
+    restatement of the reference's Newton + SparseLU."""
+    import lsdtt_gb300 as G
+    z = surfaces.fractal(64, 64, relief, 3)
+    m = np.ones_like(z, np.uint8)
+    want, n_sub, _ = H.transient(z, m, 5.0, bc, 0.01, 1.0, 2.5e4)
+    got, rep = G.hillslope_implicit(z, m, 5.0, bc, 0.01, 1.0, 2.5e4, nonlinear=True)
+    got = got.cpu().numpy()
+    rel = np.max(np.abs(got - want) / np.maximum(np.abs(want), 1.0))
+    print(f"roering relief {relief} {bc}: substeps {n_sub}, PCG iterations {rep.iterations}, max rel {rel:.3g}")
+    assert rep.converged
+    assert rel < REL_TOL
+
+
+def test_hillslope_linear_general_entry_matches_linear_entry(port):
+    import lsdtt_gb300 as G
+    z, m = _cfg1(port, 128)
+    a, _ = G.hillslope_linear_implicit(z, m, 30.0, "nnon", 0.01, 1000.0)
+    b, rep = G.hillslope_implicit(z, m, 30.0, "nnon", 0.01, 1.0, 1000.0, nonlinear=False)
+    want, _, _ = H.linear_step(z, m, 30.0, "nnon", 0.01, 1000.0)
+    rel = np.max(np.abs(b.cpu().numpy() - want) / np.maximum(np.abs(want), 1.0))
+    assert rel < REL_TOL
+    assert np.max(np.abs(a.cpu().numpy() - b.cpu().numpy())) < 1e-4
