@@ -167,6 +167,17 @@ typedef struct lsdtt_gpu_solve_report
     int32_t converged;
     double relative_residual;
     double initial_residual_inf; /* ||F||_inf before the step (m/yr) */
+    /* Filled by every hillslope solve; the learned fields stay 0 without a
+     * network. explicit_relative_residual is the largest, over the linear
+     * solves, of ||b - A x||_2 / ||b||_2 recomputed in FP64 from the final
+     * FP32 iterate (the recurrence residual above is what the 1e-8 test
+     * reads); -1 from lsdtt_gpu_hillslope_linear_implicit, which does not
+     * compute it. */
+    int32_t linear_solves;
+    int32_t network_applications;
+    int32_t rejected_solves;      /* learned solves the Jacobi judge rejected */
+    int32_t fallback_iterations;  /* Jacobi-PCG iterations run after a rejection */
+    double explicit_relative_residual;
 } lsdtt_gpu_solve_report;
 
 int lsdtt_gpu_hillslope_linear_implicit(const lsdtt_gpu_grid* grid, const float* z_dev, const uint8_t* mask_dev,
@@ -185,6 +196,70 @@ int lsdtt_gpu_hillslope_implicit(const lsdtt_gpu_grid* grid, const float* z_dev,
                                  const uint8_t* is_channel_dev, float D, float Sc, int32_t nonlinear, float dt_total,
                                  double rel_tol, int32_t max_pcg_iter, double residual_tol, int32_t max_outer,
                                  float* z_out_dev, lsdtt_gpu_solve_report* report, void* stream);
+
+/* ---- learned preconditioner -----------------------------------------------
+ * No reference counterpart: the reference solves its implicit hillslope steps
+ * with Eigen (src/cpu/lsdtt_hillslope_newton_cpu.cpp:196-675). A 4-level
+ * U-Net with additive skips maps a residual r to a correction e ~ A^-1 r:
+ *   x0 = bf16(r/rms r); e0 = relu(conv 1->16); e1 = relu(conv(pool e0) 16->32)
+ *   e2 = relu(conv(pool e1) 32->64); e3 = relu(conv(pool e2) 64->64)
+ *   d2 = relu(conv(up e3) 64->64) + e2; d1 = relu(conv(up d2) 64->32) + e1
+ *   d0 = relu(conv(up d1) 32->16) + e0; y = rms(r) * conv(d0) 16->1
+ * 3x3 convolutions with zero padding, 2x2 mean pooling, nearest upsampling,
+ * BF16 weights and activations, FP32 accumulation. The parameter vector
+ * (FP32 master copy) holds the weights of the eight convolutions in that
+ * order, each [Cout][3][3][Cin], then their biases. Images are n_rows x
+ * n_cols with both sides multiples of 8, within the capacity given at
+ * creation. */
+typedef struct lsdtt_gpu_unet lsdtt_gpu_unet;
+
+int lsdtt_gpu_unet_create(int32_t max_rows, int32_t max_cols, uint64_t seed, lsdtt_gpu_unet** out);
+int lsdtt_gpu_unet_destroy(lsdtt_gpu_unet* net);
+int64_t lsdtt_gpu_unet_num_params(const lsdtt_gpu_unet* net);
+int lsdtt_gpu_unet_get_params(const lsdtt_gpu_unet* net, float* params_host, int64_t count);
+int lsdtt_gpu_unet_set_params(lsdtt_gpu_unet* net, const float* params_host, int64_t count);
+/* y = net(r), device FP32 images */
+int lsdtt_gpu_unet_apply(lsdtt_gpu_unet* net, const float* r_dev, int32_t n_rows, int32_t n_cols, float* y_dev,
+                         void* stream);
+/* loss = sum (net(r) - e)^2 / sum e^2 and its gradient (grad_host may be
+ * NULL) without changing the weights. */
+int lsdtt_gpu_unet_loss_grad(lsdtt_gpu_unet* net, const float* r_dev, const float* e_dev, int32_t n_rows,
+                             int32_t n_cols, double* loss, float* grad_host, void* stream);
+/* One optimiser step on the pair (r, e); *loss is the loss before it.
+ * optimizer: 0 = SGD with momentum 0.9, 1 = Adam (0.9, 0.999, 1e-8). */
+int lsdtt_gpu_unet_train_step(lsdtt_gpu_unet* net, const float* r_dev, const float* e_dev, int32_t n_rows,
+                              int32_t n_cols, int32_t optimizer, float lr, double* loss, void* stream);
+
+/* Residual/correction pairs from the plain solver: the first linear system
+ * of lsdtt_gpu_hillslope_implicit's step of length dt (the lagged-coefficient
+ * operator at z for nonlinear = 1) is solved by Jacobi-PCG, and at n_pairs
+ * iterations k spread evenly over the solve the residual r_k and the
+ * remaining correction x_final - x_k are written: r_out_dev[j*N + i] =
+ * r_k[i] / A_ii (the Jacobi-scaled residual, metres, the network's input),
+ * e_out_dev[j*N + i] = x_final[i] - x_k[i]. *n_written is the number of
+ * pairs written (fewer when the solve is shorter). */
+int lsdtt_gpu_hillslope_capture_pairs(const lsdtt_gpu_grid* grid, const float* z_dev, const uint8_t* mask_dev,
+                                      const uint8_t* is_channel_dev, float D, float Sc, int32_t nonlinear, float dt,
+                                      double rel_tol, int32_t max_iter, int32_t n_pairs, float* r_out_dev,
+                                      float* e_out_dev, int32_t* n_written, void* stream);
+
+/* lsdtt_gpu_hillslope_implicit with the network as the preconditioner: each
+ * linear system is solved by flexible (Polak-Ribiere) PCG with
+ *   M^-1 r = y + D^-1 (r - A y),  y = net(D^-1 r)  (D = diag A),
+ * to the same relative residual rel_tol. Plain Jacobi-PCG is the judge and
+ * the fallback: the FP64 explicit residual of the learned iterate must be
+ * within max(rel_tol, 4x the FP32 representation floor of the iterate) of
+ * ||b||, else Jacobi-PCG restarts from that iterate (or from zero when it is
+ * not finite) and finishes the solve. A learned solve whose residual does
+ * not halve within 16 iterations is handed to Jacobi-PCG the same way, and
+ * after two rejections in one call the network is not used again in that
+ * call. The grid sides must be multiples of 8 within the network's
+ * capacity. */
+int lsdtt_gpu_hillslope_implicit_learned(const lsdtt_gpu_grid* grid, const float* z_dev, const uint8_t* mask_dev,
+                                         const uint8_t* is_channel_dev, float D, float Sc, int32_t nonlinear,
+                                         float dt_total, double rel_tol, int32_t max_pcg_iter, double residual_tol,
+                                         int32_t max_outer, lsdtt_gpu_unet* net, float* z_out_dev,
+                                         lsdtt_gpu_solve_report* report, void* stream);
 
 /* ---- LEM timestep ----------------------------------------------------------
  * run_lem_step (src/cpu/lsdtt_lem_cpu.cpp:285-732) for the D8 coupled

@@ -269,7 +269,12 @@ class _DeviceArray:
 
 class SolveReport(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_int32), ("converged", ctypes.c_int32), ("relative_residual", ctypes.c_double),
-                ("initial_residual_inf", ctypes.c_double)]
+                ("initial_residual_inf", ctypes.c_double), ("linear_solves", ctypes.c_int32),
+                ("network_applications", ctypes.c_int32), ("rejected_solves", ctypes.c_int32),
+                ("fallback_iterations", ctypes.c_int32), ("explicit_relative_residual", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class LemOptions(ctypes.Structure):
@@ -386,16 +391,23 @@ class LandscapeModel:
 
 
 def hillslope_implicit(z, mask, cell_size, boundary_conditions, D, Sc, dt, nonlinear=True, rel_tol=1e-8,
-                       max_pcg_iter=4000, residual_tol=1e-12, max_outer=200, is_channel=None, stream=None):
+                       max_pcg_iter=4000, residual_tol=1e-12, max_outer=200, is_channel=None, net=None, stream=None):
     """Backward-Euler hillslope step over dt (linear or Roering), the
-    reference's compute_hillslope_newton_transient. Returns (z CUDA tensor,
-    SolveReport with the total PCG iteration count)."""
+    reference's compute_hillslope_newton_transient. With `net` (a UNet) the
+    linear systems are solved by flexible PCG with the network as the
+    preconditioner, judged and finished by Jacobi-PCG. Returns (z CUDA
+    tensor, SolveReport with the total PCG iteration count)."""
     torch = _torch()
     L = _bind_more()
-    fn = L.lsdtt_gpu_hillslope_implicit
     vp = ctypes.c_void_p
-    fn.argtypes = [ctypes.POINTER(Grid), vp, vp, vp, ctypes.c_float, ctypes.c_float, ctypes.c_int32, ctypes.c_float,
-                   ctypes.c_double, ctypes.c_int32, ctypes.c_double, ctypes.c_int32, vp, ctypes.POINTER(SolveReport), vp]
+    args = [ctypes.POINTER(Grid), vp, vp, vp, ctypes.c_float, ctypes.c_float, ctypes.c_int32, ctypes.c_float,
+            ctypes.c_double, ctypes.c_int32, ctypes.c_double, ctypes.c_int32]
+    if net is None:
+        fn = L.lsdtt_gpu_hillslope_implicit
+        fn.argtypes = args + [vp, ctypes.POINTER(SolveReport), vp]
+    else:
+        fn = L.lsdtt_gpu_hillslope_implicit_learned
+        fn.argtypes = args + [vp, vp, ctypes.POINTER(SolveReport), vp]
     fn.restype = ctypes.c_int
     zt = _dev(z, torch.float32)
     mt = _dev(mask, torch.uint8)
@@ -403,8 +415,140 @@ def hillslope_implicit(z, mask, cell_size, boundary_conditions, D, Sc, dt, nonli
     g = make_grid(zt.shape[0], zt.shape[1], cell_size, boundary_conditions)
     out = torch.empty_like(zt)
     rep = SolveReport()
+    head = [ctypes.byref(g), vp(zt.data_ptr()), vp(mt.data_ptr()), vp(ct.data_ptr() if ct is not None else 0),
+            ctypes.c_float(D), ctypes.c_float(Sc), ctypes.c_int32(int(nonlinear)), ctypes.c_float(dt),
+            ctypes.c_double(rel_tol), ctypes.c_int32(max_pcg_iter), ctypes.c_double(residual_tol),
+            ctypes.c_int32(max_outer)]
+    tail = [vp(out.data_ptr()), ctypes.byref(rep), _stream(stream)]
+    _check(fn(*head, *tail) if net is None else fn(*head, net._h, *tail))
+    return out, rep
+
+
+# U-Net layer table: (name, Cin, Cout), the order of the parameter vector
+# (weights [Cout][3][3][Cin] of every layer, then every bias).
+UNET_LAYERS = [("enc0", 1, 16), ("enc1", 16, 32), ("enc2", 32, 64), ("enc3", 64, 64), ("dec2", 64, 64),
+               ("dec1", 64, 32), ("dec0", 32, 16), ("out", 16, 1)]
+
+
+def unet_flatten(params: dict) -> np.ndarray:
+    """{name.w, name.b} -> the library's flat FP32 parameter vector."""
+    parts = [np.asarray(params[n + ".w"], np.float32).reshape(-1) for n, _, _ in UNET_LAYERS]
+    parts += [np.asarray(params[n + ".b"], np.float32).reshape(-1) for n, _, _ in UNET_LAYERS]
+    return np.concatenate(parts)
+
+
+def unet_unflatten(vec) -> dict:
+    vec = np.asarray(vec, np.float32)
+    out, o = {}, 0
+    for n, ci, co in UNET_LAYERS:
+        k = co * 9 * ci
+        out[n + ".w"] = vec[o:o + k].reshape(co, 3, 3, ci)
+        o += k
+    for n, ci, co in UNET_LAYERS:
+        out[n + ".b"] = vec[o:o + co].copy()
+        o += co
+    return out
+
+
+class UNet:
+    """The learned hillslope preconditioner (lsdtt_gpu_unet_*): forward,
+    gradient and optimiser steps all run in liblsdtt_gb300.so."""
+
+    def __init__(self, max_rows: int, max_cols: int, seed: int = 1):
+        L = lib()
+        vp, i32, i64 = ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64
+        for name, args, res in [
+            ("lsdtt_gpu_unet_create", [i32, i32, ctypes.c_uint64, ctypes.POINTER(vp)], ctypes.c_int),
+            ("lsdtt_gpu_unet_destroy", [vp], ctypes.c_int),
+            ("lsdtt_gpu_unet_num_params", [vp], i64),
+            ("lsdtt_gpu_unet_get_params", [vp, vp, i64], ctypes.c_int),
+            ("lsdtt_gpu_unet_set_params", [vp, vp, i64], ctypes.c_int),
+            ("lsdtt_gpu_unet_apply", [vp, vp, i32, i32, vp, vp], ctypes.c_int),
+            ("lsdtt_gpu_unet_loss_grad", [vp, vp, vp, i32, i32, ctypes.POINTER(ctypes.c_double), vp, vp],
+             ctypes.c_int),
+            ("lsdtt_gpu_unet_train_step", [vp, vp, vp, i32, i32, i32, ctypes.c_float,
+                                           ctypes.POINTER(ctypes.c_double), vp], ctypes.c_int),
+        ]:
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = res
+        h = vp()
+        _check(L.lsdtt_gpu_unet_create(max_rows, max_cols, seed, ctypes.byref(h)))
+        self._h = h
+        self.n_params = int(L.lsdtt_gpu_unet_num_params(h))
+
+    def get_params(self) -> np.ndarray:
+        out = np.empty(self.n_params, np.float32)
+        _check(lib().lsdtt_gpu_unet_get_params(self._h, out.ctypes.data, self.n_params))
+        return out
+
+    def set_params(self, vec) -> None:
+        vec = np.ascontiguousarray(vec, np.float32)
+        if vec.size != self.n_params:
+            raise ValueError(f"expected {self.n_params} parameters, got {vec.size}")
+        _check(lib().lsdtt_gpu_unet_set_params(self._h, vec.ctypes.data, self.n_params))
+
+    def apply(self, r, stream=None):
+        torch = _torch()
+        rt = _dev(r, torch.float32)
+        y = torch.empty_like(rt)
+        _check(lib().lsdtt_gpu_unet_apply(self._h, ctypes.c_void_p(rt.data_ptr()), rt.shape[0], rt.shape[1],
+                                          ctypes.c_void_p(y.data_ptr()), _stream(stream)))
+        return y
+
+    def loss_grad(self, r, e, stream=None):
+        torch = _torch()
+        rt, et = _dev(r, torch.float32), _dev(e, torch.float32)
+        loss = ctypes.c_double()
+        g = np.empty(self.n_params, np.float32)
+        _check(lib().lsdtt_gpu_unet_loss_grad(self._h, ctypes.c_void_p(rt.data_ptr()), ctypes.c_void_p(et.data_ptr()),
+                                              rt.shape[0], rt.shape[1], ctypes.byref(loss), g.ctypes.data,
+                                              _stream(stream)))
+        return loss.value, g
+
+    def train_step(self, r, e, lr=1e-3, optimizer="adam", stream=None) -> float:
+        torch = _torch()
+        rt, et = _dev(r, torch.float32), _dev(e, torch.float32)
+        loss = ctypes.c_double()
+        _check(lib().lsdtt_gpu_unet_train_step(self._h, ctypes.c_void_p(rt.data_ptr()),
+                                               ctypes.c_void_p(et.data_ptr()), rt.shape[0], rt.shape[1],
+                                               {"sgd": 0, "adam": 1}[optimizer], ctypes.c_float(lr),
+                                               ctypes.byref(loss), _stream(stream)))
+        return loss.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().lsdtt_gpu_unet_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def capture_pairs(z, mask, cell_size, boundary_conditions, D, Sc, dt, n_pairs, nonlinear=True, rel_tol=1e-8,
+                  max_iter=4000, is_channel=None, stream=None):
+    """Residual/correction pairs from the plain Jacobi-PCG solve
+    (lsdtt_gpu_hillslope_capture_pairs). Returns (r, e) CUDA tensors of shape
+    [k, n_rows, n_cols], r scaled to metres (dt * residual)."""
+    torch = _torch()
+    L = lib()
+    vp = ctypes.c_void_p
+    fn = L.lsdtt_gpu_hillslope_capture_pairs
+    fn.argtypes = [ctypes.POINTER(Grid), vp, vp, vp, ctypes.c_float, ctypes.c_float, ctypes.c_int32, ctypes.c_float,
+                   ctypes.c_double, ctypes.c_int32, ctypes.c_int32, vp, vp, ctypes.POINTER(ctypes.c_int32), vp]
+    fn.restype = ctypes.c_int
+    zt = _dev(z, torch.float32)
+    mt = _dev(mask, torch.uint8)
+    ct = None if is_channel is None else _dev(is_channel, torch.uint8)
+    g = make_grid(zt.shape[0], zt.shape[1], cell_size, boundary_conditions)
+    r = torch.empty((n_pairs,) + tuple(zt.shape), dtype=torch.float32, device=zt.device)
+    e = torch.empty_like(r)
+    k = ctypes.c_int32()
     _check(fn(ctypes.byref(g), vp(zt.data_ptr()), vp(mt.data_ptr()), vp(ct.data_ptr() if ct is not None else 0),
               ctypes.c_float(D), ctypes.c_float(Sc), ctypes.c_int32(int(nonlinear)), ctypes.c_float(dt),
-              ctypes.c_double(rel_tol), ctypes.c_int32(max_pcg_iter), ctypes.c_double(residual_tol),
-              ctypes.c_int32(max_outer), vp(out.data_ptr()), ctypes.byref(rep), _stream(stream)))
-    return out, rep
+              ctypes.c_double(rel_tol), ctypes.c_int32(max_iter), ctypes.c_int32(n_pairs), vp(r.data_ptr()),
+              vp(e.data_ptr()), ctypes.byref(k), _stream(stream)))
+    return r[:k.value], e[:k.value]

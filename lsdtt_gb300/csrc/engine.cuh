@@ -65,4 +65,11 @@ cudaError_t launch_donors_outlets(lsdtt_gpu_flow* f, cudaStream_t st);
 cudaError_t build_stack(lsdtt_gpu_flow* f, bool want_topo, cudaStream_t st);
 cudaError_t accumulate(lsdtt_gpu_flow* f, const double* w, double* out, cudaStream_t st, bool* exact_path);
 
+// unet.cu: the learned preconditioner's forward pass for the hillslope
+// solver. unet_forward_dev enqueues y = net(r) on st; *y_dev points at the
+// handle's output image, valid until the next call on the handle.
+int unet_check_shape(const lsdtt_gpu_unet* U, int H, int W);
+cudaError_t unet_forward_dev(lsdtt_gpu_unet* U, const float* r_dev, int H, int W, cudaStream_t st,
+                             const float** y_dev);
+
 }  // namespace lsdtt_gb300

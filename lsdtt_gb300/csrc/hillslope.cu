@@ -17,6 +17,8 @@
 // float, as the reference rounds its double working field.
 
 #include <cmath>
+#include <string>
+#include <vector>
 
 #include "engine.cuh"
 
@@ -324,10 +326,13 @@ extern "C" int lsdtt_gpu_hillslope_linear_implicit(const lsdtt_gpu_grid* grid, c
     if (e != cudaSuccess) return cuda_fail(e, "lsdtt_gpu_hillslope_linear_implicit");
     if (report)
     {
+        *report = lsdtt_gpu_solve_report{};
         report->iterations = it;
         report->relative_residual = rel;
         report->initial_residual_inf = finf0;
         report->converged = converged ? 1 : 0;
+        report->linear_solves = 1;
+        report->explicit_relative_residual = -1.0;  // not computed on this path
     }
     if (!converged)
         return fail(LSDTT_GPU_ENOCONV, "lsdtt_gpu_hillslope_linear_implicit: Jacobi-PCG did not reach the relative "
@@ -557,14 +562,189 @@ __global__ void hsn_to_float(std::int64_t n, const double* __restrict__ a, float
     if (i < n) b[i] = static_cast<float>(a[i]);
 }
 
+// ---- flexible PCG with the learned preconditioner --------------------------
+// Per-iteration reduction slot (4 doubles): [0] p.Ap, [1] r.z, [2] r.r,
+// [3] r_old.z. beta = (r.z - r_old.z) / r_old.z_old (Polak-Ribiere), which
+// keeps conjugacy when M^-1 changes from one iteration to the next.
+
+// alpha = rz_prev / pAp; r_old = r; x += alpha p; r -= alpha Ap; acc_out[2] = r.r
+__global__ void hsf_update(std::int64_t n, const double* __restrict__ rz_prev, const double* __restrict__ acc_it,
+                           const float* __restrict__ p, const float* __restrict__ Ap, float* __restrict__ x,
+                           float* __restrict__ r, float* __restrict__ ro, double* __restrict__ acc_out)
+{
+    LSDTT_COUNT();
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const double pap = acc_it[0];
+    const float alpha = (pap > 0.0) ? static_cast<float>(*rz_prev / pap) : 0.0f;
+    double rr = 0.0;
+    if (i < n)
+    {
+        x[i] += alpha * p[i];
+        const float r0 = r[i];
+        ro[i] = r0;
+        const float ri = r0 - alpha * Ap[i];
+        r[i] = ri;
+        rr = static_cast<double>(ri) * ri;
+    }
+    for (int o = 16; o > 0; o >>= 1) rr += __shfl_down_sync(0xffffffffu, rr, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(&acc_out[2], rr);
+}
+
+// The network's input: the Jacobi-scaled residual D^-1 r (metres), which
+// carries the local stiffness of the lagged-coefficient operator.
+__global__ void hsf_input(std::int64_t n, const float* __restrict__ invd, const float* __restrict__ r,
+                          float* __restrict__ q)
+{
+    LSDTT_COUNT();
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < n) q[i] = invd[i] * r[i];
+}
+
+// y = net output on DOFs, 0 elsewhere
+__global__ void hsf_mask(std::int64_t n, const std::uint8_t* __restrict__ dof, const float* __restrict__ ynet,
+                         float* __restrict__ y)
+{
+    LSDTT_COUNT();
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = dof[i] ? ynet[i] : 0.0f;
+}
+
+// z = y + D^-1 (r - A y) (t = A y); acc_out[1] = r.z, acc_out[3] = r_old.z
+__global__ void hsf_smooth(std::int64_t n, const float* __restrict__ invd, const float* __restrict__ r,
+                           const float* __restrict__ ro, const float* __restrict__ t, float* __restrict__ z,
+                           double* __restrict__ acc_out)
+{
+    LSDTT_COUNT();
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    double rz = 0.0, roz = 0.0;
+    if (i < n)
+    {
+        const float ri = r[i];
+        const float zi = z[i] + invd[i] * (ri - t[i]);
+        z[i] = zi;
+        rz = static_cast<double>(ri) * zi;
+        roz = static_cast<double>(ro[i]) * zi;
+    }
+    for (int o = 16; o > 0; o >>= 1)
+    {
+        rz += __shfl_down_sync(0xffffffffu, rz, o);
+        roz += __shfl_down_sync(0xffffffffu, roz, o);
+    }
+    if ((threadIdx.x & 31) == 0)
+    {
+        atomicAdd(&acc_out[1], rz);
+        atomicAdd(&acc_out[3], roz);
+    }
+}
+
+// beta = (r.z - r_old.z) / rz_old; p = z + beta p (beta = 0 at a restart)
+__global__ void hsf_direction(std::int64_t n, const double* __restrict__ rz_old, const double* __restrict__ acc_new,
+                             const float* __restrict__ z, float* __restrict__ p)
+{
+    LSDTT_COUNT();
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double ro = *rz_old;
+    const float beta = (ro > 0.0) ? static_cast<float>((acc_new[1] - acc_new[3]) / ro) : 0.0f;
+    p[i] = z[i] + beta * p[i];
+}
+
+// Explicit residual res = b - A x, evaluated in FP64 from the FP32 iterate and
+// stored (FP32) in r. acc[0] += ||res||^2; acc[1] += sum_i (diag_i |x_i|
+// 2^-24)^2, the residual that rounding x to FP32 alone can leave (the
+// representation floor the judge allows for).
+__global__ void hsn_explicit(HsN P, const std::uint8_t* __restrict__ mask, const std::uint8_t* __restrict__ dof,
+                             const float4* __restrict__ alpha, const float* __restrict__ b,
+                             const float* __restrict__ x, float* __restrict__ r, double* __restrict__ acc)
+{
+    LSDTT_COUNT();
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const std::int64_t n = static_cast<std::int64_t>(P.H.nr) * P.H.nc;
+    double rr = 0.0, fl = 0.0;
+    if (i < n)
+    {
+        double res = 0.0;
+        if (dof[i])
+        {
+            const int rw = static_cast<int>(i / P.H.nc), cl = static_cast<int>(i % P.H.nc);
+            const float4 a = alpha[i];
+            const float av[4] = {a.x, a.y, a.z, a.w};
+            const double xi = x[i];
+            double diag = P.H.inv_dt, off = 0.0;
+#pragma unroll
+            for (int f = 0; f < 4; ++f)
+            {
+                const std::int64_t j = hs_nb(P.H, mask, rw, cl, kDr[f], kDc[f]);
+                if (j == i) continue;
+                diag += P.H.DA * av[f];
+                if (dof[j]) off += P.H.DA * av[f] * static_cast<double>(x[j]);
+            }
+            res = static_cast<double>(b[i]) - (diag * xi - off);
+            const double u = diag * fabs(xi) * 5.9604644775390625e-8;
+            fl = u * u;
+        }
+        r[i] = static_cast<float>(res);
+        rr = res * res;
+    }
+    for (int o = 16; o > 0; o >>= 1)
+    {
+        rr += __shfl_down_sync(0xffffffffu, rr, o);
+        fl += __shfl_down_sync(0xffffffffu, fl, o);
+    }
+    if ((threadIdx.x & 31) == 0)
+    {
+        atomicAdd(&acc[0], rr);
+        atomicAdd(&acc[1], fl);
+    }
+}
+
+// Jacobi-PCG restart from the residual in r: z = p = D^-1 r, acc[0] = r.z
+__global__ void hsn_restart(std::int64_t n, const float* __restrict__ invd, const float* __restrict__ r,
+                            float* __restrict__ p, double* __restrict__ acc)
+{
+    LSDTT_COUNT();
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    double rz = 0.0;
+    if (i < n)
+    {
+        const float zi = r[i] * invd[i];
+        p[i] = zi;
+        rz = static_cast<double>(r[i]) * zi;
+    }
+    for (int o = 16; o > 0; o >>= 1) rz += __shfl_down_sync(0xffffffffu, rz, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(&acc[0], rz);
+}
+
+__global__ void hsn_pair_finish(std::int64_t n, const float* __restrict__ x_final, const float* __restrict__ invd,
+                                float* __restrict__ r_slot, float* __restrict__ e_slot)
+{
+    LSDTT_COUNT();
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    r_slot[i] = invd[i] * r_slot[i];
+    e_slot[i] = x_final[i] - e_slot[i];
+}
+
 struct HsnBuf
 {
     std::uint8_t* dof;
     double *z, *zn, *zt, *F, *acc;
     float4* alpha;
-    float *invd, *b, *x, *r, *p, *zz, *Ap;
+    float *invd, *b, *x, *r, *p, *zz, *Ap, *ro;
     double* hacc;
 };
+
+// Statistics of the linear solves of one hillslope call.
+struct SolveStats
+{
+    int solves = 0, net_apps = 0, rejected = 0, fallback_its = 0;
+    double explicit_max = 0.0;
+};
+
+// Reductions of one linear solve: a header of 16 doubles, then kSlot
+// doubles per iteration.
+constexpr int kSlot = 4;
+inline std::size_t solve_acc_doubles(int max_iter) { return 16 + static_cast<std::size_t>(kSlot) * (max_iter + 2); }
 
 // One evaluation of alpha, F and the norms at z (device), read back.
 cudaError_t hsn_evaluate(const HsN& P, const std::uint8_t* mask, HsnBuf& B, const double* z, std::int64_t n,
@@ -580,61 +760,197 @@ cudaError_t hsn_evaluate(const HsN& P, const std::uint8_t* mask, HsnBuf& B, cons
     return e;
 }
 
-// PCG on A(alpha) dz = -F; returns iterations, sets *rel.
-cudaError_t hsn_pcg(const HsN& P, const std::uint8_t* mask, HsnBuf& B, std::int64_t n, double rel_tol, int max_iter,
-                    cudaStream_t st, int* iters, double* rel, double* acc_it_base)
+// Jacobi-PCG iterations from the state (x, r, p) with r.z in *rz0 until
+// ||r||_2 <= rel_tol * bnorm or max_iter. With snap_at (ascending), x and r
+// after iteration snap_at[j] are copied to x_snap + j*n and r_snap + j*n.
+cudaError_t jacobi_loop(const HsN& P, const std::uint8_t* mask, HsnBuf& B, std::int64_t n, double bnorm,
+                        double rel_tol, int max_iter, cudaStream_t st, double* slots, const double* rz0, int* iters,
+                        double* rel, const std::vector<int>* snap_at = nullptr, float* x_snap = nullptr,
+                        float* r_snap = nullptr, bool check = true)
 {
     const unsigned nb = grid_blocks(n, 256);
-    cudaMemsetAsync(acc_it_base, 0, sizeof(double) * (2 + 3 * (max_iter + 1)), st);
-    hsn_pcg_init<<<nb, 256, 0, st>>>(P, mask, B.dof, B.alpha, B.F, B.invd, B.b, B.x, B.r, B.p, acc_it_base);
-    cudaMemcpyAsync(B.hacc, acc_it_base, sizeof(double) * 2, cudaMemcpyDeviceToHost, st);
-    cudaError_t e = cudaStreamSynchronize(st);
-    if (e != cudaSuccess) return e;
-    const double bnorm = std::sqrt(B.hacc[1]);
     int it = 0;
-    *rel = 0.0;
-    if (bnorm == 0.0) { *iters = 0; return cudaSuccess; }
+    std::size_t next_snap = 0;
     const int kCheck = 4;
     bool done = false;
+    cudaError_t e = cudaSuccess;
     while (!done && it < max_iter)
     {
         const int batch = std::min(kCheck, max_iter - it);
         for (int k = 0; k < batch; ++k, ++it)
         {
-            double* cur = acc_it_base + 2 + 3 * it;
-            const double* rz_prev = (it == 0) ? acc_it_base : acc_it_base + 2 + 3 * (it - 1) + 1;
+            double* cur = slots + kSlot * it;
+            const double* rz_prev = (it == 0) ? rz0 : slots + kSlot * (it - 1) + 1;
             LSDTT_TIMED("hillslope_apply", 8.0 * static_cast<double>(n), st,
                         (hsn_apply<<<nb, 256, 0, st>>>(P, mask, B.dof, B.alpha, B.p, B.Ap, cur)));
             hs_update<<<nb, 256, 0, st>>>(n, rz_prev, cur, B.invd, B.p, B.Ap, B.x, B.r, B.zz, cur);
             hs_direction<<<nb, 256, 0, st>>>(n, rz_prev, cur + 1, B.zz, B.p);
+            while (snap_at && next_snap < snap_at->size() && (*snap_at)[next_snap] == it)
+            {
+                cudaMemcpyAsync(x_snap + next_snap * n, B.x, sizeof(float) * n, cudaMemcpyDeviceToDevice, st);
+                cudaMemcpyAsync(r_snap + next_snap * n, B.r, sizeof(float) * n, cudaMemcpyDeviceToDevice, st);
+                ++next_snap;
+            }
         }
-        cudaMemcpyAsync(B.hacc, acc_it_base + 2 + 3 * (it - 1), sizeof(double) * 3, cudaMemcpyDeviceToHost, st);
+        if (!check) continue;
+        cudaMemcpyAsync(B.hacc, slots + kSlot * (it - 1), sizeof(double) * 3, cudaMemcpyDeviceToHost, st);
         e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) return e;
         *rel = std::sqrt(B.hacc[2]) / bnorm;
         done = *rel <= rel_tol;
     }
     *iters = it;
-    return cudaSuccess;
+    return cudaGetLastError();
+}
+
+// ||b - A x||_2 and the FP32 representation floor, both relative to bnorm;
+// leaves the explicit residual in B.r.
+cudaError_t explicit_residual(const HsN& P, const std::uint8_t* mask, HsnBuf& B, std::int64_t n, double bnorm,
+                              double* acc2, cudaStream_t st, double* rel_exp, double* rel_floor)
+{
+    cudaMemsetAsync(acc2, 0, sizeof(double) * 2, st);
+    hsn_explicit<<<grid_blocks(n, 256), 256, 0, st>>>(P, mask, B.dof, B.alpha, B.b, B.x, B.r, acc2);
+    cudaMemcpyAsync(B.hacc, acc2, sizeof(double) * 2, cudaMemcpyDeviceToHost, st);
+    const cudaError_t e = cudaStreamSynchronize(st);
+    *rel_exp = std::sqrt(B.hacc[0]) / bnorm;
+    *rel_floor = std::sqrt(B.hacc[1]) / bnorm;
+    return e;
+}
+
+// The judge's tolerance on the explicit residual: the requested relative
+// residual, or 4x the floor that rounding the iterate to FP32 leaves,
+// whichever is larger.
+constexpr double kJudgeFloor = 4.0;
+
+// Solve A(alpha) dz = -F to rel_tol: Jacobi-PCG, or flexible PCG with the
+// network when net is given (then judged, and finished by Jacobi-PCG when
+// rejected). Sets *iters (all PCG iterations) and *rel (final recurrence
+// residual).
+cudaError_t hsn_pcg(const HsN& P, const std::uint8_t* mask, HsnBuf& B, std::int64_t n, double rel_tol, int max_iter,
+                    cudaStream_t st, int* iters, double* rel, double* acc, lsdtt_gpu_unet* net, SolveStats& S)
+{
+    // After two rejected learned solves the rest of the call is plain Jacobi-PCG.
+    constexpr int kMaxRejected = 2;
+    if (S.rejected >= kMaxRejected) net = nullptr;
+    const unsigned nb = grid_blocks(n, 256);
+    cudaMemsetAsync(acc, 0, sizeof(double) * solve_acc_doubles(max_iter), st);
+    hsn_pcg_init<<<nb, 256, 0, st>>>(P, mask, B.dof, B.alpha, B.F, B.invd, B.b, B.x, B.r, B.p, acc);
+    cudaMemcpyAsync(B.hacc, acc, sizeof(double) * 2, cudaMemcpyDeviceToHost, st);
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return e;
+    const double bnorm = std::sqrt(B.hacc[1]);
+    *rel = 0.0;
+    *iters = 0;
+    ++S.solves;
+    if (bnorm == 0.0) return cudaSuccess;
+    double* slots = acc + 16;
+    double rel_exp = 0.0, rel_floor = 0.0;
+    if (!net)
+    {
+        e = jacobi_loop(P, mask, B, n, bnorm, rel_tol, max_iter, st, slots, acc, iters, rel);
+        if (e == cudaSuccess) e = explicit_residual(P, mask, B, n, bnorm, acc + 4, st, &rel_exp, &rel_floor);
+        if (e == cudaSuccess) S.explicit_max = std::max(S.explicit_max, rel_exp);
+        return e;
+    }
+    // Flexible PCG. Initial slot acc[8..11]; iteration slots from acc + 16.
+    const int H = P.H.nr, W = P.H.nc;
+    double* dummy = acc + 6;
+    auto precondition = [&](double* slot) -> cudaError_t {
+        const float* ynet = nullptr;
+        hsf_input<<<nb, 256, 0, st>>>(n, B.invd, B.r, B.zz);
+        cudaError_t pe = unet_forward_dev(net, B.zz, H, W, st, &ynet);
+        ++S.net_apps;
+        hsf_mask<<<nb, 256, 0, st>>>(n, B.dof, ynet, B.zz);
+        hsn_apply<<<nb, 256, 0, st>>>(P, mask, B.dof, B.alpha, B.zz, B.Ap, dummy);
+        hsf_smooth<<<nb, 256, 0, st>>>(n, B.invd, B.r, B.ro, B.Ap, B.zz, slot);
+        return pe;
+    };
+    cudaMemcpyAsync(B.ro, B.r, sizeof(float) * n, cudaMemcpyDeviceToDevice, st);
+    e = precondition(acc + 8);
+    cudaMemcpyAsync(B.p, B.zz, sizeof(float) * n, cudaMemcpyDeviceToDevice, st);
+    int it = 0;
+    bool converged = false, broke = false;
+    const int kCheck = 4;
+    const int kStall = 16;  // iterations over which the residual must at least halve
+    std::vector<double> hist;
+    while (e == cudaSuccess && !converged && !broke && it < max_iter)
+    {
+        const int batch = std::min(kCheck, max_iter - it);
+        for (int k = 0; k < batch && e == cudaSuccess; ++k, ++it)
+        {
+            double* cur = slots + kSlot * it;
+            const double* rz_prev = (it == 0) ? acc + 9 : slots + kSlot * (it - 1) + 1;
+            LSDTT_TIMED("hillslope_apply", 8.0 * static_cast<double>(n), st,
+                        (hsn_apply<<<nb, 256, 0, st>>>(P, mask, B.dof, B.alpha, B.p, B.Ap, cur)));
+            hsf_update<<<nb, 256, 0, st>>>(n, rz_prev, cur, B.p, B.Ap, B.x, B.r, B.ro, cur);
+            e = precondition(cur);
+            hsf_direction<<<nb, 256, 0, st>>>(n, rz_prev, cur, B.zz, B.p);
+        }
+        if (e != cudaSuccess) break;
+        cudaMemcpyAsync(B.hacc, slots + kSlot * (it - 1), sizeof(double) * 4, cudaMemcpyDeviceToHost, st);
+        e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) break;
+        *rel = std::sqrt(B.hacc[2]) / bnorm;
+        if (!std::isfinite(*rel) || !(B.hacc[0] > 0.0) || !(B.hacc[1] > 0.0)) broke = true;
+        converged = !broke && *rel <= rel_tol;
+        hist.push_back(*rel);
+        const std::size_t back = kStall / kCheck;
+        if (!converged && hist.size() > back && *rel > 0.5 * hist[hist.size() - 1 - back]) broke = true;
+    }
+    if (e != cudaSuccess) return e;
+    *iters = it;
+    // The judge: explicit FP64 residual of the learned iterate.
+    e = explicit_residual(P, mask, B, n, bnorm, acc + 4, st, &rel_exp, &rel_floor);
+    if (e != cudaSuccess) return e;
+    const bool finite = std::isfinite(rel_exp);
+    if (converged && finite && rel_exp <= std::max(rel_tol, kJudgeFloor * rel_floor))
+    {
+        S.explicit_max = std::max(S.explicit_max, rel_exp);
+        return cudaSuccess;
+    }
+    // Rejected: Jacobi-PCG finishes from the learned iterate (from zero if
+    // it is not finite), with the explicit residual as its start.
+    ++S.rejected;
+    if (!finite)
+    {
+        cudaMemsetAsync(B.x, 0, sizeof(float) * n, st);
+        cudaMemcpyAsync(B.r, B.b, sizeof(float) * n, cudaMemcpyDeviceToDevice, st);
+    }
+    cudaMemsetAsync(acc + 12, 0, sizeof(double), st);
+    cudaMemsetAsync(slots, 0, sizeof(double) * kSlot * (max_iter + 1), st);
+    hsn_restart<<<nb, 256, 0, st>>>(n, B.invd, B.r, B.p, acc + 12);
+    int fit = 0;
+    e = jacobi_loop(P, mask, B, n, bnorm, rel_tol, max_iter, st, slots, acc + 12, &fit, rel);
+    S.fallback_its += fit;
+    *iters += fit;
+    if (e == cudaSuccess) e = explicit_residual(P, mask, B, n, bnorm, acc + 4, st, &rel_exp, &rel_floor);
+    if (e == cudaSuccess) S.explicit_max = std::max(S.explicit_max, rel_exp);
+    return e;
 }
 
 }  // namespace
 }  // namespace lsdtt_gb300
 
-extern "C" int lsdtt_gpu_hillslope_implicit(const lsdtt_gpu_grid* grid, const float* z_dev, const std::uint8_t* mask_dev,
-                                            const std::uint8_t* is_channel_dev, float D, float Sc, int32_t nonlinear,
-                                            float dt_total, double rel_tol, int32_t max_pcg_iter, double residual_tol,
-                                            int32_t max_outer, float* z_out_dev, lsdtt_gpu_solve_report* report,
-                                            void* stream)
+namespace lsdtt_gb300
 {
-    using namespace lsdtt_gb300;
-    if (!grid || !z_dev || !mask_dev || !z_out_dev)
-        return fail(LSDTT_GPU_EINVAL, "lsdtt_gpu_hillslope_implicit: null argument");
+namespace
+{
+
+// Shared body of the plain and learned entry points (net may be null).
+int hillslope_implicit_impl(const std::string& who, const lsdtt_gpu_grid* grid, const float* z_dev,
+                            const std::uint8_t* mask_dev, const std::uint8_t* is_channel_dev, float D, float Sc,
+                            int32_t nonlinear, float dt_total, double rel_tol, int32_t max_pcg_iter,
+                            double residual_tol, int32_t max_outer, lsdtt_gpu_unet* net, float* z_out_dev,
+                            lsdtt_gpu_solve_report* report, void* stream)
+{
+    if (!grid || !z_dev || !mask_dev || !z_out_dev) return fail(LSDTT_GPU_EINVAL, who + ": null argument");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
-        return fail(LSDTT_GPU_ENODEV, "lsdtt_gpu_hillslope_implicit: no CUDA device");
+        return fail(LSDTT_GPU_ENODEV, who + ": no CUDA device");
     if (!(grid->n_rows > 0 && grid->n_cols > 0 && grid->cell_size > 0.0))
-        return fail(LSDTT_GPU_EINVAL, "lsdtt_gpu_hillslope_implicit: raster metadata is invalid");
+        return fail(LSDTT_GPU_EINVAL, who + ": raster metadata is invalid");
+    if (net)
+        if (int sc = unet_check_shape(net, grid->n_rows, grid->n_cols)) return sc;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const std::int64_t n = static_cast<std::int64_t>(grid->n_rows) * grid->n_cols;
     const unsigned nb = grid_blocks(n, 256);
@@ -658,19 +974,20 @@ extern "C" int lsdtt_gpu_hillslope_implicit(const lsdtt_gpu_grid* grid, const fl
         // dt_total <= 0: nothing to integrate (newton_cpu.cpp:700-706).
         cudaMemcpyAsync(z_out_dev, z_dev, sizeof(float) * n, cudaMemcpyDeviceToDevice, st);
         const cudaError_t e0 = cudaStreamSynchronize(st);
-        return e0 == cudaSuccess ? LSDTT_GPU_OK : cuda_fail(e0, "lsdtt_gpu_hillslope_implicit");
+        if (report) *report = lsdtt_gpu_solve_report{};
+        return e0 == cudaSuccess ? LSDTT_GPU_OK : cuda_fail(e0, who.c_str());
     }
-    // Buffers: doubles z, zn, zt, F; float4 alpha; 7 floats; dof; reductions.
+    // Buffers: doubles z, zn, zt, F; float4 alpha; 8 floats; dof; reductions.
     HsnBuf B{};
-    const std::size_t need = static_cast<std::size_t>(n) * (4 * 8 + 16 + 7 * 4 + 1) + 64 * 256 +
-                             sizeof(double) * (8 + 3 * (kPcg + 1));
+    const std::size_t need = static_cast<std::size_t>(n) * (4 * 8 + 16 + 8 * 4 + 1) + 64 * 256 +
+                             sizeof(double) * (8 + solve_acc_doubles(kPcg));
     char* base = nullptr;
     cudaError_t e = cudaMallocAsync(&base, need, st);
     if (e == cudaSuccess) e = cudaMallocHost(&B.hacc, sizeof(double) * 8);
     if (e != cudaSuccess)
     {
         if (base) cudaFreeAsync(base, st);
-        return cuda_fail(e, "lsdtt_gpu_hillslope_implicit");
+        return cuda_fail(e, who.c_str());
     }
     char* cur = base;
     auto carve = [&](std::size_t bytes) {
@@ -690,9 +1007,11 @@ extern "C" int lsdtt_gpu_hillslope_implicit(const lsdtt_gpu_grid* grid, const fl
     B.p = reinterpret_cast<float*>(carve(4 * n));
     B.zz = reinterpret_cast<float*>(carve(4 * n));
     B.Ap = reinterpret_cast<float*>(carve(4 * n));
+    B.ro = reinterpret_cast<float*>(carve(4 * n));
     B.dof = reinterpret_cast<std::uint8_t*>(carve(n));
     B.acc = reinterpret_cast<double*>(carve(sizeof(double) * 8));
-    double* acc_it = reinterpret_cast<double*>(carve(sizeof(double) * (2 + 3 * (kPcg + 1))));
+    double* acc_it = reinterpret_cast<double*>(carve(sizeof(double) * solve_acc_doubles(kPcg)));
+    SolveStats S;
     // DOF mask via the linear set-up kernel (it only needs mask, channels, edges).
     {
         double* junk = B.F;
@@ -725,7 +1044,7 @@ extern "C" int lsdtt_gpu_hillslope_implicit(const lsdtt_gpu_grid* grid, const fl
             if (fnorm <= ftol) { converged = true; break; }
             int pit = 0;
             double rel = 0.0;
-            e = hsn_pcg(P, mask_dev, B, n, rtol, kPcg, st, &pit, &rel, acc_it);
+            e = hsn_pcg(P, mask_dev, B, n, rtol, kPcg, st, &pit, &rel, acc_it, net, S);
             if (e != cudaSuccess) break;
             total_pcg += pit;
             last_rel = rel;
@@ -795,17 +1114,161 @@ extern "C" int lsdtt_gpu_hillslope_implicit(const lsdtt_gpu_grid* grid, const fl
     }
     cudaFreeAsync(base, st);
     cudaFreeHost(B.hacc);
-    if (e != cudaSuccess) return cuda_fail(e, "lsdtt_gpu_hillslope_implicit");
+    if (e != cudaSuccess) return cuda_fail(e, who.c_str());
     if (report)
     {
+        *report = lsdtt_gpu_solve_report{};
         report->iterations = total_pcg;
         report->converged = status == LSDTT_GPU_OK ? 1 : 0;
         report->relative_residual = last_rel;
         report->initial_residual_inf = last_finf;
+        report->linear_solves = S.solves;
+        report->network_applications = S.net_apps;
+        report->rejected_solves = S.rejected;
+        report->fallback_iterations = S.fallback_its;
+        report->explicit_relative_residual = S.explicit_max;
     }
-    if (status != LSDTT_GPU_OK)
-        return fail(status, "lsdtt_gpu_hillslope_implicit: Newton failed at the minimum sub-step");
+    if (status != LSDTT_GPU_OK) return fail(status, who + ": Newton failed at the minimum sub-step");
     (void)n_sub;
     (void)total_outer;
+    return LSDTT_GPU_OK;
+}
+
+}  // namespace
+}  // namespace lsdtt_gb300
+
+extern "C" int lsdtt_gpu_hillslope_implicit(const lsdtt_gpu_grid* grid, const float* z_dev, const std::uint8_t* mask_dev,
+                                            const std::uint8_t* is_channel_dev, float D, float Sc, int32_t nonlinear,
+                                            float dt_total, double rel_tol, int32_t max_pcg_iter, double residual_tol,
+                                            int32_t max_outer, float* z_out_dev, lsdtt_gpu_solve_report* report,
+                                            void* stream)
+{
+    return lsdtt_gb300::hillslope_implicit_impl("lsdtt_gpu_hillslope_implicit", grid, z_dev, mask_dev, is_channel_dev,
+                                                D, Sc, nonlinear, dt_total, rel_tol, max_pcg_iter, residual_tol,
+                                                max_outer, nullptr, z_out_dev, report, stream);
+}
+
+extern "C" int lsdtt_gpu_hillslope_implicit_learned(const lsdtt_gpu_grid* grid, const float* z_dev,
+                                                    const std::uint8_t* mask_dev, const std::uint8_t* is_channel_dev,
+                                                    float D, float Sc, int32_t nonlinear, float dt_total,
+                                                    double rel_tol, int32_t max_pcg_iter, double residual_tol,
+                                                    int32_t max_outer, lsdtt_gpu_unet* net, float* z_out_dev,
+                                                    lsdtt_gpu_solve_report* report, void* stream)
+{
+    if (!net) return lsdtt_gb300::fail(LSDTT_GPU_EINVAL, "lsdtt_gpu_hillslope_implicit_learned: net is null");
+    return lsdtt_gb300::hillslope_implicit_impl("lsdtt_gpu_hillslope_implicit_learned", grid, z_dev, mask_dev,
+                                                is_channel_dev, D, Sc, nonlinear, dt_total, rel_tol, max_pcg_iter,
+                                                residual_tol, max_outer, net, z_out_dev, report, stream);
+}
+
+// Residual/correction pairs from the plain Jacobi-PCG solve of the first
+// linear system of a step of length dt (see the header for the layout).
+extern "C" int lsdtt_gpu_hillslope_capture_pairs(const lsdtt_gpu_grid* grid, const float* z_dev,
+                                                 const std::uint8_t* mask_dev, const std::uint8_t* is_channel_dev,
+                                                 float D, float Sc, int32_t nonlinear, float dt, double rel_tol,
+                                                 int32_t max_iter, int32_t n_pairs, float* r_out_dev,
+                                                 float* e_out_dev, int32_t* n_written, void* stream)
+{
+    using namespace lsdtt_gb300;
+    const char* who = "lsdtt_gpu_hillslope_capture_pairs";
+    if (!grid || !z_dev || !mask_dev || !r_out_dev || !e_out_dev || !n_written)
+        return fail(LSDTT_GPU_EINVAL, std::string(who) + ": null argument");
+    *n_written = 0;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        return fail(LSDTT_GPU_ENODEV, std::string(who) + ": no CUDA device");
+    if (!(grid->n_rows > 0 && grid->n_cols > 0 && grid->cell_size > 0.0) || !(dt > 0.0f) || n_pairs <= 0)
+        return fail(LSDTT_GPU_EINVAL, std::string(who) + ": invalid grid, dt or pair count");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const std::int64_t n = static_cast<std::int64_t>(grid->n_rows) * grid->n_cols;
+    const unsigned nb = grid_blocks(n, 256);
+    HsN P{};
+    P.H.nr = grid->n_rows;
+    P.H.nc = grid->n_cols;
+    const char* bc = grid->boundary_conditions;
+    P.H.bn = bc[0]; P.H.be = bc[1]; P.H.bs = bc[2]; P.H.bw = bc[3];
+    P.h = grid->cell_size;
+    P.H.DA = static_cast<double>(D) / (P.h * P.h);
+    P.H.U = 0.0;
+    P.H.inv_dt = 1.0 / static_cast<double>(dt);
+    P.Sc2 = static_cast<double>(Sc) * static_cast<double>(Sc);
+    P.cap = 0.9999;
+    P.nonlinear = nonlinear ? 1 : 0;
+    const int kPcg = max_iter > 0 ? max_iter : 2000;
+    const double rtol = rel_tol > 0 ? rel_tol : 1e-8;
+    HsnBuf B{};
+    const std::size_t need = static_cast<std::size_t>(n) * (2 * 8 + 16 + 8 * 4 + 1) + 64 * 256 +
+                             sizeof(double) * (8 + solve_acc_doubles(kPcg));
+    char* base = nullptr;
+    cudaError_t e = cudaMallocAsync(&base, need, st);
+    if (e == cudaSuccess) e = cudaMallocHost(&B.hacc, sizeof(double) * 8);
+    if (e != cudaSuccess)
+    {
+        if (base) cudaFreeAsync(base, st);
+        return cuda_fail(e, who);
+    }
+    char* cur = base;
+    auto carve = [&](std::size_t bytes) {
+        char* p = cur;
+        cur += (bytes + 255) & ~std::size_t(255);
+        return p;
+    };
+    B.z = reinterpret_cast<double*>(carve(8 * n));
+    B.F = reinterpret_cast<double*>(carve(8 * n));
+    B.zn = B.z;
+    B.alpha = reinterpret_cast<float4*>(carve(16 * n));
+    B.invd = reinterpret_cast<float*>(carve(4 * n));
+    B.b = reinterpret_cast<float*>(carve(4 * n));
+    B.x = reinterpret_cast<float*>(carve(4 * n));
+    B.r = reinterpret_cast<float*>(carve(4 * n));
+    B.p = reinterpret_cast<float*>(carve(4 * n));
+    B.zz = reinterpret_cast<float*>(carve(4 * n));
+    B.Ap = reinterpret_cast<float*>(carve(4 * n));
+    B.ro = reinterpret_cast<float*>(carve(4 * n));
+    B.dof = reinterpret_cast<std::uint8_t*>(carve(n));
+    B.acc = reinterpret_cast<double*>(carve(sizeof(double) * 8));
+    double* acc = reinterpret_cast<double*>(carve(sizeof(double) * solve_acc_doubles(kPcg)));
+    hs_setup<<<nb, 256, 0, st>>>(P.H, mask_dev, is_channel_dev, z_dev, z_dev, B.dof, B.invd, B.b, B.F);
+    hsn_to_double<<<nb, 256, 0, st>>>(n, z_dev, B.z);
+    double ev[3];
+    e = hsn_evaluate(P, mask_dev, B, B.z, n, st, ev);
+    int K = 0, written = 0;
+    double rel = 0.0;
+    auto init = [&]() -> double {
+        cudaMemsetAsync(acc, 0, sizeof(double) * solve_acc_doubles(kPcg), st);
+        hsn_pcg_init<<<nb, 256, 0, st>>>(P, mask_dev, B.dof, B.alpha, B.F, B.invd, B.b, B.x, B.r, B.p, acc);
+        cudaMemcpyAsync(B.hacc, acc, sizeof(double) * 2, cudaMemcpyDeviceToHost, st);
+        e = cudaStreamSynchronize(st);
+        return std::sqrt(B.hacc[1]);
+    };
+    if (e == cudaSuccess)
+    {
+        const double bnorm = init();
+        if (e == cudaSuccess && bnorm > 0.0)
+            e = jacobi_loop(P, mask_dev, B, n, bnorm, rtol, kPcg, st, acc + 16, acc, &K, &rel);
+        if (e == cudaSuccess && bnorm > 0.0 && K > 0)
+        {
+            // Second, identical solve with snapshots at n_pairs evenly spaced iterations.
+            std::vector<int> snaps;
+            for (int j = 0; j < n_pairs; ++j)
+            {
+                const int k = static_cast<int>(static_cast<std::int64_t>(j) * K / n_pairs);
+                if (snaps.empty() || k > snaps.back()) snaps.push_back(k);
+            }
+            init();
+            int k2 = 0;
+            if (e == cudaSuccess)
+                e = jacobi_loop(P, mask_dev, B, n, bnorm, rtol, K, st, acc + 16, acc, &k2, &rel, &snaps, e_out_dev,
+                                r_out_dev, false);
+            for (std::size_t j = 0; e == cudaSuccess && j < snaps.size(); ++j)
+                hsn_pair_finish<<<nb, 256, 0, st>>>(n, B.x, B.invd, r_out_dev + j * n, e_out_dev + j * n);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+            written = static_cast<int>(snaps.size());
+        }
+    }
+    cudaFreeAsync(base, st);
+    cudaFreeHost(B.hacc);
+    if (e != cudaSuccess) return cuda_fail(e, who);
+    *n_written = written;
     return LSDTT_GPU_OK;
 }

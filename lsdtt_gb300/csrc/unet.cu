@@ -1,0 +1,783 @@
+// unet.cu -- the learned preconditioner for the implicit hillslope solves.
+//
+// A 4-level U-Net with additive skips maps a residual r to an approximate
+// correction e ~ A^-1 r. It has no counterpart in the reference; the
+// network is defined, with its rounding points, by the CPU restatement
+// oracle/unet.py, which is also the oracle for these kernels:
+//
+//   x0 = bf16(r/rms(r));  e0 = relu(conv 1->16); e1 = relu(conv(pool) 16->32)
+//   e2 = relu(conv(pool) 32->64); e3 = relu(conv(pool) 64->64)
+//   d2 = relu(conv(up e3) 64->64) + e2; d1 = relu(conv(up d2) 64->32) + e1
+//   d0 = relu(conv(up d1) 32->16) + e0; y = rms * conv(d0) 16->1
+//
+// Activations are bf16 in NHWC layout, weights bf16 [Cout][3][3][Cin] with
+// an FP32 master copy, every accumulation FP32. The 3x3 convolutions with
+// 16..64 input channels run as implicit GEMMs on the tensor cores (bf16
+// mma.sync m16n8k16, FP32 accumulators): M = 16 output pixels per warp,
+// N = Cout, K = 9*Cin gathered straight from the NHWC activations (zero
+// padding at the borders, nearest-neighbour upsampling folded into the
+// gather). The one-channel input and output layers and the backward pass
+// (data and weight gradients, FP32) run on the CUDA cores; Adam updates the
+// FP32 master weights and re-packs bf16 copies.
+
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include <cuda_bf16.h>
+
+#include "engine.cuh"
+
+namespace lsdtt_gb300
+{
+namespace
+{
+
+constexpr int kLayers = 8;
+__host__ __device__ constexpr int layer_cin(int l)
+{
+    return l == 0 ? 1 : (l == 1 ? 16 : (l == 2 ? 32 : (l == 3 ? 64 : (l == 4 ? 64 : (l == 5 ? 64 : (l == 6 ? 32 : 16))))));
+}
+__host__ __device__ constexpr int layer_cout(int l)
+{
+    return l == 0 ? 16 : (l == 1 ? 32 : (l == 2 ? 64 : (l == 3 ? 64 : (l == 4 ? 64 : (l == 5 ? 32 : (l == 6 ? 16 : 1))))));
+}
+
+__device__ __forceinline__ float bfr(float v) { return __bfloat162float(__float2bfloat16_rn(v)); }
+
+// ---------------------------------------------------------------------------
+// forward
+// ---------------------------------------------------------------------------
+__global__ void k_sumsq(const float* __restrict__ r, std::int64_t n, double* __restrict__ acc)
+{
+    LSDTT_COUNT();
+    std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    double s = 0.0;
+    for (; i < n; i += static_cast<std::int64_t>(gridDim.x) * blockDim.x) s += static_cast<double>(r[i]) * r[i];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(acc, s);
+}
+
+// x0 = bf16(r / rms); rms computed from acc[0] = sum r^2 (n cells)
+__global__ void k_prep(const float* __restrict__ r, std::int64_t n, const double* __restrict__ acc,
+                       __nv_bfloat16* __restrict__ x0, float* __restrict__ rms_out)
+{
+    LSDTT_COUNT();
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    float rms = static_cast<float>(sqrt(acc[0] / static_cast<double>(n)));
+    if (!(rms > 0.0f)) rms = 1.0f;
+    if (i == 0) *rms_out = rms;
+    if (i < n) x0[i] = __float2bfloat16_rn(r[i] / rms);
+}
+
+// Layer 0: 1 -> 16 channels, ReLU, on CUDA cores.
+__global__ void k_conv_in(int H, int W, const __nv_bfloat16* __restrict__ x0, const float* __restrict__ w,
+                          const float* __restrict__ b, __nv_bfloat16* __restrict__ out)
+{
+    LSDTT_COUNT();
+    const std::int64_t p = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (p >= static_cast<std::int64_t>(H) * W) return;
+    const int y = static_cast<int>(p / W), x = static_cast<int>(p % W);
+    float v[9];
+#pragma unroll
+    for (int t = 0; t < 9; ++t)
+    {
+        const int yy = y + t / 3 - 1, xx = x + t % 3 - 1;
+        v[t] = (yy >= 0 && yy < H && xx >= 0 && xx < W) ? __bfloat162float(x0[static_cast<std::int64_t>(yy) * W + xx]) : 0.f;
+    }
+#pragma unroll
+    for (int co = 0; co < 16; ++co)
+    {
+        float s = b[co];
+#pragma unroll
+        for (int t = 0; t < 9; ++t) s = __fadd_rn(s, __fmul_rn(v[t], w[co * 9 + t]));
+        out[p * 16 + co] = __float2bfloat16_rn(fmaxf(s, 0.f));
+    }
+}
+
+// 2x2 mean, bf16 -> bf16 (H, W are the OUTPUT sizes)
+__global__ void k_pool(int H, int W, int C, const __nv_bfloat16* __restrict__ in, __nv_bfloat16* __restrict__ out)
+{
+    LSDTT_COUNT();
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= static_cast<std::int64_t>(H) * W * C) return;
+    const int c = static_cast<int>(i % C);
+    const std::int64_t p = i / C;
+    const int y = static_cast<int>(p / W), x = static_cast<int>(p % W);
+    const int W2 = 2 * W;
+    auto at = [&](int yy, int xx) { return __bfloat162float(in[(static_cast<std::int64_t>(yy) * W2 + xx) * C + c]); };
+    const float s = ((at(2 * y, 2 * x) + at(2 * y, 2 * x + 1)) + at(2 * y + 1, 2 * x)) + at(2 * y + 1, 2 * x + 1);
+    out[i] = __float2bfloat16_rn(s * 0.25f);
+}
+
+// Tensor-core 3x3 convolution, Cin and Cout multiples of 16 (Cin) / 8 (Cout).
+// One warp: 16 consecutive output pixels of one row x all Cout.
+//   mode 0: out = bf16(relu(acc + b))
+//   mode 1: pre = bf16(acc + b) stored; out = bf16(relu(acc + b) + skip)
+// `up`: the input is at half resolution (nearest upsampling folded in).
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(128) k_conv_tc(int H, int W, int up, const __nv_bfloat16* __restrict__ in,
+                                                 const __nv_bfloat16* __restrict__ wpk, const float* __restrict__ bias,
+                                                 int mode, const __nv_bfloat16* __restrict__ skip,
+                                                 __nv_bfloat16* __restrict__ pre, __nv_bfloat16* __restrict__ out)
+{
+    LSDTT_COUNT();
+    constexpr int NT = COUT / 8;  // n tiles
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int tiles_per_row = (W + 15) / 16;
+    const int y = warp / tiles_per_row;
+    const int x0 = (warp % tiles_per_row) * 16;
+    if (y >= H) return;
+    const int g = lane >> 2, tig = lane & 3;
+    const int Win = up ? (W >> 1) : W, Hin = up ? (H >> 1) : H;
+    float acc[NT][4];
+#pragma unroll
+    for (int t = 0; t < NT; ++t)
+        acc[t][0] = acc[t][1] = acc[t][2] = acc[t][3] = 0.f;
+    const int xa = x0 + g, xb = x0 + g + 8;  // the two pixel rows of the A fragment
+#pragma unroll 1
+    for (int tap = 0; tap < 9; ++tap)
+    {
+        const int yy = y + tap / 3 - 1;
+        const int xa2 = xa + tap % 3 - 1, xb2 = xb + tap % 3 - 1;
+        const bool va = yy >= 0 && yy < H && xa2 >= 0 && xa2 < W && xa < W;
+        const bool vb = yy >= 0 && yy < H && xb2 >= 0 && xb2 < W && xb < W;
+        const int sy = up ? (yy >> 1) : yy;
+        const std::int64_t ra = va ? (static_cast<std::int64_t>(sy) * Win + (up ? (xa2 >> 1) : xa2)) * CIN : 0;
+        const std::int64_t rb = vb ? (static_cast<std::int64_t>(sy) * Win + (up ? (xb2 >> 1) : xb2)) * CIN : 0;
+        (void)Hin;
+#pragma unroll
+        for (int kc = 0; kc < CIN / 16; ++kc)
+        {
+            const int c0 = kc * 16 + tig * 2;
+            const unsigned a0 = va ? *reinterpret_cast<const unsigned*>(in + ra + c0) : 0u;
+            const unsigned a1 = vb ? *reinterpret_cast<const unsigned*>(in + rb + c0) : 0u;
+            const unsigned a2 = va ? *reinterpret_cast<const unsigned*>(in + ra + c0 + 8) : 0u;
+            const unsigned a3 = vb ? *reinterpret_cast<const unsigned*>(in + rb + c0 + 8) : 0u;
+#pragma unroll
+            for (int nt = 0; nt < NT; ++nt)
+            {
+                const int co = nt * 8 + g;
+                const __nv_bfloat16* wp = wpk + (static_cast<std::int64_t>(co) * 9 + tap) * CIN + c0;
+                const unsigned b0 = *reinterpret_cast<const unsigned*>(wp);
+                const unsigned b1 = *reinterpret_cast<const unsigned*>(wp + 8);
+                asm volatile(
+                    "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 "
+                    "{%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, {%0, %1, %2, %3};\n"
+                    : "+f"(acc[nt][0]), "+f"(acc[nt][1]), "+f"(acc[nt][2]), "+f"(acc[nt][3])
+                    : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+            }
+        }
+    }
+    // Epilogue: c0,c1 -> pixel xa, channels nt*8 + tig*2 + {0,1}; c2,c3 -> pixel xb.
+#pragma unroll
+    for (int nt = 0; nt < NT; ++nt)
+    {
+        const int co = nt * 8 + tig * 2;
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+        {
+            const int xx = h ? xb : xa;
+            if (xx >= W) continue;
+            const std::int64_t o = (static_cast<std::int64_t>(y) * W + xx) * COUT + co;
+#pragma unroll
+            for (int q = 0; q < 2; ++q)
+            {
+                const float a = __fadd_rn(acc[nt][h * 2 + q], bias[co + q]);
+                if (mode == 0)
+                    out[o + q] = __float2bfloat16_rn(fmaxf(a, 0.f));
+                else
+                {
+                    pre[o + q] = __float2bfloat16_rn(a);
+                    out[o + q] = __float2bfloat16_rn(__fadd_rn(fmaxf(a, 0.f), __bfloat162float(skip[o + q])));
+                }
+            }
+        }
+    }
+}
+
+// Output layer: 16 -> 1 channel, times rms, FP32.
+__global__ void k_conv_out(int H, int W, const __nv_bfloat16* __restrict__ d0, const float* __restrict__ w,
+                           const float* __restrict__ b, const float* __restrict__ rms, float* __restrict__ y)
+{
+    LSDTT_COUNT();
+    const std::int64_t p = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (p >= static_cast<std::int64_t>(H) * W) return;
+    const int py = static_cast<int>(p / W), px = static_cast<int>(p % W);
+    float s = b[0];
+    for (int t = 0; t < 9; ++t)
+    {
+        const int yy = py + t / 3 - 1, xx = px + t % 3 - 1;
+        if (yy < 0 || yy >= H || xx < 0 || xx >= W) continue;
+        const __nv_bfloat16* src = d0 + (static_cast<std::int64_t>(yy) * W + xx) * 16;
+#pragma unroll
+        for (int c = 0; c < 16; ++c) s = __fadd_rn(s, __fmul_rn(__bfloat162float(src[c]), w[t * 16 + c]));
+    }
+    y[p] = __fmul_rn(s, *rms);
+}
+
+// ---------------------------------------------------------------------------
+// loss and backward (FP32, CUDA cores)
+// ---------------------------------------------------------------------------
+__global__ void k_loss_sums(const float* __restrict__ y, const float* __restrict__ e, std::int64_t n,
+                            double* __restrict__ acc)
+{
+    LSDTT_COUNT();
+    std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    double num = 0, den = 0;
+    for (; i < n; i += static_cast<std::int64_t>(gridDim.x) * blockDim.x)
+    {
+        const double d = static_cast<double>(y[i]) - e[i];
+        num += d * d;
+        den += static_cast<double>(e[i]) * e[i];
+    }
+    for (int o = 16; o > 0; o >>= 1)
+    {
+        num += __shfl_down_sync(0xffffffffu, num, o);
+        den += __shfl_down_sync(0xffffffffu, den, o);
+    }
+    if ((threadIdx.x & 31) == 0)
+    {
+        atomicAdd(&acc[0], num);
+        atomicAdd(&acc[1], den);
+    }
+}
+
+// go = 2 (y - e) / den * rms
+__global__ void k_loss_grad(const float* __restrict__ y, const float* __restrict__ e, std::int64_t n,
+                            const double* __restrict__ acc, const float* __restrict__ rms, float* __restrict__ go)
+{
+    LSDTT_COUNT();
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double den = acc[1] > 0 ? acc[1] : 1.0;
+    go[i] = static_cast<float>(2.0 * (static_cast<double>(y[i]) - e[i]) / den * (*rms));
+}
+
+// Backward of a 3x3 conv w.r.t. its input: dX[q][ci] = sum_tap sum_co
+// g[q - off(tap)][co] * w[co][tap][ci]. g is [H][W][Cout] FP32 at the conv's
+// output resolution. With `up`, X was the nearest upsampling of a half-
+// resolution field, and the result is summed over each 2x2 block (written
+// at half resolution). With `pool_from` (encoder), dX is the gradient of the
+// pooled input, which is distributed /4 onto the full-resolution skip
+// gradient `acc_full` ([2H][2W][Cin], accumulated with +=) instead.
+__global__ void k_conv_bwd_data(int H, int W, int Cin, int Cout, int up, const float* __restrict__ g,
+                                const float* __restrict__ w, float* __restrict__ dx, int pool_to_full,
+                                float* __restrict__ acc_full)
+{
+    LSDTT_COUNT();
+    const int Ho = up ? H / 2 : H, Wo = up ? W / 2 : W;  // resolution of the result
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= static_cast<std::int64_t>(Ho) * Wo * Cin) return;
+    const int ci = static_cast<int>(i % Cin);
+    const std::int64_t q = i / Cin;
+    const int qy = static_cast<int>(q / Wo), qx = static_cast<int>(q % Wo);
+    float s = 0.f;
+    const int reps = up ? 4 : 1;
+    for (int sub = 0; sub < reps; ++sub)
+    {
+        const int fy = up ? 2 * qy + (sub >> 1) : qy, fx = up ? 2 * qx + (sub & 1) : qx;
+        for (int t = 0; t < 9; ++t)
+        {
+            const int py = fy - (t / 3 - 1), px = fx - (t % 3 - 1);  // output pixel that reads (fy,fx) via tap t
+            if (py < 0 || py >= H || px < 0 || px >= W) continue;
+            const float* gp = g + (static_cast<std::int64_t>(py) * W + px) * Cout;
+            const float* wp = w + static_cast<std::int64_t>(t) * Cin + ci;
+            for (int co = 0; co < Cout; ++co) s += gp[co] * wp[static_cast<std::int64_t>(co) * 9 * Cin];
+        }
+    }
+    if (pool_to_full)
+    {
+        const int W2 = 2 * Wo;
+        const float v = s * 0.25f;
+        for (int sub = 0; sub < 4; ++sub)
+        {
+            const std::int64_t f = (static_cast<std::int64_t>(2 * qy + (sub >> 1)) * W2 + 2 * qx + (sub & 1)) * Cin + ci;
+            acc_full[f] += v;
+        }
+    }
+    else
+        dx[i] = s;
+}
+
+// Weight/bias gradients of a 3x3 conv: gw[co][tap][ci] += sum_p g[p][co] *
+// X[p + off(tap)][ci], gb[co] += sum_p g[p][co]. One block per (co, tap)
+// pair reduces over a strided pixel range; X is bf16 ([H][W][Cin], or half
+// resolution with `up`).
+__global__ void k_conv_bwd_w(int H, int W, int Cin, int Cout, int up, const float* __restrict__ g,
+                             const __nv_bfloat16* __restrict__ X, float* __restrict__ gw, float* __restrict__ gb)
+{
+    LSDTT_COUNT();
+    extern __shared__ float red[];  // [Cin + 1][32]
+    const int co = blockIdx.y / 9, t = blockIdx.y % 9;
+    const int Win = up ? W / 2 : W;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    float part[64 + 1];
+    for (int c = 0; c <= Cin; ++c) part[c] = 0.f;
+    const std::int64_t npix = static_cast<std::int64_t>(H) * W;
+    for (std::int64_t p = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; p < npix;
+         p += static_cast<std::int64_t>(gridDim.x) * blockDim.x)
+    {
+        const float gv = g[p * Cout + co];
+        if (gv == 0.f) continue;
+        if (t == 4) part[Cin] += gv;
+        const int py = static_cast<int>(p / W) + t / 3 - 1, px = static_cast<int>(p % W) + t % 3 - 1;
+        if (py < 0 || py >= H || px < 0 || px >= W) continue;
+        const __nv_bfloat16* xp = X + (static_cast<std::int64_t>(up ? py >> 1 : py) * Win + (up ? px >> 1 : px)) * Cin;
+        for (int c = 0; c < Cin; ++c) part[c] += gv * __bfloat162float(xp[c]);
+    }
+    for (int c = 0; c <= Cin; ++c)
+    {
+        float v = part[c];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) red[c * 32 + warp] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x <= Cin)
+    {
+        float v = 0.f;
+        for (int k = 0; k < nw; ++k) v += red[threadIdx.x * 32 + k];
+        if (threadIdx.x < Cin) atomicAdd(&gw[(static_cast<std::int64_t>(co) * 9 + t) * Cin + threadIdx.x], v);
+        else if (t == 4) atomicAdd(&gb[co], v);
+    }
+}
+
+// Decoder split: ga = gd * (pre > 0); gskip += gd.
+__global__ void k_relu_skip_bwd(std::int64_t n, const float* __restrict__ gd, const __nv_bfloat16* __restrict__ pre,
+                                float* __restrict__ ga, float* __restrict__ gskip)
+{
+    LSDTT_COUNT();
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float v = gd[i];
+    ga[i] = __bfloat162float(pre[i]) > 0.f ? v : 0.f;
+    gskip[i] += v;
+}
+
+// Encoder: g = gsum * (act > 0) (act = relu output, bf16).
+__global__ void k_relu_mask(std::int64_t n, const float* __restrict__ gsum, const __nv_bfloat16* __restrict__ act,
+                            float* __restrict__ g)
+{
+    LSDTT_COUNT();
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    g[i] = __bfloat162float(act[i]) > 0.f ? gsum[i] : 0.f;
+}
+
+__global__ void k_adam(std::int64_t n, float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m,
+                       float* __restrict__ v, float lr, float b1, float b2, float eps, float c1, float c2)
+{
+    LSDTT_COUNT();
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.f - b1) * gi;
+    const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    w[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+}
+
+__global__ void k_sgd(std::int64_t n, float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m,
+                      float lr, float mom)
+{
+    LSDTT_COUNT();
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float mi = mom * m[i] + g[i];
+    m[i] = mi;
+    w[i] -= lr * mi;
+}
+
+__global__ void k_pack(std::int64_t n, const float* __restrict__ w, __nv_bfloat16* __restrict__ wb)
+{
+    LSDTT_COUNT();
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < n) wb[i] = __float2bfloat16_rn(w[i]);
+}
+
+// Weights as used by the forward pass: bf16 round trip of the FP32 master.
+__global__ void k_bf16_round(std::int64_t n, const float* __restrict__ w, float* __restrict__ wr)
+{
+    LSDTT_COUNT();
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < n) wr[i] = bfr(w[i]);
+}
+
+}  // namespace
+}  // namespace lsdtt_gb300
+
+using namespace lsdtt_gb300;
+
+struct lsdtt_gpu_unet
+{
+    int maxH = 0, maxW = 0;
+    std::int64_t woff[kLayers + 1] = {};  // weight offsets into the parameter vector
+    std::int64_t boff[kLayers + 1] = {};  // bias offsets
+    std::int64_t nparam = 0;
+    float* w = nullptr;   // FP32 master: weights then biases
+    float* wr = nullptr;  // bf16-rounded copy as FP32 (CUDA-core layers, backward)
+    __nv_bfloat16* wb = nullptr;
+    float *g = nullptr, *m = nullptr, *v = nullptr;
+    long step = 0;
+    // activations (bf16, NHWC)
+    __nv_bfloat16 *x0 = nullptr, *e0 = nullptr, *p0 = nullptr, *e1 = nullptr, *p1 = nullptr, *e2 = nullptr,
+                  *p2 = nullptr, *e3 = nullptr, *a2 = nullptr, *d2 = nullptr, *a1 = nullptr, *d1 = nullptr,
+                  *a0 = nullptr, *d0 = nullptr;
+    float *y = nullptr, *go = nullptr, *rms = nullptr;
+    double* acc = nullptr;
+    double* hacc = nullptr;
+    // backward scratch (FP32), allocated by the first gradient evaluation
+    float *gA = nullptr, *gB = nullptr, *ge0 = nullptr, *ge1 = nullptr, *ge2 = nullptr, *ge3 = nullptr;
+};
+
+namespace
+{
+
+std::int64_t level_px(const lsdtt_gpu_unet* U, int l)
+{
+    return static_cast<std::int64_t>(U->maxH >> l) * (U->maxW >> l);
+}
+
+template <class T>
+cudaError_t ualloc(T** p, std::size_t count)
+{
+    return cudaMalloc(reinterpret_cast<void**>(p), sizeof(T) * (count ? count : 1));
+}
+
+int check_shape(const lsdtt_gpu_unet* U, int H, int W)
+{
+    if (H <= 0 || W <= 0 || (H & 7) || (W & 7) || H > U->maxH || W > U->maxW ||
+        static_cast<std::int64_t>(H) * W > static_cast<std::int64_t>(U->maxH) * U->maxW)
+        return fail(LSDTT_GPU_EINVAL, "lsdtt_gpu_unet: image must be a multiple of 8 on each side and fit the "
+                                      "handle's capacity (" + std::to_string(U->maxH) + " x " +
+                                          std::to_string(U->maxW) + ")");
+    return LSDTT_GPU_OK;
+}
+
+void launch_conv_tc(int l, int H, int W, int up, const __nv_bfloat16* in, const __nv_bfloat16* wpk, const float* b,
+                    int mode, const __nv_bfloat16* skip, __nv_bfloat16* pre, __nv_bfloat16* out, cudaStream_t st)
+{
+    const int warps = H * ((W + 15) / 16);
+    const unsigned blocks = static_cast<unsigned>((warps + 3) / 4);
+    const double bytes = 2.0 * static_cast<double>(H) * W * (layer_cin(l) / (up ? 4.0 : 1.0) + layer_cout(l));
+#define LSDTT_CONV_CASE(CI, CO)                                                                                     \
+    if (layer_cin(l) == CI && layer_cout(l) == CO)                                                                  \
+    {                                                                                                               \
+        LSDTT_TIMED("unet_conv_tc", bytes, st,                                                                      \
+                    (k_conv_tc<CI, CO><<<blocks, 128, 0, st>>>(H, W, up, in, wpk, b, mode, skip, pre, out)));       \
+        return;                                                                                                     \
+    }
+    LSDTT_CONV_CASE(16, 32)
+    LSDTT_CONV_CASE(32, 64)
+    LSDTT_CONV_CASE(64, 64)
+    LSDTT_CONV_CASE(64, 32)
+    LSDTT_CONV_CASE(32, 16)
+#undef LSDTT_CONV_CASE
+}
+
+// Forward pass on an H x W residual (device, FP32) -> U->y.
+cudaError_t unet_forward(lsdtt_gpu_unet* U, const float* r, int H, int W, cudaStream_t st)
+{
+    const std::int64_t n = static_cast<std::int64_t>(H) * W;
+    cudaMemsetAsync(U->acc, 0, sizeof(double), st);
+    k_sumsq<<<152 * 4, 256, 0, st>>>(r, n, U->acc);
+    k_prep<<<grid_blocks(n, 256), 256, 0, st>>>(r, n, U->acc, U->x0, U->rms);
+    const float* wr = U->wr;
+    k_conv_in<<<grid_blocks(n, 128), 128, 0, st>>>(H, W, U->x0, wr + U->woff[0], U->w + U->boff[0], U->e0);
+    int h = H / 2, w = W / 2;
+    k_pool<<<grid_blocks(static_cast<std::int64_t>(h) * w * 16, 256), 256, 0, st>>>(h, w, 16, U->e0, U->p0);
+    launch_conv_tc(1, h, w, 0, U->p0, U->wb + U->woff[1], U->w + U->boff[1], 0, nullptr, nullptr, U->e1, st);
+    h /= 2; w /= 2;
+    k_pool<<<grid_blocks(static_cast<std::int64_t>(h) * w * 32, 256), 256, 0, st>>>(h, w, 32, U->e1, U->p1);
+    launch_conv_tc(2, h, w, 0, U->p1, U->wb + U->woff[2], U->w + U->boff[2], 0, nullptr, nullptr, U->e2, st);
+    h /= 2; w /= 2;
+    k_pool<<<grid_blocks(static_cast<std::int64_t>(h) * w * 64, 256), 256, 0, st>>>(h, w, 64, U->e2, U->p2);
+    launch_conv_tc(3, h, w, 0, U->p2, U->wb + U->woff[3], U->w + U->boff[3], 0, nullptr, nullptr, U->e3, st);
+    launch_conv_tc(4, H / 4, W / 4, 1, U->e3, U->wb + U->woff[4], U->w + U->boff[4], 1, U->e2, U->a2, U->d2, st);
+    launch_conv_tc(5, H / 2, W / 2, 1, U->d2, U->wb + U->woff[5], U->w + U->boff[5], 1, U->e1, U->a1, U->d1, st);
+    launch_conv_tc(6, H, W, 1, U->d1, U->wb + U->woff[6], U->w + U->boff[6], 1, U->e0, U->a0, U->d0, st);
+    k_conv_out<<<grid_blocks(n, 128), 128, 0, st>>>(H, W, U->d0, wr + U->woff[7], U->w + U->boff[7], U->rms, U->y);
+    return cudaGetLastError();
+}
+
+// Backward pass: gradients of loss = sum (y-e)^2/sum e^2 into U->g.
+cudaError_t unet_backward(lsdtt_gpu_unet* U, const float* e, int H, int W, cudaStream_t st)
+{
+    const std::int64_t n = static_cast<std::int64_t>(H) * W;
+    cudaMemsetAsync(U->g, 0, sizeof(float) * U->nparam, st);
+    cudaMemsetAsync(U->acc + 1, 0, sizeof(double) * 2, st);
+    k_loss_sums<<<152 * 4, 256, 0, st>>>(U->y, e, n, U->acc + 1);
+    k_loss_grad<<<grid_blocks(n, 256), 256, 0, st>>>(U->y, e, n, U->acc + 1, U->rms, U->go);
+    const float* wr = U->wr;
+    auto bw = [&](int l, int h, int w, int up, const float* g, const __nv_bfloat16* X) {
+        const int ci = layer_cin(l), co = layer_cout(l);
+        const dim3 grid(64, co * 9);
+        k_conv_bwd_w<<<grid, 256, sizeof(float) * (ci + 1) * 32, st>>>(h, w, ci, co, up, g, X, U->g + U->woff[l],
+                                                                        U->g + U->boff[l]);
+    };
+    // out layer (16 -> 1): input d0 at H x W
+    bw(7, H, W, 0, U->go, U->d0);
+    k_conv_bwd_data<<<grid_blocks(n * 16, 256), 256, 0, st>>>(H, W, 16, 1, 0, U->go, wr + U->woff[7], U->gA, 0,
+                                                              nullptr);
+    // ge0 starts as the skip gradient from d0; dec0: d0 = relu(a0) + e0
+    cudaMemsetAsync(U->ge0, 0, sizeof(float) * n * 16, st);
+    k_relu_skip_bwd<<<grid_blocks(n * 16, 256), 256, 0, st>>>(n * 16, U->gA, U->a0, U->gB, U->ge0);
+    bw(6, H, W, 1, U->gB, U->d1);  // input of dec0 is up(d1)
+    const std::int64_t n1 = n / 4, n2 = n / 16, n3 = n / 64;
+    k_conv_bwd_data<<<grid_blocks(n1 * 32, 256), 256, 0, st>>>(H, W, 32, 16, 1, U->gB, wr + U->woff[6], U->gA, 0,
+                                                               nullptr);  // gd1 (half res) in gA
+    cudaMemsetAsync(U->ge1, 0, sizeof(float) * n1 * 32, st);
+    k_relu_skip_bwd<<<grid_blocks(n1 * 32, 256), 256, 0, st>>>(n1 * 32, U->gA, U->a1, U->gB, U->ge1);
+    bw(5, H / 2, W / 2, 1, U->gB, U->d2);
+    k_conv_bwd_data<<<grid_blocks(n2 * 64, 256), 256, 0, st>>>(H / 2, W / 2, 64, 32, 1, U->gB, wr + U->woff[5], U->gA,
+                                                               0, nullptr);  // gd2
+    cudaMemsetAsync(U->ge2, 0, sizeof(float) * n2 * 64, st);
+    k_relu_skip_bwd<<<grid_blocks(n2 * 64, 256), 256, 0, st>>>(n2 * 64, U->gA, U->a2, U->gB, U->ge2);
+    bw(4, H / 4, W / 4, 1, U->gB, U->e3);
+    k_conv_bwd_data<<<grid_blocks(n3 * 64, 256), 256, 0, st>>>(H / 4, W / 4, 64, 64, 1, U->gB, wr + U->woff[4],
+                                                               U->ge3, 0, nullptr);  // ge3 (1/8 res)
+    // encoder 3: e3 = relu(conv(p2)); p2 = pool(e2)
+    k_relu_mask<<<grid_blocks(n3 * 64, 256), 256, 0, st>>>(n3 * 64, U->ge3, U->e3, U->gB);
+    bw(3, H / 8, W / 8, 0, U->gB, U->p2);
+    k_conv_bwd_data<<<grid_blocks(n3 * 64, 256), 256, 0, st>>>(H / 8, W / 8, 64, 64, 0, U->gB, wr + U->woff[3],
+                                                               nullptr, 1, U->ge2);
+    k_relu_mask<<<grid_blocks(n2 * 64, 256), 256, 0, st>>>(n2 * 64, U->ge2, U->e2, U->gB);
+    bw(2, H / 4, W / 4, 0, U->gB, U->p1);
+    k_conv_bwd_data<<<grid_blocks(n2 * 32, 256), 256, 0, st>>>(H / 4, W / 4, 32, 64, 0, U->gB, wr + U->woff[2],
+                                                               nullptr, 1, U->ge1);
+    k_relu_mask<<<grid_blocks(n1 * 32, 256), 256, 0, st>>>(n1 * 32, U->ge1, U->e1, U->gB);
+    bw(1, H / 2, W / 2, 0, U->gB, U->p0);
+    k_conv_bwd_data<<<grid_blocks(n1 * 16, 256), 256, 0, st>>>(H / 2, W / 2, 16, 32, 0, U->gB, wr + U->woff[1],
+                                                               nullptr, 1, U->ge0);
+    k_relu_mask<<<grid_blocks(n * 16, 256), 256, 0, st>>>(n * 16, U->ge0, U->e0, U->gB);
+    bw(0, H, W, 0, U->gB, U->x0);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+namespace lsdtt_gb300
+{
+int unet_check_shape(const lsdtt_gpu_unet* U, int H, int W) { return check_shape(U, H, W); }
+
+cudaError_t unet_forward_dev(lsdtt_gpu_unet* U, const float* r_dev, int H, int W, cudaStream_t st,
+                             const float** y_dev)
+{
+    *y_dev = U->y;
+    return unet_forward(U, r_dev, H, W, st);
+}
+}  // namespace lsdtt_gb300
+
+extern "C" {
+
+int lsdtt_gpu_unet_create(int32_t max_rows, int32_t max_cols, uint64_t seed, lsdtt_gpu_unet** out)
+{
+    if (!out) return fail(LSDTT_GPU_EINVAL, "lsdtt_gpu_unet_create: out is null");
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        return fail(LSDTT_GPU_ENODEV, "lsdtt_gpu_unet_create: no CUDA device");
+    if (max_rows <= 0 || max_cols <= 0 || (max_rows & 7) || (max_cols & 7))
+        return fail(LSDTT_GPU_EINVAL, "lsdtt_gpu_unet_create: capacity must be positive multiples of 8");
+    auto* U = new lsdtt_gpu_unet();
+    U->maxH = max_rows;
+    U->maxW = max_cols;
+    std::int64_t off = 0;
+    for (int l = 0; l < kLayers; ++l)
+    {
+        U->woff[l] = off;
+        off += static_cast<std::int64_t>(layer_cout(l)) * 9 * layer_cin(l);
+    }
+    U->woff[kLayers] = off;
+    for (int l = 0; l < kLayers; ++l)
+    {
+        U->boff[l] = off;
+        off += layer_cout(l);
+    }
+    U->boff[kLayers] = off;
+    U->nparam = off;
+    // He initialisation from a splitmix-seeded Box-Muller stream, on the host.
+    std::vector<float> h(static_cast<std::size_t>(off), 0.0f);
+    std::uint64_t s = seed ? seed : 0x1234567ULL;
+    auto next = [&]() {
+        s += 0x9E3779B97F4A7C15ULL;
+        std::uint64_t x = s;
+        x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ULL;
+        x = (x ^ (x >> 27)) * 0x94D049BB133111EBULL;
+        x ^= x >> 31;
+        return (static_cast<double>(x >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+    };
+    for (int l = 0; l < kLayers; ++l)
+    {
+        const double std_dev = (l == kLayers - 1) ? 0.1 * std::sqrt(1.0 / (9.0 * layer_cin(l)))
+                                                  : std::sqrt(2.0 / (9.0 * layer_cin(l)));
+        for (std::int64_t i = U->woff[l]; i < U->woff[l + 1]; ++i)
+        {
+            const double u1 = next(), u2 = next();
+            h[static_cast<std::size_t>(i)] =
+                static_cast<float>(std_dev * std::sqrt(-2.0 * std::log(u1)) * std::cos(6.283185307179586 * u2));
+        }
+    }
+    const std::int64_t px0 = level_px(U, 0);
+    cudaError_t e = ualloc(&U->w, off);
+    if (e == cudaSuccess) e = ualloc(&U->wr, off);
+    if (e == cudaSuccess) e = ualloc(&U->wb, off);
+    if (e == cudaSuccess) e = ualloc(&U->g, off);
+    if (e == cudaSuccess) e = ualloc(&U->m, off);
+    if (e == cudaSuccess) e = ualloc(&U->v, off);
+    if (e == cudaSuccess) e = ualloc(&U->x0, px0);
+    if (e == cudaSuccess) e = ualloc(&U->e0, px0 * 16);
+    if (e == cudaSuccess) e = ualloc(&U->a0, px0 * 16);
+    if (e == cudaSuccess) e = ualloc(&U->d0, px0 * 16);
+    if (e == cudaSuccess) e = ualloc(&U->p0, level_px(U, 1) * 16);
+    if (e == cudaSuccess) e = ualloc(&U->e1, level_px(U, 1) * 32);
+    if (e == cudaSuccess) e = ualloc(&U->a1, level_px(U, 1) * 32);
+    if (e == cudaSuccess) e = ualloc(&U->d1, level_px(U, 1) * 32);
+    if (e == cudaSuccess) e = ualloc(&U->p1, level_px(U, 2) * 32);
+    if (e == cudaSuccess) e = ualloc(&U->e2, level_px(U, 2) * 64);
+    if (e == cudaSuccess) e = ualloc(&U->a2, level_px(U, 2) * 64);
+    if (e == cudaSuccess) e = ualloc(&U->d2, level_px(U, 2) * 64);
+    if (e == cudaSuccess) e = ualloc(&U->p2, level_px(U, 3) * 64);
+    if (e == cudaSuccess) e = ualloc(&U->e3, level_px(U, 3) * 64);
+    if (e == cudaSuccess) e = ualloc(&U->y, px0);
+    if (e == cudaSuccess) e = ualloc(&U->go, px0);
+    if (e == cudaSuccess) e = ualloc(&U->rms, 1);
+    if (e == cudaSuccess) e = ualloc(&U->acc, 4);
+    if (e == cudaSuccess) e = cudaMallocHost(reinterpret_cast<void**>(&U->hacc), sizeof(double) * 4);
+    if (e == cudaSuccess) e = cudaMemcpy(U->w, h.data(), sizeof(float) * off, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(U->m, 0, sizeof(float) * off);
+    if (e == cudaSuccess) e = cudaMemset(U->v, 0, sizeof(float) * off);
+    if (e != cudaSuccess)
+    {
+        lsdtt_gpu_unet_destroy(U);
+        return cuda_fail(e, "lsdtt_gpu_unet_create");
+    }
+    k_pack<<<grid_blocks(off, 256), 256>>>(off, U->w, U->wb);
+    k_bf16_round<<<grid_blocks(off, 256), 256>>>(off, U->w, U->wr);
+    e = cudaDeviceSynchronize();
+    if (e != cudaSuccess)
+    {
+        lsdtt_gpu_unet_destroy(U);
+        return cuda_fail(e, "lsdtt_gpu_unet_create");
+    }
+    *out = U;
+    return LSDTT_GPU_OK;
+}
+
+int lsdtt_gpu_unet_destroy(lsdtt_gpu_unet* U)
+{
+    if (!U) return LSDTT_GPU_OK;
+    void* ptrs[] = {U->w, U->wr, U->wb, U->g, U->m, U->v, U->x0, U->e0, U->a0, U->d0, U->p0, U->e1, U->a1, U->d1, U->p1,
+                    U->e2, U->a2, U->d2, U->p2, U->e3, U->y, U->go, U->rms, U->acc, U->gA, U->gB, U->ge0, U->ge1,
+                    U->ge2, U->ge3};
+    for (void* p : ptrs) cudaFree(p);
+    cudaFreeHost(U->hacc);
+    delete U;
+    return LSDTT_GPU_OK;
+}
+
+int64_t lsdtt_gpu_unet_num_params(const lsdtt_gpu_unet* U) { return U ? U->nparam : 0; }
+
+int lsdtt_gpu_unet_get_params(const lsdtt_gpu_unet* U, float* host, int64_t count)
+{
+    if (!U || !host || count != U->nparam) return fail(LSDTT_GPU_EINVAL, "lsdtt_gpu_unet_get_params: bad argument");
+    return cudaMemcpy(host, U->w, sizeof(float) * count, cudaMemcpyDeviceToHost) == cudaSuccess
+               ? LSDTT_GPU_OK
+               : fail(LSDTT_GPU_ECUDA, "lsdtt_gpu_unet_get_params: copy failed");
+}
+
+int lsdtt_gpu_unet_set_params(lsdtt_gpu_unet* U, const float* host, int64_t count)
+{
+    if (!U || !host || count != U->nparam) return fail(LSDTT_GPU_EINVAL, "lsdtt_gpu_unet_set_params: bad argument");
+    if (cudaMemcpy(U->w, host, sizeof(float) * count, cudaMemcpyHostToDevice) != cudaSuccess)
+        return fail(LSDTT_GPU_ECUDA, "lsdtt_gpu_unet_set_params: copy failed");
+    k_pack<<<grid_blocks(count, 256), 256>>>(count, U->w, U->wb);
+    k_bf16_round<<<grid_blocks(count, 256), 256>>>(count, U->w, U->wr);
+    return cudaDeviceSynchronize() == cudaSuccess ? LSDTT_GPU_OK : fail(LSDTT_GPU_ECUDA, "lsdtt_gpu_unet_set_params");
+}
+
+// y = U(r) for an H x W residual (device, FP32), written to y_dev.
+int lsdtt_gpu_unet_apply(lsdtt_gpu_unet* U, const float* r_dev, int32_t H, int32_t W, float* y_dev, void* stream)
+{
+    if (!U || !r_dev || !y_dev) return fail(LSDTT_GPU_EINVAL, "lsdtt_gpu_unet_apply: null argument");
+    if (int s = check_shape(U, H, W)) return s;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaError_t e = unet_forward(U, r_dev, H, W, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(y_dev, U->y, sizeof(float) * static_cast<std::size_t>(H) * W, cudaMemcpyDeviceToDevice, st);
+    return e == cudaSuccess ? LSDTT_GPU_OK : cuda_fail(e, "lsdtt_gpu_unet_apply");
+}
+
+// Loss and parameter gradients (FP32, [nparam] into grad_host when given)
+// without updating the weights; for gradient checks.
+int lsdtt_gpu_unet_loss_grad(lsdtt_gpu_unet* U, const float* r_dev, const float* e_dev, int32_t H, int32_t W,
+                             double* loss, float* grad_host, void* stream)
+{
+    if (!U || !r_dev || !e_dev) return fail(LSDTT_GPU_EINVAL, "lsdtt_gpu_unet_loss_grad: null argument");
+    if (int s = check_shape(U, H, W)) return s;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaError_t e = cudaSuccess;
+    if (!U->gA)
+    {
+        // Backward scratch (FP32, 4x the bf16 activations): only when training.
+        const std::int64_t px0 = level_px(U, 0);
+        e = ualloc(&U->gA, px0 * 16);
+        if (e == cudaSuccess) e = ualloc(&U->gB, px0 * 16);
+        if (e == cudaSuccess) e = ualloc(&U->ge0, px0 * 16);
+        if (e == cudaSuccess) e = ualloc(&U->ge1, level_px(U, 1) * 32);
+        if (e == cudaSuccess) e = ualloc(&U->ge2, level_px(U, 2) * 64);
+        if (e == cudaSuccess) e = ualloc(&U->ge3, level_px(U, 3) * 64);
+        if (e != cudaSuccess)
+        {
+            void* bufs[] = {U->gA, U->gB, U->ge0, U->ge1, U->ge2, U->ge3};
+            for (void* b : bufs) cudaFree(b);
+            U->gA = U->gB = U->ge0 = U->ge1 = U->ge2 = U->ge3 = nullptr;
+            return cuda_fail(e, "lsdtt_gpu_unet_loss_grad");
+        }
+    }
+    e = unet_forward(U, r_dev, H, W, st);
+    if (e == cudaSuccess) e = unet_backward(U, e_dev, H, W, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(U->hacc, U->acc + 1, sizeof(double) * 2, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && grad_host)
+        e = cudaMemcpyAsync(grad_host, U->g, sizeof(float) * U->nparam, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(e, "lsdtt_gpu_unet_loss_grad");
+    if (loss) *loss = U->hacc[0] / (U->hacc[1] > 0 ? U->hacc[1] : 1.0);
+    return LSDTT_GPU_OK;
+}
+
+// One optimiser step on the pair (r, e); returns the loss before the step.
+int lsdtt_gpu_unet_train_step(lsdtt_gpu_unet* U, const float* r_dev, const float* e_dev, int32_t H, int32_t W,
+                              int32_t optimizer, float lr, double* loss, void* stream)
+{
+    if (optimizer != 0 && optimizer != 1)
+        return fail(LSDTT_GPU_EINVAL, "lsdtt_gpu_unet_train_step: optimizer must be 0 (SGD) or 1 (Adam)");
+    int s = lsdtt_gpu_unet_loss_grad(U, r_dev, e_dev, H, W, loss, nullptr, stream);
+    if (s != LSDTT_GPU_OK) return s;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    ++U->step;
+    const unsigned nb = grid_blocks(U->nparam, 256);
+    if (optimizer == 1)
+    {
+        const float b1 = 0.9f, b2 = 0.999f;
+        const float c1 = 1.0f - std::pow(b1, static_cast<float>(U->step));
+        const float c2 = 1.0f - std::pow(b2, static_cast<float>(U->step));
+        k_adam<<<nb, 256, 0, st>>>(U->nparam, U->w, U->g, U->m, U->v, lr, b1, b2, 1e-8f, c1, c2);
+    }
+    else
+        k_sgd<<<nb, 256, 0, st>>>(U->nparam, U->w, U->g, U->m, lr, 0.9f);
+    k_pack<<<nb, 256, 0, st>>>(U->nparam, U->w, U->wb);
+    k_bf16_round<<<nb, 256, 0, st>>>(U->nparam, U->w, U->wr);
+    const cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? LSDTT_GPU_OK : cuda_fail(e, "lsdtt_gpu_unet_train_step");
+}
+
+}  // extern "C"
+
+namespace lsdtt_gb300
+{
+LSDTT_DEFINE_LAUNCH_READER(unet)
+}  // namespace lsdtt_gb300
