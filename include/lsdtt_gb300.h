@@ -309,6 +309,72 @@ int lsdtt_gpu_lem_destroy(lsdtt_gpu_lem* lem);
 /* Advances z_dev (in place) by one timestep. stats may be NULL. */
 int lsdtt_gpu_lem_step(lsdtt_gpu_lem* lem, float* z_dev, lsdtt_gpu_lem_stats* stats, void* stream);
 
+/* ---- batched ensembles -----------------------------------------------------
+ * Parameter-sweep ensembles of independent LEM runs on grids of different
+ * shapes. Each member advances exactly as lsdtt_gpu_lem_step would advance
+ * it alone (same fill, D8 receivers, contributing counts, stream power,
+ * linear implicit hillslope solved to the member's own relative residual,
+ * uplift and boundary restore); the reference runs one grid per lsdtt-lem
+ * process (src/cpu/lsdtt_lem_cpu.cpp:285-732), so this has no counterpart
+ * beyond that loop. The members' cells are packed back to back in one
+ * device buffer and every stage is one launch over all members; a step is
+ * replayed as one captured CUDA graph whose fill-pass, stream-power level
+ * and PCG iteration schedule is taken from an eager step and autotuned. A
+ * step that outgrows the captured schedule is detected on the device,
+ * undone and rerun eagerly, and the graph is captured again. */
+typedef struct lsdtt_gpu_member
+{
+    lsdtt_gpu_grid grid;
+    lsdtt_gpu_lem_options options;
+} lsdtt_gpu_member;
+
+typedef struct lsdtt_gpu_ensemble lsdtt_gpu_ensemble;
+
+/* use_graph = 0 runs every step eagerly (host-driven loops). */
+int lsdtt_gpu_ensemble_create(const lsdtt_gpu_member* members, int32_t n_members, int32_t use_graph,
+                              lsdtt_gpu_ensemble** out, void* stream);
+int lsdtt_gpu_ensemble_destroy(lsdtt_gpu_ensemble* ens);
+/* Packed layout: member k's cells are [offsets[k], offsets[k] + n_rows*n_cols)
+ * of the packed buffers; offsets has n_members + 1 entries (the last is the
+ * packed length). */
+int lsdtt_gpu_ensemble_offsets(const lsdtt_gpu_ensemble* ens, int64_t* offsets_host);
+/* Member k's surface and validity mask (device arrays of its grid). The
+ * mask also fixes the member's boundary flats. */
+int lsdtt_gpu_ensemble_set_member(lsdtt_gpu_ensemble* ens, int32_t k, const float* z_dev, const uint8_t* mask_dev,
+                                  void* stream);
+int lsdtt_gpu_ensemble_get_member(const lsdtt_gpu_ensemble* ens, int32_t k, float* z_dev, void* stream);
+/* Advances every member by n_steps steps. stats (n_members entries, may be
+ * NULL) receive the last step's statistics; p999_local_elevation_change is
+ * not computed in an ensemble and is 0. */
+int lsdtt_gpu_ensemble_step(lsdtt_gpu_ensemble* ens, int32_t n_steps, lsdtt_gpu_lem_stats* stats, void* stream);
+
+typedef struct lsdtt_gpu_ensemble_info
+{
+    int64_t packed_cells;         /* packed buffer length */
+    int64_t member_cells;         /* sum of the members' n_rows * n_cols */
+    int32_t graph_enabled;
+    int32_t graph_captures;
+    int32_t graph_replays;
+    int32_t eager_steps;
+    int32_t fill_pass_cap;        /* captured schedule */
+    int32_t depth_cap;
+    int32_t sweep_split_level;    /* levels from here on run in one block */
+    int32_t sweep_block;          /* threads per block of the level launches */
+    int32_t hillslope_iteration_cap;
+    int32_t last_fill_passes;     /* of the last eager step */
+    int32_t last_max_depth;
+    int32_t last_hillslope_iterations;
+    double tuned_sweep_ms;        /* autotuner: best stream-power sweep time */
+    double untuned_sweep_ms;      /* ... and one launch per level */
+} lsdtt_gpu_ensemble_info;
+
+int lsdtt_gpu_ensemble_get_info(const lsdtt_gpu_ensemble* ens, lsdtt_gpu_ensemble_info* info);
+/* The next captured step uses these fill-pass and PCG-iteration counts (0:
+ * the recorded count plus margin) instead of the tuned ones, once; a
+ * replay that outgrows them is undone and rerun like any other. */
+int lsdtt_gpu_ensemble_override_schedule(lsdtt_gpu_ensemble* ens, int32_t fill_pass_cap,
+                                         int32_t hillslope_iteration_cap);
+
 /* ---- whole routing pass with host buffers ---------------------------------
  * fill_pits(z, min_slope, bc) then lsdtt_flowinfo on the filled surface, then
  * the results copied back: filled elevations, int64 receivers, topological

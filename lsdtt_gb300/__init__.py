@@ -296,6 +296,24 @@ class LemStats(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
 
 
+class Member(ctypes.Structure):
+    _fields_ = [("grid", Grid), ("options", LemOptions)]
+
+
+class EnsembleInfo(ctypes.Structure):
+    _fields_ = [("packed_cells", ctypes.c_int64), ("member_cells", ctypes.c_int64),
+                ("graph_enabled", ctypes.c_int32), ("graph_captures", ctypes.c_int32),
+                ("graph_replays", ctypes.c_int32), ("eager_steps", ctypes.c_int32),
+                ("fill_pass_cap", ctypes.c_int32), ("depth_cap", ctypes.c_int32),
+                ("sweep_split_level", ctypes.c_int32), ("sweep_block", ctypes.c_int32),
+                ("hillslope_iteration_cap", ctypes.c_int32), ("last_fill_passes", ctypes.c_int32),
+                ("last_max_depth", ctypes.c_int32), ("last_hillslope_iterations", ctypes.c_int32),
+                ("tuned_sweep_ms", ctypes.c_double), ("untuned_sweep_ms", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 def _bind_more():
     L = lib()
     vp, i32, f32, f64 = ctypes.c_void_p, ctypes.c_int32, ctypes.c_float, ctypes.c_double
@@ -305,6 +323,14 @@ def _bind_more():
         "lsdtt_gpu_lem_create": [ctypes.POINTER(Grid), vp, ctypes.POINTER(LemOptions), ctypes.POINTER(vp), vp],
         "lsdtt_gpu_lem_destroy": [vp],
         "lsdtt_gpu_lem_step": [vp, vp, ctypes.POINTER(LemStats), vp],
+        "lsdtt_gpu_ensemble_create": [ctypes.POINTER(Member), i32, i32, ctypes.POINTER(vp), vp],
+        "lsdtt_gpu_ensemble_destroy": [vp],
+        "lsdtt_gpu_ensemble_offsets": [vp, vp],
+        "lsdtt_gpu_ensemble_set_member": [vp, i32, vp, vp, vp],
+        "lsdtt_gpu_ensemble_get_member": [vp, i32, vp, vp],
+        "lsdtt_gpu_ensemble_step": [vp, i32, ctypes.POINTER(LemStats), vp],
+        "lsdtt_gpu_ensemble_get_info": [vp, ctypes.POINTER(EnsembleInfo)],
+        "lsdtt_gpu_ensemble_override_schedule": [vp, i32, i32],
     }.items():
         fn = getattr(L, name)
         fn.argtypes = args
@@ -381,6 +407,87 @@ class LandscapeModel:
     def close(self):
         if getattr(self, "_h", None):
             lib().lsdtt_gpu_lem_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Ensemble:
+    """A batched ensemble of independent LEM runs (lsdtt_gpu_ensemble_*):
+    every member advances exactly as LandscapeModel.step would advance it
+    alone, all members in one launch per stage, one CUDA graph per step.
+
+    members: sequence of dicts with z, mask (optional), cell_size,
+    boundary_conditions and any LandscapeModel option."""
+
+    _DEFAULTS = dict(timestep=100.0, erodibility=1e-3, m_exponent=0.45, n_exponent=1.0, uplift_rate=1e-4,
+                     hillslope_diffusivity=1e-3, slope_clamp=1e-5, baselevel_fall_rate=0.0, fill_min_slope=0.0,
+                     enable_hillslope=True, divide_area_by_dx=True, hillslope_rel_tol=1e-8, hillslope_max_iter=2000)
+
+    def __init__(self, members, use_graph=True, stream=None):
+        torch = _torch()
+        L = _bind_more()
+        arr = (Member * len(members))()
+        self.shapes = []
+        for k, spec in enumerate(members):
+            spec = dict(spec)
+            z = np.asarray(spec.pop("z"), np.float32)
+            spec.pop("mask", None)
+            cell = spec.pop("cell_size")
+            bc = spec.pop("boundary_conditions", "oooo")
+            o = dict(self._DEFAULTS)
+            unknown = set(spec) - set(o)
+            if unknown:
+                raise TypeError(f"unknown member options {sorted(unknown)}")
+            o.update(spec)
+            arr[k].grid = make_grid(z.shape[0], z.shape[1], cell, bc)
+            arr[k].options = LemOptions(o["timestep"], o["erodibility"], o["m_exponent"], o["n_exponent"],
+                                        o["uplift_rate"], o["hillslope_diffusivity"], o["slope_clamp"],
+                                        o["baselevel_fall_rate"], o["fill_min_slope"], int(o["enable_hillslope"]),
+                                        int(o["divide_area_by_dx"]), o["hillslope_rel_tol"], o["hillslope_max_iter"])
+            self.shapes.append(z.shape)
+        h = ctypes.c_void_p()
+        _check(L.lsdtt_gpu_ensemble_create(arr, len(members), int(use_graph), ctypes.byref(h), _stream(stream)))
+        self._h = h
+        self.n_members = len(members)
+        for k, spec in enumerate(members):
+            zt = _dev(spec["z"], torch.float32)
+            m = spec.get("mask")
+            mt = _dev(np.ones(zt.shape, np.uint8) if m is None else m, torch.uint8)
+            _check(L.lsdtt_gpu_ensemble_set_member(self._h, k, ctypes.c_void_p(zt.data_ptr()),
+                                                   ctypes.c_void_p(mt.data_ptr()), _stream(stream)))
+
+    def step(self, n_steps=1, want_stats=False, stream=None):
+        stats = (LemStats * self.n_members)() if want_stats else None
+        _check(lib().lsdtt_gpu_ensemble_step(self._h, n_steps, stats, _stream(stream)))
+        return [s.as_dict() for s in stats] if want_stats else None
+
+    def get(self, k, stream=None):
+        torch = _torch()
+        out = torch.empty(self.shapes[k], dtype=torch.float32, device="cuda")
+        _check(lib().lsdtt_gpu_ensemble_get_member(self._h, k, ctypes.c_void_p(out.data_ptr()), _stream(stream)))
+        return out
+
+    def offsets(self):
+        off = np.empty(self.n_members + 1, np.int64)
+        _check(lib().lsdtt_gpu_ensemble_offsets(self._h, off.ctypes.data))
+        return off
+
+    def override_schedule(self, fill_pass_cap=0, hillslope_iteration_cap=0):
+        _check(lib().lsdtt_gpu_ensemble_override_schedule(self._h, fill_pass_cap, hillslope_iteration_cap))
+
+    def info(self):
+        i = EnsembleInfo()
+        _check(lib().lsdtt_gpu_ensemble_get_info(self._h, ctypes.byref(i)))
+        return i.as_dict()
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().lsdtt_gpu_ensemble_destroy(self._h)
             self._h = None
 
     def __del__(self):

@@ -134,6 +134,7 @@ unsigned long long launches_lem();
 unsigned long long launches_stack();
 unsigned long long launches_stream_power();
 unsigned long long launches_unet();
+unsigned long long launches_ensemble();
 
 namespace
 {
@@ -169,7 +170,8 @@ extern "C" {
 unsigned long long lsdtt_gpu_launch_count(void)
 {
     return launches_abi() + launches_d8() + launches_fill() + launches_hillslope() + launches_lem() +
-           launches_stack() + launches_stream_power() + launches_unet();
+           launches_stack() + launches_stream_power() + launches_unet() +
+           launches_ensemble();
 }
 
 int lsdtt_gpu_profile_enable(int32_t on)

@@ -49,6 +49,47 @@ struct lsdtt_gpu_flow
 namespace lsdtt_gb300
 {
 
+// ---- packed ensembles ------------------------------------------------------
+// Ensemble members are stored back to back in one flat buffer: member k owns
+// cells [base, base + nr*nc) in its own row-major order, and every base is a
+// multiple of kPackAlign so that a 256-thread block never straddles two
+// members. Receivers, outlets and the stack use packed (global) indices.
+constexpr std::int64_t kPackAlign = 256;
+
+struct PackedMember
+{
+    std::int64_t base;
+    std::int32_t nr, nc;
+    double cell;
+    double nodata;
+    char bc[4];
+    std::int32_t tile_base;  // first 32x32 fill tile of this member
+    std::int32_t ntx, nty;   // fill tiles across, down
+};
+
+struct Packed
+{
+    const PackedMember* m;            // [n_members] (device)
+    const std::uint16_t* blk_member;  // [n / kPackAlign]: member of each aligned block
+    std::int64_t n;                   // packed length (multiple of kPackAlign)
+    std::int32_t n_members;
+};
+
+__host__ __device__ inline Grid member_grid(const PackedMember& M)
+{
+    Grid g{};
+    g.nr = M.nr;
+    g.nc = M.nc;
+    g.cell = M.cell;
+    g.nodata = M.nodata;
+    g.bc[0] = M.bc[0];
+    g.bc[1] = M.bc[1];
+    g.bc[2] = M.bc[2];
+    g.bc[3] = M.bc[3];
+    g.n = static_cast<std::int64_t>(M.nr) * M.nc;
+    return g;
+}
+
 // Thread-local error message shared by every entry point.
 void set_error(const std::string& msg);
 int fail(int status, const std::string& msg);
@@ -62,7 +103,9 @@ cudaError_t launch_donors_outlets(lsdtt_gpu_flow* f, cudaStream_t st);
 
 // stack.cu: Euler tour of the receiver forest, list ranking, s-vector,
 // contributing counts, depths, heights and the Kahn topological order.
-cudaError_t build_stack(lsdtt_gpu_flow* f, bool want_topo, cudaStream_t st);
+// With `packed`, f holds a packed ensemble (f->g.n = packed length, global
+// receivers) and the tour links are found member by member.
+cudaError_t build_stack(lsdtt_gpu_flow* f, bool want_topo, cudaStream_t st, const Packed* packed = nullptr);
 cudaError_t accumulate(lsdtt_gpu_flow* f, const double* w, double* out, cudaStream_t st, bool* exact_path);
 
 // unet.cu: the learned preconditioner's forward pass for the hillslope

@@ -1,0 +1,1320 @@
+// ensemble.cu -- batched LEM ensembles: many independent grids advanced
+// together, one launch per stage over the packed cells of every member.
+//
+// Layout. Member k owns packed cells [base_k, base_k + nr_k*nc_k) in its own
+// row-major order; bases are multiples of kPackAlign (256), so a 256-thread
+// block belongs to exactly one member and finds it in blk_member. Fill tiles
+// (32 x 32) are numbered member by member (tile_member). Receivers, outlets,
+// the Euler tour and the stream-power level order use packed indices, so the
+// members' receiver forests form one forest and the stack code runs on it
+// unchanged.
+//
+// Step (per member, the single-grid lsdtt_gpu_lem_step):
+//   fill (optional) -> D8 receivers -> outlets -> Euler-tour s-vector
+//   (contributing counts, depth) -> area = count*dx^2 -> stream power swept
+//   by depth level -> linear implicit hillslope by Jacobi-PCG, per-member
+//   scalars and convergence -> uplift and boundary restore -> statistics.
+// The per-cell arithmetic is the single-grid code's own (d8_cell.cuh,
+// fill_tile.cuh, sp_node.cuh, hs_stencil.cuh, lem_cell.cuh).
+//
+// Schedule. The loops whose trip counts depend on the data (fill passes,
+// depth levels, PCG iterations) are host-driven in an eager step, which
+// records their counts. The step is then captured as one CUDA graph with
+// those counts plus margin; every loop body is gated on the device (an
+// inactive fill tile, an empty level or a converged member returns at
+// once), and a loop that needs more than its captured count raises an
+// overflow flag. After a replay the host reads the flags with the
+// statistics; on overflow it restores the step's input surface (copied at
+// the start of the step), reruns the step eagerly and captures again.
+//
+// Autotuner. The stream-power sweep runs the large depth levels as one
+// launch each and the tail of small levels inside one block (levels-per-
+// block: the block walks level after level with a barrier between them).
+// The split level and the block size of the level launches are chosen by
+// timing the candidate schedules on the first eager step.
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "engine.cuh"
+#include "d8_cell.cuh"
+#include "fill_tile.cuh"
+#include "hs_stencil.cuh"
+#include "lem_cell.cuh"
+#include "sp_node.cuh"
+
+namespace lsdtt_gb300
+{
+namespace
+{
+
+// Per-member constants.
+struct EnsParams
+{
+    SpParams sp;
+    Hs hs;
+    float inv_card, inv_diag;
+    float fill_eps, L, Ld;
+    float udz, bl;
+    double dw;        // dx^2, the default accumulation weight
+    double rel_tol;   // hillslope PCG relative residual
+    int fill_on, per_ns, per_ew, hill_on, max_iter;
+};
+
+// Flags: [0] fill changed in the last pass, [1] fill overflow, [2] depth
+// overflow, [3] PCG overflow, [4] PCG not converged within max_iter,
+// [5] active PCG members (eager loop), [6] fill did not converge (eager).
+constexpr int kFlags = 8;
+
+__device__ __forceinline__ int member_of(const Packed& P, std::int64_t i)
+{
+    return P.blk_member[i / kPackAlign];
+}
+
+// ---- fill ----------------------------------------------------------------
+__global__ void ens_interior(Packed P, const EnsParams* __restrict__ prm, const float* __restrict__ z,
+                             const std::uint8_t* __restrict__ mask, int* __restrict__ nd)
+{
+    LSDTT_COUNT();
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    const int m = member_of(P, i);
+    const PackedMember& M = P.m[m];
+    const std::int64_t local = i - M.base;
+    if (local >= static_cast<std::int64_t>(M.nr) * M.nc || !prm[m].fill_on) return;
+    if (fill_interior_invalid(M.nr, M.nc, z + M.base, mask + M.base, M.nodata, local)) nd[m] = 1;
+}
+
+__global__ void ens_fill_init(Packed P, const EnsParams* __restrict__ prm, const float* __restrict__ z,
+                              const std::uint8_t* __restrict__ mask, const int* __restrict__ nd, float* __restrict__ F,
+                              std::uint8_t* __restrict__ kind)
+{
+    LSDTT_COUNT();
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    const int m = member_of(P, i);
+    const PackedMember& M = P.m[m];
+    const EnsParams& q = prm[m];
+    const std::int64_t local = i - M.base;
+    if (local >= static_cast<std::int64_t>(M.nr) * M.nc)
+    {
+        F[i] = 0.0f;
+        kind[i] = 0;
+        return;
+    }
+    if (!q.fill_on)
+    {
+        F[i] = z[i];
+        kind[i] = 0;
+        return;
+    }
+    fill_init_cell(M.nr, M.nc, q.per_ns, q.per_ew, z + M.base, mask + M.base, M.nodata, nd[m], F + M.base,
+                   kind + M.base, local);
+}
+
+__global__ void ens_dirty_init(std::int32_t T, const std::uint16_t* __restrict__ tile_member,
+                               const EnsParams* __restrict__ prm, std::uint8_t* __restrict__ d0,
+                               std::uint8_t* __restrict__ d1)
+{
+    LSDTT_COUNT();
+    const std::int32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= T) return;
+    const std::uint8_t v = prm[tile_member[t]].fill_on ? 1 : 0;
+    d0[t] = v;
+    d1[t] = v;
+}
+
+__global__ void __launch_bounds__(256) ens_fill_relax(Packed P, const EnsParams* __restrict__ prm,
+                                                      const std::uint16_t* __restrict__ tile_member,
+                                                      const float* __restrict__ z,
+                                                      const std::uint8_t* __restrict__ kind, float* __restrict__ F,
+                                                      int* __restrict__ changed,
+                                                      const std::uint8_t* __restrict__ din,
+                                                      std::uint8_t* __restrict__ dout)
+{
+    LSDTT_COUNT();
+    const int m = tile_member[blockIdx.x];
+    const PackedMember& M = P.m[m];
+    const EnsParams& q = prm[m];
+    const int local = static_cast<int>(blockIdx.x) - M.tile_base;
+    fill_relax_tile(M.nr, M.nc, q.per_ns, q.per_ew, q.L, q.Ld, q.fill_eps, z + M.base, kind + M.base, F + M.base,
+                    changed, din + M.tile_base, dout + M.tile_base, local % M.ntx, local / M.ntx, M.ntx, M.nty);
+}
+
+__global__ void ens_flag_copy(const int* __restrict__ src, int* __restrict__ dst)
+{
+    LSDTT_COUNT();
+    if (*src) *dst = 1;
+}
+
+// ---- D8, outlets, area -----------------------------------------------------
+__global__ void __launch_bounds__(256) ens_receivers(Packed P, const EnsParams* __restrict__ prm,
+                                                     const float* __restrict__ zf,
+                                                     const std::uint8_t* __restrict__ mask,
+                                                     std::int64_t* __restrict__ receiver,
+                                                     std::uint8_t* __restrict__ dir,
+                                                     unsigned long long* __restrict__ err)
+{
+    LSDTT_COUNT();
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    const int m = member_of(P, i);
+    const PackedMember& M = P.m[m];
+    const std::int64_t local = i - M.base;
+    if (local >= static_cast<std::int64_t>(M.nr) * M.nc)
+    {
+        receiver[i] = kNodataReceiver;
+        dir[i] = kNoDir;
+        return;
+    }
+    const Grid g = member_grid(M);
+    const EnsParams& q = prm[m];
+    // The LEM's engine: interior nodata drains, pits are outlets.
+    d8_receiver_cell(g, zf + M.base, mask + M.base, nullptr, 1, 1, q.inv_card, q.inv_diag, receiver + M.base,
+                     dir + M.base, err, static_cast<int>(local / M.nc), static_cast<int>(local % M.nc), M.base);
+    const std::int64_t r = receiver[i];
+    if (r >= 0) receiver[i] = r + M.base;
+}
+
+__global__ void ens_outlet_flag(std::int64_t n, const std::uint8_t* __restrict__ mask,
+                                const std::uint8_t* __restrict__ dir, std::uint8_t* __restrict__ flag)
+{
+    LSDTT_COUNT();
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < n) flag[i] = (mask[i] && dir[i] == kNoDir) ? 1 : 0;
+}
+
+__global__ void ens_scatter(const std::uint8_t* __restrict__ flag, const std::int64_t* __restrict__ pos,
+                            std::int64_t n, std::int64_t* __restrict__ out)
+{
+    LSDTT_COUNT();
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < n && flag[i]) out[pos[i]] = i;
+}
+
+// Contributing area = count * dx^2: exact when n_valid * m < 2^53 for dx^2 =
+// m * 2^e (checked per member on the host), which is the reference's
+// accumulate() total in any order (stack.cu, accumulate).
+__global__ void ens_area(Packed P, const EnsParams* __restrict__ prm, const std::uint8_t* __restrict__ mask,
+                         const std::uint64_t* __restrict__ size, double* __restrict__ area)
+{
+    LSDTT_COUNT();
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    area[i] = mask[i] ? static_cast<double>(size[i]) * prm[member_of(P, i)].dw : 0.0;
+}
+
+// ---- depth levels and the stream-power sweep -------------------------------
+__global__ void ens_depth_hist(std::int64_t n, const std::uint8_t* __restrict__ mask,
+                               const std::int32_t* __restrict__ depth, std::uint32_t cap,
+                               std::uint32_t* __restrict__ count, std::uint32_t* __restrict__ maxd,
+                               int* __restrict__ overflow)
+{
+    LSDTT_COUNT();
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n || !mask[i]) return;
+    const std::int32_t d = depth[i];
+    if (d < 0) return;
+    if (static_cast<std::uint32_t>(d) >= cap)
+    {
+        *overflow = 1;
+        return;
+    }
+    atomicAdd(&count[d], 1u);
+    atomicMax(maxd, static_cast<std::uint32_t>(d));
+}
+
+__global__ void ens_depth_scatter(std::int64_t n, const std::uint8_t* __restrict__ mask,
+                                  const std::int32_t* __restrict__ depth, std::uint32_t cap,
+                                  const std::uint32_t* __restrict__ start, std::uint32_t* __restrict__ fillc,
+                                  std::uint32_t* __restrict__ order)
+{
+    LSDTT_COUNT();
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n || !mask[i]) return;
+    const std::int32_t d = depth[i];
+    if (d < 0 || static_cast<std::uint32_t>(d) >= cap) return;
+    order[start[d] + atomicAdd(&fillc[d], 1u)] = static_cast<std::uint32_t>(i);
+}
+
+__global__ void ens_copy(const float* __restrict__ a, float* __restrict__ b, std::int64_t n)
+{
+    LSDTT_COUNT();
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < n) b[i] = a[i];
+}
+
+struct SweepArgs
+{
+    Packed P;
+    const EnsParams* prm;
+    const std::uint32_t* order;
+    const std::uint32_t* start;   // level offsets, [cap + 1]
+    const std::uint32_t* maxd;    // deepest level present
+    const std::int64_t* receiver;
+    const std::uint8_t* dir;
+    const double* area;
+    const float* z_old;
+    float* z;
+};
+
+__device__ __forceinline__ void sweep_node(const SweepArgs& A, std::uint32_t flat)
+{
+    sp_node(A.prm[member_of(A.P, flat)].sp, A.P.n, flat, A.receiver, A.dir, A.area, A.z_old, nullptr, A.z);
+}
+
+// One depth level (offsets read on the device; grid-stride over the level).
+__global__ void ens_sp_level(SweepArgs A, int k)
+{
+    LSDTT_COUNT();
+    const std::uint32_t lo = A.start[k], hi = A.start[k + 1];
+    for (std::uint32_t j = lo + blockIdx.x * blockDim.x + threadIdx.x; j < hi; j += gridDim.x * blockDim.x)
+        sweep_node(A, A.order[j]);
+}
+
+// Levels k0 .. maxd in one block: a barrier between levels orders each
+// level's writes before the next level's reads.
+__global__ void __launch_bounds__(1024) ens_sp_tail(SweepArgs A, int k0)
+{
+    LSDTT_COUNT();
+    const int kmax = static_cast<int>(*A.maxd);
+    for (int k = k0; k <= kmax; ++k)
+    {
+        const std::uint32_t lo = A.start[k], hi = A.start[k + 1];
+        for (std::uint32_t j = lo + threadIdx.x; j < hi; j += blockDim.x) sweep_node(A, A.order[j]);
+        __syncthreads();
+    }
+}
+
+// ---- hillslope: Jacobi-PCG with per-member scalars -----------------------
+// Reduction slots: slot s (s = iteration + 1; slot 0 holds r.z of the start)
+// has 4 doubles per member: [0] p.Ap, [1] r.z, [2] r.r.
+constexpr int kHsSlot = 4;
+
+__device__ __forceinline__ void warp_add(double* dst, double v)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0 && v != 0.0) atomicAdd(dst, v);
+}
+
+// hs_setup (hillslope.cu) for every member at once: DOF flags, Jacobi
+// inverse diagonal, b = -F of the linear law at z = z^n; hs_bb[m] = ||b||^2.
+__global__ void ens_hs_setup(Packed P, const EnsParams* __restrict__ prm, const std::uint8_t* __restrict__ mask,
+                             const float* __restrict__ z, std::uint8_t* __restrict__ dof, float* __restrict__ inv_diag,
+                             float* __restrict__ b, double* __restrict__ hs_bb)
+{
+    LSDTT_COUNT();
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int m = member_of(P, i < P.n ? i : P.n - 1);
+    const PackedMember& M = P.m[m];
+    const EnsParams& q = prm[m];
+    const Hs& H = q.hs;
+    double bb = 0.0;
+    if (i < P.n)
+    {
+        const std::int64_t local = i - M.base;
+        bool is_dof = false;
+        if (local < static_cast<std::int64_t>(M.nr) * M.nc && q.hill_on)
+        {
+            const int r = static_cast<int>(local / M.nc), c = static_cast<int>(local % M.nc);
+            const std::uint8_t* mk = mask + M.base;
+            is_dof = mk[local] && !hs_dirichlet_edge(H, r, c);
+            if (is_dof)
+            {
+                const float* zm = z + M.base;
+                const double zp = zm[local];
+                double flux = 0.0;
+                int nf = 0;
+#pragma unroll
+                for (int f = 0; f < 4; ++f)
+                {
+                    const std::int64_t j = hs_nb(H, mk, r, c, kDr[f], kDc[f]);
+                    flux += static_cast<double>(zm[j]) - zp;
+                    nf += (j != local) ? 1 : 0;
+                }
+                double F = -H.U - H.DA * flux;
+                F += H.inv_dt * (zp - static_cast<double>(zm[local]));
+                b[i] = static_cast<float>(-F);
+                inv_diag[i] = static_cast<float>(1.0 / (H.inv_dt + H.DA * nf));
+                bb = F * F;
+            }
+        }
+        dof[i] = is_dof ? 1 : 0;
+        if (!is_dof)
+        {
+            b[i] = 0.0f;
+            inv_diag[i] = 0.0f;
+        }
+    }
+    warp_add(&hs_bb[m], bb);
+}
+
+// x = 0, r = b, p = M^-1 r; slot 0 [1] = r.z
+__global__ void ens_hs_init(Packed P, const float* __restrict__ b, const float* __restrict__ inv_diag,
+                            float* __restrict__ x, float* __restrict__ r, float* __restrict__ p,
+                            double* __restrict__ slot0)
+{
+    LSDTT_COUNT();
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int m = member_of(P, i < P.n ? i : P.n - 1);
+    double rz = 0.0;
+    if (i < P.n)
+    {
+        const float ri = b[i];
+        const float zi = ri * inv_diag[i];
+        x[i] = 0.0f;
+        r[i] = ri;
+        p[i] = zi;
+        rz = static_cast<double>(ri) * zi;
+    }
+    warp_add(&slot0[m * kHsSlot + 1], rz);
+}
+
+// done[m] = no hillslope or nothing to solve; iters[m] = 0
+__global__ void ens_hs_start(int M, const EnsParams* __restrict__ prm, const double* __restrict__ hs_bb,
+                             int* __restrict__ done, int* __restrict__ iters)
+{
+    LSDTT_COUNT();
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= M) return;
+    done[m] = (!prm[m].hill_on || hs_bb[m] == 0.0) ? 1 : 0;
+    iters[m] = 0;
+}
+
+__global__ void ens_hs_apply(Packed P, const EnsParams* __restrict__ prm, const std::uint8_t* __restrict__ mask,
+                             const std::uint8_t* __restrict__ dof, const int* __restrict__ done,
+                             const float* __restrict__ p, float* __restrict__ Ap, double* __restrict__ cur)
+{
+    LSDTT_COUNT();
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int m = member_of(P, i < P.n ? i : P.n - 1);
+    if (done[m]) return;
+    const PackedMember& M = P.m[m];
+    const Hs& H = prm[m].hs;
+    double pap = 0.0;
+    if (i < P.n)
+    {
+        float v = 0.0f;
+        if (dof[i])
+        {
+            const std::int64_t local = i - M.base;
+            const int r = static_cast<int>(local / M.nc), c = static_cast<int>(local % M.nc);
+            const std::uint8_t* mk = mask + M.base;
+            const std::uint8_t* dm = dof + M.base;
+            const float* pm = p + M.base;
+            const float pi = p[i];
+            float s = 0.0f;
+            int nf = 0;
+#pragma unroll
+            for (int f = 0; f < 4; ++f)
+            {
+                const std::int64_t j = hs_nb(H, mk, r, c, kDr[f], kDc[f]);
+                if (j == local) continue;
+                ++nf;
+                if (dm[j]) s += pm[j];
+            }
+            v = static_cast<float>((H.inv_dt + H.DA * nf) * pi - H.DA * s);
+            pap = static_cast<double>(pi) * v;
+        }
+        Ap[i] = v;
+    }
+    warp_add(&cur[m * kHsSlot + 0], pap);
+}
+
+__global__ void ens_hs_update(Packed P, const int* __restrict__ done, const double* __restrict__ prev,
+                              const float* __restrict__ inv_diag, const float* __restrict__ p,
+                              const float* __restrict__ Ap, float* __restrict__ x, float* __restrict__ r,
+                              float* __restrict__ zz, double* __restrict__ cur)
+{
+    LSDTT_COUNT();
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int m = member_of(P, i < P.n ? i : P.n - 1);
+    if (done[m]) return;
+    const double pap = cur[m * kHsSlot + 0];
+    const float alpha = (pap > 0.0) ? static_cast<float>(prev[m * kHsSlot + 1] / pap) : 0.0f;
+    double rz = 0.0, rr = 0.0;
+    if (i < P.n)
+    {
+        x[i] += alpha * p[i];
+        const float ri = r[i] - alpha * Ap[i];
+        r[i] = ri;
+        const float zi = ri * inv_diag[i];
+        zz[i] = zi;
+        rz = static_cast<double>(ri) * zi;
+        rr = static_cast<double>(ri) * ri;
+    }
+    warp_add(&cur[m * kHsSlot + 1], rz);
+    warp_add(&cur[m * kHsSlot + 2], rr);
+}
+
+__global__ void ens_hs_direction(Packed P, const int* __restrict__ done, const double* __restrict__ prev,
+                                 const double* __restrict__ cur, const float* __restrict__ zz, float* __restrict__ p)
+{
+    LSDTT_COUNT();
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    const int m = member_of(P, i);
+    if (done[m]) return;
+    const double ro = prev[m * kHsSlot + 1];
+    const float beta = (ro > 0.0) ? static_cast<float>(cur[m * kHsSlot + 1] / ro) : 0.0f;
+    p[i] = zz[i] + beta * p[i];
+}
+
+// After iteration `it` (0-based, it + 1 a multiple of 4 or the last one):
+// the single-grid convergence test per member. flags[5] counts the members
+// still iterating; flags[4] marks a member that reached max_iter.
+__global__ void ens_hs_check(int M, const EnsParams* __restrict__ prm, int it, const double* __restrict__ cur,
+                             const double* __restrict__ hs_bb, int* __restrict__ done, int* __restrict__ iters,
+                             int* __restrict__ flags)
+{
+    LSDTT_COUNT();
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= M || done[m]) return;
+    const EnsParams& q = prm[m];
+    const double rel = sqrt(cur[m * kHsSlot + 2]) / sqrt(hs_bb[m]);
+    iters[m] = it + 1;
+    if (rel <= q.rel_tol)
+        done[m] = 1;
+    else if (it + 1 >= q.max_iter)
+    {
+        done[m] = 1;
+        flags[4] = 1;
+    }
+    else
+        atomicAdd(&flags[5], 1);
+}
+
+// After the captured iterations: a member still iterating overflows.
+__global__ void ens_hs_overflow(int M, const int* __restrict__ done, int* __restrict__ flags)
+{
+    LSDTT_COUNT();
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m < M && !done[m]) flags[3] = 1;
+}
+
+__global__ void ens_hs_finish(std::int64_t n, const std::uint8_t* __restrict__ dof, const float* __restrict__ zsp,
+                              const float* __restrict__ x, float* __restrict__ out)
+{
+    LSDTT_COUNT();
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    out[i] = dof[i] ? static_cast<float>(static_cast<double>(zsp[i]) + static_cast<double>(x[i])) : zsp[i];
+}
+
+// ---- uplift, boundary restore, statistics ----------------------------------
+__global__ void ens_boundary_flag(Packed P, const std::uint8_t* __restrict__ mask, std::uint8_t* __restrict__ flag)
+{
+    LSDTT_COUNT();
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    const PackedMember& M = P.m[member_of(P, i)];
+    const std::int64_t local = i - M.base;
+    flag[i] = (local < static_cast<std::int64_t>(M.nr) * M.nc &&
+               boundary_flat_cell(M.nr, M.nc, M.bc, mask + M.base, local))
+                  ? 1
+                  : 0;
+}
+
+__global__ void ens_uplift(Packed P, const EnsParams* __restrict__ prm, const std::uint8_t* __restrict__ mask,
+                           const std::uint8_t* __restrict__ bflag, const float* __restrict__ z_before,
+                           float* __restrict__ z)
+{
+    LSDTT_COUNT();
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    const EnsParams& q = prm[member_of(P, i)];
+    float v = z[i];
+    if (mask[i]) v = __fadd_rn(v, q.udz);
+    if (bflag[i]) v = __fsub_rn(z_before[i], q.bl);
+    z[i] = v;
+}
+
+__device__ __forceinline__ void warp_max_mapped(double* dst, double v)
+{
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+    if ((threadIdx.x & 31) == 0)
+    {
+        unsigned long long u = __double_as_longlong(v);
+        u = (u & 0x8000000000000000ull) ? ~u : (u | 0x8000000000000000ull);
+        atomicMax(reinterpret_cast<unsigned long long*>(dst), u);
+    }
+}
+
+// lem_stats (lem.cu) per member: [0] sum before, [1] sum after, [2] erosion
+// sum, [3] valid count, [4..7] mapped maxima (before, after, |dz|, erosion).
+__global__ void ens_stats(Packed P, const EnsParams* __restrict__ prm, const std::uint8_t* __restrict__ mask,
+                          const float* __restrict__ zb, const float* __restrict__ za, double* __restrict__ acc)
+{
+    LSDTT_COUNT();
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int m = member_of(P, i < P.n ? i : P.n - 1);
+    double sb = 0, sa = 0, mb = -1e30, ma = -1e30, ml = 0, se = 0, me = 0, nv = 0;
+    if (i < P.n && mask[i])
+    {
+        const double b = zb[i], a = za[i];
+        sb = b;
+        sa = a;
+        mb = b;
+        ma = a;
+        ml = fabs(a - b);
+        const double ero = b - (a - static_cast<double>(prm[m].udz));
+        if (ero > 0.0) { se = ero; me = ero; }
+        nv = 1;
+    }
+    double* A = acc + m * 8;
+    warp_add(&A[0], sb);
+    warp_add(&A[1], sa);
+    warp_add(&A[2], se);
+    warp_add(&A[3], nv);
+    warp_max_mapped(&A[4], mb);
+    warp_max_mapped(&A[5], ma);
+    warp_max_mapped(&A[6], ml);
+    warp_max_mapped(&A[7], me);
+}
+
+double unmap_max_host(double stored)
+{
+    unsigned long long u;
+    std::memcpy(&u, &stored, sizeof(u));
+    u = (u & 0x8000000000000000ull) ? (u & ~0x8000000000000000ull) : ~u;
+    double v;
+    std::memcpy(&v, &u, sizeof(v));
+    return v;
+}
+
+bool exact_area(double dw, std::int64_t nv)
+{
+    if (!(dw > 0.0) || !std::isfinite(dw)) return false;
+    int e = 0;
+    const double fr = std::frexp(dw, &e);
+    std::uint64_t m = static_cast<std::uint64_t>(std::ldexp(fr, 53));
+    while (m && !(m & 1)) m >>= 1;
+    return static_cast<long double>(m) * static_cast<long double>(nv) < 9007199254740992.0L;
+}
+
+}  // namespace
+}  // namespace lsdtt_gb300
+
+using namespace lsdtt_gb300;
+
+struct lsdtt_gpu_ensemble
+{
+    int M = 0;
+    std::vector<lsdtt_gpu_member> members;
+    std::vector<PackedMember> pm;
+    std::vector<EnsParams> prm_h;
+    std::int64_t N = 0, member_cells = 0;
+    std::int32_t T = 0;
+    PackedMember* d_pm = nullptr;
+    EnsParams* d_prm = nullptr;
+    std::uint16_t* blk_member = nullptr;
+    std::uint16_t* tile_member = nullptr;
+    Packed P{};
+    // state and stage buffers
+    float *z = nullptr, *zf = nullptr, *zsp = nullptr, *zpre = nullptr;
+    std::uint8_t *mask = nullptr, *kind = nullptr, *bflag = nullptr, *dirty = nullptr, *oflag = nullptr;
+    std::int64_t* pos = nullptr;
+    int* nd = nullptr;
+    lsdtt_gpu_flow* f = nullptr;
+    double* area = nullptr;
+    std::uint32_t *order = nullptr, *lstart = nullptr, *lcount = nullptr, *lfill = nullptr, *maxd = nullptr;
+    std::uint8_t* dof = nullptr;
+    float *invd = nullptr, *b = nullptr, *x = nullptr, *r = nullptr, *p = nullptr, *zz = nullptr, *Ap = nullptr;
+    double *hs_bb = nullptr, *hs_acc = nullptr;
+    int *done = nullptr, *iters = nullptr;
+    double* stats_acc = nullptr;
+    int* flags = nullptr;
+    // pinned host mirrors
+    double* h_stats = nullptr;
+    int* h_flags = nullptr;
+    int* h_iters = nullptr;
+    std::uint32_t* h_maxd = nullptr;
+    unsigned long long* h_err = nullptr;
+    int max_iter_all = 1000;
+    int max_pass_all = 64;
+    // schedule
+    bool use_graph = true, captured = false, tuned = false;
+    int fill_cap = 0, depth_cap = 0, split = 1, sweep_block = 256, it_cap = 0;
+    std::vector<unsigned> level_blocks;  // grid of each captured level launch
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaStream_t own = nullptr;  // private stream: the legacy default stream cannot be captured
+    std::uint32_t tail = 0;      // tuned: levels of at most `tail` cells run in one block (0: none)
+    int ov_fill = 0, ov_it = 0;  // one-shot schedule override for the next capture
+    lsdtt_gpu_ensemble_info info{};
+    bool ready = false;  // every member set at least once
+    std::vector<char> member_set;
+};
+
+namespace
+{
+
+struct StepRecord
+{
+    int fill_passes = 0;
+    int max_depth = 0;
+    int pcg_iters = 0;
+    std::vector<std::uint32_t> level_size;  // [max_depth + 1]
+};
+
+void free_ensemble(lsdtt_gpu_ensemble* E)
+{
+    if (E->exec) cudaGraphExecDestroy(E->exec);
+    if (E->graph) cudaGraphDestroy(E->graph);
+    void* bufs[] = {E->d_pm, E->d_prm, E->blk_member, E->tile_member, E->z, E->zf, E->zsp, E->zpre, E->kind, E->bflag, E->dirty, E->oflag, E->pos, E->nd, E->area, E->order, E->lstart, E->lcount,
+                    E->lfill, E->maxd, E->dof, E->invd, E->b, E->x, E->r, E->p, E->zz, E->Ap, E->hs_bb, E->hs_acc,
+                    E->done, E->iters, E->stats_acc, E->flags};
+    for (void* q : bufs) cudaFree(q);
+    void* hb[] = {E->h_stats, E->h_flags, E->h_iters, E->h_maxd, E->h_err};
+    for (void* q : hb) cudaFreeHost(q);
+    if (E->f) lsdtt_gpu_flow_destroy(E->f);
+    if (E->own) cudaStreamDestroy(E->own);
+    delete E;
+}
+
+// Sweep launches for levels 1 .. split-1 (one launch each), then the tail.
+void enqueue_sweep(lsdtt_gpu_ensemble* E, const SweepArgs& A, int split, int block,
+                   const std::vector<unsigned>& blocks, cudaStream_t st)
+{
+    for (int k = 1; k < split; ++k)
+        ens_sp_level<<<blocks[static_cast<std::size_t>(k)], block, 0, st>>>(A, k);
+    ens_sp_tail<<<1, 1024, 0, st>>>(A, split);
+    (void)E;
+}
+
+// Blocks of each level launch for a level-size profile.
+std::vector<unsigned> level_grid(const std::vector<std::uint32_t>& size, int split, int block, double margin)
+{
+    std::vector<unsigned> g(static_cast<std::size_t>(std::max(split, 1)), 1u);
+    for (int k = 1; k < split; ++k)
+    {
+        const double s = k < static_cast<int>(size.size()) ? size[static_cast<std::size_t>(k)] : 0.0;
+        const double want = std::ceil(s * margin / block) + 1.0;
+        g[static_cast<std::size_t>(k)] = static_cast<unsigned>(std::min(want, 152.0 * 16.0));
+    }
+    return g;
+}
+
+// First level from which every level holds at most `tail` cells.
+int split_for(const std::vector<std::uint32_t>& size, std::uint32_t tail)
+{
+    int k = static_cast<int>(size.size());
+    while (k > 1 && size[static_cast<std::size_t>(k - 1)] <= tail) --k;
+    return std::max(k, 1);
+}
+
+// One step. eager: host-driven loops (records the schedule in *rec and
+// autotunes the sweep on the first call); otherwise the captured schedule.
+cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRecord* rec)
+{
+    const std::int64_t N = E->N;
+    const unsigned nb = grid_blocks(N, 256);
+    const int M = E->M;
+    const unsigned mb = static_cast<unsigned>((M + 127) / 128);
+    cudaError_t e = cudaSuccess;
+    cudaMemcpyAsync(E->zpre, E->z, sizeof(float) * N, cudaMemcpyDeviceToDevice, st);
+    cudaMemsetAsync(E->flags, 0, sizeof(int) * kFlags, st);
+    // 0. fill
+    cudaMemsetAsync(E->nd, 0, sizeof(int) * M, st);
+    ens_interior<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->z, E->mask, E->nd);
+    ens_fill_init<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->z, E->mask, E->nd, E->zf, E->kind);
+    ens_dirty_init<<<grid_blocks(E->T, 256), 256, 0, st>>>(E->T, E->tile_member, E->d_prm, E->dirty,
+                                                           E->dirty + E->T);
+    const dim3 fblock(32, 8);
+    auto relax = [&](int pass) {
+        ens_fill_relax<<<E->T, fblock, 0, st>>>(E->P, E->d_prm, E->tile_member, E->z, E->kind, E->zf, E->flags,
+                                                E->dirty + (pass & 1) * E->T, E->dirty + ((pass + 1) & 1) * E->T);
+    };
+    int passes = 0;
+    if (eager)
+    {
+        for (;;)
+        {
+            cudaMemsetAsync(E->flags, 0, sizeof(int), st);
+            for (int k = 0; k < 4; ++k, ++passes) relax(passes);
+            cudaMemcpyAsync(E->h_flags, E->flags, sizeof(int), cudaMemcpyDeviceToHost, st);
+            e = cudaStreamSynchronize(st);
+            if (e != cudaSuccess) return e;
+            if (E->h_flags[0] == 0) break;
+            if (passes > E->max_pass_all) return cudaErrorLaunchTimeout;
+        }
+        rec->fill_passes = passes;
+    }
+    else
+    {
+        for (int k = 0; k < E->fill_cap; ++k)
+        {
+            if (k == E->fill_cap - 1) cudaMemsetAsync(E->flags, 0, sizeof(int), st);
+            relax(k);
+        }
+        ens_flag_copy<<<1, 1, 0, st>>>(E->flags, E->flags + 1);
+    }
+    // 1. D8 receivers, outlets, s-vector (contributing counts, depth)
+    lsdtt_gpu_flow* f = E->f;
+    cudaMemsetAsync(f->derr, 0, sizeof(unsigned long long) * 4, st);
+    ens_receivers<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->zf, E->mask, f->receiver, f->dir, f->derr);
+    ens_outlet_flag<<<nb, 256, 0, st>>>(N, E->mask, f->dir, E->oflag);
+    f->ws.used = 0;
+    e = exclusive_scan<std::uint8_t, std::int64_t>(E->oflag, N, E->pos, f->dscal + 1, f->ws, st);
+    if (e != cudaSuccess) return e;
+    ens_scatter<<<nb, 256, 0, st>>>(E->oflag, E->pos, N, f->outlets);
+    f->ws.used = 0;
+    e = build_stack(f, false, st, &E->P);
+    if (e != cudaSuccess) return e;
+    ens_area<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->mask, f->sv_size, E->area);
+    // 2. depth levels
+    const std::uint32_t cap = eager ? static_cast<std::uint32_t>(N + 1) : static_cast<std::uint32_t>(E->depth_cap);
+    cudaMemsetAsync(E->maxd, 0, sizeof(std::uint32_t), st);
+    cudaMemsetAsync(E->lcount, 0, sizeof(std::uint32_t) * (static_cast<std::size_t>(cap) + 2), st);
+    ens_depth_hist<<<nb, 256, 0, st>>>(N, E->mask, f->depth, cap, E->lcount, E->maxd, E->flags + 2);
+    std::uint32_t scan_len = cap + 1;
+    if (eager)
+    {
+        cudaMemcpyAsync(E->h_maxd, E->maxd, sizeof(std::uint32_t), cudaMemcpyDeviceToHost, st);
+        e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return e;
+        scan_len = *E->h_maxd + 2;
+    }
+    f->ws.used = 0;
+    e = exclusive_scan<std::uint32_t, std::uint32_t>(E->lcount, scan_len, E->lstart,
+                                                     static_cast<std::uint32_t*>(nullptr), f->ws, st);
+    if (e != cudaSuccess) return e;
+    cudaMemsetAsync(E->lfill, 0, sizeof(std::uint32_t) * scan_len, st);
+    ens_depth_scatter<<<nb, 256, 0, st>>>(N, E->mask, f->depth, cap, E->lstart, E->lfill, E->order);
+    // 3. stream power, swept by depth level
+    ens_copy<<<nb, 256, 0, st>>>(E->zf, E->zsp, N);
+    SweepArgs A{E->P, E->d_prm, E->order, E->lstart, E->maxd, f->receiver, f->dir, E->area, E->zf, E->zsp};
+    if (eager)
+    {
+        const std::uint32_t D = *E->h_maxd;
+        std::vector<std::uint32_t> start(static_cast<std::size_t>(D) + 2);
+        cudaMemcpyAsync(start.data(), E->lstart, sizeof(std::uint32_t) * (D + 2), cudaMemcpyDeviceToHost, st);
+        e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return e;
+        rec->max_depth = static_cast<int>(D);
+        rec->level_size.assign(static_cast<std::size_t>(D) + 1, 0u);
+        for (std::uint32_t k = 0; k <= D; ++k) rec->level_size[k] = start[k + 1] - start[k];
+        if (!E->tuned)
+        {
+            // Autotune the levels-per-block split and the level block size:
+            // time each candidate schedule on this step's levels.
+            const std::uint32_t tails[] = {0u, 256u, 1024u, 4096u, 16384u};
+            const int blocks[] = {128, 256, 512};
+            cudaEvent_t t0, t1;
+            cudaEventCreate(&t0);
+            cudaEventCreate(&t1);
+            double best = 1e30, one_per_level = 0.0;
+            std::uint32_t best_tail = 0;
+            int best_block = 256;
+            for (std::uint32_t tail : tails)
+                for (int blk : blocks)
+                {
+                    const int sp = tail == 0 ? static_cast<int>(D) + 1 : split_for(rec->level_size, tail);
+                    const auto g = level_grid(rec->level_size, sp, blk, 1.0);
+                    float ms_best = 1e30f;
+                    for (int rep = 0; rep < 2; ++rep)
+                    {
+                        ens_copy<<<nb, 256, 0, st>>>(E->zf, E->zsp, N);
+                        cudaEventRecord(t0, st);
+                        enqueue_sweep(E, A, sp, blk, g, st);
+                        cudaEventRecord(t1, st);
+                        e = cudaEventSynchronize(t1);
+                        if (e != cudaSuccess) break;
+                        float ms = 0.0f;
+                        cudaEventElapsedTime(&ms, t0, t1);
+                        ms_best = std::min(ms_best, ms);
+                    }
+                    if (e != cudaSuccess) break;
+                    if (tail == 0 && blk == 256) one_per_level = ms_best;
+                    if (ms_best < best)
+                    {
+                        best = ms_best;
+                        best_tail = tail;
+                        best_block = blk;
+                    }
+                }
+            cudaEventDestroy(t0);
+            cudaEventDestroy(t1);
+            if (e != cudaSuccess) return e;
+            // Keep the tail threshold, not the level index: the split is
+            // recomputed from each recorded profile.
+            E->tail = best_tail;
+            E->sweep_block = best_block;
+            E->info.tuned_sweep_ms = best;
+            E->info.untuned_sweep_ms = one_per_level;
+            E->tuned = true;
+            ens_copy<<<nb, 256, 0, st>>>(E->zf, E->zsp, N);
+        }
+        const int sp = E->tail == 0 ? static_cast<int>(D) + 1 : split_for(rec->level_size, E->tail);
+        E->split = sp;
+        enqueue_sweep(E, A, sp, E->sweep_block, level_grid(rec->level_size, sp, E->sweep_block, 1.0), st);
+    }
+    else
+        enqueue_sweep(E, A, E->split, E->sweep_block, E->level_blocks, st);
+    // 4. hillslope: Jacobi-PCG per member
+    const std::size_t slot_bytes = sizeof(double) * kHsSlot * M;
+    const int itmax = eager ? E->max_iter_all : E->it_cap;
+    cudaMemsetAsync(E->hs_bb, 0, sizeof(double) * M, st);
+    cudaMemsetAsync(E->hs_acc, 0, slot_bytes * (static_cast<std::size_t>(itmax) + 1), st);
+    ens_hs_setup<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->mask, E->zsp, E->dof, E->invd, E->b, E->hs_bb);
+    ens_hs_init<<<nb, 256, 0, st>>>(E->P, E->b, E->invd, E->x, E->r, E->p, E->hs_acc);
+    ens_hs_start<<<mb, 128, 0, st>>>(M, E->d_prm, E->hs_bb, E->done, E->iters);
+    int it = 0;
+    for (; it < itmax;)
+    {
+        const int batch = std::min(4, itmax - it);
+        for (int k = 0; k < batch; ++k, ++it)
+        {
+            const double* prev = E->hs_acc + static_cast<std::size_t>(kHsSlot) * M * it;
+            double* cur = E->hs_acc + static_cast<std::size_t>(kHsSlot) * M * (it + 1);
+            ens_hs_apply<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->mask, E->dof, E->done, E->p, E->Ap, cur);
+            ens_hs_update<<<nb, 256, 0, st>>>(E->P, E->done, prev, E->invd, E->p, E->Ap, E->x, E->r, E->zz, cur);
+            ens_hs_direction<<<nb, 256, 0, st>>>(E->P, E->done, prev, cur, E->zz, E->p);
+        }
+        if (eager) cudaMemsetAsync(E->flags + 5, 0, sizeof(int), st);
+        ens_hs_check<<<mb, 128, 0, st>>>(M, E->d_prm, it - 1,
+                                        E->hs_acc + static_cast<std::size_t>(kHsSlot) * M * it, E->hs_bb, E->done,
+                                        E->iters, E->flags);
+        if (eager)
+        {
+            cudaMemcpyAsync(E->h_flags + 5, E->flags + 5, sizeof(int), cudaMemcpyDeviceToHost, st);
+            e = cudaStreamSynchronize(st);
+            if (e != cudaSuccess) return e;
+            if (E->h_flags[5] == 0) break;
+        }
+    }
+    if (eager) rec->pcg_iters = it;
+    else ens_hs_overflow<<<mb, 128, 0, st>>>(M, E->done, E->flags);
+    ens_hs_finish<<<nb, 256, 0, st>>>(N, E->dof, E->zsp, E->x, E->z);
+    // 5. uplift + boundary restore, statistics, flags to the host
+    ens_uplift<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->mask, E->bflag, E->zf, E->z);
+    cudaMemsetAsync(E->stats_acc, 0, sizeof(double) * 8 * M, st);
+    ens_stats<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->mask, E->zf, E->z, E->stats_acc);
+    cudaMemcpyAsync(E->h_stats, E->stats_acc, sizeof(double) * 8 * M, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(E->h_flags, E->flags, sizeof(int) * kFlags, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(E->h_iters, E->iters, sizeof(int) * M, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(E->h_err, f->derr, sizeof(unsigned long long) * 4, cudaMemcpyDeviceToHost, st);
+    return cudaGetLastError();
+}
+
+// Capture one step with the schedule derived from the record.
+cudaError_t capture(lsdtt_gpu_ensemble* E, const StepRecord& rec, cudaStream_t st)
+{
+    if (E->exec) cudaGraphExecDestroy(E->exec);
+    if (E->graph) cudaGraphDestroy(E->graph);
+    E->exec = nullptr;
+    E->graph = nullptr;
+    E->fill_cap = std::max(8, ((rec.fill_passes + std::max(8, rec.fill_passes / 4)) + 3) / 4 * 4);
+    E->depth_cap = std::max(rec.max_depth * 2, rec.max_depth + 256) + 2;
+    E->depth_cap = static_cast<int>(std::min<std::int64_t>(E->depth_cap, E->N + 1));
+    E->it_cap = std::min(E->max_iter_all, std::max(8, (rec.pcg_iters + std::max(8, rec.pcg_iters / 2) + 3) / 4 * 4));
+    if (E->ov_fill > 0) E->fill_cap = E->ov_fill;
+    if (E->ov_it > 0) E->it_cap = E->ov_it;
+    E->ov_fill = E->ov_it = 0;
+    // levels of this profile above the tuned tail threshold get a launch each
+    E->split = E->tail == 0 ? rec.max_depth + 1 : split_for(rec.level_size, E->tail);
+    E->level_blocks = level_grid(rec.level_size, E->split, E->sweep_block, 1.5);
+    cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return e;
+    StepRecord dummy;
+    cudaError_t e_run = run_step(E, st, false, &dummy);
+    cudaGraph_t g = nullptr;
+    e = cudaStreamEndCapture(st, &g);
+    if (e_run != cudaSuccess) e = e_run;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&E->exec, g, 0);
+    if (e != cudaSuccess)
+    {
+        if (g) cudaGraphDestroy(g);
+        return e;
+    }
+    E->graph = g;
+    E->captured = true;
+    ++E->info.graph_captures;
+    return cudaSuccess;
+}
+
+void fill_stats(const lsdtt_gpu_ensemble* E, lsdtt_gpu_lem_stats* stats)
+{
+    for (int m = 0; m < E->M; ++m)
+    {
+        const double* A = E->h_stats + 8 * m;
+        const lsdtt_gpu_lem_options& o = E->members[static_cast<std::size_t>(m)].options;
+        const double nv = A[3];
+        const double inv_dt = 1.0 / static_cast<double>(o.timestep);
+        const double inv_n = nv > 0 ? 1.0 / nv : 0.0;
+        lsdtt_gpu_lem_stats& s = stats[m];
+        s.delta_max_elevation = static_cast<float>(std::fabs(unmap_max_host(A[5]) - unmap_max_host(A[4])));
+        s.delta_mean_elevation = static_cast<float>(std::fabs((A[1] - A[0]) * inv_n));
+        s.max_local_elevation_change = static_cast<float>(unmap_max_host(A[6]));
+        const double me = unmap_max_host(A[7]);
+        s.mean_erosion_rate = static_cast<float>(A[2] * inv_n * inv_dt);
+        s.max_erosion_rate = static_cast<float>((me > 0 ? me : 0.0) * inv_dt);
+        s.hillslope_iterations = E->h_iters[m];
+        s.p999_local_elevation_change = 0.0f;
+        s.reserved = 0;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int lsdtt_gpu_ensemble_create(const lsdtt_gpu_member* members, int32_t n_members, int32_t use_graph,
+                              lsdtt_gpu_ensemble** out, void* stream)
+{
+    const char* who = "lsdtt_gpu_ensemble_create";
+    if (!members || !out || n_members <= 0) return fail(LSDTT_GPU_EINVAL, std::string(who) + ": bad argument");
+    *out = nullptr;
+    if (n_members > 65535) return fail(LSDTT_GPU_EINVAL, std::string(who) + ": at most 65535 members");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        return fail(LSDTT_GPU_ENODEV, std::string(who) + ": no CUDA device");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    auto* E = new lsdtt_gpu_ensemble();
+    E->M = n_members;
+    E->use_graph = use_graph != 0;
+    E->members.assign(members, members + n_members);
+    E->member_set.assign(static_cast<std::size_t>(n_members), 0);
+    std::int64_t base = 0;
+    std::int32_t tiles = 0;
+    for (int k = 0; k < n_members; ++k)
+    {
+        const lsdtt_gpu_grid& g = members[k].grid;
+        const lsdtt_gpu_lem_options& o = members[k].options;
+        const std::string mk = std::string(who) + ": member " + std::to_string(k);
+        if (!(g.n_rows > 0 && g.n_cols > 0 && g.cell_size > 0.0) ||
+            static_cast<std::int64_t>(g.n_rows) * g.n_cols >= (std::int64_t(1) << 31))
+        {
+            free_ensemble(E);
+            return fail(LSDTT_GPU_EINVAL, mk + ": raster metadata is invalid");
+        }
+        if (!(o.timestep > 0.0f))
+        {
+            free_ensemble(E);
+            return fail(LSDTT_GPU_EINVAL, mk + ": timestep must be positive");
+        }
+        auto is_p = [&](int i) { return g.boundary_conditions[i] == 'p' || g.boundary_conditions[i] == 'P'; };
+        if (is_p(0) != is_p(2) || is_p(1) != is_p(3) || (is_p(0) && is_p(1)))
+        {
+            free_ensemble(E);
+            return fail(LSDTT_GPU_EINVAL, mk + ": periodic boundary flags must pair up and leave one axis open");
+        }
+        const std::int64_t n = static_cast<std::int64_t>(g.n_rows) * g.n_cols;
+        if (!exact_area(g.cell_size * g.cell_size, n))
+        {
+            free_ensemble(E);
+            return fail(LSDTT_GPU_EINVAL, mk + ": cell_size^2 * cells is not exact in double; the packed "
+                                               "accumulation needs the exact contributing-area path");
+        }
+        PackedMember P{};
+        P.base = base;
+        P.nr = g.n_rows;
+        P.nc = g.n_cols;
+        P.cell = g.cell_size;
+        P.nodata = g.no_data_value;
+        std::memcpy(P.bc, g.boundary_conditions, 4);
+        P.tile_base = tiles;
+        P.ntx = (g.n_cols + 31) / 32;
+        P.nty = (g.n_rows + 31) / 32;
+        tiles += P.ntx * P.nty;
+        base += (n + kPackAlign - 1) / kPackAlign * kPackAlign;
+        E->member_cells += n;
+        E->pm.push_back(P);
+        EnsParams q{};
+        q.sp.K = o.erodibility;
+        q.sp.m = o.m_exponent;
+        q.sp.n = o.n_exponent;
+        q.sp.dt = o.timestep;
+        q.sp.threshold = 0.0f;
+        q.sp.slope_clamp = o.slope_clamp;
+        q.sp.dx = static_cast<float>(g.cell_size);
+        q.sp.dx_diag = q.sp.dx * static_cast<float>(1.4142135623730950488);
+        q.sp.divide_by_dx = o.divide_area_by_dx;
+        q.sp.n_is_one = std::fabs(o.n_exponent - 1.0f) < 1e-6f ? 1 : 0;
+        q.hs.nr = g.n_rows;
+        q.hs.nc = g.n_cols;
+        q.hs.bn = g.boundary_conditions[0];
+        q.hs.be = g.boundary_conditions[1];
+        q.hs.bs = g.boundary_conditions[2];
+        q.hs.bw = g.boundary_conditions[3];
+        q.hs.DA = static_cast<double>(o.hillslope_diffusivity) / (g.cell_size * g.cell_size);
+        q.hs.inv_dt = 1.0 / static_cast<double>(o.timestep);
+        q.hs.U = 0.0;
+        q.inv_card = static_cast<float>(1.0 / g.cell_size);
+        q.inv_diag = static_cast<float>(1.0 / (g.cell_size * 1.4142135623730950488));
+        q.fill_on = o.fill_min_slope > 0.0f ? 1 : 0;
+        q.fill_eps = o.fill_min_slope > 0.0f ? o.fill_min_slope : 0.0f;
+        q.L = static_cast<float>(g.cell_size);
+        q.Ld = q.L * static_cast<float>(1.4142135623730950488);
+        q.per_ns = is_p(0);
+        q.per_ew = is_p(1);
+        q.udz = o.uplift_rate * o.timestep;
+        q.bl = o.baselevel_fall_rate * o.timestep;
+        q.dw = g.cell_size * g.cell_size;
+        q.hill_on = o.enable_hillslope ? 1 : 0;
+        q.rel_tol = o.hillslope_rel_tol > 0 ? o.hillslope_rel_tol : 1e-8;
+        q.max_iter = o.hillslope_max_iter > 0 ? o.hillslope_max_iter : 1000;
+        E->prm_h.push_back(q);
+        E->max_iter_all = std::max(E->max_iter_all, q.max_iter);
+        E->max_pass_all = std::max<int>(E->max_pass_all, 4 * (g.n_rows + g.n_cols) + 64);
+    }
+    E->N = base;
+    E->T = tiles;
+    const std::int64_t N = E->N;
+    if (2 * N >= (std::int64_t(1) << 32))
+    {
+        free_ensemble(E);
+        return fail(LSDTT_GPU_EINVAL, std::string(who) + ": the packed ensemble exceeds 2^31 cells");
+    }
+    std::vector<std::uint16_t> blk(static_cast<std::size_t>(N / kPackAlign));
+    std::vector<std::uint16_t> tm(static_cast<std::size_t>(tiles));
+    for (int k = 0; k < n_members; ++k)
+    {
+        const PackedMember& P = E->pm[static_cast<std::size_t>(k)];
+        const std::int64_t n = static_cast<std::int64_t>(P.nr) * P.nc;
+        const std::int64_t nblk = (n + kPackAlign - 1) / kPackAlign;
+        for (std::int64_t b = 0; b < nblk; ++b) blk[static_cast<std::size_t>(P.base / kPackAlign + b)] = k;
+        for (int t = 0; t < P.ntx * P.nty; ++t) tm[static_cast<std::size_t>(P.tile_base + t)] = k;
+    }
+    // The stack runs on the packed forest: one flow engine over N cells.
+    lsdtt_gpu_grid fg{};
+    fg.n_rows = 1;
+    fg.n_cols = static_cast<std::int32_t>(N);
+    fg.cell_size = 1.0;
+    fg.no_data_value = -9999.0;
+    std::memcpy(fg.boundary_conditions, "oooo", 4);
+    int s = lsdtt_gpu_flow_create(&fg, &E->f);
+    if (s != LSDTT_GPU_OK)
+    {
+        free_ensemble(E);
+        return s;
+    }
+    E->mask = E->f->mask;  // the stack reads the engine's mask
+    if (cudaStreamCreateWithFlags(&E->own, cudaStreamNonBlocking) != cudaSuccess)
+    {
+        free_ensemble(E);
+        return fail(LSDTT_GPU_ECUDA, std::string(who) + ": stream creation failed");
+    }
+    cudaError_t e = cudaSuccess;
+    auto alloc = [&](auto** p, std::size_t count) {
+        if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(p), sizeof(**p) * (count ? count : 1));
+    };
+    const std::size_t n = static_cast<std::size_t>(N);
+    alloc(&E->d_pm, static_cast<std::size_t>(n_members));
+    alloc(&E->d_prm, static_cast<std::size_t>(n_members));
+    alloc(&E->blk_member, blk.size());
+    alloc(&E->tile_member, tm.size());
+    alloc(&E->z, n);
+    alloc(&E->zf, n);
+    alloc(&E->zsp, n);
+    alloc(&E->zpre, n);
+    alloc(&E->kind, n);
+    alloc(&E->bflag, n);
+    alloc(&E->dirty, 2 * static_cast<std::size_t>(tiles));
+    alloc(&E->oflag, n);
+    alloc(&E->pos, n);
+    alloc(&E->nd, static_cast<std::size_t>(n_members));
+    alloc(&E->area, n);
+    alloc(&E->order, n);
+    alloc(&E->lstart, n + 3);
+    alloc(&E->lcount, n + 3);
+    alloc(&E->lfill, n + 3);
+    alloc(&E->maxd, 1);
+    alloc(&E->dof, n);
+    alloc(&E->invd, n);
+    alloc(&E->b, n);
+    alloc(&E->x, n);
+    alloc(&E->r, n);
+    alloc(&E->p, n);
+    alloc(&E->zz, n);
+    alloc(&E->Ap, n);
+    alloc(&E->hs_bb, static_cast<std::size_t>(n_members));
+    alloc(&E->hs_acc, static_cast<std::size_t>(kHsSlot) * n_members * (static_cast<std::size_t>(E->max_iter_all) + 2));
+    alloc(&E->done, static_cast<std::size_t>(n_members));
+    alloc(&E->iters, static_cast<std::size_t>(n_members));
+    alloc(&E->stats_acc, 8 * static_cast<std::size_t>(n_members));
+    alloc(&E->flags, kFlags);
+    if (e == cudaSuccess) e = cudaMallocHost(&E->h_stats, sizeof(double) * 8 * n_members);
+    if (e == cudaSuccess) e = cudaMallocHost(&E->h_flags, sizeof(int) * kFlags);
+    if (e == cudaSuccess) e = cudaMallocHost(&E->h_iters, sizeof(int) * n_members);
+    if (e == cudaSuccess) e = cudaMallocHost(&E->h_maxd, sizeof(std::uint32_t));
+    if (e == cudaSuccess) e = cudaMallocHost(&E->h_err, sizeof(unsigned long long) * 4);
+    if (e != cudaSuccess)
+    {
+        free_ensemble(E);
+        return cuda_fail(e, who);
+    }
+    cudaMemcpyAsync(E->d_pm, E->pm.data(), sizeof(PackedMember) * n_members, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(E->d_prm, E->prm_h.data(), sizeof(EnsParams) * n_members, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(E->blk_member, blk.data(), sizeof(std::uint16_t) * blk.size(), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(E->tile_member, tm.data(), sizeof(std::uint16_t) * tm.size(), cudaMemcpyHostToDevice, st);
+    cudaMemsetAsync(E->z, 0, sizeof(float) * n, st);
+    cudaMemsetAsync(E->mask, 0, n, st);
+    E->P.m = E->d_pm;
+    E->P.blk_member = E->blk_member;
+    E->P.n = N;
+    E->P.n_members = n_members;
+    e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess)
+    {
+        free_ensemble(E);
+        return cuda_fail(e, who);
+    }
+    E->info.packed_cells = N;
+    E->info.member_cells = E->member_cells;
+    E->info.graph_enabled = E->use_graph ? 1 : 0;
+    *out = E;
+    return LSDTT_GPU_OK;
+}
+
+int lsdtt_gpu_ensemble_destroy(lsdtt_gpu_ensemble* E)
+{
+    if (E) free_ensemble(E);
+    return LSDTT_GPU_OK;
+}
+
+int lsdtt_gpu_ensemble_offsets(const lsdtt_gpu_ensemble* E, int64_t* offsets)
+{
+    if (!E || !offsets) return fail(LSDTT_GPU_EINVAL, "lsdtt_gpu_ensemble_offsets: null argument");
+    for (int k = 0; k < E->M; ++k) offsets[k] = E->pm[static_cast<std::size_t>(k)].base;
+    offsets[E->M] = E->N;
+    return LSDTT_GPU_OK;
+}
+
+int lsdtt_gpu_ensemble_set_member(lsdtt_gpu_ensemble* E, int32_t k, const float* z_dev, const uint8_t* mask_dev,
+                                  void* stream)
+{
+    if (!E || !z_dev || !mask_dev || k < 0 || k >= E->M)
+        return fail(LSDTT_GPU_EINVAL, "lsdtt_gpu_ensemble_set_member: bad argument");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const PackedMember& P = E->pm[static_cast<std::size_t>(k)];
+    const std::size_t n = static_cast<std::size_t>(P.nr) * P.nc;
+    cudaMemcpyAsync(E->z + P.base, z_dev, sizeof(float) * n, cudaMemcpyDeviceToDevice, st);
+    cudaMemcpyAsync(E->mask + P.base, mask_dev, n, cudaMemcpyDeviceToDevice, st);
+    ens_boundary_flag<<<grid_blocks(E->N, 256), 256, 0, st>>>(E->P, E->mask, E->bflag);
+    // Mask changes alter the valid count the stack checks against.
+    E->member_set[static_cast<std::size_t>(k)] = 1;
+    E->ready = std::all_of(E->member_set.begin(), E->member_set.end(), [](char c) { return c != 0; });
+    E->captured = false;  // the valid count (a captured constant) may have changed
+    const cudaError_t e = cudaStreamSynchronize(st);
+    return e == cudaSuccess ? LSDTT_GPU_OK : cuda_fail(e, "lsdtt_gpu_ensemble_set_member");
+}
+
+int lsdtt_gpu_ensemble_get_member(const lsdtt_gpu_ensemble* E, int32_t k, float* z_dev, void* stream)
+{
+    if (!E || !z_dev || k < 0 || k >= E->M) return fail(LSDTT_GPU_EINVAL, "lsdtt_gpu_ensemble_get_member: bad argument");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const PackedMember& P = E->pm[static_cast<std::size_t>(k)];
+    cudaMemcpyAsync(z_dev, E->z + P.base, sizeof(float) * static_cast<std::size_t>(P.nr) * P.nc,
+                    cudaMemcpyDeviceToDevice, st);
+    const cudaError_t e = cudaStreamSynchronize(st);
+    return e == cudaSuccess ? LSDTT_GPU_OK : cuda_fail(e, "lsdtt_gpu_ensemble_get_member");
+}
+
+int lsdtt_gpu_ensemble_step(lsdtt_gpu_ensemble* E, int32_t n_steps, lsdtt_gpu_lem_stats* stats, void* stream)
+{
+    const char* who = "lsdtt_gpu_ensemble_step";
+    if (!E || n_steps < 0) return fail(LSDTT_GPU_EINVAL, std::string(who) + ": bad argument");
+    if (!E->ready) return fail(LSDTT_GPU_ESTATE, std::string(who) + ": every member needs a surface and a mask");
+    // Work runs on the handle's own stream, after the caller's stream.
+    cudaError_t e0 = cudaStreamSynchronize(static_cast<cudaStream_t>(stream));
+    if (e0 != cudaSuccess) return cuda_fail(e0, who);
+    cudaStream_t st = E->own;
+    const bool graph_ok = E->use_graph && !profiling_enabled();
+    for (int s = 0; s < n_steps; ++s)
+    {
+        cudaError_t e = cudaSuccess;
+        bool ran = false;
+        if (graph_ok && E->captured)
+        {
+            e = cudaGraphLaunch(E->exec, st);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+            if (e != cudaSuccess) return cuda_fail(e, who);
+            ++E->info.graph_replays;
+            const int* F = E->h_flags;
+            if (F[1] || F[2] || F[3])
+            {
+                // Outgrew the captured schedule: undo and rerun eagerly.
+                cudaMemcpyAsync(E->z, E->zpre, sizeof(float) * E->N, cudaMemcpyDeviceToDevice, st);
+                E->captured = false;
+            }
+            else
+                ran = true;
+        }
+        if (!ran)
+        {
+            if (E->f->n_valid < 0 || !E->captured)
+            {
+                // The stack checks s-vector ranges against the valid count.
+                std::int64_t nv = 0;
+                std::vector<std::uint8_t> hm(static_cast<std::size_t>(E->N));
+                e = cudaMemcpyAsync(hm.data(), E->mask, hm.size(), cudaMemcpyDeviceToHost, st);
+                if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+                if (e != cudaSuccess) return cuda_fail(e, who);
+                for (std::uint8_t v : hm) nv += v ? 1 : 0;
+                E->f->n_valid = nv;
+            }
+            StepRecord rec;
+            e = run_step(E, st, true, &rec);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+            if (e == cudaErrorLaunchTimeout) return fail(LSDTT_GPU_ETIMEOUT, std::string(who) + ": fill did not converge");
+            if (e != cudaSuccess) return cuda_fail(e, who);
+            ++E->info.eager_steps;
+            E->info.last_fill_passes = rec.fill_passes;
+            E->info.last_max_depth = rec.max_depth;
+            E->info.last_hillslope_iterations = rec.pcg_iters;
+            if (graph_ok)
+            {
+                // Keep the eager step's flags and statistics: capturing
+                // enqueues nothing that runs.
+                std::vector<int> fl(E->h_flags, E->h_flags + kFlags);
+                std::vector<double> sv(E->h_stats, E->h_stats + 8 * E->M);
+                std::vector<int> itv(E->h_iters, E->h_iters + E->M);
+                e = capture(E, rec, st);
+                if (e != cudaSuccess) return cuda_fail(e, "lsdtt_gpu_ensemble_step (graph capture)");
+                std::copy(fl.begin(), fl.end(), E->h_flags);
+                std::copy(sv.begin(), sv.end(), E->h_stats);
+                std::copy(itv.begin(), itv.end(), E->h_iters);
+            }
+        }
+        if ((E->h_err[0] & 0xffffffffull) != 0)
+            return fail(LSDTT_GPU_ECYCLIC, std::string(who) + ": the receiver graph of a member has a cycle");
+        if (E->h_flags[4])
+            return fail(LSDTT_GPU_ENOCONV, std::string(who) + ": a member's hillslope Jacobi-PCG did not reach its "
+                                                              "relative residual within hillslope_max_iter");
+    }
+    E->info.fill_pass_cap = E->fill_cap;
+    E->info.depth_cap = E->depth_cap;
+    E->info.sweep_split_level = E->split;
+    E->info.sweep_block = E->sweep_block;
+    E->info.hillslope_iteration_cap = E->it_cap;
+    if (stats) fill_stats(E, stats);
+    return LSDTT_GPU_OK;
+}
+
+int lsdtt_gpu_ensemble_override_schedule(lsdtt_gpu_ensemble* E, int32_t fill_pass_cap, int32_t hillslope_iteration_cap)
+{
+    if (!E || fill_pass_cap < 0 || hillslope_iteration_cap < 0)
+        return fail(LSDTT_GPU_EINVAL, "lsdtt_gpu_ensemble_override_schedule: bad argument");
+    E->ov_fill = fill_pass_cap;
+    E->ov_it = hillslope_iteration_cap;
+    E->captured = false;
+    return LSDTT_GPU_OK;
+}
+
+int lsdtt_gpu_ensemble_get_info(const lsdtt_gpu_ensemble* E, lsdtt_gpu_ensemble_info* info)
+{
+    if (!E || !info) return fail(LSDTT_GPU_EINVAL, "lsdtt_gpu_ensemble_get_info: null argument");
+    *info = E->info;
+    return LSDTT_GPU_OK;
+}
+
+}  // extern "C"
+
+namespace lsdtt_gb300
+{
+LSDTT_DEFINE_LAUNCH_READER(ensemble)
+}  // namespace lsdtt_gb300

@@ -16,15 +16,13 @@
 #include <vector>
 
 #include "engine.cuh"
+#include "lem_cell.cuh"
 
 namespace lsdtt_gb300
 {
 namespace
 {
 
-// build_boundary_flats (src/cpu/lsdtt_lem_cpu.cpp:735-808): valid cells with
-// an off-grid neighbour across a fixed ('o'/'b') edge, or a masked in-grid
-// neighbour in a direction whose edge is fixed.
 __global__ void boundary_flag(int nr, int nc, const char* bc4, const std::uint8_t* __restrict__ mask,
                               std::uint8_t* __restrict__ flag)
 {
@@ -32,27 +30,7 @@ __global__ void boundary_flag(int nr, int nc, const char* bc4, const std::uint8_
     const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     const std::int64_t n = static_cast<std::int64_t>(nr) * nc;
     if (i >= n) return;
-    flag[i] = 0;
-    if (!mask[i]) return;
-    const bool fn = bc4[0] == 'o' || bc4[0] == 'b', fe = bc4[1] == 'o' || bc4[1] == 'b';
-    const bool fs = bc4[2] == 'o' || bc4[2] == 'b', fw = bc4[3] == 'o' || bc4[3] == 'b';
-    const int r = static_cast<int>(i / nc), c = static_cast<int>(i % nc);
-    bool edge = false;
-    for (int dr = -1; dr <= 1 && !edge; ++dr)
-        for (int dc = -1; dc <= 1; ++dc)
-        {
-            if (dr == 0 && dc == 0) continue;
-            const int r2 = r + dr, c2 = c + dc;
-            if (r2 < 0) { if (fn) edge = true; }
-            else if (r2 >= nr) { if (fs) edge = true; }
-            else if (c2 < 0) { if (fw) edge = true; }
-            else if (c2 >= nc) { if (fe) edge = true; }
-            else if (!mask[static_cast<std::int64_t>(r2) * nc + c2])
-            {
-                if ((dr == -1 && fn) || (dr == 1 && fs) || (dc == -1 && fw) || (dc == 1 && fe)) edge = true;
-            }
-        }
-    flag[i] = edge ? 1 : 0;
+    flag[i] = boundary_flat_cell(nr, nc, bc4, mask, i) ? 1 : 0;
 }
 
 __global__ void lem_uplift_restore(std::int64_t n, const std::uint8_t* __restrict__ mask,

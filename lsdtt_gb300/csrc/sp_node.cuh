@@ -1,0 +1,79 @@
+// sp_node.cuh -- the per-node implicit stream-power update, shared by the
+// single-grid sweep (stream_power.cu) and the packed ensemble (ensemble.cu).
+#pragma once
+
+#include <cmath>
+
+#include "common.cuh"
+
+namespace lsdtt_gb300
+{
+namespace
+{
+
+struct SpParams
+{
+    float K, m, n, dt, threshold, slope_clamp, dx, dx_diag;
+    int divide_by_dx;
+    int n_is_one;
+};
+
+// The implicit update of node `flat` from its receiver's final elevation
+// (stream_power_cpu.cpp:236-318). Any receiver-before-donor order gives the
+// reference's bits: a node reads only z_old[self] and z[receiver]. Indices
+// are those of the arrays passed (n = their length).
+__device__ __forceinline__ void sp_node(const SpParams& P, std::int64_t n, std::int64_t flat,
+                                        const std::int64_t* __restrict__ receiver, const std::uint8_t* __restrict__ dir,
+                                        const double* __restrict__ area_d, const float* __restrict__ z_old,
+                                        const float* __restrict__ kfield, float* __restrict__ z)
+{
+    const std::int64_t recv = receiver[flat];
+    if (recv < 0 || recv >= n) return;  // outlets and nodata are not eroded
+    const float dx_eff = (dir[flat] & 1u) ? P.dx_diag : P.dx;
+    double area = area_d[flat];
+    if (P.divide_by_dx) area = __ddiv_rn(area, static_cast<double>(P.dx));
+    if (P.threshold > 0.0f && area < static_cast<double>(P.threshold)) return;
+    const float zo = z_old[flat];
+    const float zr = z[recv];
+    if (zr >= zo) return;
+    const double tol = __dmul_rn(static_cast<double>(P.slope_clamp), static_cast<double>(dx_eff));
+    const float Ki = kfield ? kfield[flat] : P.K;
+    const double kam = __dmul_rn(static_cast<double>(Ki), pow(area, static_cast<double>(P.m)));
+    float zn = zo;
+    if (P.n_is_one)
+    {
+        const double spf = __dmul_rn(kam, static_cast<double>(__fdiv_rn(P.dt, dx_eff)));
+        const double num = __dadd_rn(static_cast<double>(zo), __dmul_rn(static_cast<double>(zr), spf));
+        zn = static_cast<float>(__ddiv_rn(num, __dadd_rn(1.0, spf)));
+        if (__fsub_rn(zn, zo) > static_cast<float>(tol) || isnan(zn)) zn = zo;
+    }
+    else
+    {
+        double eps = tol + 1.0;
+        int it = 0;
+        const double nd = static_cast<double>(P.n);
+        const double kdt = __dmul_rn(kam, static_cast<double>(P.dt));
+        const double ndx = static_cast<double>(__fdiv_rn(P.n, dx_eff));
+        do
+        {
+            const double slope = static_cast<double>(__fdiv_rn(__fsub_rn(zn, zr), dx_eff));
+            if (slope <= 0.0) eps = 0.0;
+            else
+            {
+                const double fz = __dadd_rn(static_cast<double>(__fsub_rn(zn, zo)), __dmul_rn(kdt, pow(slope, nd)));
+                const double fdz = __dadd_rn(1.0, __dmul_rn(__dmul_rn(kdt, ndx), pow(slope, __dsub_rn(nd, 1.0))));
+                eps = __ddiv_rn(fz, fdz);
+            }
+            zn = __fsub_rn(zn, static_cast<float>(eps));
+            ++it;
+            if (it > 100) eps = tol / 2.0;
+        } while (fabs(eps) > tol);
+        if (__fsub_rn(zn, zo) > static_cast<float>(tol) || isnan(zn)) zn = zo;
+        if (zn < zr) zn = __fadd_rn(zr, __fmul_rn(P.slope_clamp, dx_eff));
+    }
+    z[flat] = zn;
+}
+
+
+}  // namespace
+}  // namespace lsdtt_gb300

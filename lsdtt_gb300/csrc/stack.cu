@@ -107,6 +107,25 @@ __global__ void links_kernel(Grid g, const std::uint8_t* __restrict__ mask, cons
         next_sib[d[i]] = (i + 1 < k) ? static_cast<std::uint32_t>(d[i + 1]) : kNone;
 }
 
+// links_kernel for a packed ensemble: each member's donors in its own
+// geometry, written as packed indices.
+__global__ void links_packed(Packed P, const std::uint8_t* __restrict__ mask, const std::uint8_t* __restrict__ dir,
+                             std::uint32_t* __restrict__ first_child, std::uint32_t* __restrict__ next_sib)
+{
+    LSDTT_COUNT();
+    const std::int64_t flat = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (flat >= P.n || !mask[flat]) return;
+    const PackedMember M = P.m[P.blk_member[flat / kPackAlign]];
+    const Grid g = member_grid(M);
+    const std::int64_t local = flat - M.base;
+    if (local >= g.n) return;
+    std::int64_t d[8];
+    const int k = donor_list(g, mask + M.base, dir + M.base, local, d);
+    first_child[flat] = k ? static_cast<std::uint32_t>(M.base + d[0]) : kNone;
+    for (int i = 0; i < k; ++i)
+        next_sib[M.base + d[i]] = (i + 1 < k) ? static_cast<std::uint32_t>(M.base + d[i + 1]) : kNone;
+}
+
 __global__ void root_links_kernel(const std::int64_t* __restrict__ outlets, const std::int64_t* __restrict__ n_out,
                                   std::uint32_t* __restrict__ next_sib, std::uint32_t* __restrict__ head)
 {
@@ -510,7 +529,7 @@ int bits_for(std::uint64_t v)
 
 }  // namespace
 
-cudaError_t build_stack(lsdtt_gpu_flow* f, bool want_topo, cudaStream_t st)
+cudaError_t build_stack(lsdtt_gpu_flow* f, bool want_topo, cudaStream_t st, const Packed* packed)
 {
     const Grid& g = f->g;
     const std::int64_t n = g.n;
@@ -526,7 +545,13 @@ cudaError_t build_stack(lsdtt_gpu_flow* f, bool want_topo, cudaStream_t st)
     std::int32_t* p1 = ws.take<std::int32_t>(2 * n);
     if (!first_child || !next_sib || !succ || !head || !p0 || !p1) return cudaErrorMemoryAllocation;
 
-    links_kernel<<<nb, 256, 0, st>>>(g, f->mask, f->dir, first_child, next_sib);
+    if (packed)
+    {
+        if (want_topo) return cudaErrorInvalidValue;  // the ensemble needs the s-vector only
+        links_packed<<<nb, 256, 0, st>>>(*packed, f->mask, f->dir, first_child, next_sib);
+    }
+    else
+        links_kernel<<<nb, 256, 0, st>>>(g, f->mask, f->dir, first_child, next_sib);
     root_links_kernel<<<grid_blocks(n, 256), 256, 0, st>>>(f->outlets, f->dscal + 1, next_sib, head);
     succ_kernel<<<nb, 256, 0, st>>>(g, f->mask, f->receiver, first_child, next_sib, succ);
 

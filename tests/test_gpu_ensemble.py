@@ -1,0 +1,123 @@
+"""The batched ensemble against its members run one at a time.
+
+Every member of an lsdtt_gpu_ensemble must advance exactly as the
+single-grid LandscapeModel advances it alone (which the LEM tests in
+test_gpu_lem_path.py hold to the oracle). Members differ in shape (non-
+square, not multiples of the tile or block size), boundary string
+(including a periodic axis), fill on/off, stream-power exponent (n = 1, 1.5,
+2), erodibility, diffusivity, uplift and hillslope on/off.
+
+Bars: elevations within 1e-5 relative (the LEM bar; the only source of
+difference is the order of the FP64 atomic reductions inside Jacobi-PCG);
+the graph-replayed steps give the same result as eager steps to the same
+bar; the schedule counters show the graph was captured and replayed.
+"""
+import numpy as np
+import pytest
+
+from tests import surfaces
+
+pytestmark = pytest.mark.gpu
+
+REL = 1e-5
+
+
+def _members(port):
+    specs = []
+    z = port.noise_tilt_surface(96, 130, 30.0, 3, 0.0, 1.0, "nnon", 0.001)
+    specs.append(dict(z=z, cell_size=30.0, boundary_conditions="nnon", timestep=1000.0, erodibility=1e-5,
+                      m_exponent=0.5, n_exponent=1.0, uplift_rate=1e-3, hillslope_diffusivity=0.01,
+                      fill_min_slope=1e-4))
+    z = surfaces.fractal(200, 72, 40.0, 5).astype(np.float32)
+    specs.append(dict(z=z, cell_size=10.0, boundary_conditions="oooo", timestep=500.0, erodibility=3e-5,
+                      m_exponent=0.4, n_exponent=1.5, uplift_rate=2e-3, hillslope_diffusivity=0.05,
+                      fill_min_slope=1e-4))
+    z = port.noise_tilt_surface(128, 128, 20.0, 9, 0.0, 1.0, "nnon", 0.001)
+    specs.append(dict(z=z, cell_size=20.0, boundary_conditions="nnon", timestep=1000.0, erodibility=1e-4,
+                      m_exponent=0.6, n_exponent=2.0, uplift_rate=1e-4, hillslope_diffusivity=0.002,
+                      fill_min_slope=0.0))
+    z = surfaces.fractal(64, 80, 20.0, 11).astype(np.float32)
+    specs.append(dict(z=z, cell_size=30.0, boundary_conditions="opop", timestep=1000.0, erodibility=2e-5,
+                      m_exponent=0.45, n_exponent=1.0, uplift_rate=5e-4, hillslope_diffusivity=0.02,
+                      fill_min_slope=1e-4))
+    z = port.noise_tilt_surface(40, 48, 30.0, 13, 0.0, 1.0, "nnon", 0.001)
+    specs.append(dict(z=z, cell_size=30.0, boundary_conditions="nnon", timestep=1000.0, erodibility=1e-5,
+                      m_exponent=0.5, n_exponent=1.5, uplift_rate=1e-3, hillslope_diffusivity=0.01,
+                      fill_min_slope=1e-4, enable_hillslope=False))
+    return specs
+
+
+def _alone(G, spec, steps):
+    spec = dict(spec)
+    z = spec.pop("z")
+    cell = spec.pop("cell_size")
+    bc = spec.pop("boundary_conditions")
+    model = G.LandscapeModel(z, np.ones_like(z, np.uint8), cell, bc, **spec)
+    its = []
+    for _ in range(steps):
+        its.append(model.step()["hillslope_iterations"])
+    return model.z.cpu().numpy(), its
+
+
+def _rel(a, b):
+    return float(np.max(np.abs(a - b)) / max(float(np.ptp(b)), 1.0))
+
+
+@pytest.mark.parametrize("use_graph", [False, True])
+def test_ensemble_matches_members_alone(port, use_graph):
+    import lsdtt_gb300 as G
+    specs = _members(port)
+    steps = 6
+    ens = G.Ensemble(specs, use_graph=use_graph)
+    for _ in range(steps - 1):
+        ens.step()
+    stats = ens.step(want_stats=True)
+    info = ens.info()
+    worst = 0.0
+    for k, spec in enumerate(specs):
+        z_alone, its = _alone(G, spec, steps)
+        got = ens.get(k).cpu().numpy()
+        err = _rel(got, z_alone)
+        worst = max(worst, err)
+        print(f"member {k} {spec['z'].shape} bc={spec['boundary_conditions']}: rel diff {err:.2e}; "
+              f"PCG iterations alone {its[-1]} ensemble {stats[k]['hillslope_iterations']}")
+        assert err <= REL, (k, err)
+        assert abs(stats[k]["hillslope_iterations"] - its[-1]) <= 4
+    print("info", info)
+    if use_graph:
+        assert info["graph_captures"] >= 1 and info["graph_replays"] >= steps - 2
+    else:
+        assert info["eager_steps"] == steps and info["graph_replays"] == 0
+
+
+def test_graph_and_eager_agree_and_recover_from_overflow(port):
+    import lsdtt_gb300 as G
+    specs = _members(port)
+    a = G.Ensemble(specs, use_graph=True)
+    b = G.Ensemble(specs, use_graph=False)
+    for _ in range(3):
+        a.step()
+        b.step()
+    # Capture the next step with a schedule far too short for the fill and
+    # the PCG: the replay after it must detect the overflow on the device,
+    # undo the step and rerun it eagerly, then capture a fitting schedule.
+    a.override_schedule(fill_pass_cap=4, hillslope_iteration_cap=4)
+    before = a.info()
+    for _ in range(5):
+        a.step()
+        b.step()
+    after = a.info()
+    print("info before", before, "after", after)
+    assert after["graph_captures"] >= before["graph_captures"] + 2
+    assert after["eager_steps"] >= before["eager_steps"] + 2
+    for k in range(len(specs)):
+        assert _rel(a.get(k).cpu().numpy(), b.get(k).cpu().numpy()) <= REL
+
+
+def test_ensemble_errors():
+    import lsdtt_gb300 as G
+    z = np.zeros((16, 16), np.float32)
+    with pytest.raises(G.GpuError):
+        G.Ensemble([dict(z=z, cell_size=30.0, boundary_conditions="pppp")])
+    with pytest.raises(G.GpuError):
+        G.Ensemble([dict(z=z, cell_size=30.0, timestep=-1.0)])
