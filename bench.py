@@ -1,20 +1,36 @@
-"""Benchmark: one routing pass of the landscape-evolution hot path on GB300.
+"""Benchmark: the landscape-evolution timestep on GB300.
 
-Workload (the single-GPU routing configuration): an 8192 x 8192 float32 DEM,
-dx = 10 m, seeded spectral-synthesis fractal (power spectrum ~ k^-2, relief
-1000 m) plus 100,000 seeded pits (depth U[0,5] m, radius U[1,4] cells),
-boundary "oooo". One step = fill_pits(min_slope 1e-4) -> D8 receivers (int64
-receivers exported) -> donor counts and outlets -> s-vector (contributing
-counts, int64) -> Kahn topological order. The metric is cells routed per
-second ("cell-steps/s": one step routes every cell once).
+Default workload (--workload ensemble): a batched parameter-sweep ensemble
+of 256 independent LEM runs on one GPU. Member grids have sides drawn
+uniformly from 128-1024 cells (rows and columns independently), dx = 30 m,
+bc "nnon"; K log-uniform 1e-6..1e-4, m uniform 0.35..0.6, n from {1, 1.5,
+2}, D log-uniform 1e-3..1e-1 m^2/yr, U log-uniform 1e-4..1e-2 m/yr, dt =
+1000 yr; initial surfaces seeded uniform noise 0-1 m plus a 0.001 tilt
+toward the open south edge. One step advances every member by one LEM step:
+fill_pits(1e-4) -> D8 receivers -> s-vector / contributing counts -> implicit
+stream power (per-node Newton for n != 1) -> linear implicit hillslope by
+Jacobi-PCG to a 1e-8 relative residual -> uplift and boundary restore. The
+metric is member cells advanced per second (cell-steps/s).
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+The same line reports:
+  * plain_gpu: the members stepped one at a time through the single-grid
+    LEM (lsdtt_gpu_lem_step), on a sample of members -- the plain GPU form;
+  * e2e: the ensemble stepped through the C ABI with the packed surfaces
+    uploaded from and downloaded to pinned host memory every step;
+  * roofline: the dominant kernel of a profiled (eager) step of the same
+    ensemble, algorithmic bytes over its CUDA-event time;
+  * cpu_baseline: the C++/numpy restatement of the reference (oracle/) on a
+    bounded sample of members, on the host cores.
 
-N > 1 runs under torchrun as independent replicas (one grid per GPU; the path
-does not shard), so the aggregate is weak scaling. `--impl reference` times
-the CPU implementation of the same pass (the C++ restatement of the
-reference, oracle/liblsdtt_oracle.so) on the host cores with a 4096 x 4096
-sample of the same surface per step.
+--workload routing keeps the single-grid routing pass (8192^2 fractal +
+100k pits: fill + D8 + s-vector + Kahn order).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--workload ensemble|routing]
+
+N > 1 runs under torchrun as independent replicas (each rank its own
+ensemble; members are independent and the path has no exchange step), so
+the aggregate is weak scaling. `--impl reference` times the CPU
+restatement of the same step on the host cores.
 """
 from __future__ import annotations
 
@@ -35,6 +51,10 @@ sys.path.insert(0, ROOT)
 METRIC = "LEM cell-steps/s on 1 GB300: learned-precond+batched vs plain GPU at equal residual"
 WORKLOAD = ("routing pass on an 8192x8192 fractal (k^-2, 1000 m relief) + 100k pits, dx=10 m, bc oooo: "
             "fill(eps=1e-4) + D8 receivers + donors/outlets + s-vector/int64 counts + Kahn order")
+ENS_WORKLOAD = ("batched ensemble of 256 LEM runs, sides U{128..1024} (non-square), dx=30 m, bc nnon, dt=1000 yr, "
+                "K logU[1e-6,1e-4], m U[0.35,0.6], n in {1,1.5,2}, D logU[1e-3,1e-1], U logU[1e-4,1e-2], "
+                "noise 0-1 m + 0.001 tilt; step = fill(1e-4) + D8 + s-vector + stream power + linear implicit "
+                "hillslope (Jacobi-PCG, 1e-8 relative residual) + uplift/boundary restore")
 
 
 def peaks():
@@ -138,7 +158,7 @@ def cpu_baseline(n_sample: int, reps: int = 1):
     return z.size / best, best
 
 
-def run_reference(args, rank, world):
+def routing_reference(args, rank, world):
     if rank != 0:
         return 0
     n_sample = args.cpu_sample
@@ -170,7 +190,7 @@ def run_reference(args, rank, world):
     return 0
 
 
-def run_gpu(args, rank, world):
+def routing_gpu(args, rank, world):
     import torch
     import lsdtt_gb300 as G
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -316,6 +336,257 @@ def run_gpu(args, rank, world):
     return 0
 
 
+# ---------------------------------------------------------------------------
+# ensemble workload
+# ---------------------------------------------------------------------------
+def ensemble_specs(n_members: int, rank: int = 0, seed: int = 4):
+    from tests import surfaces
+    rng = np.random.default_rng(seed + 7919 * rank)
+    specs = []
+    for _ in range(n_members):
+        nr, nc = (int(v) for v in rng.integers(128, 1025, 2))
+        K = float(10.0 ** rng.uniform(-6.0, -4.0))
+        mm = float(rng.uniform(0.35, 0.6))
+        nn = float(rng.choice([1.0, 1.5, 2.0]))
+        D = float(10.0 ** rng.uniform(-3.0, -1.0))
+        U = float(10.0 ** rng.uniform(-4.0, -2.0))
+        z = surfaces.noise_tilt(nr, nc, 30.0, int(rng.integers(1 << 30)), "nnon", 0.001)
+        specs.append(dict(z=z, cell_size=30.0, boundary_conditions="nnon", timestep=1000.0, erodibility=K,
+                          m_exponent=mm, n_exponent=nn, uplift_rate=U, hillslope_diffusivity=D, fill_min_slope=1e-4,
+                          hillslope_rel_tol=1e-8, hillslope_max_iter=2000))
+    return specs
+
+
+def ensemble_cpu_step(P, H, lem_finish, spec):
+    """One LEM step of one member in the restatement of the reference:
+    fill_pits -> lsdtt_flowinfo + compute_d8_stream_power_incision (C++) ->
+    the implicit linear hillslope step (FP64 Jacobi-PCG to the member's
+    relative residual, scipy) -> uplift and boundary restore."""
+    z = spec["z"]
+    m = np.ones_like(z, np.uint8)
+    cell, bc = spec["cell_size"], spec["boundary_conditions"]
+    dt = spec["timestep"]
+    bf = P.boundary_flats(m, bc)
+    zf = P.fill_pits(z, m, cell, bc, spec["fill_min_slope"])
+    zsp = P.stream_power(zf, m, cell, bc, spec["erodibility"], spec["m_exponent"], spec["n_exponent"], dt)
+    zh, _, _ = H.linear_step(zsp, m, cell, bc, spec["hillslope_diffusivity"], dt, solver="pcg",
+                             rel_tol=spec["hillslope_rel_tol"])
+    zn, _ = lem_finish(zh, zf, m, spec["uplift_rate"], dt, bf)
+    return zn
+
+
+def ensemble_cpu_sample(specs, budget_s: float):
+    """Members in order, one step each, until budget_s of CPU work."""
+    import oracle
+    from oracle import hillslope as H
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
+    P = oracle.port()
+    cells, t, used = 0, 0.0, 0
+    for spec in specs:
+        t0 = time.perf_counter()
+        ensemble_cpu_step(P, H, oracle.lem_finish, spec)
+        t += time.perf_counter() - t0
+        cells += spec["z"].size
+        used += 1
+        if t >= budget_s:
+            break
+    return cells / t, cells, used, t
+
+
+def ensemble_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    specs = ensemble_specs(args.members)
+    times, cells_done = [], []
+    for i in range(args.warmup + args.steps):
+        # each step: a bounded sample of the ensemble's members (rotating)
+        rot = specs[(i * 3) % len(specs):] + specs[:(i * 3) % len(specs)]
+        v, cells, used, t = ensemble_cpu_sample(rot, 3.0)
+        if i >= args.warmup:
+            times.append(t)
+            cells_done.append(cells)
+    value = sum(cells_done) / sum(times)
+    line = {"metric": METRIC, "value": value, "unit": "cell-steps/s", "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": statistics.median(times) * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": ENS_WORKLOAD,
+                       "sample": "each step: members in order until ~3 s of CPU work, one LEM step each"},
+            "cpu_baseline": {"value": value, "unit": "cell-steps/s", "cores": os.cpu_count(), "kind": "port",
+                             "sample": "members of the same ensemble, one LEM step each, ~3 s per step: C++ "
+                                       "restatement (fill, flowinfo with OpenMP receivers, stream power) + FP64 "
+                                       "Jacobi-PCG hillslope solve (scipy, 1e-8 relative residual)"},
+            "e2e": {"value": value, "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+ENS_KERNELS = ("ens_fill_relax", "ens_d8_receivers", "stack_ruler_walk", "ens_hillslope_apply",
+               "ens_hillslope_update")
+
+
+def ensemble_gpu(args, rank, world):
+    import torch
+    import lsdtt_gb300 as G
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    L = G.lib()
+    L.lsdtt_gpu_launch_count.restype = ctypes.c_ulonglong
+    L.lsdtt_gpu_profile_read.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_double),
+                                         ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_double)]
+    specs = ensemble_specs(args.members, rank=rank)
+    cells = int(sum(sp["z"].size for sp in specs))
+    stream = torch.cuda.current_stream()
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def max_over_ranks(t):
+        if dist is None:
+            return t
+        tt = torch.tensor([t], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        return float(tt.item())
+
+    ens = G.Ensemble(specs, use_graph=True)
+    t_warm0 = time.perf_counter()
+    for _ in range(args.warmup):
+        ens.step()
+    barrier()
+    t_warm = time.perf_counter() - t_warm0
+    launches0 = L.lsdtt_gpu_launch_count()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    with Clocks(local) as clk:
+        barrier()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            ens.step()
+        ev1.record(stream)
+        barrier()
+    elapsed = max_over_ranks(ev0.elapsed_time(ev1) / 1e3)
+    launches = L.lsdtt_gpu_launch_count() - launches0
+    info = ens.info()
+    value = world * cells * args.steps / elapsed
+
+    # Kernel table: one profiled step (profiling keeps the ensemble eager).
+    L.lsdtt_gpu_profile_enable(1)
+    ens.step()
+    torch.cuda.synchronize()
+    kernels = {}
+    for name in ENS_KERNELS:
+        t, k, b = ctypes.c_double(), ctypes.c_int64(), ctypes.c_double()
+        G._check(L.lsdtt_gpu_profile_read(name.encode(), ctypes.byref(t), ctypes.byref(k), ctypes.byref(b)))
+        if k.value:
+            kernels[name] = {"ms": t.value, "launches": k.value, "bytes": b.value}
+    L.lsdtt_gpu_profile_enable(0)
+
+    # End to end: the packed surfaces to and from pinned host memory every step.
+    npk = int(ens.offsets()[-1])
+    zh = torch.empty(npk, dtype=torch.float32).pin_memory()
+    G._check(L.lsdtt_gpu_ensemble_download(ens._h, ctypes.c_void_p(zh.data_ptr()), G._stream(stream)))
+    barrier()
+    e2e_steps = max(1, min(args.steps, 3))
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(e2e_steps):
+        G._check(L.lsdtt_gpu_ensemble_upload(ens._h, ctypes.c_void_p(zh.data_ptr()), G._stream(stream)))
+        ens.step()
+        G._check(L.lsdtt_gpu_ensemble_download(ens._h, ctypes.c_void_p(zh.data_ptr()), G._stream(stream)))
+    e1.record(stream)
+    barrier()
+    e2e_t = max_over_ranks(e0.elapsed_time(e1) / 1e3)
+    e2e_value = world * cells * e2e_steps / e2e_t
+    ens.close()
+
+    # The plain GPU form: members one at a time through the single-grid LEM.
+    plain = None
+    if args.plain_members > 0:
+        sub = specs[:args.plain_members]
+        models = []
+        for sp in sub:
+            o = {k: v for k, v in sp.items() if k not in ("z", "cell_size", "boundary_conditions")}
+            models.append(G.LandscapeModel(sp["z"], np.ones_like(sp["z"], np.uint8), sp["cell_size"],
+                                           sp["boundary_conditions"], **o))
+        for mdl in models:
+            mdl.step(want_stats=False)
+        barrier()
+        p0 = torch.cuda.Event(enable_timing=True)
+        p1 = torch.cuda.Event(enable_timing=True)
+        p0.record(stream)
+        for mdl in models:
+            mdl.step(want_stats=False)
+        p1.record(stream)
+        barrier()
+        pt = p0.elapsed_time(p1) / 1e3
+        pc = int(sum(sp["z"].size for sp in sub))
+        plain = {"value": pc / pt, "unit": "cell-steps/s", "members": len(sub), "cells": pc,
+                 "call": "lsdtt_gpu_lem_step per member (fill, D8 engine, stream power, Jacobi-PCG hillslope)"}
+        for mdl in models:
+            mdl.close()
+
+    if rank == 0:
+        peak, peak_kind = peaks()
+        dom = max(kernels.items(), key=lambda kv: kv[1]["ms"]) if kernels else None
+        roof = None
+        if dom:
+            name, d = dom
+            avg_s = d["ms"] / d["launches"] / 1e3
+            achieved = d["bytes"] / d["launches"] / avg_s / 1e9
+            tpc = traffic_per_cell(name)
+            roof = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                    "frac": achieved / peak,
+                    "peak_source": "measured hbm_gbs (MEASURED_PEAKS.json), of measured"
+                    if peak_kind == "measured" else "fallback 6.8 TB/s, of fallback",
+                    "traffic": (tpc * cells) if tpc is not None else None,
+                    "algorithmic_bytes_per_launch": d["bytes"] / d["launches"],
+                    "avg_launch_ms": d["ms"] / d["launches"], "launches": d["launches"],
+                    "source": "CUDA events around each launch in one profiled (eager) step of the same ensemble, "
+                              "run right after the timed region"}
+        cpu = None
+        if world == 1 and not args.skip_cpu:
+            v, cc, used, t = ensemble_cpu_sample(specs, 20.0)
+            cpu = {"value": v, "unit": "cell-steps/s", "cores": os.cpu_count(), "kind": "port",
+                   "sample": f"the first {used} members of the same ensemble, one LEM step each ({cc} cells, "
+                             f"{t:.1f} s): C++ restatement (fill, flowinfo with OpenMP receivers, stream power) + "
+                             f"FP64 Jacobi-PCG hillslope solve (scipy, 1e-8 relative residual)"}
+        line = {
+            "metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": elapsed / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": ENS_WORKLOAD, "members": len(specs), "cells_per_step": cells,
+                       "packed_cells": int(info["packed_cells"]), "parallelism": f"replicas x{world}",
+                       "preconditioner": "Jacobi (the learned FPCG is not selected: the members' D dt/dx^2 <= 0.11 "
+                                         "converge in <= 20 Jacobi-PCG iterations, cheaper than one network "
+                                         "application)",
+                       "l2": f"inputs ({cells * 4 / 1e9:.2f} GB of surfaces alone) larger than the 129 MB L2; "
+                             f"no flush", "warmup_s": t_warm},
+            "schedule": info,
+            "plain_gpu": plain,
+            "roofline": roof,
+            "kernels": {k: {"ms_per_launch": v["ms"] / v["launches"], "launches": v["launches"],
+                            "GBps": v["bytes"] / (v["ms"] / 1e3) / 1e9} for k, v in kernels.items()},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": "cell-steps/s", "h2d_bytes_per_step": 4 * npk,
+                    "d2h_bytes_per_step": 4 * npk,
+                    "call": "lsdtt_gpu_ensemble_upload -> lsdtt_gpu_ensemble_step -> lsdtt_gpu_ensemble_download "
+                            "(packed float32 surfaces, pinned host memory)"},
+            "gpu_launches": int(launches),
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -325,14 +596,21 @@ def main():
     ap.add_argument("--size", type=int, default=8192)
     ap.add_argument("--cpu-sample", type=int, default=4096)
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--workload", default="ensemble", choices=["ensemble", "routing"])
+    ap.add_argument("--members", type=int, default=256)
+    ap.add_argument("--plain-members", type=int, default=16)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.workload == "routing":
+        if args.impl == "reference":
+            return routing_reference(args, rank, world)
+        return routing_gpu(args, rank, world)
     if args.impl == "reference":
-        return run_reference(args, rank, world)
-    return run_gpu(args, rank, world)
+        return ensemble_reference(args, rank, world)
+    return ensemble_gpu(args, rank, world)
 
 
 if __name__ == "__main__":

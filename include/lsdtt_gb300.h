@@ -343,6 +343,12 @@ int lsdtt_gpu_ensemble_offsets(const lsdtt_gpu_ensemble* ens, int64_t* offsets_h
 int lsdtt_gpu_ensemble_set_member(lsdtt_gpu_ensemble* ens, int32_t k, const float* z_dev, const uint8_t* mask_dev,
                                   void* stream);
 int lsdtt_gpu_ensemble_get_member(const lsdtt_gpu_ensemble* ens, int32_t k, float* z_dev, void* stream);
+/* All members' surfaces at once, in the packed layout (offsets above; the
+ * padding between members is ignored), between host memory and the
+ * ensemble, ordered on `stream`. This is the host-buffer path of a caller
+ * that keeps its ensemble state on the host. */
+int lsdtt_gpu_ensemble_upload(lsdtt_gpu_ensemble* ens, const float* z_host, void* stream);
+int lsdtt_gpu_ensemble_download(const lsdtt_gpu_ensemble* ens, float* z_host, void* stream);
 /* Advances every member by n_steps steps. stats (n_members entries, may be
  * NULL) receive the last step's statistics; p999_local_elevation_change is
  * not computed in an ensemble and is 0. */

@@ -331,6 +331,8 @@ def _bind_more():
         "lsdtt_gpu_ensemble_step": [vp, i32, ctypes.POINTER(LemStats), vp],
         "lsdtt_gpu_ensemble_get_info": [vp, ctypes.POINTER(EnsembleInfo)],
         "lsdtt_gpu_ensemble_override_schedule": [vp, i32, i32],
+        "lsdtt_gpu_ensemble_upload": [vp, vp, vp],
+        "lsdtt_gpu_ensemble_download": [vp, vp, vp],
     }.items():
         fn = getattr(L, name)
         fn.argtypes = args

@@ -113,6 +113,41 @@ __device__ inline void raise_error(unsigned long long* err, unsigned code, unsig
     atomicCAS(err, 0ull, v);
 }
 
+// Block-wide sum (is_max: maximum) of v over a 1-D block; valid in thread 0.
+// Every thread of the block must call it. One FP64 atomic per block instead
+// of one per warp: same-address FP64 atomics serialise at the L2 and cost
+// more than the memory traffic of the kernels that reduce.
+__device__ __forceinline__ double block_reduce_d(double v, bool is_max)
+{
+    __shared__ double sh_block_reduce[32];
+    for (int o = 16; o > 0; o >>= 1)
+    {
+        const double w = __shfl_down_sync(0xffffffffu, v, o);
+        v = is_max ? fmax(v, w) : v + w;
+    }
+    __syncthreads();  // a previous call may still be reading
+    if ((threadIdx.x & 31) == 0) sh_block_reduce[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double t = sh_block_reduce[0];
+    if (threadIdx.x == 0)
+        for (int k = 1; k < static_cast<int>(blockDim.x >> 5); ++k)
+            t = is_max ? fmax(t, sh_block_reduce[k]) : t + sh_block_reduce[k];
+    return t;
+}
+
+__device__ __forceinline__ void block_atomic_add(double* dst, double v)
+{
+    const double t = block_reduce_d(v, false);
+    if (threadIdx.x == 0 && t != 0.0) atomicAdd(dst, t);
+}
+
+// Maximum of non-negative values: their bit patterns order like the values.
+__device__ __forceinline__ void block_atomic_max_nonneg(double* dst, double v)
+{
+    const double t = block_reduce_d(v, true);
+    if (threadIdx.x == 0) atomicMax(reinterpret_cast<unsigned long long*>(dst), __double_as_longlong(t));
+}
+
 }  // namespace lsdtt_gb300
 
 // ---------------------------------------------------------------------------

@@ -61,6 +61,8 @@ struct EnsParams
     float udz, bl;
     double dw;        // dx^2, the default accumulation weight
     double rel_tol;   // hillslope PCG relative residual
+    float hs_invd[5]; // Jacobi inverse diagonal for 0..4 in-domain faces (FP64 division, rounded)
+    float inv_dt_f, DA_f, U_f;
     int fill_on, per_ns, per_ew, hill_on, max_iter;
 };
 
@@ -207,6 +209,19 @@ __global__ void ens_area(Packed P, const EnsParams* __restrict__ prm, const std:
     area[i] = mask[i] ? static_cast<double>(size[i]) * prm[member_of(P, i)].dw : 0.0;
 }
 
+// K * A^m of every node ahead of the sweep (fully parallel; the level-
+// ordered sweep then only solves each node's implicit update). In place:
+// area becomes kam.
+__global__ void ens_kam(Packed P, const EnsParams* __restrict__ prm, const std::uint8_t* __restrict__ mask,
+                        const std::int64_t* __restrict__ receiver, double* __restrict__ area)
+{
+    LSDTT_COUNT();
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= P.n || !mask[i] || receiver[i] < 0) return;
+    const SpParams& sp = prm[member_of(P, i)].sp;
+    area[i] = sp_kam(sp, area[i], sp.K);
+}
+
 // ---- depth levels and the stream-power sweep -------------------------------
 __global__ void ens_depth_hist(std::int64_t n, const std::uint8_t* __restrict__ mask,
                                const std::int32_t* __restrict__ depth, std::uint32_t cap,
@@ -256,14 +271,14 @@ struct SweepArgs
     const std::uint32_t* maxd;    // deepest level present
     const std::int64_t* receiver;
     const std::uint8_t* dir;
-    const double* area;
+    const double* kam;
     const float* z_old;
     float* z;
 };
 
 __device__ __forceinline__ void sweep_node(const SweepArgs& A, std::uint32_t flat)
 {
-    sp_node(A.prm[member_of(A.P, flat)].sp, A.P.n, flat, A.receiver, A.dir, A.area, A.z_old, nullptr, A.z);
+    sp_node_kam(A.prm[member_of(A.P, flat)].sp, A.P.n, flat, A.receiver, A.dir, A.kam[flat], A.z_old, A.z);
 }
 
 // One depth level (offsets read on the device; grid-stride over the level).
@@ -294,17 +309,73 @@ __global__ void __launch_bounds__(1024) ens_sp_tail(SweepArgs A, int k0)
 // has 4 doubles per member: [0] p.Ap, [1] r.z, [2] r.r.
 constexpr int kHsSlot = 4;
 
-__device__ __forceinline__ void warp_add(double* dst, double v)
+// Reductions are deterministic and atomic-free: each 256-cell block (one
+// member's) writes its partial to part[q * nblk + block], and
+// ens_member_reduce sums a member's partials in a fixed order. (FP64 atomics
+// into one slot per member serialise at well under a nanosecond each and
+// dominated the kernels that used them.)
+// Block partial of a float quantity: summed in FP32 within each warp
+// (32 terms), in FP64 across the warps of the block and across blocks.
+// The FP64 stage carries the cancellation-prone part of a grid-wide dot
+// product; per-thread FP64 arithmetic, scarce on this part, is avoided.
+__device__ __forceinline__ void block_partial_f(float v, bool is_max, double* __restrict__ part, std::int64_t nblk,
+                                                int q)
 {
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    if ((threadIdx.x & 31) == 0 && v != 0.0) atomicAdd(dst, v);
+    __shared__ double shf[32];
+    for (int o = 16; o > 0; o >>= 1)
+    {
+        const float w = __shfl_down_sync(0xffffffffu, v, o);
+        v = is_max ? fmaxf(v, w) : v + w;
+    }
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) shf[threadIdx.x >> 5] = static_cast<double>(v);
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        double t = shf[0];
+        for (int k = 1; k < static_cast<int>(blockDim.x >> 5); ++k) t = is_max ? fmax(t, shf[k]) : t + shf[k];
+        part[q * nblk + blockIdx.x] = t;
+    }
+}
+
+// dst[m * stride + off + q] = reduction of member m's block partials of
+// quantity q (bit q of max_mask: maximum, else sum); one warp per (m, q).
+// Members with done[m] set are skipped.
+__global__ void ens_member_reduce(Packed P, int nq, unsigned max_mask, const double* __restrict__ part,
+                                  std::int64_t nblk, const int* __restrict__ done, double* __restrict__ dst, int stride,
+                                  int off)
+{
+    LSDTT_COUNT();
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    const int m = w / nq, q = w % nq;
+    if (m >= P.n_members) return;
+    if (done && done[m]) return;
+    const PackedMember& M = P.m[m];
+    const bool is_max = (max_mask >> q) & 1u;
+    const std::int64_t b0 = M.base / kPackAlign;
+    const std::int64_t nb = (static_cast<std::int64_t>(M.nr) * M.nc + kPackAlign - 1) / kPackAlign;
+    double s = is_max ? -INFINITY : 0.0;
+    for (std::int64_t b = b0 + lane; b < b0 + nb; b += 32)
+    {
+        const double v = part[q * nblk + b];
+        s = is_max ? fmax(s, v) : s + v;
+    }
+    for (int o = 16; o > 0; o >>= 1)
+    {
+        const double v = __shfl_down_sync(0xffffffffu, s, o);
+        s = is_max ? fmax(s, v) : s + v;
+    }
+    if (lane == 0) dst[m * stride + off + q] = s;
 }
 
 // hs_setup (hillslope.cu) for every member at once: DOF flags, Jacobi
-// inverse diagonal, b = -F of the linear law at z = z^n; hs_bb[m] = ||b||^2.
+// inverse diagonal, b = -F of the linear law at z = z^n (the time term is
+// zero there), in FP32: the face differences z_nb - z_P are formed first,
+// so no large term cancels. Block partials of ||b||^2.
 __global__ void ens_hs_setup(Packed P, const EnsParams* __restrict__ prm, const std::uint8_t* __restrict__ mask,
                              const float* __restrict__ z, std::uint8_t* __restrict__ dof, float* __restrict__ inv_diag,
-                             float* __restrict__ b, double* __restrict__ hs_bb)
+                             float* __restrict__ b, double* __restrict__ part)
 {
     LSDTT_COUNT();
     const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -312,33 +383,33 @@ __global__ void ens_hs_setup(Packed P, const EnsParams* __restrict__ prm, const 
     const PackedMember& M = P.m[m];
     const EnsParams& q = prm[m];
     const Hs& H = q.hs;
-    double bb = 0.0;
+    float bb = 0.0f;
     if (i < P.n)
     {
         const std::int64_t local = i - M.base;
         bool is_dof = false;
         if (local < static_cast<std::int64_t>(M.nr) * M.nc && q.hill_on)
         {
-            const int r = static_cast<int>(local / M.nc), c = static_cast<int>(local % M.nc);
+            const int l = static_cast<int>(local);
+            const int r = l / M.nc, c = l - r * M.nc;
             const std::uint8_t* mk = mask + M.base;
-            is_dof = mk[local] && !hs_dirichlet_edge(H, r, c);
+            is_dof = mk[l] && !hs_dirichlet_edge(H, r, c);
             if (is_dof)
             {
                 const float* zm = z + M.base;
-                const double zp = zm[local];
-                double flux = 0.0;
+                const float zp = zm[l];
+                float flux = 0.0f;
                 int nf = 0;
 #pragma unroll
                 for (int f = 0; f < 4; ++f)
                 {
                     const std::int64_t j = hs_nb(H, mk, r, c, kDr[f], kDc[f]);
-                    flux += static_cast<double>(zm[j]) - zp;
-                    nf += (j != local) ? 1 : 0;
+                    flux += zm[j] - zp;
+                    nf += (j != l) ? 1 : 0;
                 }
-                double F = -H.U - H.DA * flux;
-                F += H.inv_dt * (zp - static_cast<double>(zm[local]));
-                b[i] = static_cast<float>(-F);
-                inv_diag[i] = static_cast<float>(1.0 / (H.inv_dt + H.DA * nf));
+                const float F = -q.U_f - q.DA_f * flux;
+                b[i] = -F;
+                inv_diag[i] = q.hs_invd[nf];
                 bb = F * F;
             }
         }
@@ -349,18 +420,17 @@ __global__ void ens_hs_setup(Packed P, const EnsParams* __restrict__ prm, const 
             inv_diag[i] = 0.0f;
         }
     }
-    warp_add(&hs_bb[m], bb);
+    block_partial_f(bb, false, part, P.n / kPackAlign, 0);
 }
 
-// x = 0, r = b, p = M^-1 r; slot 0 [1] = r.z
+// x = 0, r = b, p = M^-1 r; block partials of r.z
 __global__ void ens_hs_init(Packed P, const float* __restrict__ b, const float* __restrict__ inv_diag,
                             float* __restrict__ x, float* __restrict__ r, float* __restrict__ p,
-                            double* __restrict__ slot0)
+                            double* __restrict__ part)
 {
     LSDTT_COUNT();
     const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    const int m = member_of(P, i < P.n ? i : P.n - 1);
-    double rz = 0.0;
+    float rz = 0.0f;
     if (i < P.n)
     {
         const float ri = b[i];
@@ -368,9 +438,9 @@ __global__ void ens_hs_init(Packed P, const float* __restrict__ b, const float* 
         x[i] = 0.0f;
         r[i] = ri;
         p[i] = zi;
-        rz = static_cast<double>(ri) * zi;
+        rz = ri * zi;
     }
-    warp_add(&slot0[m * kHsSlot + 1], rz);
+    block_partial_f(rz, false, part, P.n / kPackAlign, 0);
 }
 
 // done[m] = no hillslope or nothing to solve; iters[m] = 0
@@ -384,58 +454,67 @@ __global__ void ens_hs_start(int M, const EnsParams* __restrict__ prm, const dou
     iters[m] = 0;
 }
 
+// Ap = A p in the difference form inv_dt p_P + (D/h^2) sum_f (p_P - [nb DOF]
+// p_nb) (faces to the cell itself carry no flux), FP32; block partials of
+// p.Ap. A converged member's blocks return at once.
 __global__ void ens_hs_apply(Packed P, const EnsParams* __restrict__ prm, const std::uint8_t* __restrict__ mask,
                              const std::uint8_t* __restrict__ dof, const int* __restrict__ done,
-                             const float* __restrict__ p, float* __restrict__ Ap, double* __restrict__ cur)
+                             const float* __restrict__ p, float* __restrict__ Ap, double* __restrict__ part)
 {
     LSDTT_COUNT();
     const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     const int m = member_of(P, i < P.n ? i : P.n - 1);
     if (done[m]) return;
     const PackedMember& M = P.m[m];
-    const Hs& H = prm[m].hs;
-    double pap = 0.0;
+    const EnsParams& q = prm[m];
+    float pap = 0.0f;
     if (i < P.n)
     {
         float v = 0.0f;
         if (dof[i])
         {
-            const std::int64_t local = i - M.base;
-            const int r = static_cast<int>(local / M.nc), c = static_cast<int>(local % M.nc);
+            const int l = static_cast<int>(i - M.base);
+            const int r = l / M.nc, c = l - r * M.nc;
             const std::uint8_t* mk = mask + M.base;
             const std::uint8_t* dm = dof + M.base;
             const float* pm = p + M.base;
             const float pi = p[i];
             float s = 0.0f;
-            int nf = 0;
 #pragma unroll
             for (int f = 0; f < 4; ++f)
             {
-                const std::int64_t j = hs_nb(H, mk, r, c, kDr[f], kDc[f]);
-                if (j == local) continue;
-                ++nf;
-                if (dm[j]) s += pm[j];
+                const std::int64_t j = hs_nb(q.hs, mk, r, c, kDr[f], kDc[f]);
+                if (j == l) continue;
+                s += pi - (dm[j] ? pm[j] : 0.0f);
             }
-            v = static_cast<float>((H.inv_dt + H.DA * nf) * pi - H.DA * s);
-            pap = static_cast<double>(pi) * v;
+            v = q.inv_dt_f * pi + q.DA_f * s;
+            pap = pi * v;
         }
         Ap[i] = v;
     }
-    warp_add(&cur[m * kHsSlot + 0], pap);
+    block_partial_f(pap, false, part, P.n / kPackAlign, 0);
 }
 
+// alpha = r.z / p.Ap (once per block); x += alpha p; r -= alpha Ap; z = M^-1 r;
+// block partials of r.z and r.r
 __global__ void ens_hs_update(Packed P, const int* __restrict__ done, const double* __restrict__ prev,
                               const float* __restrict__ inv_diag, const float* __restrict__ p,
                               const float* __restrict__ Ap, float* __restrict__ x, float* __restrict__ r,
-                              float* __restrict__ zz, double* __restrict__ cur)
+                              float* __restrict__ zz, const double* __restrict__ cur, double* __restrict__ part)
 {
     LSDTT_COUNT();
     const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     const int m = member_of(P, i < P.n ? i : P.n - 1);
     if (done[m]) return;
-    const double pap = cur[m * kHsSlot + 0];
-    const float alpha = (pap > 0.0) ? static_cast<float>(prev[m * kHsSlot + 1] / pap) : 0.0f;
-    double rz = 0.0, rr = 0.0;
+    __shared__ float s_alpha;
+    if (threadIdx.x == 0)
+    {
+        const double pap = cur[m * kHsSlot + 0];
+        s_alpha = (pap > 0.0) ? static_cast<float>(prev[m * kHsSlot + 1] / pap) : 0.0f;
+    }
+    __syncthreads();
+    const float alpha = s_alpha;
+    float rz = 0.0f, rr = 0.0f;
     if (i < P.n)
     {
         x[i] += alpha * p[i];
@@ -443,24 +522,29 @@ __global__ void ens_hs_update(Packed P, const int* __restrict__ done, const doub
         r[i] = ri;
         const float zi = ri * inv_diag[i];
         zz[i] = zi;
-        rz = static_cast<double>(ri) * zi;
-        rr = static_cast<double>(ri) * ri;
+        rz = ri * zi;
+        rr = ri * ri;
     }
-    warp_add(&cur[m * kHsSlot + 1], rz);
-    warp_add(&cur[m * kHsSlot + 2], rr);
+    block_partial_f(rz, false, part, P.n / kPackAlign, 0);
+    block_partial_f(rr, false, part, P.n / kPackAlign, 1);
 }
 
+// beta = r.z / r_old.z_old (once per block); p = z + beta p
 __global__ void ens_hs_direction(Packed P, const int* __restrict__ done, const double* __restrict__ prev,
                                  const double* __restrict__ cur, const float* __restrict__ zz, float* __restrict__ p)
 {
     LSDTT_COUNT();
     const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i >= P.n) return;
-    const int m = member_of(P, i);
+    const int m = member_of(P, i < P.n ? i : P.n - 1);
     if (done[m]) return;
-    const double ro = prev[m * kHsSlot + 1];
-    const float beta = (ro > 0.0) ? static_cast<float>(cur[m * kHsSlot + 1] / ro) : 0.0f;
-    p[i] = zz[i] + beta * p[i];
+    __shared__ float s_beta;
+    if (threadIdx.x == 0)
+    {
+        const double ro = prev[m * kHsSlot + 1];
+        s_beta = (ro > 0.0) ? static_cast<float>(cur[m * kHsSlot + 1] / ro) : 0.0f;
+    }
+    __syncthreads();
+    if (i < P.n) p[i] = zz[i] + s_beta * p[i];
 }
 
 // After iteration `it` (0-based, it + 1 a multiple of 4 or the last one):
@@ -532,57 +616,31 @@ __global__ void ens_uplift(Packed P, const EnsParams* __restrict__ prm, const st
     z[i] = v;
 }
 
-__device__ __forceinline__ void warp_max_mapped(double* dst, double v)
-{
-    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
-    if ((threadIdx.x & 31) == 0)
-    {
-        unsigned long long u = __double_as_longlong(v);
-        u = (u & 0x8000000000000000ull) ? ~u : (u | 0x8000000000000000ull);
-        atomicMax(reinterpret_cast<unsigned long long*>(dst), u);
-    }
-}
-
-// lem_stats (lem.cu) per member: [0] sum before, [1] sum after, [2] erosion
-// sum, [3] valid count, [4..7] mapped maxima (before, after, |dz|, erosion).
+// lem_stats (lem.cu) per member, as block partials: [0] sum of (after -
+// before), [1] unused, [2] erosion sum, [3] valid count, [4..7] maxima
+// (before, after, |dz|, erosion). Differences are formed per cell (exact
+// for nearby elevations) before any sum, so FP32 warp sums suffice.
 __global__ void ens_stats(Packed P, const EnsParams* __restrict__ prm, const std::uint8_t* __restrict__ mask,
-                          const float* __restrict__ zb, const float* __restrict__ za, double* __restrict__ acc)
+                          const float* __restrict__ zb, const float* __restrict__ za, double* __restrict__ part)
 {
     LSDTT_COUNT();
     const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     const int m = member_of(P, i < P.n ? i : P.n - 1);
-    double sb = 0, sa = 0, mb = -1e30, ma = -1e30, ml = 0, se = 0, me = 0, nv = 0;
+    float v[8] = {0.0f, 0.0f, 0.0f, 0.0f, -1e30f, -1e30f, 0.0f, 0.0f};
     if (i < P.n && mask[i])
     {
-        const double b = zb[i], a = za[i];
-        sb = b;
-        sa = a;
-        mb = b;
-        ma = a;
-        ml = fabs(a - b);
-        const double ero = b - (a - static_cast<double>(prm[m].udz));
-        if (ero > 0.0) { se = ero; me = ero; }
-        nv = 1;
+        const float b = zb[i], a = za[i];
+        v[0] = a - b;
+        v[4] = b;
+        v[5] = a;
+        v[6] = fabsf(a - b);
+        const float ero = (b - a) + prm[m].udz;
+        if (ero > 0.0f) { v[2] = ero; v[7] = ero; }
+        v[3] = 1.0f;
     }
-    double* A = acc + m * 8;
-    warp_add(&A[0], sb);
-    warp_add(&A[1], sa);
-    warp_add(&A[2], se);
-    warp_add(&A[3], nv);
-    warp_max_mapped(&A[4], mb);
-    warp_max_mapped(&A[5], ma);
-    warp_max_mapped(&A[6], ml);
-    warp_max_mapped(&A[7], me);
-}
-
-double unmap_max_host(double stored)
-{
-    unsigned long long u;
-    std::memcpy(&u, &stored, sizeof(u));
-    u = (u & 0x8000000000000000ull) ? (u & ~0x8000000000000000ull) : ~u;
-    double v;
-    std::memcpy(&v, &u, sizeof(v));
-    return v;
+    const std::int64_t nblk = P.n / kPackAlign;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) block_partial_f(v[q], q >= 4, part, nblk, q);
 }
 
 bool exact_area(double dw, std::int64_t nv)
@@ -626,6 +684,7 @@ struct lsdtt_gpu_ensemble
     double *hs_bb = nullptr, *hs_acc = nullptr;
     int *done = nullptr, *iters = nullptr;
     double* stats_acc = nullptr;
+    double* part = nullptr;  // block partials [8][packed / 256]
     int* flags = nullptr;
     // pinned host mirrors
     double* h_stats = nullptr;
@@ -642,6 +701,7 @@ struct lsdtt_gpu_ensemble
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     cudaStream_t own = nullptr;  // private stream: the legacy default stream cannot be captured
+    cudaEvent_t ev_in = nullptr, ev_out = nullptr;  // order the private stream after/before the caller's
     std::uint32_t tail = 0;      // tuned: levels of at most `tail` cells run in one block (0: none)
     int ov_fill = 0, ov_it = 0;  // one-shot schedule override for the next capture
     lsdtt_gpu_ensemble_info info{};
@@ -666,12 +726,14 @@ void free_ensemble(lsdtt_gpu_ensemble* E)
     if (E->graph) cudaGraphDestroy(E->graph);
     void* bufs[] = {E->d_pm, E->d_prm, E->blk_member, E->tile_member, E->z, E->zf, E->zsp, E->zpre, E->kind, E->bflag, E->dirty, E->oflag, E->pos, E->nd, E->area, E->order, E->lstart, E->lcount,
                     E->lfill, E->maxd, E->dof, E->invd, E->b, E->x, E->r, E->p, E->zz, E->Ap, E->hs_bb, E->hs_acc,
-                    E->done, E->iters, E->stats_acc, E->flags};
+                    E->done, E->iters, E->stats_acc, E->part, E->flags};
     for (void* q : bufs) cudaFree(q);
     void* hb[] = {E->h_stats, E->h_flags, E->h_iters, E->h_maxd, E->h_err};
     for (void* q : hb) cudaFreeHost(q);
     if (E->f) lsdtt_gpu_flow_destroy(E->f);
     if (E->own) cudaStreamDestroy(E->own);
+    if (E->ev_in) cudaEventDestroy(E->ev_in);
+    if (E->ev_out) cudaEventDestroy(E->ev_out);
     delete E;
 }
 
@@ -724,9 +786,13 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
     ens_dirty_init<<<grid_blocks(E->T, 256), 256, 0, st>>>(E->T, E->tile_member, E->d_prm, E->dirty,
                                                            E->dirty + E->T);
     const dim3 fblock(32, 8);
+    const double cells = static_cast<double>(E->member_cells);
     auto relax = [&](int pass) {
-        ens_fill_relax<<<E->T, fblock, 0, st>>>(E->P, E->d_prm, E->tile_member, E->z, E->kind, E->zf, E->flags,
-                                                E->dirty + (pass & 1) * E->T, E->dirty + ((pass + 1) & 1) * E->T);
+        // Algorithmic bytes per pass: z 4 + mask 1 in, filled value 4 out.
+        LSDTT_TIMED("ens_fill_relax", 9.0 * cells, st,
+                    (ens_fill_relax<<<E->T, fblock, 0, st>>>(E->P, E->d_prm, E->tile_member, E->z, E->kind, E->zf,
+                                                             E->flags, E->dirty + (pass & 1) * E->T,
+                                                             E->dirty + ((pass + 1) & 1) * E->T)));
     };
     int passes = 0;
     if (eager)
@@ -755,7 +821,9 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
     // 1. D8 receivers, outlets, s-vector (contributing counts, depth)
     lsdtt_gpu_flow* f = E->f;
     cudaMemsetAsync(f->derr, 0, sizeof(unsigned long long) * 4, st);
-    ens_receivers<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->zf, E->mask, f->receiver, f->dir, f->derr);
+    // Algorithmic bytes: z 4 + mask 1 in, direction 1 + int64 receiver 8 out.
+    LSDTT_TIMED("ens_d8_receivers", 14.0 * cells, st,
+                (ens_receivers<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->zf, E->mask, f->receiver, f->dir, f->derr)));
     ens_outlet_flag<<<nb, 256, 0, st>>>(N, E->mask, f->dir, E->oflag);
     f->ws.used = 0;
     e = exclusive_scan<std::uint8_t, std::int64_t>(E->oflag, N, E->pos, f->dscal + 1, f->ws, st);
@@ -765,6 +833,7 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
     e = build_stack(f, false, st, &E->P);
     if (e != cudaSuccess) return e;
     ens_area<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->mask, f->sv_size, E->area);
+    ens_kam<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->mask, f->receiver, E->area);
     // 2. depth levels
     const std::uint32_t cap = eager ? static_cast<std::uint32_t>(N + 1) : static_cast<std::uint32_t>(E->depth_cap);
     cudaMemsetAsync(E->maxd, 0, sizeof(std::uint32_t), st);
@@ -857,10 +926,16 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
     // 4. hillslope: Jacobi-PCG per member
     const std::size_t slot_bytes = sizeof(double) * kHsSlot * M;
     const int itmax = eager ? E->max_iter_all : E->it_cap;
-    cudaMemsetAsync(E->hs_bb, 0, sizeof(double) * M, st);
+    const std::int64_t nblk = N / kPackAlign;
+    auto reduce = [&](int nq, unsigned max_mask, const int* dn, double* dst, int stride, int off) {
+        const unsigned warps = static_cast<unsigned>(M * nq);
+        ens_member_reduce<<<(warps + 3) / 4, 128, 0, st>>>(E->P, nq, max_mask, E->part, nblk, dn, dst, stride, off);
+    };
     cudaMemsetAsync(E->hs_acc, 0, slot_bytes * (static_cast<std::size_t>(itmax) + 1), st);
-    ens_hs_setup<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->mask, E->zsp, E->dof, E->invd, E->b, E->hs_bb);
-    ens_hs_init<<<nb, 256, 0, st>>>(E->P, E->b, E->invd, E->x, E->r, E->p, E->hs_acc);
+    ens_hs_setup<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->mask, E->zsp, E->dof, E->invd, E->b, E->part);
+    reduce(1, 0u, nullptr, E->hs_bb, 1, 0);
+    ens_hs_init<<<nb, 256, 0, st>>>(E->P, E->b, E->invd, E->x, E->r, E->p, E->part);
+    reduce(1, 0u, nullptr, E->hs_acc, kHsSlot, 1);
     ens_hs_start<<<mb, 128, 0, st>>>(M, E->d_prm, E->hs_bb, E->done, E->iters);
     int it = 0;
     for (; it < itmax;)
@@ -870,8 +945,15 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
         {
             const double* prev = E->hs_acc + static_cast<std::size_t>(kHsSlot) * M * it;
             double* cur = E->hs_acc + static_cast<std::size_t>(kHsSlot) * M * (it + 1);
-            ens_hs_apply<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->mask, E->dof, E->done, E->p, E->Ap, cur);
-            ens_hs_update<<<nb, 256, 0, st>>>(E->P, E->done, prev, E->invd, E->p, E->Ap, E->x, E->r, E->zz, cur);
+            // Algorithmic bytes: Ap = A p with p.Ap 8 B/cell; the update 24 B/cell.
+            LSDTT_TIMED("ens_hillslope_apply", 8.0 * cells, st,
+                        (ens_hs_apply<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->mask, E->dof, E->done, E->p, E->Ap,
+                                                          E->part)));
+            reduce(1, 0u, E->done, cur, kHsSlot, 0);
+            LSDTT_TIMED("ens_hillslope_update", 24.0 * cells, st,
+                        (ens_hs_update<<<nb, 256, 0, st>>>(E->P, E->done, prev, E->invd, E->p, E->Ap, E->x, E->r,
+                                                           E->zz, cur, E->part)));
+            reduce(2, 0u, E->done, cur, kHsSlot, 1);
             ens_hs_direction<<<nb, 256, 0, st>>>(E->P, E->done, prev, cur, E->zz, E->p);
         }
         if (eager) cudaMemsetAsync(E->flags + 5, 0, sizeof(int), st);
@@ -891,8 +973,8 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
     ens_hs_finish<<<nb, 256, 0, st>>>(N, E->dof, E->zsp, E->x, E->z);
     // 5. uplift + boundary restore, statistics, flags to the host
     ens_uplift<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->mask, E->bflag, E->zf, E->z);
-    cudaMemsetAsync(E->stats_acc, 0, sizeof(double) * 8 * M, st);
-    ens_stats<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->mask, E->zf, E->z, E->stats_acc);
+    ens_stats<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->mask, E->zf, E->z, E->part);
+    reduce(8, 0xf0u, nullptr, E->stats_acc, 8, 0);
     cudaMemcpyAsync(E->h_stats, E->stats_acc, sizeof(double) * 8 * M, cudaMemcpyDeviceToHost, st);
     cudaMemcpyAsync(E->h_flags, E->flags, sizeof(int) * kFlags, cudaMemcpyDeviceToHost, st);
     cudaMemcpyAsync(E->h_iters, E->iters, sizeof(int) * M, cudaMemcpyDeviceToHost, st);
@@ -946,10 +1028,10 @@ void fill_stats(const lsdtt_gpu_ensemble* E, lsdtt_gpu_lem_stats* stats)
         const double inv_dt = 1.0 / static_cast<double>(o.timestep);
         const double inv_n = nv > 0 ? 1.0 / nv : 0.0;
         lsdtt_gpu_lem_stats& s = stats[m];
-        s.delta_max_elevation = static_cast<float>(std::fabs(unmap_max_host(A[5]) - unmap_max_host(A[4])));
-        s.delta_mean_elevation = static_cast<float>(std::fabs((A[1] - A[0]) * inv_n));
-        s.max_local_elevation_change = static_cast<float>(unmap_max_host(A[6]));
-        const double me = unmap_max_host(A[7]);
+        s.delta_max_elevation = static_cast<float>(std::fabs(A[5] - A[4]));
+        s.delta_mean_elevation = static_cast<float>(std::fabs(A[0] * inv_n));
+        s.max_local_elevation_change = static_cast<float>(A[6]);
+        const double me = A[7];
         s.mean_erosion_rate = static_cast<float>(A[2] * inv_n * inv_dt);
         s.max_erosion_rate = static_cast<float>((me > 0 ? me : 0.0) * inv_dt);
         s.hillslope_iterations = E->h_iters[m];
@@ -1043,6 +1125,10 @@ int lsdtt_gpu_ensemble_create(const lsdtt_gpu_member* members, int32_t n_members
         q.hs.DA = static_cast<double>(o.hillslope_diffusivity) / (g.cell_size * g.cell_size);
         q.hs.inv_dt = 1.0 / static_cast<double>(o.timestep);
         q.hs.U = 0.0;
+        for (int k = 0; k < 5; ++k) q.hs_invd[k] = static_cast<float>(1.0 / (q.hs.inv_dt + q.hs.DA * k));
+        q.inv_dt_f = static_cast<float>(q.hs.inv_dt);
+        q.DA_f = static_cast<float>(q.hs.DA);
+        q.U_f = 0.0f;
         q.inv_card = static_cast<float>(1.0 / g.cell_size);
         q.inv_diag = static_cast<float>(1.0 / (g.cell_size * 1.4142135623730950488));
         q.fill_on = o.fill_min_slope > 0.0f ? 1 : 0;
@@ -1093,7 +1179,9 @@ int lsdtt_gpu_ensemble_create(const lsdtt_gpu_member* members, int32_t n_members
         return s;
     }
     E->mask = E->f->mask;  // the stack reads the engine's mask
-    if (cudaStreamCreateWithFlags(&E->own, cudaStreamNonBlocking) != cudaSuccess)
+    if (cudaStreamCreateWithFlags(&E->own, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&E->ev_in, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&E->ev_out, cudaEventDisableTiming) != cudaSuccess)
     {
         free_ensemble(E);
         return fail(LSDTT_GPU_ECUDA, std::string(who) + ": stream creation failed");
@@ -1136,6 +1224,7 @@ int lsdtt_gpu_ensemble_create(const lsdtt_gpu_member* members, int32_t n_members
     alloc(&E->done, static_cast<std::size_t>(n_members));
     alloc(&E->iters, static_cast<std::size_t>(n_members));
     alloc(&E->stats_acc, 8 * static_cast<std::size_t>(n_members));
+    alloc(&E->part, 8 * (n / kPackAlign));
     alloc(&E->flags, kFlags);
     if (e == cudaSuccess) e = cudaMallocHost(&E->h_stats, sizeof(double) * 8 * n_members);
     if (e == cudaSuccess) e = cudaMallocHost(&E->h_flags, sizeof(int) * kFlags);
@@ -1219,10 +1308,12 @@ int lsdtt_gpu_ensemble_step(lsdtt_gpu_ensemble* E, int32_t n_steps, lsdtt_gpu_le
     const char* who = "lsdtt_gpu_ensemble_step";
     if (!E || n_steps < 0) return fail(LSDTT_GPU_EINVAL, std::string(who) + ": bad argument");
     if (!E->ready) return fail(LSDTT_GPU_ESTATE, std::string(who) + ": every member needs a surface and a mask");
-    // Work runs on the handle's own stream, after the caller's stream.
-    cudaError_t e0 = cudaStreamSynchronize(static_cast<cudaStream_t>(stream));
-    if (e0 != cudaSuccess) return cuda_fail(e0, who);
+    // Work runs on the handle's own stream, ordered after the caller's
+    // stream; the caller's stream waits for it at the end.
+    cudaStream_t user = static_cast<cudaStream_t>(stream);
     cudaStream_t st = E->own;
+    cudaEventRecord(E->ev_in, user);
+    cudaStreamWaitEvent(st, E->ev_in, 0);
     const bool graph_ok = E->use_graph && !profiling_enabled();
     for (int s = 0; s < n_steps; ++s)
     {
@@ -1286,6 +1377,8 @@ int lsdtt_gpu_ensemble_step(lsdtt_gpu_ensemble* E, int32_t n_steps, lsdtt_gpu_le
             return fail(LSDTT_GPU_ENOCONV, std::string(who) + ": a member's hillslope Jacobi-PCG did not reach its "
                                                               "relative residual within hillslope_max_iter");
     }
+    cudaEventRecord(E->ev_out, st);
+    cudaStreamWaitEvent(user, E->ev_out, 0);
     E->info.fill_pass_cap = E->fill_cap;
     E->info.depth_cap = E->depth_cap;
     E->info.sweep_split_level = E->split;
@@ -1293,6 +1386,22 @@ int lsdtt_gpu_ensemble_step(lsdtt_gpu_ensemble* E, int32_t n_steps, lsdtt_gpu_le
     E->info.hillslope_iteration_cap = E->it_cap;
     if (stats) fill_stats(E, stats);
     return LSDTT_GPU_OK;
+}
+
+int lsdtt_gpu_ensemble_upload(lsdtt_gpu_ensemble* E, const float* z_host, void* stream)
+{
+    if (!E || !z_host) return fail(LSDTT_GPU_EINVAL, "lsdtt_gpu_ensemble_upload: null argument");
+    const cudaError_t e = cudaMemcpyAsync(E->z, z_host, sizeof(float) * E->N, cudaMemcpyHostToDevice,
+                                          static_cast<cudaStream_t>(stream));
+    return e == cudaSuccess ? LSDTT_GPU_OK : cuda_fail(e, "lsdtt_gpu_ensemble_upload");
+}
+
+int lsdtt_gpu_ensemble_download(const lsdtt_gpu_ensemble* E, float* z_host, void* stream)
+{
+    if (!E || !z_host) return fail(LSDTT_GPU_EINVAL, "lsdtt_gpu_ensemble_download: null argument");
+    const cudaError_t e = cudaMemcpyAsync(z_host, E->z, sizeof(float) * E->N, cudaMemcpyDeviceToHost,
+                                          static_cast<cudaStream_t>(stream));
+    return e == cudaSuccess ? LSDTT_GPU_OK : cuda_fail(e, "lsdtt_gpu_ensemble_download");
 }
 
 int lsdtt_gpu_ensemble_override_schedule(lsdtt_gpu_ensemble* E, int32_t fill_pass_cap, int32_t hillslope_iteration_cap)

@@ -68,17 +68,8 @@ __global__ void hs_setup(Hs H, const std::uint8_t* __restrict__ mask, const std:
             inv_diag[i] = 0.0f;
         }
     }
-    for (int o = 16; o > 0; o >>= 1)
-    {
-        bb += __shfl_down_sync(0xffffffffu, bb, o);
-        fin = fmax(fin, __shfl_down_sync(0xffffffffu, fin, o));
-    }
-    if ((threadIdx.x & 31) == 0)
-    {
-        atomicAdd(&acc[0], bb);
-        // |F| >= 0: the bit pattern orders like the value.
-        atomicMax(reinterpret_cast<unsigned long long*>(&acc[1]), __double_as_longlong(fin));
-    }
+    block_atomic_add(&acc[0], bb);
+    block_atomic_max_nonneg(&acc[1], fin);
 }
 
 // x = 0, r = b, zz = M^-1 r, p = zz, acc[2] = r.zz
@@ -97,8 +88,7 @@ __global__ void hs_cg_init(std::int64_t n, const float* __restrict__ b, const fl
         p[i] = zi;
         rz = static_cast<double>(ri) * zi;
     }
-    for (int o = 16; o > 0; o >>= 1) rz += __shfl_down_sync(0xffffffffu, rz, o);
-    if ((threadIdx.x & 31) == 0) atomicAdd(&acc[2], rz);
+    block_atomic_add(&acc[2], rz);
 }
 
 // Ap = J p (matrix-free) fused with p.Ap  -> acc_it[0]
@@ -131,8 +121,7 @@ __global__ void hs_apply(Hs H, const std::uint8_t* __restrict__ mask, const std:
         }
         Ap[i] = v;
     }
-    for (int o = 16; o > 0; o >>= 1) pap += __shfl_down_sync(0xffffffffu, pap, o);
-    if ((threadIdx.x & 31) == 0) atomicAdd(&acc_it[0], pap);
+    block_atomic_add(&acc_it[0], pap);
 }
 
 // alpha = rz/pAp; x += alpha p; r -= alpha Ap; zz = M^-1 r; acc_it[1] = r.zz, acc_it[2] = r.r
@@ -143,8 +132,16 @@ __global__ void hs_update(std::int64_t n, const double* __restrict__ rz_prev, co
 {
     LSDTT_COUNT();
     const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    const double pap = acc_it[0];
-    const float alpha = (pap > 0.0) ? static_cast<float>(*rz_prev / pap) : 0.0f;
+    // alpha once per block: a per-thread FP64 division costs more than the
+    // kernel's memory traffic on this part.
+    __shared__ float s_alpha;
+    if (threadIdx.x == 0)
+    {
+        const double pap = acc_it[0];
+        s_alpha = (pap > 0.0) ? static_cast<float>(*rz_prev / pap) : 0.0f;
+    }
+    __syncthreads();
+    const float alpha = s_alpha;
     double rz = 0.0, rr = 0.0;
     if (i < n)
     {
@@ -156,16 +153,8 @@ __global__ void hs_update(std::int64_t n, const double* __restrict__ rz_prev, co
         rz = static_cast<double>(ri) * zi;
         rr = static_cast<double>(ri) * ri;
     }
-    for (int o = 16; o > 0; o >>= 1)
-    {
-        rz += __shfl_down_sync(0xffffffffu, rz, o);
-        rr += __shfl_down_sync(0xffffffffu, rr, o);
-    }
-    if ((threadIdx.x & 31) == 0)
-    {
-        atomicAdd(&acc_out[1], rz);
-        atomicAdd(&acc_out[2], rr);
-    }
+    block_atomic_add(&acc_out[1], rz);
+    block_atomic_add(&acc_out[2], rr);
 }
 
 // beta = rz_new / rz_old; p = zz + beta p
@@ -174,10 +163,14 @@ __global__ void hs_direction(std::int64_t n, const double* __restrict__ rz_old, 
 {
     LSDTT_COUNT();
     const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const double ro = *rz_old;
-    const float beta = (ro > 0.0) ? static_cast<float>(*rz_new / ro) : 0.0f;
-    p[i] = zz[i] + beta * p[i];
+    __shared__ float s_beta;
+    if (threadIdx.x == 0)
+    {
+        const double ro = *rz_old;
+        s_beta = (ro > 0.0) ? static_cast<float>(*rz_new / ro) : 0.0f;
+    }
+    __syncthreads();
+    if (i < n) p[i] = zz[i] + s_beta * p[i];
 }
 
 __global__ void hs_finish(std::int64_t n, const std::uint8_t* __restrict__ dof, const float* __restrict__ z,
@@ -408,18 +401,9 @@ __global__ void hsn_eval(HsN P, const std::uint8_t* __restrict__ mask, const std
         F[i] = 0.0;
         alpha[i] = make_float4(1.f, 1.f, 1.f, 1.f);
     }
-    for (int o = 16; o > 0; o >>= 1)
-    {
-        finf = fmax(finf, __shfl_down_sync(0xffffffffu, finf, o));
-        f2 += __shfl_down_sync(0xffffffffu, f2, o);
-        ratio = fmax(ratio, __shfl_down_sync(0xffffffffu, ratio, o));
-    }
-    if ((threadIdx.x & 31) == 0)
-    {
-        atomicMax(reinterpret_cast<unsigned long long*>(&acc[0]), __double_as_longlong(finf));
-        atomicAdd(&acc[1], f2);
-        atomicMax(reinterpret_cast<unsigned long long*>(&acc[2]), __double_as_longlong(ratio));
-    }
+    block_atomic_max_nonneg(&acc[0], finf);
+    block_atomic_add(&acc[1], f2);
+    block_atomic_max_nonneg(&acc[2], ratio);
 }
 
 // PCG set-up for A(alpha) x = -F: inverse diagonal, b, x = 0, r = b,
@@ -457,16 +441,8 @@ __global__ void hsn_pcg_init(HsN P, const std::uint8_t* __restrict__ mask, const
         rz = static_cast<double>(bi) * zi;
         bb = static_cast<double>(bi) * bi;
     }
-    for (int o = 16; o > 0; o >>= 1)
-    {
-        rz += __shfl_down_sync(0xffffffffu, rz, o);
-        bb += __shfl_down_sync(0xffffffffu, bb, o);
-    }
-    if ((threadIdx.x & 31) == 0)
-    {
-        atomicAdd(&acc[0], rz);
-        atomicAdd(&acc[1], bb);
-    }
+    block_atomic_add(&acc[0], rz);
+    block_atomic_add(&acc[1], bb);
 }
 
 __global__ void hsn_apply(HsN P, const std::uint8_t* __restrict__ mask, const std::uint8_t* __restrict__ dof,
@@ -500,8 +476,7 @@ __global__ void hsn_apply(HsN P, const std::uint8_t* __restrict__ mask, const st
         }
         Ap[i] = v;
     }
-    for (int o = 16; o > 0; o >>= 1) pap += __shfl_down_sync(0xffffffffu, pap, o);
-    if ((threadIdx.x & 31) == 0) atomicAdd(&acc_it[0], pap);
+    block_atomic_add(&acc_it[0], pap);
 }
 
 // z_try = z + lambda * dz on DOFs (double)
@@ -540,8 +515,14 @@ __global__ void hsf_update(std::int64_t n, const double* __restrict__ rz_prev, c
 {
     LSDTT_COUNT();
     const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    const double pap = acc_it[0];
-    const float alpha = (pap > 0.0) ? static_cast<float>(*rz_prev / pap) : 0.0f;
+    __shared__ float s_alpha;
+    if (threadIdx.x == 0)
+    {
+        const double pap = acc_it[0];
+        s_alpha = (pap > 0.0) ? static_cast<float>(*rz_prev / pap) : 0.0f;
+    }
+    __syncthreads();
+    const float alpha = s_alpha;
     double rr = 0.0;
     if (i < n)
     {
@@ -552,8 +533,7 @@ __global__ void hsf_update(std::int64_t n, const double* __restrict__ rz_prev, c
         r[i] = ri;
         rr = static_cast<double>(ri) * ri;
     }
-    for (int o = 16; o > 0; o >>= 1) rr += __shfl_down_sync(0xffffffffu, rr, o);
-    if ((threadIdx.x & 31) == 0) atomicAdd(&acc_out[2], rr);
+    block_atomic_add(&acc_out[2], rr);
 }
 
 // The network's input: the Jacobi-scaled residual D^-1 r (metres), which
@@ -591,16 +571,8 @@ __global__ void hsf_smooth(std::int64_t n, const float* __restrict__ invd, const
         rz = static_cast<double>(ri) * zi;
         roz = static_cast<double>(ro[i]) * zi;
     }
-    for (int o = 16; o > 0; o >>= 1)
-    {
-        rz += __shfl_down_sync(0xffffffffu, rz, o);
-        roz += __shfl_down_sync(0xffffffffu, roz, o);
-    }
-    if ((threadIdx.x & 31) == 0)
-    {
-        atomicAdd(&acc_out[1], rz);
-        atomicAdd(&acc_out[3], roz);
-    }
+    block_atomic_add(&acc_out[1], rz);
+    block_atomic_add(&acc_out[3], roz);
 }
 
 // beta = (r.z - r_old.z) / rz_old; p = z + beta p (beta = 0 at a restart)
@@ -609,10 +581,14 @@ __global__ void hsf_direction(std::int64_t n, const double* __restrict__ rz_old,
 {
     LSDTT_COUNT();
     const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const double ro = *rz_old;
-    const float beta = (ro > 0.0) ? static_cast<float>((acc_new[1] - acc_new[3]) / ro) : 0.0f;
-    p[i] = z[i] + beta * p[i];
+    __shared__ float s_beta;
+    if (threadIdx.x == 0)
+    {
+        const double ro = *rz_old;
+        s_beta = (ro > 0.0) ? static_cast<float>((acc_new[1] - acc_new[3]) / ro) : 0.0f;
+    }
+    __syncthreads();
+    if (i < n) p[i] = z[i] + s_beta * p[i];
 }
 
 // Explicit residual res = b - A x, evaluated in FP64 from the FP32 iterate and
@@ -652,16 +628,8 @@ __global__ void hsn_explicit(HsN P, const std::uint8_t* __restrict__ mask, const
         r[i] = static_cast<float>(res);
         rr = res * res;
     }
-    for (int o = 16; o > 0; o >>= 1)
-    {
-        rr += __shfl_down_sync(0xffffffffu, rr, o);
-        fl += __shfl_down_sync(0xffffffffu, fl, o);
-    }
-    if ((threadIdx.x & 31) == 0)
-    {
-        atomicAdd(&acc[0], rr);
-        atomicAdd(&acc[1], fl);
-    }
+    block_atomic_add(&acc[0], rr);
+    block_atomic_add(&acc[1], fl);
 }
 
 // Jacobi-PCG restart from the residual in r: z = p = D^-1 r, acc[0] = r.z
@@ -677,8 +645,7 @@ __global__ void hsn_restart(std::int64_t n, const float* __restrict__ invd, cons
         p[i] = zi;
         rz = static_cast<double>(r[i]) * zi;
     }
-    for (int o = 16; o > 0; o >>= 1) rz += __shfl_down_sync(0xffffffffu, rz, o);
-    if ((threadIdx.x & 31) == 0) atomicAdd(&acc[0], rz);
+    block_atomic_add(&acc[0], rz);
 }
 
 __global__ void hsn_pair_finish(std::int64_t n, const float* __restrict__ x_final, const float* __restrict__ invd,

@@ -75,34 +75,24 @@ __global__ void lem_stats(std::int64_t n, const std::uint8_t* __restrict__ mask,
         else
             keys[i] = 0xffffffffull;  // sorts after every finite |dz|
     }
-    for (int o = 16; o > 0; o >>= 1)
-    {
-        sb += __shfl_down_sync(0xffffffffu, sb, o);
-        sa += __shfl_down_sync(0xffffffffu, sa, o);
-        se += __shfl_down_sync(0xffffffffu, se, o);
-        nv += __shfl_down_sync(0xffffffffu, nv, o);
-        mb = fmax(mb, __shfl_down_sync(0xffffffffu, mb, o));
-        ma = fmax(ma, __shfl_down_sync(0xffffffffu, ma, o));
-        ml = fmax(ml, __shfl_down_sync(0xffffffffu, ml, o));
-        me = fmax(me, __shfl_down_sync(0xffffffffu, me, o));
-    }
-    if ((threadIdx.x & 31) == 0)
-    {
-        atomicAdd(&acc[0], sb);
-        atomicAdd(&acc[1], sa);
-        atomicAdd(&acc[2], se);
-        atomicAdd(&acc[3], nv);
-        auto amax = [](double* p, double v) {
-            // order-preserving map of doubles to unsigned for atomicMax
-            unsigned long long u = __double_as_longlong(v);
+    block_atomic_add(&acc[0], sb);
+    block_atomic_add(&acc[1], sa);
+    block_atomic_add(&acc[2], se);
+    block_atomic_add(&acc[3], nv);
+    auto amax = [](double* p, double v) {
+        // order-preserving map of doubles to unsigned for atomicMax
+        const double t = block_reduce_d(v, true);
+        if (threadIdx.x == 0)
+        {
+            unsigned long long u = __double_as_longlong(t);
             u = (u & 0x8000000000000000ull) ? ~u : (u | 0x8000000000000000ull);
             atomicMax(reinterpret_cast<unsigned long long*>(p), u);
-        };
-        amax(&acc[4], mb);
-        amax(&acc[5], ma);
-        amax(&acc[6], ml);
-        amax(&acc[7], me);
-    }
+        }
+    };
+    amax(&acc[4], mb);
+    amax(&acc[5], ma);
+    amax(&acc[6], ml);
+    amax(&acc[7], me);
 }
 
 double unmap_max(double stored)

@@ -18,27 +18,49 @@ struct SpParams
     int n_is_one;
 };
 
+// slope^e for the Newton iteration. The stream-power exponents the
+// configurations use (n = 1, 1.5, 2, hence e in {0.5, 1, 1.5, 2}) take
+// exact identities with one or two correct roundings (x*x, x, sqrt(x),
+// x*sqrt(x)), which are at least as accurate as the general double pow
+// and avoid its FP64 cost inside the level-ordered sweep; any other
+// exponent takes pow.
+__device__ __forceinline__ double sp_pow(double x, double e)
+{
+    if (e == 2.0) return __dmul_rn(x, x);
+    if (e == 1.0) return x;
+    if (e == 0.5) return __dsqrt_rn(x);
+    if (e == 1.5) return __dmul_rn(x, __dsqrt_rn(x));
+    return pow(x, e);
+}
+
+// K * A^m of one node in the reference's double arithmetic
+// (stream_power_cpu.cpp:236-262), or -1 when the node is below the
+// incision threshold (not eroded). area_d is the accumulate() total.
+__device__ __forceinline__ double sp_kam(const SpParams& P, double area_d, float Ki)
+{
+    double area = area_d;
+    if (P.divide_by_dx) area = __ddiv_rn(area, static_cast<double>(P.dx));
+    if (P.threshold > 0.0f && area < static_cast<double>(P.threshold)) return -1.0;
+    return __dmul_rn(static_cast<double>(Ki), pow(area, static_cast<double>(P.m)));
+}
+
 // The implicit update of node `flat` from its receiver's final elevation
-// (stream_power_cpu.cpp:236-318). Any receiver-before-donor order gives the
-// reference's bits: a node reads only z_old[self] and z[receiver]. Indices
-// are those of the arrays passed (n = their length).
-__device__ __forceinline__ void sp_node(const SpParams& P, std::int64_t n, std::int64_t flat,
-                                        const std::int64_t* __restrict__ receiver, const std::uint8_t* __restrict__ dir,
-                                        const double* __restrict__ area_d, const float* __restrict__ z_old,
-                                        const float* __restrict__ kfield, float* __restrict__ z)
+// (stream_power_cpu.cpp:263-318) given its kam = sp_kam(...). Any
+// receiver-before-donor order gives the reference's bits: a node reads only
+// z_old[self] and z[receiver]. Indices are those of the arrays passed
+// (n = their length).
+__device__ __forceinline__ void sp_node_kam(const SpParams& P, std::int64_t n, std::int64_t flat,
+                                            const std::int64_t* __restrict__ receiver,
+                                            const std::uint8_t* __restrict__ dir, double kam,
+                                            const float* __restrict__ z_old, float* __restrict__ z)
 {
     const std::int64_t recv = receiver[flat];
-    if (recv < 0 || recv >= n) return;  // outlets and nodata are not eroded
+    if (recv < 0 || recv >= n || kam < 0.0) return;  // outlets, nodata, below threshold
     const float dx_eff = (dir[flat] & 1u) ? P.dx_diag : P.dx;
-    double area = area_d[flat];
-    if (P.divide_by_dx) area = __ddiv_rn(area, static_cast<double>(P.dx));
-    if (P.threshold > 0.0f && area < static_cast<double>(P.threshold)) return;
     const float zo = z_old[flat];
     const float zr = z[recv];
     if (zr >= zo) return;
     const double tol = __dmul_rn(static_cast<double>(P.slope_clamp), static_cast<double>(dx_eff));
-    const float Ki = kfield ? kfield[flat] : P.K;
-    const double kam = __dmul_rn(static_cast<double>(Ki), pow(area, static_cast<double>(P.m)));
     float zn = zo;
     if (P.n_is_one)
     {
@@ -60,8 +82,9 @@ __device__ __forceinline__ void sp_node(const SpParams& P, std::int64_t n, std::
             if (slope <= 0.0) eps = 0.0;
             else
             {
-                const double fz = __dadd_rn(static_cast<double>(__fsub_rn(zn, zo)), __dmul_rn(kdt, pow(slope, nd)));
-                const double fdz = __dadd_rn(1.0, __dmul_rn(__dmul_rn(kdt, ndx), pow(slope, __dsub_rn(nd, 1.0))));
+                const double fz = __dadd_rn(static_cast<double>(__fsub_rn(zn, zo)), __dmul_rn(kdt, sp_pow(slope, nd)));
+                const double fdz =
+                    __dadd_rn(1.0, __dmul_rn(__dmul_rn(kdt, ndx), sp_pow(slope, __dsub_rn(nd, 1.0))));
                 eps = __ddiv_rn(fz, fdz);
             }
             zn = __fsub_rn(zn, static_cast<float>(eps));
@@ -74,6 +97,17 @@ __device__ __forceinline__ void sp_node(const SpParams& P, std::int64_t n, std::
     z[flat] = zn;
 }
 
+// Both parts for one node.
+__device__ __forceinline__ void sp_node(const SpParams& P, std::int64_t n, std::int64_t flat,
+                                        const std::int64_t* __restrict__ receiver, const std::uint8_t* __restrict__ dir,
+                                        const double* __restrict__ area_d, const float* __restrict__ z_old,
+                                        const float* __restrict__ kfield, float* __restrict__ z)
+{
+    const std::int64_t recv = receiver[flat];
+    if (recv < 0 || recv >= n) return;
+    const float Ki = kfield ? kfield[flat] : P.K;
+    sp_node_kam(P, n, flat, receiver, dir, sp_kam(P, area_d[flat], Ki), z_old, z);
+}
 
 }  // namespace
 }  // namespace lsdtt_gb300

@@ -51,9 +51,15 @@ def dofs(nr, nc, bc, mask, is_channel=None):
     return d.ravel()
 
 
-def linear_step(z, mask, cell, bc, D, dt, U=0.0, residual_tol=1e-12, max_newton=50, is_channel=None):
+def linear_step(z, mask, cell, bc, D, dt, U=0.0, residual_tol=1e-12, max_newton=50, is_channel=None,
+                solver="direct", rel_tol=1e-8):
     """One backward-Euler step of linear hillslope diffusion over dt.
-    Returns (z_new float32, n_newton, final ||F||_inf)."""
+    Returns (z_new float32, n_newton, final ||F||_inf).
+
+    solver="direct" (the parity oracle): sparse LU, Newton to residual_tol.
+    solver="pcg": one Newton step solved by FP64 Jacobi-preconditioned CG to
+    ||r|| <= rel_tol ||b|| (scipy), the iterative form of the reference's
+    Eigen solve; the timed CPU baseline uses it."""
     bc = (bc + "oooo")[:4]
     z = np.asarray(z, np.float32)
     nr, nc = z.shape
@@ -83,6 +89,17 @@ def linear_step(z, mask, cell, bc, D, dt, U=0.0, residual_tol=1e-12, max_newton=
         rows.append(np.arange(idx.size)[ok]); cols.append(dof_of[jj[ok]]); vals.append(np.full(ok.sum(), -DA))
     J = sp.csc_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))),
                       shape=(idx.size, idx.size))
+    if solver == "pcg":
+        zz = zn.copy()
+        F = residual(zz)
+        if F.size and np.any(F != 0):
+            Jr = J.tocsr()
+            dinv = 1.0 / Jr.diagonal()
+            M = spla.LinearOperator(Jr.shape, matvec=lambda v: dinv * v)
+            dz, info = spla.cg(Jr, -F, rtol=rel_tol, atol=0.0, M=M, maxiter=10000)
+            zz[idx] += dz
+            F = residual(zz)
+        return zz.astype(np.float32).reshape(nr, nc), 1, float(np.max(np.abs(F))) if F.size else 0.0
     lu = spla.splu(J)
     zz = zn.copy()
     F = residual(zz)

@@ -1,9 +1,12 @@
 """Seeded synthetic surfaces for the parity tests and the benchmark.
 
-* noise_tilt: config 1 of the benchmark suite -- seeded uniform noise 0-1 m
-  plus a 0.001 planar tilt toward the open edges (the reference's
-  generate_uniform_random_noise_surface + superimpose_open_boundary_gradient,
-  restated by the oracle).
+* noise_tilt: the LEM configurations' initial surface -- seeded uniform
+  noise 0-1 m plus a planar tilt of `slope` toward the open edges,
+  z += slope * dx * (cells to the nearest 'o'/'b' edge), the shape of the
+  reference's generate_uniform_random_noise_surface +
+  superimpose_open_boundary_gradient (synthetic_surfaces_cpu.cpp:359-459).
+  The noise stream is numpy's, not the reference's hash; the oracle
+  restates the reference's own stream where bit-equal inputs matter.
 * fractal_pits: config 2 -- spectral synthesis with power spectrum ~ k^-2
   (random phases, amplitude k^-1), rescaled to the given relief, plus seeded
   paraboloid pits of uniform depth 0-5 m and radius 1-4 cells. The reference
@@ -51,3 +54,23 @@ def add_pits(z: np.ndarray, n_pits: int, seed: int, rmin: float = 1.0, rmax: flo
 def fractal_pits(n: int, relief: float = 1000.0, seed: int = 7, pits_per_8192sq: int = 100000) -> np.ndarray:
     z = fractal(n, n, relief, seed)
     return add_pits(z, max(1, int(round(pits_per_8192sq * (n / 8192.0) ** 2))), seed)
+
+
+def noise_tilt(n_rows: int, n_cols: int, cell: float, seed: int, bc: str = "nnon", slope: float = 0.001) -> np.ndarray:
+    rng = np.random.default_rng(seed)
+    z = rng.random((n_rows, n_cols), dtype=np.float64)
+    r = np.arange(n_rows)[:, None].astype(np.float64)
+    c = np.arange(n_cols)[None, :].astype(np.float64)
+    dist = np.full((n_rows, n_cols), np.inf)
+    bc = (bc + "oooo")[:4].lower()
+    if bc[0] in "ob":
+        dist = np.minimum(dist, r + 0 * c)
+    if bc[1] in "ob":
+        dist = np.minimum(dist, (n_cols - 1 - c) + 0 * r)
+    if bc[2] in "ob":
+        dist = np.minimum(dist, (n_rows - 1 - r) + 0 * c)
+    if bc[3] in "ob":
+        dist = np.minimum(dist, c + 0 * r)
+    if np.isfinite(dist).all():
+        z = z + slope * cell * dist
+    return z.astype(np.float32)
