@@ -197,32 +197,45 @@ __global__ void ens_scatter(const std::uint8_t* __restrict__ flag, const std::in
     if (i < n && flag[i]) out[pos[i]] = i;
 }
 
-// Contributing area = count * dx^2: exact when n_valid * m < 2^53 for dx^2 =
-// m * 2^e (checked per member on the host), which is the reference's
-// accumulate() total in any order (stack.cu, accumulate).
-__global__ void ens_area(Packed P, const EnsParams* __restrict__ prm, const std::uint8_t* __restrict__ mask,
-                         const std::uint64_t* __restrict__ size, double* __restrict__ area)
+// K * A^m per node ahead of the sweep, fully parallel (the level-ordered
+// sweep then only solves each node's implicit update). A = count * dx^2
+// (divided by dx when the member says so) is exact when n_valid * m < 2^53
+// for dx^2 = m * 2^e (checked per member on the host): the reference's
+// accumulate() total in any order (stack.cu, accumulate). Counts below
+// kKamTab take a per-member table built once with the same arithmetic.
+constexpr int kKamTab = 4096;
+
+__global__ void ens_kam_table(Packed P, const EnsParams* __restrict__ prm, double* __restrict__ tab)
 {
     LSDTT_COUNT();
-    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i >= P.n) return;
-    area[i] = mask[i] ? static_cast<double>(size[i]) * prm[member_of(P, i)].dw : 0.0;
+    const std::int64_t t = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (t >= static_cast<std::int64_t>(P.n_members) * kKamTab) return;
+    const int m = static_cast<int>(t / kKamTab), c = static_cast<int>(t % kKamTab);
+    const EnsParams& q = prm[m];
+    tab[t] = sp_kam(q.sp, static_cast<double>(c) * q.dw, q.sp.K);
 }
 
-// K * A^m of every node ahead of the sweep (fully parallel; the level-
-// ordered sweep then only solves each node's implicit update). In place:
-// area becomes kam.
 __global__ void ens_kam(Packed P, const EnsParams* __restrict__ prm, const std::uint8_t* __restrict__ mask,
-                        const std::int64_t* __restrict__ receiver, double* __restrict__ area)
+                        const std::int64_t* __restrict__ receiver, const std::uint64_t* __restrict__ size,
+                        const double* __restrict__ tab, double* __restrict__ kam)
 {
     LSDTT_COUNT();
     const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= P.n || !mask[i] || receiver[i] < 0) return;
-    const SpParams& sp = prm[member_of(P, i)].sp;
-    area[i] = sp_kam(sp, area[i], sp.K);
+    const int m = member_of(P, i);
+    const std::uint64_t c = size[i];
+    if (c < static_cast<std::uint64_t>(kKamTab))
+        kam[i] = tab[static_cast<std::int64_t>(m) * kKamTab + static_cast<std::int64_t>(c)];
+    else
+    {
+        const EnsParams& q = prm[m];
+        kam[i] = sp_kam(q.sp, static_cast<double>(c) * q.dw, q.sp.K);
+    }
 }
 
 // ---- depth levels and the stream-power sweep -------------------------------
+// Depth histogram and scatter with warp-aggregated atomics: lanes of a warp
+// holding the same depth (neighbouring cells mostly do) share one atomic.
 __global__ void ens_depth_hist(std::int64_t n, const std::uint8_t* __restrict__ mask,
                                const std::int32_t* __restrict__ depth, std::uint32_t cap,
                                std::uint32_t* __restrict__ count, std::uint32_t* __restrict__ maxd,
@@ -230,16 +243,20 @@ __global__ void ens_depth_hist(std::int64_t n, const std::uint8_t* __restrict__ 
 {
     LSDTT_COUNT();
     const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i >= n || !mask[i]) return;
-    const std::int32_t d = depth[i];
-    if (d < 0) return;
-    if (static_cast<std::uint32_t>(d) >= cap)
+    int key = -1;
+    if (i < n && mask[i])
     {
-        *overflow = 1;
-        return;
+        const std::int32_t d = depth[i];
+        if (d >= 0 && static_cast<std::uint32_t>(d) >= cap) *overflow = 1;
+        else if (d >= 0) key = d;
     }
-    atomicAdd(&count[d], 1u);
-    atomicMax(maxd, static_cast<std::uint32_t>(d));
+    const unsigned peers = __match_any_sync(0xffffffffu, key);
+    const int lane = threadIdx.x & 31;
+    if (key >= 0 && lane == __ffs(peers) - 1)
+    {
+        atomicAdd(&count[key], static_cast<unsigned>(__popc(peers)));
+        atomicMax(maxd, static_cast<std::uint32_t>(key));
+    }
 }
 
 __global__ void ens_depth_scatter(std::int64_t n, const std::uint8_t* __restrict__ mask,
@@ -249,10 +266,23 @@ __global__ void ens_depth_scatter(std::int64_t n, const std::uint8_t* __restrict
 {
     LSDTT_COUNT();
     const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i >= n || !mask[i]) return;
-    const std::int32_t d = depth[i];
-    if (d < 0 || static_cast<std::uint32_t>(d) >= cap) return;
-    order[start[d] + atomicAdd(&fillc[d], 1u)] = static_cast<std::uint32_t>(i);
+    int key = -1;
+    if (i < n && mask[i])
+    {
+        const std::int32_t d = depth[i];
+        if (d >= 0 && static_cast<std::uint32_t>(d) < cap) key = d;
+    }
+    const unsigned peers = __match_any_sync(0xffffffffu, key);
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(peers) - 1;
+    std::uint32_t base = 0;
+    if (key >= 0 && lane == leader) base = atomicAdd(&fillc[key], static_cast<unsigned>(__popc(peers)));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (key >= 0)
+    {
+        const unsigned rank = __popc(peers & ((1u << lane) - 1u));
+        order[start[key] + base + rank] = static_cast<std::uint32_t>(i);
+    }
 }
 
 __global__ void ens_copy(const float* __restrict__ a, float* __restrict__ b, std::int64_t n)
@@ -480,12 +510,27 @@ __global__ void ens_hs_apply(Packed P, const EnsParams* __restrict__ prm, const 
             const float* pm = p + M.base;
             const float pi = p[i];
             float s = 0.0f;
-#pragma unroll
-            for (int f = 0; f < 4; ++f)
+            if (r > 0 && r < M.nr - 1 && c > 0 && c < M.nc - 1)
             {
-                const std::int64_t j = hs_nb(q.hs, mk, r, c, kDr[f], kDc[f]);
-                if (j == l) continue;
-                s += pi - (dm[j] ? pm[j] : 0.0f);
+                // interior: the in-grid neighbour, or the cell itself when masked
+                const int nbr[4] = {l - M.nc, l + 1, l + M.nc, l - 1};
+#pragma unroll
+                for (int f = 0; f < 4; ++f)
+                {
+                    const int j = nbr[f];
+                    if (!mk[j]) continue;
+                    s += pi - (dm[j] ? pm[j] : 0.0f);
+                }
+            }
+            else
+            {
+#pragma unroll
+                for (int f = 0; f < 4; ++f)
+                {
+                    const std::int64_t j = hs_nb(q.hs, mk, r, c, kDr[f], kDc[f]);
+                    if (j == l) continue;
+                    s += pi - (dm[j] ? pm[j] : 0.0f);
+                }
             }
             v = q.inv_dt_f * pi + q.DA_f * s;
             pap = pi * v;
@@ -685,6 +730,7 @@ struct lsdtt_gpu_ensemble
     int *done = nullptr, *iters = nullptr;
     double* stats_acc = nullptr;
     double* part = nullptr;  // block partials [8][packed / 256]
+    double* kam_tab = nullptr;  // [n_members][kKamTab]
     int* flags = nullptr;
     // pinned host mirrors
     double* h_stats = nullptr;
@@ -726,7 +772,7 @@ void free_ensemble(lsdtt_gpu_ensemble* E)
     if (E->graph) cudaGraphDestroy(E->graph);
     void* bufs[] = {E->d_pm, E->d_prm, E->blk_member, E->tile_member, E->z, E->zf, E->zsp, E->zpre, E->kind, E->bflag, E->dirty, E->oflag, E->pos, E->nd, E->area, E->order, E->lstart, E->lcount,
                     E->lfill, E->maxd, E->dof, E->invd, E->b, E->x, E->r, E->p, E->zz, E->Ap, E->hs_bb, E->hs_acc,
-                    E->done, E->iters, E->stats_acc, E->part, E->flags};
+                    E->done, E->iters, E->stats_acc, E->part, E->kam_tab, E->flags};
     for (void* q : bufs) cudaFree(q);
     void* hb[] = {E->h_stats, E->h_flags, E->h_iters, E->h_maxd, E->h_err};
     for (void* q : hb) cudaFreeHost(q);
@@ -832,8 +878,7 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
     f->ws.used = 0;
     e = build_stack(f, false, st, &E->P);
     if (e != cudaSuccess) return e;
-    ens_area<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->mask, f->sv_size, E->area);
-    ens_kam<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->mask, f->receiver, E->area);
+    ens_kam<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->mask, f->receiver, f->sv_size, E->kam_tab, E->area);
     // 2. depth levels
     const std::uint32_t cap = eager ? static_cast<std::uint32_t>(N + 1) : static_cast<std::uint32_t>(E->depth_cap);
     cudaMemsetAsync(E->maxd, 0, sizeof(std::uint32_t), st);
@@ -1225,6 +1270,7 @@ int lsdtt_gpu_ensemble_create(const lsdtt_gpu_member* members, int32_t n_members
     alloc(&E->iters, static_cast<std::size_t>(n_members));
     alloc(&E->stats_acc, 8 * static_cast<std::size_t>(n_members));
     alloc(&E->part, 8 * (n / kPackAlign));
+    alloc(&E->kam_tab, static_cast<std::size_t>(n_members) * kKamTab);
     alloc(&E->flags, kFlags);
     if (e == cudaSuccess) e = cudaMallocHost(&E->h_stats, sizeof(double) * 8 * n_members);
     if (e == cudaSuccess) e = cudaMallocHost(&E->h_flags, sizeof(int) * kFlags);
@@ -1246,6 +1292,8 @@ int lsdtt_gpu_ensemble_create(const lsdtt_gpu_member* members, int32_t n_members
     E->P.blk_member = E->blk_member;
     E->P.n = N;
     E->P.n_members = n_members;
+    ens_kam_table<<<grid_blocks(static_cast<std::int64_t>(n_members) * kKamTab, 256), 256, 0, st>>>(E->P, E->d_prm,
+                                                                                                   E->kam_tab);
     e = cudaStreamSynchronize(st);
     if (e != cudaSuccess)
     {

@@ -152,10 +152,10 @@ __device__ __forceinline__ void fill_relax_tile(int nr, int nc, bool per_ns, boo
             float m = INFINITY;
             int md = -1;
 #pragma unroll
+            // The halo load already resolved every neighbour: periodic axes
+            // are wrapped into the tile and off-grid positions hold kind 0.
             for (int d = 0; d < 8; ++d)
             {
-                int rr, cc;
-                if (!fill_nb(nr, nc, per_ns, per_ew, r, c, d, rr, cc)) continue;
                 const int ar = lr + d8_dr(d), ac = lc + d8_dc(d);
                 if (sk[ar][ac] == 0) continue;
                 const float v = sF[ar][ac];
