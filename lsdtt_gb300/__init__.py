@@ -308,7 +308,9 @@ class EnsembleInfo(ctypes.Structure):
                 ("sweep_split_level", ctypes.c_int32), ("sweep_block", ctypes.c_int32),
                 ("hillslope_iteration_cap", ctypes.c_int32), ("last_fill_passes", ctypes.c_int32),
                 ("last_max_depth", ctypes.c_int32), ("last_hillslope_iterations", ctypes.c_int32),
-                ("tuned_sweep_ms", ctypes.c_double), ("untuned_sweep_ms", ctypes.c_double)]
+                ("tuned_sweep_ms", ctypes.c_double), ("untuned_sweep_ms", ctypes.c_double),
+                ("sweep_dataflow", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("dataflow_sweep_ms", ctypes.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -330,7 +332,7 @@ def _bind_more():
         "lsdtt_gpu_ensemble_get_member": [vp, i32, vp, vp],
         "lsdtt_gpu_ensemble_step": [vp, i32, ctypes.POINTER(LemStats), vp],
         "lsdtt_gpu_ensemble_get_info": [vp, ctypes.POINTER(EnsembleInfo)],
-        "lsdtt_gpu_ensemble_override_schedule": [vp, i32, i32],
+        "lsdtt_gpu_ensemble_override_schedule": [vp, i32, i32, i32],
         "lsdtt_gpu_ensemble_upload": [vp, vp, vp],
         "lsdtt_gpu_ensemble_download": [vp, vp, vp],
     }.items():
@@ -479,8 +481,11 @@ class Ensemble:
         _check(lib().lsdtt_gpu_ensemble_offsets(self._h, off.ctypes.data))
         return off
 
-    def override_schedule(self, fill_pass_cap=0, hillslope_iteration_cap=0):
-        _check(lib().lsdtt_gpu_ensemble_override_schedule(self._h, fill_pass_cap, hillslope_iteration_cap))
+    def override_schedule(self, fill_pass_cap=0, hillslope_iteration_cap=0, sweep_mode=-1):
+        """Force a schedule (tests): caps for the next capture; sweep_mode 0
+        (level launches), 1 (dataflow) or -1 (autotuned)."""
+        _check(lib().lsdtt_gpu_ensemble_override_schedule(self._h, fill_pass_cap, hillslope_iteration_cap,
+                                                          sweep_mode))
 
     def info(self):
         i = EnsembleInfo()

@@ -39,6 +39,8 @@
 #include <string>
 #include <vector>
 
+#include <cuda/atomic>
+
 #include "engine.cuh"
 #include "d8_cell.cuh"
 #include "fill_tile.cuh"
@@ -175,8 +177,10 @@ __global__ void __launch_bounds__(256) ens_receivers(Packed P, const EnsParams* 
     const Grid g = member_grid(M);
     const EnsParams& q = prm[m];
     // The LEM's engine: interior nodata drains, pits are outlets.
+    const int l = static_cast<int>(local);  // member grids hold < 2^31 cells
+    const int row = l / M.nc;
     d8_receiver_cell(g, zf + M.base, mask + M.base, nullptr, 1, 1, q.inv_card, q.inv_diag, receiver + M.base,
-                     dir + M.base, err, static_cast<int>(local / M.nc), static_cast<int>(local % M.nc), M.base);
+                     dir + M.base, err, row, l - row * M.nc, M.base);
     const std::int64_t r = receiver[i];
     if (r >= 0) receiver[i] = r + M.base;
 }
@@ -334,6 +338,110 @@ __global__ void __launch_bounds__(1024) ens_sp_tail(SweepArgs A, int k0)
     }
 }
 
+// In-order dataflow sweep (no level barriers). Persistent warps claim
+// 64-node chunks of the level-ordered list with an atomic counter; each node
+// waits until its receiver's word zg[] carries this sweep's generation,
+// solves its update and publishes its own word. A word is {generation (high
+// 32 bits), float bits of z (low 32)}: value and flag travel in one aligned
+// 64-bit store, so neither side needs a fence. Chunks are claimed in list
+// order and a receiver always precedes its donors in the list, so every
+// wait is on a node already held by a running warp (or finished); within a
+// chunk each lane takes its nodes in list order. Waits are bounded; a wait
+// that runs out sets the abort flag, which ends every other wait at once,
+// and the host reports the step as failed.
+constexpr int kSpinLimit = 1 << 22;
+constexpr std::uint32_t kDfChunk = 64;
+
+__device__ __forceinline__ unsigned long long df_word(std::uint32_t gen, float z)
+{
+    return (static_cast<unsigned long long>(gen) << 32) | __float_as_uint(z);
+}
+
+__global__ void ens_gen_bump(std::uint32_t* __restrict__ gen)
+{
+    LSDTT_COUNT();
+    *gen += 1u;
+}
+
+// Level 0 (outlets: not eroded) is final from the start.
+__global__ void ens_mark_roots(SweepArgs A, const std::uint32_t* __restrict__ gen,
+                               unsigned long long* __restrict__ zg)
+{
+    LSDTT_COUNT();
+    const std::uint32_t g = *gen;
+    const std::uint32_t lo = A.start[0], hi = A.start[1];
+    for (std::uint32_t j = lo + blockIdx.x * blockDim.x + threadIdx.x; j < hi; j += gridDim.x * blockDim.x)
+    {
+        const std::uint32_t flat = A.order[j];
+        cuda::atomic_ref<unsigned long long, cuda::thread_scope_device>(zg[flat])
+            .store(df_word(g, A.z_old[flat]), cuda::memory_order_relaxed);
+    }
+}
+
+__global__ void __launch_bounds__(256) ens_sp_dataflow(SweepArgs A, const std::uint32_t* __restrict__ gen,
+                                                       std::uint32_t* __restrict__ next,
+                                                       unsigned long long* __restrict__ zg,
+                                                       int* __restrict__ abort_flag)
+{
+    LSDTT_COUNT();
+    const std::uint32_t g = *gen;
+    const std::uint32_t lo = A.start[1];
+    const std::uint32_t hi = A.start[*A.maxd + 1];
+    const int lane = threadIdx.x & 31;
+    for (;;)
+    {
+        std::uint32_t c = 0;
+        if (lane == 0) c = atomicAdd(next, kDfChunk);
+        c = __shfl_sync(0xffffffffu, c, 0);
+        if (lo + c >= hi) break;
+        for (std::uint32_t k = static_cast<std::uint32_t>(lane); k < kDfChunk; k += 32)
+        {
+            const std::uint32_t j = lo + c + k;
+            if (j >= hi) break;
+            const std::uint32_t flat = A.order[j];
+            const std::int64_t recv = A.receiver[flat];
+            const float zo = A.z_old[flat];
+            float zn = zo;
+            if (recv >= 0)
+            {
+                cuda::atomic_ref<unsigned long long, cuda::thread_scope_device> wr(zg[recv]);
+                unsigned long long w = wr.load(cuda::memory_order_relaxed);
+                int spins = 0;
+                bool ok = true;
+                while (static_cast<std::uint32_t>(w >> 32) != g)
+                {
+                    if (++spins > kSpinLimit || *reinterpret_cast<volatile int*>(abort_flag))
+                    {
+                        atomicExch(abort_flag, 1);
+                        ok = false;
+                        break;
+                    }
+                    __nanosleep(32);
+                    w = wr.load(cuda::memory_order_relaxed);
+                }
+                const double kam = A.kam[flat];
+                if (ok && kam >= 0.0)
+                    zn = sp_solve(A.prm[member_of(A.P, flat)].sp, (A.dir[flat] & 1u) != 0, kam, zo,
+                                  __uint_as_float(static_cast<std::uint32_t>(w)));
+            }
+            cuda::atomic_ref<unsigned long long, cuda::thread_scope_device>(zg[flat])
+                .store(df_word(g, zn), cuda::memory_order_relaxed);
+        }
+    }
+}
+
+// The swept elevations back into z (cells this sweep did not reach keep
+// theirs).
+__global__ void ens_sp_extract(std::int64_t n, const std::uint32_t* __restrict__ gen,
+                               const unsigned long long* __restrict__ zg, float* __restrict__ z)
+{
+    LSDTT_COUNT();
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const unsigned long long w = zg[i];
+    if (static_cast<std::uint32_t>(w >> 32) == *gen) z[i] = __uint_as_float(static_cast<std::uint32_t>(w));
+}
+
 // ---- hillslope: Jacobi-PCG with per-member scalars -----------------------
 // Reduction slots: slot s (s = iteration + 1; slot 0 holds r.z of the start)
 // has 4 doubles per member: [0] p.Ap, [1] r.z, [2] r.r.
@@ -417,7 +525,7 @@ __global__ void ens_hs_setup(Packed P, const EnsParams* __restrict__ prm, const 
     if (i < P.n)
     {
         const std::int64_t local = i - M.base;
-        bool is_dof = false;
+        bool is_dof = false, fast = false;
         if (local < static_cast<std::int64_t>(M.nr) * M.nc && q.hill_on)
         {
             const int l = static_cast<int>(local);
@@ -426,6 +534,12 @@ __global__ void ens_hs_setup(Packed P, const EnsParams* __restrict__ prm, const 
             is_dof = mk[l] && !hs_dirichlet_edge(H, r, c);
             if (is_dof)
             {
+                // Fast cell (dof = 3): interior, and all four neighbours
+                // in-grid, valid and themselves DOFs (not on a Dirichlet
+                // edge), so the stencil needs no boundary rules.
+                if (r > 1 && r < M.nr - 2 && c > 1 && c < M.nc - 2 && mk[l - M.nc] && mk[l + 1] && mk[l + M.nc] &&
+                    mk[l - 1])
+                    fast = true;
                 const float* zm = z + M.base;
                 const float zp = zm[l];
                 float flux = 0.0f;
@@ -443,7 +557,7 @@ __global__ void ens_hs_setup(Packed P, const EnsParams* __restrict__ prm, const 
                 bb = F * F;
             }
         }
-        dof[i] = is_dof ? 1 : 0;
+        dof[i] = is_dof ? (fast ? 3 : 1) : 0;
         if (!is_dof)
         {
             b[i] = 0.0f;
@@ -501,7 +615,17 @@ __global__ void ens_hs_apply(Packed P, const EnsParams* __restrict__ prm, const 
     if (i < P.n)
     {
         float v = 0.0f;
-        if (dof[i])
+        const std::uint8_t kd = dof[i];
+        if (kd == 3)
+        {
+            const float pi = p[i];
+            const int nc = M.nc;
+            // the general path's sum, in its order (N, E, S, W)
+            const float s = (((pi - p[i - nc]) + (pi - p[i + 1])) + (pi - p[i + nc])) + (pi - p[i - 1]);
+            v = q.inv_dt_f * pi + q.DA_f * s;
+            pap = pi * v;
+        }
+        else if (kd)
         {
             const int l = static_cast<int>(i - M.base);
             const int r = l / M.nc, c = l - r * M.nc;
@@ -749,6 +873,11 @@ struct lsdtt_gpu_ensemble
     cudaStream_t own = nullptr;  // private stream: the legacy default stream cannot be captured
     cudaEvent_t ev_in = nullptr, ev_out = nullptr;  // order the private stream after/before the caller's
     std::uint32_t tail = 0;      // tuned: levels of at most `tail` cells run in one block (0: none)
+    int sweep_mode = 0;          // tuned: 0 level launches (+ tail), 1 in-order dataflow
+    bool forced_mode = false;    // sweep_mode set by the caller, not the autotuner
+    int df_grid = 0;             // persistent blocks of the dataflow sweep
+    unsigned long long* zg = nullptr;  // dataflow {generation, z} word per cell
+    std::uint32_t* dfc = nullptr;    // [0] generation, [1] chunk counter
     int ov_fill = 0, ov_it = 0;  // one-shot schedule override for the next capture
     lsdtt_gpu_ensemble_info info{};
     bool ready = false;  // every member set at least once
@@ -772,7 +901,7 @@ void free_ensemble(lsdtt_gpu_ensemble* E)
     if (E->graph) cudaGraphDestroy(E->graph);
     void* bufs[] = {E->d_pm, E->d_prm, E->blk_member, E->tile_member, E->z, E->zf, E->zsp, E->zpre, E->kind, E->bflag, E->dirty, E->oflag, E->pos, E->nd, E->area, E->order, E->lstart, E->lcount,
                     E->lfill, E->maxd, E->dof, E->invd, E->b, E->x, E->r, E->p, E->zz, E->Ap, E->hs_bb, E->hs_acc,
-                    E->done, E->iters, E->stats_acc, E->part, E->kam_tab, E->flags};
+                    E->done, E->iters, E->stats_acc, E->part, E->kam_tab, E->flags, E->zg, E->dfc};
     for (void* q : bufs) cudaFree(q);
     void* hb[] = {E->h_stats, E->h_flags, E->h_iters, E->h_maxd, E->h_err};
     for (void* q : hb) cudaFreeHost(q);
@@ -785,12 +914,20 @@ void free_ensemble(lsdtt_gpu_ensemble* E)
 
 // Sweep launches for levels 1 .. split-1 (one launch each), then the tail.
 void enqueue_sweep(lsdtt_gpu_ensemble* E, const SweepArgs& A, int split, int block,
-                   const std::vector<unsigned>& blocks, cudaStream_t st)
+                   const std::vector<unsigned>& blocks, cudaStream_t st, int mode)
 {
+    if (mode == 1)
+    {
+        ens_gen_bump<<<1, 1, 0, st>>>(E->dfc);
+        ens_mark_roots<<<152 * 4, 256, 0, st>>>(A, E->dfc, E->zg);
+        cudaMemsetAsync(E->dfc + 1, 0, sizeof(std::uint32_t), st);
+        ens_sp_dataflow<<<E->df_grid, 256, 0, st>>>(A, E->dfc, E->dfc + 1, E->zg, E->flags + 7);
+        ens_sp_extract<<<grid_blocks(E->N, 256), 256, 0, st>>>(E->N, E->dfc, E->zg, A.z);
+        return;
+    }
     for (int k = 1; k < split; ++k)
         ens_sp_level<<<blocks[static_cast<std::size_t>(k)], block, 0, st>>>(A, k);
     ens_sp_tail<<<1, 1024, 0, st>>>(A, split);
-    (void)E;
 }
 
 // Blocks of each level launch for a level-size profile.
@@ -923,17 +1060,27 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
             double best = 1e30, one_per_level = 0.0;
             std::uint32_t best_tail = 0;
             int best_block = 256;
+            int best_mode = 0;
+            // candidate schedules: level launches with each tail threshold and
+            // block size, then the dataflow sweep (tail = ~0u marks it)
+            std::vector<std::pair<std::uint32_t, int>> cands;
             for (std::uint32_t tail : tails)
-                for (int blk : blocks)
+                for (int blk : blocks) cands.push_back({tail, blk});
+            cands.push_back({~0u, 256});
+            for (const auto& cand : cands)
                 {
-                    const int sp = tail == 0 ? static_cast<int>(D) + 1 : split_for(rec->level_size, tail);
+                    const std::uint32_t tail = cand.first;
+                    const int blk = cand.second;
+                    const int mode = tail == ~0u ? 1 : 0;
+                    const int sp = (tail == 0 || mode == 1) ? static_cast<int>(D) + 1
+                                                            : split_for(rec->level_size, tail);
                     const auto g = level_grid(rec->level_size, sp, blk, 1.0);
                     float ms_best = 1e30f;
                     for (int rep = 0; rep < 2; ++rep)
                     {
                         ens_copy<<<nb, 256, 0, st>>>(E->zf, E->zsp, N);
                         cudaEventRecord(t0, st);
-                        enqueue_sweep(E, A, sp, blk, g, st);
+                        enqueue_sweep(E, A, sp, blk, g, st, mode);
                         cudaEventRecord(t1, st);
                         e = cudaEventSynchronize(t1);
                         if (e != cudaSuccess) break;
@@ -943,11 +1090,20 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
                     }
                     if (e != cudaSuccess) break;
                     if (tail == 0 && blk == 256) one_per_level = ms_best;
+                    if (mode == 1) E->info.dataflow_sweep_ms = ms_best;
+                    // a dataflow run that hit its wait limit is not a candidate
+                    if (mode == 1)
+                    {
+                        int ab = 0;
+                        cudaMemcpy(&ab, E->flags + 7, sizeof(int), cudaMemcpyDeviceToHost);
+                        if (ab) { cudaMemset(E->flags + 7, 0, sizeof(int)); continue; }
+                    }
                     if (ms_best < best)
                     {
                         best = ms_best;
-                        best_tail = tail;
+                        best_tail = mode == 1 ? 0u : tail;
                         best_block = blk;
+                        best_mode = mode;
                     }
                 }
             cudaEventDestroy(t0);
@@ -957,6 +1113,7 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
             // recomputed from each recorded profile.
             E->tail = best_tail;
             E->sweep_block = best_block;
+            if (!E->forced_mode) E->sweep_mode = best_mode;
             E->info.tuned_sweep_ms = best;
             E->info.untuned_sweep_ms = one_per_level;
             E->tuned = true;
@@ -964,10 +1121,11 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
         }
         const int sp = E->tail == 0 ? static_cast<int>(D) + 1 : split_for(rec->level_size, E->tail);
         E->split = sp;
-        enqueue_sweep(E, A, sp, E->sweep_block, level_grid(rec->level_size, sp, E->sweep_block, 1.0), st);
+        enqueue_sweep(E, A, sp, E->sweep_block, level_grid(rec->level_size, sp, E->sweep_block, 1.0), st,
+                      E->sweep_mode);
     }
     else
-        enqueue_sweep(E, A, E->split, E->sweep_block, E->level_blocks, st);
+        enqueue_sweep(E, A, E->split, E->sweep_block, E->level_blocks, st, E->sweep_mode);
     // 4. hillslope: Jacobi-PCG per member
     const std::size_t slot_bytes = sizeof(double) * kHsSlot * M;
     const int itmax = eager ? E->max_iter_all : E->it_cap;
@@ -1271,6 +1429,8 @@ int lsdtt_gpu_ensemble_create(const lsdtt_gpu_member* members, int32_t n_members
     alloc(&E->stats_acc, 8 * static_cast<std::size_t>(n_members));
     alloc(&E->part, 8 * (n / kPackAlign));
     alloc(&E->kam_tab, static_cast<std::size_t>(n_members) * kKamTab);
+    alloc(&E->zg, n);
+    alloc(&E->dfc, 2);
     alloc(&E->flags, kFlags);
     if (e == cudaSuccess) e = cudaMallocHost(&E->h_stats, sizeof(double) * 8 * n_members);
     if (e == cudaSuccess) e = cudaMallocHost(&E->h_flags, sizeof(int) * kFlags);
@@ -1288,6 +1448,15 @@ int lsdtt_gpu_ensemble_create(const lsdtt_gpu_member* members, int32_t n_members
     cudaMemcpyAsync(E->tile_member, tm.data(), sizeof(std::uint16_t) * tm.size(), cudaMemcpyHostToDevice, st);
     cudaMemsetAsync(E->z, 0, sizeof(float) * n, st);
     cudaMemsetAsync(E->mask, 0, n, st);
+    cudaMemsetAsync(E->zg, 0, sizeof(unsigned long long) * n, st);
+    cudaMemsetAsync(E->dfc, 0, sizeof(std::uint32_t) * 2, st);
+    {
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ens_sp_dataflow, 256, 0);
+        E->df_grid = std::max(1, sms * std::max(1, per_sm));
+    }
     E->P.m = E->d_pm;
     E->P.blk_member = E->blk_member;
     E->P.n = N;
@@ -1419,6 +1588,8 @@ int lsdtt_gpu_ensemble_step(lsdtt_gpu_ensemble* E, int32_t n_steps, lsdtt_gpu_le
                 std::copy(itv.begin(), itv.end(), E->h_iters);
             }
         }
+        if (E->h_flags[7])
+            return fail(LSDTT_GPU_ETIMEOUT, std::string(who) + ": the dataflow stream-power sweep hit its wait limit");
         if ((E->h_err[0] & 0xffffffffull) != 0)
             return fail(LSDTT_GPU_ECYCLIC, std::string(who) + ": the receiver graph of a member has a cycle");
         if (E->h_flags[4])
@@ -1431,6 +1602,7 @@ int lsdtt_gpu_ensemble_step(lsdtt_gpu_ensemble* E, int32_t n_steps, lsdtt_gpu_le
     E->info.depth_cap = E->depth_cap;
     E->info.sweep_split_level = E->split;
     E->info.sweep_block = E->sweep_block;
+    E->info.sweep_dataflow = E->sweep_mode;
     E->info.hillslope_iteration_cap = E->it_cap;
     if (stats) fill_stats(E, stats);
     return LSDTT_GPU_OK;
@@ -1452,12 +1624,18 @@ int lsdtt_gpu_ensemble_download(const lsdtt_gpu_ensemble* E, float* z_host, void
     return e == cudaSuccess ? LSDTT_GPU_OK : cuda_fail(e, "lsdtt_gpu_ensemble_download");
 }
 
-int lsdtt_gpu_ensemble_override_schedule(lsdtt_gpu_ensemble* E, int32_t fill_pass_cap, int32_t hillslope_iteration_cap)
+int lsdtt_gpu_ensemble_override_schedule(lsdtt_gpu_ensemble* E, int32_t fill_pass_cap, int32_t hillslope_iteration_cap,
+                                         int32_t sweep_mode)
 {
-    if (!E || fill_pass_cap < 0 || hillslope_iteration_cap < 0)
+    if (!E || fill_pass_cap < 0 || hillslope_iteration_cap < 0 || sweep_mode < -1 || sweep_mode > 1)
         return fail(LSDTT_GPU_EINVAL, "lsdtt_gpu_ensemble_override_schedule: bad argument");
     E->ov_fill = fill_pass_cap;
     E->ov_it = hillslope_iteration_cap;
+    if (sweep_mode >= 0)
+    {
+        E->sweep_mode = sweep_mode;
+        E->forced_mode = true;
+    }
     E->captured = false;
     return LSDTT_GPU_OK;
 }

@@ -46,7 +46,8 @@ __device__ __forceinline__ void fill_init_cell(int nr, int nc, bool per_ns, bool
                                                const std::uint8_t* __restrict__ mask, double nodata, int interior_nd,
                                                float* __restrict__ F, std::uint8_t* __restrict__ kind, std::int64_t i)
 {
-    const int r = static_cast<int>(i / nc), c = static_cast<int>(i % nc);
+    const int r = static_cast<int>(i / nc);
+    const int c = static_cast<int>(i - static_cast<std::int64_t>(r) * nc);
     auto valid_at = [&](std::int64_t k) {
         return mask[k] != 0 && !(isnan(nodata) ? isnan(z[k]) : static_cast<double>(z[k]) == nodata);
     };

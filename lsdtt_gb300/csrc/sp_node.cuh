@@ -44,22 +44,14 @@ __device__ __forceinline__ double sp_kam(const SpParams& P, double area_d, float
     return __dmul_rn(static_cast<double>(Ki), pow(area, static_cast<double>(P.m)));
 }
 
-// The implicit update of node `flat` from its receiver's final elevation
-// (stream_power_cpu.cpp:263-318) given its kam = sp_kam(...). Any
-// receiver-before-donor order gives the reference's bits: a node reads only
-// z_old[self] and z[receiver]. Indices are those of the arrays passed
-// (n = their length).
-__device__ __forceinline__ void sp_node_kam(const SpParams& P, std::int64_t n, std::int64_t flat,
-                                            const std::int64_t* __restrict__ receiver,
-                                            const std::uint8_t* __restrict__ dir, double kam,
-                                            const float* __restrict__ z_old, float* __restrict__ z)
+// The implicit update of one node (stream_power_cpu.cpp:263-318): its new
+// elevation from its own old elevation zo, its receiver's final elevation
+// zr, kam = sp_kam(...) and the step length to the receiver. Returns zo when
+// the node is not eroded.
+__device__ __forceinline__ float sp_solve(const SpParams& P, bool diagonal, double kam, float zo, float zr)
 {
-    const std::int64_t recv = receiver[flat];
-    if (recv < 0 || recv >= n || kam < 0.0) return;  // outlets, nodata, below threshold
-    const float dx_eff = (dir[flat] & 1u) ? P.dx_diag : P.dx;
-    const float zo = z_old[flat];
-    const float zr = z[recv];
-    if (zr >= zo) return;
+    if (zr >= zo) return zo;
+    const float dx_eff = diagonal ? P.dx_diag : P.dx;
     const double tol = __dmul_rn(static_cast<double>(P.slope_clamp), static_cast<double>(dx_eff));
     float zn = zo;
     if (P.n_is_one)
@@ -94,7 +86,23 @@ __device__ __forceinline__ void sp_node_kam(const SpParams& P, std::int64_t n, s
         if (__fsub_rn(zn, zo) > static_cast<float>(tol) || isnan(zn)) zn = zo;
         if (zn < zr) zn = __fadd_rn(zr, __fmul_rn(P.slope_clamp, dx_eff));
     }
-    z[flat] = zn;
+    return zn;
+}
+
+// sp_solve for node `flat` with its own loads and store. Any receiver-
+// before-donor order gives the reference's bits: a node reads only
+// z_old[self] and z[receiver]. Indices are those of the arrays passed
+// (n = their length).
+__device__ __forceinline__ void sp_node_kam(const SpParams& P, std::int64_t n, std::int64_t flat,
+                                            const std::int64_t* __restrict__ receiver,
+                                            const std::uint8_t* __restrict__ dir, double kam,
+                                            const float* __restrict__ z_old, float* __restrict__ z)
+{
+    const std::int64_t recv = receiver[flat];
+    if (recv < 0 || recv >= n || kam < 0.0) return;  // outlets, nodata, below threshold
+    const float zo = z_old[flat];
+    const float zn = sp_solve(P, (dir[flat] & 1u) != 0, kam, zo, z[recv]);
+    z[flat] = zn;  // zo when not eroded: z[flat] already holds it
 }
 
 // Both parts for one node.

@@ -63,12 +63,13 @@ def _rel(a, b):
     return float(np.max(np.abs(a - b)) / max(float(np.ptp(b)), 1.0))
 
 
-@pytest.mark.parametrize("use_graph", [False, True])
-def test_ensemble_matches_members_alone(port, use_graph):
+@pytest.mark.parametrize("use_graph,sweep_mode", [(False, 0), (True, 0), (False, 1), (True, 1)])
+def test_ensemble_matches_members_alone(port, use_graph, sweep_mode):
     import lsdtt_gb300 as G
     specs = _members(port)
     steps = 6
     ens = G.Ensemble(specs, use_graph=use_graph)
+    ens.override_schedule(sweep_mode=sweep_mode)
     for _ in range(steps - 1):
         ens.step()
     stats = ens.step(want_stats=True)
@@ -82,8 +83,12 @@ def test_ensemble_matches_members_alone(port, use_graph):
         print(f"member {k} {spec['z'].shape} bc={spec['boundary_conditions']}: rel diff {err:.2e}; "
               f"PCG iterations alone {its[-1]} ensemble {stats[k]['hillslope_iterations']}")
         assert err <= REL, (k, err)
+        # routing and stream power are the single-grid rules: report exactness
+        if err == 0.0:
+            print(f"member {k}: bit-identical")
         assert abs(stats[k]["hillslope_iterations"] - its[-1]) <= 4
     print("info", info)
+    assert info["sweep_dataflow"] == sweep_mode
     if use_graph:
         assert info["graph_captures"] >= 1 and info["graph_replays"] >= steps - 2
     else:
