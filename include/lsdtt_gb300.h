@@ -283,6 +283,8 @@ typedef struct lsdtt_gpu_lem_options
     int32_t divide_area_by_dx;    /* reference default 1 */
     double hillslope_rel_tol;     /* PCG relative residual, e.g. 1e-8 */
     int32_t hillslope_max_iter;
+    int32_t hillslope_nonlinear;  /* 1: Roering critical-slope law (enable_nonlinear_hillslopes) */
+    float critical_slope;         /* Sc of the Roering law */
 } lsdtt_gpu_lem_options;
 
 /* lsdtt_lem_step_stats (src/cpu/lsdtt_lem_cpu.hpp:185-211) */
@@ -306,8 +308,16 @@ typedef struct lsdtt_gpu_lem lsdtt_gpu_lem;
 int lsdtt_gpu_lem_create(const lsdtt_gpu_grid* grid, const uint8_t* mask_dev, const lsdtt_gpu_lem_options* options,
                          lsdtt_gpu_lem** out, void* stream);
 int lsdtt_gpu_lem_destroy(lsdtt_gpu_lem* lem);
-/* Advances z_dev (in place) by one timestep. stats may be NULL. */
+/* Advances z_dev (in place) by one timestep. stats may be NULL. With the
+ * Roering law (or a preconditioner attached) the hillslope stage is
+ * lsdtt_gpu_hillslope_implicit over the timestep (the reference's
+ * compute_hillslope_newton_transient); otherwise one linear
+ * backward-Euler step. */
 int lsdtt_gpu_lem_step(lsdtt_gpu_lem* lem, float* z_dev, lsdtt_gpu_lem_stats* stats, void* stream);
+/* Attach a trained network (NULL detaches): the hillslope solves of later
+ * steps use lsdtt_gpu_hillslope_implicit_learned. The network must fit the
+ * grid (sides multiples of 8 within its capacity) and outlive its use. */
+int lsdtt_gpu_lem_set_preconditioner(lsdtt_gpu_lem* lem, lsdtt_gpu_unet* net);
 
 /* ---- batched ensembles -----------------------------------------------------
  * Parameter-sweep ensembles of independent LEM runs on grids of different

@@ -283,7 +283,8 @@ class LemOptions(ctypes.Structure):
                 ("hillslope_diffusivity", ctypes.c_float), ("slope_clamp", ctypes.c_float),
                 ("baselevel_fall_rate", ctypes.c_float), ("fill_min_slope", ctypes.c_float),
                 ("enable_hillslope", ctypes.c_int32), ("divide_area_by_dx", ctypes.c_int32),
-                ("hillslope_rel_tol", ctypes.c_double), ("hillslope_max_iter", ctypes.c_int32)]
+                ("hillslope_rel_tol", ctypes.c_double), ("hillslope_max_iter", ctypes.c_int32),
+                ("hillslope_nonlinear", ctypes.c_int32), ("critical_slope", ctypes.c_float)]
 
 
 class LemStats(ctypes.Structure):
@@ -388,7 +389,8 @@ class LandscapeModel:
     def __init__(self, z, mask, cell_size, boundary_conditions="oooo", *, timestep=100.0, erodibility=1e-3,
                  m_exponent=0.45, n_exponent=1.0, uplift_rate=1e-4, hillslope_diffusivity=1e-3,
                  enable_hillslope=True, slope_clamp=1e-5, baselevel_fall_rate=0.0, fill_min_slope=0.0,
-                 divide_area_by_dx=True, hillslope_rel_tol=1e-8, hillslope_max_iter=2000, stream=None):
+                 divide_area_by_dx=True, hillslope_rel_tol=1e-8, hillslope_max_iter=2000, hillslope_nonlinear=False,
+                 critical_slope=1.0, stream=None):
         torch = _torch()
         L = _bind_more()
         self.z = _dev(z, torch.float32).clone()
@@ -396,11 +398,20 @@ class LandscapeModel:
         self.grid = make_grid(self.z.shape[0], self.z.shape[1], cell_size, boundary_conditions)
         self.options = LemOptions(timestep, erodibility, m_exponent, n_exponent, uplift_rate, hillslope_diffusivity,
                                   slope_clamp, baselevel_fall_rate, fill_min_slope, int(enable_hillslope),
-                                  int(divide_area_by_dx), hillslope_rel_tol, hillslope_max_iter)
+                                  int(divide_area_by_dx), hillslope_rel_tol, hillslope_max_iter,
+                                  int(hillslope_nonlinear), critical_slope)
         h = ctypes.c_void_p()
         _check(L.lsdtt_gpu_lem_create(ctypes.byref(self.grid), ctypes.c_void_p(self.mask.data_ptr()),
                                       ctypes.byref(self.options), ctypes.byref(h), _stream(stream)))
         self._h = h
+
+    def set_preconditioner(self, net: Optional["UNet"]):
+        """Use a trained UNet in the hillslope solves (None: Jacobi-PCG)."""
+        fn = lib().lsdtt_gpu_lem_set_preconditioner
+        fn.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        fn.restype = ctypes.c_int
+        _check(fn(self._h, net._h if net is not None else None))
+        self._net = net  # keep it alive while attached
 
     def step(self, stream=None, want_stats=True):
         st = LemStats()
@@ -452,7 +463,8 @@ class Ensemble:
             arr[k].options = LemOptions(o["timestep"], o["erodibility"], o["m_exponent"], o["n_exponent"],
                                         o["uplift_rate"], o["hillslope_diffusivity"], o["slope_clamp"],
                                         o["baselevel_fall_rate"], o["fill_min_slope"], int(o["enable_hillslope"]),
-                                        int(o["divide_area_by_dx"]), o["hillslope_rel_tol"], o["hillslope_max_iter"])
+                                        int(o["divide_area_by_dx"]), o["hillslope_rel_tol"], o["hillslope_max_iter"],
+                                        0, 1.0)
             self.shapes.append(z.shape)
         h = ctypes.c_void_p()
         _check(L.lsdtt_gpu_ensemble_create(arr, len(members), int(use_graph), ctypes.byref(h), _stream(stream)))

@@ -141,6 +141,25 @@ __device__ __forceinline__ void block_atomic_add(double* dst, double v)
     if (threadIdx.x == 0 && t != 0.0) atomicAdd(dst, t);
 }
 
+// Sum of a float quantity: FP32 within each warp (32 terms), FP64 across the
+// warps of the block and across blocks (one atomic per block). The FP64
+// stage carries the cancellation-prone part of a grid-wide dot product;
+// per-thread FP64 arithmetic, scarce on this part, is avoided.
+__device__ __forceinline__ void block_atomic_add_f(double* dst, float v)
+{
+    __shared__ double sh_block_add_f[32];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) sh_block_add_f[threadIdx.x >> 5] = static_cast<double>(v);
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        double t = sh_block_add_f[0];
+        for (int k = 1; k < static_cast<int>(blockDim.x >> 5); ++k) t += sh_block_add_f[k];
+        if (t != 0.0) atomicAdd(dst, t);
+    }
+}
+
 // Maximum of non-negative values: their bit patterns order like the values.
 __device__ __forceinline__ void block_atomic_max_nonneg(double* dst, double v)
 {

@@ -1281,6 +1281,11 @@ int lsdtt_gpu_ensemble_create(const lsdtt_gpu_member* members, int32_t n_members
             free_ensemble(E);
             return fail(LSDTT_GPU_EINVAL, mk + ": timestep must be positive");
         }
+        if (o.enable_hillslope && o.hillslope_nonlinear)
+        {
+            free_ensemble(E);
+            return fail(LSDTT_GPU_EINVAL, mk + ": ensembles run the linear hillslope law");
+        }
         auto is_p = [&](int i) { return g.boundary_conditions[i] == 'p' || g.boundary_conditions[i] == 'P'; };
         if (is_p(0) != is_p(2) || is_p(1) != is_p(3) || (is_p(0) && is_p(1)))
         {

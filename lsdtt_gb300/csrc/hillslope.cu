@@ -98,30 +98,32 @@ __global__ void hs_apply(Hs H, const std::uint8_t* __restrict__ mask, const std:
     LSDTT_COUNT();
     const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     const std::int64_t n = static_cast<std::int64_t>(H.nr) * H.nc;
-    double pap = 0.0;
+    // FP32 difference form inv_dt p_P + (D/h^2) sum_f (p_P - [nb DOF] p_nb):
+    // no large terms cancel, and no FP64 per cell.
+    const float inv_dt = static_cast<float>(H.inv_dt), DA = static_cast<float>(H.DA);
+    float pap = 0.0f;
     if (i < n)
     {
         float v = 0.0f;
         if (dof[i])
         {
-            const int r = static_cast<int>(i / H.nc), c = static_cast<int>(i % H.nc);
+            const int r = static_cast<int>(i / H.nc);
+            const int c = static_cast<int>(i - static_cast<std::int64_t>(r) * H.nc);
             const float pi = p[i];
             float s = 0.0f;
-            int nf = 0;
 #pragma unroll
             for (int f = 0; f < 4; ++f)
             {
                 const std::int64_t j = hs_nb(H, mask, r, c, kDr[f], kDc[f]);
                 if (j == i) continue;
-                ++nf;
-                if (dof[j]) s += p[j];
+                s += pi - (dof[j] ? p[j] : 0.0f);
             }
-            v = static_cast<float>((H.inv_dt + H.DA * nf) * pi - H.DA * s);
-            pap = static_cast<double>(pi) * v;
+            v = inv_dt * pi + DA * s;
+            pap = pi * v;
         }
         Ap[i] = v;
     }
-    block_atomic_add(&acc_it[0], pap);
+    block_atomic_add_f(&acc_it[0], pap);
 }
 
 // alpha = rz/pAp; x += alpha p; r -= alpha Ap; zz = M^-1 r; acc_it[1] = r.zz, acc_it[2] = r.r
@@ -142,7 +144,7 @@ __global__ void hs_update(std::int64_t n, const double* __restrict__ rz_prev, co
     }
     __syncthreads();
     const float alpha = s_alpha;
-    double rz = 0.0, rr = 0.0;
+    float rz = 0.0f, rr = 0.0f;
     if (i < n)
     {
         x[i] += alpha * p[i];
@@ -150,11 +152,11 @@ __global__ void hs_update(std::int64_t n, const double* __restrict__ rz_prev, co
         r[i] = ri;
         const float zi = ri * inv_diag[i];
         zz[i] = zi;
-        rz = static_cast<double>(ri) * zi;
-        rr = static_cast<double>(ri) * ri;
+        rz = ri * zi;
+        rr = ri * ri;
     }
-    block_atomic_add(&acc_out[1], rz);
-    block_atomic_add(&acc_out[2], rr);
+    block_atomic_add_f(&acc_out[1], rz);
+    block_atomic_add_f(&acc_out[2], rr);
 }
 
 // beta = rz_new / rz_old; p = zz + beta p
@@ -452,31 +454,35 @@ __global__ void hsn_apply(HsN P, const std::uint8_t* __restrict__ mask, const st
     LSDTT_COUNT();
     const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     const std::int64_t n = static_cast<std::int64_t>(P.H.nr) * P.H.nc;
-    double pap = 0.0;
+    // FP32 difference form inv_dt p_P + (D/h^2) sum_f alpha_f (p_P - [nb DOF]
+    // p_nb). alpha is a property of the face (the same value from both
+    // sides), so the operator stays symmetric.
+    const float inv_dt = static_cast<float>(P.H.inv_dt), DA = static_cast<float>(P.H.DA);
+    float pap = 0.0f;
     if (i < n)
     {
         float v = 0.0f;
         if (dof[i])
         {
-            const int rr = static_cast<int>(i / P.H.nc), cc = static_cast<int>(i % P.H.nc);
+            const int rr = static_cast<int>(i / P.H.nc);
+            const int cc = static_cast<int>(i - static_cast<std::int64_t>(rr) * P.H.nc);
             const float4 a = alpha[i];
             const float av[4] = {a.x, a.y, a.z, a.w};
             const float pi = p[i];
-            double diag = P.H.inv_dt, off = 0.0;
+            float s = 0.0f;
 #pragma unroll
             for (int f = 0; f < 4; ++f)
             {
                 const std::int64_t j = hs_nb(P.H, mask, rr, cc, kDr[f], kDc[f]);
                 if (j == i) continue;
-                diag += P.H.DA * av[f];
-                if (dof[j]) off += P.H.DA * av[f] * p[j];
+                s += av[f] * (pi - (dof[j] ? p[j] : 0.0f));
             }
-            v = static_cast<float>(diag * pi - off);
-            pap = static_cast<double>(pi) * v;
+            v = inv_dt * pi + DA * s;
+            pap = pi * v;
         }
         Ap[i] = v;
     }
-    block_atomic_add(&acc_it[0], pap);
+    block_atomic_add_f(&acc_it[0], pap);
 }
 
 // z_try = z + lambda * dz on DOFs (double)
@@ -505,8 +511,8 @@ __global__ void hsn_to_float(std::int64_t n, const double* __restrict__ a, float
 
 // ---- flexible PCG with the learned preconditioner --------------------------
 // Per-iteration reduction slot (4 doubles): [0] p.Ap, [1] r.z, [2] r.r,
-// [3] r_old.z. beta = (r.z - r_old.z) / r_old.z_old (Polak-Ribiere), which
-// keeps conjugacy when M^-1 changes from one iteration to the next.
+// [3] z.(r - r_old). beta = z.(r - r_old) / r_old.z_old (Polak-Ribiere),
+// which keeps conjugacy when M^-1 changes from one iteration to the next.
 
 // alpha = rz_prev / pAp; r_old = r; x += alpha p; r -= alpha Ap; acc_out[2] = r.r
 __global__ void hsf_update(std::int64_t n, const double* __restrict__ rz_prev, const double* __restrict__ acc_it,
@@ -523,7 +529,7 @@ __global__ void hsf_update(std::int64_t n, const double* __restrict__ rz_prev, c
     }
     __syncthreads();
     const float alpha = s_alpha;
-    double rr = 0.0;
+    float rr = 0.0f;
     if (i < n)
     {
         x[i] += alpha * p[i];
@@ -531,9 +537,9 @@ __global__ void hsf_update(std::int64_t n, const double* __restrict__ rz_prev, c
         ro[i] = r0;
         const float ri = r0 - alpha * Ap[i];
         r[i] = ri;
-        rr = static_cast<double>(ri) * ri;
+        rr = ri * ri;
     }
-    block_atomic_add(&acc_out[2], rr);
+    block_atomic_add_f(&acc_out[2], rr);
 }
 
 // The network's input: the Jacobi-scaled residual D^-1 r (metres), which
@@ -555,27 +561,27 @@ __global__ void hsf_mask(std::int64_t n, const std::uint8_t* __restrict__ dof, c
     if (i < n) y[i] = dof[i] ? ynet[i] : 0.0f;
 }
 
-// z = y + D^-1 (r - A y) (t = A y); acc_out[1] = r.z, acc_out[3] = r_old.z
+// z = y + D^-1 (r - A y) (t = A y); acc_out[1] = r.z, acc_out[3] = z.(r - r_old)
 __global__ void hsf_smooth(std::int64_t n, const float* __restrict__ invd, const float* __restrict__ r,
                            const float* __restrict__ ro, const float* __restrict__ t, float* __restrict__ z,
                            double* __restrict__ acc_out)
 {
     LSDTT_COUNT();
     const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    double rz = 0.0, roz = 0.0;
+    float rz = 0.0f, roz = 0.0f;
     if (i < n)
     {
         const float ri = r[i];
         const float zi = z[i] + invd[i] * (ri - t[i]);
         z[i] = zi;
-        rz = static_cast<double>(ri) * zi;
-        roz = static_cast<double>(ro[i]) * zi;
+        rz = ri * zi;
+        roz = zi * (ri - ro[i]);  // the Polak-Ribiere numerator, formed per element
     }
-    block_atomic_add(&acc_out[1], rz);
-    block_atomic_add(&acc_out[3], roz);
+    block_atomic_add_f(&acc_out[1], rz);
+    block_atomic_add_f(&acc_out[3], roz);
 }
 
-// beta = (r.z - r_old.z) / rz_old; p = z + beta p (beta = 0 at a restart)
+// beta = z.(r - r_old) / rz_old; p = z + beta p (beta = 0 at a restart)
 __global__ void hsf_direction(std::int64_t n, const double* __restrict__ rz_old, const double* __restrict__ acc_new,
                              const float* __restrict__ z, float* __restrict__ p)
 {
@@ -585,7 +591,7 @@ __global__ void hsf_direction(std::int64_t n, const double* __restrict__ rz_old,
     if (threadIdx.x == 0)
     {
         const double ro = *rz_old;
-        s_beta = (ro > 0.0) ? static_cast<float>((acc_new[1] - acc_new[3]) / ro) : 0.0f;
+        s_beta = (ro > 0.0) ? static_cast<float>(acc_new[3] / ro) : 0.0f;
     }
     __syncthreads();
     if (i < n) p[i] = z[i] + s_beta * p[i];

@@ -134,6 +134,7 @@ struct lsdtt_gpu_lem
     std::uint64_t* k1 = nullptr;
     std::uint32_t* v1 = nullptr;
     Scratch ws{};
+    lsdtt_gpu_unet* net = nullptr;  // learned preconditioner, not owned
 };
 
 extern "C" {
@@ -166,7 +167,10 @@ int lsdtt_gpu_lem_create(const lsdtt_gpu_grid* grid, const std::uint8_t* mask_de
     if (e == cudaSuccess) e = cudaMalloc(&L->k1, sizeof(std::uint64_t) * n);
     if (e == cudaSuccess) e = cudaMalloc(&L->v0, sizeof(std::uint32_t) * n);
     if (e == cudaSuccess) e = cudaMalloc(&L->v1, sizeof(std::uint32_t) * n);
-    const std::size_t wsb = static_cast<std::size_t>(n) / 256 * 8 + (std::size_t(16) << 20);
+    // Radix-sort scratch of the p99.9 statistic: two per-tile histograms of
+    // 256 counts (tiles of kSortTile keys) plus the scan's partial sums.
+    const std::size_t tiles = static_cast<std::size_t>((n + kSortTile - 1) / kSortTile);
+    const std::size_t wsb = tiles * 256 * 4 * 3 + (std::size_t(16) << 20);
     if (e == cudaSuccess) e = cudaMalloc(&L->ws.base, wsb);
     L->ws.cap = wsb;
     if (e != cudaSuccess)
@@ -235,9 +239,22 @@ int lsdtt_gpu_lem_step(lsdtt_gpu_lem* L, float* z_dev, lsdtt_gpu_lem_stats* stat
     if (o.enable_hillslope)
     {
         lsdtt_gpu_solve_report rep{};
-        s = lsdtt_gpu_hillslope_linear_implicit(&L->grid, L->zsp, L->mask, nullptr, o.hillslope_diffusivity,
-                                                o.timestep, o.hillslope_rel_tol > 0 ? o.hillslope_rel_tol : 1e-8,
-                                                o.hillslope_max_iter, z_dev, &rep, stream);
+        const double tol = o.hillslope_rel_tol > 0 ? o.hillslope_rel_tol : 1e-8;
+        if (o.hillslope_nonlinear || L->net)
+        {
+            // compute_hillslope_newton_transient over the whole timestep
+            if (L->net)
+                s = lsdtt_gpu_hillslope_implicit_learned(&L->grid, L->zsp, L->mask, nullptr, o.hillslope_diffusivity,
+                                                         o.critical_slope, o.hillslope_nonlinear, o.timestep, tol,
+                                                         o.hillslope_max_iter, 0.0, 0, L->net, z_dev, &rep, stream);
+            else
+                s = lsdtt_gpu_hillslope_implicit(&L->grid, L->zsp, L->mask, nullptr, o.hillslope_diffusivity,
+                                                 o.critical_slope, o.hillslope_nonlinear, o.timestep, tol,
+                                                 o.hillslope_max_iter, 0.0, 0, z_dev, &rep, stream);
+        }
+        else
+            s = lsdtt_gpu_hillslope_linear_implicit(&L->grid, L->zsp, L->mask, nullptr, o.hillslope_diffusivity,
+                                                    o.timestep, tol, o.hillslope_max_iter, z_dev, &rep, stream);
         if (s != LSDTT_GPU_OK) return s;
         hs_it = rep.iterations;
     }
@@ -285,6 +302,15 @@ int lsdtt_gpu_lem_step(lsdtt_gpu_lem* L, float* z_dev, lsdtt_gpu_lem_stats* stat
             stats->p999_local_elevation_change = v;
         }
     }
+    return LSDTT_GPU_OK;
+}
+
+int lsdtt_gpu_lem_set_preconditioner(lsdtt_gpu_lem* L, lsdtt_gpu_unet* net)
+{
+    if (!L) return fail(LSDTT_GPU_EINVAL, "lsdtt_gpu_lem_set_preconditioner: lem is null");
+    if (net)
+        if (int sc = unet_check_shape(net, L->grid.n_rows, L->grid.n_cols)) return sc;
+    L->net = net;
     return LSDTT_GPU_OK;
 }
 

@@ -190,7 +190,7 @@ __global__ void __launch_bounds__(128) k_conv_tc(int H, int W, int up, const __n
                     out[o + q] = __float2bfloat16_rn(fmaxf(a, 0.f));
                 else
                 {
-                    pre[o + q] = __float2bfloat16_rn(a);
+                    if (pre) pre[o + q] = __float2bfloat16_rn(a);  // kept for the backward pass only
                     out[o + q] = __float2bfloat16_rn(__fadd_rn(fmaxf(a, 0.f), __bfloat162float(skip[o + q])));
                 }
             }
@@ -429,7 +429,8 @@ struct lsdtt_gpu_unet
     float *y = nullptr, *go = nullptr, *rms = nullptr;
     double* acc = nullptr;
     double* hacc = nullptr;
-    // backward scratch (FP32), allocated by the first gradient evaluation
+    // training-only buffers (decoder pre-activations a0..a2 above, FP32
+    // backward scratch), allocated by the first gradient evaluation
     float *gA = nullptr, *gB = nullptr, *ge0 = nullptr, *ge1 = nullptr, *ge2 = nullptr, *ge3 = nullptr;
 };
 
@@ -478,8 +479,10 @@ void launch_conv_tc(int l, int H, int W, int up, const __nv_bfloat16* in, const 
 #undef LSDTT_CONV_CASE
 }
 
-// Forward pass on an H x W residual (device, FP32) -> U->y.
-cudaError_t unet_forward(lsdtt_gpu_unet* U, const float* r, int H, int W, cudaStream_t st)
+// Forward pass on an H x W residual (device, FP32) -> U->y. Without
+// `for_training` the decoder pre-activations (needed only by the backward
+// pass) are not stored.
+cudaError_t unet_forward(lsdtt_gpu_unet* U, const float* r, int H, int W, cudaStream_t st, bool for_training)
 {
     const std::int64_t n = static_cast<std::int64_t>(H) * W;
     cudaMemsetAsync(U->acc, 0, sizeof(double), st);
@@ -496,9 +499,12 @@ cudaError_t unet_forward(lsdtt_gpu_unet* U, const float* r, int H, int W, cudaSt
     h /= 2; w /= 2;
     k_pool<<<grid_blocks(static_cast<std::int64_t>(h) * w * 64, 256), 256, 0, st>>>(h, w, 64, U->e2, U->p2);
     launch_conv_tc(3, h, w, 0, U->p2, U->wb + U->woff[3], U->w + U->boff[3], 0, nullptr, nullptr, U->e3, st);
-    launch_conv_tc(4, H / 4, W / 4, 1, U->e3, U->wb + U->woff[4], U->w + U->boff[4], 1, U->e2, U->a2, U->d2, st);
-    launch_conv_tc(5, H / 2, W / 2, 1, U->d2, U->wb + U->woff[5], U->w + U->boff[5], 1, U->e1, U->a1, U->d1, st);
-    launch_conv_tc(6, H, W, 1, U->d1, U->wb + U->woff[6], U->w + U->boff[6], 1, U->e0, U->a0, U->d0, st);
+    launch_conv_tc(4, H / 4, W / 4, 1, U->e3, U->wb + U->woff[4], U->w + U->boff[4], 1, U->e2,
+                   for_training ? U->a2 : nullptr, U->d2, st);
+    launch_conv_tc(5, H / 2, W / 2, 1, U->d2, U->wb + U->woff[5], U->w + U->boff[5], 1, U->e1,
+                   for_training ? U->a1 : nullptr, U->d1, st);
+    launch_conv_tc(6, H, W, 1, U->d1, U->wb + U->woff[6], U->w + U->boff[6], 1, U->e0,
+                   for_training ? U->a0 : nullptr, U->d0, st);
     k_conv_out<<<grid_blocks(n, 128), 128, 0, st>>>(H, W, U->d0, wr + U->woff[7], U->w + U->boff[7], U->rms, U->y);
     return cudaGetLastError();
 }
@@ -567,7 +573,7 @@ cudaError_t unet_forward_dev(lsdtt_gpu_unet* U, const float* r_dev, int H, int W
                              const float** y_dev)
 {
     *y_dev = U->y;
-    return unet_forward(U, r_dev, H, W, st);
+    return unet_forward(U, r_dev, H, W, st, false);
 }
 }  // namespace lsdtt_gb300
 
@@ -630,15 +636,12 @@ int lsdtt_gpu_unet_create(int32_t max_rows, int32_t max_cols, uint64_t seed, lsd
     if (e == cudaSuccess) e = ualloc(&U->v, off);
     if (e == cudaSuccess) e = ualloc(&U->x0, px0);
     if (e == cudaSuccess) e = ualloc(&U->e0, px0 * 16);
-    if (e == cudaSuccess) e = ualloc(&U->a0, px0 * 16);
     if (e == cudaSuccess) e = ualloc(&U->d0, px0 * 16);
     if (e == cudaSuccess) e = ualloc(&U->p0, level_px(U, 1) * 16);
     if (e == cudaSuccess) e = ualloc(&U->e1, level_px(U, 1) * 32);
-    if (e == cudaSuccess) e = ualloc(&U->a1, level_px(U, 1) * 32);
     if (e == cudaSuccess) e = ualloc(&U->d1, level_px(U, 1) * 32);
     if (e == cudaSuccess) e = ualloc(&U->p1, level_px(U, 2) * 32);
     if (e == cudaSuccess) e = ualloc(&U->e2, level_px(U, 2) * 64);
-    if (e == cudaSuccess) e = ualloc(&U->a2, level_px(U, 2) * 64);
     if (e == cudaSuccess) e = ualloc(&U->d2, level_px(U, 2) * 64);
     if (e == cudaSuccess) e = ualloc(&U->p2, level_px(U, 3) * 64);
     if (e == cudaSuccess) e = ualloc(&U->e3, level_px(U, 3) * 64);
@@ -705,7 +708,7 @@ int lsdtt_gpu_unet_apply(lsdtt_gpu_unet* U, const float* r_dev, int32_t H, int32
     if (!U || !r_dev || !y_dev) return fail(LSDTT_GPU_EINVAL, "lsdtt_gpu_unet_apply: null argument");
     if (int s = check_shape(U, H, W)) return s;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    cudaError_t e = unet_forward(U, r_dev, H, W, st);
+    cudaError_t e = unet_forward(U, r_dev, H, W, st, false);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(y_dev, U->y, sizeof(float) * static_cast<std::size_t>(H) * W, cudaMemcpyDeviceToDevice, st);
     return e == cudaSuccess ? LSDTT_GPU_OK : cuda_fail(e, "lsdtt_gpu_unet_apply");
@@ -724,7 +727,11 @@ int lsdtt_gpu_unet_loss_grad(lsdtt_gpu_unet* U, const float* r_dev, const float*
     {
         // Backward scratch (FP32, 4x the bf16 activations): only when training.
         const std::int64_t px0 = level_px(U, 0);
-        e = ualloc(&U->gA, px0 * 16);
+        // decoder pre-activations (ReLU masks of the backward pass)
+        e = ualloc(&U->a0, px0 * 16);
+        if (e == cudaSuccess) e = ualloc(&U->a1, level_px(U, 1) * 32);
+        if (e == cudaSuccess) e = ualloc(&U->a2, level_px(U, 2) * 64);
+        if (e == cudaSuccess) e = ualloc(&U->gA, px0 * 16);
         if (e == cudaSuccess) e = ualloc(&U->gB, px0 * 16);
         if (e == cudaSuccess) e = ualloc(&U->ge0, px0 * 16);
         if (e == cudaSuccess) e = ualloc(&U->ge1, level_px(U, 1) * 32);
@@ -732,13 +739,14 @@ int lsdtt_gpu_unet_loss_grad(lsdtt_gpu_unet* U, const float* r_dev, const float*
         if (e == cudaSuccess) e = ualloc(&U->ge3, level_px(U, 3) * 64);
         if (e != cudaSuccess)
         {
-            void* bufs[] = {U->gA, U->gB, U->ge0, U->ge1, U->ge2, U->ge3};
+            void* bufs[] = {U->a0, U->a1, U->a2, U->gA, U->gB, U->ge0, U->ge1, U->ge2, U->ge3};
             for (void* b : bufs) cudaFree(b);
+            U->a0 = U->a1 = U->a2 = nullptr;
             U->gA = U->gB = U->ge0 = U->ge1 = U->ge2 = U->ge3 = nullptr;
             return cuda_fail(e, "lsdtt_gpu_unet_loss_grad");
         }
     }
-    e = unet_forward(U, r_dev, H, W, st);
+    e = unet_forward(U, r_dev, H, W, st, true);
     if (e == cudaSuccess) e = unet_backward(U, e_dev, H, W, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(U->hacc, U->acc + 1, sizeof(double) * 2, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess && grad_host)

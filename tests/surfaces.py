@@ -74,3 +74,22 @@ def noise_tilt(n_rows: int, n_cols: int, cell: float, seed: int, bc: str = "nnon
     if np.isfinite(dist).all():
         z = z + slope * cell * dist
     return z.astype(np.float32)
+
+
+def fractal_subcritical(n_rows: int, n_cols: int, cell: float, critical_slope: float, seed: int,
+                        target: float = 0.8, beta: float = 2.0):
+    """A k^-2 fractal scaled so that its steepest slope -- the larger of the
+    central-difference gradient magnitude and the face slope |dz|/dx over
+    the whole grid -- is target * critical_slope: the Roering law is well
+    posed on it everywhere (slopes at or above Sc have no feasible implicit
+    step). Returns (z, relief in m)."""
+    z = fractal(n_rows, n_cols, 1.0, seed, beta)
+    smax = 0.0
+    for r0 in range(0, n_rows, 2048):  # row bands keep the temporaries small
+        w = z[max(0, r0 - 1):min(n_rows, r0 + 2049)].astype(np.float64)
+        gx = (w[1:-1, 2:] - w[1:-1, :-2]) / (2.0 * cell)
+        gy = (w[2:, 1:-1] - w[:-2, 1:-1]) / (2.0 * cell)
+        smax = max(smax, float(np.sqrt(gx * gx + gy * gy).max()))
+        smax = max(smax, float(np.abs(np.diff(w, axis=1)).max()) / cell, float(np.abs(np.diff(w, axis=0)).max()) / cell)
+    scale = target * critical_slope / smax
+    return (z * np.float32(scale)).astype(np.float32), scale
