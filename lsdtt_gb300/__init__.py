@@ -594,6 +594,8 @@ class UNet:
              ctypes.c_int),
             ("lsdtt_gpu_unet_train_step", [vp, vp, vp, i32, i32, i32, ctypes.c_float,
                                            ctypes.POINTER(ctypes.c_double), vp], ctypes.c_int),
+            ("lsdtt_gpu_unet_set_conv_kernel", [vp, i32], ctypes.c_int),
+            ("lsdtt_gpu_unet_status", [vp], ctypes.c_int),
         ]:
             fn = getattr(L, name)
             fn.argtypes = args
@@ -602,6 +604,14 @@ class UNet:
         _check(L.lsdtt_gpu_unet_create(max_rows, max_cols, seed, ctypes.byref(h)))
         self._h = h
         self.n_params = int(L.lsdtt_gpu_unet_num_params(h))
+
+    def set_conv_kernel(self, kind: str) -> None:
+        """'mma' (mma.sync m16n8k16) or 'tcgen05' (UMMA, accumulator in TMEM)."""
+        _check(lib().lsdtt_gpu_unet_set_conv_kernel(self._h, {"mma": 0, "tcgen05": 1}[kind]))
+
+    def status(self) -> None:
+        """Raises if a tensor-core convolution gave up waiting for its MMAs."""
+        _check(lib().lsdtt_gpu_unet_status(self._h))
 
     def get_params(self) -> np.ndarray:
         out = np.empty(self.n_params, np.float32)

@@ -20,6 +20,7 @@
 // (data and weight gradients, FP32) run on the CUDA cores; Adam updates the
 // FP32 master weights and re-packs bf16 copies.
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -196,6 +197,246 @@ __global__ void __launch_bounds__(128) k_conv_tc(int H, int W, int up, const __n
             }
         }
     }
+}
+
+// ---------------------------------------------------------------------------
+// The same convolutions on the 5th-generation tensor cores (tcgen05).
+//
+// One CTA (4 warps) works through tiles of kTcM = 128 consecutive output
+// pixels of one row; each tile is one UMMA of M = 128, N = COUT per K-step,
+// K = 9 taps x CIN in steps of 16, BF16 operands from shared memory, FP32
+// accumulator in tensor memory (TMEM), issued by one thread.
+//
+// Shared memory, canonical K-major layouts without swizzle (8-row x 16-byte
+// core matrices):
+//   halo: the 3 x 130 input pixels the tile reads (zero outside the image,
+//         nearest upsampling folded in), stored per row as CIN/8 chunks of
+//         130 contiguous 16-byte pixel rows. The A operand of tap (dy, dx)
+//         is then a descriptor into it: start = row dy + dx pixels, the
+//         8-row groups 128 B apart (SBO), the K chunks one chunk apart (LBO).
+//   B:    the layer's weights for all 9 taps, per tap [COUT/8 groups][CIN/8
+//         chunks][8 rows x 16 B], staged once per CTA.
+// The epilogue reads the accumulator with tcgen05.ld (warp w owns TMEM lanes
+// = tile pixels 32w..32w+31) and fuses bias, ReLU, the decoder skip and the
+// BF16 store. Every wait on the MMA barrier is bounded: on expiry the kernel
+// records an error, waits once more (bounded) for its MMAs, frees its TMEM
+// and returns.
+constexpr int kTcM = 128;
+constexpr int kHaloW = kTcM + 2;
+constexpr int kChunkBytes = kHaloW * 16;
+constexpr int kTcSpin = 1 << 22;
+
+template <int CIN, int COUT>
+struct Tc5Layout
+{
+    static constexpr int kChunks = CIN / 8;
+    static constexpr int kRowBytes = kChunks * kChunkBytes;
+    static constexpr int kHaloBytes = 3 * kRowBytes;
+    static constexpr int kSboB = kChunks * 128;
+    static constexpr int kTapBytes = (COUT / 8) * kSboB;
+    static constexpr int kBBytes = 9 * kTapBytes;
+    static constexpr int kBarOff = kHaloBytes + kBBytes;  // mbarrier (8 B) then TMEM address (4 B)
+    // At least 64 KB: the A descriptors span 16 groups x 2080 B if their two
+    // byte offsets were read the other way round; keep any such read inside.
+    static constexpr int kSmem = (kBarOff + 64) > 65536 ? (kBarOff + 64) : 65536;
+    static constexpr int kTmemCols = COUT < 32 ? 32 : COUT;
+    static_assert(CIN % 16 == 0 && COUT % 16 == 0 && COUT <= 256, "UMMA shape");
+    static_assert(kSmem <= 227 * 1024, "shared memory");
+};
+
+// Shared-memory matrix descriptor: start, leading (K) and stride (M/N) byte
+// offsets in 16-byte units, descriptor version 1, no swizzle.
+__device__ __forceinline__ std::uint64_t tc5_desc(std::uint32_t addr, std::uint32_t lbo, std::uint32_t sbo)
+{
+    return static_cast<std::uint64_t>((addr >> 4) & 0x3FFFu) |
+           (static_cast<std::uint64_t>((lbo >> 4) & 0x3FFFu) << 16) |
+           (static_cast<std::uint64_t>((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+// Instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both
+// K-major, N = COUT, M = 128.
+template <int N>
+__device__ __forceinline__ constexpr std::uint32_t tc5_idesc()
+{
+    return (1u << 4) | (1u << 7) | (1u << 10) | (static_cast<std::uint32_t>(N >> 3) << 17) |
+           (static_cast<std::uint32_t>(kTcM >> 4) << 24);
+}
+
+__device__ __forceinline__ bool tc5_wait(std::uint32_t mbar, std::uint32_t phase)
+{
+    for (int spin = 0; spin < kTcSpin; ++spin)
+    {
+        std::uint32_t ok;
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(ok)
+            : "r"(mbar), "r"(phase)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(128) k_conv_tc5(int H, int W, int up, const __nv_bfloat16* __restrict__ in,
+                                                  const __nv_bfloat16* __restrict__ wpk,
+                                                  const float* __restrict__ bias, int mode,
+                                                  const __nv_bfloat16* __restrict__ skip,
+                                                  __nv_bfloat16* __restrict__ pre, __nv_bfloat16* __restrict__ out,
+                                                  unsigned* __restrict__ err)
+{
+    LSDTT_COUNT();
+    using Lt = Tc5Layout<CIN, COUT>;
+    extern __shared__ __align__(1024) unsigned char tc5_smem[];
+    unsigned char* halo = tc5_smem;
+    unsigned char* bsm = tc5_smem + Lt::kHaloBytes;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const std::uint32_t halo_s = static_cast<std::uint32_t>(__cvta_generic_to_shared(halo));
+    const std::uint32_t b_s = static_cast<std::uint32_t>(__cvta_generic_to_shared(bsm));
+    const std::uint32_t mbar_s = static_cast<std::uint32_t>(__cvta_generic_to_shared(tc5_smem + Lt::kBarOff));
+    const std::uint32_t tslot_s = mbar_s + 16;
+    const std::uint32_t* tslot = reinterpret_cast<const std::uint32_t*>(tc5_smem + Lt::kBarOff + 16);
+
+    // the layer's weights, all taps, in the B layout
+    for (int q = tid; q < 9 * COUT * Lt::kChunks; q += blockDim.x)
+    {
+        const int kc = q % Lt::kChunks;
+        const int rest = q / Lt::kChunks;
+        const int n = rest % COUT, t = rest / COUT;
+        const uint4 v = *reinterpret_cast<const uint4*>(wpk + (static_cast<std::int64_t>(n) * 9 + t) * CIN + kc * 8);
+        *reinterpret_cast<uint4*>(bsm + t * Lt::kTapBytes + (n >> 3) * Lt::kSboB + kc * 128 + (n & 7) * 16) = v;
+    }
+    if (warp == 0)
+    {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tslot_s),
+                     "r"(Lt::kTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0)
+    {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar_s) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const std::uint32_t tmem = *tslot;
+
+    const int Win = up ? (W >> 1) : W;
+    const int tpr = (W + kTcM - 1) / kTcM;
+    const int tiles = H * tpr;
+    std::uint32_t phase = 0;
+    bool failed = false;
+    for (int tile = blockIdx.x; tile < tiles && !failed; tile += gridDim.x)
+    {
+        const int y = tile / tpr, x0 = (tile - y * tpr) * kTcM;
+        for (int q = tid; q < 3 * kHaloW * Lt::kChunks; q += blockDim.x)
+        {
+            const int kc = q % Lt::kChunks;
+            const int rest = q / Lt::kChunks;
+            const int j = rest % kHaloW, dy = rest / kHaloW;
+            const int yy = y + dy - 1, xx = x0 - 1 + j;
+            uint4 v = make_uint4(0u, 0u, 0u, 0u);
+            if (yy >= 0 && yy < H && xx >= 0 && xx < W)
+            {
+                const int sy = up ? (yy >> 1) : yy, sx = up ? (xx >> 1) : xx;
+                v = *reinterpret_cast<const uint4*>(in + (static_cast<std::int64_t>(sy) * Win + sx) * CIN + kc * 8);
+            }
+            *reinterpret_cast<uint4*>(halo + dy * Lt::kRowBytes + kc * kChunkBytes + j * 16) = v;
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        if (tid == 0)
+        {
+            constexpr std::uint32_t idesc = tc5_idesc<COUT>();
+            std::uint32_t accum = 0;
+#pragma unroll 1
+            for (int t = 0; t < 9; ++t)
+            {
+                const int dy = t / 3, dx = t - dy * 3;
+#pragma unroll
+                for (int ks = 0; ks < CIN / 16; ++ks)
+                {
+                    const std::uint64_t ad =
+                        tc5_desc(halo_s + dy * Lt::kRowBytes + 2 * ks * kChunkBytes + dx * 16, kChunkBytes, 128);
+                    const std::uint64_t bd = tc5_desc(b_s + t * Lt::kTapBytes + 2 * ks * 128, 128, Lt::kSboB);
+                    asm volatile(
+                        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+                        "l"(ad), "l"(bd), "r"(idesc), "r"(accum)
+                        : "memory");
+                    accum = 1;
+                }
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar_s)
+                         : "memory");
+        }
+        const bool ok = tc5_wait(mbar_s, phase);
+        if (__syncthreads_or(ok ? 0 : 1))  // block-uniform: every thread leaves together
+        {
+            if (tid == 0) atomicOr(err, 1u);
+            if (!ok) tc5_wait(mbar_s, phase);  // once more for the MMAs in flight, then leave
+            failed = true;
+        }
+        phase ^= 1u;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const int m = warp * 32 + lane;
+        const int x = x0 + m;
+        const std::int64_t o = (static_cast<std::int64_t>(y) * W + x) * COUT;
+#pragma unroll
+        for (int n0 = 0; n0 < COUT; n0 += 16)
+        {
+            std::uint32_t r[16];
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+                "%14, %15}, [%16];\n"
+                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                  "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                  "=r"(r[15])
+                : "r"(tmem + (static_cast<std::uint32_t>(warp * 32) << 16) + static_cast<std::uint32_t>(n0)));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            if (x < W && !failed)
+            {
+                alignas(16) __nv_bfloat16 ov[16];
+                alignas(16) __nv_bfloat16 pv[16];
+                alignas(16) __nv_bfloat16 sv[16];
+                if (mode == 1)
+                {
+                    *reinterpret_cast<uint4*>(sv) = *reinterpret_cast<const uint4*>(skip + o + n0);
+                    *reinterpret_cast<uint4*>(sv + 8) = *reinterpret_cast<const uint4*>(skip + o + n0 + 8);
+                }
+#pragma unroll
+                for (int j = 0; j < 16; ++j)
+                {
+                    const float a = __fadd_rn(__uint_as_float(r[j]), bias[n0 + j]);
+                    if (mode == 0)
+                        ov[j] = __float2bfloat16_rn(fmaxf(a, 0.f));
+                    else
+                    {
+                        pv[j] = __float2bfloat16_rn(a);
+                        ov[j] = __float2bfloat16_rn(__fadd_rn(fmaxf(a, 0.f), __bfloat162float(sv[j])));
+                    }
+                }
+                *reinterpret_cast<uint4*>(out + o + n0) = *reinterpret_cast<const uint4*>(ov);
+                *reinterpret_cast<uint4*>(out + o + n0 + 8) = *reinterpret_cast<const uint4*>(ov + 8);
+                if (mode == 1 && pre)
+                {
+                    *reinterpret_cast<uint4*>(pre + o + n0) = *reinterpret_cast<const uint4*>(pv);
+                    *reinterpret_cast<uint4*>(pre + o + n0 + 8) = *reinterpret_cast<const uint4*>(pv + 8);
+                }
+            }
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncthreads();
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(Lt::kTmemCols)
+                     : "memory");
 }
 
 // Output layer: 16 -> 1 channel, times rms, FP32.
@@ -417,6 +658,8 @@ struct lsdtt_gpu_unet
     std::int64_t woff[kLayers + 1] = {};  // weight offsets into the parameter vector
     std::int64_t boff[kLayers + 1] = {};  // bias offsets
     std::int64_t nparam = 0;
+    int conv_kind = 1;          // 0: mma.sync convolutions, 1: tcgen05 (default)
+    unsigned* d_err = nullptr;  // device error word of the tcgen05 kernels
     float* w = nullptr;   // FP32 master: weights then biases
     float* wr = nullptr;  // bf16-rounded copy as FP32 (CUDA-core layers, backward)
     __nv_bfloat16* wb = nullptr;
@@ -436,6 +679,9 @@ struct lsdtt_gpu_unet
 
 namespace
 {
+
+int unet_conv_kind(const lsdtt_gpu_unet* U) { return U->conv_kind; }
+unsigned* unet_err(const lsdtt_gpu_unet* U) { return U->d_err; }
 
 std::int64_t level_px(const lsdtt_gpu_unet* U, int l)
 {
@@ -458,17 +704,44 @@ int check_shape(const lsdtt_gpu_unet* U, int H, int W)
     return LSDTT_GPU_OK;
 }
 
-void launch_conv_tc(int l, int H, int W, int up, const __nv_bfloat16* in, const __nv_bfloat16* wpk, const float* b,
-                    int mode, const __nv_bfloat16* skip, __nv_bfloat16* pre, __nv_bfloat16* out, cudaStream_t st)
+// Persistent grid of the tcgen05 kernel: every SM, as many CTAs as fit.
+template <int CI, int CO>
+unsigned tc5_grid(int tiles)
+{
+    static int per_sm = -1, sms = 0;
+    if (per_sm < 0)
+    {
+        cudaFuncSetAttribute(k_conv_tc5<CI, CO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             Tc5Layout<CI, CO>::kSmem);
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_conv_tc5<CI, CO>, 128, Tc5Layout<CI, CO>::kSmem);
+        // every resident CTA holds its TMEM columns for its whole life
+        per_sm = std::min(per_sm, 512 / Tc5Layout<CI, CO>::kTmemCols);
+        if (per_sm < 1) per_sm = 1;
+    }
+    return static_cast<unsigned>(std::max(1, std::min(tiles, sms * per_sm)));
+}
+
+void launch_conv_tc(const lsdtt_gpu_unet* U, int l, int H, int W, int up, const __nv_bfloat16* in,
+                    const __nv_bfloat16* wpk, const float* b, int mode, const __nv_bfloat16* skip,
+                    __nv_bfloat16* pre, __nv_bfloat16* out, cudaStream_t st)
 {
     const int warps = H * ((W + 15) / 16);
     const unsigned blocks = static_cast<unsigned>((warps + 3) / 4);
     const double bytes = 2.0 * static_cast<double>(H) * W * (layer_cin(l) / (up ? 4.0 : 1.0) + layer_cout(l));
+    const int tiles = H * ((W + kTcM - 1) / kTcM);
 #define LSDTT_CONV_CASE(CI, CO)                                                                                     \
     if (layer_cin(l) == CI && layer_cout(l) == CO)                                                                  \
     {                                                                                                               \
-        LSDTT_TIMED("unet_conv_tc", bytes, st,                                                                      \
-                    (k_conv_tc<CI, CO><<<blocks, 128, 0, st>>>(H, W, up, in, wpk, b, mode, skip, pre, out)));       \
+        if (unet_conv_kind(U) == 1)                                                                                 \
+            LSDTT_TIMED("unet_conv_tc5", bytes, st,                                                                 \
+                        (k_conv_tc5<CI, CO><<<tc5_grid<CI, CO>(tiles), 128, Tc5Layout<CI, CO>::kSmem, st>>>(       \
+                            H, W, up, in, wpk, b, mode, skip, pre, out, unet_err(U))));                            \
+        else                                                                                                        \
+            LSDTT_TIMED("unet_conv_tc", bytes, st,                                                                  \
+                        (k_conv_tc<CI, CO><<<blocks, 128, 0, st>>>(H, W, up, in, wpk, b, mode, skip, pre, out)));   \
         return;                                                                                                     \
     }
     LSDTT_CONV_CASE(16, 32)
@@ -492,18 +765,18 @@ cudaError_t unet_forward(lsdtt_gpu_unet* U, const float* r, int H, int W, cudaSt
     k_conv_in<<<grid_blocks(n, 128), 128, 0, st>>>(H, W, U->x0, wr + U->woff[0], U->w + U->boff[0], U->e0);
     int h = H / 2, w = W / 2;
     k_pool<<<grid_blocks(static_cast<std::int64_t>(h) * w * 16, 256), 256, 0, st>>>(h, w, 16, U->e0, U->p0);
-    launch_conv_tc(1, h, w, 0, U->p0, U->wb + U->woff[1], U->w + U->boff[1], 0, nullptr, nullptr, U->e1, st);
+    launch_conv_tc(U, 1, h, w, 0, U->p0, U->wb + U->woff[1], U->w + U->boff[1], 0, nullptr, nullptr, U->e1, st);
     h /= 2; w /= 2;
     k_pool<<<grid_blocks(static_cast<std::int64_t>(h) * w * 32, 256), 256, 0, st>>>(h, w, 32, U->e1, U->p1);
-    launch_conv_tc(2, h, w, 0, U->p1, U->wb + U->woff[2], U->w + U->boff[2], 0, nullptr, nullptr, U->e2, st);
+    launch_conv_tc(U, 2, h, w, 0, U->p1, U->wb + U->woff[2], U->w + U->boff[2], 0, nullptr, nullptr, U->e2, st);
     h /= 2; w /= 2;
     k_pool<<<grid_blocks(static_cast<std::int64_t>(h) * w * 64, 256), 256, 0, st>>>(h, w, 64, U->e2, U->p2);
-    launch_conv_tc(3, h, w, 0, U->p2, U->wb + U->woff[3], U->w + U->boff[3], 0, nullptr, nullptr, U->e3, st);
-    launch_conv_tc(4, H / 4, W / 4, 1, U->e3, U->wb + U->woff[4], U->w + U->boff[4], 1, U->e2,
+    launch_conv_tc(U, 3, h, w, 0, U->p2, U->wb + U->woff[3], U->w + U->boff[3], 0, nullptr, nullptr, U->e3, st);
+    launch_conv_tc(U, 4, H / 4, W / 4, 1, U->e3, U->wb + U->woff[4], U->w + U->boff[4], 1, U->e2,
                    for_training ? U->a2 : nullptr, U->d2, st);
-    launch_conv_tc(5, H / 2, W / 2, 1, U->d2, U->wb + U->woff[5], U->w + U->boff[5], 1, U->e1,
+    launch_conv_tc(U, 5, H / 2, W / 2, 1, U->d2, U->wb + U->woff[5], U->w + U->boff[5], 1, U->e1,
                    for_training ? U->a1 : nullptr, U->d1, st);
-    launch_conv_tc(6, H, W, 1, U->d1, U->wb + U->woff[6], U->w + U->boff[6], 1, U->e0,
+    launch_conv_tc(U, 6, H, W, 1, U->d1, U->wb + U->woff[6], U->w + U->boff[6], 1, U->e0,
                    for_training ? U->a0 : nullptr, U->d0, st);
     k_conv_out<<<grid_blocks(n, 128), 128, 0, st>>>(H, W, U->d0, wr + U->woff[7], U->w + U->boff[7], U->rms, U->y);
     return cudaGetLastError();
@@ -649,6 +922,8 @@ int lsdtt_gpu_unet_create(int32_t max_rows, int32_t max_cols, uint64_t seed, lsd
     if (e == cudaSuccess) e = ualloc(&U->go, px0);
     if (e == cudaSuccess) e = ualloc(&U->rms, 1);
     if (e == cudaSuccess) e = ualloc(&U->acc, 4);
+    if (e == cudaSuccess) e = ualloc(&U->d_err, 1);
+    if (e == cudaSuccess) e = cudaMemset(U->d_err, 0, sizeof(unsigned));
     if (e == cudaSuccess) e = cudaMallocHost(reinterpret_cast<void**>(&U->hacc), sizeof(double) * 4);
     if (e == cudaSuccess) e = cudaMemcpy(U->w, h.data(), sizeof(float) * off, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemset(U->m, 0, sizeof(float) * off);
@@ -675,7 +950,7 @@ int lsdtt_gpu_unet_destroy(lsdtt_gpu_unet* U)
     if (!U) return LSDTT_GPU_OK;
     void* ptrs[] = {U->w, U->wr, U->wb, U->g, U->m, U->v, U->x0, U->e0, U->a0, U->d0, U->p0, U->e1, U->a1, U->d1, U->p1,
                     U->e2, U->a2, U->d2, U->p2, U->e3, U->y, U->go, U->rms, U->acc, U->gA, U->gB, U->ge0, U->ge1,
-                    U->ge2, U->ge3};
+                    U->ge2, U->ge3, U->d_err};
     for (void* p : ptrs) cudaFree(p);
     cudaFreeHost(U->hacc);
     delete U;
@@ -683,6 +958,23 @@ int lsdtt_gpu_unet_destroy(lsdtt_gpu_unet* U)
 }
 
 int64_t lsdtt_gpu_unet_num_params(const lsdtt_gpu_unet* U) { return U ? U->nparam : 0; }
+
+int lsdtt_gpu_unet_set_conv_kernel(lsdtt_gpu_unet* U, int32_t kind)
+{
+    if (!U || (kind != 0 && kind != 1)) return fail(LSDTT_GPU_EINVAL, "lsdtt_gpu_unet_set_conv_kernel: bad argument");
+    U->conv_kind = kind;
+    return LSDTT_GPU_OK;
+}
+
+int lsdtt_gpu_unet_status(const lsdtt_gpu_unet* U)
+{
+    if (!U) return fail(LSDTT_GPU_EINVAL, "lsdtt_gpu_unet_status: null");
+    unsigned h = 0;
+    if (cudaMemcpy(&h, U->d_err, sizeof(h), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return fail(LSDTT_GPU_ECUDA, "lsdtt_gpu_unet_status: copy failed");
+    if (h) return fail(LSDTT_GPU_ETIMEOUT, "lsdtt_gpu_unet: a tensor-core convolution hit its barrier wait limit");
+    return LSDTT_GPU_OK;
+}
 
 int lsdtt_gpu_unet_get_params(const lsdtt_gpu_unet* U, float* host, int64_t count)
 {

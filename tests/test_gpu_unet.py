@@ -1,7 +1,8 @@
 """The learned hillslope preconditioner on the GPU.
 
 - forward pass and parameter gradients of the CUDA U-Net against the CPU
-  oracle (oracle/unet.py) on the same BF16 weights;
+  oracle (oracle/unet.py) on the same BF16 weights, and the tcgen05
+  convolutions against the mma.sync ones;
 - parameter round trip and shape errors;
 - training on residual/correction pairs captured from the plain solver
   lowers the loss;
@@ -51,6 +52,27 @@ def test_forward_matches_oracle(shape):
     err = _rel(y, y_ref)
     print(f"forward {shape}: relative L2 error {err:.3e}")
     assert err < FWD_TOL
+
+
+@pytest.mark.parametrize("shape", [(32, 32), (48, 64), (256, 392)])
+def test_tcgen05_convolutions_match_mma_and_oracle(shape):
+    # The tcgen05 (UMMA) convolutions against the mma.sync ones and the CPU
+    # oracle on the same BF16 weights; 256 x 392 has rows that are not a
+    # multiple of the 128-pixel tile.
+    import lsdtt_gb300 as G
+    P = _params()
+    r = np.random.default_rng(6).normal(0, 2.0, shape).astype(np.float32)
+    net = G.UNet(256, 392)
+    net.set_params(G.unet_flatten(P))
+    net.set_conv_kernel("mma")
+    y_mma = net.apply(r).cpu().numpy()
+    net.set_conv_kernel("tcgen05")
+    y_tc5 = net.apply(r).cpu().numpy()
+    net.status()
+    y_ref, _ = unet.forward(P, r)
+    e_mma, e_tc5, e_pair = _rel(y_mma, y_ref), _rel(y_tc5, y_ref), _rel(y_tc5, y_mma)
+    print(f"{shape}: mma.sync vs oracle {e_mma:.2e}, tcgen05 vs oracle {e_tc5:.2e}, tcgen05 vs mma.sync {e_pair:.2e}")
+    assert e_tc5 < FWD_TOL and e_pair < FWD_TOL
 
 
 def test_gradients_match_oracle():
