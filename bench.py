@@ -707,10 +707,25 @@ def hillslope_gpu(args, rank, world):
             res.setdefault(form, []).append({"s": time.perf_counter() - t0, **rep.as_dict()})
             res.setdefault(form + "_z", []).append(zo)
     diffs = [float(((a - b).abs().max()).item()) for a, b in zip(res.pop("plain_z"), res.pop("learned_z"))]
+    # kernel table of one more learned solve (CUDA events per launch)
+    L = G.lib()
+    L.lsdtt_gpu_profile_read.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_double),
+                                         ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_double)]
+    L.lsdtt_gpu_profile_enable(1)
+    G.hillslope_implicit(z, m, 5.0, "oooo", 0.01, 1.0, dt, nonlinear=True, rel_tol=1e-8, max_pcg_iter=20000, net=net)
+    torch.cuda.synchronize()
+    kernels = {}
+    for name in ("unet_conv_tc5", "unet_conv_tc", "unet_conv_in", "unet_conv_out", "unet_pool", "hillslope_apply"):
+        t, k, b = ctypes.c_double(), ctypes.c_int64(), ctypes.c_double()
+        G._check(L.lsdtt_gpu_profile_read(name.encode(), ctypes.byref(t), ctypes.byref(k), ctypes.byref(b)))
+        if k.value:
+            kernels[name] = {"total_ms": t.value, "launches": k.value, "GBps": b.value / (t.value / 1e3) / 1e9}
+    L.lsdtt_gpu_profile_enable(0)
     line = {"workload": f"Roering implicit hillslope step {n}x{n}, dx=5 m, k^-2 fractal scaled to a steepest "
                         f"slope of 0.8 Sc, D=0.01, Sc=1.0, dt={dt} (D dt/dx^2 = 10), PCG 1e-8", "reliefs_m": reliefs,
             "training": tinfo,
-            "plain": res["plain"], "learned": res["learned"], "max_abs_surface_diff_m": diffs}
+            "plain": res["plain"], "learned": res["learned"], "max_abs_surface_diff_m": diffs,
+            "learned_solve_kernels": kernels}
     if rank == 0:
         print(json.dumps(line), flush=True)
     return 0

@@ -87,14 +87,17 @@ __global__ void k_conv_in(int H, int W, const __nv_bfloat16* __restrict__ x0, co
         const int yy = y + t / 3 - 1, xx = x + t % 3 - 1;
         v[t] = (yy >= 0 && yy < H && xx >= 0 && xx < W) ? __bfloat162float(x0[static_cast<std::int64_t>(yy) * W + xx]) : 0.f;
     }
+    alignas(16) __nv_bfloat16 o16[16];
 #pragma unroll
     for (int co = 0; co < 16; ++co)
     {
         float s = b[co];
 #pragma unroll
         for (int t = 0; t < 9; ++t) s = __fadd_rn(s, __fmul_rn(v[t], w[co * 9 + t]));
-        out[p * 16 + co] = __float2bfloat16_rn(fmaxf(s, 0.f));
+        o16[co] = __float2bfloat16_rn(fmaxf(s, 0.f));
     }
+    *reinterpret_cast<uint4*>(out + p * 16) = *reinterpret_cast<const uint4*>(o16);
+    *reinterpret_cast<uint4*>(out + p * 16 + 8) = *reinterpret_cast<const uint4*>(o16 + 8);
 }
 
 // 2x2 mean, bf16 -> bf16 (H, W are the OUTPUT sizes)
@@ -231,15 +234,17 @@ struct Tc5Layout
 {
     static constexpr int kChunks = CIN / 8;
     static constexpr int kRowBytes = kChunks * kChunkBytes;
-    static constexpr int kHaloBytes = 3 * kRowBytes;
+    static constexpr int kHaloBytes = 3 * kRowBytes;      // one halo buffer (two are kept)
     static constexpr int kSboB = kChunks * 128;
     static constexpr int kTapBytes = (COUT / 8) * kSboB;
     static constexpr int kBBytes = 9 * kTapBytes;
-    static constexpr int kBarOff = kHaloBytes + kBBytes;  // mbarrier (8 B) then TMEM address (4 B)
+    static constexpr int kBOff = 2 * kHaloBytes;
+    static constexpr int kBarOff = kBOff + kBBytes;        // two mbarriers (16 B) then the TMEM address
     // At least 64 KB: the A descriptors span 16 groups x 2080 B if their two
     // byte offsets were read the other way round; keep any such read inside.
     static constexpr int kSmem = (kBarOff + 64) > 65536 ? (kBarOff + 64) : 65536;
-    static constexpr int kTmemCols = COUT < 32 ? 32 : COUT;
+    static constexpr int kAccCols = COUT < 32 ? 32 : COUT;
+    static constexpr int kTmemCols = 2 * kAccCols;         // two accumulators
     static_assert(CIN % 16 == 0 && COUT % 16 == 0 && COUT <= 256, "UMMA shape");
     static_assert(kSmem <= 227 * 1024, "shared memory");
 };
@@ -277,6 +282,63 @@ __device__ __forceinline__ bool tc5_wait(std::uint32_t mbar, std::uint32_t phase
     return false;
 }
 
+// Stage the 3 x 130-pixel input halo of tile (y, x0) with 16-byte cp.async
+// copies (zero-filled outside the image; nearest upsampling folded in).
+template <int CIN>
+__device__ __forceinline__ void tc5_stage(std::uint32_t halo_s, const __nv_bfloat16* __restrict__ in, int H, int W,
+                                          int Win, int up, int y, int x0)
+{
+    constexpr int kCh = CIN / 8;
+    for (int q = threadIdx.x; q < 3 * kHaloW * kCh; q += blockDim.x)
+    {
+        const int kc = q % kCh;
+        const int rest = q / kCh;
+        const int j = rest % kHaloW, dy = rest / kHaloW;
+        const int yy = y + dy - 1, xx = x0 - 1 + j;
+        const bool inside = yy >= 0 && yy < H && xx >= 0 && xx < W;
+        const int sy = inside ? (up ? (yy >> 1) : yy) : 0, sx = inside ? (up ? (xx >> 1) : xx) : 0;
+        const __nv_bfloat16* src = in + (static_cast<std::int64_t>(sy) * Win + sx) * CIN + kc * 8;
+        const std::uint32_t dst = halo_s + dy * (kCh * kChunkBytes) + kc * kChunkBytes + j * 16;
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(inside ? 16 : 0)
+                     : "memory");
+    }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+
+// Issue the 9 x CIN/16 UMMAs of one tile into accumulator column `acc`, then
+// commit to the tile's barrier (one thread).
+template <int CIN, int COUT>
+__device__ __forceinline__ void tc5_issue(std::uint32_t tmem_acc, std::uint32_t halo_s, std::uint32_t b_s,
+                                          std::uint32_t mbar_s)
+{
+    using Lt = Tc5Layout<CIN, COUT>;
+    constexpr std::uint32_t idesc = tc5_idesc<COUT>();
+    std::uint32_t accum = 0;
+#pragma unroll 1
+    for (int t = 0; t < 9; ++t)
+    {
+        const int dy = t / 3, dx = t - dy * 3;
+#pragma unroll
+        for (int ks = 0; ks < CIN / 16; ++ks)
+        {
+            const std::uint64_t ad =
+                tc5_desc(halo_s + dy * Lt::kRowBytes + 2 * ks * kChunkBytes + dx * 16, kChunkBytes, 128);
+            const std::uint64_t bd = tc5_desc(b_s + t * Lt::kTapBytes + 2 * ks * 128, 128, Lt::kSboB);
+            asm volatile(
+                "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_acc),
+                "l"(ad), "l"(bd), "r"(idesc), "r"(accum)
+                : "memory");
+            accum = 1;
+        }
+    }
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar_s)
+                 : "memory");
+}
+
+// Pipelined over a CTA's tiles: while the tensor core works on tile i, the
+// CTA stages tile i + 1 (second halo buffer) and then drains tile i's
+// accumulator (second TMEM accumulator) through the epilogue.
 template <int CIN, int COUT>
 __global__ void __launch_bounds__(128) k_conv_tc5(int H, int W, int up, const __nv_bfloat16* __restrict__ in,
                                                   const __nv_bfloat16* __restrict__ wpk,
@@ -288,16 +350,14 @@ __global__ void __launch_bounds__(128) k_conv_tc5(int H, int W, int up, const __
     LSDTT_COUNT();
     using Lt = Tc5Layout<CIN, COUT>;
     extern __shared__ __align__(1024) unsigned char tc5_smem[];
-    unsigned char* halo = tc5_smem;
-    unsigned char* bsm = tc5_smem + Lt::kHaloBytes;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const std::uint32_t halo_s = static_cast<std::uint32_t>(__cvta_generic_to_shared(halo));
-    const std::uint32_t b_s = static_cast<std::uint32_t>(__cvta_generic_to_shared(bsm));
-    const std::uint32_t mbar_s = static_cast<std::uint32_t>(__cvta_generic_to_shared(tc5_smem + Lt::kBarOff));
+    const std::uint32_t base_s = static_cast<std::uint32_t>(__cvta_generic_to_shared(tc5_smem));
+    const std::uint32_t b_s = base_s + Lt::kBOff;
+    const std::uint32_t mbar_s = base_s + Lt::kBarOff;  // [0], [8]: per accumulator
     const std::uint32_t tslot_s = mbar_s + 16;
     const std::uint32_t* tslot = reinterpret_cast<const std::uint32_t*>(tc5_smem + Lt::kBarOff + 16);
+    unsigned char* bsm = tc5_smem + Lt::kBOff;
 
-    // the layer's weights, all taps, in the B layout
     for (int q = tid; q < 9 * COUT * Lt::kChunks; q += blockDim.x)
     {
         const int kc = q % Lt::kChunks;
@@ -316,74 +376,52 @@ __global__ void __launch_bounds__(128) k_conv_tc5(int H, int W, int up, const __
     if (tid == 0)
     {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar_s) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar_s + 8) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
+    const int Win = up ? (W >> 1) : W;
+    const int tpr = (W + kTcM - 1) / kTcM;
+    const int tiles = H * tpr;
+    int tile = blockIdx.x;
+    // prologue: stage the first tile
+    if (tile < tiles) tc5_stage<CIN>(base_s, in, H, W, Win, up, tile / tpr, (tile % tpr) * kTcM);
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const std::uint32_t tmem = *tslot;
+    if (tid == 0 && tile < tiles) tc5_issue<CIN, COUT>(tmem, base_s, b_s, mbar_s);
 
-    const int Win = up ? (W >> 1) : W;
-    const int tpr = (W + kTcM - 1) / kTcM;
-    const int tiles = H * tpr;
-    std::uint32_t phase = 0;
+    std::uint32_t phase[2] = {0u, 0u};
     bool failed = false;
-    for (int tile = blockIdx.x; tile < tiles && !failed; tile += gridDim.x)
+    for (int it = 0; tile < tiles && !failed; ++it, tile += gridDim.x)
     {
-        const int y = tile / tpr, x0 = (tile - y * tpr) * kTcM;
-        for (int q = tid; q < 3 * kHaloW * Lt::kChunks; q += blockDim.x)
-        {
-            const int kc = q % Lt::kChunks;
-            const int rest = q / Lt::kChunks;
-            const int j = rest % kHaloW, dy = rest / kHaloW;
-            const int yy = y + dy - 1, xx = x0 - 1 + j;
-            uint4 v = make_uint4(0u, 0u, 0u, 0u);
-            if (yy >= 0 && yy < H && xx >= 0 && xx < W)
-            {
-                const int sy = up ? (yy >> 1) : yy, sx = up ? (xx >> 1) : xx;
-                v = *reinterpret_cast<const uint4*>(in + (static_cast<std::int64_t>(sy) * Win + sx) * CIN + kc * 8);
-            }
-            *reinterpret_cast<uint4*>(halo + dy * Lt::kRowBytes + kc * kChunkBytes + j * 16) = v;
-        }
+        const int cur = it & 1, nxt = cur ^ 1;
+        const int ntile = tile + static_cast<int>(gridDim.x);
+        // stage the next tile into the other halo buffer while the tensor
+        // core works on this one (its MMAs read only halo[cur])
+        if (ntile < tiles)
+            tc5_stage<CIN>(base_s + nxt * Lt::kHaloBytes, in, H, W, Win, up, ntile / tpr, (ntile % tpr) * kTcM);
+        asm volatile("cp.async.wait_group 0;\n" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-        __syncthreads();
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        if (tid == 0)
-        {
-            constexpr std::uint32_t idesc = tc5_idesc<COUT>();
-            std::uint32_t accum = 0;
-#pragma unroll 1
-            for (int t = 0; t < 9; ++t)
-            {
-                const int dy = t / 3, dx = t - dy * 3;
-#pragma unroll
-                for (int ks = 0; ks < CIN / 16; ++ks)
-                {
-                    const std::uint64_t ad =
-                        tc5_desc(halo_s + dy * Lt::kRowBytes + 2 * ks * kChunkBytes + dx * 16, kChunkBytes, 128);
-                    const std::uint64_t bd = tc5_desc(b_s + t * Lt::kTapBytes + 2 * ks * 128, 128, Lt::kSboB);
-                    asm volatile(
-                        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-                        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
-                        "l"(ad), "l"(bd), "r"(idesc), "r"(accum)
-                        : "memory");
-                    accum = 1;
-                }
-            }
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar_s)
-                         : "memory");
-        }
-        const bool ok = tc5_wait(mbar_s, phase);
+        // this tile's MMAs
+        const bool ok = tc5_wait(mbar_s + 8 * cur, phase[cur]);
         if (__syncthreads_or(ok ? 0 : 1))  // block-uniform: every thread leaves together
         {
             if (tid == 0) atomicOr(err, 1u);
-            if (!ok) tc5_wait(mbar_s, phase);  // once more for the MMAs in flight, then leave
+            if (!ok) tc5_wait(mbar_s + 8 * cur, phase[cur]);  // once more for the MMAs in flight
             failed = true;
+            break;
         }
-        phase ^= 1u;
+        phase[cur] ^= 1u;
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        // next tile's MMAs into the other accumulator (the barrier above also
+        // ordered every thread's staging of halo[nxt] before them)
+        if (tid == 0 && ntile < tiles)
+            tc5_issue<CIN, COUT>(tmem + nxt * Lt::kAccCols, base_s + nxt * Lt::kHaloBytes, b_s, mbar_s + 8 * nxt);
+        // epilogue of this tile
+        const int y = tile / tpr, x0 = (tile % tpr) * kTcM;
         const int m = warp * 32 + lane;
         const int x = x0 + m;
         const std::int64_t o = (static_cast<std::int64_t>(y) * W + x) * COUT;
@@ -397,9 +435,10 @@ __global__ void __launch_bounds__(128) k_conv_tc5(int H, int W, int up, const __
                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
                   "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
                   "=r"(r[15])
-                : "r"(tmem + (static_cast<std::uint32_t>(warp * 32) << 16) + static_cast<std::uint32_t>(n0)));
+                : "r"(tmem + cur * Lt::kAccCols + (static_cast<std::uint32_t>(warp * 32) << 16) +
+                      static_cast<std::uint32_t>(n0)));
             asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-            if (x < W && !failed)
+            if (x < W)
             {
                 alignas(16) __nv_bfloat16 ov[16];
                 alignas(16) __nv_bfloat16 pv[16];
@@ -430,9 +469,13 @@ __global__ void __launch_bounds__(128) k_conv_tc5(int H, int W, int up, const __
                 }
             }
         }
+        // accumulator[cur] and halo[cur] are free once every warp is past here
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     if (warp == 0)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(Lt::kTmemCols)
@@ -453,8 +496,11 @@ __global__ void k_conv_out(int H, int W, const __nv_bfloat16* __restrict__ d0, c
         const int yy = py + t / 3 - 1, xx = px + t % 3 - 1;
         if (yy < 0 || yy >= H || xx < 0 || xx >= W) continue;
         const __nv_bfloat16* src = d0 + (static_cast<std::int64_t>(yy) * W + xx) * 16;
+        alignas(16) __nv_bfloat16 v16[16];
+        *reinterpret_cast<uint4*>(v16) = *reinterpret_cast<const uint4*>(src);
+        *reinterpret_cast<uint4*>(v16 + 8) = *reinterpret_cast<const uint4*>(src + 8);
 #pragma unroll
-        for (int c = 0; c < 16; ++c) s = __fadd_rn(s, __fmul_rn(__bfloat162float(src[c]), w[t * 16 + c]));
+        for (int c = 0; c < 16; ++c) s = __fadd_rn(s, __fmul_rn(__bfloat162float(v16[c]), w[t * 16 + c]));
     }
     y[p] = __fmul_rn(s, *rms);
 }
@@ -762,9 +808,14 @@ cudaError_t unet_forward(lsdtt_gpu_unet* U, const float* r, int H, int W, cudaSt
     k_sumsq<<<152 * 4, 256, 0, st>>>(r, n, U->acc);
     k_prep<<<grid_blocks(n, 256), 256, 0, st>>>(r, n, U->acc, U->x0, U->rms);
     const float* wr = U->wr;
-    k_conv_in<<<grid_blocks(n, 128), 128, 0, st>>>(H, W, U->x0, wr + U->woff[0], U->w + U->boff[0], U->e0);
+    // Algorithmic bytes: x0 2 in, e0 32 out per pixel.
+    LSDTT_TIMED("unet_conv_in", 34.0 * static_cast<double>(n), st,
+                (k_conv_in<<<grid_blocks(n, 128), 128, 0, st>>>(H, W, U->x0, wr + U->woff[0], U->w + U->boff[0],
+                                                                 U->e0)));
     int h = H / 2, w = W / 2;
-    k_pool<<<grid_blocks(static_cast<std::int64_t>(h) * w * 16, 256), 256, 0, st>>>(h, w, 16, U->e0, U->p0);
+    LSDTT_TIMED("unet_pool", 40.0 * static_cast<double>(h) * w * 4, st,
+                (k_pool<<<grid_blocks(static_cast<std::int64_t>(h) * w * 16, 256), 256, 0, st>>>(h, w, 16, U->e0,
+                                                                                                  U->p0)));
     launch_conv_tc(U, 1, h, w, 0, U->p0, U->wb + U->woff[1], U->w + U->boff[1], 0, nullptr, nullptr, U->e1, st);
     h /= 2; w /= 2;
     k_pool<<<grid_blocks(static_cast<std::int64_t>(h) * w * 32, 256), 256, 0, st>>>(h, w, 32, U->e1, U->p1);
@@ -778,7 +829,10 @@ cudaError_t unet_forward(lsdtt_gpu_unet* U, const float* r, int H, int W, cudaSt
                    for_training ? U->a1 : nullptr, U->d1, st);
     launch_conv_tc(U, 6, H, W, 1, U->d1, U->wb + U->woff[6], U->w + U->boff[6], 1, U->e0,
                    for_training ? U->a0 : nullptr, U->d0, st);
-    k_conv_out<<<grid_blocks(n, 128), 128, 0, st>>>(H, W, U->d0, wr + U->woff[7], U->w + U->boff[7], U->rms, U->y);
+    // Algorithmic bytes: d0 32 in, y 4 out per pixel.
+    LSDTT_TIMED("unet_conv_out", 36.0 * static_cast<double>(n), st,
+                (k_conv_out<<<grid_blocks(n, 128), 128, 0, st>>>(H, W, U->d0, wr + U->woff[7], U->w + U->boff[7],
+                                                                  U->rms, U->y)));
     return cudaGetLastError();
 }
 
