@@ -455,6 +455,10 @@ def ensemble_gpu(args, rank, world):
         return float(tt.item())
 
     ens = G.Ensemble(specs, use_graph=True)
+    if args.sweep_mode >= 0:
+        # pin the stream-power sweep schedule (a profiler distorts the
+        # autotuner's own timings)
+        ens.override_schedule(sweep_mode=args.sweep_mode)
     t_warm0 = time.perf_counter()
     for _ in range(args.warmup):
         ens.step()
@@ -731,6 +735,38 @@ def hillslope_gpu(args, rank, world):
     return 0
 
 
+def unet_gpu(args, rank, world):
+    """Network applications on one residual image (--size, default 2048):
+    the U-Net forward pass alone, CUDA-event time per application and the
+    tensor-core convolution share."""
+    import torch
+    import lsdtt_gb300 as G
+    n = args.size if args.size != 8192 else 2048
+    net = G.UNet(n, n, seed=3)
+    r = torch.randn(n, n, device="cuda", generator=torch.Generator(device="cuda").manual_seed(1))
+    for _ in range(args.warmup):
+        net.apply(r)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        net.apply(r)
+    e1.record()
+    torch.cuda.synchronize()
+    net.status()
+    ms = e0.elapsed_time(e1) / args.steps
+    # useful FLOPs of one application (2 * 9 * Cin * Cout per output pixel per layer)
+    flops = 0.0
+    for (name, ci, co), px in zip(G.UNET_LAYERS, [n * n, n * n / 4, n * n / 16, n * n / 64, n * n / 16, n * n / 4,
+                                                   n * n, n * n]):
+        flops += 2.0 * 9 * ci * co * px
+    if rank == 0:
+        print(json.dumps({"workload": f"U-Net forward on a {n}x{n} residual", "ms_per_application": ms,
+                          "tflops": flops / (ms / 1e3) / 1e12, "steps": args.steps}), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -740,10 +776,11 @@ def main():
     ap.add_argument("--size", type=int, default=8192)
     ap.add_argument("--cpu-sample", type=int, default=4096)
     ap.add_argument("--skip-cpu", action="store_true")
-    ap.add_argument("--workload", default="ensemble", choices=["ensemble", "routing", "large", "hillslope"])
+    ap.add_argument("--workload", default="ensemble", choices=["ensemble", "routing", "large", "hillslope", "unet"])
     ap.add_argument("--train-surfaces", type=int, default=64)
     ap.add_argument("--train-steps", type=int, default=2000)
     ap.add_argument("--members", type=int, default=256)
+    ap.add_argument("--sweep-mode", type=int, default=-1, help="ensemble sweep: -1 autotuned, 0 levels, 1 dataflow")
     ap.add_argument("--plain-members", type=int, default=16)
     args = ap.parse_args()
     if args.warmup < 3:
@@ -754,6 +791,8 @@ def main():
         return large_gpu(args, rank, world)
     if args.workload == "hillslope":
         return hillslope_gpu(args, rank, world)
+    if args.workload == "unet":
+        return unet_gpu(args, rank, world)
     if args.workload == "routing":
         if args.impl == "reference":
             return routing_reference(args, rank, world)

@@ -219,21 +219,48 @@ __global__ void ens_kam_table(Packed P, const EnsParams* __restrict__ prm, doubl
     tab[t] = sp_kam(q.sp, static_cast<double>(c) * q.dw, q.sp.K);
 }
 
+// Table lookups in place; nodes with larger counts (a few percent, spread
+// so that about half of all warps would hold one) are appended to a compact
+// list with warp-aggregated slots and done densely by ens_kam_big, so no
+// warp idles through the FP64 pow for one lane.
 __global__ void ens_kam(Packed P, const EnsParams* __restrict__ prm, const std::uint8_t* __restrict__ mask,
                         const std::int64_t* __restrict__ receiver, const std::uint64_t* __restrict__ size,
-                        const double* __restrict__ tab, double* __restrict__ kam)
+                        const double* __restrict__ tab, double* __restrict__ kam, std::uint32_t* __restrict__ big,
+                        std::uint32_t* __restrict__ n_big)
 {
     LSDTT_COUNT();
     const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i >= P.n || !mask[i] || receiver[i] < 0) return;
-    const int m = member_of(P, i);
-    const std::uint64_t c = size[i];
-    if (c < static_cast<std::uint64_t>(kKamTab))
-        kam[i] = tab[static_cast<std::int64_t>(m) * kKamTab + static_cast<std::int64_t>(c)];
-    else
+    bool need = false;
+    if (i < P.n && mask[i] && receiver[i] >= 0)
     {
-        const EnsParams& q = prm[m];
-        kam[i] = sp_kam(q.sp, static_cast<double>(c) * q.dw, q.sp.K);
+        const int m = member_of(P, i);
+        const std::uint64_t c = size[i];
+        if (c < static_cast<std::uint64_t>(kKamTab))
+            kam[i] = tab[static_cast<std::int64_t>(m) * kKamTab + static_cast<std::int64_t>(c)];
+        else
+            need = true;
+    }
+    const unsigned bal = __ballot_sync(0xffffffffu, need);
+    if (!bal) return;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(bal) - 1;
+    std::uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(n_big, static_cast<unsigned>(__popc(bal)));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (need) big[base + __popc(bal & ((1u << lane) - 1u))] = static_cast<std::uint32_t>(i);
+}
+
+__global__ void ens_kam_big(Packed P, const EnsParams* __restrict__ prm, const std::uint64_t* __restrict__ size,
+                            const std::uint32_t* __restrict__ big, const std::uint32_t* __restrict__ n_big,
+                            double* __restrict__ kam)
+{
+    LSDTT_COUNT();
+    const std::uint32_t nb = *n_big;
+    for (std::uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < nb; k += gridDim.x * blockDim.x)
+    {
+        const std::uint32_t i = big[k];
+        const EnsParams& q = prm[member_of(P, i)];
+        kam[i] = sp_kam(q.sp, static_cast<double>(size[i]) * q.dw, q.sp.K);
     }
 }
 
@@ -601,14 +628,30 @@ __global__ void ens_hs_start(int M, const EnsParams* __restrict__ prm, const dou
 // Ap = A p in the difference form inv_dt p_P + (D/h^2) sum_f (p_P - [nb DOF]
 // p_nb) (faces to the cell itself carry no flux), FP32; block partials of
 // p.Ap. A converged member's blocks return at once.
+// Fused with the CG direction update of the previous iteration: with `fuse`,
+// p = z + beta p_src is formed on the fly at the cell and its neighbours
+// (beta = r.z / r_old.z_old of this member, once per block) and written to
+// p_dst, the buffer the update then reads; without it p_dst already holds p.
 __global__ void ens_hs_apply(Packed P, const EnsParams* __restrict__ prm, const std::uint8_t* __restrict__ mask,
-                             const std::uint8_t* __restrict__ dof, const int* __restrict__ done,
-                             const float* __restrict__ p, float* __restrict__ Ap, double* __restrict__ part)
+                             const std::uint8_t* __restrict__ dof, const int* __restrict__ done, int fuse,
+                             const double* __restrict__ rz_new, const double* __restrict__ rz_old,
+                             const float* __restrict__ zz, const float* __restrict__ p_src,
+                             float* __restrict__ p_dst, float* __restrict__ Ap, double* __restrict__ part)
 {
     LSDTT_COUNT();
     const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     const int m = member_of(P, i < P.n ? i : P.n - 1);
     if (done[m]) return;
+    __shared__ float s_beta;
+    if (threadIdx.x == 0)
+    {
+        const double ro = fuse ? rz_old[m * kHsSlot + 1] : 0.0;
+        s_beta = (fuse && ro > 0.0) ? static_cast<float>(rz_new[m * kHsSlot + 1] / ro) : 0.0f;
+    }
+    __syncthreads();
+    const float beta = s_beta;
+    // p at any cell of the packed buffer
+    auto pv = [&](std::int64_t k) { return fuse ? zz[k] + beta * p_src[k] : p_dst[k]; };
     const PackedMember& M = P.m[m];
     const EnsParams& q = prm[m];
     float pap = 0.0f;
@@ -616,12 +659,13 @@ __global__ void ens_hs_apply(Packed P, const EnsParams* __restrict__ prm, const 
     {
         float v = 0.0f;
         const std::uint8_t kd = dof[i];
+        const float pi = pv(i);
+        if (fuse) p_dst[i] = pi;
         if (kd == 3)
         {
-            const float pi = p[i];
             const int nc = M.nc;
             // the general path's sum, in its order (N, E, S, W)
-            const float s = (((pi - p[i - nc]) + (pi - p[i + 1])) + (pi - p[i + nc])) + (pi - p[i - 1]);
+            const float s = (((pi - pv(i - nc)) + (pi - pv(i + 1))) + (pi - pv(i + nc))) + (pi - pv(i - 1));
             v = q.inv_dt_f * pi + q.DA_f * s;
             pap = pi * v;
         }
@@ -631,8 +675,6 @@ __global__ void ens_hs_apply(Packed P, const EnsParams* __restrict__ prm, const 
             const int r = l / M.nc, c = l - r * M.nc;
             const std::uint8_t* mk = mask + M.base;
             const std::uint8_t* dm = dof + M.base;
-            const float* pm = p + M.base;
-            const float pi = p[i];
             float s = 0.0f;
             if (r > 0 && r < M.nr - 1 && c > 0 && c < M.nc - 1)
             {
@@ -643,7 +685,7 @@ __global__ void ens_hs_apply(Packed P, const EnsParams* __restrict__ prm, const 
                 {
                     const int j = nbr[f];
                     if (!mk[j]) continue;
-                    s += pi - (dm[j] ? pm[j] : 0.0f);
+                    s += pi - (dm[j] ? pv(M.base + j) : 0.0f);
                 }
             }
             else
@@ -653,7 +695,7 @@ __global__ void ens_hs_apply(Packed P, const EnsParams* __restrict__ prm, const 
                 {
                     const std::int64_t j = hs_nb(q.hs, mk, r, c, kDr[f], kDc[f]);
                     if (j == l) continue;
-                    s += pi - (dm[j] ? pm[j] : 0.0f);
+                    s += pi - (dm[j] ? pv(M.base + j) : 0.0f);
                 }
             }
             v = q.inv_dt_f * pi + q.DA_f * s;
@@ -696,24 +738,6 @@ __global__ void ens_hs_update(Packed P, const int* __restrict__ done, const doub
     }
     block_partial_f(rz, false, part, P.n / kPackAlign, 0);
     block_partial_f(rr, false, part, P.n / kPackAlign, 1);
-}
-
-// beta = r.z / r_old.z_old (once per block); p = z + beta p
-__global__ void ens_hs_direction(Packed P, const int* __restrict__ done, const double* __restrict__ prev,
-                                 const double* __restrict__ cur, const float* __restrict__ zz, float* __restrict__ p)
-{
-    LSDTT_COUNT();
-    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    const int m = member_of(P, i < P.n ? i : P.n - 1);
-    if (done[m]) return;
-    __shared__ float s_beta;
-    if (threadIdx.x == 0)
-    {
-        const double ro = prev[m * kHsSlot + 1];
-        s_beta = (ro > 0.0) ? static_cast<float>(cur[m * kHsSlot + 1] / ro) : 0.0f;
-    }
-    __syncthreads();
-    if (i < P.n) p[i] = zz[i] + s_beta * p[i];
 }
 
 // After iteration `it` (0-based, it + 1 a multiple of 4 or the last one):
@@ -850,6 +874,7 @@ struct lsdtt_gpu_ensemble
     std::uint32_t *order = nullptr, *lstart = nullptr, *lcount = nullptr, *lfill = nullptr, *maxd = nullptr;
     std::uint8_t* dof = nullptr;
     float *invd = nullptr, *b = nullptr, *x = nullptr, *r = nullptr, *p = nullptr, *zz = nullptr, *Ap = nullptr;
+    float* p2 = nullptr;  // second CG direction buffer (the fused direction update alternates)
     double *hs_bb = nullptr, *hs_acc = nullptr;
     int *done = nullptr, *iters = nullptr;
     double* stats_acc = nullptr;
@@ -900,7 +925,7 @@ void free_ensemble(lsdtt_gpu_ensemble* E)
     if (E->exec) cudaGraphExecDestroy(E->exec);
     if (E->graph) cudaGraphDestroy(E->graph);
     void* bufs[] = {E->d_pm, E->d_prm, E->blk_member, E->tile_member, E->z, E->zf, E->zsp, E->zpre, E->kind, E->bflag, E->dirty, E->oflag, E->pos, E->nd, E->area, E->order, E->lstart, E->lcount,
-                    E->lfill, E->maxd, E->dof, E->invd, E->b, E->x, E->r, E->p, E->zz, E->Ap, E->hs_bb, E->hs_acc,
+                    E->lfill, E->maxd, E->dof, E->invd, E->b, E->x, E->r, E->p, E->p2, E->zz, E->Ap, E->hs_bb, E->hs_acc,
                     E->done, E->iters, E->stats_acc, E->part, E->kam_tab, E->flags, E->zg, E->dfc};
     for (void* q : bufs) cudaFree(q);
     void* hb[] = {E->h_stats, E->h_flags, E->h_iters, E->h_maxd, E->h_err};
@@ -1015,7 +1040,10 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
     f->ws.used = 0;
     e = build_stack(f, false, st, &E->P);
     if (e != cudaSuccess) return e;
-    ens_kam<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->mask, f->receiver, f->sv_size, E->kam_tab, E->area);
+    cudaMemsetAsync(E->dfc + 1, 0, sizeof(std::uint32_t), st);  // count of large-count nodes
+    ens_kam<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->mask, f->receiver, f->sv_size, E->kam_tab, E->area, E->lfill,
+                                E->dfc + 1);
+    ens_kam_big<<<152 * 8, 256, 0, st>>>(E->P, E->d_prm, f->sv_size, E->lfill, E->dfc + 1, E->area);
     // 2. depth levels
     const std::uint32_t cap = eager ? static_cast<std::uint32_t>(N + 1) : static_cast<std::uint32_t>(E->depth_cap);
     cudaMemsetAsync(E->maxd, 0, sizeof(std::uint32_t), st);
@@ -1149,15 +1177,19 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
             const double* prev = E->hs_acc + static_cast<std::size_t>(kHsSlot) * M * it;
             double* cur = E->hs_acc + static_cast<std::size_t>(kHsSlot) * M * (it + 1);
             // Algorithmic bytes: Ap = A p with p.Ap 8 B/cell; the update 24 B/cell.
-            LSDTT_TIMED("ens_hillslope_apply", 8.0 * cells, st,
-                        (ens_hs_apply<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->mask, E->dof, E->done, E->p, E->Ap,
-                                                          E->part)));
+            // p_it lives in pbuf[it % 2]; iteration it >= 1 forms it inside the apply
+            float* p_it = (it & 1) ? E->p2 : E->p;
+            const float* p_prev = (it & 1) ? E->p : E->p2;
+            const double* older = (it >= 1) ? E->hs_acc + static_cast<std::size_t>(kHsSlot) * M * (it - 1) : prev;
+            // Algorithmic bytes: p 4 in (+ z 4 when fused), Ap 4 out (+ p 4 when fused).
+            LSDTT_TIMED("ens_hillslope_apply", (it ? 16.0 : 8.0) * cells, st,
+                        (ens_hs_apply<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->mask, E->dof, E->done, it ? 1 : 0, prev,
+                                                          older, E->zz, p_prev, p_it, E->Ap, E->part)));
             reduce(1, 0u, E->done, cur, kHsSlot, 0);
             LSDTT_TIMED("ens_hillslope_update", 24.0 * cells, st,
-                        (ens_hs_update<<<nb, 256, 0, st>>>(E->P, E->done, prev, E->invd, E->p, E->Ap, E->x, E->r,
+                        (ens_hs_update<<<nb, 256, 0, st>>>(E->P, E->done, prev, E->invd, p_it, E->Ap, E->x, E->r,
                                                            E->zz, cur, E->part)));
             reduce(2, 0u, E->done, cur, kHsSlot, 1);
-            ens_hs_direction<<<nb, 256, 0, st>>>(E->P, E->done, prev, cur, E->zz, E->p);
         }
         if (eager) cudaMemsetAsync(E->flags + 5, 0, sizeof(int), st);
         ens_hs_check<<<mb, 128, 0, st>>>(M, E->d_prm, it - 1,
@@ -1425,6 +1457,7 @@ int lsdtt_gpu_ensemble_create(const lsdtt_gpu_member* members, int32_t n_members
     alloc(&E->x, n);
     alloc(&E->r, n);
     alloc(&E->p, n);
+    alloc(&E->p2, n);
     alloc(&E->zz, n);
     alloc(&E->Ap, n);
     alloc(&E->hs_bb, static_cast<std::size_t>(n_members));

@@ -205,7 +205,7 @@ __global__ void __launch_bounds__(128) k_conv_tc(int H, int W, int up, const __n
 // ---------------------------------------------------------------------------
 // The same convolutions on the 5th-generation tensor cores (tcgen05).
 //
-// One CTA (4 warps) works through tiles of kTcM = 128 consecutive output
+// One CTA (8 warps) works through tiles of kTcM = 128 consecutive output
 // pixels of one row; each tile is one UMMA of M = 128, N = COUT per K-step,
 // K = 9 taps x CIN in steps of 16, BF16 operands from shared memory, FP32
 // accumulator in tensor memory (TMEM), issued by one thread.
@@ -220,8 +220,8 @@ __global__ void __launch_bounds__(128) k_conv_tc(int H, int W, int up, const __n
 //   B:    the layer's weights for all 9 taps, per tap [COUT/8 groups][CIN/8
 //         chunks][8 rows x 16 B], staged once per CTA.
 // The epilogue reads the accumulator with tcgen05.ld (warp w owns TMEM lanes
-// = tile pixels 32w..32w+31) and fuses bias, ReLU, the decoder skip and the
-// BF16 store. Every wait on the MMA barrier is bounded: on expiry the kernel
+// = tile pixels 32(w % 4)..+31; warps w and w + 4 split the columns) and
+// fuses bias, ReLU, the decoder skip and the BF16 store. Every wait on the MMA barrier is bounded: on expiry the kernel
 // records an error, waits once more (bounded) for its MMAs, frees its TMEM
 // and returns.
 constexpr int kTcM = 128;
@@ -340,7 +340,7 @@ __device__ __forceinline__ void tc5_issue(std::uint32_t tmem_acc, std::uint32_t 
 // CTA stages tile i + 1 (second halo buffer) and then drains tile i's
 // accumulator (second TMEM accumulator) through the epilogue.
 template <int CIN, int COUT>
-__global__ void __launch_bounds__(128) k_conv_tc5(int H, int W, int up, const __nv_bfloat16* __restrict__ in,
+__global__ void __launch_bounds__(256) k_conv_tc5(int H, int W, int up, const __nv_bfloat16* __restrict__ in,
                                                   const __nv_bfloat16* __restrict__ wpk,
                                                   const float* __restrict__ bias, int mode,
                                                   const __nv_bfloat16* __restrict__ skip,
@@ -420,13 +420,16 @@ __global__ void __launch_bounds__(128) k_conv_tc5(int H, int W, int up, const __
         // ordered every thread's staging of halo[nxt] before them)
         if (tid == 0 && ntile < tiles)
             tc5_issue<CIN, COUT>(tmem + nxt * Lt::kAccCols, base_s + nxt * Lt::kHaloBytes, b_s, mbar_s + 8 * nxt);
-        // epilogue of this tile
+        // epilogue of this tile: warp w reads TMEM lanes 32 (w % 4) ..
+        // (its tile pixels); warps w and w + 4 take alternate 16-column
+        // chunks of the accumulator
         const int y = tile / tpr, x0 = (tile % tpr) * kTcM;
-        const int m = warp * 32 + lane;
+        const int quarter = warp & 3, half = warp >> 2;
+        const int m = quarter * 32 + lane;
         const int x = x0 + m;
         const std::int64_t o = (static_cast<std::int64_t>(y) * W + x) * COUT;
 #pragma unroll
-        for (int n0 = 0; n0 < COUT; n0 += 16)
+        for (int n0 = 16 * half; n0 < COUT; n0 += 32)
         {
             std::uint32_t r[16];
             asm volatile(
@@ -435,7 +438,7 @@ __global__ void __launch_bounds__(128) k_conv_tc5(int H, int W, int up, const __
                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
                   "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
                   "=r"(r[15])
-                : "r"(tmem + cur * Lt::kAccCols + (static_cast<std::uint32_t>(warp * 32) << 16) +
+                : "r"(tmem + cur * Lt::kAccCols + (static_cast<std::uint32_t>(quarter * 32) << 16) +
                       static_cast<std::uint32_t>(n0)));
             asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
             if (x < W)
@@ -762,7 +765,7 @@ unsigned tc5_grid(int tiles)
         int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_conv_tc5<CI, CO>, 128, Tc5Layout<CI, CO>::kSmem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_conv_tc5<CI, CO>, 256, Tc5Layout<CI, CO>::kSmem);
         // every resident CTA holds its TMEM columns for its whole life
         per_sm = std::min(per_sm, 512 / Tc5Layout<CI, CO>::kTmemCols);
         if (per_sm < 1) per_sm = 1;
@@ -783,7 +786,7 @@ void launch_conv_tc(const lsdtt_gpu_unet* U, int l, int H, int W, int up, const 
     {                                                                                                               \
         if (unet_conv_kind(U) == 1)                                                                                 \
             LSDTT_TIMED("unet_conv_tc5", bytes, st,                                                                 \
-                        (k_conv_tc5<CI, CO><<<tc5_grid<CI, CO>(tiles), 128, Tc5Layout<CI, CO>::kSmem, st>>>(       \
+                        (k_conv_tc5<CI, CO><<<tc5_grid<CI, CO>(tiles), 256, Tc5Layout<CI, CO>::kSmem, st>>>(       \
                             H, W, up, in, wpk, b, mode, skip, pre, out, unet_err(U))));                            \
         else                                                                                                        \
             LSDTT_TIMED("unet_conv_tc", bytes, st,                                                                  \
