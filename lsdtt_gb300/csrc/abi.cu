@@ -244,6 +244,7 @@ int lsdtt_gpu_flow_create(const lsdtt_gpu_grid* grid, lsdtt_gpu_flow** out)
     alloc(&f->topo_pos, n);
     alloc(&f->dscal, 4);
     alloc(&f->derr, 4);
+    alloc(&f->dundec, 1);
     // Workspace: the Euler-tour ranking peaks at ~72 B per cell (tour links,
     // two prefix arrays and the level-0 ruler walk state); the range-max
     // structure and the sort need ~58 B per cell after the tour is released.
@@ -278,6 +279,7 @@ int lsdtt_gpu_flow_destroy(lsdtt_gpu_flow* f)
     cudaFree(f->topo_pos);
     cudaFree(f->dscal);
     cudaFree(f->derr);
+    cudaFree(f->dundec);
     cudaFree(f->ws.base);
     cudaFreeHost(f->hscal);
     cudaFreeHost(f->herr);

@@ -20,6 +20,8 @@
 // at c. The outlet list is the row-major compaction of valid cells with no
 // receiver.
 
+#include <algorithm>
+
 #include "engine.cuh"
 #include "d8_cell.cuh"
 
@@ -28,20 +30,47 @@ namespace lsdtt_gb300
 namespace
 {
 
+// Tile pass over 128 x 32 tiles (d8_receivers_tile), tiles across fastest.
 __global__ void __launch_bounds__(256) receivers_kernel(Grid g, const float* __restrict__ z,
                                                         const std::uint8_t* __restrict__ mask,
                                                         const std::uint8_t* __restrict__ forced,
                                                         int interior_nodata_is_outlet, int allow_pits, float inv_card,
                                                         float inv_diag, std::int64_t* __restrict__ receiver,
-                                                        std::uint8_t* __restrict__ dir,
-                                                        unsigned long long* __restrict__ err)
+                                                        std::uint8_t* __restrict__ dir, unsigned* __restrict__ undecided)
 {
     LSDTT_COUNT();
-    const int col = blockIdx.x * blockDim.x + threadIdx.x;
-    const int row = blockIdx.y * blockDim.y + threadIdx.y;
-    if (row >= g.nr || col >= g.nc) return;
-    d8_receiver_cell(g, z, mask, forced, interior_nodata_is_outlet, allow_pits, inv_card, inv_diag, receiver, dir, err,
-                     row, col);
+    const int ntx = (g.nc + kD8TileCols - 1) / kD8TileCols;
+    d8_receivers_tile(g, z, mask, forced, interior_nodata_is_outlet, allow_pits, inv_card, inv_diag, receiver, dir,
+                      undecided, static_cast<int>(blockIdx.x) % ntx, static_cast<int>(blockIdx.x) / ntx, 0);
+}
+
+// Fixup pass: every perimeter cell, then (only when the tile pass raised the
+// flag) every cell it left undecided.
+__global__ void __launch_bounds__(256) receivers_fixup(Grid g, const float* __restrict__ z,
+                                                       const std::uint8_t* __restrict__ mask,
+                                                       const std::uint8_t* __restrict__ forced,
+                                                       int interior_nodata_is_outlet, int allow_pits, float inv_card,
+                                                       float inv_diag, std::int64_t* __restrict__ receiver,
+                                                       std::uint8_t* __restrict__ dir,
+                                                       unsigned long long* __restrict__ err,
+                                                       const unsigned* __restrict__ undecided)
+{
+    LSDTT_COUNT();
+    const std::int64_t stride = static_cast<std::int64_t>(gridDim.x) * blockDim.x;
+    const std::int64_t t0 = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const std::int64_t P = d8_perimeter(g.nr, g.nc);
+    for (std::int64_t i = t0; i < P; i += stride)
+    {
+        int row, col;
+        d8_perimeter_cell(g.nr, g.nc, i, row, col);
+        d8_fixup_cell(g, z, mask, forced, interior_nodata_is_outlet, allow_pits, inv_card, inv_diag, receiver, dir,
+                      err, row, col, 0, 0);
+    }
+    if (*undecided == 0u) return;
+    for (std::int64_t i = t0; i < g.n; i += stride)
+        if (dir[i] == kD8Undecided)
+            d8_fixup_cell(g, z, mask, forced, interior_nodata_is_outlet, allow_pits, inv_card, inv_diag, receiver,
+                          dir, err, static_cast<int>(i / g.nc), static_cast<int>(i % g.nc), 0, 0);
 }
 
 // Donor counts by gather (cell c counts neighbours d with dir(d) pointing to
@@ -111,15 +140,21 @@ cudaError_t launch_receivers(lsdtt_gpu_flow* f, const float* z, const std::uint8
                              const std::uint8_t* forced_plane, int interior_nodata_is_outlet,
                              int allow_pits_as_outlets, cudaStream_t st)
 {
-    const dim3 block(32, 8);
-    const dim3 grid((f->g.nc + 31) / 32, (f->g.nr + 7) / 8);
+    const std::int64_t tiles = static_cast<std::int64_t>((f->g.nc + kD8TileCols - 1) / kD8TileCols) *
+                               ((f->g.nr + kD8TileRows - 1) / kD8TileRows);
     const float inv_card = static_cast<float>(1.0 / f->g.cell);
     const float inv_diag = static_cast<float>(1.0 / (f->g.cell * 1.4142135623730950488));
+    cudaMemsetAsync(f->dundec, 0, sizeof(unsigned), st);
     // Algorithmic bytes: z 4 + mask 1 in, direction 1 + int64 receiver 8 out.
     LSDTT_TIMED("d8_receivers", 14.0 * static_cast<double>(f->g.n), st,
-                (receivers_kernel<<<grid, block, 0, st>>>(f->g, z, mask, forced_plane, interior_nodata_is_outlet,
-                                                          allow_pits_as_outlets, inv_card, inv_diag, f->receiver,
-                                                          f->dir, f->derr)));
+                (receivers_kernel<<<static_cast<unsigned>(tiles), 256, 0, st>>>(
+                    f->g, z, mask, forced_plane, interior_nodata_is_outlet, allow_pits_as_outlets, inv_card, inv_diag,
+                    f->receiver, f->dir, f->dundec)));
+    const std::int64_t P = d8_perimeter(f->g.nr, f->g.nc);
+    const unsigned fix_blocks = static_cast<unsigned>(std::min<std::int64_t>((P + 255) / 256 + 152, 152 * 4));
+    receivers_fixup<<<fix_blocks, 256, 0, st>>>(f->g, z, mask, forced_plane, interior_nodata_is_outlet,
+                                                allow_pits_as_outlets, inv_card, inv_diag, f->receiver, f->dir,
+                                                f->derr, f->dundec);
     return cudaGetLastError();
 }
 

@@ -29,6 +29,7 @@ struct lsdtt_gpu_flow
     // Device scalars: [0] n_valid, [1] n_outlets, [2] max height, [3] spare.
     std::int64_t* dscal = nullptr;
     unsigned long long* derr = nullptr;  // [0] error word, [1] first unresolved flat
+    unsigned* dundec = nullptr;          // receivers tile pass left undecided cells
     std::int64_t* hscal = nullptr;       // pinned host mirror of dscal
     unsigned long long* herr = nullptr;  // pinned host mirror of derr
     // Workspace for the list ranking, RMQ and sort.
@@ -65,6 +66,9 @@ struct PackedMember
     char bc[4];
     std::int32_t tile_base;  // first 32x32 fill tile of this member
     std::int32_t ntx, nty;   // fill tiles across, down
+    std::int32_t rtile_base;  // first 128 x 32 receiver tile of this member
+    std::int32_t nrx;         // receiver tiles across (x nty down)
+    std::int64_t perim_base;  // first perimeter cell of this member in the fixup numbering
 };
 
 struct Packed

@@ -155,34 +155,67 @@ __global__ void ens_flag_copy(const int* __restrict__ src, int* __restrict__ dst
 }
 
 // ---- D8, outlets, area -----------------------------------------------------
+// D8 receivers, tile pass: one block per 128 x 32 receiver tile of a member
+// (d8_receivers_tile on the member's own grid; receivers written as packed
+// indices).
 __global__ void __launch_bounds__(256) ens_receivers(Packed P, const EnsParams* __restrict__ prm,
+                                                     const std::uint16_t* __restrict__ rtile_member,
                                                      const float* __restrict__ zf,
                                                      const std::uint8_t* __restrict__ mask,
                                                      std::int64_t* __restrict__ receiver,
-                                                     std::uint8_t* __restrict__ dir,
-                                                     unsigned long long* __restrict__ err)
+                                                     std::uint8_t* __restrict__ dir, unsigned* __restrict__ undecided)
 {
     LSDTT_COUNT();
-    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i >= P.n) return;
-    const int m = member_of(P, i);
+    const int m = rtile_member[blockIdx.x];
     const PackedMember& M = P.m[m];
-    const std::int64_t local = i - M.base;
-    if (local >= static_cast<std::int64_t>(M.nr) * M.nc)
-    {
-        receiver[i] = kNodataReceiver;
-        dir[i] = kNoDir;
-        return;
-    }
-    const Grid g = member_grid(M);
     const EnsParams& q = prm[m];
+    const int local = static_cast<int>(blockIdx.x) - M.rtile_base;
     // The LEM's engine: interior nodata drains, pits are outlets.
-    const int l = static_cast<int>(local);  // member grids hold < 2^31 cells
-    const int row = l / M.nc;
-    d8_receiver_cell(g, zf + M.base, mask + M.base, nullptr, 1, 1, q.inv_card, q.inv_diag, receiver + M.base,
-                     dir + M.base, err, row, l - row * M.nc, M.base);
-    const std::int64_t r = receiver[i];
-    if (r >= 0) receiver[i] = r + M.base;
+    d8_receivers_tile(member_grid(M), zf + M.base, mask + M.base, nullptr, 1, 1, q.inv_card, q.inv_diag,
+                      receiver + M.base, dir + M.base, undecided, local % M.nrx, local / M.nrx, M.base);
+}
+
+// D8 receivers, fixup pass: every member's perimeter cells, then (only when
+// the tile pass raised the flag) every cell it left undecided.
+__global__ void __launch_bounds__(256) ens_receivers_fixup(Packed P, const EnsParams* __restrict__ prm,
+                                                           std::int64_t perim, const float* __restrict__ zf,
+                                                           const std::uint8_t* __restrict__ mask,
+                                                           std::int64_t* __restrict__ receiver,
+                                                           std::uint8_t* __restrict__ dir,
+                                                           unsigned long long* __restrict__ err,
+                                                           const unsigned* __restrict__ undecided)
+{
+    LSDTT_COUNT();
+    const std::int64_t stride = static_cast<std::int64_t>(gridDim.x) * blockDim.x;
+    const std::int64_t t0 = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    for (std::int64_t i = t0; i < perim; i += stride)
+    {
+        int lo = 0, hi = P.n_members - 1;  // last member with perim_base <= i
+        while (lo < hi)
+        {
+            const int mid = (lo + hi + 1) >> 1;
+            if (P.m[mid].perim_base <= i) lo = mid;
+            else hi = mid - 1;
+        }
+        const PackedMember& M = P.m[lo];
+        const EnsParams& q = prm[lo];
+        int row, col;
+        d8_perimeter_cell(M.nr, M.nc, i - M.perim_base, row, col);
+        d8_fixup_cell(member_grid(M), zf + M.base, mask + M.base, nullptr, 1, 1, q.inv_card, q.inv_diag,
+                      receiver + M.base, dir + M.base, err, row, col, M.base, M.base);
+    }
+    if (*undecided == 0u) return;
+    for (std::int64_t i = t0; i < P.n; i += stride)
+    {
+        if (dir[i] != kD8Undecided) continue;
+        const int m = P.blk_member[i / kPackAlign];
+        const PackedMember& M = P.m[m];
+        const EnsParams& q = prm[m];
+        const std::int64_t local = i - M.base;
+        d8_fixup_cell(member_grid(M), zf + M.base, mask + M.base, nullptr, 1, 1, q.inv_card, q.inv_diag,
+                      receiver + M.base, dir + M.base, err, static_cast<int>(local / M.nc),
+                      static_cast<int>(local % M.nc), M.base, M.base);
+    }
 }
 
 __global__ void ens_outlet_flag(std::int64_t n, const std::uint8_t* __restrict__ mask,
@@ -859,10 +892,14 @@ struct lsdtt_gpu_ensemble
     std::vector<EnsParams> prm_h;
     std::int64_t N = 0, member_cells = 0;
     std::int32_t T = 0;
+    std::int32_t S = 0;      // receiver tiles (128 x 32 cells)
+    std::int64_t perim = 0;  // perimeter cells of all members
     PackedMember* d_pm = nullptr;
     EnsParams* d_prm = nullptr;
     std::uint16_t* blk_member = nullptr;
     std::uint16_t* tile_member = nullptr;
+    std::uint16_t* strip_member = nullptr;  // [S]: member of each 128 x 32 receiver tile
+    unsigned* undecided = nullptr;          // receivers tile pass left undecided cells
     Packed P{};
     // state and stage buffers
     float *z = nullptr, *zf = nullptr, *zsp = nullptr, *zpre = nullptr;
@@ -924,7 +961,7 @@ void free_ensemble(lsdtt_gpu_ensemble* E)
 {
     if (E->exec) cudaGraphExecDestroy(E->exec);
     if (E->graph) cudaGraphDestroy(E->graph);
-    void* bufs[] = {E->d_pm, E->d_prm, E->blk_member, E->tile_member, E->z, E->zf, E->zsp, E->zpre, E->kind, E->bflag, E->dirty, E->oflag, E->pos, E->nd, E->area, E->order, E->lstart, E->lcount,
+    void* bufs[] = {E->d_pm, E->d_prm, E->blk_member, E->tile_member, E->strip_member, E->undecided, E->z, E->zf, E->zsp, E->zpre, E->kind, E->bflag, E->dirty, E->oflag, E->pos, E->nd, E->area, E->order, E->lstart, E->lcount,
                     E->lfill, E->maxd, E->dof, E->invd, E->b, E->x, E->r, E->p, E->p2, E->zz, E->Ap, E->hs_bb, E->hs_acc,
                     E->done, E->iters, E->stats_acc, E->part, E->kam_tab, E->flags, E->zg, E->dfc};
     for (void* q : bufs) cudaFree(q);
@@ -1030,8 +1067,13 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
     lsdtt_gpu_flow* f = E->f;
     cudaMemsetAsync(f->derr, 0, sizeof(unsigned long long) * 4, st);
     // Algorithmic bytes: z 4 + mask 1 in, direction 1 + int64 receiver 8 out.
+    cudaMemsetAsync(E->undecided, 0, sizeof(unsigned), st);
     LSDTT_TIMED("ens_d8_receivers", 14.0 * cells, st,
-                (ens_receivers<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->zf, E->mask, f->receiver, f->dir, f->derr)));
+                (ens_receivers<<<E->S, 256, 0, st>>>(E->P, E->d_prm, E->strip_member, E->zf, E->mask, f->receiver,
+                                                     f->dir, E->undecided)));
+    ens_receivers_fixup<<<static_cast<unsigned>(std::min<std::int64_t>((E->perim + 255) / 256 + 152, 152 * 4)), 256, 0,
+                          st>>>(E->P, E->d_prm, E->perim, E->zf, E->mask, f->receiver, f->dir, f->derr,
+                                E->undecided);
     ens_outlet_flag<<<nb, 256, 0, st>>>(N, E->mask, f->dir, E->oflag);
     f->ws.used = 0;
     e = exclusive_scan<std::uint8_t, std::int64_t>(E->oflag, N, E->pos, f->dscal + 1, f->ws, st);
@@ -1297,6 +1339,8 @@ int lsdtt_gpu_ensemble_create(const lsdtt_gpu_member* members, int32_t n_members
     E->member_set.assign(static_cast<std::size_t>(n_members), 0);
     std::int64_t base = 0;
     std::int32_t tiles = 0;
+    std::int32_t strips = 0;     // 128 x 32 receiver tiles
+    std::int64_t perim = 0;      // perimeter cells of all members
     for (int k = 0; k < n_members; ++k)
     {
         const lsdtt_gpu_grid& g = members[k].grid;
@@ -1342,6 +1386,11 @@ int lsdtt_gpu_ensemble_create(const lsdtt_gpu_member* members, int32_t n_members
         P.ntx = (g.n_cols + 31) / 32;
         P.nty = (g.n_rows + 31) / 32;
         tiles += P.ntx * P.nty;
+        P.rtile_base = strips;
+        P.nrx = (g.n_cols + kD8TileCols - 1) / kD8TileCols;
+        strips += P.nrx * P.nty;
+        P.perim_base = perim;
+        perim += d8_perimeter(g.n_rows, g.n_cols);
         base += (n + kPackAlign - 1) / kPackAlign * kPackAlign;
         E->member_cells += n;
         E->pm.push_back(P);
@@ -1389,6 +1438,8 @@ int lsdtt_gpu_ensemble_create(const lsdtt_gpu_member* members, int32_t n_members
     }
     E->N = base;
     E->T = tiles;
+    E->S = strips;
+    E->perim = perim;
     const std::int64_t N = E->N;
     if (2 * N >= (std::int64_t(1) << 32))
     {
@@ -1397,6 +1448,7 @@ int lsdtt_gpu_ensemble_create(const lsdtt_gpu_member* members, int32_t n_members
     }
     std::vector<std::uint16_t> blk(static_cast<std::size_t>(N / kPackAlign));
     std::vector<std::uint16_t> tm(static_cast<std::size_t>(tiles));
+    std::vector<std::uint16_t> sm(static_cast<std::size_t>(strips));
     for (int k = 0; k < n_members; ++k)
     {
         const PackedMember& P = E->pm[static_cast<std::size_t>(k)];
@@ -1404,6 +1456,7 @@ int lsdtt_gpu_ensemble_create(const lsdtt_gpu_member* members, int32_t n_members
         const std::int64_t nblk = (n + kPackAlign - 1) / kPackAlign;
         for (std::int64_t b = 0; b < nblk; ++b) blk[static_cast<std::size_t>(P.base / kPackAlign + b)] = k;
         for (int t = 0; t < P.ntx * P.nty; ++t) tm[static_cast<std::size_t>(P.tile_base + t)] = k;
+        for (int t = 0; t < P.nrx * P.nty; ++t) sm[static_cast<std::size_t>(P.rtile_base + t)] = k;
     }
     // The stack runs on the packed forest: one flow engine over N cells.
     lsdtt_gpu_grid fg{};
@@ -1435,6 +1488,8 @@ int lsdtt_gpu_ensemble_create(const lsdtt_gpu_member* members, int32_t n_members
     alloc(&E->d_prm, static_cast<std::size_t>(n_members));
     alloc(&E->blk_member, blk.size());
     alloc(&E->tile_member, tm.size());
+    alloc(&E->strip_member, sm.size());
+    alloc(&E->undecided, 1);
     alloc(&E->z, n);
     alloc(&E->zf, n);
     alloc(&E->zsp, n);
@@ -1484,9 +1539,13 @@ int lsdtt_gpu_ensemble_create(const lsdtt_gpu_member* members, int32_t n_members
     cudaMemcpyAsync(E->d_prm, E->prm_h.data(), sizeof(EnsParams) * n_members, cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(E->blk_member, blk.data(), sizeof(std::uint16_t) * blk.size(), cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(E->tile_member, tm.data(), sizeof(std::uint16_t) * tm.size(), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(E->strip_member, sm.data(), sizeof(std::uint16_t) * sm.size(), cudaMemcpyHostToDevice, st);
     cudaMemsetAsync(E->z, 0, sizeof(float) * n, st);
     cudaMemsetAsync(E->mask, 0, n, st);
     cudaMemsetAsync(E->zg, 0, sizeof(unsigned long long) * n, st);
+    // padding cells between members: no receiver, no direction, ever
+    cudaMemsetAsync(E->f->receiver, 0xFF, sizeof(std::int64_t) * n, st);
+    cudaMemsetAsync(E->f->dir, 0xFF, n, st);
     cudaMemsetAsync(E->dfc, 0, sizeof(std::uint32_t) * 2, st);
     {
         int dev = 0, sms = 0, per_sm = 0;

@@ -101,3 +101,42 @@ def test_gpu_unresolved_sink_message():
         G.FlowInfo(z, m, 10.0, "nnnn")
     assert "could not assign a receiver at row 0, col 0" in str(e.value)
     assert e.value.status == G.EUNRESOLVED
+
+
+def _adversarial_surfaces():
+    """Elevations aimed at every branch of the receiver ranking."""
+    rng = np.random.default_rng(17)
+    shape = (97, 101)  # crosses 32-cell tile seams, ragged last tile
+    r, c = np.mgrid[0:shape[0], 0:shape[1]].astype(np.float64)
+    out = {}
+    # exact ties inside a class and between classes
+    out["small_ints"] = rng.integers(0, 4, shape).astype(np.float32)
+    # planes whose best cardinal and diagonal drops are consecutive convergents
+    # of sqrt2 (8119/5741, 19601/13860): cross-class near-ties below 2^-18
+    p1 = 2.0e6 + 5741.0 * (shape[0] - r) + 2378.0 * (shape[1] - c)
+    p2 = 8.0e6 + 13860.0 * (shape[0] - r) + 5741.0 * (shape[1] - c)
+    out["sqrt2_planes"] = np.where(r < shape[0] // 2, p1, p2).astype(np.float32)
+    # drops that dwarf tiny, zero, subnormal and signed-zero neighbours
+    pool = np.array([1e9, 3e8, 1.0, 0.0, -0.0, 1e-30, -1e-30, 2e-38, 1e-44, -1e-44, 5e-7, -3.0], np.float32)
+    out["magnitudes"] = pool[rng.integers(0, pool.size, shape)]
+    # fractal relief with infinities and NaNs under masked cells (a valid
+    # cell must hold a finite value)
+    f = surfaces.fractal(shape[0], shape[1], 300.0, 7).astype(np.float32) - 150.0
+    pick = rng.random(shape)
+    f[pick < 0.004] = np.inf
+    f[(pick >= 0.004) & (pick < 0.008)] = -np.inf
+    f[(pick >= 0.008) & (pick < 0.010)] = np.nan
+    out["nonfinite"] = f
+    return out
+
+
+@pytest.mark.parametrize("name", ["small_ints", "sqrt2_planes", "magnitudes", "nonfinite"])
+def test_gpu_receivers_adversarial(port, name):
+    z = _adversarial_surfaces()[name]
+    rng = np.random.default_rng(5)
+    full = np.ones_like(z, np.uint8)
+    holes = (rng.random(z.shape) > 0.05).astype(np.uint8)
+    for m in (full, holes):
+        m = m & np.isfinite(z).astype(np.uint8)
+        for cell, bc in ((10.0, "oooo"), (3.0, "popo"), (0.7, "nnon")):
+            _compare_with_oracle(port, z, m, cell, bc)
