@@ -30,18 +30,34 @@ namespace lsdtt_gb300
 namespace
 {
 
-// Tile pass over 128 x 32 tiles (d8_receivers_tile), tiles across fastest.
+// Tile t of the grid: tiles across fastest.
+struct GridTiles
+{
+    Grid g;
+    const float* z;
+    const std::uint8_t* mask;
+    std::int64_t* receiver;
+    std::uint8_t* dir;
+    float inv_card, inv_diag;
+    int ntx;
+    __device__ D8Job operator()(int t) const
+    {
+        return D8Job{g, z, mask, receiver, dir, inv_card, inv_diag, t % ntx, t / ntx, 0};
+    }
+};
+
+// Tile pass, one block per 128 x 32 tile (d8_receivers_tile).
 __global__ void __launch_bounds__(256) receivers_kernel(Grid g, const float* __restrict__ z,
                                                         const std::uint8_t* __restrict__ mask,
                                                         const std::uint8_t* __restrict__ forced,
                                                         int interior_nodata_is_outlet, int allow_pits, float inv_card,
                                                         float inv_diag, std::int64_t* __restrict__ receiver,
-                                                        std::uint8_t* __restrict__ dir, unsigned* __restrict__ undecided)
+                                                        std::uint8_t* __restrict__ dir,
+                                                        unsigned* __restrict__ undecided)
 {
     LSDTT_COUNT();
-    const int ntx = (g.nc + kD8TileCols - 1) / kD8TileCols;
-    d8_receivers_tile(g, z, mask, forced, interior_nodata_is_outlet, allow_pits, inv_card, inv_diag, receiver, dir,
-                      undecided, static_cast<int>(blockIdx.x) % ntx, static_cast<int>(blockIdx.x) / ntx, 0);
+    const GridTiles jobs{g, z, mask, receiver, dir, inv_card, inv_diag, (g.nc + kD8TileCols - 1) / kD8TileCols};
+    d8_receivers_tile(jobs(static_cast<int>(blockIdx.x)), forced, interior_nodata_is_outlet, allow_pits, undecided);
 }
 
 // Fixup pass: every perimeter cell, then (only when the tile pass raised the

@@ -209,38 +209,54 @@ __device__ __noinline__ D8Out d8_receiver_cell(const Grid& g, const float* __res
 // unexcused pit); the fixup pass replaces it.
 constexpr std::uint8_t kD8Undecided = 254;
 
-// Tile pass: the receivers of the interior cells of a 128 x 32 tile of grid
-// g, run by 256 threads. The tile and a one-cell halo are staged in shared
-// memory (elevations, NaN where masked, and validity bytes) with 16-byte
-// loads where the row layout allows; each thread then ranks 4 consecutive
-// cells of 4 rows from 16-byte shared reads and writes 4 int64 receivers and
-// 4 direction codes with vector stores. The ranking is branch-free and the
-// kernel makes no calls: an interior cell it cannot settle gets
-// kD8Undecided and raises *undecided; cells on the grid's perimeter get
+// Tile pass: the receivers of the interior cells of a 128 x 32 tile, one
+// block of 256 threads per tile. The tile and a one-cell halo are staged in
+// shared memory (elevations, NaN where masked, and validity bytes) with
+// 16-byte loads where the rows are 16-byte aligned; each thread then ranks 4
+// consecutive cells of 4 rows from 16-byte shared reads and writes 4 int64
+// receivers and 4 direction codes with vector stores. The ranking is
+// branch-free and the pass makes no calls: an interior cell it cannot settle
+// gets kD8Undecided and raises *undecided; cells on a grid's perimeter get
 // provisional values. d8_fixup_cell settles both.
 constexpr int kD8TileCols = 128;
 constexpr int kD8TileRows = 32;
 
-__device__ __forceinline__ void d8_receivers_tile(const Grid& g, const float* __restrict__ z,
-                                                  const std::uint8_t* __restrict__ mask,
-                                                  const std::uint8_t* __restrict__ forced,
-                                                  int interior_nodata_is_outlet, int allow_pits, float inv_card,
-                                                  float inv_diag, std::int64_t* __restrict__ receiver,
-                                                  std::uint8_t* __restrict__ dir, unsigned* __restrict__ undecided,
-                                                  int tx, int ty, std::int64_t rec_base)
+struct D8TileBuf
 {
-    constexpr int TH = kD8TileRows;
-    __shared__ __align__(16) float sz[TH + 2][136];  // column c0 + k at index 4 + k
-    __shared__ __align__(16) std::uint8_t sm[TH + 2][136];
+    float sz[kD8TileRows + 2][136];  // column c0 + k at index 4 + k
+    std::uint8_t sm[kD8TileRows + 2][136];
+};
+
+// One tile of work: the grid it belongs to, its planes and its position.
+struct D8Job
+{
+    Grid g;
+    const float* z;
+    const std::uint8_t* mask;
+    std::int64_t* receiver;
+    std::uint8_t* dir;
+    float inv_card, inv_diag;
+    int tx, ty;
+    std::int64_t rec_base;
+};
+
+__device__ __forceinline__ bool d8_job_vec(const D8Job& J)
+{
+    return (J.g.nc & 3) == 0 && (reinterpret_cast<std::uintptr_t>(J.z) & 15u) == 0 &&
+           (reinterpret_cast<std::uintptr_t>(J.receiver) & 15u) == 0 &&
+           (reinterpret_cast<std::uintptr_t>(J.mask) & 3u) == 0 && (reinterpret_cast<std::uintptr_t>(J.dir) & 3u) == 0;
+}
+
+// Stages a tile (16-byte loads when vec); returns whether this thread saw an
+// invalid cell inside the grid.
+__device__ __forceinline__ int d8_stage(const D8Job& J, D8TileBuf& B, bool vec)
+{
     const float kNan = __int_as_float(0x7fc00000);
-    const int c0 = tx * kD8TileCols, r0 = ty * TH;
+    const Grid& g = J.g;
+    const int c0 = J.tx * kD8TileCols, r0 = J.ty * kD8TileRows;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const bool vec = (g.nc & 3) == 0 && (reinterpret_cast<std::uintptr_t>(z) & 15u) == 0 &&
-                     (reinterpret_cast<std::uintptr_t>(receiver) & 15u) == 0 &&
-                     (reinterpret_cast<std::uintptr_t>(mask) & 3u) == 0 &&
-                     (reinterpret_cast<std::uintptr_t>(dir) & 3u) == 0;
     int masked = 0;
-    for (int lr = w; lr < TH + 2; lr += 8)
+    for (int lr = w; lr < kD8TileRows + 2; lr += 8)
     {
         const int r = r0 - 1 + lr, c = c0 + 4 * lane;
         float a[4] = {kNan, kNan, kNan, kNan};
@@ -250,8 +266,8 @@ __device__ __forceinline__ void d8_receivers_tile(const Grid& g, const float* __
             const std::int64_t f = static_cast<std::int64_t>(r) * g.nc + c;
             if (vec && c + 4 <= g.nc)
             {
-                const float4 q = *reinterpret_cast<const float4*>(z + f);
-                ok = *reinterpret_cast<const unsigned*>(mask + f);
+                const float4 q = *reinterpret_cast<const float4*>(J.z + f);
+                ok = *reinterpret_cast<const unsigned*>(J.mask + f);
                 a[0] = q.x;
                 a[1] = q.y;
                 a[2] = q.z;
@@ -263,22 +279,26 @@ __device__ __forceinline__ void d8_receivers_tile(const Grid& g, const float* __
                 for (int j = 0; j < 4; ++j)
                     if (c + j < g.nc)
                     {
-                        a[j] = z[f + j];
-                        ok |= static_cast<unsigned>(mask[f + j]) << (8 * j);
+                        a[j] = J.z[f + j];
+                        ok |= static_cast<unsigned>(J.mask[f + j]) << (8 * j);
                     }
             }
-#pragma unroll
-            for (int j = 0; j < 4; ++j)
+            const unsigned zero = __vcmpeq4(ok, 0u);  // 0xff in each invalid byte
+            if (zero != 0u)
             {
-                const bool v = ((ok >> (8 * j)) & 0xffu) != 0u;
-                masked |= (c + j < g.nc) && !v;
-                a[j] = v ? a[j] : kNan;
+#pragma unroll
+                for (int j = 0; j < 4; ++j)
+                    if ((zero >> (8 * j)) & 1u)
+                    {
+                        a[j] = kNan;
+                        masked |= c + j < g.nc;
+                    }
             }
         }
-        *reinterpret_cast<float4*>(&sz[lr][4 + 4 * lane]) = make_float4(a[0], a[1], a[2], a[3]);
-        *reinterpret_cast<unsigned*>(&sm[lr][4 + 4 * lane]) = ok;
+        *reinterpret_cast<float4*>(&B.sz[lr][4 + 4 * lane]) = make_float4(a[0], a[1], a[2], a[3]);
+        *reinterpret_cast<unsigned*>(&B.sm[lr][4 + 4 * lane]) = ok;
     }
-    if (threadIdx.x < 2 * (TH + 2))  // halo columns c0 - 1 and c0 + 128
+    if (threadIdx.x < 2 * (kD8TileRows + 2))  // halo columns c0 - 1 and c0 + 128
     {
         const int lr = threadIdx.x >> 1, side = threadIdx.x & 1;
         const int r = r0 - 1 + lr, c = side ? c0 + kD8TileCols : c0 - 1;
@@ -287,50 +307,76 @@ __device__ __forceinline__ void d8_receivers_tile(const Grid& g, const float* __
         if (r >= 0 && r < g.nr && c >= 0 && c < g.nc)
         {
             const std::int64_t f = static_cast<std::int64_t>(r) * g.nc + c;
-            m = mask[f];
-            const float zf = z[f];
+            m = J.mask[f];
+            const float zf = J.z[f];
             v = m ? zf : kNan;
             masked |= (m == 0);
         }
-        sz[lr][side ? 132 : 3] = v;
-        sm[lr][side ? 132 : 3] = m;
+        B.sz[lr][side ? 132 : 3] = v;
+        B.sm[lr][side ? 132 : 3] = m;
     }
-    const bool tile_masked = __syncthreads_or(masked) != 0;
-    const bool inner = r0 >= 1 && r0 + TH <= g.nr - 1 && c0 >= 1 && c0 + kD8TileCols <= g.nc - 1;
+    return masked;
+}
+
+// Ranks the tile staged in B. kMasked: the tile holds invalid cells or a
+// forced-outlet plane is given (otherwise every cell is valid and none is
+// forced); kInner: the tile lies inside the grid's perimeter (every cell is
+// interior, no row or column is ragged). Returns whether an interior cell was
+// left undecided.
+template <bool kMasked, bool kInner>
+__device__ __forceinline__ bool d8_rank_tile(const D8Job& J, const D8TileBuf& B, const int* soff, bool vec,
+                                             const std::uint8_t* __restrict__ forced, int interior_nodata_is_outlet,
+                                             int allow_pits)
+{
+    constexpr int TH = kD8TileRows;
+    const Grid& g = J.g;
+    const float inv_card = J.inv_card, inv_diag = J.inv_diag;
+    const int c0 = J.tx * kD8TileCols, r0 = J.ty * TH;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int lc = 4 + 4 * lane, cb = c0 + 4 * lane;
     bool raise = false;
 #pragma unroll
     for (int q = 0; q < TH / 8; ++q)
     {
         const int lr = 1 + w + 8 * q, r = r0 + lr - 1;
-        if (r >= g.nr || cb >= g.nc) continue;
+        if (!kInner && (r >= g.nr || cb >= g.nc)) continue;
         float u[6], m_[6], d_[6];
         {
-            const float4 a = *reinterpret_cast<const float4*>(&sz[lr - 1][lc]);
-            const float4 b = *reinterpret_cast<const float4*>(&sz[lr][lc]);
-            const float4 e = *reinterpret_cast<const float4*>(&sz[lr + 1][lc]);
-            u[0] = sz[lr - 1][lc - 1];
+            const float4 a = *reinterpret_cast<const float4*>(&B.sz[lr - 1][lc]);
+            const float4 b = *reinterpret_cast<const float4*>(&B.sz[lr][lc]);
+            const float4 e = *reinterpret_cast<const float4*>(&B.sz[lr + 1][lc]);
+            u[0] = B.sz[lr - 1][lc - 1];
             u[1] = a.x;
             u[2] = a.y;
             u[3] = a.z;
             u[4] = a.w;
-            u[5] = sz[lr - 1][lc + 4];
-            m_[0] = sz[lr][lc - 1];
+            u[5] = B.sz[lr - 1][lc + 4];
+            m_[0] = B.sz[lr][lc - 1];
             m_[1] = b.x;
             m_[2] = b.y;
             m_[3] = b.z;
             m_[4] = b.w;
-            m_[5] = sz[lr][lc + 4];
-            d_[0] = sz[lr + 1][lc - 1];
+            m_[5] = B.sz[lr][lc + 4];
+            d_[0] = B.sz[lr + 1][lc - 1];
             d_[1] = e.x;
             d_[2] = e.y;
             d_[3] = e.z;
             d_[4] = e.w;
-            d_[5] = sz[lr + 1][lc + 4];
+            d_[5] = B.sz[lr + 1][lc + 4];
         }
-        const unsigned okc = *reinterpret_cast<const unsigned*>(&sm[lr][lc]);
+        const unsigned okc = *reinterpret_cast<const unsigned*>(&B.sm[lr][lc]);
+        // Pair minima shared by neighbouring cells: the vertical pair of
+        // column k serves the cardinal minimum of cell k - 1 and the diagonal
+        // minima of cells k - 2 and k; the horizontal pair k, k + 2 serves
+        // the cardinal minimum of cell k.
+        float vmin[6], hmin[4];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) vmin[k] = fminf(u[k], d_[k]);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) hmin[k] = fminf(m_[k], m_[k + 2]);
         const std::int64_t row_flat = static_cast<std::int64_t>(r) * g.nc;
-        const bool row_inner = inner || (r >= 1 && r <= g.nr - 2);
+        const std::int64_t rec_row = row_flat + cb + J.rec_base;  // receiver of cell j: rec_row + j + offset
+        const bool row_inner = kInner || (r >= 1 && r <= g.nr - 2);
         std::int64_t rec[4];
         unsigned dirs = 0;
 #pragma unroll
@@ -339,81 +385,75 @@ __device__ __forceinline__ void d8_receivers_tile(const Grid& g, const float* __
             const int c = cb + j;
             const std::int64_t flat = row_flat + c;
             const float zc = m_[j + 1];
-            // best (lowest, first of equal) neighbour per class; 8 = none
-            float b0 = zc, b1 = zc;
-            int d0 = 8, d1 = 8;
-#define LSDTT_D8_TAKE(zn, d, bz, bd)      \
-    {                                     \
-        const float v_ = (zn);            \
-        const bool t_ = v_ < bz;          \
-        bz = t_ ? v_ : bz;                \
-        bd = t_ ? (d) : bd;               \
-    }
-            LSDTT_D8_TAKE(u[j + 1], 0, b0, d0);
-            LSDTT_D8_TAKE(u[j + 2], 1, b1, d1);
-            LSDTT_D8_TAKE(m_[j + 2], 2, b0, d0);
-            LSDTT_D8_TAKE(d_[j + 2], 3, b1, d1);
-            LSDTT_D8_TAKE(d_[j + 1], 4, b0, d0);
-            LSDTT_D8_TAKE(d_[j], 5, b1, d1);
-            LSDTT_D8_TAKE(m_[j], 6, b0, d0);
-            LSDTT_D8_TAKE(u[j], 7, b1, d1);
-#undef LSDTT_D8_TAKE
+            const float zN = u[j + 1], zNE = u[j + 2], zE = m_[j + 2], zSE = d_[j + 2];
+            const float zS = d_[j + 1], zSW = d_[j];  // W = m_[j], NW = u[j]: the class fallbacks below
+            // Lowest neighbour per class (fminf skips the NaNs of masked
+            // cells); downhill when strictly below zc.
+            const float cmin = fminf(vmin[j + 1], hmin[j]);
+            const float dmin = fminf(vmin[j], vmin[j + 2]);
+            const bool hc = cmin < zc, hd = dmin < zc;
             // The rule of d8_decide, branch-free: float screen of the two
             // class winners (quotients within 4 * 2^-24 of the exact ones,
             // margin 2^-18); the winning class's merge bound (its lowest
             // neighbour at least 2^-20 of the drop away from zero); normal
             // quotients when both classes compete. Everything else is left
             // to the fixup pass.
-            const float dz0 = __fsub_rn(zc, b0), dz1 = __fsub_rn(zc, b1);
-            const float sc = __fmul_rn(dz0, inv_card), sd = __fmul_rn(dz1, inv_diag);
+            const float dzc = __fsub_rn(zc, cmin), dzd = __fsub_rn(zc, dmin);
+            const float sc = __fmul_rn(dzc, inv_card), sd = __fmul_rn(dzd, inv_diag);
             const bool cw = sc > __fmul_rn(sd, 1.0f + 3.814697265625e-06f);
             const bool dw = sd > __fmul_rn(sc, 1.0f + 3.814697265625e-06f);
-            const float bw = cw ? b0 : b1, dzw = cw ? dz0 : dz1;
-            const bool none = (d0 & d1) == 8;
-            const bool both = (d0 | d1) < 8;
+            const bool card = hc && (!hd || cw);
+            const float bw = card ? cmin : dmin, dzw = card ? dzc : dzd;
+            // first neighbour of the winning class (direction order) at its minimum
+            const float q0 = card ? zN : zNE, q1 = card ? zE : zSE, q2 = card ? zS : zSW;
+            int k = (q2 == bw) ? 2 : 3;
+            k = (q1 == bw) ? 1 : k;
+            k = (q0 == bw) ? 0 : k;
+            const int bd = 2 * k + (card ? 0 : 1);
+            const bool none = !hc && !hd;
             const bool merge_ok = fabsf(bw) >= __fmul_rn(dzw, 9.5367431640625e-07f) && dzw < INFINITY;
-            const int bd = cw ? d0 : d1;
             bool allowed = false;
-            if (tile_masked)
+            if (kMasked)
             {
 #pragma unroll
-                for (int d = 0; d < 8; ++d) allowed |= sm[lr + d8_dr(d)][lc + j + d8_dc(d)] == 0;
+                for (int d = 0; d < 8; ++d) allowed |= B.sm[lr + d8_dr(d)][lc + j + d8_dc(d)] == 0;
                 allowed = allowed && interior_nodata_is_outlet != 0;
             }
             bool undec = none ? (!allowed && !allow_pits)
-                              : (!(cw || dw) || !merge_ok || (both && !(fminf(sc, sd) >= 1.17549435e-38f)));
-            // row and column steps of direction codes 0..7, packed 2 bits each (+1)
-            const int dr = ((6800 >> (2 * bd)) & 3) - 1, dc = ((425 >> (2 * bd)) & 3) - 1;
-            std::int64_t rj = flat + static_cast<std::int64_t>(dr) * g.nc + dc + rec_base;
+                              : (!merge_ok || (hc && hd && (!(cw || dw) || !(fminf(sc, sd) >= 1.17549435e-38f))));
+            std::int64_t rj = rec_row + (j + soff[bd]);
             int dj = bd;
             if (none)
             {
                 rj = kOutletReceiver;
                 dj = kNoDir;
             }
-            if (((okc >> (8 * j)) & 0xffu) == 0u)
+            if (kMasked)
             {
-                rj = kNodataReceiver;
-                dj = kNoDir;
-                undec = false;
-            }
-            else if (forced != nullptr && c < g.nc && forced[flat] != 0)
-            {
-                rj = kOutletReceiver;
-                dj = kNoDir;
-                undec = false;
+                if (((okc >> (8 * j)) & 0xffu) == 0u)
+                {
+                    rj = kNodataReceiver;
+                    dj = kNoDir;
+                    undec = false;
+                }
+                else if (forced != nullptr && c < g.nc && forced[flat] != 0)
+                {
+                    rj = kOutletReceiver;
+                    dj = kNoDir;
+                    undec = false;
+                }
             }
             if (undec) dj = kD8Undecided;
-            raise |= undec && row_inner && (inner || (c >= 1 && c <= g.nc - 2));
+            raise |= undec && (kInner || (row_inner && c >= 1 && c <= g.nc - 2));
             rec[j] = rj;
             dirs |= static_cast<unsigned>(dj & 0xff) << (8 * j);
         }
         const std::int64_t f0 = row_flat + cb;
         if (vec && cb + 4 <= g.nc)
         {
-            reinterpret_cast<longlong2*>(receiver + f0)[0] = make_longlong2(rec[0], rec[1]);
-            reinterpret_cast<longlong2*>(receiver + f0)[1] = make_longlong2(rec[2], rec[3]);
-            *reinterpret_cast<unsigned*>(dir + f0) = dirs;
+            reinterpret_cast<longlong2*>(J.receiver + f0)[0] = make_longlong2(rec[0], rec[1]);
+            reinterpret_cast<longlong2*>(J.receiver + f0)[1] = make_longlong2(rec[2], rec[3]);
+            *reinterpret_cast<unsigned*>(J.dir + f0) = dirs;
         }
         else
         {
@@ -421,12 +461,35 @@ __device__ __forceinline__ void d8_receivers_tile(const Grid& g, const float* __
             for (int j = 0; j < 4; ++j)
                 if (cb + j < g.nc)
                 {
-                    receiver[f0 + j] = rec[j];
-                    dir[f0 + j] = static_cast<std::uint8_t>(dirs >> (8 * j));
+                    J.receiver[f0 + j] = rec[j];
+                    J.dir[f0 + j] = static_cast<std::uint8_t>(dirs >> (8 * j));
                 }
         }
     }
-    if (__any_sync(0xffffffffu, raise) && lane == 0) atomicOr(undecided, 1u);
+    return raise;
+}
+
+// The tile pass for tile job J, one block.
+__device__ __forceinline__ void d8_receivers_tile(const D8Job& J, const std::uint8_t* __restrict__ forced,
+                                                  int interior_nodata_is_outlet, int allow_pits,
+                                                  unsigned* __restrict__ undecided)
+{
+    __shared__ __align__(16) D8TileBuf B;
+    __shared__ int soff[8];  // flat offset of each direction
+    const bool vec = d8_job_vec(J);
+    const int masked = d8_stage(J, B, vec);
+    if (threadIdx.x < 8) soff[threadIdx.x] = d8_dr(threadIdx.x) * J.g.nc + d8_dc(threadIdx.x);
+    const bool tile_masked = __syncthreads_or(masked) != 0 || forced != nullptr;
+    const int c0 = J.tx * kD8TileCols, r0 = J.ty * kD8TileRows;
+    const bool inner = r0 >= 1 && r0 + kD8TileRows <= J.g.nr - 1 && c0 >= 1 && c0 + kD8TileCols <= J.g.nc - 1;
+    bool raise;
+    if (tile_masked)
+        raise = inner ? d8_rank_tile<true, true>(J, B, soff, vec, forced, interior_nodata_is_outlet, allow_pits)
+                      : d8_rank_tile<true, false>(J, B, soff, vec, forced, interior_nodata_is_outlet, allow_pits);
+    else
+        raise = inner ? d8_rank_tile<false, true>(J, B, soff, vec, forced, interior_nodata_is_outlet, allow_pits)
+                      : d8_rank_tile<false, false>(J, B, soff, vec, forced, interior_nodata_is_outlet, allow_pits);
+    if (__any_sync(0xffffffffu, raise) && (threadIdx.x & 31) == 0) atomicOr(undecided, 1u);
 }
 
 // Fixup pass, one cell: the full rule from global memory (d8_receiver_cell)

@@ -155,9 +155,30 @@ __global__ void ens_flag_copy(const int* __restrict__ src, int* __restrict__ dst
 }
 
 // ---- D8, outlets, area -----------------------------------------------------
-// D8 receivers, tile pass: one block per 128 x 32 receiver tile of a member
-// (d8_receivers_tile on the member's own grid; receivers written as packed
-// indices).
+// Receiver tile t of the ensemble: a 128 x 32 tile of one member's grid,
+// receivers written as packed indices.
+struct MemberTiles
+{
+    Packed P;
+    const EnsParams* prm;
+    const std::uint16_t* rtile_member;
+    const float* zf;
+    const std::uint8_t* mask;
+    std::int64_t* receiver;
+    std::uint8_t* dir;
+    __device__ D8Job operator()(int t) const
+    {
+        const int m = rtile_member[t];
+        const PackedMember& M = P.m[m];
+        const EnsParams& q = prm[m];
+        const int local = t - M.rtile_base;
+        return D8Job{member_grid(M), zf + M.base, mask + M.base, receiver + M.base, dir + M.base,
+                     q.inv_card,      q.inv_diag,  local % M.nrx, local / M.nrx,    M.base};
+    }
+};
+
+// D8 receivers, tile pass: one block per member tile (d8_receivers_tile). The
+// LEM's engine: interior nodata drains, pits are outlets.
 __global__ void __launch_bounds__(256) ens_receivers(Packed P, const EnsParams* __restrict__ prm,
                                                      const std::uint16_t* __restrict__ rtile_member,
                                                      const float* __restrict__ zf,
@@ -166,13 +187,8 @@ __global__ void __launch_bounds__(256) ens_receivers(Packed P, const EnsParams* 
                                                      std::uint8_t* __restrict__ dir, unsigned* __restrict__ undecided)
 {
     LSDTT_COUNT();
-    const int m = rtile_member[blockIdx.x];
-    const PackedMember& M = P.m[m];
-    const EnsParams& q = prm[m];
-    const int local = static_cast<int>(blockIdx.x) - M.rtile_base;
-    // The LEM's engine: interior nodata drains, pits are outlets.
-    d8_receivers_tile(member_grid(M), zf + M.base, mask + M.base, nullptr, 1, 1, q.inv_card, q.inv_diag,
-                      receiver + M.base, dir + M.base, undecided, local % M.nrx, local / M.nrx, M.base);
+    const MemberTiles jobs{P, prm, rtile_member, zf, mask, receiver, dir};
+    d8_receivers_tile(jobs(static_cast<int>(blockIdx.x)), nullptr, 1, 1, undecided);
 }
 
 // D8 receivers, fixup pass: every member's perimeter cells, then (only when
