@@ -47,7 +47,7 @@ struct GridTiles
 };
 
 // Tile pass, one block per 128 x 32 tile (d8_receivers_tile).
-__global__ void __launch_bounds__(256) receivers_kernel(Grid g, const float* __restrict__ z,
+__global__ void __launch_bounds__(256, 5) receivers_kernel(Grid g, const float* __restrict__ z,
                                                         const std::uint8_t* __restrict__ mask,
                                                         const std::uint8_t* __restrict__ forced,
                                                         int interior_nodata_is_outlet, int allow_pits, float inv_card,

@@ -258,45 +258,54 @@ __device__ __forceinline__ int d8_stage(const D8Job& J, D8TileBuf& B, bool vec)
     int masked = 0;
     for (int lr = w; lr < kD8TileRows + 2; lr += 8)
     {
-        const int r = r0 - 1 + lr, c = c0 + 4 * lane;
-        float a[4] = {kNan, kNan, kNan, kNan};
-        unsigned ok = 0;
-        if (r >= 0 && r < g.nr)
+        const int r = r0 - 1 + lr;
+        const bool row_in = r >= 0 && r < g.nr;
+        const std::int64_t rf = static_cast<std::int64_t>(r) * g.nc + c0;
+        if (vec)
         {
-            const std::int64_t f = static_cast<std::int64_t>(r) * g.nc + c;
-            if (vec && c + 4 <= g.nc)
+            const int c = c0 + 4 * lane;
+            float a[4] = {kNan, kNan, kNan, kNan};
+            unsigned ok = 0;
+            if (row_in && c + 4 <= g.nc)
             {
-                const float4 q = *reinterpret_cast<const float4*>(J.z + f);
-                ok = *reinterpret_cast<const unsigned*>(J.mask + f);
+                const float4 q = *reinterpret_cast<const float4*>(J.z + rf + 4 * lane);
+                ok = *reinterpret_cast<const unsigned*>(J.mask + rf + 4 * lane);
                 a[0] = q.x;
                 a[1] = q.y;
                 a[2] = q.z;
                 a[3] = q.w;
-            }
-            else
-            {
+                const unsigned zero = __vcmpeq4(ok, 0u);  // 0xff in each invalid byte
+                if (zero != 0u)
+                {
+                    masked = 1;
 #pragma unroll
-                for (int j = 0; j < 4; ++j)
-                    if (c + j < g.nc)
-                    {
-                        a[j] = J.z[f + j];
-                        ok |= static_cast<unsigned>(J.mask[f + j]) << (8 * j);
-                    }
+                    for (int j = 0; j < 4; ++j)
+                        if ((zero >> (8 * j)) & 1u) a[j] = kNan;
+                }
             }
-            const unsigned zero = __vcmpeq4(ok, 0u);  // 0xff in each invalid byte
-            if (zero != 0u)
-            {
+            *reinterpret_cast<float4*>(&B.sz[lr][4 + 4 * lane]) = make_float4(a[0], a[1], a[2], a[3]);
+            *reinterpret_cast<unsigned*>(&B.sm[lr][4 + 4 * lane]) = ok;
+        }
+        else
+        {
+            // rows not 16-byte aligned: four coalesced passes of 32 columns
 #pragma unroll
-                for (int j = 0; j < 4; ++j)
-                    if ((zero >> (8 * j)) & 1u)
-                    {
-                        a[j] = kNan;
-                        masked |= c + j < g.nc;
-                    }
+            for (int j = 0; j < 4; ++j)
+            {
+                const int col = 32 * j + lane;
+                float v = kNan;
+                std::uint8_t m = 0;
+                if (row_in && c0 + col < g.nc)
+                {
+                    m = J.mask[rf + col];
+                    const float zf = J.z[rf + col];
+                    v = m ? zf : kNan;
+                    masked |= (m == 0);
+                }
+                B.sz[lr][4 + col] = v;
+                B.sm[lr][4 + col] = m;
             }
         }
-        *reinterpret_cast<float4*>(&B.sz[lr][4 + 4 * lane]) = make_float4(a[0], a[1], a[2], a[3]);
-        *reinterpret_cast<unsigned*>(&B.sm[lr][4 + 4 * lane]) = ok;
     }
     if (threadIdx.x < 2 * (kD8TileRows + 2))  // halo columns c0 - 1 and c0 + 128
     {

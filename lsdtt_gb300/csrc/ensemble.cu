@@ -179,7 +179,7 @@ struct MemberTiles
 
 // D8 receivers, tile pass: one block per member tile (d8_receivers_tile). The
 // LEM's engine: interior nodata drains, pits are outlets.
-__global__ void __launch_bounds__(256) ens_receivers(Packed P, const EnsParams* __restrict__ prm,
+__global__ void __launch_bounds__(256, 5) ens_receivers(Packed P, const EnsParams* __restrict__ prm,
                                                      const std::uint16_t* __restrict__ rtile_member,
                                                      const float* __restrict__ zf,
                                                      const std::uint8_t* __restrict__ mask,
