@@ -780,7 +780,7 @@ def main():
     ap.add_argument("--train-surfaces", type=int, default=64)
     ap.add_argument("--train-steps", type=int, default=2000)
     ap.add_argument("--members", type=int, default=256)
-    ap.add_argument("--sweep-mode", type=int, default=-1, help="ensemble sweep: -1 autotuned, 0 levels, 1 dataflow")
+    ap.add_argument("--sweep-mode", type=int, default=-1, help="ensemble sweep: -1 autotuned, 0 levels, 1 dataflow, 2 cooperative levels, 3 member clusters")
     ap.add_argument("--plain-members", type=int, default=16)
     args = ap.parse_args()
     if args.warmup < 3:

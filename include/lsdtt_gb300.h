@@ -389,9 +389,12 @@ typedef struct lsdtt_gpu_ensemble_info
     int32_t last_hillslope_iterations;
     double tuned_sweep_ms;        /* autotuner: best stream-power sweep time */
     double untuned_sweep_ms;      /* ... and one launch per level */
-    int32_t sweep_dataflow;       /* 1: the in-order dataflow sweep is in use */
+    int32_t sweep_dataflow;       /* sweep in use: 0 level launches, 1 in-order dataflow, 2 cooperative levels,
+                                     3 member clusters */
     int32_t reserved;
     double dataflow_sweep_ms;     /* autotuner: the dataflow sweep's time */
+    double coop_sweep_ms;         /* autotuner: the cooperative level sweep's best time */
+    double cluster_sweep_ms;      /* autotuner: the member-cluster sweep's time */
 } lsdtt_gpu_ensemble_info;
 
 int lsdtt_gpu_ensemble_get_info(const lsdtt_gpu_ensemble* ens, lsdtt_gpu_ensemble_info* info);
@@ -399,8 +402,10 @@ int lsdtt_gpu_ensemble_get_info(const lsdtt_gpu_ensemble* ens, lsdtt_gpu_ensembl
  * the recorded count plus margin) instead of the tuned ones, once; a
  * replay that outgrows them is undone and rerun like any other.
  * sweep_mode fixes the stream-power sweep from now on (0: one launch per
- * depth level plus the small-level tail, 1: the in-order dataflow sweep;
- * -1: leave it to the autotuner). */
+ * depth level plus the small-level tail, 1: the in-order dataflow sweep,
+ * 2: one cooperative launch with a grid barrier per level plus the tail,
+ * 3: one cluster of CTAs per member walking its own levels; -1: leave it to
+ * the autotuner). */
 int lsdtt_gpu_ensemble_override_schedule(lsdtt_gpu_ensemble* ens, int32_t fill_pass_cap,
                                          int32_t hillslope_iteration_cap, int32_t sweep_mode);
 

@@ -311,7 +311,8 @@ class EnsembleInfo(ctypes.Structure):
                 ("last_max_depth", ctypes.c_int32), ("last_hillslope_iterations", ctypes.c_int32),
                 ("tuned_sweep_ms", ctypes.c_double), ("untuned_sweep_ms", ctypes.c_double),
                 ("sweep_dataflow", ctypes.c_int32), ("reserved", ctypes.c_int32),
-                ("dataflow_sweep_ms", ctypes.c_double)]
+                ("dataflow_sweep_ms", ctypes.c_double), ("coop_sweep_ms", ctypes.c_double),
+                ("cluster_sweep_ms", ctypes.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -495,7 +496,8 @@ class Ensemble:
 
     def override_schedule(self, fill_pass_cap=0, hillslope_iteration_cap=0, sweep_mode=-1):
         """Force a schedule (tests): caps for the next capture; sweep_mode 0
-        (level launches), 1 (dataflow) or -1 (autotuned)."""
+        (level launches), 1 (dataflow), 2 (cooperative levels), 3 (member
+        clusters) or -1 (autotuned)."""
         _check(lib().lsdtt_gpu_ensemble_override_schedule(self._h, fill_pass_cap, hillslope_iteration_cap,
                                                           sweep_mode))
 

@@ -39,6 +39,7 @@
 #include <string>
 #include <vector>
 
+#include <cooperative_groups.h>
 #include <cuda/atomic>
 
 #include "engine.cuh"
@@ -47,6 +48,8 @@
 #include "hs_stencil.cuh"
 #include "lem_cell.cuh"
 #include "sp_node.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace lsdtt_gb300
 {
@@ -365,6 +368,79 @@ __global__ void ens_depth_scatter(std::int64_t n, const std::uint8_t* __restrict
     }
 }
 
+// Member-major depth order: the bucket of a valid cell is its member's
+// packed base plus its depth (a member's depths are below its cell count, so
+// members' bucket ranges do not overlap and the packed length bounds them).
+// Also the deepest level of each member.
+__global__ void ens_mdepth_hist(Packed P, const std::uint8_t* __restrict__ mask, const std::int32_t* __restrict__ depth,
+                                std::uint32_t* __restrict__ count, std::uint32_t* __restrict__ mmax)
+{
+    LSDTT_COUNT();
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    long long key = -1;
+    int m = 0;
+    std::int32_t d = 0;
+    if (i < P.n && mask[i])
+    {
+        d = depth[i];
+        if (d >= 0)
+        {
+            m = member_of(P, i);
+            key = P.m[m].base + d;
+        }
+    }
+    const unsigned peers = __match_any_sync(0xffffffffu, static_cast<unsigned long long>(key));
+    const int lane = threadIdx.x & 31;
+    if (key >= 0 && lane == __ffs(peers) - 1)
+    {
+        atomicAdd(&count[key], static_cast<unsigned>(__popc(peers)));
+        if (static_cast<std::uint32_t>(d) > mmax[m]) atomicMax(&mmax[m], static_cast<std::uint32_t>(d));
+    }
+}
+
+__global__ void ens_mdepth_scatter(Packed P, const std::uint8_t* __restrict__ mask,
+                                   const std::int32_t* __restrict__ depth, const std::uint32_t* __restrict__ start,
+                                   std::uint32_t* __restrict__ fillc, std::uint32_t* __restrict__ order)
+{
+    LSDTT_COUNT();
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    long long key = -1;
+    if (i < P.n && mask[i])
+    {
+        const std::int32_t d = depth[i];
+        if (d >= 0) key = P.m[member_of(P, i)].base + d;
+    }
+    const unsigned peers = __match_any_sync(0xffffffffu, static_cast<unsigned long long>(key));
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(peers) - 1;
+    std::uint32_t base = 0;
+    if (key >= 0 && lane == leader) base = atomicAdd(&fillc[key], static_cast<unsigned>(__popc(peers)));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (key >= 0)
+    {
+        const unsigned rank = __popc(peers & ((1u << lane) - 1u));
+        order[start[key] + base + rank] = static_cast<std::uint32_t>(i);
+    }
+}
+
+// The deepest level over all members.
+__global__ void ens_mdepth_max(int n_members, const std::uint32_t* __restrict__ mmax, std::uint32_t* __restrict__ maxd)
+{
+    LSDTT_COUNT();
+    std::uint32_t v = 0;
+    for (int m = threadIdx.x; m < n_members; m += blockDim.x) v = max(v, mmax[m]);
+    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_down_sync(0xffffffffu, v, o));
+    __shared__ std::uint32_t w[32];
+    if ((threadIdx.x & 31) == 0) w[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        std::uint32_t r = 0;
+        for (int k = 0; k < static_cast<int>(blockDim.x >> 5); ++k) r = max(r, w[k]);
+        *maxd = r;
+    }
+}
+
 __global__ void ens_copy(const float* __restrict__ a, float* __restrict__ b, std::int64_t n)
 {
     LSDTT_COUNT();
@@ -411,6 +487,163 @@ __global__ void __launch_bounds__(1024) ens_sp_tail(SweepArgs A, int k0)
         const std::uint32_t lo = A.start[k], hi = A.start[k + 1];
         for (std::uint32_t j = lo + threadIdx.x; j < hi; j += blockDim.x) sweep_node(A, A.order[j]);
         __syncthreads();
+    }
+}
+
+// Cooperative level sweep: one launch of co-resident blocks runs levels
+// 1 .. split-1 with a grid barrier between levels, then block 0 alone runs
+// the small levels split .. maxd with block barriers (as ens_sp_tail). The
+// barrier is a counter plus a generation word; its wait is bounded and a
+// wait that runs out sets the abort flag, which ends every other wait.
+// Receiver elevations are read from L2 (other SMs wrote them).
+constexpr int kBarrierSpinLimit = 1 << 22;
+
+__device__ __forceinline__ bool ens_grid_barrier(unsigned* bar, unsigned nblocks, int* abort_flag)
+{
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        cuda::atomic_ref<unsigned, cuda::thread_scope_device> count(bar[0]), gen(bar[1]);
+        cuda::atomic_ref<int, cuda::thread_scope_device> ab(*abort_flag);
+        const unsigned g = gen.load(cuda::memory_order_relaxed);
+        int good = 1;
+        __threadfence();
+        if (count.fetch_add(1u, cuda::memory_order_acq_rel) == nblocks - 1u)
+        {
+            count.store(0u, cuda::memory_order_relaxed);
+            gen.store(g + 1u, cuda::memory_order_release);
+        }
+        else
+        {
+            int spins = 0;
+            while (gen.load(cuda::memory_order_acquire) == g)
+            {
+                if (++spins > kBarrierSpinLimit || ab.load(cuda::memory_order_relaxed) != 0)
+                {
+                    ab.store(1, cuda::memory_order_relaxed);
+                    good = 0;
+                    break;
+                }
+            }
+        }
+        __threadfence();
+        ok = good;
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+__global__ void __launch_bounds__(512) ens_sp_coop(SweepArgs A, int split, unsigned* __restrict__ bar,
+                                                   int* __restrict__ abort_flag)
+{
+    LSDTT_COUNT();
+    const int kmax = static_cast<int>(*A.maxd);
+    const int kend = min(split, kmax + 1);
+    const std::uint32_t stride = gridDim.x * blockDim.x;
+    for (int k = 1; k < kend; ++k)
+    {
+        const std::uint32_t lo = A.start[k], hi = A.start[k + 1];
+        for (std::uint32_t j = lo + blockIdx.x * blockDim.x + threadIdx.x; j < hi; j += stride)
+        {
+            const std::uint32_t flat = A.order[j];
+            sp_node_kam<true>(A.prm[member_of(A.P, flat)].sp, A.P.n, flat, A.receiver, A.dir, A.kam[flat], A.z_old,
+                              A.z);
+        }
+        if (!ens_grid_barrier(bar, gridDim.x, abort_flag)) return;
+    }
+    if (blockIdx.x != 0) return;
+    for (int k = max(kend, 1); k <= kmax; ++k)
+    {
+        const std::uint32_t lo = A.start[k], hi = A.start[k + 1];
+        for (std::uint32_t j = lo + threadIdx.x; j < hi; j += blockDim.x)
+        {
+            const std::uint32_t flat = A.order[j];
+            sp_node_kam<true>(A.prm[member_of(A.P, flat)].sp, A.P.n, flat, A.receiver, A.dir, A.kam[flat], A.z_old,
+                              A.z);
+        }
+        __syncthreads();
+    }
+}
+
+constexpr unsigned kSweepClusterBlock = 128;  // largest block of the member-cluster sweep
+
+// One node of the member-cluster sweep with its independent loads done.
+struct SweepNode
+{
+    std::int64_t recv;  // < 0: nothing to do
+    double kam;
+    std::uint32_t flat;
+    float zo;
+    bool diag;
+};
+
+__device__ __forceinline__ SweepNode sweep_fetch(const SweepArgs& A, std::uint32_t j, std::uint32_t hi)
+{
+    SweepNode v{-1, -1.0, 0u, 0.0f, false};
+    if (j < hi)
+    {
+        v.flat = A.order[j];
+        v.recv = A.receiver[v.flat];
+        v.kam = A.kam[v.flat];
+        v.zo = A.z_old[v.flat];
+        v.diag = (A.dir[v.flat] & 1u) != 0;
+        if (v.recv >= A.P.n || v.kam < 0.0) v.recv = -1;  // outlets, nodata, below threshold
+    }
+    return v;
+}
+
+__device__ __forceinline__ void sweep_solve(const SweepArgs& A, const SpParams& sp, const SweepNode& v)
+{
+    if (v.recv < 0) return;
+    A.z[v.flat] = sp_solve(sp, v.diag, v.kam, v.zo, __ldcg(A.z + v.recv));
+}
+
+// Member-cluster sweep: one cluster of CTAs per member (largest members
+// first), walking the member's own depth levels from the member-major order
+// with the hardware cluster barrier between levels. Members do not wait on
+// one another, a member's nodes of one level are spread over the cluster's
+// SMs (the FP64 Newton work of a large member is not confined to one SM), and
+// a level costs a cluster barrier instead of a launch or a grid barrier. Only
+// the receiver's new elevation depends on the previous level: each thread
+// fetches its first node of level k+1 (order, receiver, K*A^m, old
+// elevation, direction) between its arrival at the cluster barrier and its
+// wait there, so a level's critical path is one L2 load, the solve and the
+// barrier.
+__global__ void __launch_bounds__(kSweepClusterBlock) ens_sp_clusters(SweepArgs A,
+                                                                      const std::uint16_t* __restrict__ perm,
+                                                                      const std::uint32_t* __restrict__ mmax)
+{
+    LSDTT_COUNT();
+    cg::cluster_group cluster = cg::this_cluster();
+    const unsigned C = cluster.num_blocks(), rank = cluster.block_rank();
+    const int m = perm[blockIdx.x / C];
+    const std::int64_t base = A.P.m[m].base;
+    const SpParams sp = A.prm[m].sp;
+    const std::uint32_t kmax = mmax[m];
+    const std::uint32_t stride = C * blockDim.x, off = rank * blockDim.x + threadIdx.x;
+    if (kmax == 0) return;  // whole clusters: kmax is the member's
+    // every CTA of the cluster is running before any arrives at its barrier
+    cluster.sync();
+    std::uint32_t lo = A.start[base + 1], hi = A.start[base + 2];
+    SweepNode cur = sweep_fetch(A, lo + off, hi);
+    std::uint32_t nhi = kmax > 1 ? A.start[base + 3] : hi;  // end of level 2
+    for (std::uint32_t k = 1; k <= kmax; ++k)
+    {
+        sweep_solve(A, sp, cur);
+        for (std::uint32_t j = lo + off + stride; j < hi; j += stride) sweep_solve(A, sp, sweep_fetch(A, j, hi));
+        // Arrive (release: this level's elevations), then fetch the next
+        // level's independent data while the cluster catches up, then wait
+        // (acquire) before any receiver elevation of it is read.
+        __syncwarp();  // the .aligned barrier wants converged warps
+        asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory");
+        const std::uint32_t nlo = hi;
+        cur = sweep_fetch(A, nlo + off, nhi);
+        const std::uint32_t nnhi = k + 1 < kmax ? A.start[base + k + 3] : nhi;
+        asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
+        lo = nlo;
+        hi = nhi;
+        nhi = nnhi;
     }
 }
 
@@ -951,9 +1184,18 @@ struct lsdtt_gpu_ensemble
     cudaStream_t own = nullptr;  // private stream: the legacy default stream cannot be captured
     cudaEvent_t ev_in = nullptr, ev_out = nullptr;  // order the private stream after/before the caller's
     std::uint32_t tail = 0;      // tuned: levels of at most `tail` cells run in one block (0: none)
-    int sweep_mode = 0;          // tuned: 0 level launches (+ tail), 1 in-order dataflow
+    int sweep_mode = 0;          // tuned: 0 level launches (+ tail), 1 in-order dataflow, 2 cooperative levels,
+                                 // 3 member clusters
     bool forced_mode = false;    // sweep_mode set by the caller, not the autotuner
     int df_grid = 0;             // persistent blocks of the dataflow sweep
+    int coop_grid = 0;           // co-resident blocks of the cooperative level sweep
+    std::uint32_t* morder = nullptr;  // [N] member-major depth order (member-cluster sweep)
+    std::uint32_t* mstart = nullptr;  // [N + 2] its bucket offsets (member base + depth)
+    std::uint32_t* mmax = nullptr;    // [M] deepest level of each member
+    std::uint16_t* perm = nullptr;    // [M] members by decreasing cell count
+    std::vector<std::uint16_t> perm_h;
+    int sweep_cluster = 8;            // CTAs per member cluster (tuned: 4 or 8)
+    unsigned* bar = nullptr;     // its grid barrier: {count, generation}
     unsigned long long* zg = nullptr;  // dataflow {generation, z} word per cell
     std::uint32_t* dfc = nullptr;    // [0] generation, [1] chunk counter
     int ov_fill = 0, ov_it = 0;  // one-shot schedule override for the next capture
@@ -977,7 +1219,7 @@ void free_ensemble(lsdtt_gpu_ensemble* E)
 {
     if (E->exec) cudaGraphExecDestroy(E->exec);
     if (E->graph) cudaGraphDestroy(E->graph);
-    void* bufs[] = {E->d_pm, E->d_prm, E->blk_member, E->tile_member, E->strip_member, E->undecided, E->z, E->zf, E->zsp, E->zpre, E->kind, E->bflag, E->dirty, E->oflag, E->pos, E->nd, E->area, E->order, E->lstart, E->lcount,
+    void* bufs[] = {E->d_pm, E->d_prm, E->blk_member, E->tile_member, E->strip_member, E->undecided, E->bar, E->morder, E->mstart, E->mmax, E->perm, E->z, E->zf, E->zsp, E->zpre, E->kind, E->bflag, E->dirty, E->oflag, E->pos, E->nd, E->area, E->order, E->lstart, E->lcount,
                     E->lfill, E->maxd, E->dof, E->invd, E->b, E->x, E->r, E->p, E->p2, E->zz, E->Ap, E->hs_bb, E->hs_acc,
                     E->done, E->iters, E->stats_acc, E->part, E->kam_tab, E->flags, E->zg, E->dfc};
     for (void* q : bufs) cudaFree(q);
@@ -991,9 +1233,43 @@ void free_ensemble(lsdtt_gpu_ensemble* E)
 }
 
 // Sweep launches for levels 1 .. split-1 (one launch each), then the tail.
-void enqueue_sweep(lsdtt_gpu_ensemble* E, const SweepArgs& A, int split, int block,
-                   const std::vector<unsigned>& blocks, cudaStream_t st, int mode)
+cudaError_t enqueue_sweep(lsdtt_gpu_ensemble* E, const SweepArgs& A, int split, int block,
+                          const std::vector<unsigned>& blocks, cudaStream_t st, int mode)
 {
+    if (mode == 3)
+    {
+        SweepArgs B = A;
+        B.order = E->morder;
+        B.start = E->mstart;
+        cudaLaunchConfig_t cfg{};
+        const unsigned cl = static_cast<unsigned>(E->sweep_cluster);
+        cfg.gridDim = dim3(static_cast<unsigned>(E->M) * cl);
+        cfg.blockDim = dim3(static_cast<unsigned>(std::min(block, static_cast<int>(kSweepClusterBlock))));
+        cfg.stream = st;
+        cudaLaunchAttribute attr{};
+        attr.id = cudaLaunchAttributeClusterDimension;
+        attr.val.clusterDim.x = cl;
+        attr.val.clusterDim.y = 1;
+        attr.val.clusterDim.z = 1;
+        cfg.attrs = &attr;
+        cfg.numAttrs = 1;
+        return cudaLaunchKernelEx(&cfg, ens_sp_clusters, B, static_cast<const std::uint16_t*>(E->perm),
+                                  static_cast<const std::uint32_t*>(E->mmax));
+    }
+    if (mode == 2)
+    {
+        cudaMemsetAsync(E->bar, 0, sizeof(unsigned) * 2, st);
+        cudaLaunchConfig_t cfg{};
+        cfg.gridDim = dim3(static_cast<unsigned>(E->coop_grid));
+        cfg.blockDim = dim3(512);
+        cfg.stream = st;
+        cudaLaunchAttribute attr{};
+        attr.id = cudaLaunchAttributeCooperative;
+        attr.val.cooperative = 1;
+        cfg.attrs = &attr;
+        cfg.numAttrs = 1;
+        return cudaLaunchKernelEx(&cfg, ens_sp_coop, A, split, E->bar, E->flags + 7);
+    }
     if (mode == 1)
     {
         ens_gen_bump<<<1, 1, 0, st>>>(E->dfc);
@@ -1001,11 +1277,12 @@ void enqueue_sweep(lsdtt_gpu_ensemble* E, const SweepArgs& A, int split, int blo
         cudaMemsetAsync(E->dfc + 1, 0, sizeof(std::uint32_t), st);
         ens_sp_dataflow<<<E->df_grid, 256, 0, st>>>(A, E->dfc, E->dfc + 1, E->zg, E->flags + 7);
         ens_sp_extract<<<grid_blocks(E->N, 256), 256, 0, st>>>(E->N, E->dfc, E->zg, A.z);
-        return;
+        return cudaSuccess;
     }
     for (int k = 1; k < split; ++k)
         ens_sp_level<<<blocks[static_cast<std::size_t>(k)], block, 0, st>>>(A, k);
     ens_sp_tail<<<1, 1024, 0, st>>>(A, split);
+    return cudaSuccess;
 }
 
 // Blocks of each level launch for a level-size profile.
@@ -1102,25 +1379,63 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
     ens_kam<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->mask, f->receiver, f->sv_size, E->kam_tab, E->area, E->lfill,
                                 E->dfc + 1);
     ens_kam_big<<<152 * 8, 256, 0, st>>>(E->P, E->d_prm, f->sv_size, E->lfill, E->dfc + 1, E->area);
-    // 2. depth levels
-    const std::uint32_t cap = eager ? static_cast<std::uint32_t>(N + 1) : static_cast<std::uint32_t>(E->depth_cap);
-    cudaMemsetAsync(E->maxd, 0, sizeof(std::uint32_t), st);
-    cudaMemsetAsync(E->lcount, 0, sizeof(std::uint32_t) * (static_cast<std::size_t>(cap) + 2), st);
-    ens_depth_hist<<<nb, 256, 0, st>>>(N, E->mask, f->depth, cap, E->lcount, E->maxd, E->flags + 2);
-    std::uint32_t scan_len = cap + 1;
-    if (eager)
+    // 2. depth levels: the global level order (level launches, the
+    // cooperative and dataflow sweeps, and every eager step's record) and
+    // the member-major order (member-cluster sweep, and the autotuner)
+    const bool global_order = eager || E->sweep_mode != 3;
+    const bool member_order = E->sweep_mode == 3 || (eager && !E->tuned);
+    if (global_order)
     {
-        cudaMemcpyAsync(E->h_maxd, E->maxd, sizeof(std::uint32_t), cudaMemcpyDeviceToHost, st);
-        e = cudaStreamSynchronize(st);
+        const std::uint32_t cap =
+            eager ? static_cast<std::uint32_t>(N + 1) : static_cast<std::uint32_t>(E->depth_cap);
+        cudaMemsetAsync(E->maxd, 0, sizeof(std::uint32_t), st);
+        cudaMemsetAsync(E->lcount, 0, sizeof(std::uint32_t) * (static_cast<std::size_t>(cap) + 2), st);
+        ens_depth_hist<<<nb, 256, 0, st>>>(N, E->mask, f->depth, cap, E->lcount, E->maxd, E->flags + 2);
+        std::uint32_t scan_len = cap + 1;
+        if (eager)
+        {
+            cudaMemcpyAsync(E->h_maxd, E->maxd, sizeof(std::uint32_t), cudaMemcpyDeviceToHost, st);
+            e = cudaStreamSynchronize(st);
+            if (e != cudaSuccess) return e;
+            scan_len = *E->h_maxd + 2;
+        }
+        f->ws.used = 0;
+        e = exclusive_scan<std::uint32_t, std::uint32_t>(E->lcount, scan_len, E->lstart,
+                                                         static_cast<std::uint32_t*>(nullptr), f->ws, st);
         if (e != cudaSuccess) return e;
-        scan_len = *E->h_maxd + 2;
+        cudaMemsetAsync(E->lfill, 0, sizeof(std::uint32_t) * scan_len, st);
+        ens_depth_scatter<<<nb, 256, 0, st>>>(N, E->mask, f->depth, cap, E->lstart, E->lfill, E->order);
     }
-    f->ws.used = 0;
-    e = exclusive_scan<std::uint32_t, std::uint32_t>(E->lcount, scan_len, E->lstart,
-                                                     static_cast<std::uint32_t*>(nullptr), f->ws, st);
-    if (e != cudaSuccess) return e;
-    cudaMemsetAsync(E->lfill, 0, sizeof(std::uint32_t) * scan_len, st);
-    ens_depth_scatter<<<nb, 256, 0, st>>>(N, E->mask, f->depth, cap, E->lstart, E->lfill, E->order);
+    if (member_order)
+    {
+        cudaMemsetAsync(E->mmax, 0, sizeof(std::uint32_t) * M, st);
+        cudaMemsetAsync(E->lcount, 0, sizeof(std::uint32_t) * (static_cast<std::size_t>(N) + 1), st);
+        ens_mdepth_hist<<<nb, 256, 0, st>>>(E->P, E->mask, f->depth, E->lcount, E->mmax);
+        f->ws.used = 0;
+        e = exclusive_scan<std::uint32_t, std::uint32_t>(E->lcount, N + 1, E->mstart,
+                                                         static_cast<std::uint32_t*>(nullptr), f->ws, st);
+        if (e != cudaSuccess) return e;
+        cudaMemsetAsync(E->lfill, 0, sizeof(std::uint32_t) * (static_cast<std::size_t>(N) + 1), st);
+        ens_mdepth_scatter<<<nb, 256, 0, st>>>(E->P, E->mask, f->depth, E->mstart, E->lfill, E->morder);
+        if (!global_order) ens_mdepth_max<<<1, 256, 0, st>>>(M, E->mmax, E->maxd);
+        if (eager)
+        {
+            // Clusters start in member order: deepest members first (the
+            // sweep's critical path is a member's depth), then larger ones.
+            std::vector<std::uint32_t> depth_h(static_cast<std::size_t>(M));
+            cudaMemcpyAsync(depth_h.data(), E->mmax, sizeof(std::uint32_t) * M, cudaMemcpyDeviceToHost, st);
+            e = cudaStreamSynchronize(st);
+            if (e != cudaSuccess) return e;
+            std::stable_sort(E->perm_h.begin(), E->perm_h.end(), [&](std::uint16_t a, std::uint16_t b) {
+                if (depth_h[a] != depth_h[b]) return depth_h[a] > depth_h[b];
+                const PackedMember &A = E->pm[a], &B = E->pm[b];
+                return static_cast<std::int64_t>(A.nr) * A.nc > static_cast<std::int64_t>(B.nr) * B.nc;
+            });
+            cudaMemcpyAsync(E->perm, E->perm_h.data(), sizeof(std::uint16_t) * M, cudaMemcpyHostToDevice, st);
+            e = cudaStreamSynchronize(st);  // perm_h is updated again by the next eager step
+            if (e != cudaSuccess) return e;
+        }
+    }
     // 3. stream power, swept by depth level
     ens_copy<<<nb, 256, 0, st>>>(E->zf, E->zsp, N);
     SweepArgs A{E->P, E->d_prm, E->order, E->lstart, E->maxd, f->receiver, f->dir, E->area, E->zf, E->zsp};
@@ -1144,20 +1459,32 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
             cudaEventCreate(&t0);
             cudaEventCreate(&t1);
             double best = 1e30, one_per_level = 0.0;
+            int best_cluster = 0;
             std::uint32_t best_tail = 0;
             int best_block = 256;
             int best_mode = 0;
-            // candidate schedules: level launches with each tail threshold and
-            // block size, then the dataflow sweep (tail = ~0u marks it)
-            std::vector<std::pair<std::uint32_t, int>> cands;
+            // candidate schedules {tail threshold, block, mode}: level
+            // launches with each tail threshold and block size, the
+            // cooperative level sweep with each tail threshold, then the
+            // dataflow sweep
+            struct Cand
+            {
+                std::uint32_t tail;
+                int blk, mode, cluster;
+            };
+            std::vector<Cand> cands;
             for (std::uint32_t tail : tails)
-                for (int blk : blocks) cands.push_back({tail, blk});
-            cands.push_back({~0u, 256});
+                for (int blk : blocks) cands.push_back({tail, blk, 0, 0});
+            for (std::uint32_t tail : tails) cands.push_back({tail, 512, 2, 0});
+            cands.push_back({0u, 256, 1, 0});
+            for (int cl : {4, 8})
+                for (int blk : {64, 128}) cands.push_back({0u, blk, 3, cl});
             for (const auto& cand : cands)
                 {
-                    const std::uint32_t tail = cand.first;
-                    const int blk = cand.second;
-                    const int mode = tail == ~0u ? 1 : 0;
+                    const std::uint32_t tail = cand.tail;
+                    const int blk = cand.blk;
+                    const int mode = cand.mode;
+                    if (mode == 3) E->sweep_cluster = cand.cluster;
                     const int sp = (tail == 0 || mode == 1) ? static_cast<int>(D) + 1
                                                             : split_for(rec->level_size, tail);
                     const auto g = level_grid(rec->level_size, sp, blk, 1.0);
@@ -1166,7 +1493,14 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
                     {
                         ens_copy<<<nb, 256, 0, st>>>(E->zf, E->zsp, N);
                         cudaEventRecord(t0, st);
-                        enqueue_sweep(E, A, sp, blk, g, st, mode);
+                        if (enqueue_sweep(E, A, sp, blk, g, st, mode) != cudaSuccess)
+                        {
+                            cudaGetLastError();  // a launch refused (not a fault): not a candidate
+                            ms_best = 1e30f;
+                            cudaEventRecord(t1, st);
+                            cudaEventSynchronize(t1);
+                            break;
+                        }
                         cudaEventRecord(t1, st);
                         e = cudaEventSynchronize(t1);
                         if (e != cudaSuccess) break;
@@ -1175,10 +1509,17 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
                         ms_best = std::min(ms_best, ms);
                     }
                     if (e != cudaSuccess) break;
-                    if (tail == 0 && blk == 256) one_per_level = ms_best;
+                    if (mode == 0 && tail == 0 && blk == 256) one_per_level = ms_best;
                     if (mode == 1) E->info.dataflow_sweep_ms = ms_best;
-                    // a dataflow run that hit its wait limit is not a candidate
-                    if (mode == 1)
+                    if (mode == 3)
+                        E->info.cluster_sweep_ms = E->info.cluster_sweep_ms > 0.0
+                                                       ? std::min<double>(E->info.cluster_sweep_ms, ms_best)
+                                                       : ms_best;
+                    if (mode == 2)
+                        E->info.coop_sweep_ms =
+                            E->info.coop_sweep_ms > 0.0 ? std::min<double>(E->info.coop_sweep_ms, ms_best) : ms_best;
+                    // a run that hit its wait limit is not a candidate
+                    if (mode != 0)
                     {
                         int ab = 0;
                         cudaMemcpy(&ab, E->flags + 7, sizeof(int), cudaMemcpyDeviceToHost);
@@ -1190,6 +1531,7 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
                         best_tail = mode == 1 ? 0u : tail;
                         best_block = blk;
                         best_mode = mode;
+                        best_cluster = cand.cluster;
                     }
                 }
             cudaEventDestroy(t0);
@@ -1199,6 +1541,7 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
             // recomputed from each recorded profile.
             E->tail = best_tail;
             E->sweep_block = best_block;
+            if (best_cluster > 0) E->sweep_cluster = best_cluster;
             if (!E->forced_mode) E->sweep_mode = best_mode;
             E->info.tuned_sweep_ms = best;
             E->info.untuned_sweep_ms = one_per_level;
@@ -1207,11 +1550,15 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
         }
         const int sp = E->tail == 0 ? static_cast<int>(D) + 1 : split_for(rec->level_size, E->tail);
         E->split = sp;
-        enqueue_sweep(E, A, sp, E->sweep_block, level_grid(rec->level_size, sp, E->sweep_block, 1.0), st,
-                      E->sweep_mode);
+        e = enqueue_sweep(E, A, sp, E->sweep_block, level_grid(rec->level_size, sp, E->sweep_block, 1.0), st,
+                          E->sweep_mode);
+        if (e != cudaSuccess) return e;
     }
     else
-        enqueue_sweep(E, A, E->split, E->sweep_block, E->level_blocks, st, E->sweep_mode);
+    {
+        e = enqueue_sweep(E, A, E->split, E->sweep_block, E->level_blocks, st, E->sweep_mode);
+        if (e != cudaSuccess) return e;
+    }
     // 4. hillslope: Jacobi-PCG per member
     const std::size_t slot_bytes = sizeof(double) * kHsSlot * M;
     const int itmax = eager ? E->max_iter_all : E->it_cap;
@@ -1541,6 +1888,11 @@ int lsdtt_gpu_ensemble_create(const lsdtt_gpu_member* members, int32_t n_members
     alloc(&E->zg, n);
     alloc(&E->dfc, 2);
     alloc(&E->flags, kFlags);
+    alloc(&E->bar, 2);
+    alloc(&E->morder, n);
+    alloc(&E->mstart, n + 2);
+    alloc(&E->mmax, static_cast<std::size_t>(n_members));
+    alloc(&E->perm, static_cast<std::size_t>(n_members));
     if (e == cudaSuccess) e = cudaMallocHost(&E->h_stats, sizeof(double) * 8 * n_members);
     if (e == cudaSuccess) e = cudaMallocHost(&E->h_flags, sizeof(int) * kFlags);
     if (e == cudaSuccess) e = cudaMallocHost(&E->h_iters, sizeof(int) * n_members);
@@ -1556,6 +1908,16 @@ int lsdtt_gpu_ensemble_create(const lsdtt_gpu_member* members, int32_t n_members
     cudaMemcpyAsync(E->blk_member, blk.data(), sizeof(std::uint16_t) * blk.size(), cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(E->tile_member, tm.data(), sizeof(std::uint16_t) * tm.size(), cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(E->strip_member, sm.data(), sizeof(std::uint16_t) * sm.size(), cudaMemcpyHostToDevice, st);
+    {
+        std::vector<std::uint16_t> perm(static_cast<std::size_t>(n_members));
+        for (int k = 0; k < n_members; ++k) perm[static_cast<std::size_t>(k)] = static_cast<std::uint16_t>(k);
+        std::stable_sort(perm.begin(), perm.end(), [&](std::uint16_t a, std::uint16_t b) {
+            const PackedMember &A = E->pm[a], &B = E->pm[b];
+            return static_cast<std::int64_t>(A.nr) * A.nc > static_cast<std::int64_t>(B.nr) * B.nc;
+        });
+        E->perm_h = perm;
+    }
+    cudaMemcpyAsync(E->perm, E->perm_h.data(), sizeof(std::uint16_t) * E->perm_h.size(), cudaMemcpyHostToDevice, st);
     cudaMemsetAsync(E->z, 0, sizeof(float) * n, st);
     cudaMemsetAsync(E->mask, 0, n, st);
     cudaMemsetAsync(E->zg, 0, sizeof(unsigned long long) * n, st);
@@ -1569,6 +1931,9 @@ int lsdtt_gpu_ensemble_create(const lsdtt_gpu_member* members, int32_t n_members
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ens_sp_dataflow, 256, 0);
         E->df_grid = std::max(1, sms * std::max(1, per_sm));
+        per_sm = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ens_sp_coop, 512, 0);
+        E->coop_grid = std::max(1, sms * std::max(1, std::min(per_sm, 2)));
     }
     E->P.m = E->d_pm;
     E->P.blk_member = E->blk_member;
@@ -1702,7 +2067,7 @@ int lsdtt_gpu_ensemble_step(lsdtt_gpu_ensemble* E, int32_t n_steps, lsdtt_gpu_le
             }
         }
         if (E->h_flags[7])
-            return fail(LSDTT_GPU_ETIMEOUT, std::string(who) + ": the dataflow stream-power sweep hit its wait limit");
+            return fail(LSDTT_GPU_ETIMEOUT, std::string(who) + ": the stream-power sweep hit its wait limit");
         if ((E->h_err[0] & 0xffffffffull) != 0)
             return fail(LSDTT_GPU_ECYCLIC, std::string(who) + ": the receiver graph of a member has a cycle");
         if (E->h_flags[4])
@@ -1740,7 +2105,7 @@ int lsdtt_gpu_ensemble_download(const lsdtt_gpu_ensemble* E, float* z_host, void
 int lsdtt_gpu_ensemble_override_schedule(lsdtt_gpu_ensemble* E, int32_t fill_pass_cap, int32_t hillslope_iteration_cap,
                                          int32_t sweep_mode)
 {
-    if (!E || fill_pass_cap < 0 || hillslope_iteration_cap < 0 || sweep_mode < -1 || sweep_mode > 1)
+    if (!E || fill_pass_cap < 0 || hillslope_iteration_cap < 0 || sweep_mode < -1 || sweep_mode > 3)
         return fail(LSDTT_GPU_EINVAL, "lsdtt_gpu_ensemble_override_schedule: bad argument");
     E->ov_fill = fill_pass_cap;
     E->ov_it = hillslope_iteration_cap;

@@ -92,7 +92,10 @@ __device__ __forceinline__ float sp_solve(const SpParams& P, bool diagonal, doub
 // sp_solve for node `flat` with its own loads and store. Any receiver-
 // before-donor order gives the reference's bits: a node reads only
 // z_old[self] and z[receiver]. Indices are those of the arrays passed
-// (n = their length).
+// (n = their length). kCoherent reads the receiver's elevation from L2
+// (bypassing L1), for sweeps whose levels are written by other SMs of the
+// same launch.
+template <bool kCoherent = false>
 __device__ __forceinline__ void sp_node_kam(const SpParams& P, std::int64_t n, std::int64_t flat,
                                             const std::int64_t* __restrict__ receiver,
                                             const std::uint8_t* __restrict__ dir, double kam,
@@ -101,7 +104,8 @@ __device__ __forceinline__ void sp_node_kam(const SpParams& P, std::int64_t n, s
     const std::int64_t recv = receiver[flat];
     if (recv < 0 || recv >= n || kam < 0.0) return;  // outlets, nodata, below threshold
     const float zo = z_old[flat];
-    const float zn = sp_solve(P, (dir[flat] & 1u) != 0, kam, zo, z[recv]);
+    const float zr = kCoherent ? __ldcg(z + recv) : z[recv];
+    const float zn = sp_solve(P, (dir[flat] & 1u) != 0, kam, zo, zr);
     z[flat] = zn;  // zo when not eroded: z[flat] already holds it
 }
 

@@ -63,7 +63,8 @@ def _rel(a, b):
     return float(np.max(np.abs(a - b)) / max(float(np.ptp(b)), 1.0))
 
 
-@pytest.mark.parametrize("use_graph,sweep_mode", [(False, 0), (True, 0), (False, 1), (True, 1)])
+@pytest.mark.parametrize("use_graph,sweep_mode", [(False, 0), (True, 0), (False, 1), (True, 1), (False, 2), (True, 2),
+                                                     (False, 3), (True, 3)])
 def test_ensemble_matches_members_alone(port, use_graph, sweep_mode):
     import lsdtt_gb300 as G
     specs = _members(port)
