@@ -151,6 +151,34 @@ __global__ void __launch_bounds__(256) ens_fill_relax(Packed P, const EnsParams*
                     changed, din + M.tile_base, dout + M.tile_base, local % M.ntx, local / M.ntx, M.ntx, M.nty);
 }
 
+// Condition of the graph's PCG loop (a conditional WHILE node whose body is
+// two iterations and the convergence test): advance the iteration counter,
+// go on while a member is still iterating; a member still iterating at
+// itmax raises the PCG overflow flag.
+__global__ void ens_pcg_while(int* __restrict__ it_dev, int itmax, int* __restrict__ flags,
+                              cudaGraphConditionalHandle h)
+{
+    LSDTT_COUNT();
+    const int it = (*it_dev += 2);
+    const int active = flags[5];
+    flags[5] = 0;
+    if (active > 0 && it >= itmax) flags[3] = 1;
+    cudaGraphSetConditional(h, (active > 0 && it < itmax) ? 1u : 0u);
+}
+
+// Condition of the graph's fill loop (a conditional WHILE node whose body
+// is two relaxation passes): go on while the second pass changed a tile; a
+// loop that reaches max_pairs still changing raises the overflow flag.
+__global__ void ens_fill_while(const int* __restrict__ changed, int* __restrict__ count, int max_pairs,
+                               int* __restrict__ overflow, cudaGraphConditionalHandle h)
+{
+    LSDTT_COUNT();
+    const int c = ++*count;
+    const bool more = *changed != 0;
+    if (more && c >= max_pairs) *overflow = 1;
+    cudaGraphSetConditional(h, (more && c < max_pairs) ? 1u : 0u);
+}
+
 __global__ void ens_flag_copy(const int* __restrict__ src, int* __restrict__ dst)
 {
     LSDTT_COUNT();
@@ -787,12 +815,14 @@ __device__ __forceinline__ void block_partial_f(float v, bool is_max, double* __
 
 // dst[m * stride + off + q] = reduction of member m's block partials of
 // quantity q (bit q of max_mask: maximum, else sum); one warp per (m, q).
-// Members with done[m] set are skipped.
+// Members with done[m] set are skipped. With shift, dst moves by
+// *shift * shift_step (a device-side iteration's slot).
 __global__ void ens_member_reduce(Packed P, int nq, unsigned max_mask, const double* __restrict__ part,
                                   std::int64_t nblk, const int* __restrict__ done, double* __restrict__ dst, int stride,
-                                  int off)
+                                  int off, const int* __restrict__ shift = nullptr, std::int64_t shift_step = 0)
 {
     LSDTT_COUNT();
+    if (shift) dst += static_cast<std::int64_t>(*shift) * shift_step;
     const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     const int m = w / nq, q = w % nq;
@@ -914,16 +944,26 @@ __global__ void ens_hs_start(int M, const EnsParams* __restrict__ prm, const dou
 // p = z + beta p_src is formed on the fly at the cell and its neighbours
 // (beta = r.z / r_old.z_old of this member, once per block) and written to
 // p_dst, the buffer the update then reads; without it p_dst already holds p.
+// The dot products of iteration slots slot_new / slot_old of acc are read
+// (slots of kHsSlot * n_members doubles); with it_dev (a device-side loop)
+// both slots move by *it_dev and the direction update is fused whenever
+// *it_dev > 0.
 __global__ void ens_hs_apply(Packed P, const EnsParams* __restrict__ prm, const std::uint8_t* __restrict__ mask,
                              const std::uint8_t* __restrict__ dof, const int* __restrict__ done, int fuse,
-                             const double* __restrict__ rz_new, const double* __restrict__ rz_old,
-                             const float* __restrict__ zz, const float* __restrict__ p_src,
-                             float* __restrict__ p_dst, float* __restrict__ Ap, double* __restrict__ part)
+                             const double* __restrict__ acc, int slot_new, int slot_old,
+                             const int* __restrict__ it_dev, const float* __restrict__ zz,
+                             const float* __restrict__ p_src, float* __restrict__ p_dst, float* __restrict__ Ap,
+                             double* __restrict__ part)
 {
     LSDTT_COUNT();
     const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     const int m = member_of(P, i < P.n ? i : P.n - 1);
     if (done[m]) return;
+    const int sh = it_dev ? *it_dev : 0;
+    if (sh > 0) fuse = 1;
+    const std::int64_t slot = static_cast<std::int64_t>(kHsSlot) * P.n_members;
+    const double* rz_new = acc + slot * (slot_new + sh);
+    const double* rz_old = acc + slot * (slot_old + sh);
     __shared__ float s_beta;
     if (threadIdx.x == 0)
     {
@@ -989,16 +1029,20 @@ __global__ void ens_hs_apply(Packed P, const EnsParams* __restrict__ prm, const 
 }
 
 // alpha = r.z / p.Ap (once per block); x += alpha p; r -= alpha Ap; z = M^-1 r;
-// block partials of r.z and r.r
-__global__ void ens_hs_update(Packed P, const int* __restrict__ done, const double* __restrict__ prev,
-                              const float* __restrict__ inv_diag, const float* __restrict__ p,
-                              const float* __restrict__ Ap, float* __restrict__ x, float* __restrict__ r,
-                              float* __restrict__ zz, const double* __restrict__ cur, double* __restrict__ part)
+// block partials of r.z and r.r. Slots as in ens_hs_apply.
+__global__ void ens_hs_update(Packed P, const int* __restrict__ done, const double* __restrict__ acc, int slot_prev,
+                              int slot_cur, const int* __restrict__ it_dev, const float* __restrict__ inv_diag,
+                              const float* __restrict__ p, const float* __restrict__ Ap, float* __restrict__ x,
+                              float* __restrict__ r, float* __restrict__ zz, double* __restrict__ part)
 {
     LSDTT_COUNT();
     const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     const int m = member_of(P, i < P.n ? i : P.n - 1);
     if (done[m]) return;
+    const int sh = it_dev ? *it_dev : 0;
+    const std::int64_t slot = static_cast<std::int64_t>(kHsSlot) * P.n_members;
+    const double* prev = acc + slot * (slot_prev + sh);
+    const double* cur = acc + slot * (slot_cur + sh);
     __shared__ float s_alpha;
     if (threadIdx.x == 0)
     {
@@ -1024,14 +1068,20 @@ __global__ void ens_hs_update(Packed P, const int* __restrict__ done, const doub
 
 // After iteration `it` (0-based, it + 1 a multiple of 4 or the last one):
 // the single-grid convergence test per member. flags[5] counts the members
-// still iterating; flags[4] marks a member that reached max_iter.
+// still iterating; flags[4] marks a member that reached max_iter. With
+// it_dev, `it` and the slot `cur` move by *it_dev iterations.
 __global__ void ens_hs_check(int M, const EnsParams* __restrict__ prm, int it, const double* __restrict__ cur,
                              const double* __restrict__ hs_bb, int* __restrict__ done, int* __restrict__ iters,
-                             int* __restrict__ flags)
+                             int* __restrict__ flags, const int* __restrict__ it_dev = nullptr)
 {
     LSDTT_COUNT();
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= M || done[m]) return;
+    if (it_dev)
+    {
+        it += *it_dev;
+        cur += static_cast<std::int64_t>(*it_dev) * kHsSlot * M;
+    }
     const EnsParams& q = prm[m];
     const double rel = sqrt(cur[m * kHsSlot + 2]) / sqrt(hs_bb[m]);
     iters[m] = it + 1;
@@ -1182,6 +1232,9 @@ struct lsdtt_gpu_ensemble
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     cudaStream_t own = nullptr;  // private stream: the legacy default stream cannot be captured
+    cudaStream_t own2 = nullptr;  // captures the bodies of the graph's device-side loops
+    bool use_while = true;        // device-side loops (conditional WHILE nodes) in the graph
+    int* loopc = nullptr;         // [2] their trip counters (fill pass pairs, PCG iterations)
     cudaEvent_t ev_in = nullptr, ev_out = nullptr;  // order the private stream after/before the caller's
     std::uint32_t tail = 0;      // tuned: levels of at most `tail` cells run in one block (0: none)
     int sweep_mode = 0;          // tuned: 0 level launches (+ tail), 1 in-order dataflow, 2 cooperative levels,
@@ -1219,7 +1272,7 @@ void free_ensemble(lsdtt_gpu_ensemble* E)
 {
     if (E->exec) cudaGraphExecDestroy(E->exec);
     if (E->graph) cudaGraphDestroy(E->graph);
-    void* bufs[] = {E->d_pm, E->d_prm, E->blk_member, E->tile_member, E->strip_member, E->undecided, E->bar, E->morder, E->mstart, E->mmax, E->perm, E->z, E->zf, E->zsp, E->zpre, E->kind, E->bflag, E->dirty, E->oflag, E->pos, E->nd, E->area, E->order, E->lstart, E->lcount,
+    void* bufs[] = {E->d_pm, E->d_prm, E->blk_member, E->tile_member, E->strip_member, E->undecided, E->bar, E->loopc, E->morder, E->mstart, E->mmax, E->perm, E->z, E->zf, E->zsp, E->zpre, E->kind, E->bflag, E->dirty, E->oflag, E->pos, E->nd, E->area, E->order, E->lstart, E->lcount,
                     E->lfill, E->maxd, E->dof, E->invd, E->b, E->x, E->r, E->p, E->p2, E->zz, E->Ap, E->hs_bb, E->hs_acc,
                     E->done, E->iters, E->stats_acc, E->part, E->kam_tab, E->flags, E->zg, E->dfc};
     for (void* q : bufs) cudaFree(q);
@@ -1227,6 +1280,7 @@ void free_ensemble(lsdtt_gpu_ensemble* E)
     for (void* q : hb) cudaFreeHost(q);
     if (E->f) lsdtt_gpu_flow_destroy(E->f);
     if (E->own) cudaStreamDestroy(E->own);
+    if (E->own2) cudaStreamDestroy(E->own2);
     if (E->ev_in) cudaEventDestroy(E->ev_in);
     if (E->ev_out) cudaEventDestroy(E->ev_out);
     delete E;
@@ -1308,6 +1362,41 @@ int split_for(const std::vector<std::uint32_t>& size, std::uint32_t tail)
 
 // One step. eager: host-driven loops (records the schedule in *rec and
 // autotunes the sweep on the first call); otherwise the captured schedule.
+// Appends a conditional WHILE node to the graph being captured on st (after
+// the work captured so far) and captures body(st2, handle) as its body; the
+// body's last kernel sets the condition with cudaGraphSetConditional. Work
+// captured on st afterwards depends on the node.
+template <class Body>
+cudaError_t capture_while(cudaStream_t st, cudaStream_t st2, const Body& body)
+{
+    cudaStreamCaptureStatus status = cudaStreamCaptureStatusNone;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    std::size_t ndeps = 0;
+    cudaError_t e = cudaStreamGetCaptureInfo(st, &status, nullptr, &g, &deps, nullptr, &ndeps);
+    if (e != cudaSuccess) return e;
+    if (status != cudaStreamCaptureStatusActive) return cudaErrorStreamCaptureInvalidated;
+    cudaGraphConditionalHandle h = 0;
+    e = cudaGraphConditionalHandleCreate(&h, g, 1u, cudaGraphCondAssignDefault);
+    if (e != cudaSuccess) return e;
+    cudaGraphNodeParams np{};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = h;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t node = nullptr;
+    e = cudaGraphAddNode(&node, g, deps, nullptr, ndeps, &np);
+    if (e != cudaSuccess) return e;
+    e = cudaStreamBeginCaptureToGraph(st2, np.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                      cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return e;
+    body(st2, h);
+    cudaGraph_t done = nullptr;
+    e = cudaStreamEndCapture(st2, &done);
+    if (e != cudaSuccess) return e;
+    return cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+}
+
 cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRecord* rec)
 {
     const std::int64_t N = E->N;
@@ -1346,6 +1435,23 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
             if (passes > E->max_pass_all) return cudaErrorLaunchTimeout;
         }
         rec->fill_passes = passes;
+    }
+    else if (E->use_while)
+    {
+        // Device-side loop: pairs of passes until the second of a pair
+        // changes nothing (a fixed point), at most max_pass_all passes.
+        cudaMemsetAsync(E->loopc, 0, sizeof(int), st);
+        const int max_pairs = (E->max_pass_all + 1) / 2;
+        e = capture_while(st, E->own2, [&](cudaStream_t s2, cudaGraphConditionalHandle h) {
+            for (int k = 0; k < 2; ++k)
+            {
+                if (k == 1) cudaMemsetAsync(E->flags, 0, sizeof(int), s2);
+                ens_fill_relax<<<E->T, fblock, 0, s2>>>(E->P, E->d_prm, E->tile_member, E->z, E->kind, E->zf, E->flags,
+                                                        E->dirty + (k & 1) * E->T, E->dirty + ((k + 1) & 1) * E->T);
+            }
+            ens_fill_while<<<1, 1, 0, s2>>>(E->flags, E->loopc, max_pairs, E->flags + 1, h);
+        });
+        if (e != cudaSuccess) return e;
     }
     else
     {
@@ -1561,60 +1667,96 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
     }
     // 4. hillslope: Jacobi-PCG per member
     const std::size_t slot_bytes = sizeof(double) * kHsSlot * M;
-    const int itmax = eager ? E->max_iter_all : E->it_cap;
+    const std::int64_t slot_len = static_cast<std::int64_t>(kHsSlot) * M;
+    const bool device_loop = !eager && E->use_while;
+    const int itmax = (eager || device_loop) ? E->max_iter_all : E->it_cap;
     const std::int64_t nblk = N / kPackAlign;
-    auto reduce = [&](int nq, unsigned max_mask, const int* dn, double* dst, int stride, int off) {
+    auto reduce = [&](cudaStream_t s2, int nq, unsigned max_mask, const int* dn, double* dst, int stride, int off,
+                      const int* shift) {
         const unsigned warps = static_cast<unsigned>(M * nq);
-        ens_member_reduce<<<(warps + 3) / 4, 128, 0, st>>>(E->P, nq, max_mask, E->part, nblk, dn, dst, stride, off);
+        ens_member_reduce<<<(warps + 3) / 4, 128, 0, s2>>>(E->P, nq, max_mask, E->part, nblk, dn, dst, stride, off,
+                                                           shift, slot_len);
     };
     cudaMemsetAsync(E->hs_acc, 0, slot_bytes * (static_cast<std::size_t>(itmax) + 1), st);
     ens_hs_setup<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->mask, E->zsp, E->dof, E->invd, E->b, E->part);
-    reduce(1, 0u, nullptr, E->hs_bb, 1, 0);
+    reduce(st, 1, 0u, nullptr, E->hs_bb, 1, 0, nullptr);
     ens_hs_init<<<nb, 256, 0, st>>>(E->P, E->b, E->invd, E->x, E->r, E->p, E->part);
-    reduce(1, 0u, nullptr, E->hs_acc, kHsSlot, 1);
+    reduce(st, 1, 0u, nullptr, E->hs_acc, kHsSlot, 1, nullptr);
     ens_hs_start<<<mb, 128, 0, st>>>(M, E->d_prm, E->hs_bb, E->done, E->iters);
-    int it = 0;
-    for (; it < itmax;)
-    {
-        const int batch = std::min(4, itmax - it);
-        for (int k = 0; k < batch; ++k, ++it)
+    // One iteration whose slots are it / it + 1 (it_dev: plus the device-side
+    // counter); p_it lives in pbuf[it % 2] and every iteration but the first
+    // forms it inside the apply.
+    auto iteration = [&](cudaStream_t s2, int it, const int* it_dev, bool timed) {
+        float* p_it = (it & 1) ? E->p2 : E->p;
+        const float* p_prev = (it & 1) ? E->p : E->p2;
+        double* cur = E->hs_acc + slot_len * (it + 1);
+        if (timed)
         {
-            const double* prev = E->hs_acc + static_cast<std::size_t>(kHsSlot) * M * it;
-            double* cur = E->hs_acc + static_cast<std::size_t>(kHsSlot) * M * (it + 1);
-            // Algorithmic bytes: Ap = A p with p.Ap 8 B/cell; the update 24 B/cell.
-            // p_it lives in pbuf[it % 2]; iteration it >= 1 forms it inside the apply
-            float* p_it = (it & 1) ? E->p2 : E->p;
-            const float* p_prev = (it & 1) ? E->p : E->p2;
-            const double* older = (it >= 1) ? E->hs_acc + static_cast<std::size_t>(kHsSlot) * M * (it - 1) : prev;
             // Algorithmic bytes: p 4 in (+ z 4 when fused), Ap 4 out (+ p 4 when fused).
-            LSDTT_TIMED("ens_hillslope_apply", (it ? 16.0 : 8.0) * cells, st,
-                        (ens_hs_apply<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->mask, E->dof, E->done, it ? 1 : 0, prev,
-                                                          older, E->zz, p_prev, p_it, E->Ap, E->part)));
-            reduce(1, 0u, E->done, cur, kHsSlot, 0);
-            LSDTT_TIMED("ens_hillslope_update", 24.0 * cells, st,
-                        (ens_hs_update<<<nb, 256, 0, st>>>(E->P, E->done, prev, E->invd, p_it, E->Ap, E->x, E->r,
-                                                           E->zz, cur, E->part)));
-            reduce(2, 0u, E->done, cur, kHsSlot, 1);
+            LSDTT_TIMED("ens_hillslope_apply", (it ? 16.0 : 8.0) * cells, s2,
+                        (ens_hs_apply<<<nb, 256, 0, s2>>>(E->P, E->d_prm, E->mask, E->dof, E->done, it ? 1 : 0,
+                                                          E->hs_acc, it, it >= 1 ? it - 1 : it, it_dev, E->zz, p_prev,
+                                                          p_it, E->Ap, E->part)));
         }
-        if (eager) cudaMemsetAsync(E->flags + 5, 0, sizeof(int), st);
-        ens_hs_check<<<mb, 128, 0, st>>>(M, E->d_prm, it - 1,
-                                        E->hs_acc + static_cast<std::size_t>(kHsSlot) * M * it, E->hs_bb, E->done,
-                                        E->iters, E->flags);
-        if (eager)
+        else
+            ens_hs_apply<<<nb, 256, 0, s2>>>(E->P, E->d_prm, E->mask, E->dof, E->done, it ? 1 : 0, E->hs_acc, it,
+                                             it - 1, it_dev, E->zz, p_prev, p_it, E->Ap, E->part);
+        reduce(s2, 1, 0u, E->done, cur, kHsSlot, 0, it_dev);
+        if (timed)
         {
-            cudaMemcpyAsync(E->h_flags + 5, E->flags + 5, sizeof(int), cudaMemcpyDeviceToHost, st);
-            e = cudaStreamSynchronize(st);
-            if (e != cudaSuccess) return e;
-            if (E->h_flags[5] == 0) break;
+            // Algorithmic bytes: the update 24 B/cell.
+            LSDTT_TIMED("ens_hillslope_update", 24.0 * cells, s2,
+                        (ens_hs_update<<<nb, 256, 0, s2>>>(E->P, E->done, E->hs_acc, it, it + 1, it_dev, E->invd,
+                                                           p_it, E->Ap, E->x, E->r, E->zz, E->part)));
         }
+        else
+            ens_hs_update<<<nb, 256, 0, s2>>>(E->P, E->done, E->hs_acc, it, it + 1, it_dev, E->invd, p_it, E->Ap,
+                                              E->x, E->r, E->zz, E->part);
+        reduce(s2, 2, 0u, E->done, cur, kHsSlot, 1, it_dev);
+    };
+    if (device_loop)
+    {
+        // Device-side loop: two iterations and the convergence test per trip,
+        // until no member is iterating (each member stops at its own
+        // max_iter; all of them by max_iter_all).
+        cudaMemsetAsync(E->loopc + 1, 0, sizeof(int), st);
+        cudaMemsetAsync(E->flags + 5, 0, sizeof(int), st);
+        e = capture_while(st, E->own2, [&](cudaStream_t s2, cudaGraphConditionalHandle h) {
+            iteration(s2, 0, E->loopc + 1, false);
+            iteration(s2, 1, E->loopc + 1, false);
+            ens_hs_check<<<mb, 128, 0, s2>>>(M, E->d_prm, 1, E->hs_acc + slot_len * 2, E->hs_bb, E->done, E->iters,
+                                             E->flags, E->loopc + 1);
+            ens_pcg_while<<<1, 1, 0, s2>>>(E->loopc + 1, itmax, E->flags, h);
+        });
+        if (e != cudaSuccess) return e;
     }
-    if (eager) rec->pcg_iters = it;
-    else ens_hs_overflow<<<mb, 128, 0, st>>>(M, E->done, E->flags);
+    else
+    {
+        int it = 0;
+        for (; it < itmax;)
+        {
+            const int batch = std::min(4, itmax - it);
+            for (int k = 0; k < batch; ++k, ++it) iteration(st, it, nullptr, true);
+            if (eager) cudaMemsetAsync(E->flags + 5, 0, sizeof(int), st);
+            ens_hs_check<<<mb, 128, 0, st>>>(M, E->d_prm, it - 1,
+                                            E->hs_acc + static_cast<std::size_t>(kHsSlot) * M * it, E->hs_bb,
+                                            E->done, E->iters, E->flags);
+            if (eager)
+            {
+                cudaMemcpyAsync(E->h_flags + 5, E->flags + 5, sizeof(int), cudaMemcpyDeviceToHost, st);
+                e = cudaStreamSynchronize(st);
+                if (e != cudaSuccess) return e;
+                if (E->h_flags[5] == 0) break;
+            }
+        }
+        if (eager) rec->pcg_iters = it;
+        else ens_hs_overflow<<<mb, 128, 0, st>>>(M, E->done, E->flags);
+    }
     ens_hs_finish<<<nb, 256, 0, st>>>(N, E->dof, E->zsp, E->x, E->z);
     // 5. uplift + boundary restore, statistics, flags to the host
     ens_uplift<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->mask, E->bflag, E->zf, E->z);
     ens_stats<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->mask, E->zf, E->z, E->part);
-    reduce(8, 0xf0u, nullptr, E->stats_acc, 8, 0);
+    reduce(st, 8, 0xf0u, nullptr, E->stats_acc, 8, 0, nullptr);
     cudaMemcpyAsync(E->h_stats, E->stats_acc, sizeof(double) * 8 * M, cudaMemcpyDeviceToHost, st);
     cudaMemcpyAsync(E->h_flags, E->flags, sizeof(int) * kFlags, cudaMemcpyDeviceToHost, st);
     cudaMemcpyAsync(E->h_iters, E->iters, sizeof(int) * M, cudaMemcpyDeviceToHost, st);
@@ -1633,25 +1775,42 @@ cudaError_t capture(lsdtt_gpu_ensemble* E, const StepRecord& rec, cudaStream_t s
     E->depth_cap = std::max(rec.max_depth * 2, rec.max_depth + 256) + 2;
     E->depth_cap = static_cast<int>(std::min<std::int64_t>(E->depth_cap, E->N + 1));
     E->it_cap = std::min(E->max_iter_all, std::max(8, (rec.pcg_iters + std::max(8, rec.pcg_iters / 2) + 3) / 4 * 4));
+    // A one-shot override of the caps captures the capped loops (which can
+    // overflow: the recovery path), the device-side loops otherwise.
+    const bool capped = E->ov_fill > 0 || E->ov_it > 0;
+    const bool use_while = E->use_while;
+    if (capped) E->use_while = false;
     if (E->ov_fill > 0) E->fill_cap = E->ov_fill;
     if (E->ov_it > 0) E->it_cap = E->ov_it;
     E->ov_fill = E->ov_it = 0;
     // levels of this profile above the tuned tail threshold get a launch each
     E->split = E->tail == 0 ? rec.max_depth + 1 : split_for(rec.level_size, E->tail);
     E->level_blocks = level_grid(rec.level_size, E->split, E->sweep_block, 1.5);
-    cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
-    if (e != cudaSuccess) return e;
-    StepRecord dummy;
-    cudaError_t e_run = run_step(E, st, false, &dummy);
+    cudaError_t e = cudaSuccess;
     cudaGraph_t g = nullptr;
-    e = cudaStreamEndCapture(st, &g);
-    if (e_run != cudaSuccess) e = e_run;
-    if (e == cudaSuccess) e = cudaGraphInstantiate(&E->exec, g, 0);
-    if (e != cudaSuccess)
+    for (int attempt = 0; attempt < 2; ++attempt)
     {
+        e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) return e;
+        StepRecord dummy;
+        cudaError_t e_run = run_step(E, st, false, &dummy);
+        g = nullptr;
+        e = cudaStreamEndCapture(st, &g);
+        if (e_run != cudaSuccess) e = e_run;
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&E->exec, g, 0);
+        if (e == cudaSuccess) break;
         if (g) cudaGraphDestroy(g);
-        return e;
+        g = nullptr;
+        // A driver without conditional nodes: capture the capped loops.
+        if (!E->use_while)
+        {
+            if (capped) E->use_while = use_while;
+            return e;
+        }
+        cudaGetLastError();
+        E->use_while = false;
     }
+    if (capped && e == cudaSuccess) E->use_while = use_while;
     E->graph = g;
     E->captured = true;
     ++E->info.graph_captures;
@@ -1836,6 +1995,7 @@ int lsdtt_gpu_ensemble_create(const lsdtt_gpu_member* members, int32_t n_members
     }
     E->mask = E->f->mask;  // the stack reads the engine's mask
     if (cudaStreamCreateWithFlags(&E->own, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&E->own2, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&E->ev_in, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&E->ev_out, cudaEventDisableTiming) != cudaSuccess)
     {
@@ -1889,6 +2049,7 @@ int lsdtt_gpu_ensemble_create(const lsdtt_gpu_member* members, int32_t n_members
     alloc(&E->dfc, 2);
     alloc(&E->flags, kFlags);
     alloc(&E->bar, 2);
+    alloc(&E->loopc, 2);
     alloc(&E->morder, n);
     alloc(&E->mstart, n + 2);
     alloc(&E->mmax, static_cast<std::size_t>(n_members));
