@@ -151,21 +151,6 @@ __global__ void __launch_bounds__(256) ens_fill_relax(Packed P, const EnsParams*
                     changed, din + M.tile_base, dout + M.tile_base, local % M.ntx, local / M.ntx, M.ntx, M.nty);
 }
 
-// Condition of the graph's PCG loop (a conditional WHILE node whose body is
-// two iterations and the convergence test): advance the iteration counter,
-// go on while a member is still iterating; a member still iterating at
-// itmax raises the PCG overflow flag.
-__global__ void ens_pcg_while(int* __restrict__ it_dev, int itmax, int* __restrict__ flags,
-                              cudaGraphConditionalHandle h)
-{
-    LSDTT_COUNT();
-    const int it = (*it_dev += 2);
-    const int active = flags[5];
-    flags[5] = 0;
-    if (active > 0 && it >= itmax) flags[3] = 1;
-    cudaGraphSetConditional(h, (active > 0 && it < itmax) ? 1u : 0u);
-}
-
 // Condition of the graph's fill loop (a conditional WHILE node whose body
 // is two relaxation passes): go on while the second pass changed a tile; a
 // loop that reaches max_pairs still changing raises the overflow flag.
@@ -805,11 +790,20 @@ __device__ __forceinline__ void block_partial_f(float v, bool is_max, double* __
     __syncthreads();
     if ((threadIdx.x & 31) == 0) shf[threadIdx.x >> 5] = static_cast<double>(v);
     __syncthreads();
-    if (threadIdx.x == 0)
+    if (threadIdx.x < 32)
     {
-        double t = shf[0];
-        for (int k = 1; k < static_cast<int>(blockDim.x >> 5); ++k) t = is_max ? fmax(t, shf[k]) : t + shf[k];
-        part[q * nblk + blockIdx.x] = t;
+        // the warp partials as a shuffle tree: every FP64 instruction of a
+        // warp holds this part's narrow FP64 pipe for many cycles, whatever
+        // the number of active lanes
+        const int nw = static_cast<int>(blockDim.x >> 5);
+        double t = threadIdx.x < nw ? shf[threadIdx.x] : (is_max ? -INFINITY : 0.0);
+        for (int o = 16; o > 0; o >>= 1)
+        {
+            if (o >= nw) continue;
+            const double w = __shfl_down_sync(0xffffffffu, t, o);
+            t = is_max ? fmax(t, w) : t + w;
+        }
+        if (threadIdx.x == 0) part[q * nblk + blockIdx.x] = t;
     }
 }
 
@@ -942,47 +936,28 @@ __global__ void ens_hs_start(int M, const EnsParams* __restrict__ prm, const dou
 // p.Ap. A converged member's blocks return at once.
 // Fused with the CG direction update of the previous iteration: with `fuse`,
 // p = z + beta p_src is formed on the fly at the cell and its neighbours
-// (beta = r.z / r_old.z_old of this member, once per block) and written to
+// (beta = r.z / r_old.z_old of this member) and written to
 // p_dst, the buffer the update then reads; without it p_dst already holds p.
-// The dot products of iteration slots slot_new / slot_old of acc are read
-// (slots of kHsSlot * n_members doubles); with it_dev (a device-side loop)
-// both slots move by *it_dev and the direction update is fused whenever
-// *it_dev > 0.
-__global__ void ens_hs_apply(Packed P, const EnsParams* __restrict__ prm, const std::uint8_t* __restrict__ mask,
-                             const std::uint8_t* __restrict__ dof, const int* __restrict__ done, int fuse,
-                             const double* __restrict__ acc, int slot_new, int slot_old,
-                             const int* __restrict__ it_dev, const float* __restrict__ zz,
-                             const float* __restrict__ p_src, float* __restrict__ p_dst, float* __restrict__ Ap,
-                             double* __restrict__ part)
+// beta_m holds each member's beta (ens_pcg_ratio); with it_dev (a
+// device-side loop) the direction update is fused whenever *it_dev > 0.
+template <bool kFuse>
+__device__ __forceinline__ void hs_apply_block(const Packed& P, const PackedMember& M, const EnsParams& q,
+                                               const std::uint8_t* __restrict__ mask,
+                                               const std::uint8_t* __restrict__ dof, float beta,
+                                               const float* __restrict__ zz, const float* __restrict__ p_src,
+                                               float* __restrict__ p_dst, float* __restrict__ Ap,
+                                               double* __restrict__ part)
 {
-    LSDTT_COUNT();
     const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    const int m = member_of(P, i < P.n ? i : P.n - 1);
-    if (done[m]) return;
-    const int sh = it_dev ? *it_dev : 0;
-    if (sh > 0) fuse = 1;
-    const std::int64_t slot = static_cast<std::int64_t>(kHsSlot) * P.n_members;
-    const double* rz_new = acc + slot * (slot_new + sh);
-    const double* rz_old = acc + slot * (slot_old + sh);
-    __shared__ float s_beta;
-    if (threadIdx.x == 0)
-    {
-        const double ro = fuse ? rz_old[m * kHsSlot + 1] : 0.0;
-        s_beta = (fuse && ro > 0.0) ? static_cast<float>(rz_new[m * kHsSlot + 1] / ro) : 0.0f;
-    }
-    __syncthreads();
-    const float beta = s_beta;
     // p at any cell of the packed buffer
-    auto pv = [&](std::int64_t k) { return fuse ? zz[k] + beta * p_src[k] : p_dst[k]; };
-    const PackedMember& M = P.m[m];
-    const EnsParams& q = prm[m];
+    auto pv = [&](std::int64_t k) { return kFuse ? zz[k] + beta * p_src[k] : p_dst[k]; };
     float pap = 0.0f;
     if (i < P.n)
     {
         float v = 0.0f;
         const std::uint8_t kd = dof[i];
         const float pi = pv(i);
-        if (fuse) p_dst[i] = pi;
+        if (kFuse) p_dst[i] = pi;
         if (kd == 3)
         {
             const int nc = M.nc;
@@ -1028,29 +1003,42 @@ __global__ void ens_hs_apply(Packed P, const EnsParams* __restrict__ prm, const 
     block_partial_f(pap, false, part, P.n / kPackAlign, 0);
 }
 
-// alpha = r.z / p.Ap (once per block); x += alpha p; r -= alpha Ap; z = M^-1 r;
-// block partials of r.z and r.r. Slots as in ens_hs_apply.
-__global__ void ens_hs_update(Packed P, const int* __restrict__ done, const double* __restrict__ acc, int slot_prev,
-                              int slot_cur, const int* __restrict__ it_dev, const float* __restrict__ inv_diag,
-                              const float* __restrict__ p, const float* __restrict__ Ap, float* __restrict__ x,
-                              float* __restrict__ r, float* __restrict__ zz, double* __restrict__ part)
+// Blocks are kPackAlign cells, so each lies in one member (read once per
+// block); the fused and plain bodies are separate specialisations.
+__global__ void __launch_bounds__(kPackAlign) ens_hs_apply(Packed P, const EnsParams* __restrict__ prm,
+                                                           const std::uint8_t* __restrict__ mask,
+                                                           const std::uint8_t* __restrict__ dof,
+                                                           const int* __restrict__ done, int fuse,
+                                                           const float* __restrict__ beta_m,
+                                                           const int* __restrict__ it_dev,
+                                                           const float* __restrict__ zz,
+                                                           const float* __restrict__ p_src, float* __restrict__ p_dst,
+                                                           float* __restrict__ Ap, double* __restrict__ part)
+{
+    LSDTT_COUNT();
+    const int m = P.blk_member[blockIdx.x];
+    if (done[m]) return;
+    if (it_dev && *it_dev > 0) fuse = 1;
+    const PackedMember& M = P.m[m];
+    const EnsParams& q = prm[m];
+    if (fuse)
+        hs_apply_block<true>(P, M, q, mask, dof, beta_m[m], zz, p_src, p_dst, Ap, part);
+    else
+        hs_apply_block<false>(P, M, q, mask, dof, 0.0f, zz, p_src, p_dst, Ap, part);
+}
+
+// x += alpha p; r -= alpha Ap; z = M^-1 r (alpha_m: each member's
+// r.z / p.Ap, from ens_pcg_ratio); block partials of r.z and r.r.
+__global__ void ens_hs_update(Packed P, const int* __restrict__ done, const float* __restrict__ alpha_m,
+                              const float* __restrict__ inv_diag, const float* __restrict__ p,
+                              const float* __restrict__ Ap, float* __restrict__ x, float* __restrict__ r,
+                              float* __restrict__ zz, double* __restrict__ part)
 {
     LSDTT_COUNT();
     const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    const int m = member_of(P, i < P.n ? i : P.n - 1);
+    const int m = P.blk_member[blockIdx.x];  // kPackAlign-cell blocks: one member each
     if (done[m]) return;
-    const int sh = it_dev ? *it_dev : 0;
-    const std::int64_t slot = static_cast<std::int64_t>(kHsSlot) * P.n_members;
-    const double* prev = acc + slot * (slot_prev + sh);
-    const double* cur = acc + slot * (slot_cur + sh);
-    __shared__ float s_alpha;
-    if (threadIdx.x == 0)
-    {
-        const double pap = cur[m * kHsSlot + 0];
-        s_alpha = (pap > 0.0) ? static_cast<float>(prev[m * kHsSlot + 1] / pap) : 0.0f;
-    }
-    __syncthreads();
-    const float alpha = s_alpha;
+    const float alpha = alpha_m[m];
     float rz = 0.0f, rr = 0.0f;
     if (i < P.n)
     {
@@ -1102,6 +1090,40 @@ __global__ void ens_hs_overflow(int M, const int* __restrict__ done, int* __rest
     LSDTT_COUNT();
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m < M && !done[m]) flags[3] = 1;
+}
+
+// A PCG scalar per member, out[m] = num / den in double rounded to float
+// (0 when den <= 0): alpha = r.z / p.Ap after the apply's reduction, beta =
+// r.z / r_old.z_old after the update's. num and den are entries of
+// iteration slots of acc (kHsSlot * M doubles each); with it_dev both slots
+// move by *it_dev.
+__global__ void ens_pcg_ratio(int M, const int* __restrict__ done, const double* __restrict__ acc, int slot_num,
+                              int off_num, int slot_den, int off_den, const int* __restrict__ it_dev,
+                              float* __restrict__ out)
+{
+    LSDTT_COUNT();
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= M || done[m]) return;
+    const std::int64_t sh = it_dev ? *it_dev : 0;
+    const std::int64_t slot = static_cast<std::int64_t>(kHsSlot) * M;
+    const double num = acc[slot * (slot_num + sh) + m * kHsSlot + off_num];
+    const double den = acc[slot * (slot_den + sh) + m * kHsSlot + off_den];
+    out[m] = den > 0.0 ? static_cast<float>(num / den) : 0.0f;
+}
+
+// Condition of the graph's PCG loop (a conditional WHILE node whose body is
+// two iterations and the convergence test): advance the iteration counter,
+// go on while a member is still iterating; a member still iterating at
+// itmax raises the PCG overflow flag.
+__global__ void ens_pcg_while(int* __restrict__ it_dev, int itmax, int* __restrict__ flags,
+                              cudaGraphConditionalHandle h)
+{
+    LSDTT_COUNT();
+    const int it = (*it_dev += 2);
+    const int active = flags[5];
+    flags[5] = 0;
+    if (active > 0 && it >= itmax) flags[3] = 1;
+    cudaGraphSetConditional(h, (active > 0 && it < itmax) ? 1u : 0u);
 }
 
 __global__ void ens_hs_finish(std::int64_t n, const std::uint8_t* __restrict__ dof, const float* __restrict__ zsp,
@@ -1246,6 +1268,7 @@ struct lsdtt_gpu_ensemble
     std::uint32_t* mstart = nullptr;  // [N + 2] its bucket offsets (member base + depth)
     std::uint32_t* mmax = nullptr;    // [M] deepest level of each member
     std::uint16_t* perm = nullptr;    // [M] members by decreasing cell count
+    float* pcg_scal = nullptr;        // [2M] each member's PCG alpha, then beta
     std::vector<std::uint16_t> perm_h;
     int sweep_cluster = 8;            // CTAs per member cluster (tuned: 4 or 8)
     unsigned* bar = nullptr;     // its grid barrier: {count, generation}
@@ -1272,7 +1295,7 @@ void free_ensemble(lsdtt_gpu_ensemble* E)
 {
     if (E->exec) cudaGraphExecDestroy(E->exec);
     if (E->graph) cudaGraphDestroy(E->graph);
-    void* bufs[] = {E->d_pm, E->d_prm, E->blk_member, E->tile_member, E->strip_member, E->undecided, E->bar, E->loopc, E->morder, E->mstart, E->mmax, E->perm, E->z, E->zf, E->zsp, E->zpre, E->kind, E->bflag, E->dirty, E->oflag, E->pos, E->nd, E->area, E->order, E->lstart, E->lcount,
+    void* bufs[] = {E->d_pm, E->d_prm, E->blk_member, E->tile_member, E->strip_member, E->undecided, E->bar, E->loopc, E->pcg_scal, E->morder, E->mstart, E->mmax, E->perm, E->z, E->zf, E->zsp, E->zpre, E->kind, E->bflag, E->dirty, E->oflag, E->pos, E->nd, E->area, E->order, E->lstart, E->lcount,
                     E->lfill, E->maxd, E->dof, E->invd, E->b, E->x, E->r, E->p, E->p2, E->zz, E->Ap, E->hs_bb, E->hs_acc,
                     E->done, E->iters, E->stats_acc, E->part, E->kam_tab, E->flags, E->zg, E->dfc};
     for (void* q : bufs) cudaFree(q);
@@ -1690,29 +1713,34 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
         float* p_it = (it & 1) ? E->p2 : E->p;
         const float* p_prev = (it & 1) ? E->p : E->p2;
         double* cur = E->hs_acc + slot_len * (it + 1);
+        float* alpha = E->pcg_scal;
+        float* beta = E->pcg_scal + M;
         if (timed)
         {
             // Algorithmic bytes: p 4 in (+ z 4 when fused), Ap 4 out (+ p 4 when fused).
             LSDTT_TIMED("ens_hillslope_apply", (it ? 16.0 : 8.0) * cells, s2,
-                        (ens_hs_apply<<<nb, 256, 0, s2>>>(E->P, E->d_prm, E->mask, E->dof, E->done, it ? 1 : 0,
-                                                          E->hs_acc, it, it >= 1 ? it - 1 : it, it_dev, E->zz, p_prev,
-                                                          p_it, E->Ap, E->part)));
+                        (ens_hs_apply<<<nb, 256, 0, s2>>>(E->P, E->d_prm, E->mask, E->dof, E->done, it ? 1 : 0, beta,
+                                                          it_dev, E->zz, p_prev, p_it, E->Ap, E->part)));
         }
         else
-            ens_hs_apply<<<nb, 256, 0, s2>>>(E->P, E->d_prm, E->mask, E->dof, E->done, it ? 1 : 0, E->hs_acc, it,
-                                             it - 1, it_dev, E->zz, p_prev, p_it, E->Ap, E->part);
+            ens_hs_apply<<<nb, 256, 0, s2>>>(E->P, E->d_prm, E->mask, E->dof, E->done, it ? 1 : 0, beta, it_dev,
+                                             E->zz, p_prev, p_it, E->Ap, E->part);
         reduce(s2, 1, 0u, E->done, cur, kHsSlot, 0, it_dev);
+        // alpha = r.z (slot it) / p.Ap (slot it + 1)
+        ens_pcg_ratio<<<mb, 128, 0, s2>>>(M, E->done, E->hs_acc, it, 1, it + 1, 0, it_dev, alpha);
         if (timed)
         {
             // Algorithmic bytes: the update 24 B/cell.
             LSDTT_TIMED("ens_hillslope_update", 24.0 * cells, s2,
-                        (ens_hs_update<<<nb, 256, 0, s2>>>(E->P, E->done, E->hs_acc, it, it + 1, it_dev, E->invd,
-                                                           p_it, E->Ap, E->x, E->r, E->zz, E->part)));
+                        (ens_hs_update<<<nb, 256, 0, s2>>>(E->P, E->done, alpha, E->invd, p_it, E->Ap, E->x, E->r,
+                                                           E->zz, E->part)));
         }
         else
-            ens_hs_update<<<nb, 256, 0, s2>>>(E->P, E->done, E->hs_acc, it, it + 1, it_dev, E->invd, p_it, E->Ap,
-                                              E->x, E->r, E->zz, E->part);
+            ens_hs_update<<<nb, 256, 0, s2>>>(E->P, E->done, alpha, E->invd, p_it, E->Ap, E->x, E->r, E->zz,
+                                              E->part);
         reduce(s2, 2, 0u, E->done, cur, kHsSlot, 1, it_dev);
+        // beta for the next iteration = r.z (slot it + 1) / r.z (slot it)
+        ens_pcg_ratio<<<mb, 128, 0, s2>>>(M, E->done, E->hs_acc, it + 1, 1, it, 1, it_dev, beta);
     };
     if (device_loop)
     {
@@ -2050,6 +2078,7 @@ int lsdtt_gpu_ensemble_create(const lsdtt_gpu_member* members, int32_t n_members
     alloc(&E->flags, kFlags);
     alloc(&E->bar, 2);
     alloc(&E->loopc, 2);
+    alloc(&E->pcg_scal, 2 * static_cast<std::size_t>(n_members));
     alloc(&E->morder, n);
     alloc(&E->mstart, n + 2);
     alloc(&E->mmax, static_cast<std::size_t>(n_members));
