@@ -81,6 +81,14 @@ __device__ __forceinline__ int member_of(const Packed& P, std::int64_t i)
     return P.blk_member[i / kPackAlign];
 }
 
+// The member of the whole block, for kernels launched with kPackAlign-thread
+// blocks over the packed buffer (members are kPackAlign-aligned, so such a
+// block never spans two): a block-uniform index and loads.
+__device__ __forceinline__ int block_member(const Packed& P)
+{
+    return P.blk_member[blockIdx.x];
+}
+
 // ---- fill ----------------------------------------------------------------
 __global__ void ens_interior(Packed P, const EnsParams* __restrict__ prm, const float* __restrict__ z,
                              const std::uint8_t* __restrict__ mask, int* __restrict__ nd)
@@ -88,7 +96,7 @@ __global__ void ens_interior(Packed P, const EnsParams* __restrict__ prm, const 
     LSDTT_COUNT();
     const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= P.n) return;
-    const int m = member_of(P, i);
+    const int m = block_member(P);
     const PackedMember& M = P.m[m];
     const std::int64_t local = i - M.base;
     if (local >= static_cast<std::int64_t>(M.nr) * M.nc || !prm[m].fill_on) return;
@@ -102,7 +110,7 @@ __global__ void ens_fill_init(Packed P, const EnsParams* __restrict__ prm, const
     LSDTT_COUNT();
     const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= P.n) return;
-    const int m = member_of(P, i);
+    const int m = block_member(P);
     const PackedMember& M = P.m[m];
     const EnsParams& q = prm[m];
     const std::int64_t local = i - M.base;
@@ -298,7 +306,7 @@ __global__ void ens_kam(Packed P, const EnsParams* __restrict__ prm, const std::
     bool need = false;
     if (i < P.n && mask[i] && receiver[i] >= 0)
     {
-        const int m = member_of(P, i);
+        const int m = block_member(P);
         const std::uint64_t c = size[i];
         if (c < static_cast<std::uint64_t>(kKamTab))
             kam[i] = tab[static_cast<std::int64_t>(m) * kKamTab + static_cast<std::int64_t>(c)];
@@ -807,6 +815,52 @@ __device__ __forceinline__ void block_partial_f(float v, bool is_max, double* __
     }
 }
 
+// block_partial_f for NQ quantities at once (NQ divides 32; bit q of
+// max_mask: maximum, else sum): FP32 within each warp, then warp 0 gives
+// each lane one quantity and a group of warps, sums the group in FP64 and
+// combines the groups with xor shuffles: one barrier and a handful of FP64
+// instructions per block for all NQ. Call once per kernel.
+template <int NQ>
+__device__ __forceinline__ void block_partials_f(const float (&v)[NQ], unsigned max_mask, double* __restrict__ part,
+                                                 std::int64_t nblk)
+{
+    static_assert(32 % NQ == 0, "NQ must divide the warp");
+    __shared__ float sw[32][NQ];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int nw = static_cast<int>(blockDim.x >> 5);
+#pragma unroll
+    for (int q = 0; q < NQ; ++q)
+    {
+        const bool is_max = (max_mask >> q) & 1u;
+        float x = v[q];
+        for (int o = 16; o > 0; o >>= 1)
+        {
+            const float y = __shfl_down_sync(0xffffffffu, x, o);
+            x = is_max ? fmaxf(x, y) : x + y;
+        }
+        if (lane == 0) sw[wid][q] = x;
+    }
+    __syncthreads();
+    if (wid == 0)
+    {
+        constexpr int G = 32 / NQ;
+        const int q = lane % NQ, g = lane / NQ;
+        const bool is_max = (max_mask >> q) & 1u;
+        double t = is_max ? -INFINITY : 0.0;
+        for (int k = g; k < nw; k += G)
+        {
+            const double x = static_cast<double>(sw[k][q]);
+            t = is_max ? fmax(t, x) : t + x;
+        }
+        for (int o = NQ; o < 32; o <<= 1)
+        {
+            const double y = __shfl_xor_sync(0xffffffffu, t, o);
+            t = is_max ? fmax(t, y) : t + y;
+        }
+        if (g == 0) part[q * nblk + blockIdx.x] = t;
+    }
+}
+
 // dst[m * stride + off + q] = reduction of member m's block partials of
 // quantity q (bit q of max_mask: maximum, else sum); one warp per (m, q).
 // Members with done[m] set are skipped. With shift, dst moves by
@@ -850,7 +904,7 @@ __global__ void ens_hs_setup(Packed P, const EnsParams* __restrict__ prm, const 
 {
     LSDTT_COUNT();
     const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    const int m = member_of(P, i < P.n ? i : P.n - 1);
+    const int m = block_member(P);
     const PackedMember& M = P.m[m];
     const EnsParams& q = prm[m];
     const Hs& H = q.hs;
@@ -1050,8 +1104,8 @@ __global__ void ens_hs_update(Packed P, const int* __restrict__ done, const floa
         rz = ri * zi;
         rr = ri * ri;
     }
-    block_partial_f(rz, false, part, P.n / kPackAlign, 0);
-    block_partial_f(rr, false, part, P.n / kPackAlign, 1);
+    const float rv[2] = {rz, rr};
+    block_partials_f<2>(rv, 0u, part, P.n / kPackAlign);
 }
 
 // After iteration `it` (0-based, it + 1 a multiple of 4 or the last one):
@@ -1141,7 +1195,7 @@ __global__ void ens_boundary_flag(Packed P, const std::uint8_t* __restrict__ mas
     LSDTT_COUNT();
     const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= P.n) return;
-    const PackedMember& M = P.m[member_of(P, i)];
+    const PackedMember& M = P.m[block_member(P)];
     const std::int64_t local = i - M.base;
     flag[i] = (local < static_cast<std::int64_t>(M.nr) * M.nc &&
                boundary_flat_cell(M.nr, M.nc, M.bc, mask + M.base, local))
@@ -1156,7 +1210,7 @@ __global__ void ens_uplift(Packed P, const EnsParams* __restrict__ prm, const st
     LSDTT_COUNT();
     const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= P.n) return;
-    const EnsParams& q = prm[member_of(P, i)];
+    const EnsParams& q = prm[block_member(P)];
     float v = z[i];
     if (mask[i]) v = __fadd_rn(v, q.udz);
     if (bflag[i]) v = __fsub_rn(z_before[i], q.bl);
@@ -1172,7 +1226,7 @@ __global__ void ens_stats(Packed P, const EnsParams* __restrict__ prm, const std
 {
     LSDTT_COUNT();
     const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    const int m = member_of(P, i < P.n ? i : P.n - 1);
+    const int m = P.blk_member[blockIdx.x];  // kPackAlign-cell blocks: one member each
     float v[8] = {0.0f, 0.0f, 0.0f, 0.0f, -1e30f, -1e30f, 0.0f, 0.0f};
     if (i < P.n && mask[i])
     {
@@ -1185,9 +1239,7 @@ __global__ void ens_stats(Packed P, const EnsParams* __restrict__ prm, const std
         if (ero > 0.0f) { v[2] = ero; v[7] = ero; }
         v[3] = 1.0f;
     }
-    const std::int64_t nblk = P.n / kPackAlign;
-#pragma unroll
-    for (int q = 0; q < 8; ++q) block_partial_f(v[q], q >= 4, part, nblk, q);
+    block_partials_f<8>(v, 0xf0u, part, P.n / kPackAlign);
 }
 
 bool exact_area(double dw, std::int64_t nv)
