@@ -191,20 +191,31 @@ __global__ void ruler_flags(RankLevel L, std::uint8_t* __restrict__ flag)
     flag[v] = (node_valid(L, v) && (is_ruler(v) || v == *L.head)) ? 1 : 0;
 }
 
+// Per tour node of a ranking level: the ruler whose walk reached it and the
+// two prefixes from that ruler, one 16-byte record (a walk step writes one
+// sector, not three).
+struct alignas(16) RankRec
+{
+    std::uint32_t owner;
+    std::int32_t loc0, loc1, pad;
+};
+
 __global__ void ruler_scatter(const std::uint8_t* __restrict__ flag, const std::uint32_t* __restrict__ pos,
                               std::uint32_t n, std::uint32_t cap, std::uint32_t* __restrict__ rulers,
-                              std::uint32_t* __restrict__ owner)
+                              RankRec* __restrict__ rec)
 {
     LSDTT_COUNT();
     const std::uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= n || !flag[v] || pos[v] >= cap) return;  // overflow is reported by ruler_cap_check
     rulers[pos[v]] = v;
-    owner[v] = pos[v];
+    rec[v].owner = pos[v];
 }
 
-__global__ void ruler_walk(RankLevel L, const std::uint8_t* __restrict__ flag, const std::uint32_t* __restrict__ rulers,
-                           const std::uint32_t* __restrict__ n_rulers, std::uint32_t* __restrict__ owner,
-                           std::int32_t* __restrict__ loc0, std::int32_t* __restrict__ loc1,
+// A walk from ruler i to the next ruler. A node of the list is a ruler iff
+// is_ruler(v) or it is the head (ruler_flags), so the stop test needs no
+// load.
+__global__ void ruler_walk(RankLevel L, const std::uint32_t* __restrict__ rulers,
+                           const std::uint32_t* __restrict__ n_rulers, RankRec* __restrict__ rec,
                            std::int32_t* __restrict__ sub0, std::int32_t* __restrict__ sub1,
                            std::uint32_t* __restrict__ nxt, std::uint32_t* __restrict__ next_head,
                            std::uint32_t cap, unsigned long long* __restrict__ err)
@@ -213,26 +224,25 @@ __global__ void ruler_walk(RankLevel L, const std::uint8_t* __restrict__ flag, c
     const std::uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const std::uint32_t nr = *n_rulers;
     if (i >= nr || i >= cap) return;
+    const std::uint32_t head = *L.head;
     std::uint32_t v = rulers[i];
-    if (v == *L.head) *next_head = i;
+    if (v == head) *next_head = i;
     int a0 = 0, a1 = 0;
     std::uint32_t steps = 0;
     do
     {
-        owner[v] = i;
-        loc0[v] = a0;
-        loc1[v] = a1;
+        rec[v] = RankRec{i, a0, a1, 0};
         int w0, w1;
         weights(L, v, w0, w1);
         a0 += w0;
         a1 += w1;
         v = L.succ[v];
         ++steps;
-    } while (v != kEnd && !flag[v] && steps <= L.n);
+    } while (v != kEnd && !is_ruler(v) && v != head && steps <= L.n);
     if (steps > L.n) raise_error(err, kErrCycle, 0);
     sub0[i] = a0;
     sub1[i] = a1;
-    nxt[i] = (v == kEnd) ? kEnd : owner[v];
+    nxt[i] = (v == kEnd) ? kEnd : rec[v].owner;
 }
 
 __global__ void serial_rank(RankLevel L, std::int32_t* __restrict__ p0, std::int32_t* __restrict__ p1,
@@ -257,15 +267,15 @@ __global__ void serial_rank(RankLevel L, std::int32_t* __restrict__ p0, std::int
     if (steps > L.n) raise_error(err, kErrCycle, 1);
 }
 
-__global__ void rank_finish(RankLevel L, const std::uint32_t* __restrict__ owner, const std::int32_t* __restrict__ loc0,
-                            const std::int32_t* __restrict__ loc1, const std::int32_t* __restrict__ P0,
+__global__ void rank_finish(RankLevel L, const RankRec* __restrict__ rec, const std::int32_t* __restrict__ P0,
                             const std::int32_t* __restrict__ P1, std::uint32_t cap, std::int32_t* __restrict__ p0,
                             std::int32_t* __restrict__ p1, unsigned long long* __restrict__ err)
 {
     LSDTT_COUNT();
     const std::uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= L.n || !node_valid(L, v)) return;
-    const std::uint32_t o = owner[v];
+    const RankRec r = rec[v];
+    const std::uint32_t o = r.owner;
     if (o >= cap)
     {
         // Not reached by any walk: the tour does not cover every valid node.
@@ -274,15 +284,8 @@ __global__ void rank_finish(RankLevel L, const std::uint32_t* __restrict__ owner
         p1[v] = 0;
         return;
     }
-    p0[v] = P0[o] + loc0[v];
-    p1[v] = P1[o] + loc1[v];
-}
-
-__global__ void fill_u32(std::uint32_t* __restrict__ a, std::uint32_t n, std::uint32_t v)
-{
-    LSDTT_COUNT();
-    const std::uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) a[i] = v;
+    p0[v] = P0[o] + r.loc0;
+    p1[v] = P1[o] + r.loc1;
 }
 
 __global__ void ruler_cap_check(const std::uint32_t* cnt, std::uint32_t cap, unsigned long long* err)
@@ -306,12 +309,10 @@ cudaError_t rank_list(const RankLevel& L, std::int32_t* p0, std::int32_t* p1, Sc
     std::uint8_t* flag = ws.take<std::uint8_t>(L.n);
     std::uint32_t* pos = ws.take<std::uint32_t>(L.n);
     std::uint32_t* cnt = ws.take<std::uint32_t>(2);
-    std::uint32_t* owner = ws.take<std::uint32_t>(L.n);
-    std::int32_t* loc0 = ws.take<std::int32_t>(L.n);
-    std::int32_t* loc1 = ws.take<std::int32_t>(L.n);
-    if (!flag || !pos || !cnt || !owner || !loc0 || !loc1) return cudaErrorMemoryAllocation;
+    RankRec* rec = ws.take<RankRec>(L.n);
+    if (!flag || !pos || !cnt || !rec) return cudaErrorMemoryAllocation;
     const unsigned nb = grid_blocks(L.n, 256);
-    fill_u32<<<nb, 256, 0, st>>>(owner, L.n, kNone);
+    cudaMemsetAsync(rec, 0xff, sizeof(RankRec) * L.n, st);  // owner kNone: reached by no walk
     ruler_flags<<<nb, 256, 0, st>>>(L, flag);
     cudaError_t e = exclusive_scan<std::uint8_t, std::uint32_t>(flag, L.n, pos, cnt, ws, st);
     if (e != cudaSuccess) return e;
@@ -325,16 +326,16 @@ cudaError_t rank_list(const RankLevel& L, std::int32_t* p0, std::int32_t* p1, Sc
     std::int32_t* P1 = ws.take<std::int32_t>(cap);
     std::uint32_t* nhead = cnt + 1;
     if (!rulers || !nxt || !sub0 || !sub1 || !P0 || !P1) return cudaErrorMemoryAllocation;
-    ruler_scatter<<<nb, 256, 0, st>>>(flag, pos, L.n, cap, rulers, owner);
+    ruler_scatter<<<nb, 256, 0, st>>>(flag, pos, L.n, cap, rulers, rec);
     ruler_cap_check<<<1, 1, 0, st>>>(cnt, cap, err);
-    // Bytes touched per tour node: successor 4 + ruler flag 1 in, owner 4 + two prefixes 8 out.
-    LSDTT_TIMED("stack_ruler_walk", 17.0 * static_cast<double>(L.n), st,
-                (ruler_walk<<<grid_blocks(cap, 128), 128, 0, st>>>(L, flag, rulers, cnt, owner, loc0, loc1, sub0, sub1,
-                                                                   nxt, nhead, cap, err)));
+    // Bytes touched per tour node: successor 4 in, the 16-byte record out.
+    LSDTT_TIMED("stack_ruler_walk", 20.0 * static_cast<double>(L.n), st,
+                (ruler_walk<<<grid_blocks(cap, 128), 128, 0, st>>>(L, rulers, cnt, rec, sub0, sub1, nxt, nhead, cap,
+                                                                   err)));
     RankLevel up{cap, nxt, sub0, sub1, nullptr, nhead, cnt};
     e = rank_list(up, P0, P1, ws, err, st);
     if (e != cudaSuccess) return e;
-    rank_finish<<<nb, 256, 0, st>>>(L, owner, loc0, loc1, P0, P1, cap, p0, p1, err);
+    rank_finish<<<nb, 256, 0, st>>>(L, rec, P0, P1, cap, p0, p1, err);
     ws.used = mark;
     return cudaGetLastError();
 }
