@@ -110,84 +110,99 @@ __device__ __forceinline__ void fill_relax_tile(int nr, int nc, bool per_ns, boo
             return;
         }
     }
+    // Staged tile: filled values with +inf at invalid and off-grid cells (so
+    // they never win a minimum) and the elevations.
     __shared__ float sF[kH][kH];
     __shared__ float sz[kH][kH];
-    __shared__ std::uint8_t sk[kH][kH];
-    __shared__ int any;
     const int r0 = ty * kT - 1, c0 = tx * kT - 1;
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    const int lc = threadIdx.x + 1;
+    unsigned free_mask = 0;  // bit q: this thread's cell of row-step q is free (kind 1)
     for (int k = tid; k < kH * kH; k += blockDim.x * blockDim.y)
     {
-        const int lr = k / kH, lc = k % kH;
-        int r = r0 + lr, c = c0 + lc;
+        const int lr = k / kH, lcc = k % kH;
+        int r = r0 + lr, c = c0 + lcc;
         if (per_ns) { if (r < 0) r += nr; else if (r >= nr) r -= nr; }
         if (per_ew) { if (c < 0) c += nc; else if (c >= nc) c -= nc; }
+        float f = INFINITY, zz = INFINITY;
         if (r >= 0 && r < nr && c >= 0 && c < nc)
         {
             const std::int64_t g = static_cast<std::int64_t>(r) * nc + c;
-            sF[lr][lc] = F[g];
-            sz[lr][lc] = z[g];
-            sk[lr][lc] = kind[g];
+            const std::uint8_t kd = kind[g];
+            zz = z[g];
+            if (kd != 0) f = F[g];
         }
-        else
-        {
-            sF[lr][lc] = INFINITY;
-            sz[lr][lc] = INFINITY;
-            sk[lr][lc] = 0;
-        }
-    }
-    if (tid == 0) any = 0;
-    __syncthreads();
-    // Interior cells of this tile owned by this thread: 32 columns x 4 rows.
-    const int lc = threadIdx.x + 1;
-    bool tile_changed = false;
-    for (int it = 0; it < kMaxLocal; ++it)
-    {
-        bool local = false;
-#pragma unroll
-        for (int q = 0; q < kT / 8; ++q)
-        {
-            const int lr = threadIdx.y * (kT / 8) + q + 1;
-            const int r = r0 + lr, c = c0 + lc;
-            if (r >= nr || c >= nc || sk[lr][lc] != 1) continue;
-            float m = INFINITY;
-            int md = -1;
-#pragma unroll
-            // The halo load already resolved every neighbour: periodic axes
-            // are wrapped into the tile and off-grid positions hold kind 0.
-            for (int d = 0; d < 8; ++d)
-            {
-                const int ar = lr + d8_dr(d), ac = lc + d8_dc(d);
-                if (sk[ar][ac] == 0) continue;
-                const float v = sF[ar][ac];
-                if (v < m) { m = v; md = d; }
-            }
-            if (md < 0) continue;
-            const float zc = sz[lr][lc];
-            const float nv = (zc > m) ? zc : raise_from(m, min_slope, (md & 1) ? Ld : L);
-            if (nv < sF[lr][lc])
-            {
-                sF[lr][lc] = nv;
-                local = true;
-            }
-        }
-        __syncthreads();
-        if (local) any = 1;
-        __syncthreads();
-        const int a = any;
-        __syncthreads();
-        if (!a) break;
-        tile_changed = true;
-        if (tid == 0) any = 0;
-        __syncthreads();
+        sF[lr][lcc] = f;
+        sz[lr][lcc] = zz;
     }
 #pragma unroll
     for (int q = 0; q < kT / 8; ++q)
     {
         const int lr = threadIdx.y * (kT / 8) + q + 1;
         const int r = r0 + lr, c = c0 + lc;
-        if (r >= nr || c >= nc || sk[lr][lc] != 1) continue;
-        const std::int64_t g = static_cast<std::int64_t>(r) * nc + c;
+        if (r < nr && c < nc && kind[static_cast<std::int64_t>(r) * nc + c] == 1) free_mask |= 1u << q;
+    }
+    __syncthreads();
+    // Interior cells of this tile owned by this thread: 32 columns x 4 rows.
+    // Each local iteration updates the four colours of the 2 x 2 colouring
+    // (row parity, column parity) in turn, a barrier between them: cells of
+    // one colour are never neighbours, so every update reads settled values
+    // and the result depends only on the tile's inputs (the discoverer rule
+    // is not monotone, so in-place updates racing with their neighbours'
+    // reads could settle on different values run to run).
+    bool tile_changed = false;
+    const unsigned col_par = static_cast<unsigned>(lc & 1);
+    for (int it = 0; it < kMaxLocal; ++it)
+    {
+        bool local = false;
+#pragma unroll
+        for (int colour = 0; colour < 4; ++colour)
+        {
+#pragma unroll
+        for (int q = 0; q < kT / 8; ++q)
+        {
+            const int lr = threadIdx.y * (kT / 8) + q + 1;
+            if (static_cast<unsigned>(colour & 1) != col_par ||
+                static_cast<unsigned>((colour >> 1) & 1) != static_cast<unsigned>(lr & 1))
+                continue;
+            if (!((free_mask >> q) & 1u)) continue;
+            const float vN = sF[lr - 1][lc], vNE = sF[lr - 1][lc + 1], vE = sF[lr][lc + 1];
+            const float vSE = sF[lr + 1][lc + 1], vS = sF[lr + 1][lc], vSW = sF[lr + 1][lc - 1];
+            const float vW = sF[lr][lc - 1], vNW = sF[lr - 1][lc - 1];
+            // lowest neighbour; +inf: none reached yet (or none valid)
+            const float cmin = fminf(fminf(vN, vE), fminf(vS, vW));
+            const float dmin = fminf(fminf(vNE, vSE), fminf(vSW, vNW));
+            const float m = fminf(cmin, dmin);
+            if (!(m < INFINITY)) continue;
+            const float zc = sz[lr][lc];
+            float nv = zc;
+            if (!(zc > m))
+            {
+                // the first neighbour in direction order N, NE, ..., NW at m
+                // decides the step length
+                bool diag = dmin < cmin;
+                if (cmin == dmin)
+                    diag = !(vN == m) && ((vNE == m) || (!(vE == m) && ((vSE == m) ||
+                                            (!(vS == m) && ((vSW == m) || (!(vW == m)))))));
+                nv = raise_from(m, min_slope, diag ? Ld : L);
+            }
+            if (nv < sF[lr][lc])
+            {
+                sF[lr][lc] = nv;
+                local = true;
+            }
+        }
+        if (colour < 3) __syncthreads();
+        }
+        if (!__syncthreads_or(local)) break;
+        tile_changed = true;
+    }
+#pragma unroll
+    for (int q = 0; q < kT / 8; ++q)
+    {
+        if (!((free_mask >> q) & 1u)) continue;
+        const int lr = threadIdx.y * (kT / 8) + q + 1;
+        const std::int64_t g = static_cast<std::int64_t>(r0 + lr) * nc + (c0 + lc);
         if (sF[lr][lc] < F[g]) F[g] = sF[lr][lc];
     }
     if (tid == 0)
