@@ -167,7 +167,7 @@ cudaError_t launch_receivers(lsdtt_gpu_flow* f, const float* z, const std::uint8
                     f->g, z, mask, forced_plane, interior_nodata_is_outlet, allow_pits_as_outlets, inv_card, inv_diag,
                     f->receiver, f->dir, f->dundec)));
     const std::int64_t P = d8_perimeter(f->g.nr, f->g.nc);
-    const unsigned fix_blocks = static_cast<unsigned>(std::min<std::int64_t>((P + 255) / 256 + 152, 152 * 4));
+    const unsigned fix_blocks = static_cast<unsigned>(std::max<std::int64_t>((P + 255) / 256, 152 * 4));
     receivers_fixup<<<fix_blocks, 256, 0, st>>>(f->g, z, mask, forced_plane, interior_nodata_is_outlet,
                                                 allow_pits_as_outlets, inv_card, inv_diag, f->receiver, f->dir,
                                                 f->derr, f->dundec);

@@ -1545,7 +1545,8 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
     LSDTT_TIMED("ens_d8_receivers", 14.0 * cells, st,
                 (ens_receivers<<<E->S, 256, 0, st>>>(E->P, E->d_prm, E->strip_member, E->zf, E->mask, f->receiver,
                                                      f->dir, E->undecided)));
-    ens_receivers_fixup<<<static_cast<unsigned>(std::min<std::int64_t>((E->perim + 255) / 256 + 152, 152 * 4)), 256, 0,
+    // one thread per perimeter cell (each looks its member up by a binary search)
+    ens_receivers_fixup<<<static_cast<unsigned>(std::max<std::int64_t>((E->perim + 255) / 256, 152 * 4)), 256, 0,
                           st>>>(E->P, E->d_prm, E->perim, E->zf, E->mask, f->receiver, f->dir, f->derr,
                                 E->undecided);
     ens_outlet_flag<<<nb, 256, 0, st>>>(N, E->mask, f->dir, E->oflag);

@@ -116,8 +116,10 @@ __device__ __forceinline__ void fill_relax_tile(int nr, int nc, bool per_ns, boo
     __shared__ float sz[kH][kH];
     const int r0 = ty * kT - 1, c0 = tx * kT - 1;
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
-    const int lc = threadIdx.x + 1;
-    unsigned free_mask = 0;  // bit q: this thread's cell of row-step q is free (kind 1)
+    // Each thread owns one 2 x 2 block of the tile: local rows 2*by+1 .. +2,
+    // columns 2*bx+1 .. +2, so it holds one cell of each colour.
+    const int bx = tid & 15, by = tid >> 4;
+    unsigned free_mask = 0;  // bit k: this thread's cell of colour k is free (kind 1)
     for (int k = tid; k < kH * kH; k += blockDim.x * blockDim.y)
     {
         const int lr = k / kH, lcc = k % kH;
@@ -136,72 +138,67 @@ __device__ __forceinline__ void fill_relax_tile(int nr, int nc, bool per_ns, boo
         sz[lr][lcc] = zz;
     }
 #pragma unroll
-    for (int q = 0; q < kT / 8; ++q)
+    for (int k = 0; k < 4; ++k)
     {
-        const int lr = threadIdx.y * (kT / 8) + q + 1;
+        const int lr = 2 * by + 1 + (k >> 1), lc = 2 * bx + 1 + (k & 1);
         const int r = r0 + lr, c = c0 + lc;
-        if (r < nr && c < nc && kind[static_cast<std::int64_t>(r) * nc + c] == 1) free_mask |= 1u << q;
+        if (r < nr && c < nc && kind[static_cast<std::int64_t>(r) * nc + c] == 1) free_mask |= 1u << k;
     }
     __syncthreads();
-    // Interior cells of this tile owned by this thread: 32 columns x 4 rows.
     // Each local iteration updates the four colours of the 2 x 2 colouring
-    // (row parity, column parity) in turn, a barrier between them: cells of
-    // one colour are never neighbours, so every update reads settled values
-    // and the result depends only on the tile's inputs (the discoverer rule
-    // is not monotone, so in-place updates racing with their neighbours'
-    // reads could settle on different values run to run).
+    // (local row parity, column parity) in turn, a barrier between them:
+    // cells of one colour are never neighbours, so every update reads
+    // settled values and the result depends only on the tile's inputs (the
+    // discoverer rule is not monotone, so in-place updates racing with their
+    // neighbours' reads could settle on different values run to run).
     bool tile_changed = false;
-    const unsigned col_par = static_cast<unsigned>(lc & 1);
     for (int it = 0; it < kMaxLocal; ++it)
     {
         bool local = false;
 #pragma unroll
-        for (int colour = 0; colour < 4; ++colour)
+        for (int k = 0; k < 4; ++k)
         {
-#pragma unroll
-        for (int q = 0; q < kT / 8; ++q)
-        {
-            const int lr = threadIdx.y * (kT / 8) + q + 1;
-            if (static_cast<unsigned>(colour & 1) != col_par ||
-                static_cast<unsigned>((colour >> 1) & 1) != static_cast<unsigned>(lr & 1))
-                continue;
-            if (!((free_mask >> q) & 1u)) continue;
-            const float vN = sF[lr - 1][lc], vNE = sF[lr - 1][lc + 1], vE = sF[lr][lc + 1];
-            const float vSE = sF[lr + 1][lc + 1], vS = sF[lr + 1][lc], vSW = sF[lr + 1][lc - 1];
-            const float vW = sF[lr][lc - 1], vNW = sF[lr - 1][lc - 1];
-            // lowest neighbour; +inf: none reached yet (or none valid)
-            const float cmin = fminf(fminf(vN, vE), fminf(vS, vW));
-            const float dmin = fminf(fminf(vNE, vSE), fminf(vSW, vNW));
-            const float m = fminf(cmin, dmin);
-            if (!(m < INFINITY)) continue;
-            const float zc = sz[lr][lc];
-            float nv = zc;
-            if (!(zc > m))
+            const int lr = 2 * by + 1 + (k >> 1), lc = 2 * bx + 1 + (k & 1);
+            if ((free_mask >> k) & 1u)
             {
-                // the first neighbour in direction order N, NE, ..., NW at m
-                // decides the step length
-                bool diag = dmin < cmin;
-                if (cmin == dmin)
-                    diag = !(vN == m) && ((vNE == m) || (!(vE == m) && ((vSE == m) ||
-                                            (!(vS == m) && ((vSW == m) || (!(vW == m)))))));
-                nv = raise_from(m, min_slope, diag ? Ld : L);
+                const float vN = sF[lr - 1][lc], vNE = sF[lr - 1][lc + 1], vE = sF[lr][lc + 1];
+                const float vSE = sF[lr + 1][lc + 1], vS = sF[lr + 1][lc], vSW = sF[lr + 1][lc - 1];
+                const float vW = sF[lr][lc - 1], vNW = sF[lr - 1][lc - 1];
+                // lowest neighbour; +inf: none reached yet (or none valid)
+                const float cmin = fminf(fminf(vN, vE), fminf(vS, vW));
+                const float dmin = fminf(fminf(vNE, vSE), fminf(vSW, vNW));
+                const float m = fminf(cmin, dmin);
+                if (m < INFINITY)
+                {
+                    const float zc = sz[lr][lc];
+                    float nv = zc;
+                    if (!(zc > m))
+                    {
+                        // the first neighbour in direction order N, NE, ...,
+                        // NW at m decides the step length
+                        bool diag = dmin < cmin;
+                        if (cmin == dmin)
+                            diag = !(vN == m) && ((vNE == m) || (!(vE == m) && ((vSE == m) ||
+                                                    (!(vS == m) && ((vSW == m) || (!(vW == m)))))));
+                        nv = raise_from(m, min_slope, diag ? Ld : L);
+                    }
+                    if (nv < sF[lr][lc])
+                    {
+                        sF[lr][lc] = nv;
+                        local = true;
+                    }
+                }
             }
-            if (nv < sF[lr][lc])
-            {
-                sF[lr][lc] = nv;
-                local = true;
-            }
-        }
-        if (colour < 3) __syncthreads();
+            if (k < 3) __syncthreads();
         }
         if (!__syncthreads_or(local)) break;
         tile_changed = true;
     }
 #pragma unroll
-    for (int q = 0; q < kT / 8; ++q)
+    for (int k = 0; k < 4; ++k)
     {
-        if (!((free_mask >> q) & 1u)) continue;
-        const int lr = threadIdx.y * (kT / 8) + q + 1;
+        if (!((free_mask >> k) & 1u)) continue;
+        const int lr = 2 * by + 1 + (k >> 1), lc = 2 * bx + 1 + (k & 1);
         const std::int64_t g = static_cast<std::int64_t>(r0 + lr) * nc + (c0 + lc);
         if (sF[lr][lc] < F[g]) F[g] = sF[lr][lc];
     }
