@@ -627,11 +627,11 @@ __device__ __forceinline__ void sweep_solve(const SweepArgs& A, const SpParams& 
 // SMs (the FP64 Newton work of a large member is not confined to one SM), and
 // a level costs a cluster barrier instead of a launch or a grid barrier. Only
 // the receiver's new elevation depends on the previous level: each thread
-// fetches its first node of level k+1 (order, receiver, K*A^m, old
+// fetches its first two nodes of level k+1 (order, receiver, K*A^m, old
 // elevation, direction) between its arrival at the cluster barrier and its
-// wait there, so a level's critical path is one L2 load, the solve and the
-// barrier.
-__global__ void __launch_bounds__(kSweepClusterBlock) ens_sp_clusters(SweepArgs A,
+// wait there, so a level up to twice the cluster's width costs one L2 load,
+// the solves and the barrier.
+__global__ void __launch_bounds__(kSweepClusterBlock, 4) ens_sp_clusters(SweepArgs A,
                                                                       const std::uint16_t* __restrict__ perm,
                                                                       const std::uint32_t* __restrict__ mmax)
 {
@@ -647,19 +647,23 @@ __global__ void __launch_bounds__(kSweepClusterBlock) ens_sp_clusters(SweepArgs 
     // every CTA of the cluster is running before any arrives at its barrier
     cluster.sync();
     std::uint32_t lo = A.start[base + 1], hi = A.start[base + 2];
-    SweepNode cur = sweep_fetch(A, lo + off, hi);
+    SweepNode cur0 = sweep_fetch(A, lo + off, hi), cur1 = sweep_fetch(A, lo + off + stride, hi);
     std::uint32_t nhi = kmax > 1 ? A.start[base + 3] : hi;  // end of level 2
     for (std::uint32_t k = 1; k <= kmax; ++k)
     {
-        sweep_solve(A, sp, cur);
-        for (std::uint32_t j = lo + off + stride; j < hi; j += stride) sweep_solve(A, sp, sweep_fetch(A, j, hi));
+        // this thread's first two nodes of the level (independent solves),
+        // then any further ones (levels wider than twice the cluster)
+        sweep_solve(A, sp, cur0);
+        sweep_solve(A, sp, cur1);
+        for (std::uint32_t j = lo + off + 2 * stride; j < hi; j += stride) sweep_solve(A, sp, sweep_fetch(A, j, hi));
         // Arrive (release: this level's elevations), then fetch the next
         // level's independent data while the cluster catches up, then wait
         // (acquire) before any receiver elevation of it is read.
         __syncwarp();  // the .aligned barrier wants converged warps
         asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory");
         const std::uint32_t nlo = hi;
-        cur = sweep_fetch(A, nlo + off, nhi);
+        cur0 = sweep_fetch(A, nlo + off, nhi);
+        cur1 = sweep_fetch(A, nlo + off + stride, nhi);
         const std::uint32_t nnhi = k + 1 < kmax ? A.start[base + k + 3] : nhi;
         asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
         lo = nlo;
