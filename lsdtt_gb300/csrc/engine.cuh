@@ -64,10 +64,10 @@ struct PackedMember
     double cell;
     double nodata;
     char bc[4];
-    std::int32_t tile_base;  // first 32x32 fill tile of this member
+    std::int32_t tile_base;  // first fill tile (kT x kT) of this member
     std::int32_t ntx, nty;   // fill tiles across, down
     std::int32_t rtile_base;  // first 128 x 32 receiver tile of this member
-    std::int32_t nrx;         // receiver tiles across (x nty down)
+    std::int32_t nrx, nry;    // receiver tiles across, down
     std::int64_t perim_base;  // first perimeter cell of this member in the fixup numbering
 };
 

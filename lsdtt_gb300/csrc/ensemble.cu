@@ -4,7 +4,7 @@
 // Layout. Member k owns packed cells [base_k, base_k + nr_k*nc_k) in its own
 // row-major order; bases are multiples of kPackAlign (256), so a 256-thread
 // block belongs to exactly one member and finds it in blk_member. Fill tiles
-// (32 x 32) are numbered member by member (tile_member). Receivers, outlets,
+// (kT x kT) are numbered member by member (tile_member). Receivers, outlets,
 // the Euler tour and the stream-power level order use packed indices, so the
 // members' receiver forests form one forest and the stack code runs on it
 // unchanged.
@@ -1990,12 +1990,13 @@ int lsdtt_gpu_ensemble_create(const lsdtt_gpu_member* members, int32_t n_members
         P.nodata = g.no_data_value;
         std::memcpy(P.bc, g.boundary_conditions, 4);
         P.tile_base = tiles;
-        P.ntx = (g.n_cols + 31) / 32;
-        P.nty = (g.n_rows + 31) / 32;
+        P.ntx = (g.n_cols + kT - 1) / kT;
+        P.nty = (g.n_rows + kT - 1) / kT;
         tiles += P.ntx * P.nty;
         P.rtile_base = strips;
         P.nrx = (g.n_cols + kD8TileCols - 1) / kD8TileCols;
-        strips += P.nrx * P.nty;
+        P.nry = (g.n_rows + kD8TileRows - 1) / kD8TileRows;
+        strips += P.nrx * P.nry;
         P.perim_base = perim;
         perim += d8_perimeter(g.n_rows, g.n_cols);
         base += (n + kPackAlign - 1) / kPackAlign * kPackAlign;
@@ -2063,7 +2064,7 @@ int lsdtt_gpu_ensemble_create(const lsdtt_gpu_member* members, int32_t n_members
         const std::int64_t nblk = (n + kPackAlign - 1) / kPackAlign;
         for (std::int64_t b = 0; b < nblk; ++b) blk[static_cast<std::size_t>(P.base / kPackAlign + b)] = k;
         for (int t = 0; t < P.ntx * P.nty; ++t) tm[static_cast<std::size_t>(P.tile_base + t)] = k;
-        for (int t = 0; t < P.nrx * P.nty; ++t) sm[static_cast<std::size_t>(P.rtile_base + t)] = k;
+        for (int t = 0; t < P.nrx * P.nry; ++t) sm[static_cast<std::size_t>(P.rtile_base + t)] = k;
     }
     // The stack runs on the packed forest: one flow engine over N cells.
     lsdtt_gpu_grid fg{};

@@ -15,7 +15,7 @@
 //     F(c) = z(c)                        if z(c) > m(c)
 //          = raise(m(c), dir of m(c))    otherwise,   m(c) = min_nb F(nb)
 // with seeds fixed at their elevation. It is solved by tile-local relaxation
-// in shared memory (each CTA iterates its 32x32 tile to local convergence),
+// in shared memory (each CTA iterates its kT x kT tile to local convergence),
 // repeated until no tile changes. The set of raised cells and every cell
 // outside a depression match the reference exactly; inside large flats the
 // reference's FIFO processes cells in breadth-first push order rather than

@@ -13,9 +13,11 @@ namespace lsdtt_gb300
 namespace
 {
 
-constexpr int kT = 32;        // tile edge (cells)
-constexpr int kH = kT + 2;    // with halo
+constexpr int kT = 32;                                   // tile edge (cells)
+constexpr int kH = kT + 2;                               // with halo
 constexpr int kMaxLocal = 4 * kT;
+constexpr int kFillThreads = 256;                        // threads per tile (32 x 8 block)
+constexpr int kFillBlocks = (kT / 2) * (kT / 2) / kFillThreads;  // 2 x 2 blocks per thread
 
 __device__ __forceinline__ float raise_from(float zeta, float min_slope, float d)
 {
@@ -82,7 +84,7 @@ __device__ __forceinline__ bool fill_interior_invalid(int nr, int nc, const floa
 }
 
 // One relaxation pass over tile (tx, ty) of an nr x nc grid tiled ntx x nty,
-// run by one 32 x 8 thread block. dirty_in / dirty_out are the grid's
+// run by one 32 x 8 thread block (kFillThreads). dirty_in / dirty_out are the grid's
 // per-tile activity planes (ntx * nty entries).
 __device__ __forceinline__ void fill_relax_tile(int nr, int nc, bool per_ns, bool per_ew, float L, float Ld,
                                                 float min_slope, const float* __restrict__ z,
@@ -116,10 +118,10 @@ __device__ __forceinline__ void fill_relax_tile(int nr, int nc, bool per_ns, boo
     __shared__ float sz[kH][kH];
     const int r0 = ty * kT - 1, c0 = tx * kT - 1;
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
-    // Each thread owns one 2 x 2 block of the tile: local rows 2*by+1 .. +2,
-    // columns 2*bx+1 .. +2, so it holds one cell of each colour.
-    const int bx = tid & 15, by = tid >> 4;
-    unsigned free_mask = 0;  // bit k: this thread's cell of colour k is free (kind 1)
+    // Each thread owns kFillBlocks 2 x 2 blocks of the tile (block b: local
+    // rows 2*(b / (kT/2))+1 .. +2, columns 2*(b % (kT/2))+1 .. +2, b = tid +
+    // j * kFillThreads), so it holds kFillBlocks cells of each colour.
+    unsigned free_mask = 0;  // bit 4j + k: block j's cell of colour k is free (kind 1)
     for (int k = tid; k < kH * kH; k += blockDim.x * blockDim.y)
     {
         const int lr = k / kH, lcc = k % kH;
@@ -138,11 +140,16 @@ __device__ __forceinline__ void fill_relax_tile(int nr, int nc, bool per_ns, boo
         sz[lr][lcc] = zz;
     }
 #pragma unroll
-    for (int k = 0; k < 4; ++k)
+    for (int j = 0; j < kFillBlocks; ++j)
     {
-        const int lr = 2 * by + 1 + (k >> 1), lc = 2 * bx + 1 + (k & 1);
-        const int r = r0 + lr, c = c0 + lc;
-        if (r < nr && c < nc && kind[static_cast<std::int64_t>(r) * nc + c] == 1) free_mask |= 1u << k;
+        const int b = tid + j * kFillThreads, bx = b % (kT / 2), by = b / (kT / 2);
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+        {
+            const int lr = 2 * by + 1 + (k >> 1), lc = 2 * bx + 1 + (k & 1);
+            const int r = r0 + lr, c = c0 + lc;
+            if (r < nr && c < nc && kind[static_cast<std::int64_t>(r) * nc + c] == 1) free_mask |= 1u << (4 * j + k);
+        }
     }
     __syncthreads();
     // Each local iteration updates the four colours of the 2 x 2 colouring
@@ -158,8 +165,12 @@ __device__ __forceinline__ void fill_relax_tile(int nr, int nc, bool per_ns, boo
 #pragma unroll
         for (int k = 0; k < 4; ++k)
         {
+#pragma unroll
+            for (int j = 0; j < kFillBlocks; ++j)
+            {
+            const int b = tid + j * kFillThreads, bx = b % (kT / 2), by = b / (kT / 2);
             const int lr = 2 * by + 1 + (k >> 1), lc = 2 * bx + 1 + (k & 1);
-            if ((free_mask >> k) & 1u)
+            if ((free_mask >> (4 * j + k)) & 1u)
             {
                 const float vN = sF[lr - 1][lc], vNE = sF[lr - 1][lc + 1], vE = sF[lr][lc + 1];
                 const float vSE = sF[lr + 1][lc + 1], vS = sF[lr + 1][lc], vSW = sF[lr + 1][lc - 1];
@@ -189,18 +200,24 @@ __device__ __forceinline__ void fill_relax_tile(int nr, int nc, bool per_ns, boo
                     }
                 }
             }
+            }
             if (k < 3) __syncthreads();
         }
         if (!__syncthreads_or(local)) break;
         tile_changed = true;
     }
 #pragma unroll
-    for (int k = 0; k < 4; ++k)
+    for (int j = 0; j < kFillBlocks; ++j)
     {
-        if (!((free_mask >> k) & 1u)) continue;
-        const int lr = 2 * by + 1 + (k >> 1), lc = 2 * bx + 1 + (k & 1);
-        const std::int64_t g = static_cast<std::int64_t>(r0 + lr) * nc + (c0 + lc);
-        if (sF[lr][lc] < F[g]) F[g] = sF[lr][lc];
+        const int b = tid + j * kFillThreads, bx = b % (kT / 2), by = b / (kT / 2);
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+        {
+            if (!((free_mask >> (4 * j + k)) & 1u)) continue;
+            const int lr = 2 * by + 1 + (k >> 1), lc = 2 * bx + 1 + (k & 1);
+            const std::int64_t g = static_cast<std::int64_t>(r0 + lr) * nc + (c0 + lc);
+            if (sF[lr][lc] < F[g]) F[g] = sF[lr][lc];
+        }
     }
     if (tid == 0)
     {
