@@ -92,38 +92,67 @@ __device__ int donor_list(const Grid& g, const std::uint8_t* __restrict__ mask, 
     return k;
 }
 
-// first child / next sibling links. next_sibling of each donor is written
-// by its (unique) receiver.
+// first child / next sibling links of the cell at `flat` (an index into the
+// grid g's planes; written links get `base` added). next_sibling of each
+// donor is written by its (unique) receiver. Interior cells scan their eight
+// neighbours in ascending flat order (NW, N, NE, W, E, SW, S, SE) and chain
+// the donors as they are found; edge cells take donor_list.
+__device__ __forceinline__ void link_cell(const Grid& g, const std::uint8_t* __restrict__ mask,
+                                          const std::uint8_t* __restrict__ dir, std::int64_t flat, std::int64_t base,
+                                          std::uint32_t* __restrict__ first_child,
+                                          std::uint32_t* __restrict__ next_sib)
+{
+    const int row = static_cast<int>(flat / g.nc), col = static_cast<int>(flat % g.nc);
+    std::uint32_t first = kNone, prev = kNone;
+    auto chain = [&](std::int64_t nf) {
+        const std::uint32_t v = static_cast<std::uint32_t>(base + nf);
+        if (prev == kNone) first = v;
+        else next_sib[prev] = v;
+        prev = v;
+    };
+    if (is_interior(g, row, col))
+    {
+        const int order[8] = {7, 0, 1, 6, 2, 5, 4, 3};  // the codes of NW, N, NE, W, E, SW, S, SE
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+        {
+            const int d = order[i];
+            const std::int64_t nf = flat + static_cast<std::int64_t>(d8_dr(d)) * g.nc + d8_dc(d);
+            if (mask[nf] && dir[nf] == ((d + 4) & 7)) chain(nf);
+        }
+    }
+    else
+    {
+        std::int64_t d[8];
+        const int k = donor_list(g, mask, dir, flat, d);
+        for (int i = 0; i < k; ++i) chain(d[i]);
+    }
+    first_child[base + flat] = first;
+    if (prev != kNone) next_sib[prev] = kNone;
+}
+
 __global__ void links_kernel(Grid g, const std::uint8_t* __restrict__ mask, const std::uint8_t* __restrict__ dir,
                              std::uint32_t* __restrict__ first_child, std::uint32_t* __restrict__ next_sib)
 {
     LSDTT_COUNT();
     const std::int64_t flat = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (flat >= g.n || !mask[flat]) return;
-    std::int64_t d[8];
-    const int k = donor_list(g, mask, dir, flat, d);
-    first_child[flat] = k ? static_cast<std::uint32_t>(d[0]) : kNone;
-    for (int i = 0; i < k; ++i)
-        next_sib[d[i]] = (i + 1 < k) ? static_cast<std::uint32_t>(d[i + 1]) : kNone;
+    link_cell(g, mask, dir, flat, 0, first_child, next_sib);
 }
 
 // links_kernel for a packed ensemble: each member's donors in its own
-// geometry, written as packed indices.
+// geometry, written as packed indices. Blocks are kPackAlign cells, so each
+// lies in one member.
 __global__ void links_packed(Packed P, const std::uint8_t* __restrict__ mask, const std::uint8_t* __restrict__ dir,
                              std::uint32_t* __restrict__ first_child, std::uint32_t* __restrict__ next_sib)
 {
     LSDTT_COUNT();
     const std::int64_t flat = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (flat >= P.n || !mask[flat]) return;
-    const PackedMember M = P.m[P.blk_member[flat / kPackAlign]];
-    const Grid g = member_grid(M);
+    const PackedMember& M = P.m[P.blk_member[blockIdx.x]];
     const std::int64_t local = flat - M.base;
-    if (local >= g.n) return;
-    std::int64_t d[8];
-    const int k = donor_list(g, mask + M.base, dir + M.base, local, d);
-    first_child[flat] = k ? static_cast<std::uint32_t>(M.base + d[0]) : kNone;
-    for (int i = 0; i < k; ++i)
-        next_sib[M.base + d[i]] = (i + 1 < k) ? static_cast<std::uint32_t>(M.base + d[i + 1]) : kNone;
+    if (local >= static_cast<std::int64_t>(M.nr) * M.nc) return;
+    link_cell(member_grid(M), mask + M.base, dir + M.base, local, M.base, first_child, next_sib);
 }
 
 __global__ void root_links_kernel(const std::int64_t* __restrict__ outlets, const std::int64_t* __restrict__ n_out,
@@ -294,10 +323,72 @@ __global__ void ruler_cap_check(const std::uint32_t* cnt, std::uint32_t cap, uns
     if (*cnt > cap) raise_error(err, 9, *cnt);
 }
 
+// Per-cell s-vector outputs, written straight from the level-0 ranking
+// (sv_finish) or from its prefix arrays (sv_outputs). start and svec may be
+// null (a caller that needs the counts and depths only).
+struct SvOut
+{
+    Grid g;
+    const std::uint8_t* mask;
+    std::int64_t n_valid;
+    std::int64_t* start;
+    std::uint64_t* size;
+    std::int32_t* depth;
+    std::int64_t* svec;
+};
+
+__device__ __forceinline__ void sv_store(const SvOut& o, std::int64_t c, std::int32_t s, std::int32_t e,
+                                         std::int32_t dep, unsigned long long* __restrict__ err)
+{
+    if (s < 0 || e <= s || static_cast<std::int64_t>(e) > o.n_valid)
+    {
+        raise_error(err, kErrCycle, 3);
+        if (o.start) o.start[c] = kNodataReceiver;
+        o.size[c] = 0;
+        o.depth[c] = 0;
+        return;
+    }
+    if (o.start) o.start[c] = s;
+    o.size[c] = static_cast<std::uint64_t>(e - s);
+    o.depth[c] = dep;
+    if (o.svec) o.svec[s] = c;
+}
+
+__device__ __forceinline__ bool sv_masked(const SvOut& o, std::int64_t c)
+{
+    if (o.mask[c]) return false;
+    if (o.start) o.start[c] = kNodataReceiver;
+    o.size[c] = 0;
+    o.depth[c] = -1;
+    return true;
+}
+
+// rank_finish and sv_outputs in one pass over the cells of the level-0
+// (Euler tour) list: cell c's enter and exit records are adjacent.
+__global__ void sv_finish(RankLevel L, const RankRec* __restrict__ rec, const std::int32_t* __restrict__ P0,
+                          const std::int32_t* __restrict__ P1, std::uint32_t cap, SvOut o,
+                          unsigned long long* __restrict__ err)
+{
+    LSDTT_COUNT();
+    const std::int64_t c = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (c >= o.g.n || sv_masked(o, c)) return;
+    const RankRec a = rec[2 * c], b = rec[2 * c + 1];
+    if (a.owner >= cap || b.owner >= cap)
+    {
+        // Not reached by any walk: the tour does not cover every valid node.
+        raise_error(err, kErrCycle, 2);
+        sv_store(o, c, -1, -1, 0, err);
+        return;
+    }
+    sv_store(o, c, P0[a.owner] + a.loc0, P0[b.owner] + b.loc0, P1[a.owner] + a.loc1, err);
+}
+
 // Recursive list ranking. p0/p1 receive the exclusive prefix sums of the two
-// weights along the list starting at *L.head.
+// weights along the list starting at *L.head; with sv (the level-0 Euler
+// tour of a grid, longer than kSerialLimit) the per-cell s-vector outputs are
+// written instead and p0/p1 are not used.
 cudaError_t rank_list(const RankLevel& L, std::int32_t* p0, std::int32_t* p1, Scratch& ws,
-                      unsigned long long* err, cudaStream_t st)
+                      unsigned long long* err, cudaStream_t st, const SvOut* sv = nullptr)
 {
     if (L.n <= static_cast<std::uint32_t>(kSerialLimit))
     {
@@ -335,43 +426,25 @@ cudaError_t rank_list(const RankLevel& L, std::int32_t* p0, std::int32_t* p1, Sc
     RankLevel up{cap, nxt, sub0, sub1, nullptr, nhead, cnt};
     e = rank_list(up, P0, P1, ws, err, st);
     if (e != cudaSuccess) return e;
-    rank_finish<<<nb, 256, 0, st>>>(L, rec, P0, P1, cap, p0, p1, err);
+    if (sv)
+        sv_finish<<<grid_blocks(sv->g.n, 256), 256, 0, st>>>(L, rec, P0, P1, cap, *sv, err);
+    else
+        rank_finish<<<nb, 256, 0, st>>>(L, rec, P0, P1, cap, p0, p1, err);
     ws.used = mark;
     return cudaGetLastError();
 }
 
 
 
-// Per-cell s-vector outputs from the two prefix sums.
-__global__ void sv_outputs(Grid g, const std::uint8_t* __restrict__ mask, const std::int32_t* __restrict__ p0,
-                           const std::int32_t* __restrict__ p1, std::int64_t n_valid, std::int64_t* __restrict__ start,
-                           std::uint64_t* __restrict__ size, std::int32_t* __restrict__ depth,
-                           std::int64_t* __restrict__ svec, unsigned long long* __restrict__ err)
+// Per-cell s-vector outputs from the two prefix sums (lists short enough for
+// the serial ranking).
+__global__ void sv_outputs(SvOut o, const std::int32_t* __restrict__ p0, const std::int32_t* __restrict__ p1,
+                           unsigned long long* __restrict__ err)
 {
     LSDTT_COUNT();
     const std::int64_t c = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (c >= g.n) return;
-    if (!mask[c])
-    {
-        start[c] = kNodataReceiver;
-        size[c] = 0;
-        depth[c] = -1;
-        return;
-    }
-    const std::int32_t s = p0[2 * c];
-    const std::int32_t e = p0[2 * c + 1];
-    if (s < 0 || e <= s || static_cast<std::int64_t>(e) > n_valid)
-    {
-        raise_error(err, kErrCycle, 3);
-        start[c] = kNodataReceiver;
-        size[c] = 0;
-        depth[c] = 0;
-        return;
-    }
-    start[c] = s;
-    size[c] = static_cast<std::uint64_t>(e - s);
-    depth[c] = p1[2 * c];
-    svec[s] = c;
+    if (c >= o.g.n || sv_masked(o, c)) return;
+    sv_store(o, c, p0[2 * c], p0[2 * c + 1], p1[2 * c], err);
 }
 
 // ---- range max over the s-vector: blocks of 32, sparse table over blocks ----
@@ -557,10 +630,13 @@ cudaError_t build_stack(lsdtt_gpu_flow* f, bool want_topo, cudaStream_t st, cons
     succ_kernel<<<nb, 256, 0, st>>>(g, f->mask, f->receiver, first_child, next_sib, succ);
 
     RankLevel L0{static_cast<std::uint32_t>(2 * n), succ, nullptr, nullptr, f->mask, head, nullptr};
-    cudaError_t e = rank_list(L0, p0, p1, ws, f->derr, st);
+    // The ensemble reads the counts and depths only.
+    const SvOut sv{g,          f->mask, f->n_valid, packed ? nullptr : f->sv_start, f->sv_size, f->depth,
+                   packed ? nullptr : f->svec};
+    const bool fused = L0.n > static_cast<std::uint32_t>(kSerialLimit);
+    cudaError_t e = rank_list(L0, p0, p1, ws, f->derr, st, fused ? &sv : nullptr);
     if (e != cudaSuccess) return e;
-    sv_outputs<<<nb, 256, 0, st>>>(g, f->mask, p0, p1, f->n_valid, f->sv_start, f->sv_size, f->depth, f->svec,
-                                   f->derr);
+    if (!fused) sv_outputs<<<nb, 256, 0, st>>>(sv, p0, p1, f->derr);
     ws.used = mark;  // tour buffers are no longer needed
     if (!want_topo) return cudaGetLastError();
 
