@@ -212,14 +212,6 @@ __device__ __forceinline__ bool node_valid(const RankLevel& L, std::uint32_t v)
     return v < *L.count;
 }
 
-__global__ void ruler_flags(RankLevel L, std::uint8_t* __restrict__ flag)
-{
-    LSDTT_COUNT();
-    const std::uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= L.n) return;
-    flag[v] = (node_valid(L, v) && (is_ruler(v) || v == *L.head)) ? 1 : 0;
-}
-
 // Per tour node of a ranking level: the ruler whose walk reached it and the
 // two prefixes from that ruler, one 16-byte record (a walk step writes one
 // sector, not three).
@@ -229,25 +221,89 @@ struct alignas(16) RankRec
     std::int32_t loc0, loc1, pad;
 };
 
-__global__ void ruler_scatter(const std::uint8_t* __restrict__ flag, const std::uint32_t* __restrict__ pos,
-                              std::uint32_t n, std::uint32_t cap, std::uint32_t* __restrict__ rulers,
-                              RankRec* __restrict__ rec)
+// Ruler compaction in one pass: each thread takes 16 consecutive nodes, a
+// block scans its rulers and claims a range of the ruler list with one
+// atomic (ruler numbers then depend on block order; the ranks do not). Also
+// counts the level's valid nodes (cnt[2]) for the coverage check.
+constexpr int kCompactPer = 16;
+
+__global__ void __launch_bounds__(256) ruler_compact(RankLevel L, std::uint32_t cap, std::uint32_t* __restrict__ rulers,
+                                                     RankRec* __restrict__ rec, std::uint32_t* __restrict__ cnt)
 {
     LSDTT_COUNT();
-    const std::uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= n || !flag[v] || pos[v] >= cap) return;  // overflow is reported by ruler_cap_check
-    rulers[pos[v]] = v;
-    rec[v].owner = pos[v];
+    __shared__ unsigned wsum[8], wval[8], s_base;
+    const std::uint32_t head = *L.head;
+    const std::uint32_t v0 = (blockIdx.x * blockDim.x + threadIdx.x) * kCompactPer;
+    unsigned rmask = 0, nvalid = 0;
+#pragma unroll
+    for (int j = 0; j < kCompactPer; ++j)
+    {
+        const std::uint32_t v = v0 + j;
+        if (v < L.n && node_valid(L, v))
+        {
+            ++nvalid;
+            if (is_ruler(v) || v == head) rmask |= 1u << j;
+        }
+    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const unsigned nr = __popc(rmask);
+    unsigned incl = nr;
+    for (int o = 1; o < 32; o <<= 1)
+    {
+        const unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    unsigned val = nvalid;
+    for (int o = 16; o > 0; o >>= 1) val += __shfl_down_sync(0xffffffffu, val, o);
+    if (lane == 31) wsum[w] = incl;
+    if (lane == 0) wval[w] = val;
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        unsigned tot = 0, tv = 0;
+        for (int k = 0; k < static_cast<int>(blockDim.x >> 5); ++k)
+        {
+            const unsigned t = wsum[k];
+            wsum[k] = tot;
+            tot += t;
+            tv += wval[k];
+        }
+        s_base = tot ? atomicAdd(&cnt[0], tot) : 0u;
+        if (tv) atomicAdd(&cnt[2], tv);
+    }
+    __syncthreads();
+    std::uint32_t pos = s_base + wsum[w] + incl - nr;
+#pragma unroll
+    for (int j = 0; j < kCompactPer; ++j)
+        if ((rmask >> j) & 1u)
+        {
+            if (pos < cap)
+            {
+                rulers[pos] = v0 + j;
+                rec[v0 + j].owner = pos;
+            }
+            ++pos;  // a count above cap is reported by ruler_checks
+        }
+}
+
+// After the walks: too many rulers, or walks that did not cover every valid
+// node of the level (a successor structure that is not one list).
+__global__ void ruler_checks(const std::uint32_t* cnt, std::uint32_t cap, unsigned long long* err)
+{
+    LSDTT_COUNT();
+    if (cnt[0] > cap) raise_error(err, 9, cnt[0]);
+    else if (cnt[3] != cnt[2]) raise_error(err, kErrCycle, 2);
 }
 
 // A walk from ruler i to the next ruler. A node of the list is a ruler iff
-// is_ruler(v) or it is the head (ruler_flags), so the stop test needs no
+// is_ruler(v) or it is the head (ruler_compact), so the stop test needs no
 // load.
 __global__ void ruler_walk(RankLevel L, const std::uint32_t* __restrict__ rulers,
                            const std::uint32_t* __restrict__ n_rulers, RankRec* __restrict__ rec,
                            std::int32_t* __restrict__ sub0, std::int32_t* __restrict__ sub1,
                            std::uint32_t* __restrict__ nxt, std::uint32_t* __restrict__ next_head,
-                           std::uint32_t cap, unsigned long long* __restrict__ err)
+                           std::uint32_t* __restrict__ walked, std::uint32_t cap,
+                           unsigned long long* __restrict__ err)
 {
     LSDTT_COUNT();
     const std::uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -272,6 +328,11 @@ __global__ void ruler_walk(RankLevel L, const std::uint32_t* __restrict__ rulers
     sub0[i] = a0;
     sub1[i] = a1;
     nxt[i] = (v == kEnd) ? kEnd : rec[v].owner;
+    // coverage: the walks visit every valid node exactly once (one atomic per
+    // converged group of lanes)
+    const unsigned grp = __activemask();
+    const unsigned tot = __reduce_add_sync(grp, steps);
+    if ((threadIdx.x & 31) == static_cast<unsigned>(__ffs(grp) - 1)) atomicAdd(walked, tot);
 }
 
 __global__ void serial_rank(RankLevel L, std::int32_t* __restrict__ p0, std::int32_t* __restrict__ p1,
@@ -315,12 +376,6 @@ __global__ void rank_finish(RankLevel L, const RankRec* __restrict__ rec, const 
     }
     p0[v] = P0[o] + r.loc0;
     p1[v] = P1[o] + r.loc1;
-}
-
-__global__ void ruler_cap_check(const std::uint32_t* cnt, std::uint32_t cap, unsigned long long* err)
-{
-    LSDTT_COUNT();
-    if (*cnt > cap) raise_error(err, 9, *cnt);
 }
 
 // Per-cell s-vector outputs, written straight from the level-0 ranking
@@ -397,16 +452,9 @@ cudaError_t rank_list(const RankLevel& L, std::int32_t* p0, std::int32_t* p1, Sc
     }
     const std::size_t mark = ws.used;
     const std::uint32_t cap = L.n / (kRuler / 4) + 64;  // generous bound on the ruler count
-    std::uint8_t* flag = ws.take<std::uint8_t>(L.n);
-    std::uint32_t* pos = ws.take<std::uint32_t>(L.n);
-    std::uint32_t* cnt = ws.take<std::uint32_t>(2);
+    // cnt: [0] rulers, [1] the head's ruler, [2] valid nodes, [3] nodes walked
+    std::uint32_t* cnt = ws.take<std::uint32_t>(4);
     RankRec* rec = ws.take<RankRec>(L.n);
-    if (!flag || !pos || !cnt || !rec) return cudaErrorMemoryAllocation;
-    const unsigned nb = grid_blocks(L.n, 256);
-    cudaMemsetAsync(rec, 0xff, sizeof(RankRec) * L.n, st);  // owner kNone: reached by no walk
-    ruler_flags<<<nb, 256, 0, st>>>(L, flag);
-    cudaError_t e = exclusive_scan<std::uint8_t, std::uint32_t>(flag, L.n, pos, cnt, ws, st);
-    if (e != cudaSuccess) return e;
     // The ruler count is data dependent; size everything by `cap` and let the
     // kernels read the true count. A count above `cap` is reported.
     std::uint32_t* rulers = ws.take<std::uint32_t>(cap);
@@ -416,13 +464,16 @@ cudaError_t rank_list(const RankLevel& L, std::int32_t* p0, std::int32_t* p1, Sc
     std::int32_t* P0 = ws.take<std::int32_t>(cap);
     std::int32_t* P1 = ws.take<std::int32_t>(cap);
     std::uint32_t* nhead = cnt + 1;
-    if (!rulers || !nxt || !sub0 || !sub1 || !P0 || !P1) return cudaErrorMemoryAllocation;
-    ruler_scatter<<<nb, 256, 0, st>>>(flag, pos, L.n, cap, rulers, rec);
-    ruler_cap_check<<<1, 1, 0, st>>>(cnt, cap, err);
+    if (!cnt || !rec || !rulers || !nxt || !sub0 || !sub1 || !P0 || !P1) return cudaErrorMemoryAllocation;
+    const unsigned nb = grid_blocks(L.n, 256);
+    cudaMemsetAsync(cnt, 0, sizeof(std::uint32_t) * 4, st);
+    ruler_compact<<<grid_blocks((L.n + kCompactPer - 1) / kCompactPer, 256), 256, 0, st>>>(L, cap, rulers, rec, cnt);
     // Bytes touched per tour node: successor 4 in, the 16-byte record out.
     LSDTT_TIMED("stack_ruler_walk", 20.0 * static_cast<double>(L.n), st,
-                (ruler_walk<<<grid_blocks(cap, 128), 128, 0, st>>>(L, rulers, cnt, rec, sub0, sub1, nxt, nhead, cap,
-                                                                   err)));
+                (ruler_walk<<<grid_blocks(cap, 128), 128, 0, st>>>(L, rulers, cnt, rec, sub0, sub1, nxt, nhead,
+                                                                   cnt + 3, cap, err)));
+    ruler_checks<<<1, 1, 0, st>>>(cnt, cap, err);
+    cudaError_t e = cudaSuccess;
     RankLevel up{cap, nxt, sub0, sub1, nullptr, nhead, cnt};
     e = rank_list(up, P0, P1, ws, err, st);
     if (e != cudaSuccess) return e;
