@@ -868,10 +868,12 @@ __device__ __forceinline__ void block_partials_f(const float (&v)[NQ], unsigned 
 // dst[m * stride + off + q] = reduction of member m's block partials of
 // quantity q (bit q of max_mask: maximum, else sum); one warp per (m, q).
 // Members with done[m] set are skipped. With shift, dst moves by
-// *shift * shift_step (a device-side iteration's slot).
+// *shift * shift_step (a device-side iteration's slot). With tile_partials
+// the partials are per 128 x 32 member tile (ens_hs_apply_tiled).
 __global__ void ens_member_reduce(Packed P, int nq, unsigned max_mask, const double* __restrict__ part,
                                   std::int64_t nblk, const int* __restrict__ done, double* __restrict__ dst, int stride,
-                                  int off, const int* __restrict__ shift = nullptr, std::int64_t shift_step = 0)
+                                  int off, const int* __restrict__ shift = nullptr, std::int64_t shift_step = 0,
+                                  int tile_partials = 0)
 {
     LSDTT_COUNT();
     if (shift) dst += static_cast<std::int64_t>(*shift) * shift_step;
@@ -882,8 +884,10 @@ __global__ void ens_member_reduce(Packed P, int nq, unsigned max_mask, const dou
     if (done && done[m]) return;
     const PackedMember& M = P.m[m];
     const bool is_max = (max_mask >> q) & 1u;
-    const std::int64_t b0 = M.base / kPackAlign;
-    const std::int64_t nb = (static_cast<std::int64_t>(M.nr) * M.nc + kPackAlign - 1) / kPackAlign;
+    // partials per kPackAlign block of the member, or per 128 x 32 tile
+    const std::int64_t b0 = tile_partials ? M.rtile_base : M.base / kPackAlign;
+    const std::int64_t nb = tile_partials ? static_cast<std::int64_t>(M.nrx) * M.nry
+                                          : (static_cast<std::int64_t>(M.nr) * M.nc + kPackAlign - 1) / kPackAlign;
     double s = is_max ? -INFINITY : 0.0;
     for (std::int64_t b = b0 + lane; b < b0 + nb; b += 32)
     {
@@ -998,91 +1002,130 @@ __global__ void ens_hs_start(int M, const EnsParams* __restrict__ prm, const dou
 // p_dst, the buffer the update then reads; without it p_dst already holds p.
 // beta_m holds each member's beta (ens_pcg_ratio); with it_dev (a
 // device-side loop) the direction update is fused whenever *it_dev > 0.
+//
+// The apply over the members' 128 x 32 tiles (the receiver tiles), one
+// 256-thread block per tile: p (formed as z + beta p_src when fused) for the
+// tile and a one-cell halo is staged in shared memory by coalesced rows, and
+// fast cells (dof 3) read their four neighbours there, in the order of the
+// general path's sum (N, E, S, W); other DOF cells take the general path from
+// global memory. Each lane handles columns lane, lane + 32, ... of four rows,
+// so every load and store of a warp is contiguous. One p.Ap partial per tile.
 template <bool kFuse>
-__device__ __forceinline__ void hs_apply_block(const Packed& P, const PackedMember& M, const EnsParams& q,
-                                               const std::uint8_t* __restrict__ mask,
-                                               const std::uint8_t* __restrict__ dof, float beta,
-                                               const float* __restrict__ zz, const float* __restrict__ p_src,
-                                               float* __restrict__ p_dst, float* __restrict__ Ap,
-                                               double* __restrict__ part)
+__device__ __forceinline__ void hs_apply_tile(float (&sp)[kD8TileRows + 2][132], const PackedMember& M,
+                                              const EnsParams& q, int tx, int ty,
+                                              const std::uint8_t* __restrict__ mask,
+                                              const std::uint8_t* __restrict__ dof, float beta,
+                                              const float* __restrict__ zz, const float* __restrict__ p_src,
+                                              float* __restrict__ p_dst, float* __restrict__ Ap,
+                                              double* __restrict__ part, std::int64_t nblk)
 {
-    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    // p at any cell of the packed buffer
+    // sp: column c0 - 1 + k at index k
+    const int c0 = tx * kD8TileCols, r0 = ty * kD8TileRows;
+    const int nr = M.nr, nc = M.nc;
+    const std::int64_t base = M.base;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     auto pv = [&](std::int64_t k) { return kFuse ? zz[k] + beta * p_src[k] : p_dst[k]; };
-    float pap = 0.0f;
-    if (i < P.n)
+    for (int lr = w; lr < kD8TileRows + 2; lr += 8)
     {
-        float v = 0.0f;
-        const std::uint8_t kd = dof[i];
-        const float pi = pv(i);
-        if (kFuse) p_dst[i] = pi;
-        if (kd == 3)
-        {
-            const int nc = M.nc;
-            // the general path's sum, in its order (N, E, S, W)
-            const float s = (((pi - pv(i - nc)) + (pi - pv(i + 1))) + (pi - pv(i + nc))) + (pi - pv(i - 1));
-            v = q.inv_dt_f * pi + q.DA_f * s;
-            pap = pi * v;
-        }
-        else if (kd)
-        {
-            const int l = static_cast<int>(i - M.base);
-            const int r = l / M.nc, c = l - r * M.nc;
-            const std::uint8_t* mk = mask + M.base;
-            const std::uint8_t* dm = dof + M.base;
-            float s = 0.0f;
-            if (r > 0 && r < M.nr - 1 && c > 0 && c < M.nc - 1)
-            {
-                // interior: the in-grid neighbour, or the cell itself when masked
-                const int nbr[4] = {l - M.nc, l + 1, l + M.nc, l - 1};
+        const int r = r0 - 1 + lr;
+        const bool row_in = r >= 0 && r < nr;
+        const std::int64_t rb = base + static_cast<std::int64_t>(r) * nc;
 #pragma unroll
-                for (int f = 0; f < 4; ++f)
-                {
-                    const int j = nbr[f];
-                    if (!mk[j]) continue;
-                    s += pi - (dm[j] ? pv(M.base + j) : 0.0f);
-                }
-            }
-            else
-            {
-#pragma unroll
-                for (int f = 0; f < 4; ++f)
-                {
-                    const std::int64_t j = hs_nb(q.hs, mk, r, c, kDr[f], kDc[f]);
-                    if (j == l) continue;
-                    s += pi - (dm[j] ? pv(M.base + j) : 0.0f);
-                }
-            }
-            v = q.inv_dt_f * pi + q.DA_f * s;
-            pap = pi * v;
+        for (int k = 0; k < 5; ++k)
+        {
+            const int col = 32 * k + lane;  // 0 .. 159: columns c0 - 1 .. c0 + 128 are used
+            if (col >= 130) continue;
+            const int c = c0 - 1 + col;
+            sp[lr][col] = (row_in && c >= 0 && c < nc) ? pv(rb + c) : 0.0f;
         }
-        Ap[i] = v;
     }
-    block_partial_f(pap, false, part, P.n / kPackAlign, 0);
+    __syncthreads();
+    float pap = 0.0f;
+#pragma unroll
+    for (int qr = 0; qr < 4; ++qr)
+    {
+        const int lr = 1 + w * 4 + qr, r = r0 + lr - 1;
+        if (r >= nr) continue;
+        const std::int64_t rb = base + static_cast<std::int64_t>(r) * nc;
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+        {
+            const int lc = 1 + 32 * k + lane, c = c0 + lc - 1;
+            if (c >= nc) continue;
+            const std::int64_t i = rb + c;
+            const std::uint8_t kd = dof[i];
+            const float pi = sp[lr][lc];
+            if (kFuse) p_dst[i] = pi;
+            float v = 0.0f;
+            if (kd == 3)
+            {
+                const float s = (((pi - sp[lr - 1][lc]) + (pi - sp[lr][lc + 1])) + (pi - sp[lr + 1][lc])) +
+                                (pi - sp[lr][lc - 1]);
+                v = q.inv_dt_f * pi + q.DA_f * s;
+            }
+            else if (kd)
+            {
+                const int l = r * nc + c;
+                const std::uint8_t* mk = mask + base;
+                const std::uint8_t* dm = dof + base;
+                float s = 0.0f;
+                if (r > 0 && r < nr - 1 && c > 0 && c < nc - 1)
+                {
+                    // interior: the in-grid neighbour, or the cell itself when masked
+                    const int nbr[4] = {l - nc, l + 1, l + nc, l - 1};
+#pragma unroll
+                    for (int f = 0; f < 4; ++f)
+                    {
+                        const int j = nbr[f];
+                        if (!mk[j]) continue;
+                        s += pi - (dm[j] ? pv(base + j) : 0.0f);
+                    }
+                }
+                else
+                {
+#pragma unroll
+                    for (int f = 0; f < 4; ++f)
+                    {
+                        const std::int64_t j = hs_nb(q.hs, mk, r, c, kDr[f], kDc[f]);
+                        if (j == l) continue;
+                        s += pi - (dm[j] ? pv(base + j) : 0.0f);
+                    }
+                }
+                v = q.inv_dt_f * pi + q.DA_f * s;
+            }
+            pap += pi * v;
+            Ap[i] = v;
+        }
+    }
+    block_partial_f(pap, false, part, nblk, 0);
 }
 
-// Blocks are kPackAlign cells, so each lies in one member (read once per
-// block); the fused and plain bodies are separate specialisations.
-__global__ void __launch_bounds__(kPackAlign) ens_hs_apply(Packed P, const EnsParams* __restrict__ prm,
-                                                           const std::uint8_t* __restrict__ mask,
-                                                           const std::uint8_t* __restrict__ dof,
-                                                           const int* __restrict__ done, int fuse,
-                                                           const float* __restrict__ beta_m,
-                                                           const int* __restrict__ it_dev,
-                                                           const float* __restrict__ zz,
-                                                           const float* __restrict__ p_src, float* __restrict__ p_dst,
-                                                           float* __restrict__ Ap, double* __restrict__ part)
+__global__ void __launch_bounds__(256, 4) ens_hs_apply_tiled(Packed P, const EnsParams* __restrict__ prm,
+                                                          const std::uint16_t* __restrict__ rtile_member,
+                                                          const std::uint8_t* __restrict__ mask,
+                                                          const std::uint8_t* __restrict__ dof,
+                                                          const int* __restrict__ done, int fuse,
+                                                          const float* __restrict__ beta_m,
+                                                          const int* __restrict__ it_dev,
+                                                          const float* __restrict__ zz,
+                                                          const float* __restrict__ p_src, float* __restrict__ p_dst,
+                                                          float* __restrict__ Ap, double* __restrict__ part)
 {
     LSDTT_COUNT();
-    const int m = P.blk_member[blockIdx.x];
+    const int m = rtile_member[blockIdx.x];
     if (done[m]) return;
     if (it_dev && *it_dev > 0) fuse = 1;
     const PackedMember& M = P.m[m];
     const EnsParams& q = prm[m];
+    const int local = static_cast<int>(blockIdx.x) - M.rtile_base;
+    const std::int64_t nblk = P.n / kPackAlign;
+    __shared__ float sp[kD8TileRows + 2][132];
     if (fuse)
-        hs_apply_block<true>(P, M, q, mask, dof, beta_m[m], zz, p_src, p_dst, Ap, part);
+        hs_apply_tile<true>(sp, M, q, local % M.nrx, local / M.nrx, mask, dof, beta_m[m], zz, p_src, p_dst, Ap, part,
+                            nblk);
     else
-        hs_apply_block<false>(P, M, q, mask, dof, 0.0f, zz, p_src, p_dst, Ap, part);
+        hs_apply_tile<false>(sp, M, q, local % M.nrx, local / M.nrx, mask, dof, 0.0f, zz, p_src, p_dst, Ap, part,
+                             nblk);
 }
 
 // x += alpha p; r -= alpha Ap; z = M^-1 r (alpha_m: each member's
@@ -1752,10 +1795,10 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
     const int itmax = (eager || device_loop) ? E->max_iter_all : E->it_cap;
     const std::int64_t nblk = N / kPackAlign;
     auto reduce = [&](cudaStream_t s2, int nq, unsigned max_mask, const int* dn, double* dst, int stride, int off,
-                      const int* shift) {
+                      const int* shift, int tile_partials = 0) {
         const unsigned warps = static_cast<unsigned>(M * nq);
         ens_member_reduce<<<(warps + 3) / 4, 128, 0, s2>>>(E->P, nq, max_mask, E->part, nblk, dn, dst, stride, off,
-                                                           shift, slot_len);
+                                                           shift, slot_len, tile_partials);
     };
     cudaMemsetAsync(E->hs_acc, 0, slot_bytes * (static_cast<std::size_t>(itmax) + 1), st);
     ens_hs_setup<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->mask, E->zsp, E->dof, E->invd, E->b, E->part);
@@ -1776,13 +1819,14 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
         {
             // Algorithmic bytes: p 4 in (+ z 4 when fused), Ap 4 out (+ p 4 when fused).
             LSDTT_TIMED("ens_hillslope_apply", (it ? 16.0 : 8.0) * cells, s2,
-                        (ens_hs_apply<<<nb, 256, 0, s2>>>(E->P, E->d_prm, E->mask, E->dof, E->done, it ? 1 : 0, beta,
-                                                          it_dev, E->zz, p_prev, p_it, E->Ap, E->part)));
+                        (ens_hs_apply_tiled<<<E->S, 256, 0, s2>>>(E->P, E->d_prm, E->strip_member, E->mask, E->dof,
+                                                                  E->done, it ? 1 : 0, beta, it_dev, E->zz, p_prev,
+                                                                  p_it, E->Ap, E->part)));
         }
         else
-            ens_hs_apply<<<nb, 256, 0, s2>>>(E->P, E->d_prm, E->mask, E->dof, E->done, it ? 1 : 0, beta, it_dev,
-                                             E->zz, p_prev, p_it, E->Ap, E->part);
-        reduce(s2, 1, 0u, E->done, cur, kHsSlot, 0, it_dev);
+            ens_hs_apply_tiled<<<E->S, 256, 0, s2>>>(E->P, E->d_prm, E->strip_member, E->mask, E->dof, E->done,
+                                                     it ? 1 : 0, beta, it_dev, E->zz, p_prev, p_it, E->Ap, E->part);
+        reduce(s2, 1, 0u, E->done, cur, kHsSlot, 0, it_dev, 1);
         // alpha = r.z (slot it) / p.Ap (slot it + 1)
         ens_pcg_ratio<<<mb, 128, 0, s2>>>(M, E->done, E->hs_acc, it, 1, it + 1, 0, it_dev, alpha);
         if (timed)
@@ -2168,6 +2212,11 @@ int lsdtt_gpu_ensemble_create(const lsdtt_gpu_member* members, int32_t n_members
     cudaMemcpyAsync(E->perm, E->perm_h.data(), sizeof(std::uint16_t) * E->perm_h.size(), cudaMemcpyHostToDevice, st);
     cudaMemsetAsync(E->z, 0, sizeof(float) * n, st);
     cudaMemsetAsync(E->mask, 0, n, st);
+    // the PCG's padding cells (between members) stay zero: the tiled apply
+    // covers member cells only
+    cudaMemsetAsync(E->p, 0, sizeof(float) * n, st);
+    cudaMemsetAsync(E->p2, 0, sizeof(float) * n, st);
+    cudaMemsetAsync(E->Ap, 0, sizeof(float) * n, st);
     cudaMemsetAsync(E->zg, 0, sizeof(unsigned long long) * n, st);
     // padding cells between members: no receiver, no direction, ever
     cudaMemsetAsync(E->f->receiver, 0xFF, sizeof(std::int64_t) * n, st);
