@@ -297,14 +297,14 @@ __global__ void ens_kam_table(Packed P, const EnsParams* __restrict__ prm, doubl
 // list with warp-aggregated slots and done densely by ens_kam_big, so no
 // warp idles through the FP64 pow for one lane.
 __global__ void ens_kam(Packed P, const EnsParams* __restrict__ prm, const std::uint8_t* __restrict__ mask,
-                        const std::int64_t* __restrict__ receiver, const std::uint64_t* __restrict__ size,
+                        const std::uint8_t* __restrict__ dir, const std::uint64_t* __restrict__ size,
                         const double* __restrict__ tab, double* __restrict__ kam, std::uint32_t* __restrict__ big,
                         std::uint32_t* __restrict__ n_big)
 {
     LSDTT_COUNT();
     const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     bool need = false;
-    if (i < P.n && mask[i] && receiver[i] >= 0)
+    if (i < P.n && mask[i] && dir[i] != kNoDir)  // a valid cell with a receiver
     {
         const int m = block_member(P);
         const std::uint64_t c = size[i];
@@ -939,12 +939,21 @@ __global__ void ens_hs_setup(Packed P, const EnsParams* __restrict__ prm, const 
                 const float zp = zm[l];
                 float flux = 0.0f;
                 int nf = 0;
-#pragma unroll
-                for (int f = 0; f < 4; ++f)
+                if (fast)
                 {
-                    const std::int64_t j = hs_nb(H, mk, r, c, kDr[f], kDc[f]);
-                    flux += zm[j] - zp;
-                    nf += (j != l) ? 1 : 0;
+                    // the four in-grid neighbours, in the general path's order (N, E, S, W)
+                    flux = (((zm[l - M.nc] - zp) + (zm[l + 1] - zp)) + (zm[l + M.nc] - zp)) + (zm[l - 1] - zp);
+                    nf = 4;
+                }
+                else
+                {
+#pragma unroll
+                    for (int f = 0; f < 4; ++f)
+                    {
+                        const std::int64_t j = hs_nb(H, mk, r, c, kDr[f], kDc[f]);
+                        flux += zm[j] - zp;
+                        nf += (j != l) ? 1 : 0;
+                    }
                 }
                 const float F = -q.U_f - q.DA_f * flux;
                 b[i] = -F;
@@ -962,8 +971,10 @@ __global__ void ens_hs_setup(Packed P, const EnsParams* __restrict__ prm, const 
     block_partial_f(bb, false, part, P.n / kPackAlign, 0);
 }
 
-// x = 0, r = b, p = M^-1 r; block partials of r.z
+// Start from x0 (the previous step's increment; zero at non-DOF cells):
+// r = b - A x0 (A x0 in Ax0), p = M^-1 r; block partials of r.z.
 __global__ void ens_hs_init(Packed P, const float* __restrict__ b, const float* __restrict__ inv_diag,
+                            const std::uint8_t* __restrict__ dof, const float* __restrict__ Ax0,
                             float* __restrict__ x, float* __restrict__ r, float* __restrict__ p,
                             double* __restrict__ part)
 {
@@ -972,9 +983,10 @@ __global__ void ens_hs_init(Packed P, const float* __restrict__ b, const float* 
     float rz = 0.0f;
     if (i < P.n)
     {
-        const float ri = b[i];
+        const bool d = dof[i] != 0;
+        const float ri = d ? b[i] - Ax0[i] : 0.0f;
         const float zi = ri * inv_diag[i];
-        x[i] = 0.0f;
+        if (!d) x[i] = 0.0f;
         r[i] = ri;
         p[i] = zi;
         rz = ri * zi;
@@ -1605,7 +1617,7 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
     e = build_stack(f, false, st, &E->P);
     if (e != cudaSuccess) return e;
     cudaMemsetAsync(E->dfc + 1, 0, sizeof(std::uint32_t), st);  // count of large-count nodes
-    ens_kam<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->mask, f->receiver, f->sv_size, E->kam_tab, E->area, E->lfill,
+    ens_kam<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->mask, f->dir, f->sv_size, E->kam_tab, E->area, E->lfill,
                                 E->dfc + 1);
     ens_kam_big<<<152 * 8, 256, 0, st>>>(E->P, E->d_prm, f->sv_size, E->lfill, E->dfc + 1, E->area);
     // 2. depth levels: the global level order (level launches, the
@@ -1803,7 +1815,12 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
     cudaMemsetAsync(E->hs_acc, 0, slot_bytes * (static_cast<std::size_t>(itmax) + 1), st);
     ens_hs_setup<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->mask, E->zsp, E->dof, E->invd, E->b, E->part);
     reduce(st, 1, 0u, nullptr, E->hs_bb, 1, 0, nullptr);
-    ens_hs_init<<<nb, 256, 0, st>>>(E->P, E->b, E->invd, E->x, E->r, E->p, E->part);
+    // Warm start: the previous step's increment x (zero at the first step)
+    // as the initial guess; A x0 by one plain apply (p_dst = x).
+    cudaMemsetAsync(E->done, 0, sizeof(int) * M, st);
+    ens_hs_apply_tiled<<<E->S, 256, 0, st>>>(E->P, E->d_prm, E->strip_member, E->mask, E->dof, E->done, 0, E->pcg_scal,
+                                             nullptr, E->zz, E->p2, E->x, E->Ap, E->part);
+    ens_hs_init<<<nb, 256, 0, st>>>(E->P, E->b, E->invd, E->dof, E->Ap, E->x, E->r, E->p, E->part);
     reduce(st, 1, 0u, nullptr, E->hs_acc, kHsSlot, 1, nullptr);
     ens_hs_start<<<mb, 128, 0, st>>>(M, E->d_prm, E->hs_bb, E->done, E->iters);
     // One iteration whose slots are it / it + 1 (it_dev: plus the device-side
@@ -2217,6 +2234,7 @@ int lsdtt_gpu_ensemble_create(const lsdtt_gpu_member* members, int32_t n_members
     cudaMemsetAsync(E->p, 0, sizeof(float) * n, st);
     cudaMemsetAsync(E->p2, 0, sizeof(float) * n, st);
     cudaMemsetAsync(E->Ap, 0, sizeof(float) * n, st);
+    cudaMemsetAsync(E->x, 0, sizeof(float) * n, st);  // the first step's PCG starts from zero
     cudaMemsetAsync(E->zg, 0, sizeof(unsigned long long) * n, st);
     // padding cells between members: no receiver, no direction, ever
     cudaMemsetAsync(E->f->receiver, 0xFF, sizeof(std::int64_t) * n, st);
