@@ -625,6 +625,9 @@ def train_preconditioner(G, size, cell, D, Sc, dt, nonlinear, n_surfaces, pairs_
         big.set_params(net.get_params())
         net.close()
         net = big
+    conv = getattr(train_preconditioner, "conv_kernel", "")
+    if conv:
+        net.set_conv_kernel(conv)
     n_pairs = int(r.shape[0])
     del r, e, rs, es
     torch.cuda.empty_cache()
@@ -747,6 +750,8 @@ def unet_gpu(args, rank, world):
     import lsdtt_gb300 as G
     n = args.size if args.size != 8192 else 2048
     net = G.UNet(n, n, seed=3)
+    if args.conv_kernel:
+        net.set_conv_kernel(args.conv_kernel)
     r = torch.randn(n, n, device="cuda", generator=torch.Generator(device="cuda").manual_seed(1))
     for _ in range(args.warmup):
         net.apply(r)
@@ -765,9 +770,24 @@ def unet_gpu(args, rank, world):
     for (name, ci, co), px in zip(G.UNET_LAYERS, [n * n, n * n / 4, n * n / 16, n * n / 64, n * n / 16, n * n / 4,
                                                    n * n, n * n]):
         flops += 2.0 * 9 * ci * co * px
+    # per-layer table of one more application (CUDA events per launch)
+    L = G.lib()
+    L.lsdtt_gpu_profile_read.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_double),
+                                         ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_double)]
+    L.lsdtt_gpu_profile_enable(1)
+    net.apply(r)
+    torch.cuda.synchronize()
+    kernels = {}
+    for name in ["unet_prep", "unet_conv_in", "unet_pool"] + [f"unet_layer{l}" for l in range(1, 7)] + ["unet_conv_out"]:
+        t, k, b = ctypes.c_double(), ctypes.c_int64(), ctypes.c_double()
+        G._check(L.lsdtt_gpu_profile_read(name.encode(), ctypes.byref(t), ctypes.byref(k), ctypes.byref(b)))
+        if k.value:
+            kernels[name] = {"ms": round(t.value, 4), "GBps": round(b.value / (t.value / 1e3) / 1e9, 1)}
+    L.lsdtt_gpu_profile_enable(0)
     if rank == 0:
-        print(json.dumps({"workload": f"U-Net forward on a {n}x{n} residual", "ms_per_application": ms,
-                          "tflops": flops / (ms / 1e3) / 1e12, "steps": args.steps}), flush=True)
+        print(json.dumps({"workload": f"U-Net forward on a {n}x{n} residual", "conv_kernel": args.conv_kernel or "default",
+                          "ms_per_application": ms,
+                          "tflops": flops / (ms / 1e3) / 1e12, "steps": args.steps, "kernels": kernels}), flush=True)
     return 0
 
 
@@ -786,7 +806,10 @@ def main():
     ap.add_argument("--members", type=int, default=256)
     ap.add_argument("--sweep-mode", type=int, default=-1, help="ensemble sweep: -1 autotuned, 0 levels, 1 dataflow, 2 cooperative levels, 3 member clusters")
     ap.add_argument("--plain-members", type=int, default=16)
+    ap.add_argument("--conv-kernel", default="", choices=["", "mma", "tcgen05", "tcgen05_rows"],
+                    help="U-Net convolution kernels (default: the library's)")
     args = ap.parse_args()
+    train_preconditioner.conv_kernel = args.conv_kernel  # the inference network's convolutions
     if args.warmup < 3:
         args.warmup = 3
     rank = int(os.environ.get("RANK", "0"))

@@ -608,8 +608,9 @@ class UNet:
         self.n_params = int(L.lsdtt_gpu_unet_num_params(h))
 
     def set_conv_kernel(self, kind: str) -> None:
-        """'mma' (mma.sync m16n8k16) or 'tcgen05' (UMMA, accumulator in TMEM)."""
-        _check(lib().lsdtt_gpu_unet_set_conv_kernel(self._h, {"mma": 0, "tcgen05": 1}[kind]))
+        """'mma' (mma.sync m16n8k16), 'tcgen05' (UMMA, accumulator in TMEM) or
+        'tcgen05_rows' (UMMA over rolling input rows)."""
+        _check(lib().lsdtt_gpu_unet_set_conv_kernel(self._h, {"mma": 0, "tcgen05": 1, "tcgen05_rows": 2}[kind]))
 
     def status(self) -> None:
         """Raises if a tensor-core convolution gave up waiting for its MMAs."""

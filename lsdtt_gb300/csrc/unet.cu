@@ -60,23 +60,34 @@ __global__ void k_sumsq(const float* __restrict__ r, std::int64_t n, double* __r
     if ((threadIdx.x & 31) == 0) atomicAdd(acc, s);
 }
 
-// x0 = bf16(r / rms); rms computed from acc[0] = sum r^2 (n cells)
-__global__ void k_prep(const float* __restrict__ r, std::int64_t n, const double* __restrict__ acc,
-                       __nv_bfloat16* __restrict__ x0, float* __restrict__ rms_out)
+// rms from acc[0] = sum r^2 over n cells, once (FP64 is scarce on this part)
+__global__ void k_rms(std::int64_t n, const double* __restrict__ acc, float* __restrict__ rms_out)
+{
+    LSDTT_COUNT();
+    float rms = static_cast<float>(sqrt(acc[0] / static_cast<double>(n)));
+    if (!(rms > 0.0f)) rms = 1.0f;
+    *rms_out = rms;
+}
+
+// x0 = bf16(r / rms)
+__global__ void k_prep(const float* __restrict__ r, std::int64_t n, const float* __restrict__ rms_in,
+                       __nv_bfloat16* __restrict__ x0)
 {
     LSDTT_COUNT();
     const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    float rms = static_cast<float>(sqrt(acc[0] / static_cast<double>(n)));
-    if (!(rms > 0.0f)) rms = 1.0f;
-    if (i == 0) *rms_out = rms;
+    const float rms = *rms_in;
     if (i < n) x0[i] = __float2bfloat16_rn(r[i] / rms);
 }
 
 // Layer 0: 1 -> 16 channels, ReLU, on CUDA cores.
-__global__ void k_conv_in(int H, int W, const __nv_bfloat16* __restrict__ x0, const float* __restrict__ w,
-                          const float* __restrict__ b, __nv_bfloat16* __restrict__ out)
+__global__ void k_conv_in(int H, int W, const __nv_bfloat16* __restrict__ x0, const float* __restrict__ wg,
+                          const float* __restrict__ bg, __nv_bfloat16* __restrict__ out)
 {
     LSDTT_COUNT();
+    __shared__ float w[16 * 9], b[16];
+    for (int k = threadIdx.x; k < 16 * 9; k += blockDim.x) w[k] = wg[k];
+    if (threadIdx.x < 16) b[threadIdx.x] = bg[threadIdx.x];
+    __syncthreads();
     const std::int64_t p = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (p >= static_cast<std::int64_t>(H) * W) return;
     const int y = static_cast<int>(p / W), x = static_cast<int>(p % W);
@@ -100,19 +111,34 @@ __global__ void k_conv_in(int H, int W, const __nv_bfloat16* __restrict__ x0, co
     *reinterpret_cast<uint4*>(out + p * 16 + 8) = *reinterpret_cast<const uint4*>(o16 + 8);
 }
 
-// 2x2 mean, bf16 -> bf16 (H, W are the OUTPUT sizes)
+// 2x2 mean, bf16 -> bf16 (H, W are the OUTPUT sizes), eight channels per
+// thread with 16-byte loads and stores (C a multiple of 8)
 __global__ void k_pool(int H, int W, int C, const __nv_bfloat16* __restrict__ in, __nv_bfloat16* __restrict__ out)
 {
     LSDTT_COUNT();
+    const int G = C / 8;
     const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i >= static_cast<std::int64_t>(H) * W * C) return;
-    const int c = static_cast<int>(i % C);
-    const std::int64_t p = i / C;
+    if (i >= static_cast<std::int64_t>(H) * W * G) return;
+    const int c = static_cast<int>(i % G) * 8;
+    const std::int64_t p = i / G;
     const int y = static_cast<int>(p / W), x = static_cast<int>(p % W);
     const int W2 = 2 * W;
-    auto at = [&](int yy, int xx) { return __bfloat162float(in[(static_cast<std::int64_t>(yy) * W2 + xx) * C + c]); };
-    const float s = ((at(2 * y, 2 * x) + at(2 * y, 2 * x + 1)) + at(2 * y + 1, 2 * x)) + at(2 * y + 1, 2 * x + 1);
-    out[i] = __float2bfloat16_rn(s * 0.25f);
+    auto at = [&](int yy, int xx, __nv_bfloat16 (&v)[8]) {
+        *reinterpret_cast<uint4*>(v) = *reinterpret_cast<const uint4*>(in + (static_cast<std::int64_t>(yy) * W2 + xx) * C + c);
+    };
+    alignas(16) __nv_bfloat16 a[8], b[8], d[8], e[8], o[8];
+    at(2 * y, 2 * x, a);
+    at(2 * y, 2 * x + 1, b);
+    at(2 * y + 1, 2 * x, d);
+    at(2 * y + 1, 2 * x + 1, e);
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+    {
+        const float s = ((__bfloat162float(a[k]) + __bfloat162float(b[k])) + __bfloat162float(d[k])) +
+                        __bfloat162float(e[k]);
+        o[k] = __float2bfloat16_rn(s * 0.25f);
+    }
+    *reinterpret_cast<uint4*>(out + p * C + c) = *reinterpret_cast<const uint4*>(o);
 }
 
 // Tensor-core 3x3 convolution, Cin and Cout multiples of 16 (Cin) / 8 (Cout).
@@ -336,6 +362,80 @@ __device__ __forceinline__ void tc5_issue(std::uint32_t tmem_acc, std::uint32_t 
                  : "memory");
 }
 
+// Epilogue of one 128-pixel tile of output row y at x0 from the FP32
+// accumulator at TMEM column tmem_acc: warp w reads TMEM lanes 32 (w % 4) ..
+// (its tile pixels); warps w and w + 4 take alternate column chunks (8 wide
+// for 16 output channels, so that both halves work, else 16). Bias, ReLU
+// (mode 0) or ReLU plus the decoder skip (mode 1, pre-activation to `pre`
+// when given), BF16 stores. `skip_row` points at the skip values of the
+// tile's first pixel (COUT per pixel), in global or shared memory.
+template <int COUT>
+__device__ __forceinline__ void tc_epilogue(std::uint32_t tmem_acc, int y, int x0, int W, const float* __restrict__ bias,
+                                            int mode, const __nv_bfloat16* skip_row,
+                                            __nv_bfloat16* __restrict__ pre, __nv_bfloat16* __restrict__ out)
+{
+    constexpr int CW = COUT == 16 ? 8 : 16;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int quarter = warp & 3, half = warp >> 2;
+    const int m = quarter * 32 + lane;
+    const int x = x0 + m;
+    const std::int64_t o = (static_cast<std::int64_t>(y) * W + x) * COUT;
+    const std::uint32_t lane_col = tmem_acc + (static_cast<std::uint32_t>(quarter * 32) << 16);
+#pragma unroll
+    for (int n0 = CW * half; n0 < COUT; n0 += 2 * CW)
+    {
+        std::uint32_t r[CW];
+        if constexpr (CW == 8)
+            asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];\n"
+                         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                           "=r"(r[7])
+                         : "r"(lane_col + static_cast<std::uint32_t>(n0)));
+        else
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+                "%14, %15}, [%16];\n"
+                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                  "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                  "=r"(r[15])
+                : "r"(lane_col + static_cast<std::uint32_t>(n0)));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        if (x < W)
+        {
+            alignas(16) __nv_bfloat16 ov[CW];
+            alignas(16) __nv_bfloat16 pv[CW];
+            alignas(16) __nv_bfloat16 sv[CW];
+            if (mode == 1)
+            {
+#pragma unroll
+                for (int k = 0; k < CW; k += 8)
+                    *reinterpret_cast<uint4*>(sv + k) =
+                        *reinterpret_cast<const uint4*>(skip_row + m * COUT + n0 + k);
+            }
+#pragma unroll
+            for (int j = 0; j < CW; ++j)
+            {
+                const float a = __fadd_rn(__uint_as_float(r[j]), bias[n0 + j]);
+                if (mode == 0)
+                    ov[j] = __float2bfloat16_rn(fmaxf(a, 0.f));
+                else
+                {
+                    pv[j] = __float2bfloat16_rn(a);
+                    ov[j] = __float2bfloat16_rn(__fadd_rn(fmaxf(a, 0.f), __bfloat162float(sv[j])));
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < CW; k += 8)
+                *reinterpret_cast<uint4*>(out + o + n0 + k) = *reinterpret_cast<const uint4*>(ov + k);
+            if (mode == 1 && pre)
+            {
+#pragma unroll
+                for (int k = 0; k < CW; k += 8)
+                    *reinterpret_cast<uint4*>(pre + o + n0 + k) = *reinterpret_cast<const uint4*>(pv + k);
+            }
+        }
+    }
+}
+
 // Pipelined over a CTA's tiles: while the tensor core works on tile i, the
 // CTA stages tile i + 1 (second halo buffer) and then drains tile i's
 // accumulator (second TMEM accumulator) through the epilogue.
@@ -350,7 +450,7 @@ __global__ void __launch_bounds__(256) k_conv_tc5(int H, int W, int up, const __
     LSDTT_COUNT();
     using Lt = Tc5Layout<CIN, COUT>;
     extern __shared__ __align__(1024) unsigned char tc5_smem[];
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int tid = threadIdx.x, warp = tid >> 5;
     const std::uint32_t base_s = static_cast<std::uint32_t>(__cvta_generic_to_shared(tc5_smem));
     const std::uint32_t b_s = base_s + Lt::kBOff;
     const std::uint32_t mbar_s = base_s + Lt::kBarOff;  // [0], [8]: per accumulator
@@ -420,57 +520,11 @@ __global__ void __launch_bounds__(256) k_conv_tc5(int H, int W, int up, const __
         // ordered every thread's staging of halo[nxt] before them)
         if (tid == 0 && ntile < tiles)
             tc5_issue<CIN, COUT>(tmem + nxt * Lt::kAccCols, base_s + nxt * Lt::kHaloBytes, b_s, mbar_s + 8 * nxt);
-        // epilogue of this tile: warp w reads TMEM lanes 32 (w % 4) ..
-        // (its tile pixels); warps w and w + 4 take alternate 16-column
-        // chunks of the accumulator
-        const int y = tile / tpr, x0 = (tile % tpr) * kTcM;
-        const int quarter = warp & 3, half = warp >> 2;
-        const int m = quarter * 32 + lane;
-        const int x = x0 + m;
-        const std::int64_t o = (static_cast<std::int64_t>(y) * W + x) * COUT;
-#pragma unroll
-        for (int n0 = 16 * half; n0 < COUT; n0 += 32)
+        // epilogue of this tile
         {
-            std::uint32_t r[16];
-            asm volatile(
-                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
-                "%14, %15}, [%16];\n"
-                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-                  "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
-                  "=r"(r[15])
-                : "r"(tmem + cur * Lt::kAccCols + (static_cast<std::uint32_t>(quarter * 32) << 16) +
-                      static_cast<std::uint32_t>(n0)));
-            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-            if (x < W)
-            {
-                alignas(16) __nv_bfloat16 ov[16];
-                alignas(16) __nv_bfloat16 pv[16];
-                alignas(16) __nv_bfloat16 sv[16];
-                if (mode == 1)
-                {
-                    *reinterpret_cast<uint4*>(sv) = *reinterpret_cast<const uint4*>(skip + o + n0);
-                    *reinterpret_cast<uint4*>(sv + 8) = *reinterpret_cast<const uint4*>(skip + o + n0 + 8);
-                }
-#pragma unroll
-                for (int j = 0; j < 16; ++j)
-                {
-                    const float a = __fadd_rn(__uint_as_float(r[j]), bias[n0 + j]);
-                    if (mode == 0)
-                        ov[j] = __float2bfloat16_rn(fmaxf(a, 0.f));
-                    else
-                    {
-                        pv[j] = __float2bfloat16_rn(a);
-                        ov[j] = __float2bfloat16_rn(__fadd_rn(fmaxf(a, 0.f), __bfloat162float(sv[j])));
-                    }
-                }
-                *reinterpret_cast<uint4*>(out + o + n0) = *reinterpret_cast<const uint4*>(ov);
-                *reinterpret_cast<uint4*>(out + o + n0 + 8) = *reinterpret_cast<const uint4*>(ov + 8);
-                if (mode == 1 && pre)
-                {
-                    *reinterpret_cast<uint4*>(pre + o + n0) = *reinterpret_cast<const uint4*>(pv);
-                    *reinterpret_cast<uint4*>(pre + o + n0 + 8) = *reinterpret_cast<const uint4*>(pv + 8);
-                }
-            }
+            const int ty = tile / tpr, tx0 = (tile % tpr) * kTcM;
+            const __nv_bfloat16* skip_row = mode == 1 ? skip + (static_cast<std::int64_t>(ty) * W + tx0) * COUT : nullptr;
+            tc_epilogue<COUT>(tmem + cur * Lt::kAccCols, ty, tx0, W, bias, mode, skip_row, pre, out);
         }
         // accumulator[cur] and halo[cur] are free once every warp is past here
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -485,11 +539,273 @@ __global__ void __launch_bounds__(256) k_conv_tc5(int H, int W, int up, const __
                      : "memory");
 }
 
+// Rolling-row form of the tcgen05 convolution. Each persistent CTA walks
+// down a vertical segment of one 128-pixel band of the image, so tile y+1
+// needs one new input row (tile y's rows y-1..y+1 hold two of its three).
+// Input rows live in a ring of D + 4 row slots (same per-row layout as
+// k_conv_tc5: CIN/8 chunks of 130 contiguous 16-byte pixel rows); input rows
+// are staged D + 1 rows ahead of the tile that first reads them, so copies,
+// MMAs and the epilogue overlap. Decoder layers (kSkip) stage their skip rows
+// into a second ring. Waits are bounded as in k_conv_tc5.
+__host__ __device__ constexpr int tc6_smem_bytes(int cin, int cout, int d, bool skip)
+{
+    // B (9 taps of cout x cin BF16), input ring, skip ring, barriers
+    return (9 * cout * cin * 2 + 127) / 128 * 128 + (d + 4) * (cin / 8) * kChunkBytes +
+           (skip ? (d + 3) * kTcM * cout * 2 : 0) + 64;
+}
+
+template <int CIN, int COUT, int D, bool kSkip>
+struct Tc6Layout
+{
+    static constexpr int kRing = D + 4;                  // input rows: tile y's three, the next D + 1
+    static constexpr int kSkipRing = kSkip ? D + 3 : 1;  // skip rows: y .. y + D + 1, and one still being read
+    static constexpr int kChunks = CIN / 8;
+    static constexpr int kRowBytes = kChunks * kChunkBytes;
+    static constexpr int kSboB = kChunks * 128;
+    static constexpr int kTapBytes = (COUT / 8) * kSboB;
+    static constexpr int kBBytes = 9 * kTapBytes;
+    static constexpr int kRingOff = (kBBytes + 127) / 128 * 128;
+    static constexpr int kSkipOff = kRingOff + kRing * kRowBytes;  // kSkipRing decoder-skip rows
+    static constexpr int kSkipBytes = kTcM * COUT * 2;
+    static constexpr int kBarOff = kSkipOff + (kSkip ? kSkipRing * kSkipBytes : 0);  // two mbarriers, TMEM address
+    // at least 64 KB, as in Tc5Layout
+    static constexpr int kSmem = (kBarOff + 64) > 65536 ? (kBarOff + 64) : 65536;
+    static constexpr int kAccCols = COUT < 32 ? 32 : COUT;
+    static constexpr int kTmemCols = 2 * kAccCols;
+    static_assert(CIN % 16 == 0 && COUT % 16 == 0 && COUT <= 256, "UMMA shape");
+    static_assert(kBarOff + 64 == tc6_smem_bytes(CIN, COUT, D, kSkip), "layout size");
+    static_assert(kSmem <= 227 * 1024, "shared memory");
+};
+
+template <int R>
+__device__ __forceinline__ int tc6_slot(int row) { return (row + 1) % R; }  // rows >= -1
+
+// Stage input row `row` of the 130-pixel window at x0 - 1 into its slot of
+// an R-slot ring (zero-filled outside the image; nearest upsampling folded
+// in). The caller commits the cp.async group.
+template <int CIN, int R>
+__device__ __forceinline__ void tc6_stage_row(std::uint32_t ring_s, const __nv_bfloat16* __restrict__ in, int H,
+                                              int W, int Win, int up, int row, int x0)
+{
+    constexpr int kCh = CIN / 8;
+    const std::uint32_t slot_s = ring_s + tc6_slot<R>(row) * (kCh * kChunkBytes);
+    const bool row_in = row >= 0 && row < H;
+    const int sy = row_in ? (up ? (row >> 1) : row) : 0;
+    for (int q = threadIdx.x; q < kHaloW * kCh; q += blockDim.x)
+    {
+        const int kc = q % kCh, j = q / kCh;
+        const int xx = x0 - 1 + j;
+        const bool inside = row_in && xx >= 0 && xx < W;
+        const int sx = inside ? (up ? (xx >> 1) : xx) : 0;
+        const __nv_bfloat16* src = in + (static_cast<std::int64_t>(sy) * Win + sx) * CIN + kc * 8;
+        const std::uint32_t dst = slot_s + kc * kChunkBytes + j * 16;
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(inside ? 16 : 0)
+                     : "memory");
+    }
+}
+
+// Stage the decoder-skip values of output row `row` (128 pixels at x0,
+// COUT channels each, zero past the image edge) into slot row % S of an
+// S-slot ring. Issued ahead of the row's epilogue, which then reads the
+// values from shared memory.
+template <int COUT, int S>
+__device__ __forceinline__ void tc6_stage_skip(std::uint32_t skip_s, const __nv_bfloat16* __restrict__ skip, int W,
+                                               int row, int x0)
+{
+    constexpr int kCh = COUT / 8;
+    const std::uint32_t slot_s = skip_s + (row % S) * (kTcM * COUT * 2);
+    for (int q = threadIdx.x; q < kTcM * kCh; q += blockDim.x)
+    {
+        const int c = q % kCh, m = q / kCh;
+        const int x = x0 + m;
+        const bool inside = x < W;
+        const __nv_bfloat16* src = skip + (static_cast<std::int64_t>(row) * W + (inside ? x : 0)) * COUT + c * 8;
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(slot_s + m * (COUT * 2) + c * 16),
+                     "l"(src), "r"(inside ? 16 : 0)
+                     : "memory");
+    }
+}
+
+// The 9 x CIN/16 UMMAs of output row y (input rows y-1..y+1 in the ring)
+// into accumulator column `tmem_acc`, committed to `mbar_s` (one thread).
+template <int CIN, int COUT, int D, bool kSkip>
+__device__ __forceinline__ void tc6_issue(std::uint32_t tmem_acc, std::uint32_t ring_s, std::uint32_t b_s, int y,
+                                          std::uint32_t mbar_s)
+{
+    using Lt = Tc6Layout<CIN, COUT, D, kSkip>;
+    constexpr std::uint32_t idesc = tc5_idesc<COUT>();
+    std::uint32_t accum = 0;
+#pragma unroll 1
+    for (int t = 0; t < 9; ++t)
+    {
+        const int dy = t / 3, dx = t - dy * 3;
+        const std::uint32_t row_s = ring_s + tc6_slot<Lt::kRing>(y + dy - 1) * Lt::kRowBytes;
+#pragma unroll
+        for (int ks = 0; ks < CIN / 16; ++ks)
+        {
+            const std::uint64_t ad = tc5_desc(row_s + 2 * ks * kChunkBytes + dx * 16, kChunkBytes, 128);
+            const std::uint64_t bd = tc5_desc(b_s + t * Lt::kTapBytes + 2 * ks * 128, 128, Lt::kSboB);
+            asm volatile(
+                "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_acc),
+                "l"(ad), "l"(bd), "r"(idesc), "r"(accum)
+                : "memory");
+            accum = 1;
+        }
+    }
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar_s)
+                 : "memory");
+}
+
+// Per output row y of a CTA's segment [y0, y1): stage the input row tile
+// y+D+1 will need and the skip row of tile y+D+1, make sure tile y+1's rows
+// have landed, issue tile y+1's MMAs into the other accumulator, wait for
+// tile y's MMAs and drain them. Copies run D rows ahead (D + 1 cp.async
+// groups in flight). An input slot is restaged only after the MMAs that read
+// it completed (tile y's MMAs read rows y-1..y+1, and row y+D+2 goes to row
+// y-2's slot); a skip slot only after every thread passed the barrier that
+// follows its last epilogue.
+template <int CIN, int COUT, int D, bool kSkip>
+__global__ void __launch_bounds__(256) k_conv_tc6(int H, int W, int up, const __nv_bfloat16* __restrict__ in,
+                                                  const __nv_bfloat16* __restrict__ wpk,
+                                                  const float* __restrict__ bias, int mode,
+                                                  const __nv_bfloat16* __restrict__ skip,
+                                                  __nv_bfloat16* __restrict__ pre, __nv_bfloat16* __restrict__ out,
+                                                  unsigned* __restrict__ err)
+{
+    LSDTT_COUNT();
+    using Lt = Tc6Layout<CIN, COUT, D, kSkip>;
+    constexpr int R = Lt::kRing, S = Lt::kSkipRing;
+    extern __shared__ __align__(1024) unsigned char tc6_smem[];
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const std::uint32_t base_s = static_cast<std::uint32_t>(__cvta_generic_to_shared(tc6_smem));
+    const std::uint32_t b_s = base_s;
+    const std::uint32_t ring_s = base_s + Lt::kRingOff;
+    const std::uint32_t mbar_s = base_s + Lt::kBarOff;  // [0], [8]: per accumulator
+    const std::uint32_t tslot_s = mbar_s + 16;
+    const std::uint32_t* tslot = reinterpret_cast<const std::uint32_t*>(tc6_smem + Lt::kBarOff + 16);
+
+    for (int q = tid; q < 9 * COUT * Lt::kChunks; q += blockDim.x)
+    {
+        const int kc = q % Lt::kChunks;
+        const int rest = q / Lt::kChunks;
+        const int n = rest % COUT, t = rest / COUT;
+        const uint4 v = *reinterpret_cast<const uint4*>(wpk + (static_cast<std::int64_t>(n) * 9 + t) * CIN + kc * 8);
+        *reinterpret_cast<uint4*>(tc6_smem + t * Lt::kTapBytes + (n >> 3) * Lt::kSboB + kc * 128 + (n & 7) * 16) = v;
+    }
+    if (warp == 0)
+    {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tslot_s),
+                     "r"(Lt::kTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0)
+    {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar_s) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar_s + 8) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const std::uint32_t tmem = *tslot;
+    const int Win = up ? (W >> 1) : W;
+    const int nb = (W + kTcM - 1) / kTcM;                                   // 128-pixel bands
+    const int segs = max(1, static_cast<int>(gridDim.x) / nb);  // row segments per band: one item per CTA
+    const int rps = (H + segs - 1) / segs;
+    const int items = nb * segs;
+    const std::uint32_t skip_s = base_s + Lt::kSkipOff;
+    const bool has_skip = kSkip && mode == 1;
+    std::uint32_t phase[2] = {0u, 0u};
+    bool failed = false;
+    for (int item = blockIdx.x; item < items && !failed; item += gridDim.x)
+    {
+        const int x0 = (item % nb) * kTcM;
+        const int y0 = (item / nb) * rps, y1 = min(H, y0 + rps);
+        if (y0 >= y1) continue;  // block-uniform
+        // every thread is past the last item's epilogue (skip slots) before
+        // this item's staging
+        __syncthreads();
+        // prologue: group 0 = rows y0-1 .. y0+1 and skip row y0 (tile y0);
+        // group k = 1..D: row y0+k+1 and skip row y0+k (tile y0+k)
+        for (int r = y0 - 1; r <= y0 + 1; ++r) tc6_stage_row<CIN, R>(ring_s, in, H, W, Win, up, r, x0);
+        if (has_skip) tc6_stage_skip<COUT, S>(skip_s, skip, W, y0, x0);
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+#pragma unroll
+        for (int k = 1; k <= D; ++k)
+        {
+            if (y0 + k < y1)
+            {
+                tc6_stage_row<CIN, R>(ring_s, in, H, W, Win, up, y0 + k + 1, x0);
+                if (has_skip) tc6_stage_skip<COUT, S>(skip_s, skip, W, y0 + k, x0);
+            }
+            asm volatile("cp.async.commit_group;\n" ::: "memory");
+        }
+        asm volatile("cp.async.wait_group %0;\n" ::"n"(D) : "memory");  // group 0
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        if (tid == 0) tc6_issue<CIN, COUT, D, kSkip>(tmem, ring_s, b_s, y0, mbar_s);
+        for (int y = y0; y < y1; ++y)
+        {
+            const int cur = (y - y0) & 1, nxt = cur ^ 1;
+            // input row y+D+2 goes to the slot of row y-2 (tile y-1's MMAs
+            // completed), skip row y+D+1 to the slot row y-2's epilogue read
+            // (every thread passed the barrier below since)
+            if (y + D + 1 < y1)
+            {
+                tc6_stage_row<CIN, R>(ring_s, in, H, W, Win, up, y + D + 2, x0);
+                if (has_skip) tc6_stage_skip<COUT, S>(skip_s, skip, W, y + D + 1, x0);
+            }
+            asm volatile("cp.async.commit_group;\n" ::: "memory");
+            // the group holding row y+2 (tile y+1) and skip row y+1, and all
+            // before it, have landed
+            asm volatile("cp.async.wait_group %0;\n" ::"n"(D) : "memory");
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            // every thread's copies, and the last epilogue's reads of the
+            // other accumulator, are ordered before tile y+1's MMAs
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncthreads();
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const bool more = y + 1 < y1;
+            if (tid == 0 && more)
+                tc6_issue<CIN, COUT, D, kSkip>(tmem + nxt * Lt::kAccCols, ring_s, b_s, y + 1, mbar_s + 8 * nxt);
+            const bool ok = tc5_wait(mbar_s + 8 * cur, phase[cur]);
+            if (__syncthreads_or(ok ? 0 : 1))  // block-uniform: every thread leaves together
+            {
+                if (tid == 0) atomicOr(err, 1u);
+                if (!ok) tc5_wait(mbar_s + 8 * cur, phase[cur]);  // once more for the MMAs in flight
+                if (more) tc5_wait(mbar_s + 8 * nxt, phase[nxt]);
+                failed = true;
+                break;
+            }
+            phase[cur] ^= 1u;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            tc_epilogue<COUT>(tmem + cur * Lt::kAccCols, y, x0, W, bias, mode,
+                              reinterpret_cast<const __nv_bfloat16*>(tc6_smem + Lt::kSkipOff +
+                                                                     (y % S) * Lt::kSkipBytes),
+                              pre, out);
+        }
+    }
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(Lt::kTmemCols)
+                     : "memory");
+}
+
 // Output layer: 16 -> 1 channel, times rms, FP32.
-__global__ void k_conv_out(int H, int W, const __nv_bfloat16* __restrict__ d0, const float* __restrict__ w,
+__global__ void k_conv_out(int H, int W, const __nv_bfloat16* __restrict__ d0, const float* __restrict__ wg,
                            const float* __restrict__ b, const float* __restrict__ rms, float* __restrict__ y)
 {
     LSDTT_COUNT();
+    __shared__ float w[9 * 16];
+    for (int k = threadIdx.x; k < 9 * 16; k += blockDim.x) w[k] = wg[k];
+    __syncthreads();
     const std::int64_t p = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (p >= static_cast<std::int64_t>(H) * W) return;
     const int py = static_cast<int>(p / W), px = static_cast<int>(p % W);
@@ -707,7 +1023,7 @@ struct lsdtt_gpu_unet
     std::int64_t woff[kLayers + 1] = {};  // weight offsets into the parameter vector
     std::int64_t boff[kLayers + 1] = {};  // bias offsets
     std::int64_t nparam = 0;
-    int conv_kind = 1;          // 0: mma.sync convolutions, 1: tcgen05 (default)
+    int conv_kind = 2;          // 0: mma.sync, 1: tcgen05 tiles, 2: tcgen05 rolling rows (default)
     unsigned* d_err = nullptr;  // device error word of the tcgen05 kernels
     float* w = nullptr;   // FP32 master: weights then biases
     float* wr = nullptr;  // bf16-rounded copy as FP32 (CUDA-core layers, backward)
@@ -753,6 +1069,28 @@ int check_shape(const lsdtt_gpu_unet* U, int H, int W)
     return LSDTT_GPU_OK;
 }
 
+// CTAs of `func` (256 threads, `smem` dynamic bytes, carveout set to all
+// shared memory) that one SM holds at once, from the device limits and the
+// function's registers, capped by the TMEM columns every resident CTA keeps
+// for its whole life. (Computed directly: the occupancy query was seen to
+// answer one CTA for these kernels where three were resident.)
+static int resident_ctas(const void* func, int smem, int tmem_cols)
+{
+    int dev = 0, smem_sm = 0, reserved = 0, regs_sm = 0, threads_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+    cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
+    cudaDeviceGetAttribute(&threads_sm, cudaDevAttrMaxThreadsPerMultiProcessor, dev);
+    cudaFuncAttributes fa{};
+    if (cudaFuncGetAttributes(&fa, func) != cudaSuccess) return 1;
+    const int per_warp_regs = (fa.numRegs * 32 + 255) / 256 * 256;  // allocation unit: 256 registers a warp
+    int n = std::min(threads_sm / 256, regs_sm / std::max(1, per_warp_regs * 8));
+    n = std::min(n, smem_sm / std::max(1, smem + static_cast<int>(fa.sharedSizeBytes) + reserved));
+    n = std::min(n, 512 / tmem_cols);
+    return std::max(1, n);
+}
+
 // Persistent grid of the tcgen05 kernel: every SM, as many CTAs as fit.
 template <int CI, int CO>
 unsigned tc5_grid(int tiles)
@@ -762,20 +1100,65 @@ unsigned tc5_grid(int tiles)
     {
         cudaFuncSetAttribute(k_conv_tc5<CI, CO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              Tc5Layout<CI, CO>::kSmem);
+        // the whole unified L1/shared array as shared memory, so that several
+        // CTAs (each holding its TMEM columns) share an SM
+        cudaFuncSetAttribute(k_conv_tc5<CI, CO>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             cudaSharedmemCarveoutMaxShared);
         int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_conv_tc5<CI, CO>, 256, Tc5Layout<CI, CO>::kSmem);
-        // every resident CTA holds its TMEM columns for its whole life
-        per_sm = std::min(per_sm, 512 / Tc5Layout<CI, CO>::kTmemCols);
-        if (per_sm < 1) per_sm = 1;
+        per_sm = resident_ctas(reinterpret_cast<const void*>(k_conv_tc5<CI, CO>), Tc5Layout<CI, CO>::kSmem,
+                               Tc5Layout<CI, CO>::kTmemCols);
     }
     return static_cast<unsigned>(std::max(1, std::min(tiles, sms * per_sm)));
 }
 
-void launch_conv_tc(const lsdtt_gpu_unet* U, int l, int H, int W, int up, const __nv_bfloat16* in,
-                    const __nv_bfloat16* wpk, const float* b, int mode, const __nv_bfloat16* skip,
-                    __nv_bfloat16* pre, __nv_bfloat16* out, cudaStream_t st)
+// Persistent grid of the rolling-row tcgen05 kernel (same rule).
+template <int CI, int CO, int D, bool SK>
+unsigned tc6_grid(int H, int W)
+{
+    using Lt = Tc6Layout<CI, CO, D, SK>;
+    static int per_sm = -1, sms = 0;
+    if (per_sm < 0)
+    {
+        cudaFuncSetAttribute(k_conv_tc6<CI, CO, D, SK>, cudaFuncAttributeMaxDynamicSharedMemorySize, Lt::kSmem);
+        cudaFuncSetAttribute(k_conv_tc6<CI, CO, D, SK>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             cudaSharedmemCarveoutMaxShared);
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        per_sm = resident_ctas(reinterpret_cast<const void*>(k_conv_tc6<CI, CO, D, SK>), Lt::kSmem, Lt::kTmemCols);
+    }
+    // at most one CTA per band row-segment of three or more rows
+    const int nb = (W + kTcM - 1) / kTcM;
+    const int most = std::max(1, nb * std::max(1, H / 3));
+    return static_cast<unsigned>(std::max(1, std::min(most, sms * per_sm)));
+}
+
+// Rolling-row launch with prefetch depth D: the skip ring only for decoder
+// layers (mode 1). (At 4096^2, D = 1 with three CTAs an SM ran the network
+// faster than the deepest prefetch that fits, which costs CTAs per SM.)
+template <int CI, int CO, int D>
+void launch_tc6(int H, int W, int up, const __nv_bfloat16* in, const __nv_bfloat16* wpk, const float* b, int mode,
+                const __nv_bfloat16* skip, __nv_bfloat16* pre, __nv_bfloat16* out, unsigned* err, double bytes,
+                cudaStream_t st)
+{
+    constexpr int DS = D, DN = D;
+    if (mode == 1)
+        LSDTT_TIMED("unet_conv_tc6", bytes, st,
+                    (k_conv_tc6<CI, CO, DS, true><<<tc6_grid<CI, CO, DS, true>(H, W), 256,
+                                                    Tc6Layout<CI, CO, DS, true>::kSmem, st>>>(
+                        H, W, up, in, wpk, b, mode, skip, pre, out, err)));
+    else
+        LSDTT_TIMED("unet_conv_tc6", bytes, st,
+                    (k_conv_tc6<CI, CO, DN, false><<<tc6_grid<CI, CO, DN, false>(H, W), 256,
+                                                     Tc6Layout<CI, CO, DN, false>::kSmem, st>>>(
+                        H, W, up, in, wpk, b, mode, skip, pre, out, err)));
+}
+
+static void launch_conv_kind(const lsdtt_gpu_unet* U, int l, int H, int W, int up, const __nv_bfloat16* in,
+                             const __nv_bfloat16* wpk, const float* b, int mode, const __nv_bfloat16* skip,
+                             __nv_bfloat16* pre, __nv_bfloat16* out, cudaStream_t st)
 {
     const int warps = H * ((W + 15) / 16);
     const unsigned blocks = static_cast<unsigned>((warps + 3) / 4);
@@ -784,7 +1167,9 @@ void launch_conv_tc(const lsdtt_gpu_unet* U, int l, int H, int W, int up, const 
 #define LSDTT_CONV_CASE(CI, CO)                                                                                     \
     if (layer_cin(l) == CI && layer_cout(l) == CO)                                                                  \
     {                                                                                                               \
-        if (unet_conv_kind(U) == 1)                                                                                 \
+        if (unet_conv_kind(U) == 2)                                                                                 \
+            launch_tc6<CI, CO, 1>(H, W, up, in, wpk, b, mode, skip, pre, out, unet_err(U), bytes, st);             \
+        else if (unet_conv_kind(U) == 1)                                                                            \
             LSDTT_TIMED("unet_conv_tc5", bytes, st,                                                                 \
                         (k_conv_tc5<CI, CO><<<tc5_grid<CI, CO>(tiles), 256, Tc5Layout<CI, CO>::kSmem, st>>>(       \
                             H, W, up, in, wpk, b, mode, skip, pre, out, unet_err(U))));                            \
@@ -801,6 +1186,18 @@ void launch_conv_tc(const lsdtt_gpu_unet* U, int l, int H, int W, int up, const 
 #undef LSDTT_CONV_CASE
 }
 
+// Tensor-core layer l, timed under its own name as well when profiling is
+// on (algorithmic bytes: input read once, output written once).
+void launch_conv_tc(const lsdtt_gpu_unet* U, int l, int H, int W, int up, const __nv_bfloat16* in,
+                    const __nv_bfloat16* wpk, const float* b, int mode, const __nv_bfloat16* skip,
+                    __nv_bfloat16* pre, __nv_bfloat16* out, cudaStream_t st)
+{
+    static const char* const kName[7] = {"", "unet_layer1", "unet_layer2", "unet_layer3",
+                                         "unet_layer4", "unet_layer5", "unet_layer6"};
+    const double bytes = 2.0 * static_cast<double>(H) * W * (layer_cin(l) / (up ? 4.0 : 1.0) + layer_cout(l));
+    LSDTT_TIMED(kName[l], bytes, st, launch_conv_kind(U, l, H, W, up, in, wpk, b, mode, skip, pre, out, st));
+}
+
 // Forward pass on an H x W residual (device, FP32) -> U->y. Without
 // `for_training` the decoder pre-activations (needed only by the backward
 // pass) are not stored.
@@ -808,8 +1205,12 @@ cudaError_t unet_forward(lsdtt_gpu_unet* U, const float* r, int H, int W, cudaSt
 {
     const std::int64_t n = static_cast<std::int64_t>(H) * W;
     cudaMemsetAsync(U->acc, 0, sizeof(double), st);
-    k_sumsq<<<152 * 4, 256, 0, st>>>(r, n, U->acc);
-    k_prep<<<grid_blocks(n, 256), 256, 0, st>>>(r, n, U->acc, U->x0, U->rms);
+    // Algorithmic bytes: r 4 in (twice), x0 2 out per pixel.
+    LSDTT_TIMED("unet_prep", 10.0 * static_cast<double>(n), st, ({
+                    k_sumsq<<<152 * 4, 256, 0, st>>>(r, n, U->acc);
+                    k_rms<<<1, 1, 0, st>>>(n, U->acc, U->rms);
+                    k_prep<<<grid_blocks(n, 256), 256, 0, st>>>(r, n, U->rms, U->x0);
+                }));
     const float* wr = U->wr;
     // Algorithmic bytes: x0 2 in, e0 32 out per pixel.
     LSDTT_TIMED("unet_conv_in", 34.0 * static_cast<double>(n), st,
@@ -817,14 +1218,18 @@ cudaError_t unet_forward(lsdtt_gpu_unet* U, const float* r, int H, int W, cudaSt
                                                                  U->e0)));
     int h = H / 2, w = W / 2;
     LSDTT_TIMED("unet_pool", 40.0 * static_cast<double>(h) * w * 4, st,
-                (k_pool<<<grid_blocks(static_cast<std::int64_t>(h) * w * 16, 256), 256, 0, st>>>(h, w, 16, U->e0,
+                (k_pool<<<grid_blocks(static_cast<std::int64_t>(h) * w * 2, 256), 256, 0, st>>>(h, w, 16, U->e0,
                                                                                                   U->p0)));
     launch_conv_tc(U, 1, h, w, 0, U->p0, U->wb + U->woff[1], U->w + U->boff[1], 0, nullptr, nullptr, U->e1, st);
     h /= 2; w /= 2;
-    k_pool<<<grid_blocks(static_cast<std::int64_t>(h) * w * 32, 256), 256, 0, st>>>(h, w, 32, U->e1, U->p1);
+    LSDTT_TIMED("unet_pool", 80.0 * static_cast<double>(h) * w * 4, st,
+                (k_pool<<<grid_blocks(static_cast<std::int64_t>(h) * w * 4, 256), 256, 0, st>>>(h, w, 32, U->e1,
+                                                                                                  U->p1)));
     launch_conv_tc(U, 2, h, w, 0, U->p1, U->wb + U->woff[2], U->w + U->boff[2], 0, nullptr, nullptr, U->e2, st);
     h /= 2; w /= 2;
-    k_pool<<<grid_blocks(static_cast<std::int64_t>(h) * w * 64, 256), 256, 0, st>>>(h, w, 64, U->e2, U->p2);
+    LSDTT_TIMED("unet_pool", 160.0 * static_cast<double>(h) * w * 4, st,
+                (k_pool<<<grid_blocks(static_cast<std::int64_t>(h) * w * 8, 256), 256, 0, st>>>(h, w, 64, U->e2,
+                                                                                                  U->p2)));
     launch_conv_tc(U, 3, h, w, 0, U->p2, U->wb + U->woff[3], U->w + U->boff[3], 0, nullptr, nullptr, U->e3, st);
     launch_conv_tc(U, 4, H / 4, W / 4, 1, U->e3, U->wb + U->woff[4], U->w + U->boff[4], 1, U->e2,
                    for_training ? U->a2 : nullptr, U->d2, st);
@@ -1018,7 +1423,7 @@ int64_t lsdtt_gpu_unet_num_params(const lsdtt_gpu_unet* U) { return U ? U->npara
 
 int lsdtt_gpu_unet_set_conv_kernel(lsdtt_gpu_unet* U, int32_t kind)
 {
-    if (!U || (kind != 0 && kind != 1)) return fail(LSDTT_GPU_EINVAL, "lsdtt_gpu_unet_set_conv_kernel: bad argument");
+    if (!U || kind < 0 || kind > 2) return fail(LSDTT_GPU_EINVAL, "lsdtt_gpu_unet_set_conv_kernel: bad argument");
     U->conv_kind = kind;
     return LSDTT_GPU_OK;
 }
