@@ -711,10 +711,12 @@ def hillslope_gpu(args, rank, world):
         m = np.ones_like(z, np.uint8)
         for form in ("plain", "learned"):
             torch.cuda.synchronize()
+            torch.cuda.nvtx.range_push("hillslope_" + form)  # lets an ncu capture select one solve
             t0 = time.perf_counter()
             zo, rep = G.hillslope_implicit(z, m, 5.0, "oooo", 0.01, 1.0, dt, nonlinear=True, rel_tol=1e-8,
                                            max_pcg_iter=20000, net=net if form == "learned" else None)
             torch.cuda.synchronize()
+            torch.cuda.nvtx.range_pop()
             res.setdefault(form, []).append({"s": time.perf_counter() - t0, **rep.as_dict()})
             res.setdefault(form + "_z", []).append(zo)
     diffs = [float(((a - b).abs().max()).item()) for a, b in zip(res.pop("plain_z"), res.pop("learned_z"))]

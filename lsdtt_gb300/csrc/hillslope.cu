@@ -41,7 +41,18 @@ __global__ void hs_setup(Hs H, const std::uint8_t* __restrict__ mask, const std:
     {
         const int r = static_cast<int>(i / H.nc), c = static_cast<int>(i % H.nc);
         const bool is_dof = mask[i] && !(chan && chan[i]) && !hs_dirichlet_edge(H, r, c);
-        dof[i] = is_dof ? 1 : 0;
+        // 3: a fast cell for the tiled operator (interior, its four
+        // neighbours in the grid and DOFs themselves), 1: any other DOF
+        bool fast = false;
+        if (is_dof && r > 0 && r < H.nr - 1 && c > 0 && c < H.nc - 1)
+        {
+            auto nb_dof = [&](int rr, int cc) {
+                const std::int64_t j = static_cast<std::int64_t>(rr) * H.nc + cc;
+                return mask[j] && !(chan && chan[j]) && !hs_dirichlet_edge(H, rr, cc);
+            };
+            fast = nb_dof(r - 1, c) && nb_dof(r, c + 1) && nb_dof(r + 1, c) && nb_dof(r, c - 1);
+        }
+        dof[i] = is_dof ? (fast ? 3 : 1) : 0;
         if (is_dof)
         {
             const double zp = z[i];
@@ -447,42 +458,323 @@ __global__ void hsn_pcg_init(HsN P, const std::uint8_t* __restrict__ mask, const
     block_atomic_add(&acc[1], bb);
 }
 
-__global__ void hsn_apply(HsN P, const std::uint8_t* __restrict__ mask, const std::uint8_t* __restrict__ dof,
-                          const float4* __restrict__ alpha, const float* __restrict__ p, float* __restrict__ Ap,
-                          double* __restrict__ acc_it)
+// ---- tiled operator and fixed-order reductions of the PCG loops ------------
+// The loops below run the operator over 128 x 32 tiles with the direction
+// (or the network's output) staged in shared memory with a one-cell halo,
+// write one partial per block instead of atomics on a single address, and
+// reduce the partials in one block in a fixed order, which also forms alpha
+// or beta once (FP64 on this part is a narrow pipe: one division per block
+// stalled every block behind its thread 0).
+constexpr int kHsTC = 128, kHsTR = 32;
+constexpr int kHsUpdBlocks = 152 * 8;  // grid of the grid-stride update kernels
+
+inline int hs_tiles(int nr, int nc) { return ((nc + kHsTC - 1) / kHsTC) * ((nr + kHsTR - 1) / kHsTR); }
+
+// FP32 sum over the warp (lane 0 gets it; 32 terms, as block_atomic_add_f).
+__device__ __forceinline__ float warp_sum_f(float v)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Block total of per-warp FP64 sums (lane 0 of each warp holds one), in warp
+// order, stored by thread 0 at dst.
+__device__ __forceinline__ void block_store_d(double v, double* dst)
+{
+    __shared__ double sh_store_d[32];
+    __syncthreads();  // a previous call may still be reading
+    if ((threadIdx.x & 31) == 0) sh_store_d[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        double t = sh_store_d[0];
+        for (int k = 1; k < static_cast<int>(blockDim.x >> 5); ++k) t += sh_store_d[k];
+        *dst = t;
+    }
+}
+
+// Operator value at a cell of the tile: inv_dt x_P + (D/h^2) sum_f alpha_f
+// (x_P - [nb DOF] x_nb) in FP32 (the difference form keeps the operator
+// symmetric: alpha is a property of the face), the faces summed in the order
+// N, E, S, W on both paths. Fast cells (dof 3: interior, all four neighbours
+// DOFs) read the neighbours from the tile; other DOFs resolve them by the
+// boundary rules and `xg` (the global value of a cell).
+template <class XG>
+__device__ __forceinline__ float hs_op_cell(const HsN& P, float inv_dt, float DA, const std::uint8_t* __restrict__ mask,
+                                            const std::uint8_t* __restrict__ dof, const float4* __restrict__ alpha,
+                                            const float (&sx)[kHsTR + 2][132], int lr, int lc, int r, int c,
+                                            std::int64_t i, std::uint8_t kd, XG xg)
+{
+    const float xi = sx[lr][lc];
+    if (kd == 0) return 0.0f;
+    const float4 a = alpha[i];
+    float s = 0.0f;
+    if (kd == 3)
+    {
+        s += a.x * (xi - sx[lr - 1][lc]);
+        s += a.y * (xi - sx[lr][lc + 1]);
+        s += a.z * (xi - sx[lr + 1][lc]);
+        s += a.w * (xi - sx[lr][lc - 1]);
+    }
+    else
+    {
+        const float av[4] = {a.x, a.y, a.z, a.w};
+#pragma unroll
+        for (int f = 0; f < 4; ++f)
+        {
+            const std::int64_t j = hs_nb(P.H, mask, r, c, kDr[f], kDc[f]);
+            if (j == i) continue;
+            s += av[f] * (xi - (dof[j] ? xg(j) : 0.0f));
+        }
+    }
+    return inv_dt * xi + DA * s;
+}
+
+// Stage x over the tile and its one-cell halo (0 outside the grid): warp w
+// loads rows w, w + 8, ...; each lane columns lane, lane + 32, ...
+template <class XG>
+__device__ __forceinline__ void hs_stage_tile(float (&sx)[kHsTR + 2][132], int nr, int nc, int r0, int c0, XG xg)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int lr = w; lr < kHsTR + 2; lr += 8)
+    {
+        const int r = r0 - 1 + lr;
+        const bool row_in = r >= 0 && r < nr;
+        const std::int64_t rb = static_cast<std::int64_t>(r) * nc;
+#pragma unroll
+        for (int k = 0; k < 5; ++k)
+        {
+            const int col = 32 * k + lane;
+            if (col >= 130) continue;
+            const int c = c0 - 1 + col;
+            sx[lr][col] = (row_in && c >= 0 && c < nc) ? xg(rb + c) : 0.0f;
+        }
+    }
+    __syncthreads();
+}
+
+// Ap = A p over one tile per block, part[tile] = p.Ap (FP32 within each
+// 32-cell warp row, FP64 beyond). With kFuse the direction update of the
+// previous iteration, p = z + beta p (beta = scal[1]), is formed while
+// staging: p_src is read, p_dst written.
+template <bool kFuse>
+__global__ void __launch_bounds__(256) hsn_apply_t(HsN P, float inv_dt, float DA, const std::uint8_t* __restrict__ mask,
+                                                   const std::uint8_t* __restrict__ dof,
+                                                   const float4* __restrict__ alpha, const float* __restrict__ scal,
+                                                   const float* __restrict__ zz, const float* __restrict__ p_src,
+                                                   float* __restrict__ p_dst, float* __restrict__ Ap,
+                                                   double* __restrict__ part)
 {
     LSDTT_COUNT();
-    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    const std::int64_t n = static_cast<std::int64_t>(P.H.nr) * P.H.nc;
-    // FP32 difference form inv_dt p_P + (D/h^2) sum_f alpha_f (p_P - [nb DOF]
-    // p_nb). alpha is a property of the face (the same value from both
-    // sides), so the operator stays symmetric.
-    const float inv_dt = static_cast<float>(P.H.inv_dt), DA = static_cast<float>(P.H.DA);
-    float pap = 0.0f;
-    if (i < n)
+    __shared__ float sx[kHsTR + 2][132];
+    const int nr = P.H.nr, nc = P.H.nc;
+    const int ntx = (nc + kHsTC - 1) / kHsTC;
+    const int c0 = (blockIdx.x % ntx) * kHsTC, r0 = (blockIdx.x / ntx) * kHsTR;
+    const float beta = kFuse ? scal[1] : 0.0f;
+    auto pg = [&](std::int64_t k) { return kFuse ? zz[k] + beta * p_src[k] : p_src[k]; };
+    hs_stage_tile(sx, nr, nc, r0, c0, pg);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    double pap_d = 0.0;
+#pragma unroll 1
+    for (int qr = 0; qr < 4; ++qr)
     {
-        float v = 0.0f;
-        if (dof[i])
-        {
-            const int rr = static_cast<int>(i / P.H.nc);
-            const int cc = static_cast<int>(i - static_cast<std::int64_t>(rr) * P.H.nc);
-            const float4 a = alpha[i];
-            const float av[4] = {a.x, a.y, a.z, a.w};
-            const float pi = p[i];
-            float s = 0.0f;
+        const int lr = 1 + w * 4 + qr, r = r0 + lr - 1;
+        if (r >= nr) break;  // warp-uniform
+        const std::int64_t rb = static_cast<std::int64_t>(r) * nc;
 #pragma unroll
-            for (int f = 0; f < 4; ++f)
+        for (int k = 0; k < 4; ++k)
+        {
+            const int lc = 1 + 32 * k + lane, c = c0 + lc - 1;
+            float pap = 0.0f;
+            if (c < nc)
             {
-                const std::int64_t j = hs_nb(P.H, mask, rr, cc, kDr[f], kDc[f]);
-                if (j == i) continue;
-                s += av[f] * (pi - (dof[j] ? p[j] : 0.0f));
+                const std::int64_t i = rb + c;
+                if (kFuse) p_dst[i] = sx[lr][lc];
+                const std::uint8_t kd = dof[i];
+                const float v = hs_op_cell(P, inv_dt, DA, mask, dof, alpha, sx, lr, lc, r, c, i, kd, pg);
+                Ap[i] = v;
+                if (kd) pap = sx[lr][lc] * v;
             }
-            v = inv_dt * pi + DA * s;
-            pap = pi * v;
+            pap = warp_sum_f(pap);
+            if (lane == 0) pap_d += static_cast<double>(pap);
         }
-        Ap[i] = v;
     }
-    block_atomic_add_f(&acc_it[0], pap);
+    block_store_d(pap_d, part + blockIdx.x);
+}
+
+// The smoothing step of the learned preconditioner over one tile per block:
+// y = [DOF] ynet (staged), t = A y, z = y + D^-1 (r - t) into zz; partials
+// part_rz[tile] = r.z and part_roz[tile] = z.(r - r_old). Same arithmetic as
+// masking, applying the operator and smoothing in three passes.
+__global__ void __launch_bounds__(256) hsf_smooth_t(HsN P, float inv_dt, float DA, const std::uint8_t* __restrict__ mask,
+                                                    const std::uint8_t* __restrict__ dof,
+                                                    const float4* __restrict__ alpha, const float* __restrict__ ynet,
+                                                    const float* __restrict__ invd, const float* __restrict__ r,
+                                                    const float* __restrict__ ro, float* __restrict__ zz,
+                                                    double* __restrict__ part_rz, double* __restrict__ part_roz)
+{
+    LSDTT_COUNT();
+    __shared__ float sx[kHsTR + 2][132];
+    const int nr = P.H.nr, nc = P.H.nc;
+    const int ntx = (nc + kHsTC - 1) / kHsTC;
+    const int c0 = (blockIdx.x % ntx) * kHsTC, r0 = (blockIdx.x / ntx) * kHsTR;
+    auto yg = [&](std::int64_t k) { return dof[k] ? ynet[k] : 0.0f; };
+    hs_stage_tile(sx, nr, nc, r0, c0, yg);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    double rz_d = 0.0, roz_d = 0.0;
+#pragma unroll 1
+    for (int qr = 0; qr < 4; ++qr)
+    {
+        const int lr = 1 + w * 4 + qr, rw = r0 + lr - 1;
+        if (rw >= nr) break;  // warp-uniform
+        const std::int64_t rb = static_cast<std::int64_t>(rw) * nc;
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+        {
+            const int lc = 1 + 32 * k + lane, c = c0 + lc - 1;
+            float rz = 0.0f, roz = 0.0f;
+            if (c < nc)
+            {
+                const std::int64_t i = rb + c;
+                const float t = hs_op_cell(P, inv_dt, DA, mask, dof, alpha, sx, lr, lc, rw, c, i, dof[i], yg);
+                const float ri = r[i];
+                const float zi = sx[lr][lc] + invd[i] * (ri - t);
+                zz[i] = zi;
+                rz = ri * zi;
+                roz = zi * (ri - ro[i]);
+            }
+            rz = warp_sum_f(rz);
+            roz = warp_sum_f(roz);
+            if (lane == 0)
+            {
+                rz_d += static_cast<double>(rz);
+                roz_d += static_cast<double>(roz);
+            }
+        }
+    }
+    block_store_d(rz_d, part_rz + blockIdx.x);
+    block_store_d(roz_d, part_roz + blockIdx.x);
+}
+
+// Jacobi-PCG update with alpha = scal[0]: x += alpha p; r -= alpha Ap;
+// zz = D^-1 r; partials part[blk] = r.z, part[G + blk] = r.r (G blocks,
+// grid-stride over 32-cell warp rows).
+__global__ void __launch_bounds__(256) hs_update_g(std::int64_t n, const float* __restrict__ scal,
+                                                  const float* __restrict__ inv_diag, const float* __restrict__ p,
+                                                  const float* __restrict__ Ap, float* __restrict__ x,
+                                                  float* __restrict__ r, float* __restrict__ zz,
+                                                  double* __restrict__ part)
+{
+    LSDTT_COUNT();
+    const float alpha = scal[0];
+    const int lane = threadIdx.x & 31;
+    double rz_d = 0.0, rr_d = 0.0;
+    const std::int64_t stride = static_cast<std::int64_t>(gridDim.x) * blockDim.x;
+    for (std::int64_t b = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + (threadIdx.x & ~31); b < n;
+         b += stride)
+    {
+        const std::int64_t i = b + lane;
+        float rz = 0.0f, rr = 0.0f;
+        if (i < n)
+        {
+            x[i] += alpha * p[i];
+            const float ri = r[i] - alpha * Ap[i];
+            r[i] = ri;
+            const float zi = ri * inv_diag[i];
+            zz[i] = zi;
+            rz = ri * zi;
+            rr = ri * ri;
+        }
+        rz = warp_sum_f(rz);
+        rr = warp_sum_f(rr);
+        if (lane == 0)
+        {
+            rz_d += static_cast<double>(rz);
+            rr_d += static_cast<double>(rr);
+        }
+    }
+    block_store_d(rz_d, part + blockIdx.x);
+    block_store_d(rr_d, part + gridDim.x + blockIdx.x);
+}
+
+// Flexible-PCG update with alpha = scal[0]: x += alpha p; r_old = r;
+// r -= alpha Ap; q = D^-1 r (the network's input); part[blk] = r.r.
+__global__ void __launch_bounds__(256) hsf_update_g(std::int64_t n, const float* __restrict__ scal,
+                                                   const float* __restrict__ invd, const float* __restrict__ p,
+                                                   const float* __restrict__ Ap, float* __restrict__ x,
+                                                   float* __restrict__ r, float* __restrict__ ro,
+                                                   float* __restrict__ q, double* __restrict__ part)
+{
+    LSDTT_COUNT();
+    const float alpha = scal[0];
+    const int lane = threadIdx.x & 31;
+    double rr_d = 0.0;
+    const std::int64_t stride = static_cast<std::int64_t>(gridDim.x) * blockDim.x;
+    for (std::int64_t b = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + (threadIdx.x & ~31); b < n;
+         b += stride)
+    {
+        const std::int64_t i = b + lane;
+        float rr = 0.0f;
+        if (i < n)
+        {
+            x[i] += alpha * p[i];
+            const float r0 = r[i];
+            ro[i] = r0;
+            const float ri = r0 - alpha * Ap[i];
+            r[i] = ri;
+            q[i] = invd[i] * ri;
+            rr = ri * ri;
+        }
+        rr = warp_sum_f(rr);
+        if (lane == 0) rr_d += static_cast<double>(rr);
+    }
+    block_store_d(rr_d, part + blockIdx.x);
+}
+
+// One block: dst[q] = sum of part[q][0 .. count[q]) in a fixed order (each
+// thread a strided run, then the warps' shuffle trees in order), for the
+// quantities with a partial array; then scal = float(num / den) when den > 0
+// (else 0), the PCG step or direction coefficient.
+struct HsRed
+{
+    const double* part[4];
+    int count[4];
+    double* dst[4];
+    const double* num;
+    const double* den;
+    float* scal;
+};
+
+__global__ void __launch_bounds__(512) hs_reduce(HsRed R)
+{
+    LSDTT_COUNT();
+    __shared__ double sh[4][16];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+    {
+        if (!R.part[q]) continue;
+        double s = 0.0;
+        for (int k = threadIdx.x; k < R.count[q]; k += blockDim.x) s += R.part[q][k];
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if (lane == 0) sh[q][w] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        for (int q = 0; q < 4; ++q)
+        {
+            if (!R.part[q]) continue;
+            double t = sh[q][0];
+            for (int k = 1; k < static_cast<int>(blockDim.x >> 5); ++k) t += sh[q][k];
+            *R.dst[q] = t;
+        }
+        if (R.scal)
+        {
+            const double den = *R.den;
+            *R.scal = (den > 0.0) ? static_cast<float>(*R.num / den) : 0.0f;
+        }
+    }
 }
 
 // z_try = z + lambda * dz on DOFs (double)
@@ -514,34 +806,6 @@ __global__ void hsn_to_float(std::int64_t n, const double* __restrict__ a, float
 // [3] z.(r - r_old). beta = z.(r - r_old) / r_old.z_old (Polak-Ribiere),
 // which keeps conjugacy when M^-1 changes from one iteration to the next.
 
-// alpha = rz_prev / pAp; r_old = r; x += alpha p; r -= alpha Ap; acc_out[2] = r.r
-__global__ void hsf_update(std::int64_t n, const double* __restrict__ rz_prev, const double* __restrict__ acc_it,
-                           const float* __restrict__ p, const float* __restrict__ Ap, float* __restrict__ x,
-                           float* __restrict__ r, float* __restrict__ ro, double* __restrict__ acc_out)
-{
-    LSDTT_COUNT();
-    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    __shared__ float s_alpha;
-    if (threadIdx.x == 0)
-    {
-        const double pap = acc_it[0];
-        s_alpha = (pap > 0.0) ? static_cast<float>(*rz_prev / pap) : 0.0f;
-    }
-    __syncthreads();
-    const float alpha = s_alpha;
-    float rr = 0.0f;
-    if (i < n)
-    {
-        x[i] += alpha * p[i];
-        const float r0 = r[i];
-        ro[i] = r0;
-        const float ri = r0 - alpha * Ap[i];
-        r[i] = ri;
-        rr = ri * ri;
-    }
-    block_atomic_add_f(&acc_out[2], rr);
-}
-
 // The network's input: the Jacobi-scaled residual D^-1 r (metres), which
 // carries the local stiffness of the lagged-coefficient operator.
 __global__ void hsf_input(std::int64_t n, const float* __restrict__ invd, const float* __restrict__ r,
@@ -550,51 +814,6 @@ __global__ void hsf_input(std::int64_t n, const float* __restrict__ invd, const 
     LSDTT_COUNT();
     const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i < n) q[i] = invd[i] * r[i];
-}
-
-// y = net output on DOFs, 0 elsewhere
-__global__ void hsf_mask(std::int64_t n, const std::uint8_t* __restrict__ dof, const float* __restrict__ ynet,
-                         float* __restrict__ y)
-{
-    LSDTT_COUNT();
-    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i < n) y[i] = dof[i] ? ynet[i] : 0.0f;
-}
-
-// z = y + D^-1 (r - A y) (t = A y); acc_out[1] = r.z, acc_out[3] = z.(r - r_old)
-__global__ void hsf_smooth(std::int64_t n, const float* __restrict__ invd, const float* __restrict__ r,
-                           const float* __restrict__ ro, const float* __restrict__ t, float* __restrict__ z,
-                           double* __restrict__ acc_out)
-{
-    LSDTT_COUNT();
-    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    float rz = 0.0f, roz = 0.0f;
-    if (i < n)
-    {
-        const float ri = r[i];
-        const float zi = z[i] + invd[i] * (ri - t[i]);
-        z[i] = zi;
-        rz = ri * zi;
-        roz = zi * (ri - ro[i]);  // the Polak-Ribiere numerator, formed per element
-    }
-    block_atomic_add_f(&acc_out[1], rz);
-    block_atomic_add_f(&acc_out[3], roz);
-}
-
-// beta = z.(r - r_old) / rz_old; p = z + beta p (beta = 0 at a restart)
-__global__ void hsf_direction(std::int64_t n, const double* __restrict__ rz_old, const double* __restrict__ acc_new,
-                             const float* __restrict__ z, float* __restrict__ p)
-{
-    LSDTT_COUNT();
-    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    __shared__ float s_beta;
-    if (threadIdx.x == 0)
-    {
-        const double ro = *rz_old;
-        s_beta = (ro > 0.0) ? static_cast<float>(acc_new[3] / ro) : 0.0f;
-    }
-    __syncthreads();
-    if (i < n) p[i] = z[i] + s_beta * p[i];
 }
 
 // Explicit residual res = b - A x, evaluated in FP64 from the FP32 iterate and
@@ -670,8 +889,31 @@ struct HsnBuf
     double *z, *zn, *zt, *F, *acc;
     float4* alpha;
     float *invd, *b, *x, *r, *p, *zz, *Ap, *ro;
+    float* p2;     // the other direction buffer of the fused apply
+    double* part;  // block partials: 4 x tiles, then 2 x kHsUpdBlocks
+    float* scal;   // [0] alpha, [1] beta of the current iteration
     double* hacc;
 };
+
+// Device bytes of p2, the partials and the scalars for an n-cell grid
+// (256-byte aligned pieces).
+inline std::size_t hsn_pcg_bytes(int nr, int nc)
+{
+    const std::size_t n = static_cast<std::size_t>(nr) * nc;
+    return (4 * n + 255) / 256 * 256 +
+           (sizeof(double) * (4 * static_cast<std::size_t>(hs_tiles(nr, nc)) + 2 * kHsUpdBlocks) + 255) / 256 * 256 +
+           256;
+}
+
+template <class Carve>
+void hsn_pcg_carve(HsnBuf& B, int nr, int nc, Carve carve)
+{
+    const std::size_t n = static_cast<std::size_t>(nr) * nc;
+    B.p2 = reinterpret_cast<float*>(carve(4 * n));
+    B.part = reinterpret_cast<double*>(
+        carve(sizeof(double) * (4 * static_cast<std::size_t>(hs_tiles(nr, nc)) + 2 * kHsUpdBlocks)));
+    B.scal = reinterpret_cast<float*>(carve(256));
+}
 
 // Statistics of the linear solves of one hillslope call.
 struct SolveStats
@@ -707,7 +949,11 @@ cudaError_t jacobi_loop(const HsN& P, const std::uint8_t* mask, HsnBuf& B, std::
                         double* rel, const std::vector<int>* snap_at = nullptr, float* x_snap = nullptr,
                         float* r_snap = nullptr, bool check = true)
 {
-    const unsigned nb = grid_blocks(n, 256);
+    const int tiles = hs_tiles(P.H.nr, P.H.nc);
+    const float inv_dt = static_cast<float>(P.H.inv_dt), DA = static_cast<float>(P.H.DA);
+    float* pbuf[2] = {B.p, B.p2};
+    double* part_ap = B.part;
+    double* part_up = B.part + 4 * static_cast<std::size_t>(tiles);
     int it = 0;
     std::size_t next_snap = 0;
     const int kCheck = 4;
@@ -720,10 +966,25 @@ cudaError_t jacobi_loop(const HsN& P, const std::uint8_t* mask, HsnBuf& B, std::
         {
             double* cur = slots + kSlot * it;
             const double* rz_prev = (it == 0) ? rz0 : slots + kSlot * (it - 1) + 1;
-            LSDTT_TIMED("hillslope_apply", 8.0 * static_cast<double>(n), st,
-                        (hsn_apply<<<nb, 256, 0, st>>>(P, mask, B.dof, B.alpha, B.p, B.Ap, cur)));
-            hs_update<<<nb, 256, 0, st>>>(n, rz_prev, cur, B.invd, B.p, B.Ap, B.x, B.r, B.zz, cur);
-            hs_direction<<<nb, 256, 0, st>>>(n, rz_prev, cur + 1, B.zz, B.p);
+            // the direction p = z + beta p of the previous iteration is
+            // formed inside the apply (the first iteration's p is given)
+            float* p = pbuf[it & 1];
+            if (it == 0)
+                LSDTT_TIMED("hillslope_apply", 8.0 * static_cast<double>(n), st,
+                            (hsn_apply_t<false><<<tiles, 256, 0, st>>>(P, inv_dt, DA, mask, B.dof, B.alpha, B.scal,
+                                                                       B.zz, p, p, B.Ap, part_ap)));
+            else
+                LSDTT_TIMED("hillslope_apply", 8.0 * static_cast<double>(n), st,
+                            (hsn_apply_t<true><<<tiles, 256, 0, st>>>(P, inv_dt, DA, mask, B.dof, B.alpha, B.scal,
+                                                                      B.zz, pbuf[(it - 1) & 1], p, B.Ap, part_ap)));
+            // p.Ap, alpha = rz_prev / p.Ap
+            hs_reduce<<<1, 512, 0, st>>>(HsRed{{part_ap, nullptr, nullptr, nullptr}, {tiles, 0, 0, 0},
+                                               {cur, nullptr, nullptr, nullptr}, rz_prev, cur, B.scal});
+            hs_update_g<<<kHsUpdBlocks, 256, 0, st>>>(n, B.scal, B.invd, p, B.Ap, B.x, B.r, B.zz, part_up);
+            // r.z, r.r, beta = r.z / rz_prev
+            hs_reduce<<<1, 512, 0, st>>>(HsRed{{nullptr, part_up, part_up + kHsUpdBlocks, nullptr},
+                                               {0, kHsUpdBlocks, kHsUpdBlocks, 0},
+                                               {nullptr, cur + 1, cur + 2, nullptr}, cur + 1, rz_prev, B.scal + 1});
             while (snap_at && next_snap < snap_at->size() && (*snap_at)[next_snap] == it)
             {
                 cudaMemcpyAsync(x_snap + next_snap * n, B.x, sizeof(float) * n, cudaMemcpyDeviceToDevice, st);
@@ -793,19 +1054,28 @@ cudaError_t hsn_pcg(const HsN& P, const std::uint8_t* mask, HsnBuf& B, std::int6
     }
     // Flexible PCG. Initial slot acc[8..11]; iteration slots from acc + 16.
     const int H = P.H.nr, W = P.H.nc;
-    double* dummy = acc + 6;
-    auto precondition = [&](double* slot) -> cudaError_t {
+    const int tiles = hs_tiles(H, W);
+    const float inv_dt = static_cast<float>(P.H.inv_dt), DA = static_cast<float>(P.H.DA);
+    float* pbuf[2] = {B.p, B.p2};
+    double* part_ap = B.part;
+    double* part_rz = B.part + tiles;
+    double* part_roz = B.part + 2 * static_cast<std::size_t>(tiles);
+    double* part_rr = B.part + 4 * static_cast<std::size_t>(tiles);
+    // z = y + D^-1 (r - A y), y = the network applied to q = D^-1 r (in zz),
+    // masked to the DOFs; partials of r.z and z.(r - r_old)
+    auto precondition = [&]() -> cudaError_t {
         const float* ynet = nullptr;
-        hsf_input<<<nb, 256, 0, st>>>(n, B.invd, B.r, B.zz);
         cudaError_t pe = unet_forward_dev(net, B.zz, H, W, st, &ynet);
         ++S.net_apps;
-        hsf_mask<<<nb, 256, 0, st>>>(n, B.dof, ynet, B.zz);
-        hsn_apply<<<nb, 256, 0, st>>>(P, mask, B.dof, B.alpha, B.zz, B.Ap, dummy);
-        hsf_smooth<<<nb, 256, 0, st>>>(n, B.invd, B.r, B.ro, B.Ap, B.zz, slot);
+        hsf_smooth_t<<<tiles, 256, 0, st>>>(P, inv_dt, DA, mask, B.dof, B.alpha, ynet, B.invd, B.r, B.ro, B.zz,
+                                            part_rz, part_roz);
         return pe;
     };
     cudaMemcpyAsync(B.ro, B.r, sizeof(float) * n, cudaMemcpyDeviceToDevice, st);
-    e = precondition(acc + 8);
+    hsf_input<<<nb, 256, 0, st>>>(n, B.invd, B.r, B.zz);
+    e = precondition();
+    hs_reduce<<<1, 512, 0, st>>>(HsRed{{nullptr, part_rz, nullptr, part_roz}, {0, tiles, 0, tiles},
+                                       {nullptr, acc + 9, nullptr, acc + 11}, nullptr, nullptr, nullptr});
     cudaMemcpyAsync(B.p, B.zz, sizeof(float) * n, cudaMemcpyDeviceToDevice, st);
     int it = 0;
     bool converged = false, broke = false;
@@ -819,11 +1089,24 @@ cudaError_t hsn_pcg(const HsN& P, const std::uint8_t* mask, HsnBuf& B, std::int6
         {
             double* cur = slots + kSlot * it;
             const double* rz_prev = (it == 0) ? acc + 9 : slots + kSlot * (it - 1) + 1;
-            LSDTT_TIMED("hillslope_apply", 8.0 * static_cast<double>(n), st,
-                        (hsn_apply<<<nb, 256, 0, st>>>(P, mask, B.dof, B.alpha, B.p, B.Ap, cur)));
-            hsf_update<<<nb, 256, 0, st>>>(n, rz_prev, cur, B.p, B.Ap, B.x, B.r, B.ro, cur);
-            e = precondition(cur);
-            hsf_direction<<<nb, 256, 0, st>>>(n, rz_prev, cur, B.zz, B.p);
+            // p = z + beta p of the previous iteration inside the apply
+            float* p = pbuf[it & 1];
+            if (it == 0)
+                LSDTT_TIMED("hillslope_apply", 8.0 * static_cast<double>(n), st,
+                            (hsn_apply_t<false><<<tiles, 256, 0, st>>>(P, inv_dt, DA, mask, B.dof, B.alpha, B.scal,
+                                                                       B.zz, p, p, B.Ap, part_ap)));
+            else
+                LSDTT_TIMED("hillslope_apply", 8.0 * static_cast<double>(n), st,
+                            (hsn_apply_t<true><<<tiles, 256, 0, st>>>(P, inv_dt, DA, mask, B.dof, B.alpha, B.scal,
+                                                                      B.zz, pbuf[(it - 1) & 1], p, B.Ap, part_ap)));
+            // p.Ap, alpha = rz_prev / p.Ap
+            hs_reduce<<<1, 512, 0, st>>>(HsRed{{part_ap, nullptr, nullptr, nullptr}, {tiles, 0, 0, 0},
+                                               {cur, nullptr, nullptr, nullptr}, rz_prev, cur, B.scal});
+            hsf_update_g<<<kHsUpdBlocks, 256, 0, st>>>(n, B.scal, B.invd, p, B.Ap, B.x, B.r, B.ro, B.zz, part_rr);
+            e = precondition();
+            // r.z, r.r, z.(r - r_old); beta = z.(r - r_old) / rz_prev (Polak-Ribiere)
+            hs_reduce<<<1, 512, 0, st>>>(HsRed{{nullptr, part_rz, part_rr, part_roz}, {0, tiles, kHsUpdBlocks, tiles},
+                                               {nullptr, cur + 1, cur + 2, cur + 3}, cur + 3, rz_prev, B.scal + 1});
         }
         if (e != cudaSuccess) break;
         cudaMemcpyAsync(B.hacc, slots + kSlot * (it - 1), sizeof(double) * 4, cudaMemcpyDeviceToHost, st);
@@ -919,7 +1202,7 @@ int hillslope_implicit_impl(const std::string& who, const lsdtt_gpu_grid* grid, 
     // Buffers: doubles z, zn, zt, F; float4 alpha; 8 floats; dof; reductions.
     HsnBuf B{};
     const std::size_t need = static_cast<std::size_t>(n) * (4 * 8 + 16 + 8 * 4 + 1) + 64 * 256 +
-                             sizeof(double) * (8 + solve_acc_doubles(kPcg));
+                             sizeof(double) * (8 + solve_acc_doubles(kPcg)) + hsn_pcg_bytes(P.H.nr, P.H.nc);
     char* base = nullptr;
     cudaError_t e = cudaMallocAsync(&base, need, st);
     if (e == cudaSuccess) e = cudaMallocHost(&B.hacc, sizeof(double) * 8);
@@ -950,6 +1233,7 @@ int hillslope_implicit_impl(const std::string& who, const lsdtt_gpu_grid* grid, 
     B.dof = reinterpret_cast<std::uint8_t*>(carve(n));
     B.acc = reinterpret_cast<double*>(carve(sizeof(double) * 8));
     double* acc_it = reinterpret_cast<double*>(carve(sizeof(double) * solve_acc_doubles(kPcg)));
+    hsn_pcg_carve(B, P.H.nr, P.H.nc, carve);
     SolveStats S;
     // DOF mask via the linear set-up kernel (it only needs mask, channels, edges).
     {
@@ -1137,7 +1421,7 @@ extern "C" int lsdtt_gpu_hillslope_capture_pairs(const lsdtt_gpu_grid* grid, con
     const double rtol = rel_tol > 0 ? rel_tol : 1e-8;
     HsnBuf B{};
     const std::size_t need = static_cast<std::size_t>(n) * (2 * 8 + 16 + 8 * 4 + 1) + 64 * 256 +
-                             sizeof(double) * (8 + solve_acc_doubles(kPcg));
+                             sizeof(double) * (8 + solve_acc_doubles(kPcg)) + hsn_pcg_bytes(P.H.nr, P.H.nc);
     char* base = nullptr;
     cudaError_t e = cudaMallocAsync(&base, need, st);
     if (e == cudaSuccess) e = cudaMallocHost(&B.hacc, sizeof(double) * 8);
@@ -1167,6 +1451,7 @@ extern "C" int lsdtt_gpu_hillslope_capture_pairs(const lsdtt_gpu_grid* grid, con
     B.dof = reinterpret_cast<std::uint8_t*>(carve(n));
     B.acc = reinterpret_cast<double*>(carve(sizeof(double) * 8));
     double* acc = reinterpret_cast<double*>(carve(sizeof(double) * solve_acc_doubles(kPcg)));
+    hsn_pcg_carve(B, P.H.nr, P.H.nc, carve);
     hs_setup<<<nb, 256, 0, st>>>(P.H, mask_dev, is_channel_dev, z_dev, z_dev, B.dof, B.invd, B.b, B.F);
     hsn_to_double<<<nb, 256, 0, st>>>(n, z_dev, B.z);
     double ev[3];
