@@ -728,7 +728,8 @@ def hillslope_gpu(args, rank, world):
     G.hillslope_implicit(z, m, 5.0, "oooo", 0.01, 1.0, dt, nonlinear=True, rel_tol=1e-8, max_pcg_iter=20000, net=net)
     torch.cuda.synchronize()
     kernels = {}
-    for name in ("unet_conv_tc5", "unet_conv_tc", "unet_conv_in", "unet_conv_out", "unet_pool", "hillslope_apply"):
+    for name in ["unet_prep", "unet_conv_in", "unet_pool"] + [f"unet_layer{l}" for l in range(1, 7)] + \
+            ["unet_conv_out", "hillslope_apply"]:
         t, k, b = ctypes.c_double(), ctypes.c_int64(), ctypes.c_double()
         G._check(L.lsdtt_gpu_profile_read(name.encode(), ctypes.byref(t), ctypes.byref(k), ctypes.byref(b)))
         if k.value:
@@ -808,7 +809,7 @@ def main():
     ap.add_argument("--members", type=int, default=256)
     ap.add_argument("--sweep-mode", type=int, default=-1, help="ensemble sweep: -1 autotuned, 0 levels, 1 dataflow, 2 cooperative levels, 3 member clusters")
     ap.add_argument("--plain-members", type=int, default=16)
-    ap.add_argument("--conv-kernel", default="", choices=["", "mma", "tcgen05", "tcgen05_rows"],
+    ap.add_argument("--conv-kernel", default="", choices=["", "mma", "tcgen05", "tcgen05_rows", "tcgen05_ws"],
                     help="U-Net convolution kernels (default: the library's)")
     args = ap.parse_args()
     train_preconditioner.conv_kernel = args.conv_kernel  # the inference network's convolutions

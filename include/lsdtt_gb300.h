@@ -221,8 +221,10 @@ int lsdtt_gpu_unet_set_params(lsdtt_gpu_unet* net, const float* params_host, int
 /* Convolution kernels of the 16-64-channel layers: 0 = mma.sync (m16n8k16
  * BF16), 1 = tcgen05 (UMMA M=128, FP32 accumulator in tensor memory, one
  * 3-row halo per 128-pixel tile), 2 = tcgen05 over rolling input rows (each
- * CTA walks down a 128-pixel band, one new input row per tile; the
- * default). 1 and 2 give identical bits. */
+ * CTA walks down a 128-pixel band, one new input row per tile), 3 = the
+ * rolling-row form with producer, MMA and epilogue warps meeting at
+ * mbarriers (the default). Kinds 1-3 also run the 16 -> 1 output layer on
+ * the tensor cores and give identical bits. */
 int lsdtt_gpu_unet_set_conv_kernel(lsdtt_gpu_unet* net, int32_t kind);
 /* LSDTT_GPU_ETIMEOUT when a tcgen05 convolution gave up waiting for its
  * MMAs since the handle was created (the outputs of that call are invalid). */

@@ -608,9 +608,11 @@ class UNet:
         self.n_params = int(L.lsdtt_gpu_unet_num_params(h))
 
     def set_conv_kernel(self, kind: str) -> None:
-        """'mma' (mma.sync m16n8k16), 'tcgen05' (UMMA, accumulator in TMEM) or
-        'tcgen05_rows' (UMMA over rolling input rows)."""
-        _check(lib().lsdtt_gpu_unet_set_conv_kernel(self._h, {"mma": 0, "tcgen05": 1, "tcgen05_rows": 2}[kind]))
+        """'mma' (mma.sync m16n8k16), 'tcgen05' (UMMA, accumulator in TMEM),
+        'tcgen05_rows' (UMMA over rolling input rows) or 'tcgen05_ws' (the
+        rolling-row form with warp-specialised producer, MMA and epilogue
+        roles; the default)."""
+        _check(lib().lsdtt_gpu_unet_set_conv_kernel(self._h, {"mma": 0, "tcgen05": 1, "tcgen05_rows": 2, "tcgen05_ws": 3}[kind]))
 
     def status(self) -> None:
         """Raises if a tensor-core convolution gave up waiting for its MMAs."""

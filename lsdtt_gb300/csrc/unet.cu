@@ -331,6 +331,28 @@ __device__ __forceinline__ void tc5_stage(std::uint32_t halo_s, const __nv_bfloa
     asm volatile("cp.async.commit_group;\n" ::: "memory");
 }
 
+// One kind::f16 UMMA (M = 128) into tmem_acc; `accum` 0 overwrites the
+// accumulator, 1 adds to it.
+__device__ __forceinline__ void umma_f16(std::uint32_t tmem_acc, std::uint64_t ad, std::uint64_t bd,
+                                         std::uint32_t idesc, std::uint32_t accum)
+{
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_acc),
+        "l"(ad), "l"(bd), "r"(idesc), "r"(accum)
+        : "memory");
+}
+
+// A shared-memory descriptor's start field is the byte address >> 4 in its
+// low 14 bits, so a descriptor for an address `off` bytes further on is the
+// same descriptor plus off >> 4 (shared addresses stay below 2^18, so the
+// field never carries). The issuing thread adds constants instead of
+// rebuilding 64-bit descriptors for each of up to 36 UMMAs a tile.
+__device__ __forceinline__ std::uint64_t desc_plus(std::uint64_t d, std::uint32_t off)
+{
+    return d + static_cast<std::uint64_t>(off >> 4);
+}
+
 // Issue the 9 x CIN/16 UMMAs of one tile into accumulator column `acc`, then
 // commit to the tile's barrier (one thread).
 template <int CIN, int COUT>
@@ -339,24 +361,16 @@ __device__ __forceinline__ void tc5_issue(std::uint32_t tmem_acc, std::uint32_t 
 {
     using Lt = Tc5Layout<CIN, COUT>;
     constexpr std::uint32_t idesc = tc5_idesc<COUT>();
-    std::uint32_t accum = 0;
-#pragma unroll 1
+    const std::uint64_t ad0 = tc5_desc(halo_s, kChunkBytes, 128);
+    const std::uint64_t bd0 = tc5_desc(b_s, 128, Lt::kSboB);
+#pragma unroll
     for (int t = 0; t < 9; ++t)
     {
         const int dy = t / 3, dx = t - dy * 3;
 #pragma unroll
         for (int ks = 0; ks < CIN / 16; ++ks)
-        {
-            const std::uint64_t ad =
-                tc5_desc(halo_s + dy * Lt::kRowBytes + 2 * ks * kChunkBytes + dx * 16, kChunkBytes, 128);
-            const std::uint64_t bd = tc5_desc(b_s + t * Lt::kTapBytes + 2 * ks * 128, 128, Lt::kSboB);
-            asm volatile(
-                "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-                "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_acc),
-                "l"(ad), "l"(bd), "r"(idesc), "r"(accum)
-                : "memory");
-            accum = 1;
-        }
+            umma_f16(tmem_acc, desc_plus(ad0, dy * Lt::kRowBytes + 2 * ks * kChunkBytes + dx * 16),
+                     desc_plus(bd0, t * Lt::kTapBytes + 2 * ks * 128), idesc, (t | ks) ? 1u : 0u);
     }
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar_s)
                  : "memory");
@@ -634,24 +648,19 @@ __device__ __forceinline__ void tc6_issue(std::uint32_t tmem_acc, std::uint32_t 
 {
     using Lt = Tc6Layout<CIN, COUT, D, kSkip>;
     constexpr std::uint32_t idesc = tc5_idesc<COUT>();
-    std::uint32_t accum = 0;
-#pragma unroll 1
+    const std::uint64_t bd0 = tc5_desc(b_s, 128, Lt::kSboB);
+    std::uint64_t rowd[3];
+#pragma unroll
+    for (int dy = 0; dy < 3; ++dy)
+        rowd[dy] = tc5_desc(ring_s + tc6_slot<Lt::kRing>(y + dy - 1) * Lt::kRowBytes, kChunkBytes, 128);
+#pragma unroll
     for (int t = 0; t < 9; ++t)
     {
         const int dy = t / 3, dx = t - dy * 3;
-        const std::uint32_t row_s = ring_s + tc6_slot<Lt::kRing>(y + dy - 1) * Lt::kRowBytes;
 #pragma unroll
         for (int ks = 0; ks < CIN / 16; ++ks)
-        {
-            const std::uint64_t ad = tc5_desc(row_s + 2 * ks * kChunkBytes + dx * 16, kChunkBytes, 128);
-            const std::uint64_t bd = tc5_desc(b_s + t * Lt::kTapBytes + 2 * ks * 128, 128, Lt::kSboB);
-            asm volatile(
-                "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-                "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_acc),
-                "l"(ad), "l"(bd), "r"(idesc), "r"(accum)
-                : "memory");
-            accum = 1;
-        }
+            umma_f16(tmem_acc, desc_plus(rowd[dy], 2 * ks * kChunkBytes + dx * 16),
+                     desc_plus(bd0, t * Lt::kTapBytes + 2 * ks * 128), idesc, (t | ks) ? 1u : 0u);
     }
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar_s)
                  : "memory");
@@ -794,6 +803,476 @@ __global__ void __launch_bounds__(256) k_conv_tc6(int H, int W, int up, const __
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(Lt::kTmemCols)
+                     : "memory");
+}
+
+// ---------------------------------------------------------------------------
+// Warp-specialised rolling-row convolution (same UMMAs and epilogue
+// arithmetic as k_conv_tc6, so the same bits). Roles of the 288 threads:
+//   warps 0-3  epilogue: thread m drains TMEM lane m (pixel m of the tile),
+//              all COUT columns, adds bias / ReLU / skip and stores;
+//   warps 4-7  producers: stage input rows (and decoder skip rows) with
+//              cp.async, two groups in flight, and signal each row when it
+//              has landed;
+//   warp 8     MMA: lane 0 issues a tile's UMMAs once its three rows are
+//              full and its accumulator is empty, then frees the oldest row.
+// The roles meet only at mbarriers (full / empty rings for input rows, skip
+// rows and the two accumulators), so copies, MMAs and epilogues of
+// different rows overlap instead of running in lockstep behind block-wide
+// barriers. Every wait is bounded: a role that gives up raises the shared
+// abort flag and the error word, the others leave at their next wait, and
+// the MMA thread waits (bounded) for its last UMMAs before TMEM is freed.
+// ---------------------------------------------------------------------------
+constexpr int kWsThreads = 288;
+
+// Tiles the MMA warp issues together: their UMMA chains interleave into G
+// accumulators. A tile's 9 x CIN/16 UMMAs accumulate into one TMEM column
+// block one after another, and with N = 16..64 each UMMA is short, so a
+// single chain runs at the accumulation latency, not the tensor pipe's rate;
+// independent chains fill the gaps.
+constexpr int kWsGroup = 1;  // measured: pairs of tiles ran no faster (the A reads from shared memory bound first)
+constexpr int kWsLagDefault = 2;
+
+// Shared bytes of the warp-specialised kernel with producer lag L: L + 2 + G
+// input row slots, L + 2 skip row slots, 2G accumulators.
+__host__ __device__ constexpr int ws_smem_bytes(int cin, int cout, bool skip, int lag, int g)
+{
+    return (9 * cout * cin * 2 + 127) / 128 * 128 + (lag + 2 + g) * (cin / 8) * kChunkBytes +
+           (skip ? (lag + 2) * kTcM * cout * 2 : 0) + 8 * (2 * (lag + 2 + g) + 2 * (lag + 2) + 4 * g + 1) + 16;
+}
+
+// Lag 2 where it fits one CTA's shared memory, else 1 (the ring needs
+// L + 2 + G input slots and L + 2 >= G + L skip slots for the roles never to
+// wait on one another in a cycle).
+__host__ __device__ constexpr int ws_fit_lag(int cin, int cout, bool skip)
+{
+    return ws_smem_bytes(cin, cout, skip, kWsLagDefault, kWsGroup) <= 227 * 1024 ? kWsLagDefault : 1;
+}
+
+template <int CIN, int COUT, bool kSkip, int L = ws_fit_lag(CIN, COUT, kSkip), int G = kWsGroup>
+struct WsLayout
+{
+    static constexpr int kWsLag = L;          // producer cp.async groups in flight
+    static constexpr int kWsRing = L + 2 + G;  // input row slots
+    static constexpr int kWsSkip = L + 2;      // skip row slots
+    static constexpr int kG = G;
+    static constexpr int kAccs = 2 * G;        // accumulators: G being drained, G being computed
+    static constexpr int kChunks = CIN / 8;
+    static constexpr int kRowBytes = kChunks * kChunkBytes;
+    static constexpr int kSboB = kChunks * 128;
+    static constexpr int kTapBytes = (COUT / 8) * kSboB;
+    static constexpr int kBBytes = 9 * kTapBytes;
+    static constexpr int kRingOff = (kBBytes + 127) / 128 * 128;
+    static constexpr int kSkipOff = kRingOff + kWsRing * kRowBytes;
+    static constexpr int kSkipBytes = kTcM * COUT * 2;
+    static constexpr int kBarOff = kSkipOff + (kSkip ? kWsSkip * kSkipBytes : 0);
+    // mbarriers: full_in[R], empty_in[R], full_skip[S], empty_skip[S],
+    // acc_full[2G], acc_empty[2G], done
+    static constexpr int kFullIn = 0, kEmptyIn = kWsRing, kFullSkip = 2 * kWsRing, kEmptySkip = kFullSkip + kWsSkip,
+                         kAccFull = kEmptySkip + kWsSkip, kAccEmpty = kAccFull + kAccs, kDone = kAccEmpty + kAccs,
+                         kBars = kDone + 1;
+    static constexpr int kTmemOff = kBarOff + 8 * kBars;  // TMEM base address, then the abort flag
+    static constexpr int kAbortOff = kTmemOff + 4;
+    static constexpr int kSmem = kAbortOff + 12;
+    static constexpr int kAccCols = COUT < 32 ? 32 : COUT;
+    static constexpr int kTmemCols = kAccs * kAccCols;
+    static_assert(CIN % 16 == 0 && COUT % 16 == 0 && COUT <= 256, "UMMA shape");
+    static_assert(kTmemCols == 64 || kTmemCols == 128 || kTmemCols == 256 || kTmemCols == 512, "TMEM allocation");
+    static_assert(kSmem == ws_smem_bytes(CIN, COUT, kSkip, L, G), "layout size");
+    static_assert(kSmem <= 227 * 1024, "shared memory");
+};
+
+__device__ __forceinline__ void mbar_init(std::uint32_t bar, std::uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(std::uint32_t bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void tc_commit(std::uint32_t bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+                 : "memory");
+}
+
+// Bounded wait for the phase of `bar` with the given parity: at most 2^20
+// tries of at most ~1 us each (the suspend-time hint), so about a second in
+// all; gives up early once another role raised the abort flag. On failure
+// raises it.
+constexpr int kWsSpin = 1 << 20;
+__device__ __forceinline__ bool ws_wait(std::uint32_t bar, std::uint32_t parity, volatile int* abort_flag)
+{
+    for (int spin = 0; spin < kWsSpin; ++spin)
+    {
+        std::uint32_t ok;
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\nselp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(ok)
+            : "r"(bar), "r"(parity), "r"(1000)
+            : "memory");
+        if (ok) return true;
+        if ((spin & 63) == 63 && *abort_flag) return false;
+    }
+    *abort_flag = 1;
+    return false;
+}
+
+// Input row `row` of the 130-pixel window at x0 - 1 into the slot at slot_s
+// (zero outside the image, nearest upsampling folded in), by `nt` threads.
+template <int CIN>
+__device__ __forceinline__ void ws_stage_row(std::uint32_t slot_s, const __nv_bfloat16* __restrict__ in, int H, int W,
+                                             int Win, int up, int row, int x0, int t, int nt)
+{
+    constexpr int kCh = CIN / 8;
+    const bool row_in = row >= 0 && row < H;
+    const int sy = row_in ? (up ? (row >> 1) : row) : 0;
+    for (int q = t; q < kHaloW * kCh; q += nt)
+    {
+        const int kc = q % kCh, j = q / kCh;
+        const int xx = x0 - 1 + j;
+        const bool inside = row_in && xx >= 0 && xx < W;
+        const int sx = inside ? (up ? (xx >> 1) : xx) : 0;
+        const __nv_bfloat16* src = in + (static_cast<std::int64_t>(sy) * Win + sx) * CIN + kc * 8;
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(slot_s + kc * kChunkBytes + j * 16),
+                     "l"(src), "r"(inside ? 16 : 0)
+                     : "memory");
+    }
+}
+
+// Skip values of output row `row` (128 pixels at x0, zero past the edge)
+// into the slot at slot_s, by `nt` threads.
+template <int COUT>
+__device__ __forceinline__ void ws_stage_skip(std::uint32_t slot_s, const __nv_bfloat16* __restrict__ skip, int W,
+                                              int row, int x0, int t, int nt)
+{
+    constexpr int kCh = COUT / 8;
+    for (int q = t; q < kTcM * kCh; q += nt)
+    {
+        const int c = q % kCh, m = q / kCh;
+        const int x = x0 + m;
+        const bool inside = x < W;
+        const __nv_bfloat16* src = skip + (static_cast<std::int64_t>(row) * W + (inside ? x : 0)) * COUT + c * 8;
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(slot_s + m * (COUT * 2) + c * 16),
+                     "l"(src), "r"(inside ? 16 : 0)
+                     : "memory");
+    }
+}
+
+// The UMMAs of g <= G consecutive tiles, interleaved: tile i reads input
+// rows row_s[i .. i+2] and accumulates into column block acc[i]; each
+// tile's 9 x CIN/16 UMMAs keep their order (one thread).
+template <int CIN, int COUT, int G>
+__device__ __forceinline__ void ws_issue_group(std::uint32_t tmem, const std::uint32_t (&acc)[G],
+                                               const std::uint32_t (&row_s)[G + 2], int g, std::uint32_t b_s)
+{
+    using Lt = WsLayout<CIN, COUT, false>;
+    constexpr std::uint32_t idesc = tc5_idesc<COUT>();
+    const std::uint64_t bd0 = tc5_desc(b_s, 128, Lt::kSboB);
+    std::uint64_t rowd[G + 2];
+#pragma unroll
+    for (int k = 0; k < G + 2; ++k) rowd[k] = tc5_desc(row_s[k], kChunkBytes, 128);
+#pragma unroll
+    for (int t = 0; t < 9; ++t)
+    {
+        const int dy = t / 3, dx = t - dy * 3;
+#pragma unroll
+        for (int ks = 0; ks < CIN / 16; ++ks)
+        {
+            const std::uint64_t bd = desc_plus(bd0, t * Lt::kTapBytes + 2 * ks * 128);
+#pragma unroll
+            for (int i = 0; i < G; ++i)
+                if (i < g)
+                    umma_f16(tmem + acc[i], desc_plus(rowd[i + dy], 2 * ks * kChunkBytes + dx * 16), bd, idesc,
+                             (t | ks) ? 1u : 0u);
+        }
+    }
+}
+
+// Epilogue thread of pixel m = 32 warp + lane (warps 0-3): its TMEM lane 16
+// columns at a time, the accumulator handed back to the MMA warp after the
+// last load, the same arithmetic as tc_epilogue. skip_row: the tile's skip
+// values in shared memory (mode 1).
+template <int COUT>
+__device__ __forceinline__ void ws_epilogue(std::uint32_t tmem_acc, int warp, int lane, int y, int x0, int W,
+                                            const float* __restrict__ bias, int mode, const __nv_bfloat16* skip_row,
+                                            __nv_bfloat16* __restrict__ pre, __nv_bfloat16* __restrict__ out,
+                                            std::uint32_t acc_empty, float* __restrict__ yout,
+                                            const float* __restrict__ rms)
+{
+    const int m = warp * 32 + lane;
+    const int x = x0 + m;
+    const std::uint32_t lane_col = tmem_acc + (static_cast<std::uint32_t>(warp * 32) << 16);
+    const std::int64_t o = (static_cast<std::int64_t>(y) * W + x) * COUT;
+#pragma unroll
+    for (int n0 = 0; n0 < COUT; n0 += 16)
+    {
+        std::uint32_t r[16];
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+            "%14, %15}, [%16];\n"
+            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+              "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+            : "r"(lane_col + static_cast<std::uint32_t>(n0)));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        if (n0 + 16 == COUT)
+        {
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            mbar_arrive(acc_empty);
+        }
+        if (x >= W) continue;
+        if (mode == 2)
+        {
+            // output layer: one channel (column 0; the padded weight rows
+            // are zero), plus bias, times the input's rms, FP32
+            if (n0 == 0) yout[static_cast<std::int64_t>(y) * W + x] = __fmul_rn(__fadd_rn(__uint_as_float(r[0]), bias[0]), *rms);
+            continue;
+        }
+        alignas(16) __nv_bfloat16 ov[16];
+        alignas(16) __nv_bfloat16 pv[16];
+        alignas(16) __nv_bfloat16 sv[16];
+        if (mode == 1)
+        {
+            *reinterpret_cast<uint4*>(sv) = *reinterpret_cast<const uint4*>(skip_row + m * COUT + n0);
+            *reinterpret_cast<uint4*>(sv + 8) = *reinterpret_cast<const uint4*>(skip_row + m * COUT + n0 + 8);
+        }
+#pragma unroll
+        for (int j = 0; j < 16; ++j)
+        {
+            const float a = __fadd_rn(__uint_as_float(r[j]), bias[n0 + j]);
+            if (mode == 0)
+                ov[j] = __float2bfloat16_rn(fmaxf(a, 0.f));
+            else
+            {
+                pv[j] = __float2bfloat16_rn(a);
+                ov[j] = __float2bfloat16_rn(__fadd_rn(fmaxf(a, 0.f), __bfloat162float(sv[j])));
+            }
+        }
+        *reinterpret_cast<uint4*>(out + o + n0) = *reinterpret_cast<const uint4*>(ov);
+        *reinterpret_cast<uint4*>(out + o + n0 + 8) = *reinterpret_cast<const uint4*>(ov + 8);
+        if (mode == 1 && pre)
+        {
+            *reinterpret_cast<uint4*>(pre + o + n0) = *reinterpret_cast<const uint4*>(pv);
+            *reinterpret_cast<uint4*>(pre + o + n0 + 8) = *reinterpret_cast<const uint4*>(pv + 8);
+        }
+    }
+}
+
+// Items: 128-pixel bands x row segments, one per CTA where the grid allows
+// (as k_conv_tc6). Within an item, row k is image row y0 - 1 + k (k = 0 ..
+// n + 1 for n tiles) and tile j reads rows j .. j + 2; sequence numbers run
+// on across items, so slot = seq % ring and the phase parity = (seq / ring)
+// & 1. kSkip: decoder layer (mode 1), skip rows staged by the producers.
+template <int CIN, int COUT, bool kSkip>
+__global__ void __launch_bounds__(kWsThreads, CIN == 64 ? 1 : 3) k_conv_ws(int H, int W, int up, const __nv_bfloat16* __restrict__ in,
+                                                        const __nv_bfloat16* __restrict__ wpk,
+                                                        const float* __restrict__ bias, int mode,
+                                                        const __nv_bfloat16* __restrict__ skip,
+                                                        __nv_bfloat16* __restrict__ pre,
+                                                        __nv_bfloat16* __restrict__ out, unsigned* __restrict__ err,
+                                                        float* __restrict__ yout, const float* __restrict__ rms)
+{
+    LSDTT_COUNT();
+    using Lt = WsLayout<CIN, COUT, kSkip>;
+    constexpr int R = Lt::kWsRing, S = Lt::kWsSkip;
+    extern __shared__ __align__(1024) unsigned char ws_smem[];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const std::uint32_t base_s = static_cast<std::uint32_t>(__cvta_generic_to_shared(ws_smem));
+    const std::uint32_t b_s = base_s, ring_s = base_s + Lt::kRingOff, skip_s = base_s + Lt::kSkipOff;
+    const std::uint32_t bar_s = base_s + Lt::kBarOff;
+    auto bar = [&](int k) { return bar_s + 8u * static_cast<std::uint32_t>(k); };
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(ws_smem + Lt::kAbortOff);
+
+    for (int q = tid; q < 9 * COUT * Lt::kChunks; q += blockDim.x)
+    {
+        const int kc = q % Lt::kChunks;
+        const int rest = q / Lt::kChunks;
+        const int n = rest % COUT, t = rest / COUT;
+        const uint4 v = *reinterpret_cast<const uint4*>(wpk + (static_cast<std::int64_t>(n) * 9 + t) * CIN + kc * 8);
+        *reinterpret_cast<uint4*>(ws_smem + t * Lt::kTapBytes + (n >> 3) * Lt::kSboB + kc * 128 + (n & 7) * 16) = v;
+    }
+    // the weights, stored by the generic proxy, are read by the UMMAs
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    if (tid == 0)
+    {
+        for (int k = 0; k < R; ++k)
+        {
+            mbar_init(bar(Lt::kFullIn + k), 128);
+            mbar_init(bar(Lt::kEmptyIn + k), 1);
+        }
+        if (kSkip)
+            for (int k = 0; k < S; ++k)
+            {
+                mbar_init(bar(Lt::kFullSkip + k), 128);
+                mbar_init(bar(Lt::kEmptySkip + k), 128);
+            }
+        for (int k = 0; k < Lt::kAccs; ++k)
+        {
+            mbar_init(bar(Lt::kAccFull + k), 1);
+            mbar_init(bar(Lt::kAccEmpty + k), 128);
+        }
+        mbar_init(bar(Lt::kDone), 1);
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 8)
+    {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(base_s + Lt::kTmemOff),
+                     "r"(Lt::kTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const std::uint32_t tmem = *reinterpret_cast<const std::uint32_t*>(ws_smem + Lt::kTmemOff);
+    const int Win = up ? (W >> 1) : W;
+    const int nb = (W + kTcM - 1) / kTcM;
+    const int segs = max(1, static_cast<int>(gridDim.x) / nb);
+    const int rps = (H + segs - 1) / segs;
+    const int items = nb * segs;
+    bool ok = true;
+
+    if (warp >= 4 && warp < 8)
+    {
+        // producers: row k of an item, and with it (k >= 2) tile k-2's skip
+        // row; step k - L is signalled once its group has landed
+        constexpr int L = Lt::kWsLag;
+        const int pt = tid - 128;
+        std::uint32_t q = 0, u = 0;
+        for (int item = blockIdx.x; item < items && ok; item += gridDim.x)
+        {
+            const int x0 = (item % nb) * kTcM;
+            const int y0 = (item / nb) * rps, y1 = min(H, y0 + rps);
+            if (y0 >= y1) continue;
+            const int n_rows = y1 - y0 + 2;
+            const std::uint32_t qb = q;
+            auto signal = [&](int k) {
+                mbar_arrive(bar(Lt::kFullIn + static_cast<int>((qb + k) % R)));
+                if (kSkip && k >= 2) mbar_arrive(bar(Lt::kFullSkip + static_cast<int>((u + k - 2) % S)));
+            };
+            for (int k = 0; k < n_rows; ++k)
+            {
+                const std::uint32_t qk = qb + static_cast<std::uint32_t>(k);
+                const int slot = static_cast<int>(qk % R);
+                if (qk >= static_cast<std::uint32_t>(R))
+                    ok = ws_wait(bar(Lt::kEmptyIn + slot), ((qk / R) - 1) & 1u, abort_flag);
+                if (!ok) break;
+                ws_stage_row<CIN>(ring_s + slot * Lt::kRowBytes, in, H, W, Win, up, y0 - 1 + k, x0, pt, 128);
+                if (kSkip && k >= 2)
+                {
+                    const std::uint32_t uu = u + static_cast<std::uint32_t>(k - 2);
+                    const int sk = static_cast<int>(uu % S);
+                    if (uu >= static_cast<std::uint32_t>(S))
+                        ok = ws_wait(bar(Lt::kEmptySkip + sk), ((uu / S) - 1) & 1u, abort_flag);
+                    if (ok) ws_stage_skip<COUT>(skip_s + sk * Lt::kSkipBytes, skip, W, y0 + k - 2, x0, pt, 128);
+                }
+                asm volatile("cp.async.commit_group;\n" ::: "memory");
+                if (!ok) break;
+                asm volatile("cp.async.wait_group %0;\n" ::"n"(L) : "memory");
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                if (k >= L) signal(k - L);
+            }
+            asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            if (ok)
+                for (int k = max(0, n_rows - L); k < n_rows; ++k) signal(k);
+            q = qb + static_cast<std::uint32_t>(n_rows);
+            u += static_cast<std::uint32_t>(y1 - y0);
+        }
+        asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    }
+    else if (warp == 8)
+    {
+        if (lane == 0)
+        {
+            // MMA: tiles j .. j+g-1 (g <= G) once rows j .. j+g+1 are full
+            // and their accumulators drained; then rows j .. j+g-1 (tile
+            // j+i is the last reader of row j+i) are freed. Tile u uses
+            // accumulator u % 2G.
+            constexpr int G = Lt::kG, NA = Lt::kAccs;
+            std::uint32_t q = 0, u = 0;
+            for (int item = blockIdx.x; item < items && ok; item += gridDim.x)
+            {
+                const int y0 = (item / nb) * rps, y1 = min(H, y0 + rps);
+                if (y0 >= y1) continue;
+                const int n_tiles = y1 - y0;
+                const std::uint32_t qb = q;
+                std::uint32_t next_row = qb;  // first row not yet waited for
+                for (int j = 0; j < n_tiles && ok; j += G)
+                {
+                    const int g = min(G, n_tiles - j);
+                    for (; next_row <= qb + static_cast<std::uint32_t>(j + g + 1) && ok; ++next_row)
+                        ok = ws_wait(bar(Lt::kFullIn + static_cast<int>(next_row % R)), (next_row / R) & 1u, abort_flag);
+                    std::uint32_t acc[G];
+                    std::uint32_t rows[G + 2];
+#pragma unroll
+                    for (int i = 0; i < G; ++i)
+                    {
+                        const std::uint32_t ui = u + static_cast<std::uint32_t>(i);
+                        acc[i] = static_cast<std::uint32_t>((ui % NA) * Lt::kAccCols);
+                        if (ok && i < g && ui >= static_cast<std::uint32_t>(NA))
+                            ok = ws_wait(bar(Lt::kAccEmpty + static_cast<int>(ui % NA)), ((ui / NA) - 1) & 1u,
+                                         abort_flag);
+                    }
+#pragma unroll
+                    for (int k = 0; k < G + 2; ++k)
+                        rows[k] = ring_s + ((qb + static_cast<std::uint32_t>(j + k)) % R) * Lt::kRowBytes;
+                    if (!ok) break;
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    ws_issue_group<CIN, COUT, G>(tmem, acc, rows, g, b_s);
+                    for (int i = 0; i < g; ++i)
+                        tc_commit(bar(Lt::kAccFull + static_cast<int>((u + static_cast<std::uint32_t>(i)) % NA)));
+                    for (int i = 0; i < g; ++i)
+                        tc_commit(bar(Lt::kEmptyIn + static_cast<int>((qb + static_cast<std::uint32_t>(j + i)) % R)));
+                    u += static_cast<std::uint32_t>(g);
+                }
+                if (!ok) break;
+                tc_commit(bar(Lt::kEmptyIn + static_cast<int>((qb + n_tiles) % R)));
+                tc_commit(bar(Lt::kEmptyIn + static_cast<int>((qb + n_tiles + 1) % R)));
+                q = qb + static_cast<std::uint32_t>(n_tiles + 2);
+            }
+            // every UMMA issued has completed before TMEM is freed
+            tc_commit(bar(Lt::kDone));
+            if (!tc5_wait(bar(Lt::kDone), 0)) ok = false;
+        }
+    }
+    else
+    {
+        // epilogue (warps 0-3)
+        std::uint32_t u = 0;
+        for (int item = blockIdx.x; item < items && ok; item += gridDim.x)
+        {
+            const int x0 = (item % nb) * kTcM;
+            const int y0 = (item / nb) * rps, y1 = min(H, y0 + rps);
+            if (y0 >= y1) continue;
+            for (int y = y0; y < y1; ++y, ++u)
+            {
+                const int a = static_cast<int>(u % Lt::kAccs);
+                ok = ws_wait(bar(Lt::kAccFull + a), (u / Lt::kAccs) & 1u, abort_flag);
+                const int sk = static_cast<int>(u % S);
+                if (ok && kSkip) ok = ws_wait(bar(Lt::kFullSkip + sk), (u / S) & 1u, abort_flag);
+                if (!ok) break;
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                ws_epilogue<COUT>(tmem + a * Lt::kAccCols, warp, lane, y, x0, W, bias, mode,
+                                  reinterpret_cast<const __nv_bfloat16*>(ws_smem + Lt::kSkipOff + sk * Lt::kSkipBytes),
+                                  pre, out, bar(Lt::kAccEmpty + a), yout, rms);
+                if (kSkip) mbar_arrive(bar(Lt::kEmptySkip + sk));
+            }
+        }
+    }
+    if (!ok)
+    {
+        *abort_flag = 1;
+        atomicOr(err, 1u);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (warp == 8)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(Lt::kTmemCols)
                      : "memory");
 }
@@ -997,6 +1476,15 @@ __global__ void k_sgd(std::int64_t n, float* __restrict__ w, const float* __rest
     w[i] -= lr * mi;
 }
 
+// The output layer's weights (1 x 9 x 16, FP32 at w_out) as a 16 x 9 x 16
+// BF16 block whose rows 1..15 are zero, for the UMMA form of that layer.
+__global__ void k_pack_out(const float* __restrict__ w_out, __nv_bfloat16* __restrict__ wb_out)
+{
+    LSDTT_COUNT();
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < 16 * 144) wb_out[i] = __float2bfloat16_rn(i < 144 ? w_out[i] : 0.0f);
+}
+
 __global__ void k_pack(std::int64_t n, const float* __restrict__ w, __nv_bfloat16* __restrict__ wb)
 {
     LSDTT_COUNT();
@@ -1023,7 +1511,10 @@ struct lsdtt_gpu_unet
     std::int64_t woff[kLayers + 1] = {};  // weight offsets into the parameter vector
     std::int64_t boff[kLayers + 1] = {};  // bias offsets
     std::int64_t nparam = 0;
-    int conv_kind = 2;          // 0: mma.sync, 1: tcgen05 tiles, 2: tcgen05 rolling rows (default)
+    std::int64_t wb_out_off = 0;  // BF16 offset of the padded output-layer block in wb (64-element aligned:
+                                  // the convolution kernels read weights with 16-byte loads)
+    int conv_kind = 3;          // 0: mma.sync, 1: tcgen05 tiles, 2: tcgen05 rolling rows, 3: warp-specialised
+                                // rolling rows (default)
     unsigned* d_err = nullptr;  // device error word of the tcgen05 kernels
     float* w = nullptr;   // FP32 master: weights then biases
     float* wr = nullptr;  // bf16-rounded copy as FP32 (CUDA-core layers, backward)
@@ -1069,12 +1560,12 @@ int check_shape(const lsdtt_gpu_unet* U, int H, int W)
     return LSDTT_GPU_OK;
 }
 
-// CTAs of `func` (256 threads, `smem` dynamic bytes, carveout set to all
+// CTAs of `func` (`threads` a CTA, `smem` dynamic bytes, carveout set to all
 // shared memory) that one SM holds at once, from the device limits and the
 // function's registers, capped by the TMEM columns every resident CTA keeps
 // for its whole life. (Computed directly: the occupancy query was seen to
 // answer one CTA for these kernels where three were resident.)
-static int resident_ctas(const void* func, int smem, int tmem_cols)
+static int resident_ctas(const void* func, int smem, int tmem_cols, int threads = 256)
 {
     int dev = 0, smem_sm = 0, reserved = 0, regs_sm = 0, threads_sm = 0;
     cudaGetDevice(&dev);
@@ -1085,7 +1576,7 @@ static int resident_ctas(const void* func, int smem, int tmem_cols)
     cudaFuncAttributes fa{};
     if (cudaFuncGetAttributes(&fa, func) != cudaSuccess) return 1;
     const int per_warp_regs = (fa.numRegs * 32 + 255) / 256 * 256;  // allocation unit: 256 registers a warp
-    int n = std::min(threads_sm / 256, regs_sm / std::max(1, per_warp_regs * 8));
+    int n = std::min(threads_sm / threads, regs_sm / std::max(1, per_warp_regs * ((threads + 31) / 32)));
     n = std::min(n, smem_sm / std::max(1, smem + static_cast<int>(fa.sharedSizeBytes) + reserved));
     n = std::min(n, 512 / tmem_cols);
     return std::max(1, n);
@@ -1135,6 +1626,48 @@ unsigned tc6_grid(int H, int W)
     return static_cast<unsigned>(std::max(1, std::min(most, sms * per_sm)));
 }
 
+// Grid of the warp-specialised kernel (same rule as tc6_grid).
+template <int CI, int CO, bool SK>
+unsigned ws_grid(int H, int W)
+{
+    using Lt = WsLayout<CI, CO, SK>;
+    static int per_sm = -1, sms = 0;
+    if (per_sm < 0)
+    {
+        cudaFuncSetAttribute(k_conv_ws<CI, CO, SK>, cudaFuncAttributeMaxDynamicSharedMemorySize, Lt::kSmem);
+        cudaFuncSetAttribute(k_conv_ws<CI, CO, SK>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             cudaSharedmemCarveoutMaxShared);
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        per_sm = resident_ctas(reinterpret_cast<const void*>(k_conv_ws<CI, CO, SK>), Lt::kSmem, Lt::kTmemCols,
+                               kWsThreads);
+    }
+    const int nb = (W + kTcM - 1) / kTcM;
+    const int most = std::max(1, nb * std::max(1, H / 3));
+    return static_cast<unsigned>(std::max(1, std::min(most, sms * per_sm)));
+}
+
+// mode 0 (encoder), 1 (decoder, skip rows staged) or 2 (the output layer:
+// FP32 y = (column 0 + bias) x rms).
+template <int CI, int CO>
+void launch_ws(int H, int W, int up, const __nv_bfloat16* in, const __nv_bfloat16* wpk, const float* b, int mode,
+               const __nv_bfloat16* skip, __nv_bfloat16* pre, __nv_bfloat16* out, unsigned* err, double bytes,
+               cudaStream_t st, float* yout = nullptr, const float* rms = nullptr)
+{
+    if (mode == 1)
+        LSDTT_TIMED("unet_conv_ws", bytes, st,
+                    (k_conv_ws<CI, CO, true><<<ws_grid<CI, CO, true>(H, W), kWsThreads,
+                                               WsLayout<CI, CO, true>::kSmem, st>>>(H, W, up, in, wpk, b, mode,
+                                                                                    skip, pre, out, err, yout, rms)));
+    else
+        LSDTT_TIMED("unet_conv_ws", bytes, st,
+                    (k_conv_ws<CI, CO, false><<<ws_grid<CI, CO, false>(H, W), kWsThreads,
+                                                WsLayout<CI, CO, false>::kSmem, st>>>(H, W, up, in, wpk, b, mode,
+                                                                                      skip, pre, out, err, yout,
+                                                                                      rms)));
+}
+
 // Rolling-row launch with prefetch depth D: the skip ring only for decoder
 // layers (mode 1). (At 4096^2, D = 1 with three CTAs an SM ran the network
 // faster than the deepest prefetch that fits, which costs CTAs per SM.)
@@ -1167,7 +1700,9 @@ static void launch_conv_kind(const lsdtt_gpu_unet* U, int l, int H, int W, int u
 #define LSDTT_CONV_CASE(CI, CO)                                                                                     \
     if (layer_cin(l) == CI && layer_cout(l) == CO)                                                                  \
     {                                                                                                               \
-        if (unet_conv_kind(U) == 2)                                                                                 \
+        if (unet_conv_kind(U) == 3)                                                                                 \
+            launch_ws<CI, CO>(H, W, up, in, wpk, b, mode, skip, pre, out, unet_err(U), bytes, st);                 \
+        else if (unet_conv_kind(U) == 2)                                                                            \
             launch_tc6<CI, CO, 1>(H, W, up, in, wpk, b, mode, skip, pre, out, unet_err(U), bytes, st);             \
         else if (unet_conv_kind(U) == 1)                                                                            \
             LSDTT_TIMED("unet_conv_tc5", bytes, st,                                                                 \
@@ -1237,10 +1772,17 @@ cudaError_t unet_forward(lsdtt_gpu_unet* U, const float* r, int H, int W, cudaSt
                    for_training ? U->a1 : nullptr, U->d1, st);
     launch_conv_tc(U, 6, H, W, 1, U->d1, U->wb + U->woff[6], U->w + U->boff[6], 1, U->e0,
                    for_training ? U->a0 : nullptr, U->d0, st);
-    // Algorithmic bytes: d0 32 in, y 4 out per pixel.
-    LSDTT_TIMED("unet_conv_out", 36.0 * static_cast<double>(n), st,
-                (k_conv_out<<<grid_blocks(n, 128), 128, 0, st>>>(H, W, U->d0, wr + U->woff[7], U->w + U->boff[7],
-                                                                  U->rms, U->y)));
+    // Algorithmic bytes: d0 32 in, y 4 out per pixel. The tcgen05 kinds run
+    // the 16 -> 1 layer as a 16 -> 16 UMMA convolution with zero weight
+    // rows 1..15 (wb_out), reading column 0.
+    if (unet_conv_kind(U) >= 1)
+        LSDTT_TIMED("unet_conv_out", 36.0 * static_cast<double>(n), st,
+                    (launch_ws<16, 16>(H, W, 0, U->d0, U->wb + U->wb_out_off, U->w + U->boff[7], 2, nullptr, nullptr,
+                                       nullptr, unet_err(U), 36.0 * static_cast<double>(n), st, U->y, U->rms)));
+    else
+        LSDTT_TIMED("unet_conv_out", 36.0 * static_cast<double>(n), st,
+                    (k_conv_out<<<grid_blocks(n, 128), 128, 0, st>>>(H, W, U->d0, wr + U->woff[7], U->w + U->boff[7],
+                                                                      U->rms, U->y)));
     return cudaGetLastError();
 }
 
@@ -1365,7 +1907,16 @@ int lsdtt_gpu_unet_create(int32_t max_rows, int32_t max_cols, uint64_t seed, lsd
     const std::int64_t px0 = level_px(U, 0);
     cudaError_t e = ualloc(&U->w, off);
     if (e == cudaSuccess) e = ualloc(&U->wr, off);
-    if (e == cudaSuccess) e = ualloc(&U->wb, off);
+    U->wb_out_off = (off + 63) / 64 * 64;
+    // the convolution kernels stage weights with 16-byte loads: every
+    // layer's BF16 block must start on a 16-byte boundary
+    for (int l = 1; l < kLayers; ++l)
+        if ((U->woff[l] * 2) % 16 != 0)
+        {
+            lsdtt_gpu_unet_destroy(U);
+            return fail(LSDTT_GPU_EINVAL, "lsdtt_gpu_unet_create: unaligned weight block");
+        }
+    if (e == cudaSuccess) e = ualloc(&U->wb, U->wb_out_off + 16 * 144);  // then the padded output-layer block
     if (e == cudaSuccess) e = ualloc(&U->g, off);
     if (e == cudaSuccess) e = ualloc(&U->m, off);
     if (e == cudaSuccess) e = ualloc(&U->v, off);
@@ -1396,6 +1947,7 @@ int lsdtt_gpu_unet_create(int32_t max_rows, int32_t max_cols, uint64_t seed, lsd
         return cuda_fail(e, "lsdtt_gpu_unet_create");
     }
     k_pack<<<grid_blocks(off, 256), 256>>>(off, U->w, U->wb);
+    k_pack_out<<<9, 256>>>(U->w + U->woff[7], U->wb + U->wb_out_off);
     k_bf16_round<<<grid_blocks(off, 256), 256>>>(off, U->w, U->wr);
     e = cudaDeviceSynchronize();
     if (e != cudaSuccess)
@@ -1423,7 +1975,7 @@ int64_t lsdtt_gpu_unet_num_params(const lsdtt_gpu_unet* U) { return U ? U->npara
 
 int lsdtt_gpu_unet_set_conv_kernel(lsdtt_gpu_unet* U, int32_t kind)
 {
-    if (!U || kind < 0 || kind > 2) return fail(LSDTT_GPU_EINVAL, "lsdtt_gpu_unet_set_conv_kernel: bad argument");
+    if (!U || kind < 0 || kind > 3) return fail(LSDTT_GPU_EINVAL, "lsdtt_gpu_unet_set_conv_kernel: bad argument");
     U->conv_kind = kind;
     return LSDTT_GPU_OK;
 }
@@ -1452,6 +2004,7 @@ int lsdtt_gpu_unet_set_params(lsdtt_gpu_unet* U, const float* host, int64_t coun
     if (cudaMemcpy(U->w, host, sizeof(float) * count, cudaMemcpyHostToDevice) != cudaSuccess)
         return fail(LSDTT_GPU_ECUDA, "lsdtt_gpu_unet_set_params: copy failed");
     k_pack<<<grid_blocks(count, 256), 256>>>(count, U->w, U->wb);
+    k_pack_out<<<9, 256>>>(U->w + U->woff[7], U->wb + U->wb_out_off);
     k_bf16_round<<<grid_blocks(count, 256), 256>>>(count, U->w, U->wr);
     return cudaDeviceSynchronize() == cudaSuccess ? LSDTT_GPU_OK : fail(LSDTT_GPU_ECUDA, "lsdtt_gpu_unet_set_params");
 }
@@ -1532,6 +2085,7 @@ int lsdtt_gpu_unet_train_step(lsdtt_gpu_unet* U, const float* r_dev, const float
     else
         k_sgd<<<nb, 256, 0, st>>>(U->nparam, U->w, U->g, U->m, lr, 0.9f);
     k_pack<<<nb, 256, 0, st>>>(U->nparam, U->w, U->wb);
+    k_pack_out<<<9, 256, 0, st>>>(U->w + U->woff[7], U->wb + U->wb_out_off);
     k_bf16_round<<<nb, 256, 0, st>>>(U->nparam, U->w, U->wr);
     const cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? LSDTT_GPU_OK : cuda_fail(e, "lsdtt_gpu_unet_train_step");

@@ -69,11 +69,12 @@ def test_tcgen05_convolutions_match_mma_and_oracle(shape):
     net.set_conv_kernel("tcgen05")
     y_tc5 = net.apply(r).cpu().numpy()
     net.status()
-    net.set_conv_kernel("tcgen05_rows")
-    y_tc6 = net.apply(r).cpu().numpy()
-    net.status()
-    # the rolling-row kernel issues the same UMMAs and epilogue: same bits
-    assert np.array_equal(y_tc6.view(np.uint32), y_tc5.view(np.uint32))
+    for kind in ("tcgen05_rows", "tcgen05_ws"):
+        net.set_conv_kernel(kind)
+        y_rows = net.apply(r).cpu().numpy()
+        net.status()
+        # the rolling-row kernels issue the same UMMAs and epilogue: same bits
+        assert np.array_equal(y_rows.view(np.uint32), y_tc5.view(np.uint32)), kind
     y_ref, _ = unet.forward(P, r)
     e_mma, e_tc5, e_pair = _rel(y_mma, y_ref), _rel(y_tc5, y_ref), _rel(y_tc5, y_mma)
     print(f"{shape}: mma.sync vs oracle {e_mma:.2e}, tcgen05 vs oracle {e_tc5:.2e}, tcgen05 vs mma.sync {e_pair:.2e}")
