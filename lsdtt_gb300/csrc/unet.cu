@@ -79,36 +79,61 @@ __global__ void k_prep(const float* __restrict__ r, std::int64_t n, const float*
     if (i < n) x0[i] = __float2bfloat16_rn(r[i] / rms);
 }
 
-// Layer 0: 1 -> 16 channels, ReLU, on CUDA cores.
-__global__ void k_conv_in(int H, int W, const __nv_bfloat16* __restrict__ x0, const float* __restrict__ wg,
-                          const float* __restrict__ bg, __nv_bfloat16* __restrict__ out)
+// Layer 0 (1 -> 16 channels on CUDA cores: bias first, then the nine taps
+// in order, ReLU, BF16) fused with the first 2x2 mean pool: thread (i, j) of
+// the (H/2) x (W/2) grid computes e0 at its four pixels (2i + a, 2j + b) and
+// p0(i, j) = (((a + b) + c) + d) x 0.25 of their BF16 values, the order
+// k_pool uses, so e0 is written once and not read back.
+__global__ void k_conv_in_pool(int H, int W, const __nv_bfloat16* __restrict__ x0, const float* __restrict__ wg,
+                               const float* __restrict__ bg, __nv_bfloat16* __restrict__ e0,
+                               __nv_bfloat16* __restrict__ p0)
 {
     LSDTT_COUNT();
     __shared__ float w[16 * 9], b[16];
     for (int k = threadIdx.x; k < 16 * 9; k += blockDim.x) w[k] = wg[k];
     if (threadIdx.x < 16) b[threadIdx.x] = bg[threadIdx.x];
     __syncthreads();
-    const std::int64_t p = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (p >= static_cast<std::int64_t>(H) * W) return;
-    const int y = static_cast<int>(p / W), x = static_cast<int>(p % W);
-    float v[9];
+    const int h = H / 2, wd = W / 2;
+    const std::int64_t t = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (t >= static_cast<std::int64_t>(h) * wd) return;
+    const int i = static_cast<int>(t / wd), j = static_cast<int>(t % wd);
+    float v[4][4];  // x0 rows 2i-1 .. 2i+2, columns 2j-1 .. 2j+2 (0 outside)
 #pragma unroll
-    for (int t = 0; t < 9; ++t)
+    for (int rr = 0; rr < 4; ++rr)
+#pragma unroll
+        for (int cc = 0; cc < 4; ++cc)
+        {
+            const int yy = 2 * i - 1 + rr, xx = 2 * j - 1 + cc;
+            v[rr][cc] = (yy >= 0 && yy < H && xx >= 0 && xx < W)
+                            ? __bfloat162float(x0[static_cast<std::int64_t>(yy) * W + xx])
+                            : 0.f;
+        }
+    float pool[16];
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
     {
-        const int yy = y + t / 3 - 1, xx = x + t % 3 - 1;
-        v[t] = (yy >= 0 && yy < H && xx >= 0 && xx < W) ? __bfloat162float(x0[static_cast<std::int64_t>(yy) * W + xx]) : 0.f;
-    }
-    alignas(16) __nv_bfloat16 o16[16];
+        const int a = q >> 1, bq = q & 1;  // pixels (0,0), (0,1), (1,0), (1,1): k_pool's order
+        alignas(16) __nv_bfloat16 o16[16];
 #pragma unroll
-    for (int co = 0; co < 16; ++co)
-    {
-        float s = b[co];
+        for (int co = 0; co < 16; ++co)
+        {
+            float s = b[co];
 #pragma unroll
-        for (int t = 0; t < 9; ++t) s = __fadd_rn(s, __fmul_rn(v[t], w[co * 9 + t]));
-        o16[co] = __float2bfloat16_rn(fmaxf(s, 0.f));
+            for (int tp = 0; tp < 9; ++tp) s = __fadd_rn(s, __fmul_rn(v[a + tp / 3][bq + tp % 3], w[co * 9 + tp]));
+            o16[co] = __float2bfloat16_rn(fmaxf(s, 0.f));
+            const float e = __bfloat162float(o16[co]);
+            pool[co] = (q == 0) ? e : pool[co] + e;
+        }
+        __nv_bfloat16* dst = e0 + (static_cast<std::int64_t>(2 * i + a) * W + 2 * j + bq) * 16;
+        *reinterpret_cast<uint4*>(dst) = *reinterpret_cast<const uint4*>(o16);
+        *reinterpret_cast<uint4*>(dst + 8) = *reinterpret_cast<const uint4*>(o16 + 8);
     }
-    *reinterpret_cast<uint4*>(out + p * 16) = *reinterpret_cast<const uint4*>(o16);
-    *reinterpret_cast<uint4*>(out + p * 16 + 8) = *reinterpret_cast<const uint4*>(o16 + 8);
+    alignas(16) __nv_bfloat16 p16[16];
+#pragma unroll
+    for (int co = 0; co < 16; ++co) p16[co] = __float2bfloat16_rn(pool[co] * 0.25f);
+    __nv_bfloat16* pd = p0 + t * 16;
+    *reinterpret_cast<uint4*>(pd) = *reinterpret_cast<const uint4*>(p16);
+    *reinterpret_cast<uint4*>(pd + 8) = *reinterpret_cast<const uint4*>(p16 + 8);
 }
 
 // 2x2 mean, bf16 -> bf16 (H, W are the OUTPUT sizes), eight channels per
@@ -1748,13 +1773,11 @@ cudaError_t unet_forward(lsdtt_gpu_unet* U, const float* r, int H, int W, cudaSt
                 }));
     const float* wr = U->wr;
     // Algorithmic bytes: x0 2 in, e0 32 out per pixel.
-    LSDTT_TIMED("unet_conv_in", 34.0 * static_cast<double>(n), st,
-                (k_conv_in<<<grid_blocks(n, 128), 128, 0, st>>>(H, W, U->x0, wr + U->woff[0], U->w + U->boff[0],
-                                                                 U->e0)));
+    // Algorithmic bytes: x0 2 in, e0 32 out, p0 8 out per pixel.
     int h = H / 2, w = W / 2;
-    LSDTT_TIMED("unet_pool", 40.0 * static_cast<double>(h) * w * 4, st,
-                (k_pool<<<grid_blocks(static_cast<std::int64_t>(h) * w * 2, 256), 256, 0, st>>>(h, w, 16, U->e0,
-                                                                                                  U->p0)));
+    LSDTT_TIMED("unet_conv_in", 42.0 * static_cast<double>(n), st,
+                (k_conv_in_pool<<<grid_blocks(static_cast<std::int64_t>(h) * w, 128), 128, 0, st>>>(
+                    H, W, U->x0, wr + U->woff[0], U->w + U->boff[0], U->e0, U->p0)));
     launch_conv_tc(U, 1, h, w, 0, U->p0, U->wb + U->woff[1], U->w + U->boff[1], 0, nullptr, nullptr, U->e1, st);
     h /= 2; w /= 2;
     LSDTT_TIMED("unet_pool", 80.0 * static_cast<double>(h) * w * 4, st,
