@@ -864,7 +864,8 @@ constexpr int kWsLagDefault = 2;
 __host__ __device__ constexpr int ws_smem_bytes(int cin, int cout, bool skip, int lag, int g)
 {
     return (9 * cout * cin * 2 + 127) / 128 * 128 + (lag + 2 + g) * (cin / 8) * kChunkBytes +
-           (skip ? (lag + 2) * kTcM * cout * 2 : 0) + 8 * (2 * (lag + 2 + g) + 2 * (lag + 2) + 4 * g + 1) + 16;
+           (skip ? (lag + 2) * kTcM * cout * 2 : 0) + 8 * (2 * (lag + 2 + g) + 2 * (lag + 2) + 4 * g + 1) + 16 +
+           4 * cout;
 }
 
 // Lag 2 where it fits one CTA's shared memory, else 1 (the ring needs
@@ -899,7 +900,8 @@ struct WsLayout
                          kBars = kDone + 1;
     static constexpr int kTmemOff = kBarOff + 8 * kBars;  // TMEM base address, then the abort flag
     static constexpr int kAbortOff = kTmemOff + 4;
-    static constexpr int kSmem = kAbortOff + 12;
+    static constexpr int kBiasOff = kTmemOff + 16;  // the layer's COUT biases (FP32)
+    static constexpr int kSmem = kBiasOff + 4 * COUT;
     static constexpr int kAccCols = COUT < 32 ? 32 : COUT;
     static constexpr int kTmemCols = kAccs * kAccCols;
     static_assert(CIN % 16 == 0 && COUT % 16 == 0 && COUT <= 256, "UMMA shape");
@@ -1119,6 +1121,10 @@ __global__ void __launch_bounds__(kWsThreads, CIN == 64 ? 1 : 3) k_conv_ws(int H
         const uint4 v = *reinterpret_cast<const uint4*>(wpk + (static_cast<std::int64_t>(n) * 9 + t) * CIN + kc * 8);
         *reinterpret_cast<uint4*>(ws_smem + t * Lt::kTapBytes + (n >> 3) * Lt::kSboB + kc * 128 + (n & 7) * 16) = v;
     }
+    // biases into shared memory: the epilogue reads them every row (the
+    // output layer, mode 2, has one)
+    float* bias_s = reinterpret_cast<float*>(ws_smem + Lt::kBiasOff);
+    for (int k = tid; k < COUT; k += blockDim.x) bias_s[k] = (mode == 2 && k > 0) ? 0.0f : bias[k];
     // the weights, stored by the generic proxy, are read by the UMMAs
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     if (tid == 0)
@@ -1282,7 +1288,7 @@ __global__ void __launch_bounds__(kWsThreads, CIN == 64 ? 1 : 3) k_conv_ws(int H
                 if (ok && kSkip) ok = ws_wait(bar(Lt::kFullSkip + sk), (u / S) & 1u, abort_flag);
                 if (!ok) break;
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                ws_epilogue<COUT>(tmem + a * Lt::kAccCols, warp, lane, y, x0, W, bias, mode,
+                ws_epilogue<COUT>(tmem + a * Lt::kAccCols, warp, lane, y, x0, W, bias_s, mode,
                                   reinterpret_cast<const __nv_bfloat16*>(ws_smem + Lt::kSkipOff + sk * Lt::kSkipBytes),
                                   pre, out, bar(Lt::kAccEmpty + a), yout, rms);
                 if (kSkip) mbar_arrive(bar(Lt::kEmptySkip + sk));
