@@ -444,6 +444,110 @@ __global__ void ens_mdepth_scatter(Packed P, const std::uint8_t* __restrict__ ma
     }
 }
 
+// Member-major depth order, one CTA per member (blockIdx.x = m): a
+// shared-memory histogram of the member's depths (bins 0 .. cap-1), its
+// exclusive scan, bucket starts start[base + d] = base + (the member's
+// cells above depth d) for d = 0 .. deepest + 1, then the scatter through
+// shared-memory cursors, so member m's nodes sit at order[base ..] level by
+// level (within a level in no fixed order: its nodes are independent). The
+// sweep reads start[base + 1 .. base + deepest + 1] and the ranges between
+// them, as with the global counting sort, which needs a scan over every
+// bucket of the packed grid. A depth at or beyond `cap` raises *overflow
+// (the host reruns the step eagerly and captures with a larger cap).
+constexpr int kMdSortThreads = 1024;
+constexpr std::size_t kMdSortMaxSmem = 200 * 1024;  // bins for depths up to ~51,000 levels
+
+__global__ void __launch_bounds__(kMdSortThreads) ens_mdepth_sort(Packed P, const std::uint8_t* __restrict__ mask,
+                                                                  const std::int32_t* __restrict__ depth,
+                                                                  std::uint32_t cap, std::uint32_t* __restrict__ start,
+                                                                  std::uint32_t* __restrict__ order,
+                                                                  std::uint32_t* __restrict__ mmax,
+                                                                  int* __restrict__ overflow)
+{
+    LSDTT_COUNT();
+    extern __shared__ std::uint32_t md_hist[];  // cap + 1 bins
+    __shared__ std::uint32_t s_max, s_warp[kMdSortThreads / 32];
+    __shared__ int s_over;
+    const int m = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const PackedMember& M = P.m[m];
+    const std::int64_t base = M.base, n = static_cast<std::int64_t>(M.nr) * M.nc;
+    for (std::uint32_t k = tid; k <= cap; k += blockDim.x) md_hist[k] = 0;
+    if (tid == 0)
+    {
+        s_max = 0;
+        s_over = 0;
+    }
+    __syncthreads();
+    std::uint32_t dmax = 0;
+    for (std::int64_t l = tid; l < n; l += blockDim.x)
+    {
+        const std::int64_t i = base + l;
+        if (!mask[i]) continue;
+        const std::int32_t d = depth[i];
+        if (d < 0) continue;
+        if (static_cast<std::uint32_t>(d) >= cap)
+        {
+            s_over = 1;
+            continue;
+        }
+        atomicAdd(&md_hist[d], 1u);
+        dmax = max(dmax, static_cast<std::uint32_t>(d));
+    }
+    for (int o = 16; o > 0; o >>= 1) dmax = max(dmax, __shfl_down_sync(0xffffffffu, dmax, o));
+    if (lane == 0) atomicMax(&s_max, dmax);
+    __syncthreads();
+    if (s_over)  // block-uniform
+    {
+        if (tid == 0) *overflow = 1;
+        return;
+    }
+    // exclusive scan of bins 0 .. D+1 (bin D+1 is empty: the end of level D)
+    const std::uint32_t D = s_max, nbins = D + 2;
+    const std::uint32_t per = (nbins + blockDim.x - 1) / blockDim.x;
+    const std::uint32_t lo = min(nbins, tid * per), hi = min(nbins, lo + per);
+    std::uint32_t sum = 0;
+    for (std::uint32_t k = lo; k < hi; ++k) sum += md_hist[k];
+    std::uint32_t incl = sum;
+    for (int o = 1; o < 32; o <<= 1)
+    {
+        const std::uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    if (lane == 31) s_warp[warp] = incl;
+    __syncthreads();
+    if (warp == 0)
+    {
+        const int nw = static_cast<int>(blockDim.x >> 5);
+        std::uint32_t w = lane < nw ? s_warp[lane] : 0u, wi = w;
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            const std::uint32_t v = __shfl_up_sync(0xffffffffu, wi, o);
+            if (lane >= o) wi += v;
+        }
+        if (lane < nw) s_warp[lane] = wi - w;  // exclusive prefix of the warps
+    }
+    __syncthreads();
+    std::uint32_t run = s_warp[warp] + incl - sum;
+    for (std::uint32_t k = lo; k < hi; ++k)
+    {
+        const std::uint32_t c = md_hist[k];
+        md_hist[k] = run;
+        start[base + k] = static_cast<std::uint32_t>(base) + run;
+        run += c;
+    }
+    if (tid == 0) mmax[m] = D;
+    __syncthreads();
+    for (std::int64_t l = tid; l < n; l += blockDim.x)
+    {
+        const std::int64_t i = base + l;
+        if (!mask[i]) continue;
+        const std::int32_t d = depth[i];
+        if (d < 0) continue;
+        const std::uint32_t pos = atomicAdd(&md_hist[d], 1u);
+        order[base + pos] = static_cast<std::uint32_t>(i);
+    }
+}
+
 // The deepest level over all members.
 __global__ void ens_mdepth_max(int n_members, const std::uint32_t* __restrict__ mmax, std::uint32_t* __restrict__ maxd)
 {
@@ -1649,15 +1753,29 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
     }
     if (member_order)
     {
-        cudaMemsetAsync(E->mmax, 0, sizeof(std::uint32_t) * M, st);
-        cudaMemsetAsync(E->lcount, 0, sizeof(std::uint32_t) * (static_cast<std::size_t>(N) + 1), st);
-        ens_mdepth_hist<<<nb, 256, 0, st>>>(E->P, E->mask, f->depth, E->lcount, E->mmax);
-        f->ws.used = 0;
-        e = exclusive_scan<std::uint32_t, std::uint32_t>(E->lcount, N + 1, E->mstart,
-                                                         static_cast<std::uint32_t*>(nullptr), f->ws, st);
-        if (e != cudaSuccess) return e;
-        cudaMemsetAsync(E->lfill, 0, sizeof(std::uint32_t) * (static_cast<std::size_t>(N) + 1), st);
-        ens_mdepth_scatter<<<nb, 256, 0, st>>>(E->P, E->mask, f->depth, E->mstart, E->lfill, E->morder);
+        // one CTA per member while the depth histogram fits shared memory
+        // (eager steps know the deepest level; captured steps use the cap)
+        const std::uint32_t mcap =
+            eager ? *E->h_maxd + 1 : static_cast<std::uint32_t>(std::min<std::int64_t>(E->depth_cap, N + 1));
+        const std::size_t md_smem = sizeof(std::uint32_t) * (static_cast<std::size_t>(mcap) + 1);
+        if (md_smem <= kMdSortMaxSmem)
+        {
+            LSDTT_TIMED("ens_member_depth_sort", 9.0 * static_cast<double>(N), st,
+                        (ens_mdepth_sort<<<static_cast<unsigned>(M), kMdSortThreads, md_smem, st>>>(
+                            E->P, E->mask, f->depth, mcap, E->mstart, E->morder, E->mmax, E->flags + 2)));
+        }
+        else
+        {
+            cudaMemsetAsync(E->mmax, 0, sizeof(std::uint32_t) * M, st);
+            cudaMemsetAsync(E->lcount, 0, sizeof(std::uint32_t) * (static_cast<std::size_t>(N) + 1), st);
+            ens_mdepth_hist<<<nb, 256, 0, st>>>(E->P, E->mask, f->depth, E->lcount, E->mmax);
+            f->ws.used = 0;
+            e = exclusive_scan<std::uint32_t, std::uint32_t>(E->lcount, N + 1, E->mstart,
+                                                             static_cast<std::uint32_t*>(nullptr), f->ws, st);
+            if (e != cudaSuccess) return e;
+            cudaMemsetAsync(E->lfill, 0, sizeof(std::uint32_t) * (static_cast<std::size_t>(N) + 1), st);
+            ens_mdepth_scatter<<<nb, 256, 0, st>>>(E->P, E->mask, f->depth, E->mstart, E->lfill, E->morder);
+        }
         if (!global_order) ens_mdepth_max<<<1, 256, 0, st>>>(M, E->mmax, E->maxd);
         if (eager)
         {
@@ -2000,6 +2118,9 @@ int lsdtt_gpu_ensemble_create(const lsdtt_gpu_member* members, int32_t n_members
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
         return fail(LSDTT_GPU_ENODEV, std::string(who) + ": no CUDA device");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (cudaFuncSetAttribute(ens_mdepth_sort, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(kMdSortMaxSmem)) != cudaSuccess)
+        return cuda_fail(cudaGetLastError(), "lsdtt_gpu_ensemble_create: shared memory of the member depth sort");
     auto* E = new lsdtt_gpu_ensemble();
     E->M = n_members;
     E->use_graph = use_graph != 0;
