@@ -142,21 +142,85 @@ __global__ void ens_dirty_init(std::int32_t T, const std::uint16_t* __restrict__
     d1[t] = v;
 }
 
-__global__ void __launch_bounds__(256) ens_fill_relax(Packed P, const EnsParams* __restrict__ prm,
-                                                      const std::uint16_t* __restrict__ tile_member,
-                                                      const float* __restrict__ z,
-                                                      const std::uint8_t* __restrict__ kind, float* __restrict__ F,
-                                                      int* __restrict__ changed,
-                                                      const std::uint8_t* __restrict__ din,
-                                                      std::uint8_t* __restrict__ dout)
+// Active tiles of a fill pass, one thread per tile: tile t is active when
+// it or one of its eight neighbours in its member's tile grid (periodic axes
+// wrap) changed in the previous pass. Clears dirty_out[t] (the relaxation
+// of an active tile sets it again), appends the active tiles to `list`
+// (warp-aggregated) and counts them (cnt[0]) and their cells (cnt[1]).
+__global__ void ens_fill_active(Packed P, const EnsParams* __restrict__ prm,
+                                const std::uint16_t* __restrict__ tile_member, std::int32_t T,
+                                const std::uint8_t* __restrict__ din, std::uint8_t* __restrict__ dout,
+                                std::int32_t* __restrict__ list, unsigned long long* __restrict__ cnt)
 {
     LSDTT_COUNT();
-    const int m = tile_member[blockIdx.x];
-    const PackedMember& M = P.m[m];
-    const EnsParams& q = prm[m];
-    const int local = static_cast<int>(blockIdx.x) - M.tile_base;
-    fill_relax_tile(M.nr, M.nc, q.per_ns, q.per_ew, q.L, q.Ld, q.fill_eps, z + M.base, kind + M.base, F + M.base,
-                    changed, din + M.tile_base, dout + M.tile_base, local % M.ntx, local / M.ntx, M.ntx, M.nty);
+    const std::int32_t t = static_cast<std::int32_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    bool active = false;
+    unsigned cells = 0;
+    if (t < T)
+    {
+        const int m = tile_member[t];
+        const PackedMember& M = P.m[m];
+        const EnsParams& q = prm[m];
+        const int local = t - M.tile_base, tx = local % M.ntx, ty = local / M.ntx;
+        const std::uint8_t* d = din + M.tile_base;
+        for (int dy = -1; dy <= 1 && !active; ++dy)
+            for (int dx = -1; dx <= 1; ++dx)
+            {
+                int yy = ty + dy, xx = tx + dx;
+                if (q.per_ns) yy = (yy + M.nty) % M.nty;
+                if (q.per_ew) xx = (xx + M.ntx) % M.ntx;
+                if (yy < 0 || yy >= M.nty || xx < 0 || xx >= M.ntx) continue;
+                if (d[yy * M.ntx + xx])
+                {
+                    active = true;
+                    break;
+                }
+            }
+        dout[t] = 0;
+        if (active)
+            cells = static_cast<unsigned>(min(kT, M.nr - ty * kT)) * static_cast<unsigned>(min(kT, M.nc - tx * kT));
+    }
+    const unsigned bal = __ballot_sync(0xffffffffu, active);
+    const int lane = threadIdx.x & 31;
+    for (int o = 16; o > 0; o >>= 1) cells += __shfl_down_sync(0xffffffffu, cells, o);
+    unsigned long long base = 0;
+    if (lane == 0 && bal)
+    {
+        base = atomicAdd(&cnt[0], static_cast<unsigned long long>(__popc(bal)));
+        atomicAdd(&cnt[1], static_cast<unsigned long long>(cells));
+    }
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (active) list[base + __popc(bal & ((1u << lane) - 1u))] = t;
+}
+
+// Fill relaxation over the listed active tiles: a persistent grid, block w
+// relaxes tiles w, w + grid, ... of the list (fill_relax_tile with its gate
+// skipped: a pass over every tile spent ~0.2 ms only on inactive tiles
+// reading their neighbours' flags and leaving).
+__global__ void __launch_bounds__(256) ens_fill_relax_list(Packed P, const EnsParams* __restrict__ prm,
+                                                           const std::uint16_t* __restrict__ tile_member,
+                                                           const float* __restrict__ z,
+                                                           const std::uint8_t* __restrict__ kind,
+                                                           float* __restrict__ F, int* __restrict__ changed,
+                                                           const std::uint8_t* __restrict__ din,
+                                                           std::uint8_t* __restrict__ dout,
+                                                           const std::int32_t* __restrict__ list,
+                                                           const unsigned long long* __restrict__ cnt)
+{
+    LSDTT_COUNT();
+    const std::int64_t n = static_cast<std::int64_t>(cnt[0]);
+    for (std::int64_t w = blockIdx.x; w < n; w += gridDim.x)
+    {
+        const int t = list[w];
+        const int m = tile_member[t];
+        const PackedMember& M = P.m[m];
+        const EnsParams& q = prm[m];
+        const int local = t - M.tile_base;
+        fill_relax_tile(M.nr, M.nc, q.per_ns, q.per_ew, q.L, q.Ld, q.fill_eps, z + M.base, kind + M.base,
+                        F + M.base, changed, din + M.tile_base, dout + M.tile_base, local % M.ntx, local / M.ntx,
+                        M.ntx, M.nty, false);
+        __syncthreads();  // the tile's shared arrays are staged again for the next tile
+    }
 }
 
 // Condition of the graph's fill loop (a conditional WHILE node whose body
@@ -691,7 +755,7 @@ __global__ void __launch_bounds__(512) ens_sp_coop(SweepArgs A, int split, unsig
     }
 }
 
-constexpr unsigned kSweepClusterBlock = 128;  // largest block of the member-cluster sweep
+constexpr unsigned kSweepClusterBlock = 256;  // largest block of the member-cluster sweep
 
 // One node of the member-cluster sweep with its independent loads done.
 struct SweepNode
@@ -735,7 +799,7 @@ __device__ __forceinline__ void sweep_solve(const SweepArgs& A, const SpParams& 
 // elevation, direction) between its arrival at the cluster barrier and its
 // wait there, so a level up to twice the cluster's width costs one L2 load,
 // the solves and the barrier.
-__global__ void __launch_bounds__(kSweepClusterBlock, 4) ens_sp_clusters(SweepArgs A,
+__global__ void __launch_bounds__(kSweepClusterBlock, 2) ens_sp_clusters(SweepArgs A,
                                                                       const std::uint16_t* __restrict__ perm,
                                                                       const std::uint32_t* __restrict__ mmax)
 {
@@ -1440,6 +1504,10 @@ struct lsdtt_gpu_ensemble
     // state and stage buffers
     float *z = nullptr, *zf = nullptr, *zsp = nullptr, *zpre = nullptr;
     std::uint8_t *mask = nullptr, *kind = nullptr, *bflag = nullptr, *dirty = nullptr, *oflag = nullptr;
+    std::int32_t* flist = nullptr;           // [T] active fill tiles of the current pass
+    unsigned long long* fcnt = nullptr;      // [2] their count and cells
+    unsigned long long* h_fcnt = nullptr;    // pinned copy (eager steps)
+    unsigned fill_grid = 0;                  // persistent grid of the listed relaxation
     std::int64_t* pos = nullptr;
     int* nd = nullptr;
     lsdtt_gpu_flow* f = nullptr;
@@ -1485,7 +1553,7 @@ struct lsdtt_gpu_ensemble
     std::uint16_t* perm = nullptr;    // [M] members by decreasing cell count
     float* pcg_scal = nullptr;        // [2M] each member's PCG alpha, then beta
     std::vector<std::uint16_t> perm_h;
-    int sweep_cluster = 8;            // CTAs per member cluster (tuned: 4 or 8)
+    int sweep_cluster = 8;            // CTAs per member cluster (tuned: 4, 8 or 16)
     unsigned* bar = nullptr;     // its grid barrier: {count, generation}
     unsigned long long* zg = nullptr;  // dataflow {generation, z} word per cell
     std::uint32_t* dfc = nullptr;    // [0] generation, [1] chunk counter
@@ -1512,9 +1580,9 @@ void free_ensemble(lsdtt_gpu_ensemble* E)
     if (E->graph) cudaGraphDestroy(E->graph);
     void* bufs[] = {E->d_pm, E->d_prm, E->blk_member, E->tile_member, E->strip_member, E->undecided, E->bar, E->loopc, E->pcg_scal, E->morder, E->mstart, E->mmax, E->perm, E->z, E->zf, E->zsp, E->zpre, E->kind, E->bflag, E->dirty, E->oflag, E->pos, E->nd, E->area, E->order, E->lstart, E->lcount,
                     E->lfill, E->maxd, E->dof, E->invd, E->b, E->x, E->r, E->p, E->p2, E->zz, E->Ap, E->hs_bb, E->hs_acc,
-                    E->done, E->iters, E->stats_acc, E->part, E->kam_tab, E->flags, E->zg, E->dfc};
+                    E->done, E->iters, E->stats_acc, E->part, E->kam_tab, E->flags, E->zg, E->dfc, E->flist, E->fcnt};
     for (void* q : bufs) cudaFree(q);
-    void* hb[] = {E->h_stats, E->h_flags, E->h_iters, E->h_maxd, E->h_err};
+    void* hb[] = {E->h_stats, E->h_flags, E->h_iters, E->h_maxd, E->h_err, E->h_fcnt};
     for (void* q : hb) cudaFreeHost(q);
     if (E->f) lsdtt_gpu_flow_destroy(E->f);
     if (E->own) cudaStreamDestroy(E->own);
@@ -1652,20 +1720,39 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
                                                            E->dirty + E->T);
     const dim3 fblock(32, 8);
     const double cells = static_cast<double>(E->member_cells);
-    auto relax = [&](int pass) {
-        // Algorithmic bytes per pass: z 4 + mask 1 in, filled value 4 out.
-        LSDTT_TIMED("ens_fill_relax", 9.0 * cells, st,
-                    (ens_fill_relax<<<E->T, fblock, 0, st>>>(E->P, E->d_prm, E->tile_member, E->z, E->kind, E->zf,
-                                                             E->flags, E->dirty + (pass & 1) * E->T,
-                                                             E->dirty + ((pass + 1) & 1) * E->T)));
+    const unsigned tb = static_cast<unsigned>((E->T + 255) / 256);
+    // One pass: list the active tiles, then relax only those. In eager
+    // steps the listed cells are read back, so the pass's algorithmic bytes
+    // (z 4 + mask 1 in, filled value 4 out per cell of an active tile) are
+    // those of the work done.
+    auto pass_on = [&](int pass, cudaStream_t s, bool timed) -> cudaError_t {
+        const std::uint8_t* din = E->dirty + (pass & 1) * E->T;
+        std::uint8_t* dout = E->dirty + ((pass + 1) & 1) * E->T;
+        cudaMemsetAsync(E->fcnt, 0, sizeof(unsigned long long) * 2, s);
+        ens_fill_active<<<tb, 256, 0, s>>>(E->P, E->d_prm, E->tile_member, E->T, din, dout, E->flist, E->fcnt);
+        double bytes = 9.0 * cells;
+        if (timed && profiling_enabled())
+        {
+            cudaMemcpyAsync(E->h_fcnt, E->fcnt, sizeof(unsigned long long) * 2, cudaMemcpyDeviceToHost, s);
+            const cudaError_t pe = cudaStreamSynchronize(s);
+            if (pe != cudaSuccess) return pe;
+            bytes = 9.0 * static_cast<double>(E->h_fcnt[1]);
+        }
+        LSDTT_TIMED("ens_fill_relax", bytes, s,
+                    (ens_fill_relax_list<<<E->fill_grid, fblock, 0, s>>>(E->P, E->d_prm, E->tile_member, E->z,
+                                                                         E->kind, E->zf, E->flags, din, dout,
+                                                                         E->flist, E->fcnt)));
+        return cudaSuccess;
     };
+    auto relax = [&](int pass) { return pass_on(pass, st, true); };
     int passes = 0;
     if (eager)
     {
         for (;;)
         {
             cudaMemsetAsync(E->flags, 0, sizeof(int), st);
-            for (int k = 0; k < 4; ++k, ++passes) relax(passes);
+            for (int k = 0; k < 4 && e == cudaSuccess; ++k, ++passes) e = relax(passes);
+            if (e != cudaSuccess) return e;
             cudaMemcpyAsync(E->h_flags, E->flags, sizeof(int), cudaMemcpyDeviceToHost, st);
             e = cudaStreamSynchronize(st);
             if (e != cudaSuccess) return e;
@@ -1684,8 +1771,7 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
             for (int k = 0; k < 2; ++k)
             {
                 if (k == 1) cudaMemsetAsync(E->flags, 0, sizeof(int), s2);
-                ens_fill_relax<<<E->T, fblock, 0, s2>>>(E->P, E->d_prm, E->tile_member, E->z, E->kind, E->zf, E->flags,
-                                                        E->dirty + (k & 1) * E->T, E->dirty + ((k + 1) & 1) * E->T);
+                pass_on(k, s2, false);
             }
             ens_fill_while<<<1, 1, 0, s2>>>(E->flags, E->loopc, max_pairs, E->flags + 1, h);
         });
@@ -1696,7 +1782,7 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
         for (int k = 0; k < E->fill_cap; ++k)
         {
             if (k == E->fill_cap - 1) cudaMemsetAsync(E->flags, 0, sizeof(int), st);
-            relax(k);
+            pass_on(k, st, false);
         }
         ens_flag_copy<<<1, 1, 0, st>>>(E->flags, E->flags + 1);
     }
@@ -1836,8 +1922,10 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
                 for (int blk : blocks) cands.push_back({tail, blk, 0, 0});
             for (std::uint32_t tail : tails) cands.push_back({tail, 512, 2, 0});
             cands.push_back({0u, 256, 1, 0});
-            for (int cl : {4, 8})
-                for (int blk : {64, 128}) cands.push_back({0u, blk, 3, cl});
+            // clusters of 16 CTAs are the non-portable size (allowed at
+            // creation; a launch the device refuses is no candidate)
+            for (int cl : {4, 8, 16})
+                for (int blk : {64, 128, 256}) cands.push_back({0u, blk, 3, cl});
             for (const auto& cand : cands)
                 {
                     const std::uint32_t tail = cand.tail;
@@ -2121,6 +2209,8 @@ int lsdtt_gpu_ensemble_create(const lsdtt_gpu_member* members, int32_t n_members
     if (cudaFuncSetAttribute(ens_mdepth_sort, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              static_cast<int>(kMdSortMaxSmem)) != cudaSuccess)
         return cuda_fail(cudaGetLastError(), "lsdtt_gpu_ensemble_create: shared memory of the member depth sort");
+    if (cudaFuncSetAttribute(ens_sp_clusters, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)
+        cudaGetLastError();  // without it the 16-CTA clusters are refused and not chosen
     auto* E = new lsdtt_gpu_ensemble();
     E->M = n_members;
     E->use_graph = use_graph != 0;
@@ -2288,6 +2378,8 @@ int lsdtt_gpu_ensemble_create(const lsdtt_gpu_member* members, int32_t n_members
     alloc(&E->kind, n);
     alloc(&E->bflag, n);
     alloc(&E->dirty, 2 * static_cast<std::size_t>(tiles));
+    alloc(&E->flist, static_cast<std::size_t>(tiles));
+    alloc(&E->fcnt, 2);
     alloc(&E->oflag, n);
     alloc(&E->pos, n);
     alloc(&E->nd, static_cast<std::size_t>(n_members));
@@ -2328,6 +2420,13 @@ int lsdtt_gpu_ensemble_create(const lsdtt_gpu_member* members, int32_t n_members
     if (e == cudaSuccess) e = cudaMallocHost(&E->h_iters, sizeof(int) * n_members);
     if (e == cudaSuccess) e = cudaMallocHost(&E->h_maxd, sizeof(std::uint32_t));
     if (e == cudaSuccess) e = cudaMallocHost(&E->h_err, sizeof(unsigned long long) * 4);
+    if (e == cudaSuccess) e = cudaMallocHost(&E->h_fcnt, sizeof(unsigned long long) * 2);
+    {
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        E->fill_grid = static_cast<unsigned>(std::max(1, sms) * 8);
+    }
     if (e != cudaSuccess)
     {
         free_ensemble(E);

@@ -91,10 +91,12 @@ __device__ __forceinline__ void fill_relax_tile(int nr, int nc, bool per_ns, boo
                                                 const std::uint8_t* __restrict__ kind, float* __restrict__ F,
                                                 int* __restrict__ changed, const std::uint8_t* __restrict__ dirty_in,
                                                 std::uint8_t* __restrict__ dirty_out, const int tx, const int ty,
-                                                const int ntx, const int nty)
+                                                const int ntx, const int nty, const bool gate = true)
 {
     // Active-tile gate: a tile can only change if it or one of its eight
     // neighbouring tiles changed in the previous pass (periodic axes wrap).
+    // Callers that list the active tiles beforehand skip it (gate = false).
+    if (gate)
     {
         bool active = false;
         for (int dy = -1; dy <= 1 && !active; ++dy)
