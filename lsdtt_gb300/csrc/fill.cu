@@ -66,6 +66,74 @@ __global__ void __launch_bounds__(256) fill_relax(int nr, int nc, bool per_ns, b
                     blockIdx.y, gridDim.x, gridDim.y);
 }
 
+// Active tiles of a pass, one thread per tile: tile (tx, ty) is active when
+// it or one of its eight neighbours (periodic axes wrap) changed in the
+// previous pass. Clears dirty_out (an active tile's relaxation sets it
+// again), appends the active tiles to `list` (warp-aggregated) and counts
+// them (cnt[0]) and their cells (cnt[1]).
+__global__ void fill_active(int nr, int nc, bool per_ns, bool per_ew, int ntx, int nty,
+                            const std::uint8_t* __restrict__ din, std::uint8_t* __restrict__ dout,
+                            std::int32_t* __restrict__ list, unsigned long long* __restrict__ cnt)
+{
+    LSDTT_COUNT();
+    const std::int32_t t = static_cast<std::int32_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    bool active = false;
+    unsigned cells = 0;
+    if (t < ntx * nty)
+    {
+        const int tx = t % ntx, ty = t / ntx;
+        for (int dy = -1; dy <= 1 && !active; ++dy)
+            for (int dx = -1; dx <= 1; ++dx)
+            {
+                int yy = ty + dy, xx = tx + dx;
+                if (per_ns) yy = (yy + nty) % nty;
+                if (per_ew) xx = (xx + ntx) % ntx;
+                if (yy < 0 || yy >= nty || xx < 0 || xx >= ntx) continue;
+                if (din[yy * ntx + xx])
+                {
+                    active = true;
+                    break;
+                }
+            }
+        dout[t] = 0;
+        if (active) cells = static_cast<unsigned>(min(kT, nr - ty * kT)) * static_cast<unsigned>(min(kT, nc - tx * kT));
+    }
+    const unsigned bal = __ballot_sync(0xffffffffu, active);
+    const int lane = threadIdx.x & 31;
+    for (int o = 16; o > 0; o >>= 1) cells += __shfl_down_sync(0xffffffffu, cells, o);
+    unsigned long long base = 0;
+    if (lane == 0 && bal)
+    {
+        base = atomicAdd(&cnt[0], static_cast<unsigned long long>(__popc(bal)));
+        atomicAdd(&cnt[1], static_cast<unsigned long long>(cells));
+    }
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (active) list[base + __popc(bal & ((1u << lane) - 1u))] = t;
+}
+
+// Relaxation of the listed active tiles by a persistent grid (block w takes
+// entries w, w + grid, ...), the tile gate skipped: one block per tile spent
+// most of a late pass on inactive tiles reading their neighbours' flags.
+__global__ void __launch_bounds__(256) fill_relax_list(int nr, int nc, bool per_ns, bool per_ew, float L, float Ld,
+                                                       float min_slope, const float* __restrict__ z,
+                                                       const std::uint8_t* __restrict__ kind, float* __restrict__ F,
+                                                       int* __restrict__ changed,
+                                                       const std::uint8_t* __restrict__ dirty_in,
+                                                       std::uint8_t* __restrict__ dirty_out, int ntx, int nty,
+                                                       const std::int32_t* __restrict__ list,
+                                                       const unsigned long long* __restrict__ cnt)
+{
+    LSDTT_COUNT();
+    const std::int64_t n = static_cast<std::int64_t>(cnt[0]);
+    for (std::int64_t w = blockIdx.x; w < n; w += gridDim.x)
+    {
+        const int t = list[w];
+        fill_relax_tile(nr, nc, per_ns, per_ew, L, Ld, min_slope, z, kind, F, changed, dirty_in, dirty_out, t % ntx,
+                        t / ntx, ntx, nty, false);
+        __syncthreads();  // the tile's shared arrays are staged again for the next tile
+    }
+}
+
 }  // namespace
 }  // namespace lsdtt_gb300
 
@@ -100,11 +168,17 @@ extern "C" int lsdtt_gpu_fill_pits(const lsdtt_gpu_grid* grid, const float* z_de
     int* flags = nullptr;   // [0] interior nodata, [1] changed
     int* hflag = nullptr;
     std::uint8_t* dirty = nullptr;  // two per-tile activity planes
+    std::int32_t* list = nullptr;   // active tiles of the current pass
+    unsigned long long* cnt = nullptr;  // their count and cells
+    unsigned long long* hcnt = nullptr;
     const std::int64_t ntiles = static_cast<std::int64_t>((nc + kT - 1) / kT) * ((nr + kT - 1) / kT);
     cudaError_t e = cudaMallocAsync(&kind, static_cast<std::size_t>(n), st);
     if (e == cudaSuccess) e = cudaMallocAsync(&dirty, static_cast<std::size_t>(2 * ntiles), st);
+    if (e == cudaSuccess) e = cudaMallocAsync(&list, sizeof(std::int32_t) * static_cast<std::size_t>(ntiles), st);
+    if (e == cudaSuccess) e = cudaMallocAsync(&cnt, sizeof(unsigned long long) * 2, st);
     if (e == cudaSuccess) e = cudaMallocAsync(&flags, sizeof(int) * 2, st);
     if (e == cudaSuccess) e = cudaMallocHost(&hflag, sizeof(int));
+    if (e == cudaSuccess) e = cudaMallocHost(&hcnt, sizeof(unsigned long long) * 2);
     if (e != cudaSuccess) return cuda_fail(e, "lsdtt_gpu_fill_pits");
     cudaMemsetAsync(flags, 0, sizeof(int) * 2, st);
     cudaMemsetAsync(dirty, 1, static_cast<std::size_t>(2 * ntiles), st);
@@ -120,16 +194,38 @@ extern "C" int lsdtt_gpu_fill_pits(const lsdtt_gpu_grid* grid, const float* z_de
     // few passes to keep the host out of the loop.
     const int kCheckEvery = 4;
     const long max_pass = 4L * (nr + nc) + 64;  // bound: any path crosses each tile row/column at most a few times
+    const int ntx = static_cast<int>(tiles.x), nty = static_cast<int>(tiles.y);
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const unsigned list_grid = static_cast<unsigned>(std::max(1, sms) * 8);
     long pass = 0;
     for (;;)
     {
         cudaMemsetAsync(flags + 1, 0, sizeof(int), st);
-        for (int k = 0; k < kCheckEvery; ++k, ++pass)
-            // Algorithmic bytes per pass: z 4 + mask 1 in, filled value 4 out.
-            LSDTT_TIMED("fill_relax", 9.0 * static_cast<double>(n), st,
-                        (fill_relax<<<tiles, block, 0, st>>>(nr, nc, per_ns, per_ew, L, Ld, eps, z_dev, kind, out_dev,
-                                                             flags + 1, dirty + (pass & 1) * ntiles,
-                                                             dirty + ((pass + 1) & 1) * ntiles)));
+        for (int k = 0; k < kCheckEvery && e == cudaSuccess; ++k, ++pass)
+        {
+            // Each pass lists its active tiles, then relaxes only those.
+            // Algorithmic bytes per pass: z 4 + mask 1 in, filled value 4
+            // out per relaxed cell (counted when profiling).
+            const std::uint8_t* din = dirty + (pass & 1) * ntiles;
+            std::uint8_t* dout = dirty + ((pass + 1) & 1) * ntiles;
+            cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * 2, st);
+            fill_active<<<grid_blocks(ntiles, 256), 256, 0, st>>>(nr, nc, per_ns, per_ew, ntx, nty, din, dout, list,
+                                                                   cnt);
+            double bytes = 9.0 * static_cast<double>(n);
+            if (profiling_enabled())
+            {
+                cudaMemcpyAsync(hcnt, cnt, sizeof(unsigned long long) * 2, cudaMemcpyDeviceToHost, st);
+                e = cudaStreamSynchronize(st);
+                bytes = 9.0 * static_cast<double>(hcnt[1]);
+            }
+            LSDTT_TIMED("fill_relax", bytes, st,
+                        (fill_relax_list<<<list_grid, block, 0, st>>>(nr, nc, per_ns, per_ew, L, Ld, eps, z_dev, kind,
+                                                                      out_dev, flags + 1, din, dout, ntx, nty, list,
+                                                                      cnt)));
+        }
+        if (e != cudaSuccess) break;
         cudaMemcpyAsync(hflag, flags + 1, sizeof(int), cudaMemcpyDeviceToHost, st);
         e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) break;
@@ -142,8 +238,11 @@ extern "C" int lsdtt_gpu_fill_pits(const lsdtt_gpu_grid* grid, const float* z_de
     }
     cudaFreeAsync(kind, st);
     cudaFreeAsync(dirty, st);
+    cudaFreeAsync(list, st);
+    cudaFreeAsync(cnt, st);
     cudaFreeAsync(flags, st);
     cudaFreeHost(hflag);
+    cudaFreeHost(hcnt);
     if (e == cudaErrorUnknown) return fail(LSDTT_GPU_ETIMEOUT, "lsdtt_gpu_fill_pits: relaxation did not converge");
     if (e != cudaSuccess) return cuda_fail(e, "lsdtt_gpu_fill_pits");
     return LSDTT_GPU_OK;
