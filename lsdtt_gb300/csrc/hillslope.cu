@@ -351,18 +351,49 @@ struct HsN
     double cap;
     double h;
     int nonlinear;
+    // reciprocals formed once on the host (hsn_reciprocals): FP64 division
+    // is a long instruction sequence on this part, and the evaluation would
+    // otherwise divide ~18 times per cell
+    double inv_h, inv_2h, inv_Sc2, inv_Sc;
 };
+
+inline void hsn_reciprocals(HsN& P)
+{
+    P.inv_h = 1.0 / P.h;
+    P.inv_2h = 1.0 / (2.0 * P.h);
+    P.inv_Sc2 = 1.0 / P.Sc2;
+    P.inv_Sc = 1.0 / std::sqrt(P.Sc2);
+}
+
+// Neighbour (rr, cc) of (r, c) in direction (dr, dc) by the boundary rules
+// of hs_nb (wrap on 'p', else the cell itself; a masked neighbour is the
+// cell itself), without forming the flat index.
+__device__ __forceinline__ void hs_nb_rc(const Hs& H, const std::uint8_t* mask, int r, int c, int dr, int dc, int& rr,
+                                         int& cc)
+{
+    rr = r + dr;
+    cc = c + dc;
+    if (rr < 0) rr = (H.bn == 'p') ? H.nr - 1 : r;
+    else if (rr >= H.nr) rr = (H.bs == 'p') ? 0 : r;
+    if (cc < 0) cc = (H.bw == 'p') ? H.nc - 1 : c;
+    else if (cc >= H.nc) cc = (H.be == 'p') ? 0 : c;
+    if (!hs_valid(mask, H.nc, rr, cc))
+    {
+        rr = r;
+        cc = c;
+    }
+}
 
 __device__ __forceinline__ double hs_slope_x(const HsN& P, const std::uint8_t* mask, const double* z, int r, int c)
 {
     const std::int64_t e = hs_nb(P.H, mask, r, c, 0, 1), w = hs_nb(P.H, mask, r, c, 0, -1);
-    return (z[e] - z[w]) / (2.0 * P.h);
+    return (z[e] - z[w]) * P.inv_2h;
 }
 
 __device__ __forceinline__ double hs_slope_y(const HsN& P, const std::uint8_t* mask, const double* z, int r, int c)
 {
     const std::int64_t s = hs_nb(P.H, mask, r, c, 1, 0), n = hs_nb(P.H, mask, r, c, -1, 0);
-    return (z[s] - z[n]) / (2.0 * P.h);
+    return (z[s] - z[n]) * P.inv_2h;
 }
 
 // Per DOF: face alphas (float4 N,E,S,W), residual F (double), and the
@@ -386,15 +417,16 @@ __global__ void hsn_eval(HsN P, const std::uint8_t* __restrict__ mask, const std
 #pragma unroll
         for (int f = 0; f < 4; ++f)
         {
-            const std::int64_t j = hs_nb(P.H, mask, r, c, kDr[f], kDc[f]);
-            const double sn = (z[j] - zc) / P.h;
+            int jr, jc;
+            hs_nb_rc(P.H, mask, r, c, kDr[f], kDc[f], jr, jc);
+            const std::int64_t j = static_cast<std::int64_t>(jr) * P.H.nc + jc;
+            const double sn = (z[j] - zc) * P.inv_h;
             double al = 1.0;
             if (P.nonlinear)
             {
-                const int jr = static_cast<int>(j / P.H.nc), jc = static_cast<int>(j % P.H.nc);
                 const double st = (f == 0 || f == 2) ? 0.5 * (sxc + hs_slope_x(P, mask, z, jr, jc))
                                                      : 0.5 * (syc + hs_slope_y(P, mask, z, jr, jc));
-                const double s2 = fmin((sn * sn + st * st) / P.Sc2, P.cap);
+                const double s2 = fmin((sn * sn + st * st) * P.inv_Sc2, P.cap);
                 al = 1.0 / (1.0 - s2);
             }
             a[f] = al;
@@ -407,7 +439,7 @@ __global__ void hsn_eval(HsN P, const std::uint8_t* __restrict__ mask, const std
         F[i] = Fv;
         finf = fabs(Fv);
         f2 = Fv * Fv;
-        if (P.nonlinear) ratio = sqrt(sxc * sxc + syc * syc) / sqrt(P.Sc2);
+        if (P.nonlinear) ratio = sqrt(sxc * sxc + syc * syc) * P.inv_Sc;
     }
     else if (i < n)
     {
@@ -1186,6 +1218,7 @@ int hillslope_implicit_impl(const std::string& who, const lsdtt_gpu_grid* grid, 
     P.H.U = 0.0;
     P.Sc2 = static_cast<double>(Sc) * static_cast<double>(Sc);
     P.cap = 0.9999;
+    hsn_reciprocals(P);
     P.nonlinear = nonlinear ? 1 : 0;
     const int kPcg = max_pcg_iter > 0 ? max_pcg_iter : 2000;
     const int kOuter = max_outer > 0 ? max_outer : 200;
@@ -1416,6 +1449,7 @@ extern "C" int lsdtt_gpu_hillslope_capture_pairs(const lsdtt_gpu_grid* grid, con
     P.H.inv_dt = 1.0 / static_cast<double>(dt);
     P.Sc2 = static_cast<double>(Sc) * static_cast<double>(Sc);
     P.cap = 0.9999;
+    hsn_reciprocals(P);
     P.nonlinear = nonlinear ? 1 : 0;
     const int kPcg = max_iter > 0 ? max_iter : 2000;
     const double rtol = rel_tol > 0 ? rel_tol : 1e-8;
