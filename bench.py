@@ -617,7 +617,9 @@ def train_preconditioner(G, size, cell, D, Sc, dt, nonlinear, n_surfaces, pairs_
     net = G.UNet(size, size, seed=seed)
     order = np.random.default_rng(seed).integers(0, r.shape[0], steps)
     t0 = time.perf_counter()
-    losses = [net.train_step(r[k], e[k], lr=2e-3) for k in order]
+    # Adam, one pair a step, learning rate 2e-3 cosine-decayed to 2e-4
+    lrs = 2e-4 + 0.5 * (2e-3 - 2e-4) * (1.0 + np.cos(np.pi * np.arange(steps) / max(1, steps)))
+    losses = [net.train_step(r[k], e[k], lr=float(lr)) for k, lr in zip(order, lrs)]
     torch.cuda.synchronize()
     if capacity > size:
         # an inference-only copy sized for the target grid (no training buffers)
@@ -805,7 +807,7 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--workload", default="ensemble", choices=["ensemble", "routing", "large", "hillslope", "unet"])
     ap.add_argument("--train-surfaces", type=int, default=64)
-    ap.add_argument("--train-steps", type=int, default=2000)
+    ap.add_argument("--train-steps", type=int, default=4000)
     ap.add_argument("--members", type=int, default=256)
     ap.add_argument("--sweep-mode", type=int, default=-1, help="ensemble sweep: -1 autotuned, 0 levels, 1 dataflow, 2 cooperative levels, 3 member clusters")
     ap.add_argument("--plain-members", type=int, default=16)
