@@ -455,6 +455,7 @@ def ensemble_gpu(args, rank, world):
         return float(tt.item())
 
     ens = G.Ensemble(specs, use_graph=True)
+    ens.set_member_groups(bool(args.member_groups))
     if args.sweep_mode >= 0:
         # pin the stream-power sweep schedule (a profiler distorts the
         # autotuner's own timings)
@@ -811,6 +812,8 @@ def main():
     ap.add_argument("--members", type=int, default=256)
     ap.add_argument("--sweep-mode", type=int, default=-1, help="ensemble sweep: -1 autotuned, 0 levels, 1 dataflow, 2 cooperative levels, 3 member clusters")
     ap.add_argument("--plain-members", type=int, default=16)
+    ap.add_argument("--member-groups", type=int, default=0, choices=[0, 1],
+                    help="ensemble: the deep members' sweep beside the others' sweep and hillslope solve (1) or not")
     ap.add_argument("--conv-kernel", default="", choices=["", "mma", "tcgen05", "tcgen05_rows", "tcgen05_ws"],
                     help="U-Net convolution kernels (default: the library's)")
     args = ap.parse_args()

@@ -395,7 +395,8 @@ typedef struct lsdtt_gpu_ensemble_info
     double untuned_sweep_ms;      /* ... and one launch per level */
     int32_t sweep_dataflow;       /* sweep in use: 0 level launches, 1 in-order dataflow, 2 cooperative levels,
                                      3 member clusters */
-    int32_t reserved;
+    int32_t deep_members;         /* captured steps: members in the deep group, whose sweep runs beside the
+                                     other members' sweep and hillslope solve (0: one group) */
     double dataflow_sweep_ms;     /* autotuner: the dataflow sweep's time */
     double coop_sweep_ms;         /* autotuner: the cooperative level sweep's best time */
     double cluster_sweep_ms;      /* autotuner: the member-cluster sweep's time */
@@ -412,6 +413,15 @@ int lsdtt_gpu_ensemble_get_info(const lsdtt_gpu_ensemble* ens, lsdtt_gpu_ensembl
  * the autotuner). */
 int lsdtt_gpu_ensemble_override_schedule(lsdtt_gpu_ensemble* ens, int32_t fill_pass_cap,
                                          int32_t hillslope_iteration_cap, int32_t sweep_mode);
+/* Member groups of captured steps (off by default): with the member-cluster
+ * sweep, the members deeper than 3/4 of the deepest sweep on a second,
+ * high-priority stream while the others sweep and solve their hillslope,
+ * and their own solve follows. The results are the same either way. On the
+ * 256-member benchmark ensemble it was slower (the others' PCG traffic
+ * slows the latency-bound deep sweep, and depths cluster near the
+ * deepest), so it is an option for ensembles with a few much deeper
+ * members. 1 turns it on, 0 off (the next step captures again). */
+int lsdtt_gpu_ensemble_set_member_groups(lsdtt_gpu_ensemble* ens, int32_t enabled);
 
 /* ---- whole routing pass with host buffers ---------------------------------
  * fill_pits(z, min_slope, bc) then lsdtt_flowinfo on the filled surface, then

@@ -310,7 +310,7 @@ class EnsembleInfo(ctypes.Structure):
                 ("hillslope_iteration_cap", ctypes.c_int32), ("last_fill_passes", ctypes.c_int32),
                 ("last_max_depth", ctypes.c_int32), ("last_hillslope_iterations", ctypes.c_int32),
                 ("tuned_sweep_ms", ctypes.c_double), ("untuned_sweep_ms", ctypes.c_double),
-                ("sweep_dataflow", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("sweep_dataflow", ctypes.c_int32), ("deep_members", ctypes.c_int32),
                 ("dataflow_sweep_ms", ctypes.c_double), ("coop_sweep_ms", ctypes.c_double),
                 ("cluster_sweep_ms", ctypes.c_double)]
 
@@ -335,6 +335,7 @@ def _bind_more():
         "lsdtt_gpu_ensemble_step": [vp, i32, ctypes.POINTER(LemStats), vp],
         "lsdtt_gpu_ensemble_get_info": [vp, ctypes.POINTER(EnsembleInfo)],
         "lsdtt_gpu_ensemble_override_schedule": [vp, i32, i32, i32],
+        "lsdtt_gpu_ensemble_set_member_groups": [vp, i32],
         "lsdtt_gpu_ensemble_upload": [vp, vp, vp],
         "lsdtt_gpu_ensemble_download": [vp, vp, vp],
     }.items():
@@ -500,6 +501,11 @@ class Ensemble:
         clusters) or -1 (autotuned)."""
         _check(lib().lsdtt_gpu_ensemble_override_schedule(self._h, fill_pass_cap, hillslope_iteration_cap,
                                                           sweep_mode))
+
+    def set_member_groups(self, enabled: bool) -> None:
+        """Member groups of captured steps (the deep members' sweep beside
+        the others' sweep and hillslope solve); off by default, same results."""
+        _check(lib().lsdtt_gpu_ensemble_set_member_groups(self._h, 1 if enabled else 0))
 
     def info(self):
         i = EnsembleInfo()

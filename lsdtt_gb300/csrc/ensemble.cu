@@ -142,6 +142,22 @@ __global__ void ens_dirty_init(std::int32_t T, const std::uint16_t* __restrict__
     d1[t] = v;
 }
 
+// Both pass-parity edge buffers of every fill tile from the initial field
+// (one thread per tile edge slot).
+__global__ void ens_edge_init(Packed P, const std::uint16_t* __restrict__ tile_member, std::int32_t T,
+                              const std::uint8_t* __restrict__ kind, const float* __restrict__ F,
+                              float* __restrict__ e0, float* __restrict__ e1)
+{
+    LSDTT_COUNT();
+    const std::int64_t q = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (q >= static_cast<std::int64_t>(T) * kEdge) return;
+    const int t = static_cast<int>(q / kEdge), slot = static_cast<int>(q % kEdge);
+    const PackedMember& M = P.m[tile_member[t]];
+    const int local = t - M.tile_base;
+    edge_export_from_field(M.nr, M.nc, kind + M.base, F + M.base, e0, t, local % M.ntx, local / M.ntx, slot);
+    edge_export_from_field(M.nr, M.nc, kind + M.base, F + M.base, e1, t, local % M.ntx, local / M.ntx, slot);
+}
+
 // Active tiles of a fill pass, one thread per tile: tile t is active when
 // it or one of its eight neighbours in its member's tile grid (periodic axes
 // wrap) changed in the previous pass. Clears dirty_out[t] (the relaxation
@@ -205,7 +221,9 @@ __global__ void __launch_bounds__(256) ens_fill_relax_list(Packed P, const EnsPa
                                                            const std::uint8_t* __restrict__ din,
                                                            std::uint8_t* __restrict__ dout,
                                                            const std::int32_t* __restrict__ list,
-                                                           const unsigned long long* __restrict__ cnt)
+                                                           const unsigned long long* __restrict__ cnt,
+                                                           const float* __restrict__ edges_in,
+                                                           float* __restrict__ edges_out)
 {
     LSDTT_COUNT();
     const std::int64_t n = static_cast<std::int64_t>(cnt[0]);
@@ -218,7 +236,7 @@ __global__ void __launch_bounds__(256) ens_fill_relax_list(Packed P, const EnsPa
         const int local = t - M.tile_base;
         fill_relax_tile(M.nr, M.nc, q.per_ns, q.per_ew, q.L, q.Ld, q.fill_eps, z + M.base, kind + M.base,
                         F + M.base, changed, din + M.tile_base, dout + M.tile_base, local % M.ntx, local / M.ntx,
-                        M.ntx, M.nty, false);
+                        M.ntx, M.nty, false, edges_in, edges_out, M.tile_base);
         __syncthreads();  // the tile's shared arrays are staged again for the next tile
     }
 }
@@ -959,8 +977,9 @@ constexpr int kHsSlot = 4;
 // The FP64 stage carries the cancellation-prone part of a grid-wide dot
 // product; per-thread FP64 arithmetic, scarce on this part, is avoided.
 __device__ __forceinline__ void block_partial_f(float v, bool is_max, double* __restrict__ part, std::int64_t nblk,
-                                                int q)
+                                                int q, std::int64_t blk = -1)
 {
+    if (blk < 0) blk = blockIdx.x;  // the partial's index: the block, or the block a list mapped it to
     __shared__ double shf[32];
     for (int o = 16; o > 0; o >>= 1)
     {
@@ -983,7 +1002,7 @@ __device__ __forceinline__ void block_partial_f(float v, bool is_max, double* __
             const double w = __shfl_down_sync(0xffffffffu, t, o);
             t = is_max ? fmax(t, w) : t + w;
         }
-        if (threadIdx.x == 0) part[q * nblk + blockIdx.x] = t;
+        if (threadIdx.x == 0) part[q * nblk + blk] = t;
     }
 }
 
@@ -994,8 +1013,9 @@ __device__ __forceinline__ void block_partial_f(float v, bool is_max, double* __
 // instructions per block for all NQ. Call once per kernel.
 template <int NQ>
 __device__ __forceinline__ void block_partials_f(const float (&v)[NQ], unsigned max_mask, double* __restrict__ part,
-                                                 std::int64_t nblk)
+                                                 std::int64_t nblk, std::int64_t blk = -1)
 {
+    if (blk < 0) blk = blockIdx.x;
     static_assert(32 % NQ == 0, "NQ must divide the warp");
     __shared__ float sw[32][NQ];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -1029,7 +1049,7 @@ __device__ __forceinline__ void block_partials_f(const float (&v)[NQ], unsigned 
             const double y = __shfl_xor_sync(0xffffffffu, t, o);
             t = is_max ? fmax(t, y) : t + y;
         }
-        if (g == 0) part[q * nblk + blockIdx.x] = t;
+        if (g == 0) part[q * nblk + blk] = t;
     }
 }
 
@@ -1076,11 +1096,14 @@ __global__ void ens_member_reduce(Packed P, int nq, unsigned max_mask, const dou
 // so no large term cancels. Block partials of ||b||^2.
 __global__ void ens_hs_setup(Packed P, const EnsParams* __restrict__ prm, const std::uint8_t* __restrict__ mask,
                              const float* __restrict__ z, std::uint8_t* __restrict__ dof, float* __restrict__ inv_diag,
-                             float* __restrict__ b, double* __restrict__ part)
+                             float* __restrict__ b, double* __restrict__ part,
+                             const std::int32_t* __restrict__ blist = nullptr)
 {
     LSDTT_COUNT();
-    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    const int m = block_member(P);
+    // the block: this one, or (a member group's solve) its list entry
+    const std::int64_t blk = blist ? blist[blockIdx.x] : static_cast<std::int64_t>(blockIdx.x);
+    const std::int64_t i = blk * blockDim.x + threadIdx.x;
+    const int m = P.blk_member[blk];
     const PackedMember& M = P.m[m];
     const EnsParams& q = prm[m];
     const Hs& H = q.hs;
@@ -1136,7 +1159,7 @@ __global__ void ens_hs_setup(Packed P, const EnsParams* __restrict__ prm, const 
             inv_diag[i] = 0.0f;
         }
     }
-    block_partial_f(bb, false, part, P.n / kPackAlign, 0);
+    block_partial_f(bb, false, part, P.n / kPackAlign, 0, blk);
 }
 
 // Start from x0 (the previous step's increment; zero at non-DOF cells):
@@ -1144,10 +1167,11 @@ __global__ void ens_hs_setup(Packed P, const EnsParams* __restrict__ prm, const 
 __global__ void ens_hs_init(Packed P, const float* __restrict__ b, const float* __restrict__ inv_diag,
                             const std::uint8_t* __restrict__ dof, const float* __restrict__ Ax0,
                             float* __restrict__ x, float* __restrict__ r, float* __restrict__ p,
-                            double* __restrict__ part)
+                            double* __restrict__ part, const std::int32_t* __restrict__ blist = nullptr)
 {
     LSDTT_COUNT();
-    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const std::int64_t blk = blist ? blist[blockIdx.x] : static_cast<std::int64_t>(blockIdx.x);
+    const std::int64_t i = blk * blockDim.x + threadIdx.x;
     float rz = 0.0f;
     if (i < P.n)
     {
@@ -1159,18 +1183,29 @@ __global__ void ens_hs_init(Packed P, const float* __restrict__ b, const float* 
         p[i] = zi;
         rz = ri * zi;
     }
-    block_partial_f(rz, false, part, P.n / kPackAlign, 0);
+    block_partial_f(rz, false, part, P.n / kPackAlign, 0, blk);
 }
 
 // done[m] = no hillslope or nothing to solve; iters[m] = 0
 __global__ void ens_hs_start(int M, const EnsParams* __restrict__ prm, const double* __restrict__ hs_bb,
-                             int* __restrict__ done, int* __restrict__ iters)
+                             int* __restrict__ done, int* __restrict__ iters, const std::uint8_t* __restrict__ grp,
+                             int g)
 {
     LSDTT_COUNT();
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= M) return;
+    if (grp && grp[m] != g) return;  // another member group's solve: stays done here
     done[m] = (!prm[m].hill_on || hs_bb[m] == 0.0) ? 1 : 0;
     iters[m] = 0;
+}
+
+// done[m] = 1 for the members outside group g (grp = null: every member
+// takes part), so the solve's reductions and PCG kernels skip them.
+__global__ void ens_group_done(int M, const std::uint8_t* __restrict__ grp, int g, int* __restrict__ done)
+{
+    LSDTT_COUNT();
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m < M) done[m] = (grp && grp[m] != g) ? 1 : 0;
 }
 
 // Ap = A p in the difference form inv_dt p_P + (D/h^2) sum_f (p_P - [nb DOF]
@@ -1192,7 +1227,7 @@ __global__ void ens_hs_start(int M, const EnsParams* __restrict__ prm, const dou
 // so every load and store of a warp is contiguous. One p.Ap partial per tile.
 template <bool kFuse>
 __device__ __forceinline__ void hs_apply_tile(float (&sp)[kD8TileRows + 2][132], const PackedMember& M,
-                                              const EnsParams& q, int tx, int ty,
+                                              const EnsParams& q, int tile, int tx, int ty,
                                               const std::uint8_t* __restrict__ mask,
                                               const std::uint8_t* __restrict__ dof, float beta,
                                               const float* __restrict__ zz, const float* __restrict__ p_src,
@@ -1277,7 +1312,7 @@ __device__ __forceinline__ void hs_apply_tile(float (&sp)[kD8TileRows + 2][132],
             Ap[i] = v;
         }
     }
-    block_partial_f(pap, false, part, nblk, 0);
+    block_partial_f(pap, false, part, nblk, 0, tile);
 }
 
 __global__ void __launch_bounds__(256, 4) ens_hs_apply_tiled(Packed P, const EnsParams* __restrict__ prm,
@@ -1289,23 +1324,27 @@ __global__ void __launch_bounds__(256, 4) ens_hs_apply_tiled(Packed P, const Ens
                                                           const int* __restrict__ it_dev,
                                                           const float* __restrict__ zz,
                                                           const float* __restrict__ p_src, float* __restrict__ p_dst,
-                                                          float* __restrict__ Ap, double* __restrict__ part)
+                                                          float* __restrict__ Ap, double* __restrict__ part,
+                                                          const std::int32_t* __restrict__ tlist = nullptr)
 {
     LSDTT_COUNT();
-    const int m = rtile_member[blockIdx.x];
+    // the receiver tile: this block's, or (a member group's solve) the
+    // tile its list entry names
+    const int tile = tlist ? tlist[blockIdx.x] : static_cast<int>(blockIdx.x);
+    const int m = rtile_member[tile];
     if (done[m]) return;
     if (it_dev && *it_dev > 0) fuse = 1;
     const PackedMember& M = P.m[m];
     const EnsParams& q = prm[m];
-    const int local = static_cast<int>(blockIdx.x) - M.rtile_base;
+    const int local = tile - M.rtile_base;
     const std::int64_t nblk = P.n / kPackAlign;
     __shared__ float sp[kD8TileRows + 2][132];
     if (fuse)
-        hs_apply_tile<true>(sp, M, q, local % M.nrx, local / M.nrx, mask, dof, beta_m[m], zz, p_src, p_dst, Ap, part,
-                            nblk);
+        hs_apply_tile<true>(sp, M, q, tile, local % M.nrx, local / M.nrx, mask, dof, beta_m[m], zz, p_src, p_dst, Ap,
+                            part, nblk);
     else
-        hs_apply_tile<false>(sp, M, q, local % M.nrx, local / M.nrx, mask, dof, 0.0f, zz, p_src, p_dst, Ap, part,
-                             nblk);
+        hs_apply_tile<false>(sp, M, q, tile, local % M.nrx, local / M.nrx, mask, dof, 0.0f, zz, p_src, p_dst, Ap,
+                             part, nblk);
 }
 
 // x += alpha p; r -= alpha Ap; z = M^-1 r (alpha_m: each member's
@@ -1313,11 +1352,13 @@ __global__ void __launch_bounds__(256, 4) ens_hs_apply_tiled(Packed P, const Ens
 __global__ void ens_hs_update(Packed P, const int* __restrict__ done, const float* __restrict__ alpha_m,
                               const float* __restrict__ inv_diag, const float* __restrict__ p,
                               const float* __restrict__ Ap, float* __restrict__ x, float* __restrict__ r,
-                              float* __restrict__ zz, double* __restrict__ part)
+                              float* __restrict__ zz, double* __restrict__ part,
+                              const std::int32_t* __restrict__ blist = nullptr)
 {
     LSDTT_COUNT();
-    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    const int m = P.blk_member[blockIdx.x];  // kPackAlign-cell blocks: one member each
+    const std::int64_t blk = blist ? blist[blockIdx.x] : static_cast<std::int64_t>(blockIdx.x);
+    const std::int64_t i = blk * blockDim.x + threadIdx.x;
+    const int m = P.blk_member[blk];  // kPackAlign-cell blocks: one member each
     if (done[m]) return;
     const float alpha = alpha_m[m];
     float rz = 0.0f, rr = 0.0f;
@@ -1332,7 +1373,7 @@ __global__ void ens_hs_update(Packed P, const int* __restrict__ done, const floa
         rr = ri * ri;
     }
     const float rv[2] = {rz, rr};
-    block_partials_f<2>(rv, 0u, part, P.n / kPackAlign);
+    block_partials_f<2>(rv, 0u, part, P.n / kPackAlign, blk);
 }
 
 // After iteration `it` (0-based, it + 1 a multiple of 4 or the last one):
@@ -1407,12 +1448,14 @@ __global__ void ens_pcg_while(int* __restrict__ it_dev, int itmax, int* __restri
     cudaGraphSetConditional(h, (active > 0 && it < itmax) ? 1u : 0u);
 }
 
-__global__ void ens_hs_finish(std::int64_t n, const std::uint8_t* __restrict__ dof, const float* __restrict__ zsp,
-                              const float* __restrict__ x, float* __restrict__ out)
+__global__ void ens_hs_finish(Packed P, const std::uint8_t* __restrict__ dof, const float* __restrict__ zsp,
+                              const float* __restrict__ x, float* __restrict__ out,
+                              const std::int32_t* __restrict__ blist = nullptr)
 {
     LSDTT_COUNT();
-    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    const std::int64_t blk = blist ? blist[blockIdx.x] : static_cast<std::int64_t>(blockIdx.x);
+    const std::int64_t i = blk * blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
     out[i] = dof[i] ? static_cast<float>(static_cast<double>(zsp[i]) + static_cast<double>(x[i])) : zsp[i];
 }
 
@@ -1505,6 +1548,7 @@ struct lsdtt_gpu_ensemble
     float *z = nullptr, *zf = nullptr, *zsp = nullptr, *zpre = nullptr;
     std::uint8_t *mask = nullptr, *kind = nullptr, *bflag = nullptr, *dirty = nullptr, *oflag = nullptr;
     std::int32_t* flist = nullptr;           // [T] active fill tiles of the current pass
+    float* fedge = nullptr;                  // [2][T][kEdge] pass-start tile edges of the fill
     unsigned long long* fcnt = nullptr;      // [2] their count and cells
     unsigned long long* h_fcnt = nullptr;    // pinned copy (eager steps)
     unsigned fill_grid = 0;                  // persistent grid of the listed relaxation
@@ -1538,6 +1582,20 @@ struct lsdtt_gpu_ensemble
     cudaGraphExec_t exec = nullptr;
     cudaStream_t own = nullptr;  // private stream: the legacy default stream cannot be captured
     cudaStream_t own2 = nullptr;  // captures the bodies of the graph's device-side loops
+    cudaStream_t own3 = nullptr;  // the deep member group's sweep (captured steps)
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    // Member groups of captured steps: the deep group (members deeper than
+    // half the deepest, a prefix of perm) sweeps on own3 while the shallow
+    // group sweeps and solves its hillslope on the main stream; the deep
+    // group's solve follows the join. Block / receiver-tile lists per group.
+    int n_deep = 0;
+    bool groups_on = false;                 // lsdtt_gpu_ensemble_set_member_groups (off: measured slower
+                                            // on the bench ensemble, 62.1 vs 59.9 ms a step)
+    std::vector<std::uint32_t> depth_last;  // members' deepest levels of the last eager step
+    std::uint16_t* perm_cap = nullptr;      // the member order the captured graph's sweeps use
+    std::int32_t* glist = nullptr;   // [blocks of group 0][blocks of group 1][tiles of 0][tiles of 1]
+    std::int64_t gcount[4] = {0, 0, 0, 0};
+    std::uint8_t* grp = nullptr;     // [M] 1 = deep group
     bool use_while = true;        // device-side loops (conditional WHILE nodes) in the graph
     int* loopc = nullptr;         // [2] their trip counters (fill pass pairs, PCG iterations)
     cudaEvent_t ev_in = nullptr, ev_out = nullptr;  // order the private stream after/before the caller's
@@ -1580,30 +1638,86 @@ void free_ensemble(lsdtt_gpu_ensemble* E)
     if (E->graph) cudaGraphDestroy(E->graph);
     void* bufs[] = {E->d_pm, E->d_prm, E->blk_member, E->tile_member, E->strip_member, E->undecided, E->bar, E->loopc, E->pcg_scal, E->morder, E->mstart, E->mmax, E->perm, E->z, E->zf, E->zsp, E->zpre, E->kind, E->bflag, E->dirty, E->oflag, E->pos, E->nd, E->area, E->order, E->lstart, E->lcount,
                     E->lfill, E->maxd, E->dof, E->invd, E->b, E->x, E->r, E->p, E->p2, E->zz, E->Ap, E->hs_bb, E->hs_acc,
-                    E->done, E->iters, E->stats_acc, E->part, E->kam_tab, E->flags, E->zg, E->dfc, E->flist, E->fcnt};
+                    E->done, E->iters, E->stats_acc, E->part, E->kam_tab, E->flags, E->zg, E->dfc, E->flist, E->fcnt, E->glist, E->grp, E->perm_cap, E->fedge};
     for (void* q : bufs) cudaFree(q);
     void* hb[] = {E->h_stats, E->h_flags, E->h_iters, E->h_maxd, E->h_err, E->h_fcnt};
     for (void* q : hb) cudaFreeHost(q);
     if (E->f) lsdtt_gpu_flow_destroy(E->f);
     if (E->own) cudaStreamDestroy(E->own);
     if (E->own2) cudaStreamDestroy(E->own2);
+    if (E->own3) cudaStreamDestroy(E->own3);
+    if (E->ev_fork) cudaEventDestroy(E->ev_fork);
+    if (E->ev_join) cudaEventDestroy(E->ev_join);
     if (E->ev_in) cudaEventDestroy(E->ev_in);
     if (E->ev_out) cudaEventDestroy(E->ev_out);
     delete E;
 }
 
+// Member groups of a captured graph, set right before the capture from the
+// last eager step's member order (perm_h, deepest first) and depths: the
+// deep group is the prefix of that order deeper than 3/4 of the deepest
+// member; its sweep runs beside the shallow group's sweep and hillslope
+// solve. The graph keeps its own copy of the order (perm_cap), so eager
+// steps that re-sort perm (a profiled step) leave the graph's groups, lists
+// and order consistent. Any grouping gives the same result (each group's
+// sweep precedes its own solve); only the overlap depends on it. No groups
+// when the deepest member is shallow (the sweep is short) or one group
+// would be empty.
+constexpr std::uint32_t kSplitMinDepth = 64;
+
+cudaError_t set_member_groups(lsdtt_gpu_ensemble* E, const std::vector<std::uint32_t>& depth_h, cudaStream_t st)
+{
+    const int M = E->M;
+    if (depth_h.size() != static_cast<std::size_t>(M))
+    {
+        E->n_deep = 0;
+        return cudaSuccess;
+    }
+    const std::uint32_t dmax = depth_h[E->perm_h[0]];
+    int nd = 0;
+    while (nd < M && 4ull * depth_h[E->perm_h[static_cast<std::size_t>(nd)]] > 3ull * dmax) ++nd;
+    E->n_deep = (nd > 0 && nd < M && dmax >= kSplitMinDepth) ? nd : 0;
+    std::vector<std::uint8_t> g(static_cast<std::size_t>(M), 0);
+    for (int k = 0; k < E->n_deep; ++k) g[E->perm_h[static_cast<std::size_t>(k)]] = 1;
+    std::vector<std::int32_t> lists[4];
+    for (int m = 0; m < M; ++m)
+    {
+        const PackedMember& Pm = E->pm[static_cast<std::size_t>(m)];
+        const std::int64_t b0 = Pm.base / kPackAlign;
+        const std::int64_t nbm = (static_cast<std::int64_t>(Pm.nr) * Pm.nc + kPackAlign - 1) / kPackAlign;
+        const int gm = g[static_cast<std::size_t>(m)];
+        for (std::int64_t b = b0; b < b0 + nbm; ++b) lists[gm].push_back(static_cast<std::int32_t>(b));
+        for (std::int32_t t = Pm.rtile_base; t < Pm.rtile_base + Pm.nrx * Pm.nry; ++t) lists[2 + gm].push_back(t);
+    }
+    std::vector<std::int32_t> all;
+    for (int k = 0; k < 4; ++k)
+    {
+        E->gcount[k] = static_cast<std::int64_t>(lists[k].size());
+        all.insert(all.end(), lists[k].begin(), lists[k].end());
+    }
+    cudaMemcpyAsync(E->glist, all.data(), sizeof(std::int32_t) * all.size(), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(E->grp, g.data(), static_cast<std::size_t>(M), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(E->perm_cap, E->perm_h.data(), sizeof(std::uint16_t) * M, cudaMemcpyHostToDevice, st);
+    return cudaStreamSynchronize(st);
+}
+
 // Sweep launches for levels 1 .. split-1 (one launch each), then the tail.
 cudaError_t enqueue_sweep(lsdtt_gpu_ensemble* E, const SweepArgs& A, int split, int block,
-                          const std::vector<unsigned>& blocks, cudaStream_t st, int mode)
+                          const std::vector<unsigned>& blocks, cudaStream_t st, int mode, int perm_off = 0,
+                          int perm_count = -1, const std::uint16_t* perm = nullptr)
 {
+    if (!perm) perm = E->perm;
     if (mode == 3)
     {
+        // member clusters for perm[perm_off .. perm_off + perm_count)
+        if (perm_count < 0) perm_count = E->M - perm_off;
+        if (perm_count == 0) return cudaSuccess;
         SweepArgs B = A;
         B.order = E->morder;
         B.start = E->mstart;
         cudaLaunchConfig_t cfg{};
         const unsigned cl = static_cast<unsigned>(E->sweep_cluster);
-        cfg.gridDim = dim3(static_cast<unsigned>(E->M) * cl);
+        cfg.gridDim = dim3(static_cast<unsigned>(perm_count) * cl);
         cfg.blockDim = dim3(static_cast<unsigned>(std::min(block, static_cast<int>(kSweepClusterBlock))));
         cfg.stream = st;
         cudaLaunchAttribute attr{};
@@ -1613,7 +1727,7 @@ cudaError_t enqueue_sweep(lsdtt_gpu_ensemble* E, const SweepArgs& A, int split, 
         attr.val.clusterDim.z = 1;
         cfg.attrs = &attr;
         cfg.numAttrs = 1;
-        return cudaLaunchKernelEx(&cfg, ens_sp_clusters, B, static_cast<const std::uint16_t*>(E->perm),
+        return cudaLaunchKernelEx(&cfg, ens_sp_clusters, B, static_cast<const std::uint16_t*>(perm + perm_off),
                                   static_cast<const std::uint32_t*>(E->mmax));
     }
     if (mode == 2)
@@ -1718,6 +1832,9 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
     ens_fill_init<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->z, E->mask, E->nd, E->zf, E->kind);
     ens_dirty_init<<<grid_blocks(E->T, 256), 256, 0, st>>>(E->T, E->tile_member, E->d_prm, E->dirty,
                                                            E->dirty + E->T);
+    const std::size_t edge_plane = static_cast<std::size_t>(E->T) * kEdge;
+    ens_edge_init<<<grid_blocks(static_cast<std::int64_t>(edge_plane), 256), 256, 0, st>>>(
+        E->P, E->tile_member, E->T, E->kind, E->zf, E->fedge, E->fedge + edge_plane);
     const dim3 fblock(32, 8);
     const double cells = static_cast<double>(E->member_cells);
     const unsigned tb = static_cast<unsigned>((E->T + 255) / 256);
@@ -1739,9 +1856,9 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
             bytes = 9.0 * static_cast<double>(E->h_fcnt[1]);
         }
         LSDTT_TIMED("ens_fill_relax", bytes, s,
-                    (ens_fill_relax_list<<<E->fill_grid, fblock, 0, s>>>(E->P, E->d_prm, E->tile_member, E->z,
-                                                                         E->kind, E->zf, E->flags, din, dout,
-                                                                         E->flist, E->fcnt)));
+                    (ens_fill_relax_list<<<E->fill_grid, fblock, 0, s>>>(
+                        E->P, E->d_prm, E->tile_member, E->z, E->kind, E->zf, E->flags, din, dout, E->flist, E->fcnt,
+                        E->fedge + (pass & 1) * edge_plane, E->fedge + ((pass + 1) & 1) * edge_plane)));
         return cudaSuccess;
     };
     auto relax = [&](int pass) { return pass_on(pass, st, true); };
@@ -1879,6 +1996,7 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
             cudaMemcpyAsync(E->perm, E->perm_h.data(), sizeof(std::uint16_t) * M, cudaMemcpyHostToDevice, st);
             e = cudaStreamSynchronize(st);  // perm_h is updated again by the next eager step
             if (e != cudaSuccess) return e;
+            E->depth_last = depth_h;  // member groups are set at the next capture
         }
     }
     // 3. stream power, swept by depth level
@@ -2001,12 +2119,26 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
                           E->sweep_mode);
         if (e != cudaSuccess) return e;
     }
-    else
+    const bool split_groups = !eager && E->sweep_mode == 3 && E->n_deep > 0 && E->n_deep < M;
+    if (!eager && split_groups)
+    {
+        // the deep group's clusters on own3, the shallow group's here
+        cudaEventRecord(E->ev_fork, st);
+        cudaStreamWaitEvent(E->own3, E->ev_fork, 0);
+        e = enqueue_sweep(E, A, E->split, E->sweep_block, E->level_blocks, E->own3, 3, 0, E->n_deep, E->perm_cap);
+        cudaEventRecord(E->ev_join, E->own3);
+        if (e != cudaSuccess) return e;
+        e = enqueue_sweep(E, A, E->split, E->sweep_block, E->level_blocks, st, 3, E->n_deep, M - E->n_deep,
+                          E->perm_cap);
+        if (e != cudaSuccess) return e;
+    }
+    else if (!eager)
     {
         e = enqueue_sweep(E, A, E->split, E->sweep_block, E->level_blocks, st, E->sweep_mode);
         if (e != cudaSuccess) return e;
     }
-    // 4. hillslope: Jacobi-PCG per member
+    // 4. hillslope: Jacobi-PCG per member, for every member at once or for
+    // one member group (block / receiver-tile lists; the others stay done)
     const std::size_t slot_bytes = sizeof(double) * kHsSlot * M;
     const std::int64_t slot_len = static_cast<std::int64_t>(kHsSlot) * M;
     const bool device_loop = !eager && E->use_while;
@@ -2018,93 +2150,123 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
         ens_member_reduce<<<(warps + 3) / 4, 128, 0, s2>>>(E->P, nq, max_mask, E->part, nblk, dn, dst, stride, off,
                                                            shift, slot_len, tile_partials);
     };
-    cudaMemsetAsync(E->hs_acc, 0, slot_bytes * (static_cast<std::size_t>(itmax) + 1), st);
-    ens_hs_setup<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->mask, E->zsp, E->dof, E->invd, E->b, E->part);
-    reduce(st, 1, 0u, nullptr, E->hs_bb, 1, 0, nullptr);
-    // Warm start: the previous step's increment x (zero at the first step)
-    // as the initial guess; A x0 by one plain apply (p_dst = x).
-    cudaMemsetAsync(E->done, 0, sizeof(int) * M, st);
-    ens_hs_apply_tiled<<<E->S, 256, 0, st>>>(E->P, E->d_prm, E->strip_member, E->mask, E->dof, E->done, 0, E->pcg_scal,
-                                             nullptr, E->zz, E->p2, E->x, E->Ap, E->part);
-    ens_hs_init<<<nb, 256, 0, st>>>(E->P, E->b, E->invd, E->dof, E->Ap, E->x, E->r, E->p, E->part);
-    reduce(st, 1, 0u, nullptr, E->hs_acc, kHsSlot, 1, nullptr);
-    ens_hs_start<<<mb, 128, 0, st>>>(M, E->d_prm, E->hs_bb, E->done, E->iters);
-    // One iteration whose slots are it / it + 1 (it_dev: plus the device-side
-    // counter); p_it lives in pbuf[it % 2] and every iteration but the first
-    // forms it inside the apply.
-    auto iteration = [&](cudaStream_t s2, int it, const int* it_dev, bool timed) {
-        float* p_it = (it & 1) ? E->p2 : E->p;
-        const float* p_prev = (it & 1) ? E->p : E->p2;
-        double* cur = E->hs_acc + slot_len * (it + 1);
-        float* alpha = E->pcg_scal;
-        float* beta = E->pcg_scal + M;
-        if (timed)
-        {
-            // Algorithmic bytes: p 4 in (+ z 4 when fused), Ap 4 out (+ p 4 when fused).
-            LSDTT_TIMED("ens_hillslope_apply", (it ? 16.0 : 8.0) * cells, s2,
-                        (ens_hs_apply_tiled<<<E->S, 256, 0, s2>>>(E->P, E->d_prm, E->strip_member, E->mask, E->dof,
-                                                                  E->done, it ? 1 : 0, beta, it_dev, E->zz, p_prev,
-                                                                  p_it, E->Ap, E->part)));
-        }
-        else
-            ens_hs_apply_tiled<<<E->S, 256, 0, s2>>>(E->P, E->d_prm, E->strip_member, E->mask, E->dof, E->done,
-                                                     it ? 1 : 0, beta, it_dev, E->zz, p_prev, p_it, E->Ap, E->part);
-        reduce(s2, 1, 0u, E->done, cur, kHsSlot, 0, it_dev, 1);
-        // alpha = r.z (slot it) / p.Ap (slot it + 1)
-        ens_pcg_ratio<<<mb, 128, 0, s2>>>(M, E->done, E->hs_acc, it, 1, it + 1, 0, it_dev, alpha);
-        if (timed)
-        {
-            // Algorithmic bytes: the update 24 B/cell.
-            LSDTT_TIMED("ens_hillslope_update", 24.0 * cells, s2,
-                        (ens_hs_update<<<nb, 256, 0, s2>>>(E->P, E->done, alpha, E->invd, p_it, E->Ap, E->x, E->r,
-                                                           E->zz, E->part)));
-        }
-        else
-            ens_hs_update<<<nb, 256, 0, s2>>>(E->P, E->done, alpha, E->invd, p_it, E->Ap, E->x, E->r, E->zz,
-                                              E->part);
-        reduce(s2, 2, 0u, E->done, cur, kHsSlot, 1, it_dev);
-        // beta for the next iteration = r.z (slot it + 1) / r.z (slot it)
-        ens_pcg_ratio<<<mb, 128, 0, s2>>>(M, E->done, E->hs_acc, it + 1, 1, it, 1, it_dev, beta);
-    };
-    if (device_loop)
+    struct HsGroup
     {
-        // Device-side loop: two iterations and the convergence test per trip,
-        // until no member is iterating (each member stops at its own
-        // max_iter; all of them by max_iter_all).
-        cudaMemsetAsync(E->loopc + 1, 0, sizeof(int), st);
-        cudaMemsetAsync(E->flags + 5, 0, sizeof(int), st);
-        e = capture_while(st, E->own2, [&](cudaStream_t s2, cudaGraphConditionalHandle h) {
-            iteration(s2, 0, E->loopc + 1, false);
-            iteration(s2, 1, E->loopc + 1, false);
-            ens_hs_check<<<mb, 128, 0, s2>>>(M, E->d_prm, 1, E->hs_acc + slot_len * 2, E->hs_bb, E->done, E->iters,
-                                             E->flags, E->loopc + 1);
-            ens_pcg_while<<<1, 1, 0, s2>>>(E->loopc + 1, itmax, E->flags, h);
-        });
+        const std::int32_t* blist;  // null: every block
+        unsigned nblk;
+        const std::int32_t* tlist;  // null: every receiver tile
+        unsigned ntile;
+        const std::uint8_t* grp;    // null: every member
+        int g;
+    };
+    auto hillslope_stage = [&](cudaStream_t hs, const HsGroup& G) -> cudaError_t {
+        cudaMemsetAsync(E->hs_acc, 0, slot_bytes * (static_cast<std::size_t>(itmax) + 1), hs);
+        ens_group_done<<<mb, 128, 0, hs>>>(M, G.grp, G.g, E->done);
+        ens_hs_setup<<<G.nblk, 256, 0, hs>>>(E->P, E->d_prm, E->mask, E->zsp, E->dof, E->invd, E->b, E->part, G.blist);
+        reduce(hs, 1, 0u, E->done, E->hs_bb, 1, 0, nullptr);
+        // Warm start: the previous step's increment x (zero at the first step)
+        // as the initial guess; A x0 by one plain apply (p_dst = x).
+        ens_hs_apply_tiled<<<G.ntile, 256, 0, hs>>>(E->P, E->d_prm, E->strip_member, E->mask, E->dof, E->done, 0,
+                                                    E->pcg_scal, nullptr, E->zz, E->p2, E->x, E->Ap, E->part, G.tlist);
+        ens_hs_init<<<G.nblk, 256, 0, hs>>>(E->P, E->b, E->invd, E->dof, E->Ap, E->x, E->r, E->p, E->part, G.blist);
+        reduce(hs, 1, 0u, E->done, E->hs_acc, kHsSlot, 1, nullptr);
+        ens_hs_start<<<mb, 128, 0, hs>>>(M, E->d_prm, E->hs_bb, E->done, E->iters, G.grp, G.g);
+        // One iteration whose slots are it / it + 1 (it_dev: plus the device-side
+        // counter); p_it lives in pbuf[it % 2] and every iteration but the first
+        // forms it inside the apply.
+        auto iteration = [&](cudaStream_t s2, int it, const int* it_dev, bool timed) {
+            float* p_it = (it & 1) ? E->p2 : E->p;
+            const float* p_prev = (it & 1) ? E->p : E->p2;
+            double* cur = E->hs_acc + slot_len * (it + 1);
+            float* alpha = E->pcg_scal;
+            float* beta = E->pcg_scal + M;
+            if (timed)
+            {
+                // Algorithmic bytes: p 4 in (+ z 4 when fused), Ap 4 out (+ p 4 when fused).
+                LSDTT_TIMED("ens_hillslope_apply", (it ? 16.0 : 8.0) * cells, s2,
+                            (ens_hs_apply_tiled<<<G.ntile, 256, 0, s2>>>(E->P, E->d_prm, E->strip_member, E->mask,
+                                                                         E->dof, E->done, it ? 1 : 0, beta, it_dev, E->zz,
+                                                                         p_prev, p_it, E->Ap, E->part, G.tlist)));
+            }
+            else
+                ens_hs_apply_tiled<<<G.ntile, 256, 0, s2>>>(E->P, E->d_prm, E->strip_member, E->mask, E->dof, E->done,
+                                                            it ? 1 : 0, beta, it_dev, E->zz, p_prev, p_it, E->Ap, E->part,
+                                                            G.tlist);
+            reduce(s2, 1, 0u, E->done, cur, kHsSlot, 0, it_dev, 1);
+            // alpha = r.z (slot it) / p.Ap (slot it + 1)
+            ens_pcg_ratio<<<mb, 128, 0, s2>>>(M, E->done, E->hs_acc, it, 1, it + 1, 0, it_dev, alpha);
+            if (timed)
+            {
+                // Algorithmic bytes: the update 24 B/cell.
+                LSDTT_TIMED("ens_hillslope_update", 24.0 * cells, s2,
+                            (ens_hs_update<<<G.nblk, 256, 0, s2>>>(E->P, E->done, alpha, E->invd, p_it, E->Ap, E->x,
+                                                                   E->r, E->zz, E->part, G.blist)));
+            }
+            else
+                ens_hs_update<<<G.nblk, 256, 0, s2>>>(E->P, E->done, alpha, E->invd, p_it, E->Ap, E->x, E->r, E->zz,
+                                                      E->part, G.blist);
+            reduce(s2, 2, 0u, E->done, cur, kHsSlot, 1, it_dev);
+            // beta for the next iteration = r.z (slot it + 1) / r.z (slot it)
+            ens_pcg_ratio<<<mb, 128, 0, s2>>>(M, E->done, E->hs_acc, it + 1, 1, it, 1, it_dev, beta);
+        };
+        if (device_loop)
+        {
+            // Device-side loop: two iterations and the convergence test per trip,
+            // until no member is iterating (each member stops at its own
+            // max_iter; all of them by max_iter_all).
+            cudaMemsetAsync(E->loopc + 1, 0, sizeof(int), hs);
+            cudaMemsetAsync(E->flags + 5, 0, sizeof(int), hs);
+            e = capture_while(hs, E->own2, [&](cudaStream_t s2, cudaGraphConditionalHandle h) {
+                iteration(s2, 0, E->loopc + 1, false);
+                iteration(s2, 1, E->loopc + 1, false);
+                ens_hs_check<<<mb, 128, 0, s2>>>(M, E->d_prm, 1, E->hs_acc + slot_len * 2, E->hs_bb, E->done, E->iters,
+                                                 E->flags, E->loopc + 1);
+                ens_pcg_while<<<1, 1, 0, s2>>>(E->loopc + 1, itmax, E->flags, h);
+            });
+            if (e != cudaSuccess) return e;
+        }
+        else
+        {
+            int it = 0;
+            for (; it < itmax;)
+            {
+                const int batch = std::min(4, itmax - it);
+                for (int k = 0; k < batch; ++k, ++it) iteration(hs, it, nullptr, true);
+                if (eager) cudaMemsetAsync(E->flags + 5, 0, sizeof(int), hs);
+                ens_hs_check<<<mb, 128, 0, hs>>>(M, E->d_prm, it - 1,
+                                                E->hs_acc + static_cast<std::size_t>(kHsSlot) * M * it, E->hs_bb,
+                                                E->done, E->iters, E->flags);
+                if (eager)
+                {
+                    cudaMemcpyAsync(E->h_flags + 5, E->flags + 5, sizeof(int), cudaMemcpyDeviceToHost, hs);
+                    e = cudaStreamSynchronize(hs);
+                    if (e != cudaSuccess) return e;
+                    if (E->h_flags[5] == 0) break;
+                }
+            }
+            if (eager) rec->pcg_iters = it;
+            else ens_hs_overflow<<<mb, 128, 0, hs>>>(M, E->done, E->flags);
+        }
+        ens_hs_finish<<<G.nblk, 256, 0, hs>>>(E->P, E->dof, E->zsp, E->x, E->z, G.blist);
+        return cudaSuccess;
+    };
+    if (split_groups)
+    {
+        // shallow group beside the deep group's sweep, then the deep group
+        const std::int32_t* L = E->glist;
+        const HsGroup shallow{L, static_cast<unsigned>(E->gcount[0]),
+                              L + E->gcount[0] + E->gcount[1], static_cast<unsigned>(E->gcount[2]), E->grp, 0};
+        const HsGroup deep{L + E->gcount[0], static_cast<unsigned>(E->gcount[1]),
+                           L + E->gcount[0] + E->gcount[1] + E->gcount[2], static_cast<unsigned>(E->gcount[3]),
+                           E->grp, 1};
+        e = hillslope_stage(st, shallow);
         if (e != cudaSuccess) return e;
+        cudaStreamWaitEvent(st, E->ev_join, 0);
+        e = hillslope_stage(st, deep);
     }
     else
-    {
-        int it = 0;
-        for (; it < itmax;)
-        {
-            const int batch = std::min(4, itmax - it);
-            for (int k = 0; k < batch; ++k, ++it) iteration(st, it, nullptr, true);
-            if (eager) cudaMemsetAsync(E->flags + 5, 0, sizeof(int), st);
-            ens_hs_check<<<mb, 128, 0, st>>>(M, E->d_prm, it - 1,
-                                            E->hs_acc + static_cast<std::size_t>(kHsSlot) * M * it, E->hs_bb,
-                                            E->done, E->iters, E->flags);
-            if (eager)
-            {
-                cudaMemcpyAsync(E->h_flags + 5, E->flags + 5, sizeof(int), cudaMemcpyDeviceToHost, st);
-                e = cudaStreamSynchronize(st);
-                if (e != cudaSuccess) return e;
-                if (E->h_flags[5] == 0) break;
-            }
-        }
-        if (eager) rec->pcg_iters = it;
-        else ens_hs_overflow<<<mb, 128, 0, st>>>(M, E->done, E->flags);
-    }
-    ens_hs_finish<<<nb, 256, 0, st>>>(N, E->dof, E->zsp, E->x, E->z);
+        e = hillslope_stage(st, HsGroup{nullptr, nb, nullptr, static_cast<unsigned>(E->S), nullptr, 0});
+    if (e != cudaSuccess) return e;
     // 5. uplift + boundary restore, statistics, flags to the host
     ens_uplift<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->mask, E->bflag, E->zf, E->z);
     ens_stats<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->mask, E->zf, E->z, E->part);
@@ -2138,7 +2300,9 @@ cudaError_t capture(lsdtt_gpu_ensemble* E, const StepRecord& rec, cudaStream_t s
     // levels of this profile above the tuned tail threshold get a launch each
     E->split = E->tail == 0 ? rec.max_depth + 1 : split_for(rec.level_size, E->tail);
     E->level_blocks = level_grid(rec.level_size, E->split, E->sweep_block, 1.5);
-    cudaError_t e = cudaSuccess;
+    cudaError_t e = (E->sweep_mode == 3 && E->groups_on) ? set_member_groups(E, E->depth_last, st) : cudaSuccess;
+    if (e != cudaSuccess) return e;
+    if (E->sweep_mode != 3 || !E->groups_on) E->n_deep = 0;
     cudaGraph_t g = nullptr;
     for (int attempt = 0; attempt < 2; ++attempt)
     {
@@ -2352,8 +2516,13 @@ int lsdtt_gpu_ensemble_create(const lsdtt_gpu_member* members, int32_t n_members
         return s;
     }
     E->mask = E->f->mask;  // the stack reads the engine's mask
+    int lo_prio = 0, hi_prio = 0;  // the deep group's sweep is the step's critical path
+    cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio);
     if (cudaStreamCreateWithFlags(&E->own, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&E->own2, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&E->own3, cudaStreamNonBlocking, hi_prio) != cudaSuccess ||
+        cudaEventCreateWithFlags(&E->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&E->ev_join, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&E->ev_in, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&E->ev_out, cudaEventDisableTiming) != cudaSuccess)
     {
@@ -2379,6 +2548,10 @@ int lsdtt_gpu_ensemble_create(const lsdtt_gpu_member* members, int32_t n_members
     alloc(&E->bflag, n);
     alloc(&E->dirty, 2 * static_cast<std::size_t>(tiles));
     alloc(&E->flist, static_cast<std::size_t>(tiles));
+    alloc(&E->fedge, 2 * static_cast<std::size_t>(tiles) * kEdge);
+    alloc(&E->glist, static_cast<std::size_t>(n / kPackAlign) + static_cast<std::size_t>(strips));
+    alloc(&E->grp, static_cast<std::size_t>(n_members));
+    alloc(&E->perm_cap, static_cast<std::size_t>(n_members));
     alloc(&E->fcnt, 2);
     alloc(&E->oflag, n);
     alloc(&E->pos, n);
@@ -2616,6 +2789,7 @@ int lsdtt_gpu_ensemble_step(lsdtt_gpu_ensemble* E, int32_t n_steps, lsdtt_gpu_le
     E->info.sweep_split_level = E->split;
     E->info.sweep_block = E->sweep_block;
     E->info.sweep_dataflow = E->sweep_mode;
+    E->info.deep_members = E->captured ? E->n_deep : 0;
     E->info.hillslope_iteration_cap = E->it_cap;
     if (stats) fill_stats(E, stats);
     return LSDTT_GPU_OK;
@@ -2649,6 +2823,15 @@ int lsdtt_gpu_ensemble_override_schedule(lsdtt_gpu_ensemble* E, int32_t fill_pas
         E->sweep_mode = sweep_mode;
         E->forced_mode = true;
     }
+    E->captured = false;
+    return LSDTT_GPU_OK;
+}
+
+int lsdtt_gpu_ensemble_set_member_groups(lsdtt_gpu_ensemble* E, int32_t enabled)
+{
+    if (!E || enabled < 0 || enabled > 1)
+        return fail(LSDTT_GPU_EINVAL, "lsdtt_gpu_ensemble_set_member_groups: bad argument");
+    E->groups_on = enabled != 0;
     E->captured = false;
     return LSDTT_GPU_OK;
 }

@@ -111,6 +111,19 @@ __global__ void fill_active(int nr, int nc, bool per_ns, bool per_ew, int ntx, i
     if (active) list[base + __popc(bal & ((1u << lane) - 1u))] = t;
 }
 
+// Both pass-parity edge buffers of every tile from the initial field (one
+// thread per tile edge slot).
+__global__ void fill_edge_init(int nr, int nc, int ntx, int nty, const std::uint8_t* __restrict__ kind,
+                               const float* __restrict__ F, float* __restrict__ e0, float* __restrict__ e1)
+{
+    LSDTT_COUNT();
+    const std::int64_t q = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (q >= static_cast<std::int64_t>(ntx) * nty * kEdge) return;
+    const int t = static_cast<int>(q / kEdge), slot = static_cast<int>(q % kEdge);
+    edge_export_from_field(nr, nc, kind, F, e0, t, t % ntx, t / ntx, slot);
+    edge_export_from_field(nr, nc, kind, F, e1, t, t % ntx, t / ntx, slot);
+}
+
 // Relaxation of the listed active tiles by a persistent grid (block w takes
 // entries w, w + grid, ...), the tile gate skipped: one block per tile spent
 // most of a late pass on inactive tiles reading their neighbours' flags.
@@ -121,7 +134,8 @@ __global__ void __launch_bounds__(256) fill_relax_list(int nr, int nc, bool per_
                                                        const std::uint8_t* __restrict__ dirty_in,
                                                        std::uint8_t* __restrict__ dirty_out, int ntx, int nty,
                                                        const std::int32_t* __restrict__ list,
-                                                       const unsigned long long* __restrict__ cnt)
+                                                       const unsigned long long* __restrict__ cnt,
+                                                       const float* __restrict__ edges_in, float* __restrict__ edges_out)
 {
     LSDTT_COUNT();
     const std::int64_t n = static_cast<std::int64_t>(cnt[0]);
@@ -129,7 +143,7 @@ __global__ void __launch_bounds__(256) fill_relax_list(int nr, int nc, bool per_
     {
         const int t = list[w];
         fill_relax_tile(nr, nc, per_ns, per_ew, L, Ld, min_slope, z, kind, F, changed, dirty_in, dirty_out, t % ntx,
-                        t / ntx, ntx, nty, false);
+                        t / ntx, ntx, nty, false, edges_in, edges_out, 0);
         __syncthreads();  // the tile's shared arrays are staged again for the next tile
     }
 }
@@ -169,12 +183,15 @@ extern "C" int lsdtt_gpu_fill_pits(const lsdtt_gpu_grid* grid, const float* z_de
     int* hflag = nullptr;
     std::uint8_t* dirty = nullptr;  // two per-tile activity planes
     std::int32_t* list = nullptr;   // active tiles of the current pass
+    float* edges = nullptr;         // [2][tiles][kEdge] pass-start tile edges
     unsigned long long* cnt = nullptr;  // their count and cells
     unsigned long long* hcnt = nullptr;
     const std::int64_t ntiles = static_cast<std::int64_t>((nc + kT - 1) / kT) * ((nr + kT - 1) / kT);
     cudaError_t e = cudaMallocAsync(&kind, static_cast<std::size_t>(n), st);
     if (e == cudaSuccess) e = cudaMallocAsync(&dirty, static_cast<std::size_t>(2 * ntiles), st);
     if (e == cudaSuccess) e = cudaMallocAsync(&list, sizeof(std::int32_t) * static_cast<std::size_t>(ntiles), st);
+    if (e == cudaSuccess)
+        e = cudaMallocAsync(&edges, sizeof(float) * 2 * static_cast<std::size_t>(ntiles) * kEdge, st);
     if (e == cudaSuccess) e = cudaMallocAsync(&cnt, sizeof(unsigned long long) * 2, st);
     if (e == cudaSuccess) e = cudaMallocAsync(&flags, sizeof(int) * 2, st);
     if (e == cudaSuccess) e = cudaMallocHost(&hflag, sizeof(int));
@@ -195,6 +212,10 @@ extern "C" int lsdtt_gpu_fill_pits(const lsdtt_gpu_grid* grid, const float* z_de
     const int kCheckEvery = 4;
     const long max_pass = 4L * (nr + nc) + 64;  // bound: any path crosses each tile row/column at most a few times
     const int ntx = static_cast<int>(tiles.x), nty = static_cast<int>(tiles.y);
+    const std::size_t edge_plane = static_cast<std::size_t>(ntiles) * kEdge;
+    fill_edge_init<<<grid_blocks(static_cast<std::int64_t>(edge_plane), 256), 256, 0, st>>>(nr, nc, ntx, nty, kind,
+                                                                                         out_dev, edges,
+                                                                                         edges + edge_plane);
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -223,7 +244,8 @@ extern "C" int lsdtt_gpu_fill_pits(const lsdtt_gpu_grid* grid, const float* z_de
             LSDTT_TIMED("fill_relax", bytes, st,
                         (fill_relax_list<<<list_grid, block, 0, st>>>(nr, nc, per_ns, per_ew, L, Ld, eps, z_dev, kind,
                                                                       out_dev, flags + 1, din, dout, ntx, nty, list,
-                                                                      cnt)));
+                                                                      cnt, edges + (pass & 1) * edge_plane,
+                                                                      edges + ((pass + 1) & 1) * edge_plane)));
         }
         if (e != cudaSuccess) break;
         cudaMemcpyAsync(hflag, flags + 1, sizeof(int), cudaMemcpyDeviceToHost, st);
@@ -239,6 +261,7 @@ extern "C" int lsdtt_gpu_fill_pits(const lsdtt_gpu_grid* grid, const float* z_de
     cudaFreeAsync(kind, st);
     cudaFreeAsync(dirty, st);
     cudaFreeAsync(list, st);
+    cudaFreeAsync(edges, st);
     cudaFreeAsync(cnt, st);
     cudaFreeAsync(flags, st);
     cudaFreeHost(hflag);

@@ -127,3 +127,31 @@ def test_ensemble_errors():
         G.Ensemble([dict(z=z, cell_size=30.0, boundary_conditions="pppp")])
     with pytest.raises(G.GpuError):
         G.Ensemble([dict(z=z, cell_size=30.0, timestep=-1.0)])
+
+
+def test_member_groups_give_the_same_result(port):
+    """Captured steps with member groups (the deep members' sweep on a second
+    stream beside the others' sweep and hillslope solve) against the same
+    steps with one group: identical bits, and the grouped graph ran."""
+    import lsdtt_gb300 as G
+    specs = _members(port)
+    z = port.noise_tilt_surface(384, 512, 30.0, 17, 0.0, 1.0, "nnon", 0.001)
+    specs.append(dict(z=z, cell_size=30.0, boundary_conditions="nnon", timestep=1000.0, erodibility=2e-5,
+                      m_exponent=0.5, n_exponent=1.5, uplift_rate=1e-3, hillslope_diffusivity=0.01,
+                      fill_min_slope=1e-4))
+    out = {}
+    for groups in (True, False):
+        ens = G.Ensemble(specs, use_graph=True)
+        ens.override_schedule(sweep_mode=3)
+        ens.set_member_groups(groups)
+        ens.step(4)
+        info = ens.info()
+        assert info["graph_replays"] >= 3
+        if groups:
+            assert info["deep_members"] > 0, info
+        else:
+            assert info["deep_members"] == 0
+        out[groups] = [ens.get(k).cpu().numpy() for k in range(len(specs))]
+        ens.close()
+    for k, (a, b) in enumerate(zip(out[True], out[False])):
+        assert np.array_equal(a, b), f"member {k}: max |diff| {np.max(np.abs(a - b))}"
