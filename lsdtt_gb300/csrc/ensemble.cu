@@ -142,27 +142,12 @@ __global__ void ens_dirty_init(std::int32_t T, const std::uint16_t* __restrict__
     d1[t] = v;
 }
 
-// Both pass-parity edge buffers of every fill tile from the initial field
-// (one thread per tile edge slot).
-__global__ void ens_edge_init(Packed P, const std::uint16_t* __restrict__ tile_member, std::int32_t T,
-                              const std::uint8_t* __restrict__ kind, const float* __restrict__ F,
-                              float* __restrict__ e0, float* __restrict__ e1)
-{
-    LSDTT_COUNT();
-    const std::int64_t q = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (q >= static_cast<std::int64_t>(T) * kEdge) return;
-    const int t = static_cast<int>(q / kEdge), slot = static_cast<int>(q % kEdge);
-    const PackedMember& M = P.m[tile_member[t]];
-    const int local = t - M.tile_base;
-    edge_export_from_field(M.nr, M.nc, kind + M.base, F + M.base, e0, t, local % M.ntx, local / M.ntx, slot);
-    edge_export_from_field(M.nr, M.nc, kind + M.base, F + M.base, e1, t, local % M.ntx, local / M.ntx, slot);
-}
-
 // Active tiles of a fill pass, one thread per tile: tile t is active when
 // it or one of its eight neighbours in its member's tile grid (periodic axes
 // wrap) changed in the previous pass. Clears dirty_out[t] (the relaxation
-// of an active tile sets it again), appends the active tiles to `list`
-// (warp-aggregated) and counts them (cnt[0]) and their cells (cnt[1]).
+// of an active tile sets it again) and appends the active tiles to the list
+// of their colour within their member (list + colour * T, warp-aggregated),
+// counting them (cnt[colour]) and their cells (cnt[kFillColours]).
 __global__ void ens_fill_active(Packed P, const EnsParams* __restrict__ prm,
                                 const std::uint16_t* __restrict__ tile_member, std::int32_t T,
                                 const std::uint8_t* __restrict__ din, std::uint8_t* __restrict__ dout,
@@ -172,6 +157,7 @@ __global__ void ens_fill_active(Packed P, const EnsParams* __restrict__ prm,
     const std::int32_t t = static_cast<std::int32_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     bool active = false;
     unsigned cells = 0;
+    int colour = -1;
     if (t < T)
     {
         const int m = tile_member[t];
@@ -194,23 +180,26 @@ __global__ void ens_fill_active(Packed P, const EnsParams* __restrict__ prm,
             }
         dout[t] = 0;
         if (active)
+        {
             cells = static_cast<unsigned>(min(kT, M.nr - ty * kT)) * static_cast<unsigned>(min(kT, M.nc - tx * kT));
+            colour = fill_colour(tx, ty, M.ntx, M.nty, q.per_ns, q.per_ew);
+        }
     }
-    const unsigned bal = __ballot_sync(0xffffffffu, active);
     const int lane = threadIdx.x & 31;
-    for (int o = 16; o > 0; o >>= 1) cells += __shfl_down_sync(0xffffffffu, cells, o);
+    const unsigned peers = __match_any_sync(0xffffffffu, colour);
+    const int leader = __ffs(peers) - 1;
     unsigned long long base = 0;
-    if (lane == 0 && bal)
-    {
-        base = atomicAdd(&cnt[0], static_cast<unsigned long long>(__popc(bal)));
-        atomicAdd(&cnt[1], static_cast<unsigned long long>(cells));
-    }
-    base = __shfl_sync(0xffffffffu, base, 0);
-    if (active) list[base + __popc(bal & ((1u << lane) - 1u))] = t;
+    if (active && lane == leader) base = atomicAdd(&cnt[colour], static_cast<unsigned long long>(__popc(peers)));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (active)
+        list[static_cast<std::int64_t>(colour) * T + static_cast<std::int64_t>(base) +
+             __popc(peers & ((1u << lane) - 1u))] = t;
+    for (int o = 16; o > 0; o >>= 1) cells += __shfl_down_sync(0xffffffffu, cells, o);
+    if (lane == 0 && cells) atomicAdd(&cnt[kFillColours], static_cast<unsigned long long>(cells));
 }
 
-// Fill relaxation over the listed active tiles: a persistent grid, block w
-// relaxes tiles w, w + grid, ... of the list (fill_relax_tile with its gate
+// Fill relaxation over one colour's listed active tiles: a persistent grid,
+// block w relaxes tiles w, w + grid, ... of the list (fill_relax_tile with its gate
 // skipped: a pass over every tile spent ~0.2 ms only on inactive tiles
 // reading their neighbours' flags and leaving).
 __global__ void __launch_bounds__(256) ens_fill_relax_list(Packed P, const EnsParams* __restrict__ prm,
@@ -221,12 +210,10 @@ __global__ void __launch_bounds__(256) ens_fill_relax_list(Packed P, const EnsPa
                                                            const std::uint8_t* __restrict__ din,
                                                            std::uint8_t* __restrict__ dout,
                                                            const std::int32_t* __restrict__ list,
-                                                           const unsigned long long* __restrict__ cnt,
-                                                           const float* __restrict__ edges_in,
-                                                           float* __restrict__ edges_out)
+                                                           const unsigned long long* __restrict__ count)
 {
     LSDTT_COUNT();
-    const std::int64_t n = static_cast<std::int64_t>(cnt[0]);
+    const std::int64_t n = static_cast<std::int64_t>(*count);
     for (std::int64_t w = blockIdx.x; w < n; w += gridDim.x)
     {
         const int t = list[w];
@@ -236,7 +223,7 @@ __global__ void __launch_bounds__(256) ens_fill_relax_list(Packed P, const EnsPa
         const int local = t - M.tile_base;
         fill_relax_tile(M.nr, M.nc, q.per_ns, q.per_ew, q.L, q.Ld, q.fill_eps, z + M.base, kind + M.base,
                         F + M.base, changed, din + M.tile_base, dout + M.tile_base, local % M.ntx, local / M.ntx,
-                        M.ntx, M.nty, false, edges_in, edges_out, M.tile_base);
+                        M.ntx, M.nty, false);
         __syncthreads();  // the tile's shared arrays are staged again for the next tile
     }
 }
@@ -1547,9 +1534,8 @@ struct lsdtt_gpu_ensemble
     // state and stage buffers
     float *z = nullptr, *zf = nullptr, *zsp = nullptr, *zpre = nullptr;
     std::uint8_t *mask = nullptr, *kind = nullptr, *bflag = nullptr, *dirty = nullptr, *oflag = nullptr;
-    std::int32_t* flist = nullptr;           // [T] active fill tiles of the current pass
-    float* fedge = nullptr;                  // [2][T][kEdge] pass-start tile edges of the fill
-    unsigned long long* fcnt = nullptr;      // [2] their count and cells
+    std::int32_t* flist = nullptr;           // [kFillColours][T] active fill tiles of the current pass
+    unsigned long long* fcnt = nullptr;      // [kFillColours + 1] their counts by colour, then their cells
     unsigned long long* h_fcnt = nullptr;    // pinned copy (eager steps)
     unsigned fill_grid = 0;                  // persistent grid of the listed relaxation
     std::int64_t* pos = nullptr;
@@ -1638,7 +1624,7 @@ void free_ensemble(lsdtt_gpu_ensemble* E)
     if (E->graph) cudaGraphDestroy(E->graph);
     void* bufs[] = {E->d_pm, E->d_prm, E->blk_member, E->tile_member, E->strip_member, E->undecided, E->bar, E->loopc, E->pcg_scal, E->morder, E->mstart, E->mmax, E->perm, E->z, E->zf, E->zsp, E->zpre, E->kind, E->bflag, E->dirty, E->oflag, E->pos, E->nd, E->area, E->order, E->lstart, E->lcount,
                     E->lfill, E->maxd, E->dof, E->invd, E->b, E->x, E->r, E->p, E->p2, E->zz, E->Ap, E->hs_bb, E->hs_acc,
-                    E->done, E->iters, E->stats_acc, E->part, E->kam_tab, E->flags, E->zg, E->dfc, E->flist, E->fcnt, E->glist, E->grp, E->perm_cap, E->fedge};
+                    E->done, E->iters, E->stats_acc, E->part, E->kam_tab, E->flags, E->zg, E->dfc, E->flist, E->fcnt, E->glist, E->grp, E->perm_cap};
     for (void* q : bufs) cudaFree(q);
     void* hb[] = {E->h_stats, E->h_flags, E->h_iters, E->h_maxd, E->h_err, E->h_fcnt};
     for (void* q : hb) cudaFreeHost(q);
@@ -1832,9 +1818,6 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
     ens_fill_init<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->z, E->mask, E->nd, E->zf, E->kind);
     ens_dirty_init<<<grid_blocks(E->T, 256), 256, 0, st>>>(E->T, E->tile_member, E->d_prm, E->dirty,
                                                            E->dirty + E->T);
-    const std::size_t edge_plane = static_cast<std::size_t>(E->T) * kEdge;
-    ens_edge_init<<<grid_blocks(static_cast<std::int64_t>(edge_plane), 256), 256, 0, st>>>(
-        E->P, E->tile_member, E->T, E->kind, E->zf, E->fedge, E->fedge + edge_plane);
     const dim3 fblock(32, 8);
     const double cells = static_cast<double>(E->member_cells);
     const unsigned tb = static_cast<unsigned>((E->T + 255) / 256);
@@ -1845,20 +1828,24 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
     auto pass_on = [&](int pass, cudaStream_t s, bool timed) -> cudaError_t {
         const std::uint8_t* din = E->dirty + (pass & 1) * E->T;
         std::uint8_t* dout = E->dirty + ((pass + 1) & 1) * E->T;
-        cudaMemsetAsync(E->fcnt, 0, sizeof(unsigned long long) * 2, s);
+        cudaMemsetAsync(E->fcnt, 0, sizeof(unsigned long long) * (kFillColours + 1), s);
         ens_fill_active<<<tb, 256, 0, s>>>(E->P, E->d_prm, E->tile_member, E->T, din, dout, E->flist, E->fcnt);
         double bytes = 9.0 * cells;
         if (timed && profiling_enabled())
         {
-            cudaMemcpyAsync(E->h_fcnt, E->fcnt, sizeof(unsigned long long) * 2, cudaMemcpyDeviceToHost, s);
+            cudaMemcpyAsync(E->h_fcnt, E->fcnt, sizeof(unsigned long long) * (kFillColours + 1),
+                            cudaMemcpyDeviceToHost, s);
             const cudaError_t pe = cudaStreamSynchronize(s);
             if (pe != cudaSuccess) return pe;
-            bytes = 9.0 * static_cast<double>(E->h_fcnt[1]);
+            bytes = 9.0 * static_cast<double>(E->h_fcnt[kFillColours]);
         }
-        LSDTT_TIMED("ens_fill_relax", bytes, s,
-                    (ens_fill_relax_list<<<E->fill_grid, fblock, 0, s>>>(
-                        E->P, E->d_prm, E->tile_member, E->z, E->kind, E->zf, E->flags, din, dout, E->flist, E->fcnt,
-                        E->fedge + (pass & 1) * edge_plane, E->fedge + ((pass + 1) & 1) * edge_plane)));
+        // the colours in turn: a tile reads its neighbours settled
+        LSDTT_TIMED("ens_fill_relax", bytes, s, ({
+                        for (int c = 0; c < kFillColours; ++c)
+                            ens_fill_relax_list<<<E->fill_grid, fblock, 0, s>>>(
+                                E->P, E->d_prm, E->tile_member, E->z, E->kind, E->zf, E->flags, din, dout,
+                                E->flist + static_cast<std::int64_t>(c) * E->T, E->fcnt + c);
+                    }));
         return cudaSuccess;
     };
     auto relax = [&](int pass) { return pass_on(pass, st, true); };
@@ -2547,12 +2534,11 @@ int lsdtt_gpu_ensemble_create(const lsdtt_gpu_member* members, int32_t n_members
     alloc(&E->kind, n);
     alloc(&E->bflag, n);
     alloc(&E->dirty, 2 * static_cast<std::size_t>(tiles));
-    alloc(&E->flist, static_cast<std::size_t>(tiles));
-    alloc(&E->fedge, 2 * static_cast<std::size_t>(tiles) * kEdge);
+    alloc(&E->flist, kFillColours * static_cast<std::size_t>(tiles));
     alloc(&E->glist, static_cast<std::size_t>(n / kPackAlign) + static_cast<std::size_t>(strips));
     alloc(&E->grp, static_cast<std::size_t>(n_members));
     alloc(&E->perm_cap, static_cast<std::size_t>(n_members));
-    alloc(&E->fcnt, 2);
+    alloc(&E->fcnt, kFillColours + 1);
     alloc(&E->oflag, n);
     alloc(&E->pos, n);
     alloc(&E->nd, static_cast<std::size_t>(n_members));
@@ -2593,7 +2579,7 @@ int lsdtt_gpu_ensemble_create(const lsdtt_gpu_member* members, int32_t n_members
     if (e == cudaSuccess) e = cudaMallocHost(&E->h_iters, sizeof(int) * n_members);
     if (e == cudaSuccess) e = cudaMallocHost(&E->h_maxd, sizeof(std::uint32_t));
     if (e == cudaSuccess) e = cudaMallocHost(&E->h_err, sizeof(unsigned long long) * 4);
-    if (e == cudaSuccess) e = cudaMallocHost(&E->h_fcnt, sizeof(unsigned long long) * 2);
+    if (e == cudaSuccess) e = cudaMallocHost(&E->h_fcnt, sizeof(unsigned long long) * (kFillColours + 1));
     {
         int dev = 0, sms = 0;
         cudaGetDevice(&dev);

@@ -55,13 +55,16 @@ __global__ void fill_init(int nr, int nc, bool per_ns, bool per_ew, const float*
     fill_init_cell(nr, nc, per_ns, per_ew, z, mask, nodata, *interior_nd, F, kind, i);
 }
 
+// One colour of a gated pass over every tile (block (x, y) = tile (x, y));
+// the other colours' blocks leave at once.
 __global__ void __launch_bounds__(256) fill_relax(int nr, int nc, bool per_ns, bool per_ew, float L, float Ld,
                                                   float min_slope, const float* __restrict__ z,
                                                   const std::uint8_t* __restrict__ kind, float* __restrict__ F,
                                                   int* __restrict__ changed, const std::uint8_t* __restrict__ dirty_in,
-                                                  std::uint8_t* __restrict__ dirty_out)
+                                                  std::uint8_t* __restrict__ dirty_out, int colour)
 {
     LSDTT_COUNT();
+    if (fill_colour(blockIdx.x, blockIdx.y, gridDim.x, gridDim.y, per_ns, per_ew) != colour) return;
     fill_relax_tile(nr, nc, per_ns, per_ew, L, Ld, min_slope, z, kind, F, changed, dirty_in, dirty_out, blockIdx.x,
                     blockIdx.y, gridDim.x, gridDim.y);
 }
@@ -69,16 +72,18 @@ __global__ void __launch_bounds__(256) fill_relax(int nr, int nc, bool per_ns, b
 // Active tiles of a pass, one thread per tile: tile (tx, ty) is active when
 // it or one of its eight neighbours (periodic axes wrap) changed in the
 // previous pass. Clears dirty_out (an active tile's relaxation sets it
-// again), appends the active tiles to `list` (warp-aggregated) and counts
-// them (cnt[0]) and their cells (cnt[1]).
+// again) and appends the active tiles to the list of their colour
+// (list + colour * cap, warp-aggregated), counting them (cnt[colour]) and
+// their cells (cnt[kFillColours]).
 __global__ void fill_active(int nr, int nc, bool per_ns, bool per_ew, int ntx, int nty,
                             const std::uint8_t* __restrict__ din, std::uint8_t* __restrict__ dout,
-                            std::int32_t* __restrict__ list, unsigned long long* __restrict__ cnt)
+                            std::int32_t* __restrict__ list, std::int64_t cap, unsigned long long* __restrict__ cnt)
 {
     LSDTT_COUNT();
     const std::int32_t t = static_cast<std::int32_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     bool active = false;
     unsigned cells = 0;
+    int colour = -1;
     if (t < ntx * nty)
     {
         const int tx = t % ntx, ty = t / ntx;
@@ -96,37 +101,27 @@ __global__ void fill_active(int nr, int nc, bool per_ns, bool per_ew, int ntx, i
                 }
             }
         dout[t] = 0;
-        if (active) cells = static_cast<unsigned>(min(kT, nr - ty * kT)) * static_cast<unsigned>(min(kT, nc - tx * kT));
+        if (active)
+        {
+            cells = static_cast<unsigned>(min(kT, nr - ty * kT)) * static_cast<unsigned>(min(kT, nc - tx * kT));
+            colour = fill_colour(tx, ty, ntx, nty, per_ns, per_ew);
+        }
     }
-    const unsigned bal = __ballot_sync(0xffffffffu, active);
     const int lane = threadIdx.x & 31;
-    for (int o = 16; o > 0; o >>= 1) cells += __shfl_down_sync(0xffffffffu, cells, o);
+    const unsigned peers = __match_any_sync(0xffffffffu, colour);
+    const int leader = __ffs(peers) - 1;
     unsigned long long base = 0;
-    if (lane == 0 && bal)
-    {
-        base = atomicAdd(&cnt[0], static_cast<unsigned long long>(__popc(bal)));
-        atomicAdd(&cnt[1], static_cast<unsigned long long>(cells));
-    }
-    base = __shfl_sync(0xffffffffu, base, 0);
-    if (active) list[base + __popc(bal & ((1u << lane) - 1u))] = t;
+    if (active && lane == leader) base = atomicAdd(&cnt[colour], static_cast<unsigned long long>(__popc(peers)));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (active) list[colour * cap + static_cast<std::int64_t>(base) + __popc(peers & ((1u << lane) - 1u))] = t;
+    for (int o = 16; o > 0; o >>= 1) cells += __shfl_down_sync(0xffffffffu, cells, o);
+    if (lane == 0 && cells) atomicAdd(&cnt[kFillColours], static_cast<unsigned long long>(cells));
 }
 
-// Both pass-parity edge buffers of every tile from the initial field (one
-// thread per tile edge slot).
-__global__ void fill_edge_init(int nr, int nc, int ntx, int nty, const std::uint8_t* __restrict__ kind,
-                               const float* __restrict__ F, float* __restrict__ e0, float* __restrict__ e1)
-{
-    LSDTT_COUNT();
-    const std::int64_t q = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (q >= static_cast<std::int64_t>(ntx) * nty * kEdge) return;
-    const int t = static_cast<int>(q / kEdge), slot = static_cast<int>(q % kEdge);
-    edge_export_from_field(nr, nc, kind, F, e0, t, t % ntx, t / ntx, slot);
-    edge_export_from_field(nr, nc, kind, F, e1, t, t % ntx, t / ntx, slot);
-}
-
-// Relaxation of the listed active tiles by a persistent grid (block w takes
-// entries w, w + grid, ...), the tile gate skipped: one block per tile spent
-// most of a late pass on inactive tiles reading their neighbours' flags.
+// Relaxation of one colour's listed active tiles by a persistent grid (block
+// w takes entries w, w + grid, ...), the tile gate skipped: one block per
+// tile spent most of a late pass on inactive tiles reading their
+// neighbours' flags.
 __global__ void __launch_bounds__(256) fill_relax_list(int nr, int nc, bool per_ns, bool per_ew, float L, float Ld,
                                                        float min_slope, const float* __restrict__ z,
                                                        const std::uint8_t* __restrict__ kind, float* __restrict__ F,
@@ -134,16 +129,15 @@ __global__ void __launch_bounds__(256) fill_relax_list(int nr, int nc, bool per_
                                                        const std::uint8_t* __restrict__ dirty_in,
                                                        std::uint8_t* __restrict__ dirty_out, int ntx, int nty,
                                                        const std::int32_t* __restrict__ list,
-                                                       const unsigned long long* __restrict__ cnt,
-                                                       const float* __restrict__ edges_in, float* __restrict__ edges_out)
+                                                       const unsigned long long* __restrict__ count)
 {
     LSDTT_COUNT();
-    const std::int64_t n = static_cast<std::int64_t>(cnt[0]);
+    const std::int64_t n = static_cast<std::int64_t>(*count);
     for (std::int64_t w = blockIdx.x; w < n; w += gridDim.x)
     {
         const int t = list[w];
         fill_relax_tile(nr, nc, per_ns, per_ew, L, Ld, min_slope, z, kind, F, changed, dirty_in, dirty_out, t % ntx,
-                        t / ntx, ntx, nty, false, edges_in, edges_out, 0);
+                        t / ntx, ntx, nty, false);
         __syncthreads();  // the tile's shared arrays are staged again for the next tile
     }
 }
@@ -182,20 +176,18 @@ extern "C" int lsdtt_gpu_fill_pits(const lsdtt_gpu_grid* grid, const float* z_de
     int* flags = nullptr;   // [0] interior nodata, [1] changed
     int* hflag = nullptr;
     std::uint8_t* dirty = nullptr;  // two per-tile activity planes
-    std::int32_t* list = nullptr;   // active tiles of the current pass
-    float* edges = nullptr;         // [2][tiles][kEdge] pass-start tile edges
+    std::int32_t* list = nullptr;   // active tiles of the current pass, by colour
     unsigned long long* cnt = nullptr;  // their count and cells
     unsigned long long* hcnt = nullptr;
     const std::int64_t ntiles = static_cast<std::int64_t>((nc + kT - 1) / kT) * ((nr + kT - 1) / kT);
     cudaError_t e = cudaMallocAsync(&kind, static_cast<std::size_t>(n), st);
     if (e == cudaSuccess) e = cudaMallocAsync(&dirty, static_cast<std::size_t>(2 * ntiles), st);
-    if (e == cudaSuccess) e = cudaMallocAsync(&list, sizeof(std::int32_t) * static_cast<std::size_t>(ntiles), st);
     if (e == cudaSuccess)
-        e = cudaMallocAsync(&edges, sizeof(float) * 2 * static_cast<std::size_t>(ntiles) * kEdge, st);
-    if (e == cudaSuccess) e = cudaMallocAsync(&cnt, sizeof(unsigned long long) * 2, st);
+        e = cudaMallocAsync(&list, sizeof(std::int32_t) * kFillColours * static_cast<std::size_t>(ntiles), st);
+    if (e == cudaSuccess) e = cudaMallocAsync(&cnt, sizeof(unsigned long long) * (kFillColours + 1), st);
     if (e == cudaSuccess) e = cudaMallocAsync(&flags, sizeof(int) * 2, st);
     if (e == cudaSuccess) e = cudaMallocHost(&hflag, sizeof(int));
-    if (e == cudaSuccess) e = cudaMallocHost(&hcnt, sizeof(unsigned long long) * 2);
+    if (e == cudaSuccess) e = cudaMallocHost(&hcnt, sizeof(unsigned long long) * (kFillColours + 1));
     if (e != cudaSuccess) return cuda_fail(e, "lsdtt_gpu_fill_pits");
     cudaMemsetAsync(flags, 0, sizeof(int) * 2, st);
     cudaMemsetAsync(dirty, 1, static_cast<std::size_t>(2 * ntiles), st);
@@ -212,10 +204,6 @@ extern "C" int lsdtt_gpu_fill_pits(const lsdtt_gpu_grid* grid, const float* z_de
     const int kCheckEvery = 4;
     const long max_pass = 4L * (nr + nc) + 64;  // bound: any path crosses each tile row/column at most a few times
     const int ntx = static_cast<int>(tiles.x), nty = static_cast<int>(tiles.y);
-    const std::size_t edge_plane = static_cast<std::size_t>(ntiles) * kEdge;
-    fill_edge_init<<<grid_blocks(static_cast<std::int64_t>(edge_plane), 256), 256, 0, st>>>(nr, nc, ntx, nty, kind,
-                                                                                         out_dev, edges,
-                                                                                         edges + edge_plane);
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -226,26 +214,29 @@ extern "C" int lsdtt_gpu_fill_pits(const lsdtt_gpu_grid* grid, const float* z_de
         cudaMemsetAsync(flags + 1, 0, sizeof(int), st);
         for (int k = 0; k < kCheckEvery && e == cudaSuccess; ++k, ++pass)
         {
-            // Each pass lists its active tiles, then relaxes only those.
-            // Algorithmic bytes per pass: z 4 + mask 1 in, filled value 4
-            // out per relaxed cell (counted when profiling).
+            // Each pass lists its active tiles by colour, then relaxes each
+            // colour's in turn. Algorithmic bytes per pass: z 4 + mask 1
+            // in, filled value 4 out per relaxed cell (counted when
+            // profiling).
             const std::uint8_t* din = dirty + (pass & 1) * ntiles;
             std::uint8_t* dout = dirty + ((pass + 1) & 1) * ntiles;
-            cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * 2, st);
+            cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * (kFillColours + 1), st);
             fill_active<<<grid_blocks(ntiles, 256), 256, 0, st>>>(nr, nc, per_ns, per_ew, ntx, nty, din, dout, list,
-                                                                   cnt);
+                                                                   ntiles, cnt);
             double bytes = 9.0 * static_cast<double>(n);
             if (profiling_enabled())
             {
-                cudaMemcpyAsync(hcnt, cnt, sizeof(unsigned long long) * 2, cudaMemcpyDeviceToHost, st);
+                cudaMemcpyAsync(hcnt, cnt, sizeof(unsigned long long) * (kFillColours + 1), cudaMemcpyDeviceToHost,
+                                st);
                 e = cudaStreamSynchronize(st);
-                bytes = 9.0 * static_cast<double>(hcnt[1]);
+                bytes = 9.0 * static_cast<double>(hcnt[kFillColours]);
             }
-            LSDTT_TIMED("fill_relax", bytes, st,
-                        (fill_relax_list<<<list_grid, block, 0, st>>>(nr, nc, per_ns, per_ew, L, Ld, eps, z_dev, kind,
-                                                                      out_dev, flags + 1, din, dout, ntx, nty, list,
-                                                                      cnt, edges + (pass & 1) * edge_plane,
-                                                                      edges + ((pass + 1) & 1) * edge_plane)));
+            LSDTT_TIMED("fill_relax", bytes, st, ({
+                            for (int c = 0; c < kFillColours; ++c)
+                                fill_relax_list<<<list_grid, block, 0, st>>>(nr, nc, per_ns, per_ew, L, Ld, eps, z_dev,
+                                                                             kind, out_dev, flags + 1, din, dout, ntx,
+                                                                             nty, list + c * ntiles, cnt + c);
+                        }));
         }
         if (e != cudaSuccess) break;
         cudaMemcpyAsync(hflag, flags + 1, sizeof(int), cudaMemcpyDeviceToHost, st);
@@ -261,7 +252,6 @@ extern "C" int lsdtt_gpu_fill_pits(const lsdtt_gpu_grid* grid, const float* z_de
     cudaFreeAsync(kind, st);
     cudaFreeAsync(dirty, st);
     cudaFreeAsync(list, st);
-    cudaFreeAsync(edges, st);
     cudaFreeAsync(cnt, st);
     cudaFreeAsync(flags, st);
     cudaFreeHost(hflag);
@@ -384,8 +374,10 @@ extern "C" int lsdtt_gpu_fill_pits_noalloc(const lsdtt_gpu_grid* grid, const flo
     {
         cudaMemsetAsync(flags + 1, 0, sizeof(int), st);
         for (int k = 0; k < kCheckEvery; ++k, ++pass)
-            fill_relax<<<tiles, block, 0, st>>>(nr, nc, per_ns, per_ew, L, Ld, eps, z_dev, kind, out_dev, flags + 1,
-                                                dirty + (pass & 1) * ntiles, dirty + ((pass + 1) & 1) * ntiles);
+            for (int c = 0; c < kFillColours; ++c)
+                fill_relax<<<tiles, block, 0, st>>>(nr, nc, per_ns, per_ew, L, Ld, eps, z_dev, kind, out_dev,
+                                                    flags + 1, dirty + (pass & 1) * ntiles,
+                                                    dirty + ((pass + 1) & 1) * ntiles, c);
         e = cudaMemcpyAsync(&changed, flags + 1, sizeof(int), cudaMemcpyDeviceToHost, st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) return cuda_fail(e, "lsdtt_gpu_fill_pits_noalloc");

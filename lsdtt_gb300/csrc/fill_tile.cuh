@@ -19,57 +19,23 @@ constexpr int kMaxLocal = 4 * kT;
 constexpr int kFillThreads = 256;                        // threads per tile (32 x 8 block)
 constexpr int kFillBlocks = (kT / 2) * (kT / 2) / kFillThreads;  // 2 x 2 blocks per thread
 
-// Pass-start tile edges. Each pass a tile reads its halo from the edges its
-// neighbours had at the start of the pass and exports its own at the end
-// (two buffers by pass parity), so a pass's outcome depends only on its
-// inputs, not on which tiles ran first: the discoverer rule is not
-// monotone, so halos read from a field that neighbours update during the
-// pass made the result depend on scheduling. A tile's edges: its first and
-// last valid row, then its first and last valid column, kT floats each.
-// A tile that is not relaxed in a pass keeps its edges in the other buffer
-// too: it did not change in the pass before (else it would be active), so
-// the value two passes old is still current.
-constexpr int kEdge = 4 * kT;
+// Tile colours of a fill pass. A pass relaxes its active tiles one colour
+// after another, in place; no two tiles of one colour are neighbours
+// (including diagonal and periodic ones), so a tile reads every neighbour
+// either settled in an earlier colour of this pass or untouched since the
+// last pass: the result depends only on the inputs, not on which tiles ran
+// first (the discoverer rule is not monotone, so halos read from a field
+// that neighbours update meanwhile made it depend on scheduling), and a
+// change can still cross several tiles in one pass. Colour = cx + 3 cy with
+// cx the parity of the tile column, or 2 for the last column of a periodic
+// axis with an odd tile count (it neighbours column 0); cy likewise.
+constexpr int kFillColours = 9;
 
-// The pass-start filled value of cell (r, c) (wrapped, in the grid) of a
-// neighbouring tile, on that tile's boundary.
-__device__ __forceinline__ float edge_halo(const float* __restrict__ edges, int tile_base, int ntx, int nr, int nc,
-                                           int r, int c)
+__device__ __forceinline__ int fill_colour(int tx, int ty, int ntx, int nty, bool per_ns, bool per_ew)
 {
-    const int tr = r / kT, tc = c / kT;
-    const int lr = r - tr * kT, lc = c - tc * kT;
-    const int h = min(kT, nr - tr * kT);
-    const float* e = edges + static_cast<std::int64_t>(tile_base + tr * ntx + tc) * kEdge;
-    if (lr == 0) return e[lc];
-    if (lr == h - 1) return e[kT + lc];
-    if (lc == 0) return e[2 * kT + lr];
-    return e[3 * kT + lr];  // the last valid column
-}
-
-// Edges of tile (tx, ty) from the field F (start of the relaxation): one
-// thread per edge slot; kind 0 cells (nodata, off the fill) as +inf, as the
-// tile staging holds them.
-__device__ __forceinline__ void edge_export_from_field(int nr, int nc, const std::uint8_t* __restrict__ kind,
-                                                       const float* __restrict__ F, float* __restrict__ edges,
-                                                       int tile, int tx, int ty, int slot)
-{
-    const int h = min(kT, nr - ty * kT), w = min(kT, nc - tx * kT);
-    const int e = slot / kT, k = slot % kT;
-    int r, c;
-    if (e < 2)
-    {
-        if (k >= w) return;
-        r = ty * kT + (e == 0 ? 0 : h - 1);
-        c = tx * kT + k;
-    }
-    else
-    {
-        if (k >= h) return;
-        r = ty * kT + k;
-        c = tx * kT + (e == 2 ? 0 : w - 1);
-    }
-    const std::int64_t g = static_cast<std::int64_t>(r) * nc + c;
-    edges[static_cast<std::int64_t>(tile) * kEdge + slot] = kind[g] != 0 ? F[g] : INFINITY;
+    const int cx = (per_ew && (ntx & 1) && ntx > 1 && tx == ntx - 1) ? 2 : (tx & 1);
+    const int cy = (per_ns && (nty & 1) && nty > 1 && ty == nty - 1) ? 2 : (ty & 1);
+    return cx + 3 * cy;
 }
 
 __device__ __forceinline__ float raise_from(float zeta, float min_slope, float d)
@@ -144,9 +110,7 @@ __device__ __forceinline__ void fill_relax_tile(int nr, int nc, bool per_ns, boo
                                                 const std::uint8_t* __restrict__ kind, float* __restrict__ F,
                                                 int* __restrict__ changed, const std::uint8_t* __restrict__ dirty_in,
                                                 std::uint8_t* __restrict__ dirty_out, const int tx, const int ty,
-                                                const int ntx, const int nty, const bool gate = true,
-                                                const float* __restrict__ edges_in = nullptr,
-                                                float* __restrict__ edges_out = nullptr, const int tile_base = 0)
+                                                const int ntx, const int nty, const bool gate = true)
 {
     // Active-tile gate: a tile can only change if it or one of its eight
     // neighbouring tiles changed in the previous pass (periodic axes wrap).
@@ -179,7 +143,6 @@ __device__ __forceinline__ void fill_relax_tile(int nr, int nc, bool per_ns, boo
     // rows 2*(b / (kT/2))+1 .. +2, columns 2*(b % (kT/2))+1 .. +2, b = tid +
     // j * kFillThreads), so it holds kFillBlocks cells of each colour.
     unsigned free_mask = 0;  // bit 4j + k: block j's cell of colour k is free (kind 1)
-    const int th = min(kT, nr - ty * kT), tw = min(kT, nc - tx * kT);  // the tile's valid extent
     for (int k = tid; k < kH * kH; k += blockDim.x * blockDim.y)
     {
         const int lr = k / kH, lcc = k % kH;
@@ -192,10 +155,7 @@ __device__ __forceinline__ void fill_relax_tile(int nr, int nc, bool per_ns, boo
             const std::int64_t g = static_cast<std::int64_t>(r) * nc + c;
             const std::uint8_t kd = kind[g];
             zz = z[g];
-            // halo cells (outside the tile's valid extent) from the
-            // neighbours' pass-start edges when given
-            const bool halo = lr == 0 || lr > th || lcc == 0 || lcc > tw;
-            if (kd != 0) f = (halo && edges_in) ? edge_halo(edges_in, tile_base, ntx, nr, nc, r, c) : F[g];
+            if (kd != 0) f = F[g];
         }
         sF[lr][lcc] = f;
         sz[lr][lcc] = zz;
@@ -266,21 +226,6 @@ __device__ __forceinline__ void fill_relax_tile(int nr, int nc, bool per_ns, boo
         }
         if (!__syncthreads_or(local)) break;
         tile_changed = true;
-    }
-    // this pass's edges (the relaxation ended at a barrier: sF is final)
-    if (edges_out)
-    {
-        float* eo = edges_out + static_cast<std::int64_t>(tile_base + ty * ntx + tx) * kEdge;
-        for (int k = tid; k < tw; k += blockDim.x * blockDim.y)
-        {
-            eo[k] = sF[1][1 + k];
-            eo[kT + k] = sF[th][1 + k];
-        }
-        for (int k = tid; k < th; k += blockDim.x * blockDim.y)
-        {
-            eo[2 * kT + k] = sF[1 + k][1];
-            eo[3 * kT + k] = sF[1 + k][tw];
-        }
     }
 #pragma unroll
     for (int j = 0; j < kFillBlocks; ++j)
