@@ -1538,6 +1538,7 @@ struct lsdtt_gpu_ensemble
     unsigned long long* fcnt = nullptr;      // [kFillColours + 1] their counts by colour, then their cells
     unsigned long long* h_fcnt = nullptr;    // pinned copy (eager steps)
     unsigned fill_grid = 0;                  // persistent grid of the listed relaxation
+    unsigned fill_colours = 0;               // tile colours some member can hold (fill_colour_mask)
     std::int64_t* pos = nullptr;
     int* nd = nullptr;
     lsdtt_gpu_flow* f = nullptr;
@@ -1842,9 +1843,12 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
         // the colours in turn: a tile reads its neighbours settled
         LSDTT_TIMED("ens_fill_relax", bytes, s, ({
                         for (int c = 0; c < kFillColours; ++c)
+                        {
+                            if (!((E->fill_colours >> c) & 1u)) continue;
                             ens_fill_relax_list<<<E->fill_grid, fblock, 0, s>>>(
                                 E->P, E->d_prm, E->tile_member, E->z, E->kind, E->zf, E->flags, din, dout,
                                 E->flist + static_cast<std::int64_t>(c) * E->T, E->fcnt + c);
+                        }
                     }));
         return cudaSuccess;
     };
@@ -2585,6 +2589,12 @@ int lsdtt_gpu_ensemble_create(const lsdtt_gpu_member* members, int32_t n_members
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         E->fill_grid = static_cast<unsigned>(std::max(1, sms) * 8);
+        for (const PackedMember& Pm : E->pm)
+        {
+            const lsdtt_gpu_grid& g = E->members[&Pm - E->pm.data()].grid;
+            auto per = [&](int i) { return g.boundary_conditions[i] == 'p' || g.boundary_conditions[i] == 'P'; };
+            E->fill_colours |= fill_colour_mask(Pm.ntx, Pm.nty, per(0), per(1));
+        }
     }
     if (e != cudaSuccess)
     {

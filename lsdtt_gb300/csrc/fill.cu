@@ -208,6 +208,7 @@ extern "C" int lsdtt_gpu_fill_pits(const lsdtt_gpu_grid* grid, const float* z_de
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const unsigned list_grid = static_cast<unsigned>(std::max(1, sms) * 8);
+    const unsigned colours = fill_colour_mask(ntx, nty, per_ns, per_ew);
     long pass = 0;
     for (;;)
     {
@@ -233,9 +234,12 @@ extern "C" int lsdtt_gpu_fill_pits(const lsdtt_gpu_grid* grid, const float* z_de
             }
             LSDTT_TIMED("fill_relax", bytes, st, ({
                             for (int c = 0; c < kFillColours; ++c)
+                            {
+                                if (!((colours >> c) & 1u)) continue;
                                 fill_relax_list<<<list_grid, block, 0, st>>>(nr, nc, per_ns, per_ew, L, Ld, eps, z_dev,
                                                                              kind, out_dev, flags + 1, din, dout, ntx,
                                                                              nty, list + c * ntiles, cnt + c);
+                            }
                         }));
         }
         if (e != cudaSuccess) break;
@@ -373,11 +377,15 @@ extern "C" int lsdtt_gpu_fill_pits_noalloc(const lsdtt_gpu_grid* grid, const flo
     for (;;)
     {
         cudaMemsetAsync(flags + 1, 0, sizeof(int), st);
+        const unsigned colours = fill_colour_mask(static_cast<int>(tiles.x), static_cast<int>(tiles.y), per_ns, per_ew);
         for (int k = 0; k < kCheckEvery; ++k, ++pass)
             for (int c = 0; c < kFillColours; ++c)
+            {
+                if (!((colours >> c) & 1u)) continue;
                 fill_relax<<<tiles, block, 0, st>>>(nr, nc, per_ns, per_ew, L, Ld, eps, z_dev, kind, out_dev,
                                                     flags + 1, dirty + (pass & 1) * ntiles,
                                                     dirty + ((pass + 1) & 1) * ntiles, c);
+            }
         e = cudaMemcpyAsync(&changed, flags + 1, sizeof(int), cudaMemcpyDeviceToHost, st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) return cuda_fail(e, "lsdtt_gpu_fill_pits_noalloc");

@@ -31,6 +31,19 @@ constexpr int kFillBlocks = (kT / 2) * (kT / 2) / kFillThreads;  // 2 x 2 blocks
 // axis with an odd tile count (it neighbours column 0); cy likewise.
 constexpr int kFillColours = 9;
 
+// Bit c set: colour c can hold tiles of an ntx x nty tile grid (host side:
+// the passes launch only those colours; four for a grid without wrap).
+inline unsigned fill_colour_mask(int ntx, int nty, bool per_ns, bool per_ew)
+{
+    unsigned mx = 1u | (ntx > 1 ? 2u : 0u) | ((per_ew && (ntx & 1) && ntx > 1) ? 4u : 0u);
+    unsigned my = 1u | (nty > 1 ? 2u : 0u) | ((per_ns && (nty & 1) && nty > 1) ? 4u : 0u);
+    unsigned m = 0;
+    for (int cy = 0; cy < 3; ++cy)
+        for (int cx = 0; cx < 3; ++cx)
+            if (((mx >> cx) & 1u) && ((my >> cy) & 1u)) m |= 1u << (cx + 3 * cy);
+    return m;
+}
+
 __device__ __forceinline__ int fill_colour(int tx, int ty, int ntx, int nty, bool per_ns, bool per_ew)
 {
     const int cx = (per_ew && (ntx & 1) && ntx > 1 && tx == ntx - 1) ? 2 : (tx & 1);
