@@ -188,7 +188,18 @@ extern "C" int lsdtt_gpu_fill_pits(const lsdtt_gpu_grid* grid, const float* z_de
     if (e == cudaSuccess) e = cudaMallocAsync(&flags, sizeof(int) * 2, st);
     if (e == cudaSuccess) e = cudaMallocHost(&hflag, sizeof(int));
     if (e == cudaSuccess) e = cudaMallocHost(&hcnt, sizeof(unsigned long long) * (kFillColours + 1));
-    if (e != cudaSuccess) return cuda_fail(e, "lsdtt_gpu_fill_pits");
+    if (e != cudaSuccess)
+    {
+        // whatever was allocated before the failure (cudaFree* of null is a no-op)
+        cudaFreeAsync(kind, st);
+        cudaFreeAsync(dirty, st);
+        cudaFreeAsync(list, st);
+        cudaFreeAsync(cnt, st);
+        cudaFreeAsync(flags, st);
+        cudaFreeHost(hflag);
+        cudaFreeHost(hcnt);
+        return cuda_fail(e, "lsdtt_gpu_fill_pits");
+    }
     cudaMemsetAsync(flags, 0, sizeof(int) * 2, st);
     cudaMemsetAsync(dirty, 1, static_cast<std::size_t>(2 * ntiles), st);
     fill_interior_nodata<<<grid_blocks(n, 256), 256, 0, st>>>(nr, nc, z_dev, mask_dev, grid->no_data_value, flags);
