@@ -155,3 +155,19 @@ def test_member_groups_give_the_same_result(port):
         ens.close()
     for k, (a, b) in enumerate(zip(out[True], out[False])):
         assert np.array_equal(a, b), f"member {k}: max |diff| {np.max(np.abs(a - b))}"
+
+
+def test_steps_are_deterministic(port):
+    """Two fresh ensembles stepped eagerly give identical bits: the fill
+    relaxes its active tiles colour by colour (no two tiles of a colour are
+    neighbours), so no result depends on which tiles ran first."""
+    import lsdtt_gb300 as G
+    specs = _members(port)
+    runs = []
+    for _ in range(2):
+        ens = G.Ensemble(specs, use_graph=False)
+        ens.step(2)
+        runs.append([ens.get(k).cpu().numpy() for k in range(len(specs))])
+        ens.close()
+    for k, (a, b) in enumerate(zip(*runs)):
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), f"member {k}"
