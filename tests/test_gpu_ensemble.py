@@ -163,6 +163,11 @@ def test_steps_are_deterministic(port):
     neighbours), so no result depends on which tiles ran first."""
     import lsdtt_gb300 as G
     specs = _members(port)
+    # enough tiles for a pass to run in several waves
+    z = port.noise_tilt_surface(384, 512, 30.0, 17, 0.0, 1.0, "nnon", 0.001)
+    specs.append(dict(z=z, cell_size=30.0, boundary_conditions="nnon", timestep=1000.0, erodibility=2e-5,
+                      m_exponent=0.5, n_exponent=1.5, uplift_rate=1e-3, hillslope_diffusivity=0.01,
+                      fill_min_slope=1e-4))
     runs = []
     for _ in range(2):
         ens = G.Ensemble(specs, use_graph=False)
