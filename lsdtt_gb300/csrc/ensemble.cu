@@ -1435,17 +1435,6 @@ __global__ void ens_pcg_while(int* __restrict__ it_dev, int itmax, int* __restri
     cudaGraphSetConditional(h, (active > 0 && it < itmax) ? 1u : 0u);
 }
 
-__global__ void ens_hs_finish(Packed P, const std::uint8_t* __restrict__ dof, const float* __restrict__ zsp,
-                              const float* __restrict__ x, float* __restrict__ out,
-                              const std::int32_t* __restrict__ blist = nullptr)
-{
-    LSDTT_COUNT();
-    const std::int64_t blk = blist ? blist[blockIdx.x] : static_cast<std::int64_t>(blockIdx.x);
-    const std::int64_t i = blk * blockDim.x + threadIdx.x;
-    if (i >= P.n) return;
-    out[i] = dof[i] ? static_cast<float>(static_cast<double>(zsp[i]) + static_cast<double>(x[i])) : zsp[i];
-}
-
 // ---- uplift, boundary restore, statistics ----------------------------------
 __global__ void ens_boundary_flag(Packed P, const std::uint8_t* __restrict__ mask, std::uint8_t* __restrict__ flag)
 {
@@ -1460,41 +1449,43 @@ __global__ void ens_boundary_flag(Packed P, const std::uint8_t* __restrict__ mas
                   : 0;
 }
 
-__global__ void ens_uplift(Packed P, const EnsParams* __restrict__ prm, const std::uint8_t* __restrict__ mask,
-                           const std::uint8_t* __restrict__ bflag, const float* __restrict__ z_before,
-                           float* __restrict__ z)
-{
-    LSDTT_COUNT();
-    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i >= P.n) return;
-    const EnsParams& q = prm[block_member(P)];
-    float v = z[i];
-    if (mask[i]) v = __fadd_rn(v, q.udz);
-    if (bflag[i]) v = __fsub_rn(z_before[i], q.bl);
-    z[i] = v;
-}
-
-// lem_stats (lem.cu) per member, as block partials: [0] sum of (after -
-// before), [1] unused, [2] erosion sum, [3] valid count, [4..7] maxima
-// (before, after, |dz|, erosion). Differences are formed per cell (exact
-// for nearby elevations) before any sum, so FP32 warp sums suffice.
-__global__ void ens_stats(Packed P, const EnsParams* __restrict__ prm, const std::uint8_t* __restrict__ mask,
-                          const float* __restrict__ zb, const float* __restrict__ za, double* __restrict__ part)
+// The end of a step in one pass: the hillslope increment added in double
+// (z = zsp + x on DOFs, zsp elsewhere), uplift on valid cells, the boundary
+// restore (z = z_before - bl on flagged cells), then lem_stats (lem.cu) per
+// member as block partials (zb = the surface before the step, za = after):
+// [0] sum of (after - before), [1] unused, [2] erosion sum, [3] valid count,
+// [4..7] maxima (before, after, |dz|, erosion). Differences are formed per
+// cell (exact for nearby elevations) before any sum, so FP32 warp sums
+// suffice.
+__global__ void ens_step_finish(Packed P, const EnsParams* __restrict__ prm, const std::uint8_t* __restrict__ mask,
+                                const std::uint8_t* __restrict__ bflag, const std::uint8_t* __restrict__ dof,
+                                const float* __restrict__ zsp, const float* __restrict__ x,
+                                const float* __restrict__ zb, float* __restrict__ z, double* __restrict__ part)
 {
     LSDTT_COUNT();
     const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     const int m = P.blk_member[blockIdx.x];  // kPackAlign-cell blocks: one member each
+    const EnsParams& q = prm[m];
     float v[8] = {0.0f, 0.0f, 0.0f, 0.0f, -1e30f, -1e30f, 0.0f, 0.0f};
-    if (i < P.n && mask[i])
+    if (i < P.n)
     {
-        const float b = zb[i], a = za[i];
-        v[0] = a - b;
-        v[4] = b;
-        v[5] = a;
-        v[6] = fabsf(a - b);
-        const float ero = (b - a) + prm[m].udz;
-        if (ero > 0.0f) { v[2] = ero; v[7] = ero; }
-        v[3] = 1.0f;
+        const float s = zsp[i];
+        float a = dof[i] ? static_cast<float>(static_cast<double>(s) + static_cast<double>(x[i])) : s;
+        const bool valid = mask[i] != 0;
+        if (valid) a = __fadd_rn(a, q.udz);
+        if (bflag[i]) a = __fsub_rn(zb[i], q.bl);
+        z[i] = a;
+        if (valid)
+        {
+            const float b = zb[i];
+            v[0] = a - b;
+            v[4] = b;
+            v[5] = a;
+            v[6] = fabsf(a - b);
+            const float ero = (b - a) + q.udz;
+            if (ero > 0.0f) { v[2] = ero; v[7] = ero; }
+            v[3] = 1.0f;
+        }
     }
     block_partials_f<8>(v, 0xf0u, part, P.n / kPackAlign);
 }
@@ -2238,7 +2229,6 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
             if (eager) rec->pcg_iters = it;
             else ens_hs_overflow<<<mb, 128, 0, hs>>>(M, E->done, E->flags);
         }
-        ens_hs_finish<<<G.nblk, 256, 0, hs>>>(E->P, E->dof, E->zsp, E->x, E->z, G.blist);
         return cudaSuccess;
     };
     if (split_groups)
@@ -2258,9 +2248,10 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
     else
         e = hillslope_stage(st, HsGroup{nullptr, nb, nullptr, static_cast<unsigned>(E->S), nullptr, 0});
     if (e != cudaSuccess) return e;
-    // 5. uplift + boundary restore, statistics, flags to the host
-    ens_uplift<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->mask, E->bflag, E->zf, E->z);
-    ens_stats<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->mask, E->zf, E->z, E->part);
+    // 5. the increment, uplift + boundary restore and the statistics in one
+    // pass; flags to the host
+    ens_step_finish<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->mask, E->bflag, E->dof, E->zsp, E->x, E->zf, E->z,
+                                        E->part);
     reduce(st, 8, 0xf0u, nullptr, E->stats_acc, 8, 0, nullptr);
     cudaMemcpyAsync(E->h_stats, E->stats_acc, sizeof(double) * 8 * M, cudaMemcpyDeviceToHost, st);
     cudaMemcpyAsync(E->h_flags, E->flags, sizeof(int) * kFlags, cudaMemcpyDeviceToHost, st);
