@@ -41,6 +41,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -80,7 +81,7 @@ class Clocks:
     def __init__(self, gpu: int):
         self.gpu = gpu
         self.p = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        self.path = os.path.join(tempfile.gettempdir(), f"lsdtt_gb300_clocks_{os.getpid()}.csv")
 
     def __enter__(self):
         try:

@@ -175,7 +175,7 @@ typedef struct lsdtt_gpu_solve_report
      * compute it. */
     int32_t linear_solves;
     int32_t network_applications;
-    int32_t rejected_solves;      /* learned solves the Jacobi judge rejected */
+    int32_t rejected_solves;      /* learned solves the Jacobi acceptance check rejected */
     int32_t fallback_iterations;  /* Jacobi-PCG iterations run after a rejection */
     double explicit_relative_residual;
 } lsdtt_gpu_solve_report;
@@ -257,7 +257,7 @@ int lsdtt_gpu_hillslope_capture_pairs(const lsdtt_gpu_grid* grid, const float* z
 /* lsdtt_gpu_hillslope_implicit with the network as the preconditioner: each
  * linear system is solved by flexible (Polak-Ribiere) PCG with
  *   M^-1 r = y + D^-1 (r - A y),  y = net(D^-1 r)  (D = diag A),
- * to the same relative residual rel_tol. Plain Jacobi-PCG is the judge and
+ * to the same relative residual rel_tol. Plain Jacobi-PCG is the acceptance check and
  * the fallback: the FP64 explicit residual of the learned iterate must be
  * within max(rel_tol, 4x the FP32 representation floor of the iterate) of
  * ||b||, else Jacobi-PCG restarts from that iterate (or from zero when it is

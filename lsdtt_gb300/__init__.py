@@ -529,7 +529,7 @@ def hillslope_implicit(z, mask, cell_size, boundary_conditions, D, Sc, dt, nonli
     """Backward-Euler hillslope step over dt (linear or Roering), the
     reference's compute_hillslope_newton_transient. With `net` (a UNet) the
     linear systems are solved by flexible PCG with the network as the
-    preconditioner, judged and finished by Jacobi-PCG. Returns (z CUDA
+    preconditioner, checked and finished by Jacobi-PCG. Returns (z CUDA
     tensor, SolveReport with the total PCG iteration count)."""
     torch = _torch()
     L = _bind_more()

@@ -851,7 +851,7 @@ __global__ void hsf_input(std::int64_t n, const float* __restrict__ invd, const 
 // Explicit residual res = b - A x, evaluated in FP64 from the FP32 iterate and
 // stored (FP32) in r. acc[0] += ||res||^2; acc[1] += sum_i (diag_i |x_i|
 // 2^-24)^2, the residual that rounding x to FP32 alone can leave (the
-// representation floor the judge allows for).
+// representation floor the acceptance check allows for).
 __global__ void hsn_explicit(HsN P, const std::uint8_t* __restrict__ mask, const std::uint8_t* __restrict__ dof,
                              const float4* __restrict__ alpha, const float* __restrict__ b,
                              const float* __restrict__ x, float* __restrict__ r, double* __restrict__ acc)
@@ -1049,13 +1049,13 @@ cudaError_t explicit_residual(const HsN& P, const std::uint8_t* mask, HsnBuf& B,
     return e;
 }
 
-// The judge's tolerance on the explicit residual: the requested relative
+// The acceptance check's tolerance on the explicit residual: the requested relative
 // residual, or 4x the floor that rounding the iterate to FP32 leaves,
 // whichever is larger.
-constexpr double kJudgeFloor = 4.0;
+constexpr double kAcceptFloor = 4.0;
 
 // Solve A(alpha) dz = -F to rel_tol: Jacobi-PCG, or flexible PCG with the
-// network when net is given (then judged, and finished by Jacobi-PCG when
+// network when net is given (then checked, and finished by Jacobi-PCG when
 // rejected). Sets *iters (all PCG iterations) and *rel (final recurrence
 // residual).
 cudaError_t hsn_pcg(const HsN& P, const std::uint8_t* mask, HsnBuf& B, std::int64_t n, double rel_tol, int max_iter,
@@ -1153,11 +1153,11 @@ cudaError_t hsn_pcg(const HsN& P, const std::uint8_t* mask, HsnBuf& B, std::int6
     }
     if (e != cudaSuccess) return e;
     *iters = it;
-    // The judge: explicit FP64 residual of the learned iterate.
+    // The acceptance check: explicit FP64 residual of the learned iterate.
     e = explicit_residual(P, mask, B, n, bnorm, acc + 4, st, &rel_exp, &rel_floor);
     if (e != cudaSuccess) return e;
     const bool finite = std::isfinite(rel_exp);
-    if (converged && finite && rel_exp <= std::max(rel_tol, kJudgeFloor * rel_floor))
+    if (converged && finite && rel_exp <= std::max(rel_tol, kAcceptFloor * rel_floor))
     {
         S.explicit_max = std::max(S.explicit_max, rel_exp);
         return cudaSuccess;

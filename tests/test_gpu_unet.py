@@ -7,7 +7,7 @@
 - training on residual/correction pairs captured from the plain solver
   lowers the loss;
 - flexible PCG with the trained network reaches the same 1e-8 relative
-  residual as Jacobi-PCG, passes the Jacobi judge, gives the same surface,
+  residual as Jacobi-PCG, passes the Jacobi acceptance check, gives the same surface,
   and the iteration counts of both are reported.
 
 Bars: the network runs in BF16 with FP32 accumulation in an order the
@@ -222,7 +222,7 @@ def test_learned_fpcg_matches_plain_and_reports_gain(nonlinear, relief):
     assert rep_l.relative_residual <= 1e-8 and rep_p.relative_residual <= 1e-8
     # the same surface: within 1e-5 relative of the plain solve
     np.testing.assert_allclose(zl, zp, rtol=1e-5, atol=1e-5 * float(np.abs(zp).max()))
-    # the judge: explicit residual of every accepted learned solve within the
+    # the acceptance check: explicit residual of every accepted learned solve within the
     # FP32 floor (or it was rejected and finished by Jacobi-PCG)
     assert rep_l.explicit_relative_residual < 1e-4
     # the gain: fewer Krylov iterations than plain Jacobi-PCG
