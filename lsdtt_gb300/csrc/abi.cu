@@ -245,9 +245,11 @@ int lsdtt_gpu_flow_create(const lsdtt_gpu_grid* grid, lsdtt_gpu_flow** out)
     alloc(&f->dscal, 4);
     alloc(&f->derr, 4);
     alloc(&f->dundec, 1);
-    // Workspace: the Euler-tour ranking peaks at ~72 B per cell (tour links,
-    // two prefix arrays and the level-0 ruler walk state); the range-max
-    // structure and the sort need ~58 B per cell after the tour is released.
+    // Workspace: the Euler-tour ranking peaks at ~60 B per cell (tour links
+    // 16 B, level-0 ruler records 32 B, the ruler lists and the upper
+    // levels; prefix arrays only for tours short enough for the serial
+    // ranking); the range-max structure and the sort need ~58 B per cell
+    // after the tour is released.
     f->ws_bytes = n * 84 + (std::size_t(64) << 20);
     if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&f->ws.base), f->ws_bytes);
     f->ws.cap = f->ws_bytes;

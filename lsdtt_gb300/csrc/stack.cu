@@ -40,7 +40,7 @@ namespace
 constexpr std::uint32_t kEnd = 0xffffffffu;
 constexpr std::uint32_t kNone = 0xffffffffu;
 constexpr unsigned kErrCycle = 5;
-constexpr int kRuler = 64;        // mean sublist length of the ruling set
+constexpr int kRuler = 32;        // mean sublist length of the ruling set
 constexpr int kSerialLimit = 96;  // rank lists this short with one thread
 
 __device__ __forceinline__ bool is_ruler(std::uint32_t v)
@@ -666,9 +666,12 @@ cudaError_t build_stack(lsdtt_gpu_flow* f, bool want_topo, cudaStream_t st, cons
     std::uint32_t* next_sib = ws.take<std::uint32_t>(n);
     std::uint32_t* succ = ws.take<std::uint32_t>(2 * n);
     std::uint32_t* head = ws.take<std::uint32_t>(1);
-    std::int32_t* p0 = ws.take<std::int32_t>(2 * n);
-    std::int32_t* p1 = ws.take<std::int32_t>(2 * n);
-    if (!first_child || !next_sib || !succ || !head || !p0 || !p1) return cudaErrorMemoryAllocation;
+    // A tour longer than kSerialLimit writes the s-vector outputs straight
+    // from the ruler records; only the serial ranking needs prefix arrays.
+    const bool fused = 2 * n > kSerialLimit;
+    std::int32_t* p0 = fused ? nullptr : ws.take<std::int32_t>(2 * n);
+    std::int32_t* p1 = fused ? nullptr : ws.take<std::int32_t>(2 * n);
+    if (!first_child || !next_sib || !succ || !head || (!fused && (!p0 || !p1))) return cudaErrorMemoryAllocation;
 
     if (packed)
     {
@@ -684,7 +687,6 @@ cudaError_t build_stack(lsdtt_gpu_flow* f, bool want_topo, cudaStream_t st, cons
     // The ensemble reads the counts and depths only.
     const SvOut sv{g,          f->mask, f->n_valid, packed ? nullptr : f->sv_start, f->sv_size, f->depth,
                    packed ? nullptr : f->svec};
-    const bool fused = L0.n > static_cast<std::uint32_t>(kSerialLimit);
     cudaError_t e = rank_list(L0, p0, p1, ws, f->derr, st, fused ? &sv : nullptr);
     if (e != cudaSuccess) return e;
     if (!fused) sv_outputs<<<nb, 256, 0, st>>>(sv, p0, p1, f->derr);
