@@ -1,0 +1,57 @@
+"""The routing path at its workload's full size: an 8192 x 8192 fractal
+(k^-2 spectrum, 1000 m relief) with 100,000 pits, dx = 10 m, epsilon 1e-4,
+open edges. The oracle is too slow to run inside a test at this size, so the
+outputs are checked through the size-independent properties of
+tests/routing_props.py (which the oracle's own outputs satisfy), and the
+host-buffer C-ABI route is required to give the device path's bits."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from tests import routing_props as RP
+from tests import surfaces
+
+pytestmark = pytest.mark.gpu
+
+N = 8192
+CELL = 10.0
+
+
+@pytest.fixture(scope="module")
+def surface():
+    z = surfaces.fractal_pits(N)
+    return z, np.ones_like(z, np.uint8)
+
+
+def test_routing_full_size_properties(surface):
+    import lsdtt_gb300 as G
+    z, m = surface
+    filled_d = G.fill_pits(z, m, CELL, "oooo", 1e-4)
+    filled = filled_d.cpu().numpy()
+    RP.check_fill(z, filled)
+    fi = G.FlowInfo(filled_d, m, CELL, "oooo", allow_pits_as_outlets=True)
+    try:
+        host = lambda t: t.cpu().numpy()  # noqa: E731
+        RP.check_flow(filled, CELL, host(fi.receiver()), host(fi.direction()), host(fi.donor_count()),
+                      host(fi.outlets()), host(fi.topological_order()), host(fi.s_vector()),
+                      host(fi.s_vector_start()), host(fi.s_vector_size()), host(fi.accumulate()))
+        rec_d, topo_d, size_d = host(fi.receiver()), host(fi.topological_order()), host(fi.s_vector_size())
+    finally:
+        fi.close()
+
+    # The same route through the host-buffer entry point.
+    n = z.size
+    f_h = np.empty_like(z)
+    rec = np.empty(n, np.int64)
+    topo = np.empty(n, np.int64)
+    cnt = np.empty(n, np.uint64)
+    g = G.make_grid(N, N, CELL, "oooo")
+    opts = G.FlowOptions(1, 1, 1, 1, 1)
+    vp = lambda a: ctypes.c_void_p(a.ctypes.data)  # noqa: E731
+    G._check(G.lib().lsdtt_gpu_route_host(ctypes.byref(g), vp(z), vp(m), ctypes.c_float(1e-4), ctypes.byref(opts),
+                                          vp(f_h), vp(rec), vp(topo), vp(cnt), None))
+    assert np.array_equal(f_h.view(np.uint32), filled.view(np.uint32))
+    assert np.array_equal(rec, rec_d)
+    assert np.array_equal(topo, topo_d)
+    assert np.array_equal(cnt.astype(np.int64), size_d.astype(np.int64))
