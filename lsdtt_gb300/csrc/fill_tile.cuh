@@ -147,9 +147,8 @@ __device__ __forceinline__ void fill_relax_tile(int nr, int nc, bool per_ns, boo
         }
     }
     // Staged tile: filled values with +inf at invalid and off-grid cells (so
-    // they never win a minimum) and the elevations.
+    // they never win a minimum).
     __shared__ float sF[kH][kH];
-    __shared__ float sz[kH][kH];
     const int r0 = ty * kT - 1, c0 = tx * kT - 1;
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
     // Each thread owns kFillBlocks 2 x 2 blocks of the tile (block b: local
@@ -162,17 +161,19 @@ __device__ __forceinline__ void fill_relax_tile(int nr, int nc, bool per_ns, boo
         int r = r0 + lr, c = c0 + lcc;
         if (per_ns) { if (r < 0) r += nr; else if (r >= nr) r -= nr; }
         if (per_ew) { if (c < 0) c += nc; else if (c >= nc) c -= nc; }
-        float f = INFINITY, zz = INFINITY;
+        float f = INFINITY;
         if (r >= 0 && r < nr && c >= 0 && c < nc)
         {
             const std::int64_t g = static_cast<std::int64_t>(r) * nc + c;
-            const std::uint8_t kd = kind[g];
-            zz = z[g];
-            if (kd != 0) f = F[g];
+            if (kind[g] != 0) f = F[g];
         }
         sF[lr][lcc] = f;
-        sz[lr][lcc] = zz;
     }
+    // The thread's own cells (its 2 x 2 blocks) live in registers as well:
+    // only the owner writes them, so its copies are always the values other
+    // threads read from sF. Three of a cell's eight neighbours, its own value
+    // and its elevation come from the registers.
+    float own[kFillBlocks][4], zown[kFillBlocks][4];
 #pragma unroll
     for (int j = 0; j < kFillBlocks; ++j)
     {
@@ -182,10 +183,26 @@ __device__ __forceinline__ void fill_relax_tile(int nr, int nc, bool per_ns, boo
         {
             const int lr = 2 * by + 1 + (k >> 1), lc = 2 * bx + 1 + (k & 1);
             const int r = r0 + lr, c = c0 + lc;
-            if (r < nr && c < nc && kind[static_cast<std::int64_t>(r) * nc + c] == 1) free_mask |= 1u << (4 * j + k);
+            zown[j][k] = INFINITY;
+            if (r < nr && c < nc)
+            {
+                const std::int64_t g = static_cast<std::int64_t>(r) * nc + c;
+                if (kind[g] == 1)
+                {
+                    free_mask |= 1u << (4 * j + k);
+                    zown[j][k] = z[g];
+                }
+            }
         }
     }
     __syncthreads();
+#pragma unroll
+    for (int j = 0; j < kFillBlocks; ++j)
+    {
+        const int b = tid + j * kFillThreads, bx = b % (kT / 2), by = b / (kT / 2);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) own[j][k] = sF[2 * by + 1 + (k >> 1)][2 * bx + 1 + (k & 1)];
+    }
     // Each local iteration updates the four colours of the 2 x 2 colouring
     // (local row parity, column parity) in turn, a barrier between them:
     // cells of one colour are never neighbours, so every update reads
@@ -203,19 +220,27 @@ __device__ __forceinline__ void fill_relax_tile(int nr, int nc, bool per_ns, boo
             for (int j = 0; j < kFillBlocks; ++j)
             {
             const int b = tid + j * kFillThreads, bx = b % (kT / 2), by = b / (kT / 2);
-            const int lr = 2 * by + 1 + (k >> 1), lc = 2 * bx + 1 + (k & 1);
+            const int R = 2 * by + 1, C = 2 * bx + 1;  // the block's top-left cell
+            const int lr = R + (k >> 1), lc = C + (k & 1);
             if ((free_mask >> (4 * j + k)) & 1u)
             {
-                const float vN = sF[lr - 1][lc], vNE = sF[lr - 1][lc + 1], vE = sF[lr][lc + 1];
-                const float vSE = sF[lr + 1][lc + 1], vS = sF[lr + 1][lc], vSW = sF[lr + 1][lc - 1];
-                const float vW = sF[lr][lc - 1], vNW = sF[lr - 1][lc - 1];
+                // neighbour (dy, dx): a register when it lies in this block
+                // (resolved at compile time: k, dy and dx are constants)
+                auto nb = [&](int dy, int dx) -> float {
+                    const int yy = (k >> 1) + dy, xx = (k & 1) + dx;
+                    if (yy >= 0 && yy <= 1 && xx >= 0 && xx <= 1) return own[j][2 * yy + xx];
+                    return sF[R + yy][C + xx];
+                };
+                const float vN = nb(-1, 0), vNE = nb(-1, 1), vE = nb(0, 1);
+                const float vSE = nb(1, 1), vS = nb(1, 0), vSW = nb(1, -1);
+                const float vW = nb(0, -1), vNW = nb(-1, -1);
                 // lowest neighbour; +inf: none reached yet (or none valid)
                 const float cmin = fminf(fminf(vN, vE), fminf(vS, vW));
                 const float dmin = fminf(fminf(vNE, vSE), fminf(vSW, vNW));
                 const float m = fminf(cmin, dmin);
                 if (m < INFINITY)
                 {
-                    const float zc = sz[lr][lc];
+                    const float zc = zown[j][k];
                     float nv = zc;
                     if (!(zc > m))
                     {
@@ -227,8 +252,9 @@ __device__ __forceinline__ void fill_relax_tile(int nr, int nc, bool per_ns, boo
                                                     (!(vS == m) && ((vSW == m) || (!(vW == m)))))));
                         nv = raise_from(m, min_slope, diag ? Ld : L);
                     }
-                    if (nv < sF[lr][lc])
+                    if (nv < own[j][k])
                     {
+                        own[j][k] = nv;
                         sF[lr][lc] = nv;
                         local = true;
                     }
@@ -250,7 +276,7 @@ __device__ __forceinline__ void fill_relax_tile(int nr, int nc, bool per_ns, boo
             if (!((free_mask >> (4 * j + k)) & 1u)) continue;
             const int lr = 2 * by + 1 + (k >> 1), lc = 2 * bx + 1 + (k & 1);
             const std::int64_t g = static_cast<std::int64_t>(r0 + lr) * nc + (c0 + lc);
-            if (sF[lr][lc] < F[g]) F[g] = sF[lr][lc];
+            if (own[j][k] < F[g]) F[g] = own[j][k];
         }
     }
     if (tid == 0)
