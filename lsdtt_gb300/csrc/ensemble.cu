@@ -2579,7 +2579,18 @@ int lsdtt_gpu_ensemble_create(const lsdtt_gpu_member* members, int32_t n_members
         int dev = 0, sms = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        E->fill_grid = static_cast<unsigned>(std::max(1, sms) * 8);
+        // One wave of resident blocks: with more, the blocks that are not
+        // resident start their share of the tiles only when a resident one
+        // has finished all of its own.
+        int per_sm = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ens_fill_relax_list, kFillThreads, 0) !=
+                cudaSuccess ||
+            per_sm < 1 || per_sm > 8)
+        {
+            cudaGetLastError();
+            per_sm = 8;
+        }
+        E->fill_grid = static_cast<unsigned>(std::max(1, sms) * per_sm);
         for (const PackedMember& Pm : E->pm)
         {
             const lsdtt_gpu_grid& g = E->members[&Pm - E->pm.data()].grid;
