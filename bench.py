@@ -191,6 +191,24 @@ def routing_reference(args, rank, world):
     return 0
 
 
+def rank_max(t: float, dist=None, device: str = "cuda") -> float:
+    """The largest of the ranks' values (a job's time is its slowest rank's);
+    t itself without a process group. FP64, so a time keeps its digits."""
+    if dist is None:
+        return t
+    import torch
+    tt = torch.tensor([float(t)], dtype=torch.float64, device=device)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return float(tt.item())
+
+
+def job_rate(units_per_rank: float, steps: int, t_max: float, world: int) -> float:
+    """Whole-job throughput of independent replicas (weak scaling): every
+    rank processed units_per_rank units a step for `steps` steps, and the job
+    took its slowest rank's time t_max."""
+    return world * units_per_rank * steps / t_max
+
+
 def routing_gpu(args, rank, world):
     import torch
     import lsdtt_gb300 as G
@@ -254,12 +272,8 @@ def routing_gpu(args, rank, world):
         if k.value:
             kernels[name] = {"ms": t.value, "launches": k.value, "bytes": b.value}
     L.lsdtt_gpu_profile_enable(0)
-    t_max = elapsed
-    if dist is not None:
-        tt = torch.tensor([elapsed], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_max = float(tt.item())
-    value = world * n * n * args.steps / t_max
+    t_max = rank_max(elapsed, dist)
+    value = job_rate(n * n, args.steps, t_max, world)
 
     # End to end through the public host-buffer call.
     zh = torch.from_numpy(z).pin_memory()
@@ -285,12 +299,8 @@ def routing_gpu(args, rank, world):
         e2e_step()
     e1.record(stream)
     barrier()
-    e2e_t = e0.elapsed_time(e1) / 1e3
-    if dist is not None:
-        tt = torch.tensor([e2e_t], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_t = float(tt.item())
-    e2e_value = world * n * n * e2e_steps / e2e_t
+    e2e_t = rank_max(e0.elapsed_time(e1) / 1e3, dist)
+    e2e_value = job_rate(n * n, e2e_steps, e2e_t, world)
 
     if rank == 0:
         peak, peak_kind = peaks()
@@ -449,11 +459,7 @@ def ensemble_gpu(args, rank, world):
         torch.cuda.synchronize()
 
     def max_over_ranks(t):
-        if dist is None:
-            return t
-        tt = torch.tensor([t], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        return float(tt.item())
+        return rank_max(t, dist)
 
     ens = G.Ensemble(specs, use_graph=True)
     ens.set_member_groups(bool(args.member_groups))
@@ -481,7 +487,7 @@ def ensemble_gpu(args, rank, world):
     elapsed = max_over_ranks(ev0.elapsed_time(ev1) / 1e3)
     launches = L.lsdtt_gpu_launch_count() - launches0
     info = ens.info()
-    value = world * cells * args.steps / elapsed
+    value = job_rate(cells, args.steps, elapsed, world)
 
     # Kernel table: one profiled step (profiling keeps the ensemble eager).
     # Its NVTX range lets an ncu launch list select it: ncu does not profile
@@ -515,7 +521,7 @@ def ensemble_gpu(args, rank, world):
     e1.record(stream)
     barrier()
     e2e_t = max_over_ranks(e0.elapsed_time(e1) / 1e3)
-    e2e_value = world * cells * e2e_steps / e2e_t
+    e2e_value = job_rate(cells, e2e_steps, e2e_t, world)
     ens.close()
 
     # The plain GPU form: members one at a time through the single-grid LEM.
