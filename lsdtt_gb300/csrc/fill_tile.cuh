@@ -44,7 +44,7 @@ inline unsigned fill_colour_mask(int ntx, int nty, bool per_ns, bool per_ew)
     return m;
 }
 
-__device__ __forceinline__ int fill_colour(int tx, int ty, int ntx, int nty, bool per_ns, bool per_ew)
+__host__ __device__ __forceinline__ int fill_colour(int tx, int ty, int ntx, int nty, bool per_ns, bool per_ew)
 {
     const int cx = (per_ew && (ntx & 1) && ntx > 1 && tx == ntx - 1) ? 2 : (tx & 1);
     const int cy = (per_ns && (nty & 1) && nty > 1 && ty == nty - 1) ? 2 : (ty & 1);
