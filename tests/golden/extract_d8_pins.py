@@ -6,7 +6,7 @@ object for 17 hermetic fixtures x 4 option configurations
 table as text and writes it out as JSON so that the tests need no reference
 checkout at run time.
 
-    python tests/golden/extract_d8_pins.py /path/to/lsdtt3
+    python tests/golden/extract_d8_pins.py /path/to/lsdtt3    (or set LSDTT3_SRC)
 """
 import json
 import os
@@ -34,4 +34,7 @@ def main(ref_root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("LSDTT3_SRC", "")
+    if not root:
+        sys.exit("usage: extract_d8_pins.py /path/to/lsdtt3 (or set LSDTT3_SRC)")
+    main(root)

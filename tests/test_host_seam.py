@@ -11,10 +11,11 @@ import tempfile
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = os.environ.get("LSDTT3_SRC", "/root/reference/src")
+REF = subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "print-src"], capture_output=True,
+                     text=True).stdout.strip()
 
 
-@pytest.mark.skipif(not os.path.isdir(REF), reason="no lsdtt3 checkout")
+@pytest.mark.skipif(not REF or not os.path.isdir(REF), reason="no lsdtt3 checkout")
 def test_seam_compiles_and_is_concrete():
     gxx = shutil.which("g++")
     assert gxx
