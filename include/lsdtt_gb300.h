@@ -75,6 +75,19 @@ unsigned long long lsdtt_gpu_launch_count(void);
 int lsdtt_gpu_profile_enable(int32_t on);
 int lsdtt_gpu_profile_read(const char* kernel, double* total_ms, int64_t* launches, double* bytes);
 
+/* ---- failure-detection self-tests (no reference counterpart) --------------
+ * Every wait inside this library's kernels is bounded: a wait that runs out
+ * raises an abort flag, the kernel returns, and the call reports
+ * LSDTT_GPU_ETIMEOUT while the context stays usable. These two entry points
+ * run the library's own wait routines against a condition that nothing ever
+ * satisfies, with the given poll limit: the grid barrier of the cooperative
+ * stream-power sweep (one block at a barrier that expects two) and the
+ * mbarrier wait of the warp-specialised tensor-core convolutions (a phase
+ * nobody completes). Both return LSDTT_GPU_ETIMEOUT when the wait gave up
+ * as designed; LSDTT_GPU_OK would mean it was released, a fault. */
+int lsdtt_gpu_selftest_grid_barrier(int32_t spin_limit);
+int lsdtt_gpu_selftest_mbarrier_wait(int32_t tries);
+
 /* ---- fill ----------------------------------------------------------------
  * Replaces fill_pits(const lsdtt_raster_cpu&, float min_slope,
  * const std::string& bc, int n_threads, priority_flood_queue_backend)
@@ -363,6 +376,10 @@ int lsdtt_gpu_ensemble_offsets(const lsdtt_gpu_ensemble* ens, int64_t* offsets_h
  * mask also fixes the member's boundary flats. */
 int lsdtt_gpu_ensemble_set_member(lsdtt_gpu_ensemble* ens, int32_t k, const float* z_dev, const uint8_t* mask_dev,
                                   void* stream);
+/* Member k's surface only (same grid, mask unchanged), ordered on `stream`:
+ * a caller that edits members between steps keeps the captured step graph,
+ * which set_member (a mask change) has to rebuild. */
+int lsdtt_gpu_ensemble_set_surface(lsdtt_gpu_ensemble* ens, int32_t k, const float* z_dev, void* stream);
 int lsdtt_gpu_ensemble_get_member(const lsdtt_gpu_ensemble* ens, int32_t k, float* z_dev, void* stream);
 /* All members' surfaces at once, in the packed layout (offsets above; the
  * padding between members is ignored), between host memory and the

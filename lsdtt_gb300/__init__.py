@@ -332,6 +332,7 @@ def _bind_more():
         "lsdtt_gpu_ensemble_offsets": [vp, vp],
         "lsdtt_gpu_ensemble_set_member": [vp, i32, vp, vp, vp],
         "lsdtt_gpu_ensemble_get_member": [vp, i32, vp, vp],
+        "lsdtt_gpu_ensemble_set_surface": [vp, i32, vp, vp],
         "lsdtt_gpu_ensemble_step": [vp, i32, ctypes.POINTER(LemStats), vp],
         "lsdtt_gpu_ensemble_get_info": [vp, ctypes.POINTER(EnsembleInfo)],
         "lsdtt_gpu_ensemble_override_schedule": [vp, i32, i32, i32],
@@ -483,6 +484,23 @@ class Ensemble:
         stats = (LemStats * self.n_members)() if want_stats else None
         _check(lib().lsdtt_gpu_ensemble_step(self._h, n_steps, stats, _stream(stream)))
         return [s.as_dict() for s in stats] if want_stats else None
+
+    def set(self, k, z, mask=None, stream=None):
+        """Replace member k's surface between steps. With a mask, the mask
+        too (which also fixes its boundary flats; the next step captures its
+        graph again); without one, only the elevations (the captured step
+        stays)."""
+        torch = _torch()
+        zt = _dev(z, torch.float32)
+        if tuple(zt.shape) != tuple(self.shapes[k]):
+            raise ValueError(f"member {k} is {self.shapes[k]}, got {tuple(zt.shape)}")
+        if mask is None:
+            _check(lib().lsdtt_gpu_ensemble_set_surface(self._h, k, ctypes.c_void_p(zt.data_ptr()), _stream(stream)))
+        else:
+            mt = _dev(mask, torch.uint8)
+            _check(lib().lsdtt_gpu_ensemble_set_member(self._h, k, ctypes.c_void_p(zt.data_ptr()),
+                                                       ctypes.c_void_p(mt.data_ptr()), _stream(stream)))
+        (stream or torch.cuda.current_stream()).synchronize()
 
     def get(self, k, stream=None):
         torch = _torch()

@@ -331,9 +331,22 @@ int lsdtt_gpu_flow_build(lsdtt_gpu_flow* f, const float* z_dev, const std::uint8
                                           std::to_string(b / g.nc) + ", col " + std::to_string(b % g.nc));
     }
     if (f->herr[3] != ~0ull)
-        return fail(LSDTT_GPU_EINVAL, "lsdtt_flowinfo: forced outlet flat index entry " +
-                                          std::to_string(f->herr[3]) +
-                                          " is outside the raster or lands on a nodata or masked cell");
+    {
+        // validate_forced_outlet_flats (flowinfo_cpu.cpp:969-1008): the
+        // first failing entry, with the reference's two messages.
+        const std::uint64_t i = f->herr[3];
+        std::int64_t fl = -1;
+        e = cudaMemcpy(&fl, forced_dev + i, sizeof(fl), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return cuda_fail(e, "lsdtt_gpu_flow_build");
+        if (fl < 0 || fl >= n)
+            return fail(LSDTT_GPU_EINVAL, "lsdtt_flowinfo: forced outlet flat index " + std::to_string(fl) +
+                                              " (entry " + std::to_string(i) + ") is outside the raster, which has " +
+                                              std::to_string(n) + " cells");
+        return fail(LSDTT_GPU_EINVAL, "lsdtt_flowinfo: forced outlet flat index " + std::to_string(fl) + " (entry " +
+                                          std::to_string(i) + ", row " + std::to_string(fl / g.nc) + ", col " +
+                                          std::to_string(fl % g.nc) +
+                                          ") lands on a nodata or masked cell, so it cannot act as a flow termination");
+    }
     cudaMemcpyAsync(f->derr, init, sizeof(init), cudaMemcpyHostToDevice, st);
 
     e = launch_receivers(f, z_dev, f->mask, plane, o.interior_nodata_is_outlet, o.allow_pits_as_outlets, st);

@@ -692,7 +692,8 @@ __global__ void __launch_bounds__(1024) ens_sp_tail(SweepArgs A, int k0)
 // Receiver elevations are read from L2 (other SMs wrote them).
 constexpr int kBarrierSpinLimit = 1 << 22;
 
-__device__ __forceinline__ bool ens_grid_barrier(unsigned* bar, unsigned nblocks, int* abort_flag)
+__device__ __forceinline__ bool ens_grid_barrier(unsigned* bar, unsigned nblocks, int* abort_flag,
+                                                 int spin_limit = kBarrierSpinLimit)
 {
     __shared__ int ok;
     __syncthreads();
@@ -713,7 +714,7 @@ __device__ __forceinline__ bool ens_grid_barrier(unsigned* bar, unsigned nblocks
             int spins = 0;
             while (gen.load(cuda::memory_order_acquire) == g)
             {
-                if (++spins > kBarrierSpinLimit || ab.load(cuda::memory_order_relaxed) != 0)
+                if (++spins > spin_limit || ab.load(cuda::memory_order_relaxed) != 0)
                 {
                     ab.store(1, cuda::memory_order_relaxed);
                     good = 0;
@@ -758,6 +759,18 @@ __global__ void __launch_bounds__(512) ens_sp_coop(SweepArgs A, int split, unsig
         }
         __syncthreads();
     }
+}
+
+// Failure-detection self-test of the bounded grid barrier: one block
+// arrives at a barrier that expects two arrivals, so nothing ever releases
+// its wait; the wait gives up after spin_limit polls, raises the abort flag
+// and the kernel reports it. bar[0..1] and *abort_flag start at zero.
+__global__ void ens_barrier_selftest(unsigned* __restrict__ bar, int* __restrict__ abort_flag,
+                                     int* __restrict__ released, int spin_limit)
+{
+    LSDTT_COUNT();
+    const bool ok = ens_grid_barrier(bar, 2u, abort_flag, spin_limit);
+    if (threadIdx.x == 0) *released = ok ? 1 : 0;
 }
 
 constexpr unsigned kSweepClusterBlock = 256;  // largest block of the member-cluster sweep
@@ -2693,6 +2706,19 @@ int lsdtt_gpu_ensemble_set_member(lsdtt_gpu_ensemble* E, int32_t k, const float*
     return e == cudaSuccess ? LSDTT_GPU_OK : cuda_fail(e, "lsdtt_gpu_ensemble_set_member");
 }
 
+int lsdtt_gpu_ensemble_set_surface(lsdtt_gpu_ensemble* E, int32_t k, const float* z_dev, void* stream)
+{
+    if (!E || !z_dev || k < 0 || k >= E->M) return fail(LSDTT_GPU_EINVAL, "lsdtt_gpu_ensemble_set_surface: bad argument");
+    if (!E->member_set[static_cast<std::size_t>(k)])
+        return fail(LSDTT_GPU_ESTATE, "lsdtt_gpu_ensemble_set_surface: member has no mask yet (set_member first)");
+    const PackedMember& P = E->pm[static_cast<std::size_t>(k)];
+    const std::size_t n = static_cast<std::size_t>(P.nr) * P.nc;
+    // Elevations only: the mask, the boundary flats and the captured step stay valid.
+    const cudaError_t e = cudaMemcpyAsync(E->z + P.base, z_dev, sizeof(float) * n, cudaMemcpyDeviceToDevice,
+                                          static_cast<cudaStream_t>(stream));
+    return e == cudaSuccess ? LSDTT_GPU_OK : cuda_fail(e, "lsdtt_gpu_ensemble_set_surface");
+}
+
 int lsdtt_gpu_ensemble_get_member(const lsdtt_gpu_ensemble* E, int32_t k, float* z_dev, void* stream)
 {
     if (!E || !z_dev || k < 0 || k >= E->M) return fail(LSDTT_GPU_EINVAL, "lsdtt_gpu_ensemble_get_member: bad argument");
@@ -2842,6 +2868,37 @@ int lsdtt_gpu_ensemble_get_info(const lsdtt_gpu_ensemble* E, lsdtt_gpu_ensemble_
 }
 
 }  // extern "C"
+
+// lsdtt_gpu_selftest_grid_barrier (no reference counterpart): runs the
+// cooperative sweep's bounded grid barrier against an arrival that never
+// comes. Returns LSDTT_GPU_ETIMEOUT when the wait gave up as designed (the
+// expected outcome), LSDTT_GPU_OK if it was released (a fault of the
+// barrier), another status on a CUDA error. The context stays usable.
+extern "C" int lsdtt_gpu_selftest_grid_barrier(int32_t spin_limit)
+{
+    using namespace lsdtt_gb300;
+    if (spin_limit <= 0) return fail(LSDTT_GPU_EINVAL, "lsdtt_gpu_selftest_grid_barrier: spin_limit must be positive");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        return fail(LSDTT_GPU_ENODEV, "lsdtt_gpu_selftest_grid_barrier: no CUDA device");
+    int* buf = nullptr;  // bar[2], abort flag, released
+    cudaError_t e = cudaMalloc(&buf, 4 * sizeof(int));
+    if (e != cudaSuccess) return cuda_fail(e, "lsdtt_gpu_selftest_grid_barrier");
+    int host[4] = {0, 0, 0, -1};
+    e = cudaMemset(buf, 0, 4 * sizeof(int));
+    if (e == cudaSuccess)
+    {
+        ens_barrier_selftest<<<1, 128>>>(reinterpret_cast<unsigned*>(buf), buf + 2, buf + 3, spin_limit);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(host, buf, sizeof(host), cudaMemcpyDeviceToHost);
+    cudaFree(buf);
+    if (e != cudaSuccess) return cuda_fail(e, "lsdtt_gpu_selftest_grid_barrier");
+    if (host[3] == 0 && host[2] == 1)
+        return fail(LSDTT_GPU_ETIMEOUT, "lsdtt_gpu_selftest_grid_barrier: the bounded grid barrier gave up after " +
+                                            std::to_string(spin_limit) + " polls and raised the abort flag");
+    return LSDTT_GPU_OK;
+}
 
 namespace lsdtt_gb300
 {

@@ -298,9 +298,12 @@ LSDTT_DEFINE_LAUNCH_READER(fill)
 //   * It fits grids of up to about 16.7 million cells (4096 x 4096); larger
 //     grids are rejected with LSDTT_GPU_EINVAL before any work is queued.
 //   * Host code cannot use the array's name as a device address, so the
-//     first call on each device looks the address up with
-//     cudaGetSymbolAddress (with that device current) and caches it. Make
-//     that first call before any stream capture.
+//     first call in each CUDA context looks the address up with
+//     cudaGetSymbolAddress (with that device current) and caches it under
+//     the context's process-unique id; a context created after the last
+//     lookup (for example after cudaDeviceReset tore the primary context
+//     down, which unloads the module and may move the array) looks it up
+//     again. Make the first call on a device before any stream capture.
 //   * Every call reuses the same array and clears the parts that must start
 //     from a known state. Calls whose work overlaps on the GPU (different
 //     streams, or host threads without ordering) race on the array; keep
@@ -311,7 +314,38 @@ static constexpr std::size_t kFillNoAllocBytes = (std::size_t(16) << 20) + (std:
 static __device__ __align__(256) unsigned char g_fill_noalloc_scratch[kFillNoAllocBytes];
 
 static std::mutex g_fill_noalloc_mu;
-static void* g_fill_noalloc_addr[256] = {};  // per-device address of the array, filled on first use
+// Per device: the context the cached address belongs to (its
+// process-unique id from cuCtxGetId, 0 = none yet) and the address.
+static unsigned long long g_fill_noalloc_ctx[256] = {};
+static void* g_fill_noalloc_addr[256] = {};
+
+// Process-unique id of the calling thread's current context (the driver's
+// cuCtxGetCurrent / cuCtxGetId, reached through the runtime's entry-point
+// query so the library needs no link against the driver library).
+static cudaError_t current_context_id(unsigned long long* id)
+{
+    using get_current_t = int (*)(void**);
+    using get_id_t = int (*)(void*, unsigned long long*);
+    static get_current_t get_current = nullptr;
+    static get_id_t get_id = nullptr;
+    if (!get_current || !get_id)
+    {
+        void* f0 = nullptr;
+        void* f1 = nullptr;
+        cudaDriverEntryPointQueryResult q0 = cudaDriverEntryPointSymbolNotFound, q1 = q0;
+        cudaError_t e = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f0, 12000, cudaEnableDefault, &q0);
+        if (e == cudaSuccess) e = cudaGetDriverEntryPointByVersion("cuCtxGetId", &f1, 12000, cudaEnableDefault, &q1);
+        if (e != cudaSuccess) return e;
+        if (q0 != cudaDriverEntryPointSuccess || q1 != cudaDriverEntryPointSuccess || !f0 || !f1)
+            return cudaErrorNotSupported;
+        get_current = reinterpret_cast<get_current_t>(f0);
+        get_id = reinterpret_cast<get_id_t>(f1);
+    }
+    void* ctx = nullptr;
+    if (get_current(&ctx) != 0 || !ctx) return cudaErrorDeviceUninitialized;
+    if (get_id(ctx, id) != 0) return cudaErrorDeviceUninitialized;
+    return cudaSuccess;
+}
 
 extern "C" int lsdtt_gpu_fill_pits_noalloc(const lsdtt_gpu_grid* grid, const float* z_dev,
                                            const std::uint8_t* mask_dev, float min_slope, float* out_dev,
@@ -354,15 +388,24 @@ extern "C" int lsdtt_gpu_fill_pits_noalloc(const lsdtt_gpu_grid* grid, const flo
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return cuda_fail(e, "lsdtt_gpu_fill_pits_noalloc");
     if (dev < 0 || dev >= 256) return fail(LSDTT_GPU_EINVAL, "lsdtt_gpu_fill_pits_noalloc: device index out of range");
+    // cudaSetDevice on the current device makes its primary context current
+    // (it initialises the context when this thread has none yet), so the
+    // context id below is the one the kernels will run in.
+    e = cudaSetDevice(dev);
+    if (e != cudaSuccess) return cuda_fail(e, "lsdtt_gpu_fill_pits_noalloc");
+    unsigned long long ctx = 0;
+    e = current_context_id(&ctx);
+    if (e != cudaSuccess) return cuda_fail(e, "lsdtt_gpu_fill_pits_noalloc: current context");
     void* base = nullptr;
     {
         std::lock_guard<std::mutex> lk(g_fill_noalloc_mu);
-        if (!g_fill_noalloc_addr[dev])
+        if (!g_fill_noalloc_addr[dev] || g_fill_noalloc_ctx[dev] != ctx)
         {
             void* p = nullptr;
             e = cudaGetSymbolAddress(&p, g_fill_noalloc_scratch);
             if (e != cudaSuccess) return cuda_fail(e, "lsdtt_gpu_fill_pits_noalloc: cudaGetSymbolAddress");
             g_fill_noalloc_addr[dev] = p;
+            g_fill_noalloc_ctx[dev] = ctx;
         }
         base = g_fill_noalloc_addr[dev];
     }

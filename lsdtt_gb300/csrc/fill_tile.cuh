@@ -74,7 +74,7 @@ __device__ __forceinline__ bool fill_nb(int nr, int nc, bool per_ns, bool per_ew
 }
 
 // Initial state of one cell (row-major index i of an nr x nc grid): seeds
-// hold z and are fixed, other valid cells +inf, invalid cells hold the nodata
+// (and NaN cells) hold z and are fixed, other valid cells +inf, invalid cells hold the nodata
 // value (and are never read as neighbours).
 __device__ __forceinline__ void fill_init_cell(int nr, int nc, bool per_ns, bool per_ew, const float* __restrict__ z,
                                                const std::uint8_t* __restrict__ mask, double nodata, int interior_nd,
@@ -99,8 +99,14 @@ __device__ __forceinline__ void fill_init_cell(int nr, int nc, bool per_ns, bool
             if (rr >= 0 && rr < nr && cc >= 0 && cc < nc && !valid_at(static_cast<std::int64_t>(rr) * nc + cc))
                 seed = true;
         }
-    F[i] = seed ? z[i] : INFINITY;
-    kind[i] = seed ? 2 : 1;  // 2 seed (fixed), 1 free
+    // A NaN elevation in a valid cell is kept as it is and never raised;
+    // its neighbours' minimum skips it (fminf ignores NaN), so nothing
+    // spills through it. (The reference's heap
+    // orders a NaN key arbitrarily; its output there is not defined by
+    // the algorithm.)
+    const bool nan_cell = isnan(z[i]);
+    F[i] = (seed || nan_cell) ? z[i] : INFINITY;
+    kind[i] = (seed || nan_cell) ? 2 : 1;  // 2 seed or NaN (fixed), 1 free
 }
 
 // Does cell i of an nr x nc grid flag interior nodata (an invalid cell off

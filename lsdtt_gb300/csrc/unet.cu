@@ -931,9 +931,10 @@ __device__ __forceinline__ void tc_commit(std::uint32_t bar)
 // all; gives up early once another role raised the abort flag. On failure
 // raises it.
 constexpr int kWsSpin = 1 << 20;
-__device__ __forceinline__ bool ws_wait(std::uint32_t bar, std::uint32_t parity, volatile int* abort_flag)
+__device__ __forceinline__ bool ws_wait(std::uint32_t bar, std::uint32_t parity, volatile int* abort_flag,
+                                        int tries = kWsSpin)
 {
-    for (int spin = 0; spin < kWsSpin; ++spin)
+    for (int spin = 0; spin < tries; ++spin)
     {
         std::uint32_t ok;
         asm volatile(
@@ -946,6 +947,24 @@ __device__ __forceinline__ bool ws_wait(std::uint32_t bar, std::uint32_t parity,
     }
     *abort_flag = 1;
     return false;
+}
+
+// Failure-detection self-test of the bounded mbarrier wait: one thread
+// initialises an mbarrier that expects one arrival and waits on its first
+// phase, which nothing completes; ws_wait gives up after `tries` polls and
+// raises the abort flag, and the kernel reports it.
+__global__ void ws_wait_selftest(int* __restrict__ abort_flag, int* __restrict__ released, int tries)
+{
+    LSDTT_COUNT();
+    __shared__ __align__(8) unsigned long long mbar;
+    const std::uint32_t bar = static_cast<std::uint32_t>(__cvta_generic_to_shared(&mbar));
+    if (threadIdx.x == 0)
+    {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) *released = ws_wait(bar, 0u, abort_flag, tries) ? 1 : 0;
 }
 
 // Input row `row` of the 130-pixel window at x0 - 1 into the slot at slot_s
@@ -2118,6 +2137,36 @@ int lsdtt_gpu_unet_train_step(lsdtt_gpu_unet* U, const float* r_dev, const float
     k_bf16_round<<<nb, 256, 0, st>>>(U->nparam, U->w, U->wr);
     const cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? LSDTT_GPU_OK : cuda_fail(e, "lsdtt_gpu_unet_train_step");
+}
+
+// lsdtt_gpu_selftest_mbarrier_wait (no reference counterpart): runs the
+// tensor-core convolutions' bounded mbarrier wait against a phase that never
+// completes. LSDTT_GPU_ETIMEOUT when the wait gave up as designed (the
+// expected outcome), LSDTT_GPU_OK if it was released (a fault of the wait),
+// another status on a CUDA error. The context stays usable.
+int lsdtt_gpu_selftest_mbarrier_wait(int32_t tries)
+{
+    if (tries <= 0) return fail(LSDTT_GPU_EINVAL, "lsdtt_gpu_selftest_mbarrier_wait: tries must be positive");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        return fail(LSDTT_GPU_ENODEV, "lsdtt_gpu_selftest_mbarrier_wait: no CUDA device");
+    int* buf = nullptr;  // abort flag, released
+    cudaError_t e = cudaMalloc(&buf, 2 * sizeof(int));
+    if (e != cudaSuccess) return cuda_fail(e, "lsdtt_gpu_selftest_mbarrier_wait");
+    int host[2] = {0, -1};
+    e = cudaMemset(buf, 0, 2 * sizeof(int));
+    if (e == cudaSuccess)
+    {
+        ws_wait_selftest<<<1, 32>>>(buf, buf + 1, tries);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(host, buf, sizeof(host), cudaMemcpyDeviceToHost);
+    cudaFree(buf);
+    if (e != cudaSuccess) return cuda_fail(e, "lsdtt_gpu_selftest_mbarrier_wait");
+    if (host[1] == 0 && host[0] == 1)
+        return fail(LSDTT_GPU_ETIMEOUT, "lsdtt_gpu_selftest_mbarrier_wait: the bounded mbarrier wait gave up after " +
+                                            std::to_string(tries) + " polls and raised the abort flag");
+    return LSDTT_GPU_OK;
 }
 
 }  // extern "C"

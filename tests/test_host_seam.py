@@ -1,7 +1,10 @@
 """The C++ drop-in for lsdtt3's abstract D8 seam
 (lsdtt_gb300/host/lsdtt_flowinfo_gpu.hpp) compiles against the reference's
 own headers and implements every pure virtual of lsdtt_flow_base (it is not
-abstract). Needs a reference checkout (LSDTT3_SRC or the default location);
+abstract), and the GPU overloads at the fill, stream-power and LEM seams
+(lsdtt_gb300/host/lsdtt_gpu_overloads.hpp) resolve with the reference's own
+argument lists. The same engine runs on the GPU in
+tests/test_gpu_host_engine.py, which needs no checkout. Needs a reference checkout (LSDTT3_SRC or the default location);
 skipped where there is none."""
 import os
 import shutil
@@ -28,6 +31,15 @@ std::unique_ptr<lsdtt::lsdtt_flow_base> make_gpu(const lsdtt::lsdtt_array2d_f& d
                                                  const lsdtt::lsdtt_raster_meta& meta,
                                                  const lsdtt::lsdtt_flowinfo_options& o)
 { return std::make_unique<lsdtt::lsdtt_flowinfo_gpu>(d, m, meta, o); }
+#include "lsdtt_gb300/host/lsdtt_gpu_overloads.hpp"
+// The three overloads resolve with the reference's own argument lists.
+lsdtt::lsdtt_raster_cpu sp(const lsdtt::lsdtt_raster_cpu& dem, const lsdtt::lsdtt_flowinfo_gpu& flow)
+{ return lsdtt::compute_d8_stream_power_incision(dem, flow, 1e-5f, 0.5f, 1.0f, 1000.0f, 0.0f, true, 1e-5f); }
+lsdtt::lsdtt_raster_cpu fill(const lsdtt::lsdtt_raster_cpu& r) { return lsdtt::fill_pits_gpu(r, 1e-4f, "nnon"); }
+std::pair<lsdtt::lsdtt_raster_cpu, lsdtt::lsdtt_lem_step_stats> lem(const lsdtt::lsdtt_raster_cpu& dem,
+                                                                   const lsdtt::lsdtt_lem_options& o,
+                                                                   const std::vector<std::int64_t>& bf)
+{ return lsdtt::run_lem_step_gpu(dem, o, bf); }
 """
     with tempfile.TemporaryDirectory() as td:
         f = os.path.join(td, "seam.cpp")
