@@ -125,19 +125,36 @@ class Clocks:
 
 
 def traffic_per_cell(kernel: str):
-    """DRAM bytes per cell for a kernel from the committed ncu summary
-    (profiles/ncu_traffic.txt: '<kernel> <bytes_per_cell> <note>')."""
-    p = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
+    """DRAM bytes per cell of one launch of `kernel`, from its committed ncu
+    summary (profiles/<kernel>_ncu.md, the line 'traffic_bytes_per_cell: X':
+    dram__bytes_read.sum + dram__bytes_write.sum of a captured launch over
+    the cells it covered); None when no summary exists."""
+    p = os.path.join(ROOT, "profiles", f"{kernel}_ncu.md")
     if not os.path.exists(p):
         return None
     for line in open(p):
-        parts = line.split()
-        if len(parts) >= 2 and parts[0] == kernel:
+        if line.strip().startswith("traffic_bytes_per_cell:"):
             try:
-                return float(parts[1])
-            except ValueError:
+                return float(line.split(":", 1)[1].split()[0])
+            except (ValueError, IndexError):
                 return None
     return None
+
+
+def profile_table(L):
+    """Every profile record of the library (name -> ms, launches, bytes)."""
+    need = ctypes.c_int64()
+    L.lsdtt_gpu_profile_names.argtypes = [ctypes.c_char_p, ctypes.c_int64, ctypes.POINTER(ctypes.c_int64)]
+    L.lsdtt_gpu_profile_names(None, 0, ctypes.byref(need))
+    buf = ctypes.create_string_buffer(int(need.value) + 1)
+    L.lsdtt_gpu_profile_names(buf, len(buf), ctypes.byref(need))
+    out = {}
+    for name in buf.value.decode().split():
+        t, k, b = ctypes.c_double(), ctypes.c_int64(), ctypes.c_double()
+        L.lsdtt_gpu_profile_read(name.encode(), ctypes.byref(t), ctypes.byref(k), ctypes.byref(b))
+        if k.value:
+            out[name] = {"ms": t.value, "launches": k.value, "bytes": b.value}
+    return out
 
 
 def cpu_baseline(n_sample: int, reps: int = 1):
@@ -431,8 +448,9 @@ def ensemble_reference(args, rank, world):
     return 0
 
 
-ENS_KERNELS = ("ens_fill_relax", "ens_d8_receivers", "stack_ruler_walk", "ens_hillslope_apply",
-               "ens_hillslope_update")
+# Records that time a stage of several kernels (the s-vector stage), not one
+# kernel: listed, but never the roofline's dominant kernel.
+ENS_STAGES = ("ens_stack_counts",)
 
 
 def ensemble_gpu(args, rank, world):
@@ -497,12 +515,7 @@ def ensemble_gpu(args, rank, world):
     ens.step()
     torch.cuda.synchronize()
     torch.cuda.nvtx.range_pop()
-    kernels = {}
-    for name in ENS_KERNELS:
-        t, k, b = ctypes.c_double(), ctypes.c_int64(), ctypes.c_double()
-        G._check(L.lsdtt_gpu_profile_read(name.encode(), ctypes.byref(t), ctypes.byref(k), ctypes.byref(b)))
-        if k.value:
-            kernels[name] = {"ms": t.value, "launches": k.value, "bytes": b.value}
+    kernels = profile_table(L)
     L.lsdtt_gpu_profile_enable(0)
 
     # End to end: the packed surfaces to and from pinned host memory every step.
@@ -526,8 +539,8 @@ def ensemble_gpu(args, rank, world):
 
     # The plain GPU form: members one at a time through the single-grid LEM.
     plain = None
-    if args.plain_members > 0:
-        sub = specs[:args.plain_members]
+    if args.plain_members != 0:
+        sub = specs if args.plain_members < 0 else specs[:args.plain_members]
         models = []
         for sp in sub:
             o = {k: v for k, v in sp.items() if k not in ("z", "cell_size", "boundary_conditions")}
@@ -545,14 +558,17 @@ def ensemble_gpu(args, rank, world):
         barrier()
         pt = p0.elapsed_time(p1) / 1e3
         pc = int(sum(sp["z"].size for sp in sub))
-        plain = {"value": pc / pt, "unit": "cell-steps/s", "members": len(sub), "cells": pc,
-                 "call": "lsdtt_gpu_lem_step per member (fill, D8 engine, stream power, Jacobi-PCG hillslope)"}
+        plain = {"value": pc / pt, "unit": "cell-steps/s", "members": len(sub), "cells": pc, "ms_per_step": pt * 1e3,
+                 "call": "lsdtt_gpu_lem_step per member (fill, D8 engine, stream power, Jacobi-PCG hillslope), the "
+                         "same members one grid at a time"}
         for mdl in models:
             mdl.close()
 
     if rank == 0:
         peak, peak_kind = peaks()
-        dom = max(kernels.items(), key=lambda kv: kv[1]["ms"]) if kernels else None
+        single = {k: v for k, v in kernels.items() if k not in ENS_STAGES}
+        dom = max(single.items(), key=lambda kv: kv[1]["ms"]) if single else None
+        step_ms = sum(v["ms"] for v in single.values())
         roof = None
         if dom:
             name, d = dom
@@ -564,10 +580,31 @@ def ensemble_gpu(args, rank, world):
                     "peak_source": "measured hbm_gbs (MEASURED_PEAKS.json), of measured"
                     if peak_kind == "measured" else "fallback 6.8 TB/s, of fallback",
                     "traffic": (tpc * cells) if tpc is not None else None,
+                    "traffic_source": f"profiles/{name}_ncu.md (dram bytes of a captured launch, scaled by cells)"
+                    if tpc is not None else None,
                     "algorithmic_bytes_per_launch": d["bytes"] / d["launches"],
                     "avg_launch_ms": d["ms"] / d["launches"], "launches": d["launches"],
-                    "source": "CUDA events around each launch in one profiled (eager) step of the same ensemble, "
-                              "run right after the timed region"}
+                    "share_of_step": d["ms"] / step_ms if step_ms > 0 else None,
+                    "source": "CUDA events around every kernel launch of one profiled (eager) step of the same "
+                              "ensemble, run right after the timed region; the dominant kernel is the one with the "
+                              "largest total"}
+        # The survey's >= 60% of HBM bar for the D8 receivers and the
+        # contributing counts (algorithmic bytes per cell: receivers 6 + the
+        # exported int64 receiver 8; counts 10).
+        bars = {}
+        rd = kernels.get("ens_d8_receivers")
+        if rd:
+            t = rd["ms"] + kernels.get("ens_d8_receivers_fixup", {}).get("ms", 0.0)
+            bars["d8_receivers"] = {"bytes_per_cell": 14.0, "ms": t, "achieved": 14.0 * cells / (t / 1e3) / 1e9,
+                                    "frac": 14.0 * cells / (t / 1e3) / 1e9 / peak, "bar": 0.6,
+                                    "kernels": "ens_d8_receivers + ens_d8_receivers_fixup"}
+        sc = kernels.get("ens_stack_counts")
+        if sc:
+            bars["contributing_counts"] = {"bytes_per_cell": 10.0, "ms": sc["ms"],
+                                           "achieved": 10.0 * cells / (sc["ms"] / 1e3) / 1e9,
+                                           "frac": 10.0 * cells / (sc["ms"] / 1e3) / 1e9 / peak, "bar": 0.6,
+                                           "kernels": "the s-vector stage (Euler tour links, ruling-set list "
+                                                      "ranking, count/depth outputs)"}
         cpu = None
         if world == 1 and not args.skip_cpu:
             v, cc, used, t = ensemble_cpu_sample(specs, 20.0)
@@ -588,9 +625,13 @@ def ensemble_gpu(args, rank, world):
                              f"no flush", "warmup_s": t_warm},
             "schedule": info,
             "plain_gpu": plain,
+            "batched_over_plain": (value / plain["value"]) if plain else None,
             "roofline": roof,
-            "kernels": {k: {"ms_per_launch": v["ms"] / v["launches"], "launches": v["launches"],
-                            "GBps": v["bytes"] / (v["ms"] / 1e3) / 1e9} for k, v in kernels.items()},
+            "hbm_bars": bars,
+            "kernels": {k: {"ms": v["ms"], "launches": v["launches"],
+                            "share": (v["ms"] / step_ms) if (step_ms > 0 and k not in ENS_STAGES) else None,
+                            "GBps": (v["bytes"] / (v["ms"] / 1e3) / 1e9) if v["bytes"] > 0 else None}
+                        for k, v in sorted(kernels.items(), key=lambda kv: -kv[1]["ms"])},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "cell-steps/s", "h2d_bytes_per_step": 4 * npk,
                     "d2h_bytes_per_step": 4 * npk,
@@ -818,7 +859,8 @@ def main():
     ap.add_argument("--train-steps", type=int, default=4000)
     ap.add_argument("--members", type=int, default=256)
     ap.add_argument("--sweep-mode", type=int, default=-1, help="ensemble sweep: -1 autotuned, 0 levels, 1 dataflow, 2 cooperative levels, 3 member clusters")
-    ap.add_argument("--plain-members", type=int, default=16)
+    ap.add_argument("--plain-members", type=int, default=-1,
+                    help="members stepped one at a time for the plain GPU form (-1: all of them, 0: skip)")
     ap.add_argument("--member-groups", type=int, default=0, choices=[0, 1],
                     help="ensemble: the deep members' sweep beside the others' sweep and hillslope solve (1) or not")
     ap.add_argument("--conv-kernel", default="", choices=["", "mma", "tcgen05", "tcgen05_rows", "tcgen05_ws"],

@@ -65,8 +65,9 @@ const char* lsdtt_gpu_version(void);
 /* ---- instrumentation (no reference counterpart; tracing for the backend) --
  * launch_count: kernels of this library executed since load (each kernel's
  * first block bumps a device counter; reading it synchronises the device).
- * profile_enable(1) starts recording a CUDA event pair around each hot
- * kernel launch, on the launch's own stream; profile_read sums, for one
+ * profile_enable(1) starts recording a CUDA event pair around each kernel
+ * launch of the ensemble step (and the hot launches of the single-grid
+ * path), on the launch's own stream; profile_read sums, for one
  * kernel name, the elapsed time, the number of launches and the algorithmic
  * bytes those launches move (the per-cell byte counts of the backend's
  * design notes times the cells each launch covers). profile_enable(0) stops
@@ -74,6 +75,11 @@ const char* lsdtt_gpu_version(void);
 unsigned long long lsdtt_gpu_launch_count(void);
 int lsdtt_gpu_profile_enable(int32_t on);
 int lsdtt_gpu_profile_read(const char* kernel, double* total_ms, int64_t* launches, double* bytes);
+/* The names of every kernel (or stage) with profile records, one per line
+ * in first-launch order; *needed receives the buffer size the list takes
+ * (with its terminating NUL), buf (may be NULL) the list, truncated to
+ * buflen. */
+int lsdtt_gpu_profile_names(char* buf, int64_t buflen, int64_t* needed);
 
 /* ---- failure-detection self-tests (no reference counterpart) --------------
  * Every wait inside this library's kernels is bounded: a wait that runs out
@@ -157,6 +163,31 @@ int lsdtt_gpu_flow_get_view(const lsdtt_gpu_flow* flow, lsdtt_gpu_flow_view* vie
  * reference's forward push in topological order. */
 int lsdtt_gpu_flow_accumulate(lsdtt_gpu_flow* flow, const double* weights_dev, double* out_dev,
                               void* stream);
+
+/* ---- query rasters on the D8 engine ---------------------------------------
+ * The lsdtt_flow_base rasters built on the s-vector
+ * (src/core/lsdtt_flow_base.hpp:126-491; src/cpu/lsdtt_flowinfo_cpu.cpp:
+ * 2255-2965), on a built engine with its s-vector. `kind` selects:
+ *   0 get_distance_from_outlet_raster()                           (:2255-2302)
+ *   1 get_height_above_channel_raster(values, vmask, threshold)   (:2309-2382)
+ *   2 get_height_above_channel_mask_donor_raster(values, vmask, channel_mask)
+ *                                          (:2407-2474; donor_dev = donor_flat)
+ *   3 get_distance_to_channel_raster(threshold)                   (:2482-2553)
+ *   4 get_height_to_farthest_ridge_raster(values, vmask)          (:2571-2649)
+ *   5 get_distance_to_farthest_ridge_raster()                     (:2651-2713)
+ *   6 get_downstream_path_sum_raster(values, vmask, channel_mask = sink_mask)
+ *                                                                 (:2721-2791)
+ *   7 get_upslope_sum_raster(values, vmask, include_self)         (:2800-2868)
+ *   8 get_upslope_mean_raster(values, vmask, include_self)        (:2876-2960)
+ * Device arrays of n_rows * n_cols: values (float, the elev or values
+ * argument), value_mask_dev (u8) and channel_mask_dev (u8) where the query
+ * takes them (NULL otherwise); out_dev / out_mask_dev receive the raster's
+ * data and mask (no_data_value where the mask is 0); donor_dev (int64, may
+ * be NULL) the nearest channel cell of kind 2 (-1 where none). Same bits as
+ * the reference. The engine's workspace holds the passes' arrays. */
+int lsdtt_gpu_flow_query(lsdtt_gpu_flow* flow, int32_t kind, const float* values_dev, const uint8_t* value_mask_dev,
+                         const uint8_t* channel_mask_dev, int32_t threshold, int32_t include_self, float* out_dev,
+                         uint8_t* out_mask_dev, int64_t* donor_dev, void* stream);
 
 /* ---- stream power ---------------------------------------------------------
  * compute_d8_stream_power_incision (src/cpu/lsdtt_stream_power_cpu.hpp:74-89,

@@ -244,6 +244,35 @@ class FlowInfo:
                                                ctypes.c_void_p(out.data_ptr()), _stream(stream)))
         return out
 
+    # The lsdtt_flow_base query rasters (lsdtt_gpu_flow_query kinds).
+    QUERY_KINDS = {"distance_from_outlet": 0, "height_above_channel": 1, "height_above_channel_mask": 2,
+                   "distance_to_channel": 3, "height_to_farthest_ridge": 4, "distance_to_farthest_ridge": 5,
+                   "downstream_path_sum": 6, "upslope_sum": 7, "upslope_mean": 8}
+
+    def query(self, kind, values=None, value_mask=None, channel_mask=None, threshold=1, include_self=True,
+              stream=None):
+        """One query raster by name (get_<kind>_raster of lsdtt_flowinfo;
+        channel_mask is the sink mask of downstream_path_sum). Returns
+        (data float32, mask uint8, donor int64 or None) CUDA tensors of the
+        grid's shape."""
+        torch = _torch()
+        k = self.QUERY_KINDS[kind]
+        shape = self.shape
+        vt = None if values is None else _dev(values, torch.float32).reshape(shape).contiguous()
+        vm = None if value_mask is None else _dev(value_mask, torch.uint8).reshape(shape).contiguous()
+        cm = None if channel_mask is None else _dev(channel_mask, torch.uint8).reshape(shape).contiguous()
+        out = torch.empty(shape, dtype=torch.float32, device="cuda")
+        om = torch.empty(shape, dtype=torch.uint8, device="cuda")
+        donor = torch.empty(shape, dtype=torch.int64, device="cuda") if k == 2 else None
+        vp = ctypes.c_void_p
+        fn = lib().lsdtt_gpu_flow_query
+        fn.argtypes = [vp, ctypes.c_int32, vp, vp, vp, ctypes.c_int32, ctypes.c_int32, vp, vp, vp, vp]
+        fn.restype = ctypes.c_int
+        ptr = lambda t: vp(t.data_ptr() if t is not None else 0)  # noqa: E731
+        _check(fn(self._h, k, ptr(vt), ptr(vm), ptr(cm), int(threshold), int(bool(include_self)), ptr(out), ptr(om),
+                  ptr(donor), _stream(stream)))
+        return out, om, donor
+
     def close(self):
         if getattr(self, "_h", None):
             lib().lsdtt_gpu_flow_destroy(self._h)

@@ -2,6 +2,7 @@
 // checks with the reference's messages, engine lifetime, and the mapping of
 // device error words to status codes.
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -135,6 +136,7 @@ unsigned long long launches_stack();
 unsigned long long launches_stream_power();
 unsigned long long launches_unet();
 unsigned long long launches_ensemble();
+unsigned long long launches_queries();
 
 namespace
 {
@@ -171,7 +173,7 @@ unsigned long long lsdtt_gpu_launch_count(void)
 {
     return launches_abi() + launches_d8() + launches_fill() + launches_hillslope() + launches_lem() +
            launches_stack() + launches_stream_power() + launches_unet() +
-           launches_ensemble();
+           launches_ensemble() + launches_queries();
 }
 
 int lsdtt_gpu_profile_enable(int32_t on)
@@ -207,6 +209,29 @@ int lsdtt_gpu_profile_read(const char* kernel, double* total_ms, int64_t* launch
     *total_ms = t;
     *launches = k;
     *bytes = by;
+    return LSDTT_GPU_OK;
+}
+
+int lsdtt_gpu_profile_names(char* buf, int64_t buflen, int64_t* needed)
+{
+    if (!needed) return fail(LSDTT_GPU_EINVAL, "lsdtt_gpu_profile_names: null");
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    std::string all;
+    std::vector<std::string> seen;
+    for (const auto& r : g_prof)
+    {
+        if (std::find(seen.begin(), seen.end(), r.name) != seen.end()) continue;
+        seen.push_back(r.name);
+        all += r.name;
+        all += '\n';
+    }
+    *needed = static_cast<int64_t>(all.size()) + 1;
+    if (buf && buflen > 0)
+    {
+        const std::size_t k = std::min<std::size_t>(all.size(), static_cast<std::size_t>(buflen - 1));
+        std::memcpy(buf, all.data(), k);
+        buf[k] = '\0';
+    }
     return LSDTT_GPU_OK;
 }
 

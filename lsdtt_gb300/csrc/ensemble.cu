@@ -1819,10 +1819,12 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
     cudaMemsetAsync(E->flags, 0, sizeof(int) * kFlags, st);
     // 0. fill
     cudaMemsetAsync(E->nd, 0, sizeof(int) * M, st);
-    ens_interior<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->z, E->mask, E->nd);
-    ens_fill_init<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->z, E->mask, E->nd, E->zf, E->kind);
-    ens_dirty_init<<<grid_blocks(E->T, 256), 256, 0, st>>>(E->T, E->tile_member, E->d_prm, E->dirty,
-                                                           E->dirty + E->T);
+    LSDTT_TIMED("ens_interior", 0.0, st, (ens_interior<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->z, E->mask, E->nd)));
+    LSDTT_TIMED("ens_fill_init", 0.0, st,
+                (ens_fill_init<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->z, E->mask, E->nd, E->zf, E->kind)));
+    LSDTT_TIMED("ens_dirty_init", 0.0, st,
+                (ens_dirty_init<<<grid_blocks(E->T, 256), 256, 0, st>>>(E->T, E->tile_member, E->d_prm, E->dirty,
+                                                                        E->dirty + E->T)));
     const dim3 fblock(32, 8);
     const double cells = static_cast<double>(E->member_cells);
     const unsigned tb = static_cast<unsigned>((E->T + 255) / 256);
@@ -1834,7 +1836,12 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
         const std::uint8_t* din = E->dirty + (pass & 1) * E->T;
         std::uint8_t* dout = E->dirty + ((pass + 1) & 1) * E->T;
         cudaMemsetAsync(E->fcnt, 0, sizeof(unsigned long long) * (kFillColours + 1), s);
-        ens_fill_active<<<tb, 256, 0, s>>>(E->P, E->d_prm, E->tile_member, E->T, din, dout, E->flist, E->fcnt);
+        if (timed)
+            LSDTT_TIMED("ens_fill_active", 0.0, s,
+                        (ens_fill_active<<<tb, 256, 0, s>>>(E->P, E->d_prm, E->tile_member, E->T, din, dout, E->flist,
+                                                            E->fcnt)));
+        else
+            ens_fill_active<<<tb, 256, 0, s>>>(E->P, E->d_prm, E->tile_member, E->T, din, dout, E->flist, E->fcnt);
         double bytes = 9.0 * cells;
         if (timed && profiling_enabled())
         {
@@ -1907,21 +1914,29 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
                 (ens_receivers<<<E->S, 256, 0, st>>>(E->P, E->d_prm, E->strip_member, E->zf, E->mask, f->receiver,
                                                      f->dir, E->undecided)));
     // one thread per perimeter cell (each looks its member up by a binary search)
-    ens_receivers_fixup<<<static_cast<unsigned>(std::max<std::int64_t>((E->perim + 255) / 256, 152 * 4)), 256, 0,
-                          st>>>(E->P, E->d_prm, E->perim, E->zf, E->mask, f->receiver, f->dir, f->derr,
-                                E->undecided);
-    ens_outlet_flag<<<nb, 256, 0, st>>>(N, E->mask, f->dir, E->oflag);
+    LSDTT_TIMED("ens_d8_receivers_fixup", 0.0, st,
+                (ens_receivers_fixup<<<static_cast<unsigned>(std::max<std::int64_t>((E->perim + 255) / 256, 152 * 4)),
+                                       256, 0, st>>>(E->P, E->d_prm, E->perim, E->zf, E->mask, f->receiver, f->dir,
+                                                     f->derr, E->undecided)));
+    LSDTT_TIMED("ens_outlet_flag", 0.0, st, (ens_outlet_flag<<<nb, 256, 0, st>>>(N, E->mask, f->dir, E->oflag)));
     f->ws.used = 0;
-    e = exclusive_scan<std::uint8_t, std::int64_t>(E->oflag, N, E->pos, f->dscal + 1, f->ws, st);
+    LSDTT_TIMED("ens_outlet_scan", 0.0, st,
+                (e = exclusive_scan<std::uint8_t, std::int64_t>(E->oflag, N, E->pos, f->dscal + 1, f->ws, st)));
     if (e != cudaSuccess) return e;
-    ens_scatter<<<nb, 256, 0, st>>>(E->oflag, E->pos, N, f->outlets);
+    LSDTT_TIMED("ens_outlet_scatter", 0.0, st, (ens_scatter<<<nb, 256, 0, st>>>(E->oflag, E->pos, N, f->outlets)));
     f->ws.used = 0;
-    e = build_stack(f, false, st, &E->P);
+    // The s-vector stage (Euler tour, ruling-set list ranking): contributing
+    // counts and depths; timed as a whole (its ruler walk also on its own).
+    // Algorithmic bytes per cell: direction 1 + donor 1 in, int64 count 8
+    // out (10).
+    LSDTT_TIMED("ens_stack_counts", 10.0 * cells, st, (e = build_stack(f, false, st, &E->P)));
     if (e != cudaSuccess) return e;
     cudaMemsetAsync(E->dfc + 1, 0, sizeof(std::uint32_t), st);  // count of large-count nodes
-    ens_kam<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->mask, f->dir, f->sv_size, E->kam_tab, E->area, E->lfill,
-                                E->dfc + 1);
-    ens_kam_big<<<152 * 8, 256, 0, st>>>(E->P, E->d_prm, f->sv_size, E->lfill, E->dfc + 1, E->area);
+    LSDTT_TIMED("ens_kam", 0.0, st,
+                (ens_kam<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->mask, f->dir, f->sv_size, E->kam_tab, E->area,
+                                             E->lfill, E->dfc + 1)));
+    LSDTT_TIMED("ens_kam_big", 0.0, st,
+                (ens_kam_big<<<152 * 8, 256, 0, st>>>(E->P, E->d_prm, f->sv_size, E->lfill, E->dfc + 1, E->area)));
     // 2. depth levels: the global level order (level launches, the
     // cooperative and dataflow sweeps, and every eager step's record) and
     // the member-major order (member-cluster sweep, and the autotuner)
@@ -1933,7 +1948,8 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
             eager ? static_cast<std::uint32_t>(N + 1) : static_cast<std::uint32_t>(E->depth_cap);
         cudaMemsetAsync(E->maxd, 0, sizeof(std::uint32_t), st);
         cudaMemsetAsync(E->lcount, 0, sizeof(std::uint32_t) * (static_cast<std::size_t>(cap) + 2), st);
-        ens_depth_hist<<<nb, 256, 0, st>>>(N, E->mask, f->depth, cap, E->lcount, E->maxd, E->flags + 2);
+        LSDTT_TIMED("ens_depth_hist", 0.0, st,
+                    (ens_depth_hist<<<nb, 256, 0, st>>>(N, E->mask, f->depth, cap, E->lcount, E->maxd, E->flags + 2)));
         std::uint32_t scan_len = cap + 1;
         if (eager)
         {
@@ -1947,7 +1963,8 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
                                                          static_cast<std::uint32_t*>(nullptr), f->ws, st);
         if (e != cudaSuccess) return e;
         cudaMemsetAsync(E->lfill, 0, sizeof(std::uint32_t) * scan_len, st);
-        ens_depth_scatter<<<nb, 256, 0, st>>>(N, E->mask, f->depth, cap, E->lstart, E->lfill, E->order);
+        LSDTT_TIMED("ens_depth_scatter", 0.0, st,
+                    (ens_depth_scatter<<<nb, 256, 0, st>>>(N, E->mask, f->depth, cap, E->lstart, E->lfill, E->order)));
     }
     if (member_order)
     {
@@ -1995,7 +2012,7 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
         }
     }
     // 3. stream power, swept by depth level
-    ens_copy<<<nb, 256, 0, st>>>(E->zf, E->zsp, N);
+    LSDTT_TIMED("ens_copy", 0.0, st, (ens_copy<<<nb, 256, 0, st>>>(E->zf, E->zsp, N)));
     SweepArgs A{E->P, E->d_prm, E->order, E->lstart, E->maxd, f->receiver, f->dir, E->area, E->zf, E->zsp};
     if (eager)
     {
@@ -2110,8 +2127,12 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
         }
         const int sp = E->tail == 0 ? static_cast<int>(D) + 1 : split_for(rec->level_size, E->tail);
         E->split = sp;
-        e = enqueue_sweep(E, A, sp, E->sweep_block, level_grid(rec->level_size, sp, E->sweep_block, 1.0), st,
-                          E->sweep_mode);
+        // Algorithmic bytes per cell: z_old 4 + direction 1 + count 8 +
+        // receiver z 4 in, z 4 out (21).
+        static const char* const kSweepName[4] = {"ens_sp_levels", "ens_sp_dataflow", "ens_sp_coop", "ens_sp_clusters"};
+        LSDTT_TIMED(kSweepName[E->sweep_mode & 3], 21.0 * cells, st,
+                    (e = enqueue_sweep(E, A, sp, E->sweep_block, level_grid(rec->level_size, sp, E->sweep_block, 1.0),
+                                       st, E->sweep_mode)));
         if (e != cudaSuccess) return e;
     }
     const bool split_groups = !eager && E->sweep_mode == 3 && E->n_deep > 0 && E->n_deep < M;
@@ -2142,8 +2163,9 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
     auto reduce = [&](cudaStream_t s2, int nq, unsigned max_mask, const int* dn, double* dst, int stride, int off,
                       const int* shift, int tile_partials = 0) {
         const unsigned warps = static_cast<unsigned>(M * nq);
-        ens_member_reduce<<<(warps + 3) / 4, 128, 0, s2>>>(E->P, nq, max_mask, E->part, nblk, dn, dst, stride, off,
-                                                           shift, slot_len, tile_partials);
+        LSDTT_TIMED("ens_member_reduce", 0.0, s2,
+                    (ens_member_reduce<<<(warps + 3) / 4, 128, 0, s2>>>(E->P, nq, max_mask, E->part, nblk, dn, dst,
+                                                                        stride, off, shift, slot_len, tile_partials)));
     };
     struct HsGroup
     {
@@ -2157,13 +2179,19 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
     auto hillslope_stage = [&](cudaStream_t hs, const HsGroup& G) -> cudaError_t {
         cudaMemsetAsync(E->hs_acc, 0, slot_bytes * (static_cast<std::size_t>(itmax) + 1), hs);
         ens_group_done<<<mb, 128, 0, hs>>>(M, G.grp, G.g, E->done);
-        ens_hs_setup<<<G.nblk, 256, 0, hs>>>(E->P, E->d_prm, E->mask, E->zsp, E->dof, E->invd, E->b, E->part, G.blist);
+        LSDTT_TIMED("ens_hs_setup", 0.0, hs,
+                    (ens_hs_setup<<<G.nblk, 256, 0, hs>>>(E->P, E->d_prm, E->mask, E->zsp, E->dof, E->invd, E->b,
+                                                          E->part, G.blist)));
         reduce(hs, 1, 0u, E->done, E->hs_bb, 1, 0, nullptr);
         // Warm start: the previous step's increment x (zero at the first step)
         // as the initial guess; A x0 by one plain apply (p_dst = x).
-        ens_hs_apply_tiled<<<G.ntile, 256, 0, hs>>>(E->P, E->d_prm, E->strip_member, E->mask, E->dof, E->done, 0,
-                                                    E->pcg_scal, nullptr, E->zz, E->p2, E->x, E->Ap, E->part, G.tlist);
-        ens_hs_init<<<G.nblk, 256, 0, hs>>>(E->P, E->b, E->invd, E->dof, E->Ap, E->x, E->r, E->p, E->part, G.blist);
+        LSDTT_TIMED("ens_hs_warm_apply", 0.0, hs,
+                    (ens_hs_apply_tiled<<<G.ntile, 256, 0, hs>>>(E->P, E->d_prm, E->strip_member, E->mask, E->dof,
+                                                                 E->done, 0, E->pcg_scal, nullptr, E->zz, E->p2, E->x,
+                                                                 E->Ap, E->part, G.tlist)));
+        LSDTT_TIMED("ens_hs_init", 0.0, hs,
+                    (ens_hs_init<<<G.nblk, 256, 0, hs>>>(E->P, E->b, E->invd, E->dof, E->Ap, E->x, E->r, E->p, E->part,
+                                                         G.blist)));
         reduce(hs, 1, 0u, E->done, E->hs_acc, kHsSlot, 1, nullptr);
         ens_hs_start<<<mb, 128, 0, hs>>>(M, E->d_prm, E->hs_bb, E->done, E->iters, G.grp, G.g);
         // One iteration whose slots are it / it + 1 (it_dev: plus the device-side
@@ -2189,7 +2217,8 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
                                                             G.tlist);
             reduce(s2, 1, 0u, E->done, cur, kHsSlot, 0, it_dev, 1);
             // alpha = r.z (slot it) / p.Ap (slot it + 1)
-            ens_pcg_ratio<<<mb, 128, 0, s2>>>(M, E->done, E->hs_acc, it, 1, it + 1, 0, it_dev, alpha);
+            LSDTT_TIMED("ens_pcg_ratio", 0.0, s2,
+                        (ens_pcg_ratio<<<mb, 128, 0, s2>>>(M, E->done, E->hs_acc, it, 1, it + 1, 0, it_dev, alpha)));
             if (timed)
             {
                 // Algorithmic bytes: the update 24 B/cell.
@@ -2202,7 +2231,8 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
                                                       E->part, G.blist);
             reduce(s2, 2, 0u, E->done, cur, kHsSlot, 1, it_dev);
             // beta for the next iteration = r.z (slot it + 1) / r.z (slot it)
-            ens_pcg_ratio<<<mb, 128, 0, s2>>>(M, E->done, E->hs_acc, it + 1, 1, it, 1, it_dev, beta);
+            LSDTT_TIMED("ens_pcg_ratio", 0.0, s2,
+                        (ens_pcg_ratio<<<mb, 128, 0, s2>>>(M, E->done, E->hs_acc, it + 1, 1, it, 1, it_dev, beta)));
         };
         if (device_loop)
         {
@@ -2263,8 +2293,10 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
     if (e != cudaSuccess) return e;
     // 5. the increment, uplift + boundary restore and the statistics in one
     // pass; flags to the host
-    ens_step_finish<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->mask, E->bflag, E->dof, E->zsp, E->x, E->zf, E->z,
-                                        E->part);
+    // Algorithmic bytes per cell (uplift + restore + statistics): 12.
+    LSDTT_TIMED("ens_step_finish", 12.0 * cells, st,
+                (ens_step_finish<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->mask, E->bflag, E->dof, E->zsp, E->x, E->zf,
+                                                     E->z, E->part)));
     reduce(st, 8, 0xf0u, nullptr, E->stats_acc, 8, 0, nullptr);
     cudaMemcpyAsync(E->h_stats, E->stats_acc, sizeof(double) * 8 * M, cudaMemcpyDeviceToHost, st);
     cudaMemcpyAsync(E->h_flags, E->flags, sizeof(int) * kFlags, cudaMemcpyDeviceToHost, st);

@@ -272,6 +272,41 @@ public:
         return od.to_host();
     }
 
+    // The query rasters of lsdtt_flow_base (flowinfo_cpu.cpp:2255-2965):
+    // kind as lsdtt_gpu_flow_query; values / value_mask / channel_mask are
+    // the reference method's elev (or values), elev_mask (valid_mask) and
+    // channel_mask (sink_mask) where it takes them.
+    struct raster_out
+    {
+        std::vector<float> data;
+        std::vector<std::uint8_t> mask;
+        std::vector<std::int64_t> donor;  // kind 2 only
+    };
+    raster_out query(int kind, const std::vector<float>& values = {}, const std::vector<std::uint8_t>& value_mask = {},
+                     const std::vector<std::uint8_t>& channel_mask = {}, int threshold = 1,
+                     bool include_self = true) const
+    {
+        const std::size_t n = mask_.size();
+        auto sized = [&](std::size_t k) { return k == 0 || k == n; };
+        if (!sized(values.size()) || !sized(value_mask.size()) || !sized(channel_mask.size()))
+            throw std::invalid_argument(
+                "lsdtt_flowinfo: query inputs must have the same flat-index size as the DEM");
+        device_buffer<float> vd(values.data(), values.size()), od(n);
+        device_buffer<std::uint8_t> vm(value_mask.data(), value_mask.size()), cm(channel_mask.data(),
+                                                                                   channel_mask.size()),
+            om(n);
+        device_buffer<std::int64_t> dd(kind == 2 ? n : 0);
+        check(lsdtt_gpu_flow_query(flow_, kind, values.empty() ? nullptr : vd.get(),
+                                   value_mask.empty() ? nullptr : vm.get(), channel_mask.empty() ? nullptr : cm.get(),
+                                   threshold, include_self ? 1 : 0, od.get(), om.get(), kind == 2 ? dd.get() : nullptr,
+                                   nullptr));
+        raster_out r;
+        r.data = od.to_host();
+        r.mask = om.to_host();
+        if (kind == 2) r.donor = dd.to_host();
+        return r;
+    }
+
     // The engine's C handle and its device copies of the DEM and the mask
     // (for the stream-power call, which reads the routing on the device).
     lsdtt_gpu_flow* handle() const noexcept { return flow_; }

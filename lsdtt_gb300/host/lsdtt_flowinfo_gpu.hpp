@@ -220,47 +220,55 @@ public:
         write(get_drainage_area_exclude_outlet_raster(), p, f);
     }
 
-    // Analysis rasters built on the stack: next on the GB300 engine.
-    lsdtt_raster_result get_distance_from_outlet_raster() const override { not_yet("get_distance_from_outlet_raster"); }
-    lsdtt_raster_result get_height_above_channel_raster(const std::vector<float>&, const std::vector<uint8_t>&,
-                                                        int) const override
+    // Analysis rasters built on the stack (flowinfo_cpu.cpp:2255-2965), on the GPU.
+    lsdtt_raster_result get_distance_from_outlet_raster() const override { return query(0); }
+    lsdtt_raster_result get_height_above_channel_raster(const std::vector<float>& elev,
+                                                        const std::vector<uint8_t>& elev_mask,
+                                                        int threshold_contributing_pixels) const override
     {
-        not_yet("get_height_above_channel_raster");
+        return query(1, elev, elev_mask, {}, threshold_contributing_pixels);
     }
-    lsdtt_raster_result get_height_above_channel_mask_raster(const std::vector<float>&, const std::vector<uint8_t>&,
-                                                             const std::vector<uint8_t>&) const override
+    lsdtt_raster_result get_height_above_channel_mask_raster(const std::vector<float>& elev,
+                                                             const std::vector<uint8_t>& elev_mask,
+                                                             const std::vector<uint8_t>& channel_mask) const override
     {
-        not_yet("get_height_above_channel_mask_raster");
+        return query(2, elev, elev_mask, channel_mask);
     }
     height_above_channel_donor_result get_height_above_channel_mask_donor_raster(
-        const std::vector<float>&, const std::vector<uint8_t>&, const std::vector<uint8_t>&) const override
+        const std::vector<float>& elev, const std::vector<uint8_t>& elev_mask,
+        const std::vector<uint8_t>& channel_mask) const override
     {
-        not_yet("get_height_above_channel_mask_donor_raster");
+        auto r = engine_.query(2, elev, elev_mask, channel_mask);
+        height_above_channel_donor_result out;
+        out.height = as_raster(std::move(r));
+        out.donor_flat = std::move(r.donor);
+        return out;
     }
-    lsdtt_raster_result get_distance_to_channel_raster(int) const override { not_yet("get_distance_to_channel_raster"); }
-    lsdtt_raster_result get_height_to_farthest_ridge_raster(const std::vector<float>&,
-                                                            const std::vector<uint8_t>&) const override
+    lsdtt_raster_result get_distance_to_channel_raster(int threshold_contributing_pixels) const override
     {
-        not_yet("get_height_to_farthest_ridge_raster");
+        return query(3, {}, {}, {}, threshold_contributing_pixels);
     }
-    lsdtt_raster_result get_distance_to_farthest_ridge_raster() const override
+    lsdtt_raster_result get_height_to_farthest_ridge_raster(const std::vector<float>& elev,
+                                                            const std::vector<uint8_t>& elev_mask) const override
     {
-        not_yet("get_distance_to_farthest_ridge_raster");
+        return query(4, elev, elev_mask);
     }
-    lsdtt_raster_result get_downstream_path_sum_raster(const std::vector<float>&, const std::vector<uint8_t>&,
-                                                       const std::vector<uint8_t>&) const override
+    lsdtt_raster_result get_distance_to_farthest_ridge_raster() const override { return query(5); }
+    lsdtt_raster_result get_downstream_path_sum_raster(const std::vector<float>& values,
+                                                       const std::vector<uint8_t>& valid_mask,
+                                                       const std::vector<uint8_t>& sink_mask) const override
     {
-        not_yet("get_downstream_path_sum_raster");
+        return query(6, values, valid_mask, sink_mask);
     }
-    lsdtt_raster_result get_upslope_sum_raster(const std::vector<float>&, const std::vector<uint8_t>&,
-                                               bool) const override
+    lsdtt_raster_result get_upslope_sum_raster(const std::vector<float>& values, const std::vector<uint8_t>& valid_mask,
+                                               bool include_self) const override
     {
-        not_yet("get_upslope_sum_raster");
+        return query(7, values, valid_mask, {}, 1, include_self);
     }
-    lsdtt_raster_result get_upslope_mean_raster(const std::vector<float>&, const std::vector<uint8_t>&,
-                                                bool) const override
+    lsdtt_raster_result get_upslope_mean_raster(const std::vector<float>& values, const std::vector<uint8_t>& valid_mask,
+                                                bool include_self) const override
     {
-        not_yet("get_upslope_mean_raster");
+        return query(8, values, valid_mask, {}, 1, include_self);
     }
     void write_flow_lines(const std::string&, vector_output_format, const std::string&, bool) const override
     {
@@ -309,6 +317,19 @@ private:
     {
         static const std::vector<std::int64_t> none;
         return engine_.has_s_vector() ? (engine_.*get)() : none;
+    }
+    lsdtt_raster_result as_raster(lsdtt_gb300_host::flow_engine::raster_out&& r) const
+    {
+        lsdtt_raster_result out;
+        out.meta = meta_;
+        out.data = std::move(r.data);
+        out.mask = std::move(r.mask);
+        return out;
+    }
+    lsdtt_raster_result query(int kind, const std::vector<float>& v = {}, const std::vector<uint8_t>& vm = {},
+                              const std::vector<uint8_t>& cm = {}, int threshold = 1, bool include_self = true) const
+    {
+        return as_raster(engine_.query(kind, v, vm, cm, threshold, include_self));
     }
     [[noreturn]] static void not_yet(const char* what)
     {

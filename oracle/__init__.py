@@ -119,6 +119,101 @@ class _Lib:
             res["sv_size"] = sz
         return res
 
+    # --------------------------------------------------------------- query rasters
+    QUERY_KINDS = {"distance_from_outlet": 0, "height_above_channel": 1, "height_above_channel_mask": 2,
+                   "distance_to_channel": 3, "height_to_farthest_ridge": 4, "distance_to_farthest_ridge": 5,
+                   "downstream_path_sum": 6, "upslope_sum": 7, "upslope_mean": 8}
+
+    def flow_query(self, kind, z, mask, cell, bc="oooo", values=None, vmask=None, cmask=None, threshold=1,
+                   include_self=True, nodata=-9999.0):
+        """One lsdtt_flow_base query raster on the flow object of z (pits
+        as outlets): returns (data float32, mask uint8, donor int64 or
+        None)."""
+        z = np.ascontiguousarray(z, dtype=np.float32)
+        mask = np.ascontiguousarray(mask, dtype=np.uint8)
+        nr, nc = z.shape
+        v = None if values is None else np.ascontiguousarray(values, dtype=np.float32)
+        vm = None if vmask is None else np.ascontiguousarray(vmask, dtype=np.uint8)
+        cm = None if cmask is None else np.ascontiguousarray(cmask, dtype=np.uint8)
+        k = self.QUERY_KINDS[kind]
+        if self.prefix == "oracle_":
+            v = z if v is None else v
+            vm = mask if vm is None else vm
+            cm = np.zeros_like(mask) if cm is None else cm
+        out = np.empty_like(z)
+        om = np.empty_like(mask)
+        donor = np.empty(z.size, np.int64) if k == 2 else None
+        err = ctypes.create_string_buffer(1024)
+        f = self.fn("flow_query")
+        f.restype = ctypes.c_int
+        rc = f(_p(z, _c_f32), _p(mask, _c_u8), ctypes.c_int(nr), ctypes.c_int(nc), ctypes.c_double(cell),
+               ctypes.c_double(nodata), bc.encode(), ctypes.c_int(k), _p(v, _c_f32), _p(vm, _c_u8), _p(cm, _c_u8),
+               ctypes.c_int(threshold), ctypes.c_int(int(include_self)), _p(out, _c_f32), _p(om, _c_u8),
+               _p(donor, _c_i64), err, ctypes.c_int(1024))
+        if rc != 0:
+            raise OracleError(err.value.decode())
+        return out, om, donor
+
+    # --------------------------------------------------------------- D-infinity
+    def dinf_graph(self, z, mask, cell, bc="oooo", interior_nodata_is_outlet=True, nodata=-9999.0):
+        """The D-infinity lsdtt_flowgraph_cpu: dict of rec [n, 2] (-1 none),
+        w [n, 2], nrec, slope, bearing, donors, topo."""
+        z = np.ascontiguousarray(z, dtype=np.float32)
+        mask = np.ascontiguousarray(mask, dtype=np.uint8)
+        nr, nc = z.shape
+        n = z.size
+        rec = np.empty(2 * n, np.int64)
+        w = np.empty(2 * n, np.float32)
+        nrec = np.empty(n, np.uint8)
+        slope = np.empty(n, np.float32)
+        bearing = np.empty(n, np.float32)
+        donors = np.empty(n, np.uint8)
+        topo = np.empty(n, np.int64)
+        nt = np.zeros(1, np.int64)
+        err = ctypes.create_string_buffer(1024)
+        f = self.fn("dinf_graph")
+        f.restype = ctypes.c_int
+        rc = f(_p(z, _c_f32), _p(mask, _c_u8), ctypes.c_int(nr), ctypes.c_int(nc), ctypes.c_double(cell),
+               ctypes.c_double(nodata), bc.encode(), ctypes.c_int(int(interior_nodata_is_outlet)), _p(rec, _c_i64),
+               _p(w, _c_f32), _p(nrec, _c_u8), _p(slope, _c_f32), _p(bearing, _c_f32), _p(donors, _c_u8),
+               _p(topo, _c_i64), _p(nt, _c_i64), err, ctypes.c_int(1024))
+        if rc != 0:
+            raise OracleError(err.value.decode())
+        return dict(rec=rec.reshape(n, 2), w=w.reshape(n, 2), nrec=nrec, slope=slope, bearing=bearing,
+                    donors=donors, topo=topo[:nt[0]].copy())
+
+    def dinf_accumulate(self, z, mask, cell, bc="oooo", weights=None, nodata=-9999.0):
+        z = np.ascontiguousarray(z, dtype=np.float32)
+        mask = np.ascontiguousarray(mask, dtype=np.uint8)
+        nr, nc = z.shape
+        w = None if weights is None else np.ascontiguousarray(weights, dtype=np.float64)
+        out = np.empty(z.size, np.float64)
+        err = ctypes.create_string_buffer(1024)
+        f = self.fn("dinf_accumulate")
+        f.restype = ctypes.c_int
+        rc = f(_p(z, _c_f32), _p(mask, _c_u8), ctypes.c_int(nr), ctypes.c_int(nc), ctypes.c_double(cell),
+               ctypes.c_double(nodata), bc.encode(), _p(w, _c_f64), _p(out, _c_f64), err, ctypes.c_int(1024))
+        if rc != 0:
+            raise OracleError(err.value.decode())
+        return out
+
+    def dinf_stream_power(self, z, mask, cell, bc, K, m, n, dt, threshold_area=0.0, divide_area_by_dx=True,
+                          slope_clamp=1e-5, nodata=-9999.0):
+        z = np.ascontiguousarray(z, dtype=np.float32)
+        mask = np.ascontiguousarray(mask, dtype=np.uint8)
+        nr, nc = z.shape
+        out = np.empty_like(z)
+        err = ctypes.create_string_buffer(1024)
+        f = self.fn("dinf_stream_power")
+        f.restype = ctypes.c_int
+        rc = f(_p(z, _c_f32), _p(mask, _c_u8), ctypes.c_int(nr), ctypes.c_int(nc), ctypes.c_double(cell),
+               ctypes.c_double(nodata), bc.encode(), ctypes.c_float(K), ctypes.c_float(m), ctypes.c_float(n),
+               ctypes.c_float(dt), ctypes.c_float(threshold_area), ctypes.c_int(int(divide_area_by_dx)),
+               ctypes.c_float(slope_clamp), _p(out, _c_f32), err, ctypes.c_int(1024))
+        if rc != 0:
+            raise OracleError(err.value.decode())
+        return out
+
     # --------------------------------------------------------------- stream power
     def stream_power(self, z, mask, cell, bc, K, m, n, dt, threshold_area=0.0,
                      divide_area_by_dx=True, slope_clamp=1e-5, k_field=None,

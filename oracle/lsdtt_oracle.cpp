@@ -15,6 +15,7 @@
 
 #include <algorithm>
 #include <array>
+#include <cctype>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -571,6 +572,222 @@ std::uint64_t mix_in(std::uint64_t h, std::uint64_t v)
     return splitmix64(h ^ (v + 0x9E3779B97F4A7C15ULL + (h << 6) + (h >> 2)));
 }
 
+// ============================================================================
+// D-infinity flow graph and stream power: lsdtt_flowgraph_cpu with
+// method = d_infinity (src/cpu/lsdtt_flowgraph_cpu.cpp:87-178 constructor,
+// :423-662 build_dinf after Tarboton 1997, :874-985 topological order,
+// :988-1039 accumulate, :1179-1226 build_reverse_levels) and
+// compute_dinf_stream_power_incision (src/cpu/lsdtt_stream_power_cpu.cpp:
+// 329-602).
+// ============================================================================
+
+struct Dinf
+{
+    int nr = 0, nc = 0;
+    double cell = 1.0;
+    std::vector<std::uint8_t> valid;
+    std::vector<std::int64_t> rec;  // [2n], -1 none
+    std::vector<float> w;           // [2n]
+    std::vector<std::uint8_t> nrec, donors;
+    std::vector<float> slope, bearing;
+    std::vector<std::int64_t> topo;
+};
+
+Dinf build_dinf_graph(const float* z, const std::uint8_t* mask, int nr, int nc, double cell, double nodata,
+                      const char* bcs, bool interior_nodata_is_outlet)
+{
+    // Tarboton's eight facets: cardinal e1 and diagonal e2 offsets, the
+    // sector and sign that turn the in-facet angle into a bearing (:60-67).
+    static const int e1r[8] = {0, -1, -1, 0, 0, 1, 1, 0}, e1c[8] = {1, 0, 0, -1, -1, 0, 0, 1};
+    static const int e2r[8] = {-1, -1, -1, -1, 1, 1, 1, 1}, e2c[8] = {1, 1, -1, -1, -1, -1, 1, 1};
+    static const int ac[8] = {0, 1, 1, 2, 2, 3, 3, 4}, af[8] = {1, -1, 1, -1, 1, -1, 1, -1};
+    static const int nbr[8] = {-1, 0, 0, 1, -1, -1, 1, 1}, nbc[8] = {0, -1, 1, 0, -1, 1, -1, 1};
+    const float pi4 = static_cast<float>(M_PI / 4.0);
+    const float rad2deg = static_cast<float>(180.0 / M_PI);
+    const std::string b = bcs ? bcs : "";
+    if (b.size() != 4)
+        throw std::invalid_argument("lsdtt_flowgraph_cpu: boundary_conditions must have exactly 4 characters "
+                                    "(north, east, south, west)");
+    char c4[4];
+    for (int i = 0; i < 4; ++i) c4[i] = static_cast<char>(std::tolower(static_cast<unsigned char>(b[i])));
+    for (int i = 0; i < 4; ++i)
+        if (c4[i] != 'o' && c4[i] != 'n' && c4[i] != 'p' && c4[i] != 'b')
+            throw std::invalid_argument("lsdtt_flowgraph_cpu: boundary_conditions contains an invalid character. "
+                                        "Allowed values are o, n, p, b.");
+    if ((c4[0] == 'p') != (c4[2] == 'p'))
+        throw std::invalid_argument("lsdtt_flowgraph_cpu: north and south periodic boundary flags must match");
+    if ((c4[1] == 'p') != (c4[3] == 'p'))
+        throw std::invalid_argument("lsdtt_flowgraph_cpu: east and west periodic boundary flags must match");
+    Dinf G;
+    G.nr = nr;
+    G.nc = nc;
+    G.cell = cell;
+    const std::size_t n = static_cast<std::size_t>(nr) * nc;
+    const float ndv = static_cast<float>(nodata);
+    G.valid.assign(n, 0);
+    std::int64_t nvalid = 0;
+    for (std::size_t i = 0; i < n; ++i)
+        if (mask[i] && z[i] != ndv && std::isfinite(z[i])) { G.valid[i] = 1; ++nvalid; }
+    G.rec.assign(2 * n, -1);
+    G.w.assign(2 * n, 0.0f);
+    G.nrec.assign(n, 0);
+    G.slope.assign(n, ndv);
+    G.bearing.assign(n, ndv);
+    auto resolve = [&](int r, int c, int dr, int dc, int& rr, int& cc) {
+        rr = r + dr;
+        cc = c + dc;
+        if (rr < 0) { if (c4[0] == 'p') rr = nr - 1; else return false; }
+        if (rr >= nr) { if (c4[2] == 'p') rr = 0; else return false; }
+        if (cc < 0) { if (c4[3] == 'p') cc = nc - 1; else return false; }
+        if (cc >= nc) { if (c4[1] == 'p') cc = 0; else return false; }
+        return true;
+    };
+    const float L = static_cast<float>(cell);
+    for (int r = 0; r < nr; ++r)
+        for (int c = 0; c < nc; ++c)
+        {
+            const std::size_t f = static_cast<std::size_t>(r) * nc + c;
+            if (!G.valid[f]) continue;
+            const bool forced = (c4[0] == 'b' && r == 0) || (c4[2] == 'b' && r == nr - 1) ||
+                                (c4[1] == 'b' && c == nc - 1) || (c4[3] == 'b' && c == 0);
+            if (forced) continue;
+            if (interior_nodata_is_outlet)
+            {
+                bool touches = false;
+                for (int k = 0; k < 8 && !touches; ++k)
+                {
+                    const int rr = r + nbr[k], cc = c + nbc[k];
+                    if (rr < 0 || rr >= nr || cc < 0 || cc >= nc) continue;
+                    touches = !G.valid[static_cast<std::size_t>(rr) * nc + cc];
+                }
+                if (touches) continue;
+            }
+            const float e0 = z[f];
+            float best_s = 0.0f, best_r = 0.0f;
+            int best = -1;
+            std::int64_t b1 = -1, b2 = -1;
+            for (int a = 0; a < 8; ++a)
+            {
+                int r1, c1, r2, c2;
+                if (!resolve(r, c, e1r[a], e1c[a], r1, c1) || !resolve(r, c, e2r[a], e2c[a], r2, c2)) continue;
+                const std::int64_t f1 = static_cast<std::int64_t>(r1) * nc + c1;
+                const std::int64_t f2 = static_cast<std::int64_t>(r2) * nc + c2;
+                if (f1 == static_cast<std::int64_t>(f) || f2 == static_cast<std::int64_t>(f)) continue;
+                if (!G.valid[f1] || !G.valid[f2]) continue;
+                const float e1 = z[f1], e2 = z[f2];
+                if (e0 <= e1 && e0 <= e2) continue;
+                float rr, ss;
+                const float s1 = (e0 - e1) / L;
+                const float s2 = (e1 - e2) / L;
+                if (e0 > e1 && e0 > e2)
+                {
+                    rr = std::atan2(s2, s1);
+                    if (rr < 0.0f) { rr = 0.0f; ss = s1; }
+                    else if (rr > pi4) { rr = pi4; ss = (e0 - e2) / (L * kSqrt2f); }
+                    else ss = std::sqrt(s1 * s1 + s2 * s2);
+                }
+                else if (e0 > e1) { rr = 0.0f; ss = s1; }
+                else { rr = pi4; ss = (e0 - e2) / (L * kSqrt2f); }
+                if (ss > best_s) { best_s = ss; best_r = rr; best = a; b1 = f1; b2 = f2; }
+            }
+            if (best < 0) continue;
+            const float ang = static_cast<float>(af[best]) * best_r +
+                              static_cast<float>(ac[best]) * (static_cast<float>(M_PI) * 0.5f);
+            float bearing = 360.0f - (ang * rad2deg) + 90.0f;
+            while (bearing >= 360.0f) bearing -= 360.0f;
+            while (bearing < 0.0f) bearing += 360.0f;
+            G.slope[f] = best_s;
+            G.bearing[f] = bearing;
+            if (best_r == 0.0f) { G.nrec[f] = 1; G.rec[2 * f] = b1; G.w[2 * f] = 1.0f; }
+            else if (best_r >= pi4) { G.nrec[f] = 1; G.rec[2 * f] = b2; G.w[2 * f] = 1.0f; }
+            else
+            {
+                const float p2 = best_r / pi4;
+                const float p1 = 1.0f - p2;
+                if (b1 == b2) { G.nrec[f] = 1; G.rec[2 * f] = b1; G.w[2 * f] = 1.0f; }
+                else
+                {
+                    G.nrec[f] = 2;
+                    G.rec[2 * f] = b1;
+                    G.w[2 * f] = p1;
+                    G.rec[2 * f + 1] = b2;
+                    G.w[2 * f + 1] = p2;
+                }
+            }
+        }
+    // Donor counts (unique donors) and Kahn's order (FIFO, row-major seeds).
+    G.donors.assign(n, 0);
+    for (std::size_t f = 0; f < n; ++f)
+        for (int k = 0; k < G.nrec[f]; ++k)
+        {
+            const std::int64_t r = G.rec[2 * f + k];
+            if (k == 1 && r == G.rec[2 * f]) continue;
+            if (G.donors[r] < 255) ++G.donors[r];
+        }
+    std::vector<std::uint8_t> remaining = G.donors;
+    std::deque<std::int64_t> q;
+    for (std::size_t f = 0; f < n; ++f)
+        if (G.valid[f] && remaining[f] == 0) q.push_back(static_cast<std::int64_t>(f));
+    G.topo.reserve(static_cast<std::size_t>(nvalid));
+    while (!q.empty())
+    {
+        const std::int64_t f = q.front();
+        q.pop_front();
+        G.topo.push_back(f);
+        for (int k = 0; k < G.nrec[f]; ++k)
+        {
+            const std::int64_t r = G.rec[2 * f + k];
+            if (--remaining[r] == 0) q.push_back(r);
+        }
+    }
+    if (static_cast<std::int64_t>(G.topo.size()) != nvalid)
+        throw std::runtime_error("lsdtt_flowgraph_cpu: cycle detected in receiver graph or inconsistent cell validity. "
+                                 "Ensure the DEM is pit-filled and that valid cells have finite, non-nodata "
+                                 "elevations.");
+    return G;
+}
+
+std::vector<double> dinf_accumulate(const Dinf& G, const double* w)
+{
+    const std::size_t n = G.valid.size();
+    std::vector<double> acc(n, 0.0);
+    const double dw = G.cell * G.cell;
+    for (const std::int64_t f : G.topo) acc[f] = w ? w[f] : dw;
+    for (const std::int64_t f : G.topo)
+    {
+        const double a = acc[f];
+        for (int k = 0; k < G.nrec[f]; ++k) acc[G.rec[2 * f + k]] += a * static_cast<double>(G.w[2 * f + k]);
+    }
+    return acc;
+}
+
+// build_reverse_levels: depth 0 for cells without receivers, else one more
+// than the deepest receiver; each level in reverse topological order.
+std::vector<std::vector<std::int64_t>> dinf_reverse_levels(const Dinf& G)
+{
+    std::vector<int> depth(G.valid.size(), -1);
+    int maxd = 0;
+    for (std::int64_t i = static_cast<std::int64_t>(G.topo.size()) - 1; i >= 0; --i)
+    {
+        const std::int64_t f = G.topo[static_cast<std::size_t>(i)];
+        int d = 0;
+        for (int k = 0; k < G.nrec[f]; ++k)
+        {
+            const std::int64_t r = G.rec[2 * f + k];
+            if (r >= 0 && depth[r] >= 0) d = std::max(d, depth[r] + 1);
+        }
+        depth[f] = d;
+        maxd = std::max(maxd, d);
+    }
+    std::vector<std::vector<std::int64_t>> levels(static_cast<std::size_t>(maxd) + 1);
+    for (std::int64_t i = static_cast<std::int64_t>(G.topo.size()) - 1; i >= 0; --i)
+    {
+        const std::int64_t f = G.topo[static_cast<std::size_t>(i)];
+        levels[static_cast<std::size_t>(depth[f])].push_back(f);
+    }
+    return levels;
+}
+
 }  // namespace
 
 extern "C" {
@@ -679,6 +896,170 @@ int oracle_flowinfo(const float* z, const std::uint8_t* mask, int nr, int nc, do
             const std::vector<double> a = accumulate(F, weights);
             std::memcpy(accum, a.data(), sizeof(double) * n);
         }
+        return 0;
+    }
+    catch (const std::exception& e) { put_err(err, errlen, e.what()); return 1; }
+}
+
+// ---------------------------------------------------------------------------
+// oracle_flow_query: the lsdtt_flow_base query rasters built on the stack
+// (src/cpu/lsdtt_flowinfo_cpu.cpp:2255-2965), on a flow object built with
+// pits as outlets. kind:
+//   0 get_distance_from_outlet_raster                    (:2255-2302)
+//   1 get_height_above_channel_raster(elev, emask, thr)  (:2309-2382)
+//   2 get_height_above_channel_mask_donor_raster(elev, emask, channel_mask)
+//                                                        (:2407-2474; donor out)
+//   3 get_distance_to_channel_raster(thr)                (:2482-2553)
+//   4 get_height_to_farthest_ridge_raster(elev, emask)   (:2571-2649)
+//   5 get_distance_to_farthest_ridge_raster()            (:2651-2713)
+//   6 get_downstream_path_sum_raster(values, vmask, sink_mask) (:2721-2791)
+//   7 get_upslope_sum_raster(values, vmask, include_self)      (:2800-2868)
+//   8 get_upslope_mean_raster(values, vmask, include_self)     (:2876-2960)
+// The passes run over the s-vector in the reference's order (forward =
+// receiver before donor, reverse = donors before receiver) with its double
+// accumulators and float outputs.
+// ---------------------------------------------------------------------------
+int oracle_flow_query(const float* z, const std::uint8_t* mask, int nr, int nc, double cell, double nodata,
+                      const char* bc, int kind, const float* values, const std::uint8_t* vmask,
+                      const std::uint8_t* cmask, int threshold, int include_self, float* out,
+                      std::uint8_t* out_mask, std::int64_t* donor_out, char* err, int errlen)
+{
+    try
+    {
+        FlowOpts o;
+        o.bc = parse_bc(bc);
+        o.allow_pits_as_outlets = true;
+        Flow F = build_flow(z, mask, nr, nc, cell, nodata, o, nullptr, 0);
+        const std::size_t n = static_cast<std::size_t>(nr) * nc;
+        const float ndv = static_cast<float>(nodata);
+        const double dx = cell, dxy = cell * kSqrt2d;
+        const std::vector<std::int64_t>& sv = F.svec;
+        auto step_of = [&](std::int64_t f) {
+            const std::uint8_t d = F.dir[f];
+            return (d == 255u || d % 2u == 0u) ? dx : dxy;
+        };
+        auto dist_outlet = [&]() {
+            std::vector<double> d(n, 0.0);
+            for (const std::int64_t f : sv)
+            {
+                const std::int64_t r = F.receiver[f];
+                if (r == -2) continue;
+                d[f] = d[r] + step_of(f);
+            }
+            return d;
+        };
+        for (std::size_t i = 0; i < n; ++i) { out[i] = ndv; out_mask[i] = 0; }
+        if (kind == 0)
+        {
+            const std::vector<double> d = dist_outlet();
+            for (std::size_t i = 0; i < n; ++i)
+                if (mask[i]) { out[i] = static_cast<float>(d[i]); out_mask[i] = 1; }
+        }
+        else if (kind == 1 || kind == 2)
+        {
+            std::vector<float> ch(n, 0.0f);
+            std::vector<std::int64_t> donor(n, -1);
+            for (const std::int64_t f : sv)
+            {
+                if (!mask[f] || !vmask[f]) continue;
+                const bool is_ch = kind == 1 ? static_cast<std::int64_t>(F.sv_size[f]) >= threshold : cmask[f] != 0;
+                if (is_ch) { ch[f] = values[f]; donor[f] = f; }
+                else
+                {
+                    const std::int64_t r = F.receiver[f];
+                    if (r != -2 && donor[r] >= 0) { ch[f] = ch[r]; donor[f] = donor[r]; }
+                }
+            }
+            for (std::size_t i = 0; i < n; ++i)
+                if (mask[i] && vmask[i] && donor[i] >= 0) { out[i] = values[i] - ch[i]; out_mask[i] = 1; }
+            if (donor_out) std::memcpy(donor_out, donor.data(), sizeof(std::int64_t) * n);
+        }
+        else if (kind == 3)
+        {
+            std::vector<double> d(n, 0.0);
+            std::vector<std::uint8_t> ok(n, 0);
+            auto is_ch = [&](std::int64_t f) { return static_cast<std::int64_t>(F.sv_size[f]) >= threshold; };
+            for (const std::int64_t f : sv)
+            {
+                if (!mask[f]) continue;
+                if (is_ch(f)) { d[f] = 0.0; ok[f] = 1; continue; }
+                const std::int64_t r = F.receiver[f];
+                if (r == -2) continue;
+                if (is_ch(r)) { d[f] = step_of(f); ok[f] = 1; }
+                else if (ok[r]) { d[f] = step_of(f) + d[r]; ok[f] = 1; }
+            }
+            for (std::size_t i = 0; i < n; ++i)
+                if (mask[i] && ok[i]) { out[i] = static_cast<float>(d[i]); out_mask[i] = 1; }
+        }
+        else if (kind == 4 || kind == 5)
+        {
+            const std::vector<double> d = dist_outlet();
+            std::vector<double> up(d);
+            std::vector<float> fe(n, 0.0f);
+            if (kind == 4)
+                for (std::size_t i = 0; i < n; ++i) fe[i] = (mask[i] && vmask[i]) ? values[i] : 0.0f;
+            for (std::int64_t i = static_cast<std::int64_t>(sv.size()) - 1; i >= 0; --i)
+            {
+                const std::int64_t f = sv[static_cast<std::size_t>(i)];
+                const std::int64_t r = F.receiver[f];
+                if (r == -2) continue;
+                if (up[f] > up[r]) { up[r] = up[f]; fe[r] = fe[f]; }
+            }
+            for (std::size_t i = 0; i < n; ++i)
+            {
+                if (!mask[i]) continue;
+                if (kind == 4)
+                {
+                    if (!vmask[i]) continue;
+                    out[i] = fe[i] - values[i];
+                }
+                else
+                    out[i] = static_cast<float>(up[i] - d[i]);
+                out_mask[i] = 1;
+            }
+        }
+        else if (kind == 6)
+        {
+            std::vector<double> acc(n, 0.0);
+            for (const std::int64_t f : sv)
+            {
+                if (!mask[f]) continue;
+                if (cmask[f]) { acc[f] = 0.0; continue; }
+                const double own = vmask[f] ? static_cast<double>(values[f]) : 0.0;
+                const std::int64_t r = F.receiver[f];
+                const bool terminal = r == -2 || cmask[r] != 0;
+                acc[f] = terminal ? own : own + acc[r];
+            }
+            for (std::size_t i = 0; i < n; ++i)
+                if (mask[i] && !cmask[i]) { out[i] = static_cast<float>(acc[i]); out_mask[i] = 1; }
+        }
+        else if (kind == 7 || kind == 8)
+        {
+            std::vector<double> sum(n, 0.0);
+            std::vector<std::int64_t> cnt(n, 0);
+            for (std::size_t i = 0; i < n; ++i)
+                if (mask[i] && include_self && vmask[i]) { sum[i] = values[i]; cnt[i] = 1; }
+            for (std::int64_t i = static_cast<std::int64_t>(sv.size()) - 1; i >= 0; --i)
+            {
+                const std::int64_t f = sv[static_cast<std::size_t>(i)];
+                const std::int64_t r = F.receiver[f];
+                if (r == -2) continue;
+                sum[r] += sum[f];
+                cnt[r] += cnt[f];
+            }
+            for (std::size_t i = 0; i < n; ++i)
+            {
+                if (!mask[i]) continue;
+                if (kind == 7) { out[i] = static_cast<float>(sum[i]); out_mask[i] = 1; }
+                else if (cnt[i] > 0)
+                {
+                    out[i] = static_cast<float>(sum[i] / static_cast<double>(cnt[i]));
+                    out_mask[i] = 1;
+                }
+            }
+        }
+        else
+            throw std::invalid_argument("oracle_flow_query: unknown kind");
         return 0;
     }
     catch (const std::exception& e) { put_err(err, errlen, e.what()); return 1; }
@@ -892,6 +1273,152 @@ int oracle_noise_tilt_surface(int nr, int nc, double cell, int seed, double lo, 
             out[static_cast<std::size_t>(r) * nc + c] += slope * dx * static_cast<float>(d);
         }
     return 0;
+}
+
+// ---------------------------------------------------------------------------
+// oracle_dinf_graph: the D-infinity graph of lsdtt_flowgraph_cpu
+// (flowgraph_cpu.cpp:423-662, 874-985): per cell up to two receivers
+// (-1 none) and their weights, the receiver count, the facet slope and
+// bearing rasters (nodata where a cell has no receiver), unique-donor counts
+// and the topological order (n_topo entries).
+// ---------------------------------------------------------------------------
+int oracle_dinf_graph(const float* z, const std::uint8_t* mask, int nr, int nc, double cell, double nodata,
+                      const char* bc, int interior_nodata_is_outlet, std::int64_t* rec, float* w,
+                      std::uint8_t* nrec, float* slope, float* bearing, std::uint8_t* donors, std::int64_t* topo,
+                      std::int64_t* n_topo, char* err, int errlen)
+{
+    try
+    {
+        const Dinf G = build_dinf_graph(z, mask, nr, nc, cell, nodata, bc, interior_nodata_is_outlet != 0);
+        const std::size_t n = static_cast<std::size_t>(nr) * nc;
+        std::memcpy(rec, G.rec.data(), sizeof(std::int64_t) * 2 * n);
+        std::memcpy(w, G.w.data(), sizeof(float) * 2 * n);
+        std::memcpy(nrec, G.nrec.data(), n);
+        std::memcpy(slope, G.slope.data(), sizeof(float) * n);
+        std::memcpy(bearing, G.bearing.data(), sizeof(float) * n);
+        std::memcpy(donors, G.donors.data(), n);
+        *n_topo = static_cast<std::int64_t>(G.topo.size());
+        std::memcpy(topo, G.topo.data(), sizeof(std::int64_t) * G.topo.size());
+        return 0;
+    }
+    catch (const std::exception& e) { put_err(err, errlen, e.what()); return 1; }
+}
+
+int oracle_dinf_accumulate(const float* z, const std::uint8_t* mask, int nr, int nc, double cell, double nodata,
+                           const char* bc, const double* weights, double* out, char* err, int errlen)
+{
+    try
+    {
+        const Dinf G = build_dinf_graph(z, mask, nr, nc, cell, nodata, bc, true);
+        const std::vector<double> a = dinf_accumulate(G, weights);
+        std::memcpy(out, a.data(), sizeof(double) * a.size());
+        return 0;
+    }
+    catch (const std::exception& e) { put_err(err, errlen, e.what()); return 1; }
+}
+
+// compute_dinf_stream_power_incision (stream_power_cpu.cpp:329-602) with the
+// identity area smoothing and no width correction.
+int oracle_dinf_stream_power(const float* z, const std::uint8_t* mask, int nr, int nc, double cell, double nodata,
+                             const char* bc, float K, float m, float n, float dt, float threshold_area,
+                             int divide_area_by_dx, float slope_clamp, float* out, char* err, int errlen)
+{
+    try
+    {
+        const Dinf G = build_dinf_graph(z, mask, nr, nc, cell, nodata, bc, true);
+        const std::size_t cells = static_cast<std::size_t>(nr) * nc;
+        std::vector<float> zz(z, z + cells);
+        const float dxc = static_cast<float>(cell);
+        const float dxd = static_cast<float>(cell) * kSqrt2f;
+        const std::vector<double> area_d = dinf_accumulate(G, nullptr);
+        const auto levels = dinf_reverse_levels(G);
+        const bool n_is_one = std::abs(n - 1.0f) < 1e-6f;
+        for (const auto& level : levels)
+            for (const std::int64_t f : level)
+            {
+                if (!G.valid[f] || G.nrec[f] == 0) continue;
+                double area = area_d[f];
+                if (divide_area_by_dx) area /= dxc;
+                if (threshold_area > 0.0f && area < static_cast<double>(threshold_area)) continue;
+                const float zo = z[f];
+                float zn = zo;
+                const int nrc = G.nrec[f];
+                const float w0 = nrc > 0 ? G.w[2 * f] : 0.0f;
+                const float w1 = nrc > 1 ? G.w[2 * f + 1] : 0.0f;
+                const bool only_card = nrc == 1 || w0 >= 1.0f - 1e-6f;
+                const bool only_diag = nrc > 1 && w1 >= 1.0f - 1e-6f;
+                const bool two = nrc > 1 && !only_card && !only_diag;
+                auto recv = [&](int k) -> float {
+                    if (k >= nrc) return zo;
+                    const std::int64_t i = G.rec[2 * f + k];
+                    if (i < 0 || i >= static_cast<std::int64_t>(cells)) return zo;
+                    return zz[i];
+                };
+                const float ze1 = recv(0), ze2 = recv(1);
+                const double kam = static_cast<double>(K) * 1.0 * std::pow(area, static_cast<double>(m));
+                const double tol = static_cast<double>(slope_clamp) * dxc;
+                if (two)
+                {
+                    double eps = tol + 1.0;
+                    int it = 0;
+                    do
+                    {
+                        const double sbt = std::pow((ze1 - zn) / dxc, 2.0) + std::pow((ze2 - ze1) / dxc, 2.0);
+                        if (sbt <= 0.0) eps = 0.0;
+                        else
+                        {
+                            const double fz = zn - zo + kam * std::pow(sbt, 0.5 * n) * dt;
+                            const double fdz =
+                                1.0 - kam * n * (ze1 - zn) / (dxc * dxc) * std::pow(sbt, 0.5 * n - 1.0) * dt;
+                            eps = fz / fdz;
+                        }
+                        zn -= static_cast<float>(eps);
+                        ++it;
+                        if (it > 100) eps = tol / 2.0;
+                    } while (std::abs(eps) > tol);
+                    if ((zn - zo) > static_cast<float>(tol) || std::isnan(zn)) zn = zo;
+                    const float zmin = std::min(ze1, ze2);
+                    if (zn < zmin) zn = zmin + slope_clamp * dxc;
+                }
+                else
+                {
+                    const float zr = only_diag ? ze2 : ze1;
+                    const float dxe = only_diag ? dxd : dxc;
+                    if (zr >= zo) zn = zo;
+                    else if (n_is_one)
+                    {
+                        const double spf = kam * (dt / dxe);
+                        zn = static_cast<float>((zo + zr * spf) / (1.0 + spf));
+                        if ((zn - zo) > static_cast<float>(tol) || std::isnan(zn)) zn = zo;
+                    }
+                    else
+                    {
+                        double eps = tol + 1.0;
+                        int it = 0;
+                        do
+                        {
+                            const double slope = (zn - zr) / dxe;
+                            if (slope <= 0.0) eps = 0.0;
+                            else
+                            {
+                                const double fz = zn - zo + kam * dt * std::pow(slope, n);
+                                const double fdz = 1.0 + kam * dt * (n / dxe) * std::pow(slope, n - 1.0);
+                                eps = fz / fdz;
+                            }
+                            zn -= static_cast<float>(eps);
+                            ++it;
+                            if (it > 100) eps = tol / 2.0;
+                        } while (std::abs(eps) > tol);
+                        if ((zn - zo) > static_cast<float>(tol) || std::isnan(zn)) zn = zo;
+                        if (zn < zr) zn = static_cast<float>(zr + slope_clamp * dxe);
+                    }
+                }
+                zz[f] = zn;
+            }
+        std::memcpy(out, zz.data(), sizeof(float) * cells);
+        return 0;
+    }
+    catch (const std::exception& e) { put_err(err, errlen, e.what()); return 1; }
 }
 
 }  // extern "C"

@@ -9,6 +9,7 @@
 // Every function returns 0 on success and 1 when the reference threw; the
 // exception text is copied into `err` (NUL-terminated, truncated to errlen).
 
+#include "lsdtt_flowgraph_cpu.hpp"
 #include "lsdtt_flowinfo_cpu.hpp"
 #include "lsdtt_raster_flow_preprocessing_cpu.hpp"
 #include "lsdtt_stream_power_cpu.hpp"
@@ -223,6 +224,127 @@ int ref_lem_step_fluvial(const float* z, const std::uint8_t* mask, int nr, int n
         stats[3] = res.second.p999_local_elevation_change;
         stats[4] = res.second.mean_erosion_rate;
         stats[5] = res.second.max_erosion_rate;
+        return 0;
+    }
+    catch (const std::exception& e) { put_err(err, errlen, e.what()); return 1; }
+}
+
+// The lsdtt_flow_base query rasters of the reference's own lsdtt_flowinfo
+// (src/cpu/lsdtt_flowinfo_cpu.cpp:2255-2965), with the same `kind` codes as
+// oracle_flow_query.
+int ref_flow_query(const float* z, const std::uint8_t* mask, int nr, int nc, double cell, double nodata,
+                   const char* bc, int kind, const float* values, const std::uint8_t* vmask,
+                   const std::uint8_t* cmask, int threshold, int include_self, float* out,
+                   std::uint8_t* out_mask, std::int64_t* donor_out, char* err, int errlen)
+{
+    try
+    {
+        const std::size_t n = static_cast<std::size_t>(nr) * nc;
+        lsdtt_flowinfo_options o;
+        o.boundary_conditions = bc;
+        o.allow_pits_as_outlets = true;
+        const lsdtt_flowinfo fi(make_a2f(z, nr, nc), make_a2u8(mask, nr, nc), make_meta(nr, nc, cell, nodata), o);
+        const std::vector<float> v(values ? values : z, (values ? values : z) + n);
+        const std::vector<std::uint8_t> vm(vmask ? vmask : mask, (vmask ? vmask : mask) + n);
+        const std::vector<std::uint8_t> cm(cmask ? cmask : mask, (cmask ? cmask : mask) + n);
+        lsdtt_raster_result r;
+        switch (kind)
+        {
+        case 0: r = fi.get_distance_from_outlet_raster(); break;
+        case 1: r = fi.get_height_above_channel_raster(v, vm, threshold); break;
+        case 2:
+        {
+            auto d = fi.get_height_above_channel_mask_donor_raster(v, vm, cm);
+            r = std::move(d.height);
+            if (donor_out) std::memcpy(donor_out, d.donor_flat.data(), sizeof(std::int64_t) * n);
+            break;
+        }
+        case 3: r = fi.get_distance_to_channel_raster(threshold); break;
+        case 4: r = fi.get_height_to_farthest_ridge_raster(v, vm); break;
+        case 5: r = fi.get_distance_to_farthest_ridge_raster(); break;
+        case 6: r = fi.get_downstream_path_sum_raster(v, vm, cm); break;
+        case 7: r = fi.get_upslope_sum_raster(v, vm, include_self != 0); break;
+        case 8: r = fi.get_upslope_mean_raster(v, vm, include_self != 0); break;
+        default: put_err(err, errlen, "ref_flow_query: unknown kind"); return 1;
+        }
+        std::memcpy(out, r.data.data(), sizeof(float) * n);
+        std::memcpy(out_mask, r.mask.data(), n);
+        return 0;
+    }
+    catch (const std::exception& e) { put_err(err, errlen, e.what()); return 1; }
+}
+
+// The reference's own D-infinity lsdtt_flowgraph_cpu (flowgraph_cpu.cpp:
+// 87-178, 423-662, 874-985, 988-1039) and compute_dinf_stream_power_incision
+// (stream_power_cpu.cpp:329-602), with the outputs of oracle_dinf_*.
+static lsdtt_flowgraph_cpu make_dinf(const float* z, const std::uint8_t* mask, int nr, int nc, double cell,
+                                     double nodata, const char* bc, int interior_nodata_is_outlet)
+{
+    lsdtt_flowgraph_options o;
+    o.boundary_conditions = bc;
+    o.interior_nodata_is_outlet = interior_nodata_is_outlet != 0;
+    o.method = lsdtt_flowgraph_method::d_infinity;
+    return lsdtt_flowgraph_cpu(make_a2f(z, nr, nc), make_a2u8(mask, nr, nc), make_meta(nr, nc, cell, nodata), o);
+}
+
+int ref_dinf_graph(const float* z, const std::uint8_t* mask, int nr, int nc, double cell, double nodata,
+                   const char* bc, int interior_nodata_is_outlet, std::int64_t* rec, float* w, std::uint8_t* nrec,
+                   float* slope, float* bearing, std::uint8_t* donors, std::int64_t* topo, std::int64_t* n_topo,
+                   char* err, int errlen)
+{
+    try
+    {
+        const lsdtt_flowgraph_cpu g = make_dinf(z, mask, nr, nc, cell, nodata, bc, interior_nodata_is_outlet);
+        const std::int64_t n = static_cast<std::int64_t>(nr) * nc;
+        for (std::int64_t f = 0; f < n; ++f)
+        {
+            const std::int64_t k = g.n_receivers(f);
+            nrec[f] = static_cast<std::uint8_t>(k);
+            for (int j = 0; j < 2; ++j)
+            {
+                rec[2 * f + j] = j < k ? g.receiver_index_at(f, j) : -1;
+                w[2 * f + j] = j < k ? g.receiver_weight_at(f, j) : 0.0f;
+            }
+            donors[f] = g.donor_count()[static_cast<std::size_t>(f)];
+        }
+        const lsdtt_raster_result s = g.dinf_slopes();
+        const lsdtt_raster_result d = g.dinf_flow_direction();
+        std::memcpy(slope, s.data.data(), sizeof(float) * static_cast<std::size_t>(n));
+        std::memcpy(bearing, d.data.data(), sizeof(float) * static_cast<std::size_t>(n));
+        const auto& t = g.topological_order();
+        *n_topo = static_cast<std::int64_t>(t.size());
+        std::memcpy(topo, t.data(), sizeof(std::int64_t) * t.size());
+        return 0;
+    }
+    catch (const std::exception& e) { put_err(err, errlen, e.what()); return 1; }
+}
+
+int ref_dinf_accumulate(const float* z, const std::uint8_t* mask, int nr, int nc, double cell, double nodata,
+                        const char* bc, const double* weights, double* out, char* err, int errlen)
+{
+    try
+    {
+        const lsdtt_flowgraph_cpu g = make_dinf(z, mask, nr, nc, cell, nodata, bc, 1);
+        const std::size_t n = static_cast<std::size_t>(nr) * nc;
+        const std::vector<double> w = weights ? std::vector<double>(weights, weights + n) : std::vector<double>{};
+        const std::vector<double> a = g.accumulate(w);
+        std::memcpy(out, a.data(), sizeof(double) * n);
+        return 0;
+    }
+    catch (const std::exception& e) { put_err(err, errlen, e.what()); return 1; }
+}
+
+int ref_dinf_stream_power(const float* z, const std::uint8_t* mask, int nr, int nc, double cell, double nodata,
+                          const char* bc, float K, float m, float n, float dt, float threshold_area,
+                          int divide_area_by_dx, float slope_clamp, float* out, char* err, int errlen)
+{
+    try
+    {
+        const lsdtt_flowgraph_cpu g = make_dinf(z, mask, nr, nc, cell, nodata, bc, 1);
+        const lsdtt_raster_cpu dem = make_raster(z, mask, nr, nc, cell, nodata);
+        const lsdtt_raster_cpu r = compute_dinf_stream_power_incision(dem, g, K, m, n, dt, threshold_area,
+                                                                      divide_area_by_dx != 0, slope_clamp, 1, 1, bc);
+        std::memcpy(out, r.get_data().data(), sizeof(float) * static_cast<std::size_t>(nr) * nc);
         return 0;
     }
     catch (const std::exception& e) { put_err(err, errlen, e.what()); return 1; }

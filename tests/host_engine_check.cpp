@@ -10,7 +10,9 @@
 // Writes filled.f32, receiver.i64, direction.u8, donors.u8, outlets.i64,
 // topo.i64, svec.i64, start.i64, size.u64, area.f64, weighted.f64, sp.f32,
 // lem.f32, lem_stats.f32, upslope.i64 (for cells 0, 1, 2, ...: the slice
-// length then its cells) and errors.txt (one line per exception probe).
+// length then its cells), q_dist.f32 / q_dist_mask.u8 (distance from the
+// outlet), q_upsum.f32 (upslope sum of the weights as float) and
+// errors.txt (one line per exception probe).
 #include <cstdio>
 #include <fstream>
 #include <iostream>
@@ -94,6 +96,16 @@ int main(int argc, char** argv)
             }
         }
         write(d + "/upslope.i64", ups);
+        // two query rasters through the C++ layer
+        {
+            const auto q0 = flow.query(0);
+            write(d + "/q_dist.f32", q0.data);
+            write(d + "/q_dist_mask.u8", q0.mask);
+            std::vector<float> vals(cells);
+            for (std::size_t i = 0; i < cells; ++i) vals[i] = static_cast<float>(w[i]);
+            const auto q7 = flow.query(7, vals, mask, {}, 1, true);
+            write(d + "/q_upsum.f32", q7.data);
+        }
         write(d + "/sp.f32", H::stream_power_d8(flow, f.data(), K, m, n, dt));
 
         lsdtt_gpu_lem_options lo{};

@@ -92,6 +92,13 @@ def test_host_engine_against_oracle(port, tmp_path, case):
         checked += 1
     assert checked > 100
 
+    qd = port.flow_query("distance_from_outlet", f, mask, cell, bc)
+    assert np.array_equal(rd("q_dist.f32", np.float32).view(np.uint32), qd[0].ravel().view(np.uint32))
+    assert np.array_equal(rd("q_dist_mask.u8", np.uint8), qd[1].ravel())
+    qs = port.flow_query("upslope_sum", f, mask, cell, bc, values=w.reshape(z.shape).astype(np.float32),
+                         vmask=mask, include_self=True)
+    assert np.array_equal(rd("q_upsum.f32", np.float32).view(np.uint32), qs[0].ravel().view(np.uint32))
+
     sp = port.stream_power(f, mask, cell, bc, K, m_exp, n_exp, dt)
     assert np.array_equal(rd("sp.f32", np.float32).view(np.uint32), sp.ravel().view(np.uint32))
 

@@ -23,10 +23,11 @@ def _cfg1(port, n=512):
     return z, np.ones_like(z, np.uint8)
 
 
-# Measured share of cells whose filled value differs from the reference
-# (value-ordered GPU flood vs the reference's breadth-first FIFO order on
-# flats). Regression guards, not targets: the target is zero.
-FILL_MISMATCH_BOUND = {"noise_tilt_512": 0.05, "fractal_pits_512": 0.5}
+# Share of cells whose filled value differs from the reference (value-
+# ordered GPU flood vs the reference's global FIFO order), bounded just above
+# the measured 1.9% and 30%: regression guards, not targets (the target is
+# zero; see lsdtt_gb300/csrc/fill.cu for why the order cannot be emulated).
+FILL_MISMATCH_BOUND = {"noise_tilt_512": 0.021, "fractal_pits_512": 0.31}
 
 
 def test_fill_properties_and_reported_mismatch(port):
@@ -93,10 +94,10 @@ def test_stream_power_bitwise(port, n_exp):
     ndiff = int(np.count_nonzero(got.view(np.uint32) != want.view(np.uint32)))
     rel = float(np.max(np.abs(got - want) / np.maximum(np.abs(want), 1.0)))
     print(f"stream power n={n_exp}: {ndiff} cells differ, max rel {rel:.3g}")
-    # pow() is libm's on the CPU and CUDA's on the GPU: allow last-bit
-    # differences in a handful of cells, nothing beyond the tolerance.
-    assert ndiff <= max(8, f.size // 10000)
-    assert rel < REL_TOL
+    # Bit-exact: the n = 1 closed form and the Newton iteration follow the
+    # reference's float/double mix step for step.
+    assert ndiff == 0
+    assert rel == 0.0
 
 
 def test_hillslope_linear_vs_fp64(port):

@@ -12,7 +12,8 @@
 
 Bars: the network runs in BF16 with FP32 accumulation in an order the
 oracle does not share, so a BF16 rounding can flip between the two; the
-output is compared at 2e-2 relative L2 and every gradient tensor at 5e-2.
+output is compared at 2e-2 relative L2 (measured 3e-5 to 8e-4) and every
+gradient tensor at 1e-3 (measured 4e-7).
 """
 import numpy as np
 import pytest
@@ -23,7 +24,7 @@ from tests import surfaces
 pytestmark = pytest.mark.gpu
 
 FWD_TOL = 2e-2
-GRAD_TOL = 5e-2
+GRAD_TOL = 1e-3
 
 
 def _params(seed=3):

@@ -100,3 +100,36 @@ def test_fluvial_lem_steps_port_equal_reference(port, ref):
                                       0.5, 1.0, 1e-3, bf)
         assert _bits_equal(za, zb)
         assert _bits_equal(sa, sb)
+
+
+def test_flow_queries_port_equal_reference(port, ref):
+    """The lsdtt_flow_base query rasters (flowinfo_cpu.cpp:2255-2965): data,
+    mask and the donor raster, every kind, on every surface."""
+    for name, z, m, cell, bc in _surfaces(port):
+        f = port.fill_pits(z, m, cell, bc, 1e-4)
+        rng = np.random.default_rng(len(name))
+        vals = rng.uniform(-5.0, 50.0, z.shape).astype(np.float32)
+        vm = (rng.uniform(0, 1, z.shape) > 0.05).astype(np.uint8)
+        cm = (rng.uniform(0, 1, z.shape) > 0.97).astype(np.uint8)
+        for kind in port.QUERY_KINDS:
+            a = port.flow_query(kind, f, m, cell, bc, values=vals, vmask=vm, cmask=cm, threshold=25)
+            b = ref.flow_query(kind, f, m, cell, bc, values=vals, vmask=vm, cmask=cm, threshold=25)
+            assert _bits_equal(a[0], b[0]) and np.array_equal(a[1], b[1]), (name, kind)
+            if a[2] is not None:
+                assert np.array_equal(a[2], b[2]), (name, kind)
+
+
+def test_dinf_port_equals_reference(port, ref):
+    """The D-infinity lsdtt_flowgraph_cpu (receivers, weights, facet slopes
+    and bearings, donor counts, topological order), its accumulate and
+    compute_dinf_stream_power_incision at n = 1, 1.5, 2."""
+    for name, z, m, cell, bc in _surfaces(port)[:4]:
+        f = port.fill_pits(z, m, cell, bc, 1e-4)
+        a = port.dinf_graph(f, m, cell, bc)
+        b = ref.dinf_graph(f, m, cell, bc)
+        for key in a:
+            assert _bits_equal(a[key], b[key]), (name, key)
+        assert _bits_equal(port.dinf_accumulate(f, m, cell, bc), ref.dinf_accumulate(f, m, cell, bc)), name
+        for n_exp in (1.0, 1.5, 2.0):
+            assert _bits_equal(port.dinf_stream_power(f, m, cell, bc, 2e-5, 0.45, n_exp, 500.0),
+                               ref.dinf_stream_power(f, m, cell, bc, 2e-5, 0.45, n_exp, 500.0)), (name, n_exp)
