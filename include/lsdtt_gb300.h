@@ -189,6 +189,45 @@ int lsdtt_gpu_flow_query(lsdtt_gpu_flow* flow, int32_t kind, const float* values
                          const uint8_t* channel_mask_dev, int32_t threshold, int32_t include_self, float* out_dev,
                          uint8_t* out_mask_dev, int64_t* donor_dev, void* stream);
 
+/* ---- D-infinity flow graph ------------------------------------------------
+ * Replaces lsdtt_flowgraph_cpu(dem, mask, meta, options) with
+ * options.method = d_infinity (src/cpu/lsdtt_flowgraph_cpu.hpp:149-160;
+ * .cpp:87-178, 423-662 Tarboton's facets, 874-985 donor counts and Kahn's
+ * topological order, 988-1039 accumulate) and
+ * compute_dinf_stream_power_incision (src/cpu/lsdtt_stream_power_cpu.hpp:
+ * 113-129, .cpp:329-602; area smoothing kernel 1, no width factor). The
+ * handle owns its device arrays; build() may be called again with new
+ * elevations of the same grid. The receiver graph and the topological
+ * order are the reference's; weights and facet slopes follow its float
+ * arithmetic with the in-facet angle as the double atan2 rounded to float. */
+typedef struct lsdtt_gpu_dinf lsdtt_gpu_dinf;
+typedef struct lsdtt_gpu_dinf_view
+{
+    const int64_t* receivers;         /* [2n] per cell: receiver 0, receiver 1 (-1 none) */
+    const float* weights;             /* [2n] their flow fractions               */
+    const uint8_t* n_receivers;       /* [n]  0 (outlet, sink or invalid), 1, 2  */
+    const float* slope;               /* [n]  steepest facet slope (nodata: none) */
+    const float* bearing;             /* [n]  compass bearing, degrees (nodata: none) */
+    const uint8_t* donor_count;       /* [n]  unique donors, capped at 255        */
+    const int64_t* topological_order; /* [n_valid_cells]                          */
+    int64_t n_cells;
+    int64_t n_valid_cells;
+    int64_t n_levels;                 /* heights in the topological order         */
+} lsdtt_gpu_dinf_view;
+
+int lsdtt_gpu_dinf_create(const lsdtt_gpu_grid* grid, lsdtt_gpu_dinf** out);
+int lsdtt_gpu_dinf_destroy(lsdtt_gpu_dinf* dinf);
+int lsdtt_gpu_dinf_build(lsdtt_gpu_dinf* dinf, const float* z_dev, const uint8_t* mask_dev,
+                         int32_t interior_nodata_is_outlet, void* stream);
+int lsdtt_gpu_dinf_get_view(const lsdtt_gpu_dinf* dinf, lsdtt_gpu_dinf_view* view);
+/* accumulate(cell_weights): weights_dev NULL = cell_size^2 per valid cell. */
+int lsdtt_gpu_dinf_accumulate(lsdtt_gpu_dinf* dinf, const double* weights_dev, double* out_dev, void* stream);
+/* One implicit D-infinity stream-power step of z_dev (the surface the graph
+ * was built on) into z_out_dev. */
+int lsdtt_gpu_dinf_stream_power(lsdtt_gpu_dinf* dinf, const float* z_dev, float K, float m, float n, float dt,
+                                float incision_threshold_area, int32_t divide_area_by_dx, float slope_clamp,
+                                float* z_out_dev, void* stream);
+
 /* ---- stream power ---------------------------------------------------------
  * compute_d8_stream_power_incision (src/cpu/lsdtt_stream_power_cpu.hpp:74-89,
  * .cpp:159-326) on a built engine, moving-average kernel 1 and no width

@@ -571,6 +571,121 @@ class Ensemble:
             pass
 
 
+class DinfView(ctypes.Structure):
+    _fields_ = [("receivers", ctypes.c_void_p), ("weights", ctypes.c_void_p), ("n_receivers", ctypes.c_void_p),
+                ("slope", ctypes.c_void_p), ("bearing", ctypes.c_void_p), ("donor_count", ctypes.c_void_p),
+                ("topological_order", ctypes.c_void_p), ("n_cells", ctypes.c_int64), ("n_valid_cells", ctypes.c_int64),
+                ("n_levels", ctypes.c_int64)]
+
+
+class FlowGraphDinf:
+    """The D-infinity flow graph (lsdtt_flowgraph_cpu with method
+    d_infinity) on the GPU: receivers and weights, facet slopes and
+    bearings, donor counts, the topological order, accumulate() and
+    D-infinity stream power. Accessors return CUDA tensors valid until the
+    next build() or close()."""
+
+    def __init__(self, z, mask, cell_size, boundary_conditions="oooo", *, interior_nodata_is_outlet=True,
+                 no_data_value=-9999.0, stream=None):
+        torch = _torch()
+        L = lib()
+        vp = ctypes.c_void_p
+        for name, args in {"lsdtt_gpu_dinf_create": [ctypes.POINTER(Grid), ctypes.POINTER(vp)],
+                           "lsdtt_gpu_dinf_destroy": [vp],
+                           "lsdtt_gpu_dinf_build": [vp, vp, vp, ctypes.c_int32, vp],
+                           "lsdtt_gpu_dinf_get_view": [vp, ctypes.POINTER(DinfView)],
+                           "lsdtt_gpu_dinf_accumulate": [vp, vp, vp, vp],
+                           "lsdtt_gpu_dinf_stream_power": [vp, vp, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                                           ctypes.c_float, ctypes.c_float, ctypes.c_int32,
+                                                           ctypes.c_float, vp, vp]}.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = ctypes.c_int
+        zt = _dev(z, torch.float32)
+        self.shape = tuple(zt.shape)
+        self.grid = make_grid(zt.shape[0], zt.shape[1], cell_size, boundary_conditions, no_data_value)
+        h = vp()
+        _check(L.lsdtt_gpu_dinf_create(ctypes.byref(self.grid), ctypes.byref(h)))
+        self._h = h
+        self._inio = int(bool(interior_nodata_is_outlet))
+        self.build(zt, mask, stream=stream)
+
+    def build(self, z, mask, stream=None):
+        torch = _torch()
+        self._z = _dev(z, torch.float32)
+        self._m = _dev(mask, torch.uint8)
+        _check(lib().lsdtt_gpu_dinf_build(self._h, ctypes.c_void_p(self._z.data_ptr()),
+                                          ctypes.c_void_p(self._m.data_ptr()), self._inio, _stream(stream)))
+        v = DinfView()
+        _check(lib().lsdtt_gpu_dinf_get_view(self._h, ctypes.byref(v)))
+        self.view = v
+
+    def _arr(self, ptr, count, dtype, shape=None):
+        """Zero-copy CUDA tensor over a graph-owned device array."""
+        torch = _torch()
+        if not ptr or not count:
+            return torch.empty(0 if shape is None else shape, dtype=dtype, device="cuda")
+        t = torch.as_tensor(_DeviceArray(ptr, int(count), dtype), device="cuda")
+        return t if shape is None else t.reshape(shape)
+
+    def receivers(self):
+        torch = _torch()
+        return self._arr(self.view.receivers, 2 * self.view.n_cells, torch.int64, (self.view.n_cells, 2))
+
+    def weights(self):
+        torch = _torch()
+        return self._arr(self.view.weights, 2 * self.view.n_cells, torch.float32, (self.view.n_cells, 2))
+
+    def n_receivers(self):
+        torch = _torch()
+        return self._arr(self.view.n_receivers, self.view.n_cells, torch.uint8)
+
+    def slopes(self):
+        torch = _torch()
+        return self._arr(self.view.slope, self.view.n_cells, torch.float32)
+
+    def bearings(self):
+        torch = _torch()
+        return self._arr(self.view.bearing, self.view.n_cells, torch.float32)
+
+    def donor_count(self):
+        torch = _torch()
+        return self._arr(self.view.donor_count, self.view.n_cells, torch.uint8)
+
+    def topological_order(self):
+        torch = _torch()
+        return self._arr(self.view.topological_order, self.view.n_valid_cells, torch.int64)
+
+    def accumulate(self, weights=None, stream=None):
+        torch = _torch()
+        out = torch.empty(self.view.n_cells, dtype=torch.float64, device="cuda")
+        w = None if weights is None else _dev(weights, torch.float64).reshape(-1)
+        _check(lib().lsdtt_gpu_dinf_accumulate(self._h, ctypes.c_void_p(w.data_ptr() if w is not None else 0),
+                                               ctypes.c_void_p(out.data_ptr()), _stream(stream)))
+        return out
+
+    def stream_power(self, K, m, n, dt, incision_threshold_area=0.0, divide_area_by_dx=True, slope_clamp=1e-5,
+                     stream=None):
+        """compute_dinf_stream_power_incision on the surface the graph was built on."""
+        torch = _torch()
+        out = torch.empty_like(self._z)
+        _check(lib().lsdtt_gpu_dinf_stream_power(self._h, ctypes.c_void_p(self._z.data_ptr()), K, m, n, dt,
+                                                 incision_threshold_area, int(bool(divide_area_by_dx)), slope_clamp,
+                                                 ctypes.c_void_p(out.data_ptr()), _stream(stream)))
+        return out
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().lsdtt_gpu_dinf_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def hillslope_implicit(z, mask, cell_size, boundary_conditions, D, Sc, dt, nonlinear=True, rel_tol=1e-8,
                        max_pcg_iter=4000, residual_tol=1e-12, max_outer=200, is_channel=None, net=None, stream=None):
     """Backward-Euler hillslope step over dt (linear or Roering), the

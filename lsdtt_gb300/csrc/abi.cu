@@ -137,6 +137,7 @@ unsigned long long launches_stream_power();
 unsigned long long launches_unet();
 unsigned long long launches_ensemble();
 unsigned long long launches_queries();
+unsigned long long launches_dinf();
 
 namespace
 {
@@ -173,7 +174,7 @@ unsigned long long lsdtt_gpu_launch_count(void)
 {
     return launches_abi() + launches_d8() + launches_fill() + launches_hillslope() + launches_lem() +
            launches_stack() + launches_stream_power() + launches_unet() +
-           launches_ensemble() + launches_queries();
+           launches_ensemble() + launches_queries() + launches_dinf();
 }
 
 int lsdtt_gpu_profile_enable(int32_t on)

@@ -48,11 +48,15 @@ __device__ __forceinline__ double sp_kam(const SpParams& P, double area_d, float
 // elevation from its own old elevation zo, its receiver's final elevation
 // zr, kam = sp_kam(...) and the step length to the receiver. Returns zo when
 // the node is not eroded.
-__device__ __forceinline__ float sp_solve(const SpParams& P, bool diagonal, double kam, float zo, float zr)
+// tol_dx: the length the elevation tolerance slope_clamp * tol_dx is taken
+// over (the step length to the receiver for D8; the cardinal cell size for
+// D-infinity, stream_power_cpu.cpp:437).
+__device__ __forceinline__ float sp_solve_tol(const SpParams& P, bool diagonal, double kam, float zo, float zr,
+                                              float tol_dx)
 {
     if (zr >= zo) return zo;
     const float dx_eff = diagonal ? P.dx_diag : P.dx;
-    const double tol = __dmul_rn(static_cast<double>(P.slope_clamp), static_cast<double>(dx_eff));
+    const double tol = __dmul_rn(static_cast<double>(P.slope_clamp), static_cast<double>(tol_dx));
     float zn = zo;
     if (P.n_is_one)
     {
@@ -87,6 +91,11 @@ __device__ __forceinline__ float sp_solve(const SpParams& P, bool diagonal, doub
         if (zn < zr) zn = __fadd_rn(zr, __fmul_rn(P.slope_clamp, dx_eff));
     }
     return zn;
+}
+
+__device__ __forceinline__ float sp_solve(const SpParams& P, bool diagonal, double kam, float zo, float zr)
+{
+    return sp_solve_tol(P, diagonal, kam, zo, zr, diagonal ? P.dx_diag : P.dx);
 }
 
 // sp_solve for node `flat` with its own loads and store. Any receiver-

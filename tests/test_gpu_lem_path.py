@@ -184,3 +184,25 @@ def test_hillslope_linear_general_entry_matches_linear_entry(port):
     rel = np.max(np.abs(b.cpu().numpy() - want) / np.maximum(np.abs(want), 1.0))
     assert rel < REL_TOL
     assert np.max(np.abs(a.cpu().numpy() - b.cpu().numpy())) < 1e-4
+
+
+@pytest.mark.parametrize("bc,shape", [("popo", (160, 150)), ("opop", (96, 224)), ("popo", (100, 70))])
+def test_periodic_fill_against_oracle(port, bc, shape):
+    """The periodic fill (fill_pits with a 'p' pair: the priority flood with
+    the seam joined, raster_flow_preprocessing_cpu.cpp:744-757) against the
+    oracle: bit-exact at min_slope 0 on grids whose periodic axis has an odd
+    number of 32-cell tiles (the third tile colour) or a partial last tile;
+    at 1e-4 the differing cells are counted and bounded like the other
+    epsilon fills."""
+    import lsdtt_gb300 as G
+    z = surfaces.add_pits(surfaces.fractal(shape[0], shape[1], 200.0, 17), 40, 17)
+    m = np.ones_like(z, np.uint8)
+    want = port.fill_pits(z, m, 10.0, bc, 0.0)
+    got = G.fill_pits(z, m, 10.0, bc, 0.0).cpu().numpy()
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+    want = port.fill_pits(z, m, 10.0, bc, 1e-4)
+    got = G.fill_pits(z, m, 10.0, bc, 1e-4).cpu().numpy()
+    diff = got.view(np.uint32) != want.view(np.uint32)
+    print(f"periodic fill {bc} {shape}: epsilon 1e-4, {int(diff.sum())} of {int((want != z).sum())} raised cells "
+          f"differ")
+    assert diff.mean() <= FILL_MISMATCH_BOUND["fractal_pits_512"]
