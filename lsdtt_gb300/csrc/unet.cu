@@ -50,21 +50,61 @@ __device__ __forceinline__ float bfr(float v) { return __bfloat162float(__float2
 // ---------------------------------------------------------------------------
 // forward
 // ---------------------------------------------------------------------------
-__global__ void k_sumsq(const float* __restrict__ r, std::int64_t n, double* __restrict__ acc)
+// Grid-wide sums are taken in a fixed order, so that the same inputs give the
+// same bits on every run: each of the kRedBlocks blocks of a reduction covers
+// a fixed grid-strided share of the cells and writes its own partial (warp
+// shuffle tree, then the block's warps in index order); one block then adds
+// the partials in a fixed tree (red_partials).
+constexpr int kRedBlocks = 152 * 4;
+// Pixel shares of one weight-gradient entry (k_conv_bwd_w's grid x).
+constexpr int kWgradBlocks = 64;
+
+// The block's sum of v (all threads take part), valid in thread 0.
+__device__ __forceinline__ double block_sum_ordered(double v)
+{
+    __shared__ double sh_red[32];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    __syncthreads();  // a previous call may still be reading
+    if ((threadIdx.x & 31) == 0) sh_red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double t = 0.0;
+    if (threadIdx.x == 0)
+        for (int k = 0; k < static_cast<int>(blockDim.x >> 5); ++k) t += sh_red[k];
+    return t;
+}
+
+// out[j] = sum over b of part[j * np + b], one block per j, fixed order.
+__global__ void red_partials(const double* __restrict__ part, int np, double* __restrict__ out)
+{
+    LSDTT_COUNT();
+    const double* p = part + static_cast<std::int64_t>(blockIdx.x) * np;
+    double s = 0.0;
+    for (int b = threadIdx.x; b < np; b += blockDim.x) s += p[b];
+    s = block_sum_ordered(s);
+    if (threadIdx.x == 0) out[blockIdx.x] = s;
+}
+
+// part[blockIdx.x] = this block's share of sum r^2
+__global__ void k_sumsq(const float* __restrict__ r, std::int64_t n, double* __restrict__ part)
 {
     LSDTT_COUNT();
     std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     double s = 0.0;
     for (; i < n; i += static_cast<std::int64_t>(gridDim.x) * blockDim.x) s += static_cast<double>(r[i]) * r[i];
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-    if ((threadIdx.x & 31) == 0) atomicAdd(acc, s);
+    s = block_sum_ordered(s);
+    if (threadIdx.x == 0) part[blockIdx.x] = s;
 }
 
-// rms from acc[0] = sum r^2 over n cells, once (FP64 is scarce on this part)
-__global__ void k_rms(std::int64_t n, const double* __restrict__ acc, float* __restrict__ rms_out)
+// rms from the kRedBlocks partials of sum r^2 over n cells, summed in a fixed
+// order (FP64 is scarce on this part: one block)
+__global__ void k_rms(std::int64_t n, const double* __restrict__ part, float* __restrict__ rms_out)
 {
     LSDTT_COUNT();
-    float rms = static_cast<float>(sqrt(acc[0] / static_cast<double>(n)));
+    double s = 0.0;
+    for (int b = threadIdx.x; b < kRedBlocks; b += blockDim.x) s += part[b];
+    s = block_sum_ordered(s);
+    if (threadIdx.x != 0) return;
+    float rms = static_cast<float>(sqrt(s / static_cast<double>(n)));
     if (!(rms > 0.0f)) rms = 1.0f;
     *rms_out = rms;
 }
@@ -1356,8 +1396,9 @@ __global__ void k_conv_out(int H, int W, const __nv_bfloat16* __restrict__ d0, c
 // ---------------------------------------------------------------------------
 // loss and backward (FP32, CUDA cores)
 // ---------------------------------------------------------------------------
+// Per-block partials of sum (y-e)^2 (part[b]) and sum e^2 (part[kRedBlocks + b]).
 __global__ void k_loss_sums(const float* __restrict__ y, const float* __restrict__ e, std::int64_t n,
-                            double* __restrict__ acc)
+                            double* __restrict__ part)
 {
     LSDTT_COUNT();
     std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -1368,15 +1409,12 @@ __global__ void k_loss_sums(const float* __restrict__ y, const float* __restrict
         num += d * d;
         den += static_cast<double>(e[i]) * e[i];
     }
-    for (int o = 16; o > 0; o >>= 1)
+    num = block_sum_ordered(num);
+    den = block_sum_ordered(den);
+    if (threadIdx.x == 0)
     {
-        num += __shfl_down_sync(0xffffffffu, num, o);
-        den += __shfl_down_sync(0xffffffffu, den, o);
-    }
-    if ((threadIdx.x & 31) == 0)
-    {
-        atomicAdd(&acc[0], num);
-        atomicAdd(&acc[1], den);
+        part[blockIdx.x] = num;
+        part[kRedBlocks + blockIdx.x] = den;
     }
 }
 
@@ -1437,35 +1475,39 @@ __global__ void k_conv_bwd_data(int H, int W, int Cin, int Cout, int up, const f
         dx[i] = s;
 }
 
-// Weight/bias gradients of a 3x3 conv: gw[co][tap][ci] += sum_p g[p][co] *
-// X[p + off(tap)][ci], gb[co] += sum_p g[p][co]. One block per (co, tap)
-// pair reduces over a strided pixel range; X is bf16 ([H][W][Cin], or half
-// resolution with `up`).
+// Weight/bias gradients of a 3x3 conv: gw[co][tap][ci] = sum_p g[p][co] *
+// X[p + off(tap)][ci], gb[co] = sum_p g[p][co]. Blocks (x, co * 9 + tap)
+// reduce over the x-th grid-strided share of the pixels and write their
+// partial sums to part[((co * 9 + tap) * (Cin + 1) + c) * gridDim.x + x]
+// (c = Cin: the bias term, tap 4 only); k_conv_bwd_w_sum adds the
+// gridDim.x partials of each entry in index order, so the gradient has the
+// same bits on every run. X is bf16 ([H][W][Cin], or half resolution with
+// `up`).
 __global__ void k_conv_bwd_w(int H, int W, int Cin, int Cout, int up, const float* __restrict__ g,
-                             const __nv_bfloat16* __restrict__ X, float* __restrict__ gw, float* __restrict__ gb)
+                             const __nv_bfloat16* __restrict__ X, float* __restrict__ part)
 {
     LSDTT_COUNT();
     extern __shared__ float red[];  // [Cin + 1][32]
     const int co = blockIdx.y / 9, t = blockIdx.y % 9;
     const int Win = up ? W / 2 : W;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    float part[64 + 1];
-    for (int c = 0; c <= Cin; ++c) part[c] = 0.f;
+    float acc_c[64 + 1];
+    for (int c = 0; c <= Cin; ++c) acc_c[c] = 0.f;
     const std::int64_t npix = static_cast<std::int64_t>(H) * W;
     for (std::int64_t p = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; p < npix;
          p += static_cast<std::int64_t>(gridDim.x) * blockDim.x)
     {
         const float gv = g[p * Cout + co];
         if (gv == 0.f) continue;
-        if (t == 4) part[Cin] += gv;
+        if (t == 4) acc_c[Cin] += gv;
         const int py = static_cast<int>(p / W) + t / 3 - 1, px = static_cast<int>(p % W) + t % 3 - 1;
         if (py < 0 || py >= H || px < 0 || px >= W) continue;
         const __nv_bfloat16* xp = X + (static_cast<std::int64_t>(up ? py >> 1 : py) * Win + (up ? px >> 1 : px)) * Cin;
-        for (int c = 0; c < Cin; ++c) part[c] += gv * __bfloat162float(xp[c]);
+        for (int c = 0; c < Cin; ++c) acc_c[c] += gv * __bfloat162float(xp[c]);
     }
     for (int c = 0; c <= Cin; ++c)
     {
-        float v = part[c];
+        float v = acc_c[c];
         for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
         if (lane == 0) red[c * 32 + warp] = v;
     }
@@ -1474,9 +1516,23 @@ __global__ void k_conv_bwd_w(int H, int W, int Cin, int Cout, int up, const floa
     {
         float v = 0.f;
         for (int k = 0; k < nw; ++k) v += red[threadIdx.x * 32 + k];
-        if (threadIdx.x < Cin) atomicAdd(&gw[(static_cast<std::int64_t>(co) * 9 + t) * Cin + threadIdx.x], v);
-        else if (t == 4) atomicAdd(&gb[co], v);
+        part[(static_cast<std::int64_t>(blockIdx.y) * (Cin + 1) + threadIdx.x) * gridDim.x + blockIdx.x] = v;
     }
+}
+
+// gw / gb from the partials of k_conv_bwd_w (nx per entry), in index order.
+__global__ void k_conv_bwd_w_sum(int Cin, int Cout, int nx, const float* __restrict__ part, float* __restrict__ gw,
+                                 float* __restrict__ gb)
+{
+    LSDTT_COUNT();
+    const std::int64_t j = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (j >= static_cast<std::int64_t>(Cout) * 9 * (Cin + 1)) return;
+    const int y = static_cast<int>(j / (Cin + 1)), c = static_cast<int>(j % (Cin + 1));
+    const float* p = part + j * nx;
+    float v = 0.f;
+    for (int k = 0; k < nx; ++k) v += p[k];
+    if (c < Cin) gw[static_cast<std::int64_t>(y) * Cin + c] = v;
+    else if (y % 9 == 4) gb[y / 9] = v;
 }
 
 // Decoder split: ga = gd * (pre > 0); gskip += gd.
@@ -1577,10 +1633,12 @@ struct lsdtt_gpu_unet
                   *a0 = nullptr, *d0 = nullptr;
     float *y = nullptr, *go = nullptr, *rms = nullptr;
     double* acc = nullptr;
+    double* part = nullptr;  // per-block partial sums of the fixed-order reductions [3][kRedBlocks]
     double* hacc = nullptr;
     // training-only buffers (decoder pre-activations a0..a2 above, FP32
     // backward scratch), allocated by the first gradient evaluation
     float *gA = nullptr, *gB = nullptr, *ge0 = nullptr, *ge1 = nullptr, *ge2 = nullptr, *ge3 = nullptr;
+    float* gwpart = nullptr;  // weight-gradient partials [Cout * 9][Cin + 1][kWgradBlocks] of the widest layer
 };
 
 namespace
@@ -1789,11 +1847,10 @@ void launch_conv_tc(const lsdtt_gpu_unet* U, int l, int H, int W, int up, const 
 cudaError_t unet_forward(lsdtt_gpu_unet* U, const float* r, int H, int W, cudaStream_t st, bool for_training)
 {
     const std::int64_t n = static_cast<std::int64_t>(H) * W;
-    cudaMemsetAsync(U->acc, 0, sizeof(double), st);
     // Algorithmic bytes: r 4 in (twice), x0 2 out per pixel.
     LSDTT_TIMED("unet_prep", 10.0 * static_cast<double>(n), st, ({
-                    k_sumsq<<<152 * 4, 256, 0, st>>>(r, n, U->acc);
-                    k_rms<<<1, 1, 0, st>>>(n, U->acc, U->rms);
+                    k_sumsq<<<kRedBlocks, 256, 0, st>>>(r, n, U->part);
+                    k_rms<<<1, 256, 0, st>>>(n, U->part, U->rms);
                     k_prep<<<grid_blocks(n, 256), 256, 0, st>>>(r, n, U->rms, U->x0);
                 }));
     const float* wr = U->wr;
@@ -1838,16 +1895,18 @@ cudaError_t unet_forward(lsdtt_gpu_unet* U, const float* r, int H, int W, cudaSt
 cudaError_t unet_backward(lsdtt_gpu_unet* U, const float* e, int H, int W, cudaStream_t st)
 {
     const std::int64_t n = static_cast<std::int64_t>(H) * W;
-    cudaMemsetAsync(U->g, 0, sizeof(float) * U->nparam, st);
-    cudaMemsetAsync(U->acc + 1, 0, sizeof(double) * 2, st);
-    k_loss_sums<<<152 * 4, 256, 0, st>>>(U->y, e, n, U->acc + 1);
+    // every weight and bias entry is assigned by k_conv_bwd_w_sum below
+    k_loss_sums<<<kRedBlocks, 256, 0, st>>>(U->y, e, n, U->part + kRedBlocks);
+    red_partials<<<2, 256, 0, st>>>(U->part + kRedBlocks, kRedBlocks, U->acc + 1);
     k_loss_grad<<<grid_blocks(n, 256), 256, 0, st>>>(U->y, e, n, U->acc + 1, U->rms, U->go);
     const float* wr = U->wr;
     auto bw = [&](int l, int h, int w, int up, const float* g, const __nv_bfloat16* X) {
         const int ci = layer_cin(l), co = layer_cout(l);
-        const dim3 grid(64, co * 9);
-        k_conv_bwd_w<<<grid, 256, sizeof(float) * (ci + 1) * 32, st>>>(h, w, ci, co, up, g, X, U->g + U->woff[l],
-                                                                        U->g + U->boff[l]);
+        const dim3 grid(kWgradBlocks, co * 9);
+        k_conv_bwd_w<<<grid, 256, sizeof(float) * (ci + 1) * 32, st>>>(h, w, ci, co, up, g, X, U->gwpart);
+        const std::int64_t entries = static_cast<std::int64_t>(co) * 9 * (ci + 1);
+        k_conv_bwd_w_sum<<<grid_blocks(entries, 256), 256, 0, st>>>(ci, co, kWgradBlocks, U->gwpart,
+                                                                     U->g + U->woff[l], U->g + U->boff[l]);
     };
     // out layer (16 -> 1): input d0 at H x W
     bw(7, H, W, 0, U->go, U->d0);
@@ -1983,6 +2042,7 @@ int lsdtt_gpu_unet_create(int32_t max_rows, int32_t max_cols, uint64_t seed, lsd
     if (e == cudaSuccess) e = ualloc(&U->go, px0);
     if (e == cudaSuccess) e = ualloc(&U->rms, 1);
     if (e == cudaSuccess) e = ualloc(&U->acc, 4);
+    if (e == cudaSuccess) e = ualloc(&U->part, 3 * kRedBlocks);
     if (e == cudaSuccess) e = ualloc(&U->d_err, 1);
     if (e == cudaSuccess) e = cudaMemset(U->d_err, 0, sizeof(unsigned));
     if (e == cudaSuccess) e = cudaMallocHost(reinterpret_cast<void**>(&U->hacc), sizeof(double) * 4);
@@ -2011,8 +2071,8 @@ int lsdtt_gpu_unet_destroy(lsdtt_gpu_unet* U)
 {
     if (!U) return LSDTT_GPU_OK;
     void* ptrs[] = {U->w, U->wr, U->wb, U->g, U->m, U->v, U->x0, U->e0, U->a0, U->d0, U->p0, U->e1, U->a1, U->d1, U->p1,
-                    U->e2, U->a2, U->d2, U->p2, U->e3, U->y, U->go, U->rms, U->acc, U->gA, U->gB, U->ge0, U->ge1,
-                    U->ge2, U->ge3, U->d_err};
+                    U->e2, U->a2, U->d2, U->p2, U->e3, U->y, U->go, U->rms, U->acc, U->part, U->gA, U->gB, U->ge0,
+                    U->ge1, U->ge2, U->ge3, U->gwpart, U->d_err};
     for (void* p : ptrs) cudaFree(p);
     cudaFreeHost(U->hacc);
     delete U;
@@ -2092,12 +2152,15 @@ int lsdtt_gpu_unet_loss_grad(lsdtt_gpu_unet* U, const float* r_dev, const float*
         if (e == cudaSuccess) e = ualloc(&U->ge1, level_px(U, 1) * 32);
         if (e == cudaSuccess) e = ualloc(&U->ge2, level_px(U, 2) * 64);
         if (e == cudaSuccess) e = ualloc(&U->ge3, level_px(U, 3) * 64);
+        // widest weight-gradient reduction: Cout 64 x 9 taps x (Cin 64 + bias)
+        if (e == cudaSuccess) e = ualloc(&U->gwpart, static_cast<std::size_t>(64) * 9 * 65 * kWgradBlocks);
         if (e != cudaSuccess)
         {
-            void* bufs[] = {U->a0, U->a1, U->a2, U->gA, U->gB, U->ge0, U->ge1, U->ge2, U->ge3};
+            void* bufs[] = {U->a0, U->a1, U->a2, U->gA, U->gB, U->ge0, U->ge1, U->ge2, U->ge3, U->gwpart};
             for (void* b : bufs) cudaFree(b);
             U->a0 = U->a1 = U->a2 = nullptr;
             U->gA = U->gB = U->ge0 = U->ge1 = U->ge2 = U->ge3 = nullptr;
+            U->gwpart = nullptr;
             return cuda_fail(e, "lsdtt_gpu_unet_loss_grad");
         }
     }

@@ -1,9 +1,10 @@
 """The routing path at its workload's full size: an 8192 x 8192 fractal
 (k^-2 spectrum, 1000 m relief) with 100,000 pits, dx = 10 m, epsilon 1e-4,
-open edges. The oracle is too slow to run inside a test at this size, so the
-outputs are checked through the size-independent properties of
-tests/routing_props.py (which the oracle's own outputs satisfy), and the
-host-buffer C-ABI route is required to give the device path's bits."""
+open edges. The outputs are checked through the size-independent properties
+of tests/routing_props.py (which the oracle's own outputs satisfy), the
+host-buffer C-ABI route is required to give the device path's bits, and
+the epsilon-0 fill and every D8 output are compared bit for bit with the
+oracle (about a minute of CPU time at this size)."""
 import ctypes
 
 import numpy as np
@@ -55,3 +56,33 @@ def test_routing_full_size_properties(surface):
     assert np.array_equal(rec, rec_d)
     assert np.array_equal(topo, topo_d)
     assert np.array_equal(cnt.astype(np.int64), size_d.astype(np.int64))
+
+
+def test_routing_full_size_bitwise_against_oracle(surface, port):
+    """The same 8192 x 8192 workload compared bit for bit with the oracle:
+    the epsilon-0 fill, and every D8 output (receivers, directions, donor
+    counts, outlets, Kahn order, s-vector, starts, contributing counts,
+    drainage area) on the oracle's own epsilon fill, so that the fill's
+    order difference (row a1) does not enter the routing comparison."""
+    import lsdtt_gb300 as G
+    z, m = surface
+    want0 = port.fill_pits(z, m, CELL, "oooo", 0.0)
+    got0 = G.fill_pits(z, m, CELL, "oooo", 0.0).cpu().numpy()
+    assert np.array_equal(got0.view(np.uint32), want0.view(np.uint32))
+    del want0, got0
+    f = port.fill_pits(z, m, CELL, "oooo", 1e-4)
+    want = port.flowinfo(f, m, CELL, "oooo", allow_pits_as_outlets=True)
+    fi = G.FlowInfo(f, m, CELL, "oooo", allow_pits_as_outlets=True)
+    try:
+        host = lambda t: t.cpu().numpy()  # noqa: E731
+        assert np.array_equal(host(fi.receiver()), want["receiver"])
+        assert np.array_equal(host(fi.direction()), want["direction"])
+        assert np.array_equal(host(fi.donor_count()), want["donors"])
+        assert np.array_equal(host(fi.outlets()), want["outlets"])
+        assert np.array_equal(host(fi.topological_order()), want["topo"])
+        assert np.array_equal(host(fi.s_vector()), want["s_vector"])
+        assert np.array_equal(host(fi.s_vector_start()), want["sv_start"])
+        assert np.array_equal(host(fi.s_vector_size()).astype(np.uint64), want["sv_size"])
+        assert np.array_equal(host(fi.accumulate()).view(np.uint64), want["accum"].view(np.uint64))
+    finally:
+        fi.close()

@@ -179,6 +179,24 @@ def test_training_lowers_loss():
     assert after < 0.5 * first
 
 
+def test_training_is_reproducible():
+    """Every grid-wide sum of the loss and the gradients is taken in a fixed
+    order (per-block partials, then an ordered reduction), so two trainings
+    from the same seed on the same pairs give the same bits."""
+    import lsdtt_gb300 as G
+    r, e = _pairs(G, [31, 32], 128, False, 30.0, per=4)
+    nets = [G.UNet(128, 128, seed=5) for _ in range(2)]
+    g0 = [net.loss_grad(r[0], e[0])[1] for net in nets]
+    assert np.array_equal(g0[0].view(np.uint32), g0[1].view(np.uint32))
+    losses = [_train(G, net, r, e, 60, seed=1) for net in nets]
+    assert losses[0] == losses[1]
+    p = [net.get_params() for net in nets]
+    assert np.array_equal(p[0].view(np.uint32), p[1].view(np.uint32))
+    # and the same network evaluated twice
+    a, b = nets[0].loss_grad(r[1], e[1]), nets[0].loss_grad(r[1], e[1])
+    assert a[0] == b[0] and np.array_equal(a[1].view(np.uint32), b[1].view(np.uint32))
+
+
 def test_sgd_step_moves_against_gradient():
     import lsdtt_gb300 as G
     r, e = _pairs(G, [21], 32, False, 30.0, per=2)
