@@ -44,6 +44,7 @@
 
 #include "engine.cuh"
 #include "d8_cell.cuh"
+#include "fill_exact.cuh"
 #include "fill_tile.cuh"
 #include "hs_stencil.cuh"
 #include "lem_cell.cuh"
@@ -73,8 +74,9 @@ struct EnsParams
 
 // Flags: [0] fill changed in the last pass, [1] fill overflow, [2] depth
 // overflow, [3] PCG overflow, [4] PCG not converged within max_iter,
-// [5] active PCG members (eager loop), [6] fill did not converge (eager).
-constexpr int kFlags = 8;
+// [5] active PCG members (eager loop), [6] fill did not converge (eager),
+// [7] stream-power sweep wait limit, [8] a fill window replay failed.
+constexpr int kFlags = 9;
 
 __device__ __forceinline__ int member_of(const Packed& P, std::int64_t i)
 {
@@ -198,7 +200,8 @@ __global__ void ens_fill_active(Packed P, const EnsParams* __restrict__ prm,
     if (lane == 0 && cells) atomicAdd(&cnt[kFillColours], static_cast<unsigned long long>(cells));
 }
 
-// Fill relaxation over one colour's listed active tiles: a persistent grid,
+// Fill relaxation over one colour's listed active tiles (with eps0 at raise
+// step 0: the epsilon-0 fill): a persistent grid,
 // block w relaxes tiles w, w + grid, ... of the list (fill_relax_tile with its gate
 // skipped: a pass over every tile spent ~0.2 ms only on inactive tiles
 // reading their neighbours' flags and leaving).
@@ -210,7 +213,7 @@ __global__ void __launch_bounds__(256) ens_fill_relax_list(Packed P, const EnsPa
                                                            const std::uint8_t* __restrict__ din,
                                                            std::uint8_t* __restrict__ dout,
                                                            const std::int32_t* __restrict__ list,
-                                                           const unsigned long long* __restrict__ count)
+                                                           const unsigned long long* __restrict__ count, int eps0)
 {
     LSDTT_COUNT();
     const std::int64_t n = static_cast<std::int64_t>(*count);
@@ -221,7 +224,7 @@ __global__ void __launch_bounds__(256) ens_fill_relax_list(Packed P, const EnsPa
         const PackedMember& M = P.m[m];
         const EnsParams& q = prm[m];
         const int local = t - M.tile_base;
-        fill_relax_tile(M.nr, M.nc, q.per_ns, q.per_ew, q.L, q.Ld, q.fill_eps, z + M.base, kind + M.base,
+        fill_relax_tile(M.nr, M.nc, q.per_ns, q.per_ew, q.L, q.Ld, eps0 ? 0.0f : q.fill_eps, z + M.base, kind + M.base,
                         F + M.base, changed, din + M.tile_base, dout + M.tile_base, local % M.ntx, local / M.ntx,
                         M.ntx, M.nty, false);
         __syncthreads();  // the tile's shared arrays are staged again for the next tile
@@ -242,6 +245,12 @@ __global__ void ens_fill_while(const int* __restrict__ changed, int* __restrict_
 }
 
 __global__ void ens_flag_copy(const int* __restrict__ src, int* __restrict__ dst)
+{
+    LSDTT_COUNT();
+    if (*src) *dst = 1;
+}
+
+__global__ void ens_flag_copy_u(const unsigned* __restrict__ src, int* __restrict__ dst)
 {
     LSDTT_COUNT();
     if (*src) *dst = 1;
@@ -1537,6 +1546,16 @@ struct lsdtt_gpu_ensemble
     Packed P{};
     // state and stage buffers
     float *z = nullptr, *zf = nullptr, *zsp = nullptr, *zpre = nullptr;
+    // The epsilon fill in the reference's order (fill_exact.cuh): the
+    // epsilon-0 fill, the member table and the buffers of the replay.
+    float* zf0 = nullptr;
+    ExMember* d_exm = nullptr;
+    char* exbuf = nullptr;
+    Scratch exws{};
+    ExBuffers exB{};
+    int ex_mbits = 0;
+    bool ex_any = false;  // some member fills with min_slope > 0
+    int sms = 152;
     std::uint8_t *mask = nullptr, *kind = nullptr, *bflag = nullptr, *dirty = nullptr, *oflag = nullptr;
     std::int32_t* flist = nullptr;           // [kFillColours][T] active fill tiles of the current pass
     unsigned long long* fcnt = nullptr;      // [kFillColours + 1] their counts by colour, then their cells
@@ -1629,7 +1648,7 @@ void free_ensemble(lsdtt_gpu_ensemble* E)
     if (E->graph) cudaGraphDestroy(E->graph);
     void* bufs[] = {E->d_pm, E->d_prm, E->blk_member, E->tile_member, E->strip_member, E->undecided, E->bar, E->loopc, E->pcg_scal, E->morder, E->mstart, E->mmax, E->perm, E->z, E->zf, E->zsp, E->zpre, E->kind, E->bflag, E->dirty, E->oflag, E->pos, E->nd, E->area, E->order, E->lstart, E->lcount,
                     E->lfill, E->maxd, E->dof, E->invd, E->b, E->x, E->r, E->p, E->p2, E->zz, E->Ap, E->hs_bb, E->hs_acc,
-                    E->done, E->iters, E->stats_acc, E->part, E->kam_tab, E->flags, E->zg, E->dfc, E->flist, E->fcnt, E->glist, E->grp, E->perm_cap};
+                    E->done, E->iters, E->stats_acc, E->part, E->kam_tab, E->flags, E->zg, E->dfc, E->flist, E->fcnt, E->glist, E->grp, E->perm_cap, E->zf0, E->d_exm, E->exbuf};
     for (void* q : bufs) cudaFree(q);
     void* hb[] = {E->h_stats, E->h_flags, E->h_iters, E->h_maxd, E->h_err, E->h_fcnt};
     for (void* q : hb) cudaFreeHost(q);
@@ -1817,93 +1836,113 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
     cudaError_t e = cudaSuccess;
     cudaMemcpyAsync(E->zpre, E->z, sizeof(float) * N, cudaMemcpyDeviceToDevice, st);
     cudaMemsetAsync(E->flags, 0, sizeof(int) * kFlags, st);
-    // 0. fill
+    // 0. fill: the value-ordered relaxation (the fill itself where min_slope
+    // is 0; the estimate otherwise), then, for members with min_slope > 0,
+    // the epsilon-0 relaxation and the fill in the reference's order
     cudaMemsetAsync(E->nd, 0, sizeof(int) * M, st);
     LSDTT_TIMED("ens_interior", 0.0, st, (ens_interior<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->z, E->mask, E->nd)));
-    LSDTT_TIMED("ens_fill_init", 0.0, st,
-                (ens_fill_init<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->z, E->mask, E->nd, E->zf, E->kind)));
-    LSDTT_TIMED("ens_dirty_init", 0.0, st,
-                (ens_dirty_init<<<grid_blocks(E->T, 256), 256, 0, st>>>(E->T, E->tile_member, E->d_prm, E->dirty,
-                                                                        E->dirty + E->T)));
     const dim3 fblock(32, 8);
     const double cells = static_cast<double>(E->member_cells);
     const unsigned tb = static_cast<unsigned>((E->T + 255) / 256);
-    // One pass: list the active tiles, then relax only those. In eager
-    // steps the listed cells are read back, so the pass's algorithmic bytes
-    // (z 4 + mask 1 in, filled value 4 out per cell of an active tile) are
-    // those of the work done.
-    auto pass_on = [&](int pass, cudaStream_t s, bool timed) -> cudaError_t {
-        const std::uint8_t* din = E->dirty + (pass & 1) * E->T;
-        std::uint8_t* dout = E->dirty + ((pass + 1) & 1) * E->T;
-        cudaMemsetAsync(E->fcnt, 0, sizeof(unsigned long long) * (kFillColours + 1), s);
-        if (timed)
-            LSDTT_TIMED("ens_fill_active", 0.0, s,
-                        (ens_fill_active<<<tb, 256, 0, s>>>(E->P, E->d_prm, E->tile_member, E->T, din, dout, E->flist,
-                                                            E->fcnt)));
-        else
-            ens_fill_active<<<tb, 256, 0, s>>>(E->P, E->d_prm, E->tile_member, E->T, din, dout, E->flist, E->fcnt);
-        double bytes = 9.0 * cells;
-        if (timed && profiling_enabled())
-        {
-            cudaMemcpyAsync(E->h_fcnt, E->fcnt, sizeof(unsigned long long) * (kFillColours + 1),
-                            cudaMemcpyDeviceToHost, s);
-            const cudaError_t pe = cudaStreamSynchronize(s);
-            if (pe != cudaSuccess) return pe;
-            bytes = 9.0 * static_cast<double>(E->h_fcnt[kFillColours]);
-        }
-        // the colours in turn: a tile reads its neighbours settled
-        LSDTT_TIMED("ens_fill_relax", bytes, s, ({
-                        for (int c = 0; c < kFillColours; ++c)
-                        {
-                            if (!((E->fill_colours >> c) & 1u)) continue;
-                            ens_fill_relax_list<<<E->fill_grid, fblock, 0, s>>>(
-                                E->P, E->d_prm, E->tile_member, E->z, E->kind, E->zf, E->flags, din, dout,
-                                E->flist + static_cast<std::int64_t>(c) * E->T, E->fcnt + c);
-                        }
-                    }));
-        return cudaSuccess;
-    };
-    auto relax = [&](int pass) { return pass_on(pass, st, true); };
-    int passes = 0;
-    if (eager)
-    {
-        for (;;)
-        {
-            cudaMemsetAsync(E->flags, 0, sizeof(int), st);
-            for (int k = 0; k < 4 && e == cudaSuccess; ++k, ++passes) e = relax(passes);
-            if (e != cudaSuccess) return e;
-            cudaMemcpyAsync(E->h_flags, E->flags, sizeof(int), cudaMemcpyDeviceToHost, st);
-            e = cudaStreamSynchronize(st);
-            if (e != cudaSuccess) return e;
-            if (E->h_flags[0] == 0) break;
-            if (passes > E->max_pass_all) return cudaErrorLaunchTimeout;
-        }
-        rec->fill_passes = passes;
-    }
-    else if (E->use_while)
-    {
-        // Device-side loop: pairs of passes until the second of a pair
-        // changes nothing (a fixed point), at most max_pass_all passes.
-        cudaMemsetAsync(E->loopc, 0, sizeof(int), st);
-        const int max_pairs = (E->max_pass_all + 1) / 2;
-        e = capture_while(st, E->own2, [&](cudaStream_t s2, cudaGraphConditionalHandle h) {
-            for (int k = 0; k < 2; ++k)
+    auto relax_all = [&](float* F, int eps0, const char* name) -> cudaError_t {
+        LSDTT_TIMED("ens_fill_init", 0.0, st,
+                    (ens_fill_init<<<nb, 256, 0, st>>>(E->P, E->d_prm, E->z, E->mask, E->nd, F, E->kind)));
+        LSDTT_TIMED("ens_dirty_init", 0.0, st,
+                    (ens_dirty_init<<<grid_blocks(E->T, 256), 256, 0, st>>>(E->T, E->tile_member, E->d_prm, E->dirty,
+                                                                            E->dirty + E->T)));
+        // One pass: list the active tiles, then relax only those. In eager
+        // steps the listed cells are read back, so the pass's algorithmic
+        // bytes (z 4 + mask 1 in, filled value 4 out per cell of an active
+        // tile) are those of the work done.
+        auto pass_on = [&](int pass, cudaStream_t s, bool timed) -> cudaError_t {
+            const std::uint8_t* din = E->dirty + (pass & 1) * E->T;
+            std::uint8_t* dout = E->dirty + ((pass + 1) & 1) * E->T;
+            cudaMemsetAsync(E->fcnt, 0, sizeof(unsigned long long) * (kFillColours + 1), s);
+            if (timed)
+                LSDTT_TIMED("ens_fill_active", 0.0, s,
+                            (ens_fill_active<<<tb, 256, 0, s>>>(E->P, E->d_prm, E->tile_member, E->T, din, dout,
+                                                                E->flist, E->fcnt)));
+            else
+                ens_fill_active<<<tb, 256, 0, s>>>(E->P, E->d_prm, E->tile_member, E->T, din, dout, E->flist,
+                                                   E->fcnt);
+            double bytes = 9.0 * cells;
+            if (timed && profiling_enabled())
             {
-                if (k == 1) cudaMemsetAsync(E->flags, 0, sizeof(int), s2);
-                pass_on(k, s2, false);
+                cudaMemcpyAsync(E->h_fcnt, E->fcnt, sizeof(unsigned long long) * (kFillColours + 1),
+                                cudaMemcpyDeviceToHost, s);
+                const cudaError_t pe = cudaStreamSynchronize(s);
+                if (pe != cudaSuccess) return pe;
+                bytes = 9.0 * static_cast<double>(E->h_fcnt[kFillColours]);
             }
-            ens_fill_while<<<1, 1, 0, s2>>>(E->flags, E->loopc, max_pairs, E->flags + 1, h);
-        });
-        if (e != cudaSuccess) return e;
-    }
-    else
-    {
-        for (int k = 0; k < E->fill_cap; ++k)
+            // the colours in turn: a tile reads its neighbours settled
+            LSDTT_TIMED(name, bytes, s, ({
+                            for (int c = 0; c < kFillColours; ++c)
+                            {
+                                if (!((E->fill_colours >> c) & 1u)) continue;
+                                ens_fill_relax_list<<<E->fill_grid, fblock, 0, s>>>(
+                                    E->P, E->d_prm, E->tile_member, E->z, E->kind, F, E->flags, din, dout,
+                                    E->flist + static_cast<std::int64_t>(c) * E->T, E->fcnt + c, eps0);
+                            }
+                        }));
+            return cudaSuccess;
+        };
+        cudaError_t re = cudaSuccess;
+        int passes = 0;
+        if (eager)
         {
-            if (k == E->fill_cap - 1) cudaMemsetAsync(E->flags, 0, sizeof(int), st);
-            pass_on(k, st, false);
+            for (;;)
+            {
+                cudaMemsetAsync(E->flags, 0, sizeof(int), st);
+                for (int k = 0; k < 4 && re == cudaSuccess; ++k, ++passes) re = pass_on(passes, st, true);
+                if (re != cudaSuccess) return re;
+                cudaMemcpyAsync(E->h_flags, E->flags, sizeof(int), cudaMemcpyDeviceToHost, st);
+                re = cudaStreamSynchronize(st);
+                if (re != cudaSuccess) return re;
+                if (E->h_flags[0] == 0) break;
+                if (passes > E->max_pass_all) return cudaErrorLaunchTimeout;
+            }
+            rec->fill_passes = std::max(rec->fill_passes, passes);
         }
-        ens_flag_copy<<<1, 1, 0, st>>>(E->flags, E->flags + 1);
+        else if (E->use_while)
+        {
+            // Device-side loop: pairs of passes until the second of a pair
+            // changes nothing (a fixed point), at most max_pass_all passes.
+            cudaMemsetAsync(E->loopc, 0, sizeof(int), st);
+            const int max_pairs = (E->max_pass_all + 1) / 2;
+            re = capture_while(st, E->own2, [&](cudaStream_t s2, cudaGraphConditionalHandle h) {
+                for (int k = 0; k < 2; ++k)
+                {
+                    if (k == 1) cudaMemsetAsync(E->flags, 0, sizeof(int), s2);
+                    pass_on(k, s2, false);
+                }
+                ens_fill_while<<<1, 1, 0, s2>>>(E->flags, E->loopc, max_pairs, E->flags + 1, h);
+            });
+        }
+        else
+        {
+            for (int k = 0; k < E->fill_cap; ++k)
+            {
+                if (k == E->fill_cap - 1) cudaMemsetAsync(E->flags, 0, sizeof(int), st);
+                pass_on(k, st, false);
+            }
+            ens_flag_copy<<<1, 1, 0, st>>>(E->flags, E->flags + 1);
+        }
+        return re;
+    };
+    if (eager) rec->fill_passes = 0;
+    e = relax_all(E->zf, 0, "ens_fill_relax");
+    if (e != cudaSuccess) return e;
+    if (E->ex_any)
+    {
+        e = relax_all(E->zf0, 1, "ens_fill_relax_eps0");
+        if (e != cudaSuccess) return e;
+        // Algorithmic bytes: z, F0, F1 4 each in, F 4 out per cell (the
+        // sorts and replays are latency-bound and not counted).
+        LSDTT_TIMED("ens_fill_exact", 16.0 * cells, st,
+                    (e = ex_run(E->d_exm, E->blk_member, N, M, E->ex_mbits, E->z, E->kind, E->zf0, E->zf, E->exB,
+                                E->exws, E->sms, st)));
+        if (e != cudaSuccess) return e;
+        ens_flag_copy_u<<<1, 1, 0, st>>>(E->exB.u + 5, E->flags + 8);
     }
     // 1. D8 receivers, outlets, s-vector (contributing counts, depth)
     lsdtt_gpu_flow* f = E->f;
@@ -2620,6 +2659,50 @@ int lsdtt_gpu_ensemble_create(const lsdtt_gpu_member* members, int32_t n_members
     if (e == cudaSuccess) e = cudaMallocHost(&E->h_maxd, sizeof(std::uint32_t));
     if (e == cudaSuccess) e = cudaMallocHost(&E->h_err, sizeof(unsigned long long) * 4);
     if (e == cudaSuccess) e = cudaMallocHost(&E->h_fcnt, sizeof(unsigned long long) * (kFillColours + 1));
+    // The epsilon fill in the reference's order: member table, FIFO rings
+    // of the global-memory replay (a power of two of entries per member)
+    // and the replay's buffers.
+    std::vector<ExMember> exm(static_cast<std::size_t>(n_members));
+    {
+        std::int64_t fifo_total = 0;
+        for (int k = 0; k < n_members; ++k)
+        {
+            const PackedMember& Pm = E->pm[static_cast<std::size_t>(k)];
+            const EnsParams& q = E->prm_h[static_cast<std::size_t>(k)];
+            ExMember& x = exm[static_cast<std::size_t>(k)];
+            const std::int64_t cells_k = static_cast<std::int64_t>(Pm.nr) * Pm.nc;
+            std::int64_t cap = 2;
+            while (cap < cells_k) cap <<= 1;
+            x.base = Pm.base;
+            x.fifo_base = fifo_total;
+            x.fifo_cap = static_cast<std::uint32_t>(cap);
+            x.nr = Pm.nr;
+            x.nc = Pm.nc;
+            x.L = q.L;
+            x.Ld = q.Ld;
+            x.eps = q.fill_eps;
+            x.nodata = static_cast<float>(Pm.nodata);
+            x.per_ns = q.per_ns;
+            x.per_ew = q.per_ew;
+            x.on = (q.fill_on && q.fill_eps > 0.0f) ? 1 : 0;
+            if (x.on) E->ex_any = true;
+            fifo_total += cap;
+        }
+        while ((1 << E->ex_mbits) < n_members) ++E->ex_mbits;
+        if (E->ex_any)
+        {
+            alloc(&E->zf0, n);
+            alloc(&E->d_exm, static_cast<std::size_t>(n_members));
+            const std::size_t exb = ex_bytes(N, n_members, fifo_total);
+            alloc(&E->exbuf, exb);
+            if (e == cudaSuccess)
+            {
+                E->exws = Scratch{E->exbuf, exb, 0};
+                if (!ex_carve(E->exws, N, n_members, fifo_total, E->exB)) e = cudaErrorMemoryAllocation;
+            }
+            if (e == cudaSuccess) e = ex_setup();
+        }
+    }
     {
         int dev = 0, sms = 0;
         cudaGetDevice(&dev);
@@ -2636,6 +2719,7 @@ int lsdtt_gpu_ensemble_create(const lsdtt_gpu_member* members, int32_t n_members
             per_sm = 8;
         }
         E->fill_grid = static_cast<unsigned>(std::max(1, sms) * per_sm);
+        E->sms = std::max(1, sms);
         for (const PackedMember& Pm : E->pm)
         {
             const lsdtt_gpu_grid& g = E->members[&Pm - E->pm.data()].grid;
@@ -2649,6 +2733,7 @@ int lsdtt_gpu_ensemble_create(const lsdtt_gpu_member* members, int32_t n_members
         return cuda_fail(e, who);
     }
     cudaMemcpyAsync(E->d_pm, E->pm.data(), sizeof(PackedMember) * n_members, cudaMemcpyHostToDevice, st);
+    if (E->d_exm) cudaMemcpyAsync(E->d_exm, exm.data(), sizeof(ExMember) * n_members, cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(E->d_prm, E->prm_h.data(), sizeof(EnsParams) * n_members, cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(E->blk_member, blk.data(), sizeof(std::uint16_t) * blk.size(), cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(E->tile_member, tm.data(), sizeof(std::uint16_t) * tm.size(), cudaMemcpyHostToDevice, st);
@@ -2832,6 +2917,8 @@ int lsdtt_gpu_ensemble_step(lsdtt_gpu_ensemble* E, int32_t n_steps, lsdtt_gpu_le
         }
         if (E->h_flags[7])
             return fail(LSDTT_GPU_ETIMEOUT, std::string(who) + ": the stream-power sweep hit its wait limit");
+        if (E->h_flags[8])
+            return fail(LSDTT_GPU_EOVERFLOW, std::string(who) + ": a fill window replay outgrew its arrays");
         if ((E->h_err[0] & 0xffffffffull) != 0)
             return fail(LSDTT_GPU_ECYCLIC, std::string(who) + ": the receiver graph of a member has a cycle");
         if (E->h_flags[4])

@@ -9,24 +9,28 @@
 //     max(zeta + min_slope * d, nextafter(zeta, +inf)),   d = L or L*sqrt2 (float)
 // and otherwise keeps its elevation.
 //
-// This kernel computes the value-ordered form of that rule: every cell's
-// "discoverer" is its neighbour of lowest filled value (first in direction
-// order N, NE, ..., NW on ties), which is the fixed point of
+// Two parts. The relaxation computes the value-ordered form of that rule:
+// every cell's "discoverer" is its neighbour of lowest filled value (first
+// in direction order N, NE, ..., NW on ties), the fixed point of
 //     F(c) = z(c)                        if z(c) > m(c)
 //          = raise(m(c), dir of m(c))    otherwise,   m(c) = min_nb F(nb)
-// with seeds fixed at their elevation. It is solved by tile-local relaxation
-// in shared memory (each CTA iterates its kT x kT tile to local convergence),
-// repeated until no tile changes. The set of raised cells and every cell
-// outside a depression match the reference exactly; inside large flats the
-// reference's FIFO processes cells in breadth-first push order rather than
-// value order, so some raised values differ in the last few epsilon steps.
-// The parity tests count those cells per surface.
+// with seeds fixed at their elevation, solved by tile-local relaxation in
+// shared memory (each CTA iterates its kT x kT tile to local convergence),
+// repeated until no tile changes. With min_slope = 0 that fixed point is the
+// reference's result (the epsilon-0 fill does not depend on the order). With
+// min_slope > 0 the reference's FIFO takes raised cells in push order, not
+// value order, so the fill is then rebuilt in the reference's own order by
+// value windows (fill_window.cuh, fill_exact.cuh): the epsilon-0 fill fixes
+// where every window starts and what it sees, the epsilon relaxation only
+// estimates which window starts are worth replaying.
 
+#include <algorithm>
 #include <cmath>
 #include <mutex>
 #include <string>
 
 #include "engine.cuh"
+#include "fill_exact.cuh"
 #include "fill_tile.cuh"
 
 namespace lsdtt_gb300
@@ -147,67 +151,23 @@ __global__ void __launch_bounds__(256) fill_relax_list(int nr, int nc, bool per_
 
 using namespace lsdtt_gb300;
 
-extern "C" int lsdtt_gpu_fill_pits(const lsdtt_gpu_grid* grid, const float* z_dev, const std::uint8_t* mask_dev,
-                                   float min_slope, float* out_dev, void* stream)
+namespace
 {
-    if (!grid || !z_dev || !mask_dev || !out_dev) return fail(LSDTT_GPU_EINVAL, "lsdtt_gpu_fill_pits: null argument");
-    int ndev = 0;
-    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
-        return fail(LSDTT_GPU_ENODEV, "lsdtt_gpu_fill_pits: no CUDA device");
-    if (!(grid->n_rows > 0 && grid->n_cols > 0 && grid->cell_size > 0.0))
-        return fail(LSDTT_GPU_EINVAL, "lsdtt::fill_pits: invalid raster metadata");
-    auto is_p = [&](int i) { return grid->boundary_conditions[i] == 'p' || grid->boundary_conditions[i] == 'P'; };
-    const bool per_ns = is_p(0), per_ew = is_p(1);
-    const std::string bc(grid->boundary_conditions, 4);
-    if (per_ns != is_p(2))
-        return fail(LSDTT_GPU_EINVAL,
-                    "lsdtt::fill_pits: north and south periodic flags must match (boundary_conditions '" + bc + "')");
-    if (per_ew != is_p(3))
-        return fail(LSDTT_GPU_EINVAL,
-                    "lsdtt::fill_pits: east and west periodic flags must match (boundary_conditions '" + bc + "')");
-    if (per_ns && per_ew)
-        return fail(LSDTT_GPU_EINVAL, "lsdtt::fill_pits: boundary_conditions '" + bc +
-                                          "' is periodic in BOTH directions, so the grid has no drainage exit at all "
-                                          "and every cell would fill to the global maximum. Leave one pair open.");
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
-    const int nr = grid->n_rows, nc = grid->n_cols;
+
+// The relaxation from fill_init to its fixed point with raise step `eps`
+// (0: the epsilon-0 fill) into F. Work buffers are the caller's.
+cudaError_t relax_fill(int nr, int nc, bool per_ns, bool per_ew, float L, float Ld, float eps, const float* z_dev,
+                       const std::uint8_t* mask_dev, double nodata, float* F, std::uint8_t* kind, int* flags,
+                       int* hflag, std::uint8_t* dirty, std::int32_t* list, unsigned long long* cnt,
+                       unsigned long long* hcnt, cudaStream_t st, bool* converged)
+{
+    *converged = false;
     const std::int64_t n = static_cast<std::int64_t>(nr) * nc;
-    std::uint8_t* kind = nullptr;
-    int* flags = nullptr;   // [0] interior nodata, [1] changed
-    int* hflag = nullptr;
-    std::uint8_t* dirty = nullptr;  // two per-tile activity planes
-    std::int32_t* list = nullptr;   // active tiles of the current pass, by colour
-    unsigned long long* cnt = nullptr;  // their count and cells
-    unsigned long long* hcnt = nullptr;
     const std::int64_t ntiles = static_cast<std::int64_t>((nc + kT - 1) / kT) * ((nr + kT - 1) / kT);
-    cudaError_t e = cudaMallocAsync(&kind, static_cast<std::size_t>(n), st);
-    if (e == cudaSuccess) e = cudaMallocAsync(&dirty, static_cast<std::size_t>(2 * ntiles), st);
-    if (e == cudaSuccess)
-        e = cudaMallocAsync(&list, sizeof(std::int32_t) * kFillColours * static_cast<std::size_t>(ntiles), st);
-    if (e == cudaSuccess) e = cudaMallocAsync(&cnt, sizeof(unsigned long long) * (kFillColours + 1), st);
-    if (e == cudaSuccess) e = cudaMallocAsync(&flags, sizeof(int) * 2, st);
-    if (e == cudaSuccess) e = cudaMallocHost(&hflag, sizeof(int));
-    if (e == cudaSuccess) e = cudaMallocHost(&hcnt, sizeof(unsigned long long) * (kFillColours + 1));
-    if (e != cudaSuccess)
-    {
-        // whatever was allocated before the failure (cudaFree* of null is a no-op)
-        cudaFreeAsync(kind, st);
-        cudaFreeAsync(dirty, st);
-        cudaFreeAsync(list, st);
-        cudaFreeAsync(cnt, st);
-        cudaFreeAsync(flags, st);
-        cudaFreeHost(hflag);
-        cudaFreeHost(hcnt);
-        return cuda_fail(e, "lsdtt_gpu_fill_pits");
-    }
-    cudaMemsetAsync(flags, 0, sizeof(int) * 2, st);
+    cudaError_t e = cudaMemsetAsync(flags, 0, sizeof(int) * 2, st);
     cudaMemsetAsync(dirty, 1, static_cast<std::size_t>(2 * ntiles), st);
-    fill_interior_nodata<<<grid_blocks(n, 256), 256, 0, st>>>(nr, nc, z_dev, mask_dev, grid->no_data_value, flags);
-    fill_init<<<grid_blocks(n, 256), 256, 0, st>>>(nr, nc, per_ns, per_ew, z_dev, mask_dev, grid->no_data_value, flags,
-                                                  out_dev, kind);
-    const float L = static_cast<float>(grid->cell_size);
-    const float Ld = L * static_cast<float>(1.4142135623730950488);
-    const float eps = min_slope > 0.0f ? min_slope : 0.0f;
+    fill_interior_nodata<<<grid_blocks(n, 256), 256, 0, st>>>(nr, nc, z_dev, mask_dev, nodata, flags);
+    fill_init<<<grid_blocks(n, 256), 256, 0, st>>>(nr, nc, per_ns, per_ew, z_dev, mask_dev, nodata, flags, F, kind);
     const dim3 block(32, 8);
     const dim3 tiles((nc + kT - 1) / kT, (nr + kT - 1) / kT);
     // Global passes until no tile changes; the change flag is read back every
@@ -221,7 +181,7 @@ extern "C" int lsdtt_gpu_fill_pits(const lsdtt_gpu_grid* grid, const float* z_de
     const unsigned list_grid = static_cast<unsigned>(std::max(1, sms) * 8);
     const unsigned colours = fill_colour_mask(ntx, nty, per_ns, per_ew);
     long pass = 0;
-    for (;;)
+    while (e == cudaSuccess)
     {
         cudaMemsetAsync(flags + 1, 0, sizeof(int), st);
         for (int k = 0; k < kCheckEvery && e == cudaSuccess; ++k, ++pass)
@@ -248,8 +208,8 @@ extern "C" int lsdtt_gpu_fill_pits(const lsdtt_gpu_grid* grid, const float* z_de
                             {
                                 if (!((colours >> c) & 1u)) continue;
                                 fill_relax_list<<<list_grid, block, 0, st>>>(nr, nc, per_ns, per_ew, L, Ld, eps, z_dev,
-                                                                             kind, out_dev, flags + 1, din, dout, ntx,
-                                                                             nty, list + c * ntiles, cnt + c);
+                                                                             kind, F, flags + 1, din, dout, ntx, nty,
+                                                                             list + c * ntiles, cnt + c);
                             }
                         }));
         }
@@ -257,22 +217,141 @@ extern "C" int lsdtt_gpu_fill_pits(const lsdtt_gpu_grid* grid, const float* z_de
         cudaMemcpyAsync(hflag, flags + 1, sizeof(int), cudaMemcpyDeviceToHost, st);
         e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) break;
-        if (*hflag == 0) break;
-        if (pass > max_pass)
+        if (*hflag == 0)
         {
-            e = cudaErrorUnknown;
+            *converged = true;
             break;
         }
+        if (pass > max_pass) break;
+    }
+    return e;
+}
+
+// The fill in the reference's order for one grid: the exact-fill stages with
+// a single member. F holds the epsilon relaxation on entry.
+cudaError_t exact_fill_single(int nr, int nc, bool per_ns, bool per_ew, float L, float Ld, float eps, float nodata,
+                              const float* z, const std::uint8_t* kind, const float* F0, float* F, cudaStream_t st,
+                              unsigned* failure)
+{
+    *failure = 0;
+    const std::int64_t n = static_cast<std::int64_t>(nr) * nc;
+    const std::int64_t N = (n + 255) / 256 * 256;
+    std::int64_t fcap = 2;
+    while (fcap < n) fcap <<= 1;
+    ExMember hm{};
+    hm.base = 0;
+    hm.fifo_base = 0;
+    hm.fifo_cap = static_cast<std::uint32_t>(fcap);
+    hm.nr = nr;
+    hm.nc = nc;
+    hm.L = L;
+    hm.Ld = Ld;
+    hm.eps = eps;
+    hm.nodata = nodata;
+    hm.per_ns = per_ns ? 1 : 0;
+    hm.per_ew = per_ew ? 1 : 0;
+    hm.on = 1;
+    const std::size_t meta = ex_round(sizeof(ExMember)) + ex_round(sizeof(std::uint16_t) * static_cast<std::size_t>(N / 256));
+    const std::size_t bytes = meta + ex_bytes(N, 1, fcap);
+    char* buf = nullptr;
+    cudaError_t e = cudaMallocAsync(&buf, bytes, st);
+    if (e != cudaSuccess) return e;
+    ExMember* mem = reinterpret_cast<ExMember*>(buf);
+    std::uint16_t* blk = reinterpret_cast<std::uint16_t*>(buf + ex_round(sizeof(ExMember)));
+    Scratch ws{buf + meta, bytes - meta, 0};
+    ExBuffers B{};
+    if (!ex_carve(ws, N, 1, fcap, B)) e = cudaErrorMemoryAllocation;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(mem, &hm, sizeof(ExMember), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(blk, 0, sizeof(std::uint16_t) * static_cast<std::size_t>(N / 256), st);
+    if (e == cudaSuccess) e = ex_setup();
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = ex_run(mem, blk, N, 1, 0, z, kind, F0, F, B, ws, std::max(sms, 1), st);
+    unsigned hu[6] = {0, 0, 0, 0, 0, 0};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hu, B.u, sizeof(hu), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess) *failure = hu[5];
+    cudaFreeAsync(buf, st);
+    return e;
+}
+
+}  // namespace
+
+extern "C" int lsdtt_gpu_fill_pits(const lsdtt_gpu_grid* grid, const float* z_dev, const std::uint8_t* mask_dev,
+                                   float min_slope, float* out_dev, void* stream)
+{
+    if (!grid || !z_dev || !mask_dev || !out_dev) return fail(LSDTT_GPU_EINVAL, "lsdtt_gpu_fill_pits: null argument");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        return fail(LSDTT_GPU_ENODEV, "lsdtt_gpu_fill_pits: no CUDA device");
+    if (!(grid->n_rows > 0 && grid->n_cols > 0 && grid->cell_size > 0.0))
+        return fail(LSDTT_GPU_EINVAL, "lsdtt::fill_pits: invalid raster metadata");
+    auto is_p = [&](int i) { return grid->boundary_conditions[i] == 'p' || grid->boundary_conditions[i] == 'P'; };
+    const bool per_ns = is_p(0), per_ew = is_p(1);
+    const std::string bc(grid->boundary_conditions, 4);
+    if (per_ns != is_p(2))
+        return fail(LSDTT_GPU_EINVAL,
+                    "lsdtt::fill_pits: north and south periodic flags must match (boundary_conditions '" + bc + "')");
+    if (per_ew != is_p(3))
+        return fail(LSDTT_GPU_EINVAL,
+                    "lsdtt::fill_pits: east and west periodic flags must match (boundary_conditions '" + bc + "')");
+    if (per_ns && per_ew)
+        return fail(LSDTT_GPU_EINVAL, "lsdtt::fill_pits: boundary_conditions '" + bc +
+                                          "' is periodic in BOTH directions, so the grid has no drainage exit at all "
+                                          "and every cell would fill to the global maximum. Leave one pair open.");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int nr = grid->n_rows, nc = grid->n_cols;
+    const std::int64_t n = static_cast<std::int64_t>(nr) * nc;
+    const float eps = min_slope > 0.0f ? min_slope : 0.0f;
+    if (eps > 0.0f && n > (std::int64_t(1) << 31))
+        return fail(LSDTT_GPU_EINVAL, "lsdtt_gpu_fill_pits: grids above 2^31 cells are not supported with min_slope > 0");
+    std::uint8_t* kind = nullptr;
+    int* flags = nullptr;   // [0] interior nodata, [1] changed
+    int* hflag = nullptr;
+    std::uint8_t* dirty = nullptr;  // two per-tile activity planes
+    std::int32_t* list = nullptr;   // active tiles of the current pass, by colour
+    unsigned long long* cnt = nullptr;  // their count and cells
+    unsigned long long* hcnt = nullptr;
+    float* F0 = nullptr;            // epsilon-0 fill (min_slope > 0 only)
+    const std::int64_t ntiles = static_cast<std::int64_t>((nc + kT - 1) / kT) * ((nr + kT - 1) / kT);
+    cudaError_t e = cudaMallocAsync(&kind, static_cast<std::size_t>(n), st);
+    if (e == cudaSuccess) e = cudaMallocAsync(&dirty, static_cast<std::size_t>(2 * ntiles), st);
+    if (e == cudaSuccess)
+        e = cudaMallocAsync(&list, sizeof(std::int32_t) * kFillColours * static_cast<std::size_t>(ntiles), st);
+    if (e == cudaSuccess) e = cudaMallocAsync(&cnt, sizeof(unsigned long long) * (kFillColours + 1), st);
+    if (e == cudaSuccess) e = cudaMallocAsync(&flags, sizeof(int) * 2, st);
+    if (e == cudaSuccess && eps > 0.0f) e = cudaMallocAsync(&F0, sizeof(float) * static_cast<std::size_t>(n), st);
+    if (e == cudaSuccess) e = cudaMallocHost(&hflag, sizeof(int));
+    if (e == cudaSuccess) e = cudaMallocHost(&hcnt, sizeof(unsigned long long) * (kFillColours + 1));
+    const float L = static_cast<float>(grid->cell_size);
+    const float Ld = L * static_cast<float>(1.4142135623730950488);
+    bool converged = true;
+    unsigned failure = 0;
+    if (e == cudaSuccess)
+        e = relax_fill(nr, nc, per_ns, per_ew, L, Ld, eps, z_dev, mask_dev, grid->no_data_value, out_dev, kind, flags,
+                       hflag, dirty, list, cnt, hcnt, st, &converged);
+    if (e == cudaSuccess && converged && eps > 0.0f)
+    {
+        e = relax_fill(nr, nc, per_ns, per_ew, L, Ld, 0.0f, z_dev, mask_dev, grid->no_data_value, F0, kind, flags,
+                       hflag, dirty, list, cnt, hcnt, st, &converged);
+        if (e == cudaSuccess && converged)
+            e = exact_fill_single(nr, nc, per_ns, per_ew, L, Ld, eps, static_cast<float>(grid->no_data_value), z_dev,
+                                  kind, F0, out_dev, st, &failure);
     }
     cudaFreeAsync(kind, st);
     cudaFreeAsync(dirty, st);
     cudaFreeAsync(list, st);
     cudaFreeAsync(cnt, st);
     cudaFreeAsync(flags, st);
+    cudaFreeAsync(F0, st);
     cudaFreeHost(hflag);
     cudaFreeHost(hcnt);
-    if (e == cudaErrorUnknown) return fail(LSDTT_GPU_ETIMEOUT, "lsdtt_gpu_fill_pits: relaxation did not converge");
     if (e != cudaSuccess) return cuda_fail(e, "lsdtt_gpu_fill_pits");
+    if (!converged) return fail(LSDTT_GPU_ETIMEOUT, "lsdtt_gpu_fill_pits: relaxation did not converge");
+    if (failure)
+        return fail(LSDTT_GPU_EOVERFLOW, failure == 1 ? "lsdtt_gpu_fill_pits: a fill window outgrew its arrays"
+                                                      : "lsdtt_gpu_fill_pits: the fill window chain did not advance");
     return LSDTT_GPU_OK;
 }
 

@@ -1,0 +1,522 @@
+// fill_exact.cuh -- the epsilon fill in the reference's order over packed
+// grids (one grid = one member), from the epsilon-0 fill F0 and the
+// value-ordered estimate F1 (see fill_window.cuh for the method).
+//
+// Stages, every launch of a fixed size (no host read-back, so an ensemble
+// step can hold them in its CUDA graph):
+//   1. per cell: min neighbour F0, sort keys, pour levels;
+//   2. distinct pour levels per member, ascending (the cuts);
+//   3. candidate window starts: cuts not inside (F0(c), F1(c)] of a cell
+//      raised in the estimate;
+//   4. the valid cells of each member sorted by (F0, index);
+//   5. every candidate replayed by one warp with its state in shared memory
+//      (two sizes); raised cells staged in a pool;
+//   6. per member, one warp follows the chain of valid windows from the
+//      lowest cut, replaying any window on it that neither size could hold
+//      with its heap and FIFO in a whole block's shared memory, or, past
+//      that, in global memory;
+//   7. the chain's staged cells committed.
+#pragma once
+
+#include <cstdint>
+
+#include "common.cuh"
+#include "engine.cuh"
+#include "fill_window.cuh"
+#include "prims.cuh"
+
+namespace lsdtt_gb300
+{
+namespace
+{
+
+struct ExMember
+{
+    std::int64_t base;       // first packed cell
+    std::int64_t fifo_base;  // first entry of its global-tier FIFO ring
+    std::uint32_t fifo_cap;  // power of two >= its cells
+    std::int32_t nr, nc;
+    float L, Ld, eps, nodata;
+    std::int32_t per_ns, per_ew, on;  // on: the epsilon fill is replayed for this member
+};
+
+// Device buffers of the exact fill for N packed cells and M members.
+struct ExBuffers
+{
+    float* mnb;
+    std::uint64_t *key0, *key1, *pkey;
+    std::uint32_t *val0, *val1, *ordL;
+    float *ordF0, *ordMnb, *cuts;
+    std::int32_t* cut_member;
+    std::uint8_t *cand, *status, *chain;
+    std::int32_t* next;
+    std::uint32_t *off, *cnt;
+    int *diff, *excl;
+    std::int32_t *wl, *wl2;
+    std::uint32_t* pool_c;
+    float* pool_v;
+    float *gfv, *ghz;
+    std::uint32_t *gfc, *ghc, *stamp;
+    std::int64_t* nsorted;  // [M]
+    int *ncut, *cut_base;   // [M], [M + 1]
+    unsigned* u;            // [0] total cuts, [1] nwl, [2] work, [3] nwl2, [4] work2, [5] error
+    unsigned long long* pool_used;
+};
+
+inline std::size_t ex_round(std::size_t b) { return (b + 255) & ~std::size_t(255); }
+
+// Bytes of ExBuffers for N cells, M members and a global FIFO of fifo_total
+// entries, plus the sort and scan scratch.
+inline std::size_t ex_bytes(std::int64_t N, int M, std::int64_t fifo_total)
+{
+    const std::size_t n = static_cast<std::size_t>(N) + 1, m = static_cast<std::size_t>(M) + 1;
+    const std::size_t tiles = static_cast<std::size_t>((N + kSortTile - 1) / kSortTile) + 2;
+    std::size_t b = 0;
+    for (std::size_t w : {4, 8, 8, 8, 4, 4, 4, 4, 4, 4, 4, 1, 1, 1, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4})
+        b += ex_round(w * n);
+    b += 2 * ex_round(4 * static_cast<std::size_t>(fifo_total) + 4);
+    b += ex_round(8 * m) + 2 * ex_round(4 * m) + ex_round(64) + ex_round(8);
+    b += tiles * 256 * 4 * 2 + tiles * 64 + (256 << 10);  // sort / scan scratch
+    return b;
+}
+
+// Carve ExBuffers from ws (leaves the rest of ws for the sort and scans).
+inline bool ex_carve(Scratch& ws, std::int64_t N, int M, std::int64_t fifo_total, ExBuffers& B)
+{
+    const std::size_t n = static_cast<std::size_t>(N) + 1, m = static_cast<std::size_t>(M) + 1;
+    B.mnb = ws.take<float>(n);
+    B.key0 = ws.take<std::uint64_t>(n);
+    B.key1 = ws.take<std::uint64_t>(n);
+    B.pkey = ws.take<std::uint64_t>(n);
+    B.val0 = ws.take<std::uint32_t>(n);
+    B.val1 = ws.take<std::uint32_t>(n);
+    B.ordL = ws.take<std::uint32_t>(n);
+    B.ordF0 = ws.take<float>(n);
+    B.ordMnb = ws.take<float>(n);
+    B.cuts = ws.take<float>(n);
+    B.cut_member = ws.take<std::int32_t>(n);
+    B.cand = ws.take<std::uint8_t>(n);
+    B.status = ws.take<std::uint8_t>(n);
+    B.chain = ws.take<std::uint8_t>(n);
+    B.next = ws.take<std::int32_t>(n);
+    B.off = ws.take<std::uint32_t>(n);
+    B.cnt = ws.take<std::uint32_t>(n);
+    B.diff = ws.take<int>(n);
+    B.excl = ws.take<int>(n);
+    B.wl = ws.take<std::int32_t>(n);
+    B.wl2 = ws.take<std::int32_t>(n);
+    B.pool_c = ws.take<std::uint32_t>(n);
+    B.pool_v = ws.take<float>(n);
+    B.ghz = ws.take<float>(n);
+    B.ghc = ws.take<std::uint32_t>(n);
+    B.stamp = ws.take<std::uint32_t>(n);
+    B.gfv = ws.take<float>(static_cast<std::size_t>(fifo_total) + 1);
+    B.gfc = ws.take<std::uint32_t>(static_cast<std::size_t>(fifo_total) + 1);
+    B.nsorted = ws.take<std::int64_t>(m);
+    B.ncut = ws.take<int>(m);
+    B.cut_base = ws.take<int>(m);
+    B.u = ws.take<unsigned>(16);
+    B.pool_used = ws.take<unsigned long long>(1);
+    return B.pool_used != nullptr;
+}
+
+__device__ __forceinline__ WinGrid ex_member_grid(const ExMember& M, int m, const float* z, const std::uint8_t* kind,
+                                                  const float* F0, const ExBuffers& B)
+{
+    const int cb = B.cut_base[m];
+    return WinGrid{M.nr, M.nc, M.per_ns != 0, M.per_ew != 0, M.L, M.Ld, M.eps, z + M.base, F0 + M.base,
+                   B.mnb + M.base, kind + M.base, B.ordL + M.base, B.ordF0 + M.base, B.ordMnb + M.base,
+                   B.nsorted[m], B.cuts + cb, B.cand + cb, B.ncut[m]};
+}
+
+// 1. Per cell: the smallest F0 among valid neighbours (-inf for seeds, +inf
+// for cells never queued), the cell sort key (member, F0; 2^32-1 puts
+// invalid and NaN cells last in their member) and the pour-level key.
+// 256-thread blocks over the packed cells (a block never spans two members).
+__global__ void ex_prep(const ExMember* __restrict__ mem, const std::uint16_t* __restrict__ blk_member,
+                        std::int64_t N, const float* __restrict__ z, const std::uint8_t* __restrict__ kind,
+                        const float* __restrict__ F0, ExBuffers B)
+{
+    LSDTT_COUNT();
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int m = blk_member[blockIdx.x];
+    const ExMember M = mem[m];
+    const std::uint64_t hi = static_cast<std::uint64_t>(m) << 32;
+    const std::int64_t local = i - M.base;
+    bool valid = false;
+    if (i < N)
+    {
+        B.val0[i] = static_cast<std::uint32_t>(i);
+        float zi = 0.0f;
+        if (M.on && local < static_cast<std::int64_t>(M.nr) * M.nc && kind[i] != 0)
+        {
+            zi = z[i];
+            valid = !isnan(zi);
+        }
+        std::uint32_t plev = 0xffffffffu;
+        if (!valid)
+        {
+            B.mnb[i] = INFINITY;
+            B.key0[i] = hi | 0xffffffffull;
+        }
+        else
+        {
+            const float f = F0[i];
+            B.key0[i] = hi | float_order_key(f);
+            const int r = static_cast<int>(local / M.nc), c = static_cast<int>(local - static_cast<std::int64_t>(r) * M.nc);
+            float mn = INFINITY;
+            bool pour = false;
+            for (int d = 0; d < 8; ++d)
+            {
+                int rr, cc;
+                if (!fill_nb(M.nr, M.nc, M.per_ns != 0, M.per_ew != 0, r, c, d, rr, cc)) continue;
+                const std::int64_t j = M.base + static_cast<std::int64_t>(rr) * M.nc + cc;
+                if (kind[j] == 0) continue;
+                const float zj = z[j];
+                if (isnan(zj)) continue;
+                const float fj = F0[j];
+                mn = fminf(mn, fj);
+                if (zi <= f && zj == fj && fj == f) pour = true;
+            }
+            B.mnb[i] = (kind[i] == 2) ? -INFINITY : mn;
+            if (pour) plev = float_order_key(f);
+        }
+        B.pkey[i] = hi | plev;
+    }
+    const unsigned b = __ballot_sync(0xffffffffu, valid);
+    if ((threadIdx.x & 31) == 0 && b) atomicAdd(reinterpret_cast<unsigned long long*>(&B.nsorted[m]),
+                                                static_cast<unsigned long long>(__popc(b)));
+}
+
+// 2. First-of-run flags over the sorted pour-level keys, then the levels.
+__global__ void ex_level_flags(const std::uint64_t* __restrict__ key, std::int64_t N, std::uint32_t* __restrict__ flag)
+{
+    LSDTT_COUNT();
+    const std::int64_t k = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (k >= N) return;
+    const std::uint64_t v = key[k];
+    flag[k] = ((v & 0xffffffffull) != 0xffffffffull && (k == 0 || key[k - 1] != v)) ? 1u : 0u;
+}
+
+__global__ void ex_level_scatter(const std::uint64_t* __restrict__ key, std::int64_t N,
+                                 const std::uint32_t* __restrict__ flag, const std::uint32_t* __restrict__ pos,
+                                 ExBuffers B)
+{
+    LSDTT_COUNT();
+    const std::int64_t k = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (k >= N || !flag[k]) return;
+    const std::uint64_t v = key[k];
+    const int m = static_cast<int>(v >> 32);
+    B.cuts[pos[k]] = float_from_order_key(static_cast<std::uint32_t>(v));
+    B.cut_member[pos[k]] = m;
+    atomicAdd(&B.ncut[m], 1);
+}
+
+// 3. A cut in (F0(c), F1(c)] for a cell c raised in the value-ordered fill
+// F1 most likely lies inside a running episode (c is still waiting when the
+// heap reaches the cut): it is not replayed from. The estimate is used as it
+// is: widening it merged valid windows on LEM inputs (epsilon ramps) into a
+// few long ones, while a missed invalid cut costs one wasted replay.
+__global__ void ex_cover(const ExMember* __restrict__ mem, const std::uint16_t* __restrict__ blk_member,
+                         std::int64_t N, const float* __restrict__ z, const std::uint8_t* __restrict__ kind,
+                         const float* __restrict__ F0, const float* __restrict__ F1, ExBuffers B)
+{
+    LSDTT_COUNT();
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int m = blk_member[blockIdx.x];
+    const ExMember M = mem[m];
+    if (i >= N || !M.on || i - M.base >= static_cast<std::int64_t>(M.nr) * M.nc || kind[i] == 0 || isnan(z[i]))
+        return;
+    const float f0 = F0[i], f1 = F1[i];
+    if (!(f1 > f0)) return;
+    const int cb = B.cut_base[m], nc = B.ncut[m];
+    const int lo = static_cast<int>(win_upper_bound(B.cuts + cb, nc, f0));
+    const int hi = static_cast<int>(win_upper_bound(B.cuts + cb, nc, f1));
+    if (lo >= hi) return;
+    atomicAdd(&B.diff[cb + lo], 1);
+    atomicAdd(&B.diff[cb + hi], -1);
+}
+
+// Candidate flags (each member's lowest cut always: the first episode starts
+// there with an empty FIFO) and the candidate list; every window unreplayed.
+__global__ void ex_candidates(std::int64_t N, ExBuffers B)
+{
+    LSDTT_COUNT();
+    const std::int64_t k = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (k >= N || k >= static_cast<std::int64_t>(B.u[0])) return;
+    const int m = B.cut_member[k];
+    const bool c = k == B.cut_base[m] || B.excl[k] + B.diff[k] == 0;
+    B.cand[k] = c ? 1 : 0;
+    B.status[k] = 255;
+    B.chain[k] = 0;
+    if (c) B.wl[atomicAdd(&B.u[1], 1u)] = static_cast<std::int32_t>(k);
+}
+
+// 4. Sorted-order copies: member-local cell, F0 and mnb per sorted position
+// (a member's sorted cells occupy its own packed range).
+__global__ void ex_gather(const ExMember* __restrict__ mem, const std::uint16_t* __restrict__ blk_member,
+                          std::int64_t N, const std::uint32_t* __restrict__ ord, const float* __restrict__ F0,
+                          ExBuffers B)
+{
+    LSDTT_COUNT();
+    const std::int64_t p = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int m = blk_member[blockIdx.x];
+    const ExMember M = mem[m];
+    if (p >= N || p - M.base >= B.nsorted[m]) return;
+    const std::uint32_t c = ord[p];
+    B.ordL[p] = static_cast<std::uint32_t>(c - M.base);
+    B.ordF0[p] = F0[c];
+    B.ordMnb[p] = B.mnb[c];
+}
+
+// F before the windows write their raised cells: every valid cell at its own
+// elevation (NaN cells stay NaN), invalid cells at the nodata value.
+__global__ void ex_base(const ExMember* __restrict__ mem, const std::uint16_t* __restrict__ blk_member,
+                        std::int64_t N, const float* __restrict__ z, const std::uint8_t* __restrict__ kind,
+                        float* __restrict__ F)
+{
+    LSDTT_COUNT();
+    const std::int64_t i = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int m = blk_member[blockIdx.x];
+    const ExMember M = mem[m];
+    if (i >= N || !M.on || i - M.base >= static_cast<std::int64_t>(M.nr) * M.nc) return;
+    F[i] = kind[i] == 0 ? M.nodata : z[i];
+}
+
+// 5. Replays of the listed windows, one warp per block, the replay state in
+// shared memory (FIFO FQ, heap DH, seen set HS, raised outputs OC). A window
+// that outgrows any of them is marked kWinOverflow for the next size. Raised
+// outputs are staged in the pool and committed only for chain windows.
+template <int FQ, int DH, int HS, int OC>
+__global__ void __launch_bounds__(32) ex_windows(const ExMember* __restrict__ mem, const float* __restrict__ z,
+                                                 const std::uint8_t* __restrict__ kind, const float* __restrict__ F0,
+                                                 ExBuffers B, const std::int32_t* __restrict__ wl,
+                                                 const unsigned* __restrict__ nwl, unsigned* __restrict__ work,
+                                                 unsigned long long pool_cap, unsigned long long pop_limit)
+{
+    LSDTT_COUNT();
+    extern __shared__ __align__(16) unsigned char ex_smem[];
+    WinStore s{};
+    s.fv = reinterpret_cast<float*>(ex_smem);
+    s.fc = reinterpret_cast<std::uint32_t*>(s.fv + FQ);
+    s.fcap = FQ;
+    s.hz = reinterpret_cast<float*>(s.fc + FQ);
+    s.hc = reinterpret_cast<std::uint32_t*>(s.hz + DH);
+    s.hcap = DH;
+    s.hs = s.hc + DH;
+    s.hscap = HS;
+    s.oc = s.hs + HS;
+    s.ov = reinterpret_cast<float*>(s.oc + OC);
+    s.ocap = OC;
+    const int lane = threadIdx.x & 31;
+    const unsigned total = *nwl;
+    for (;;)
+    {
+        unsigned t = 0;
+        if (lane == 0) t = atomicAdd(work, 1u);
+        t = __shfl_sync(0xffffffffu, t, 0);
+        if (t >= total) break;
+        const int g = wl[t];
+        const int m = B.cut_member[g];
+        const WinGrid G = ex_member_grid(mem[m], m, z, kind, F0, B);
+        WinResult r = win_replay(G, g - B.cut_base[m], s, pop_limit);
+        unsigned long long base = 0;
+        if (r.status == kWinOk && r.nout)
+        {
+            if (lane == 0) base = atomicAdd(B.pool_used, static_cast<unsigned long long>(r.nout));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (base + r.nout > pool_cap) r.status = kWinOverflow;
+            else
+                for (std::uint32_t k = lane; k < r.nout; k += 32)
+                {
+                    B.pool_c[base + k] = s.oc[k];
+                    B.pool_v[base + k] = s.ov[k];
+                }
+        }
+        if (lane == 0)
+        {
+            B.next[g] = r.next;
+            B.status[g] = static_cast<std::uint8_t>(r.status);
+            B.off[g] = static_cast<std::uint32_t>(base);
+            B.cnt[g] = r.nout;
+        }
+        __syncwarp();
+    }
+}
+
+// Windows the first size could not hold, listed for the second.
+__global__ void ex_overflow_list(std::int64_t N, ExBuffers B)
+{
+    LSDTT_COUNT();
+    const std::int64_t t = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (t >= N || t >= static_cast<std::int64_t>(B.u[1])) return;
+    const int g = B.wl[t];
+    if (B.status[g] == kWinOverflow) B.wl2[atomicAdd(&B.u[3], 1u)] = g;
+}
+
+// 6. The chain of each member, one warp per member (block m): from the
+// lowest cut each window names the next valid start. A window on the chain
+// that neither shared-memory size held is replayed here: first with its FIFO
+// and heap in this block's shared memory (FQ_C, DH_C) and seen cells marked
+// by per-cell stamps, then, if that too overflows, with everything in global
+// memory; either way writing its raised cells straight into F. u[5] records
+// a failure (1: a global replay outgrew its arrays; 2: the chain did not
+// advance).
+template <int FQ_C, int DH_C>
+__global__ void __launch_bounds__(32) ex_chain(const ExMember* __restrict__ mem, const float* __restrict__ z,
+                                               const std::uint8_t* __restrict__ kind, const float* __restrict__ F0,
+                                               float* __restrict__ F, ExBuffers B)
+{
+    LSDTT_COUNT();
+    extern __shared__ __align__(16) unsigned char ex_csmem[];
+    const int lane = threadIdx.x & 31;
+    const int m = blockIdx.x;
+    const ExMember M = mem[m];
+    if (!M.on) return;
+    const WinGrid G = ex_member_grid(M, m, z, kind, F0, B);
+    const int cb = B.cut_base[m];
+    WinStore mid{};
+    mid.fv = reinterpret_cast<float*>(ex_csmem);
+    mid.fc = reinterpret_cast<std::uint32_t*>(mid.fv + FQ_C);
+    mid.fcap = FQ_C;
+    mid.hz = reinterpret_cast<float*>(mid.fc + FQ_C);
+    mid.hc = reinterpret_cast<std::uint32_t*>(mid.hz + DH_C);
+    mid.hcap = DH_C;
+    mid.stamp = B.stamp + M.base;
+    mid.out_F = F + M.base;
+    WinStore big = mid;
+    big.fv = B.gfv + M.fifo_base;
+    big.fc = B.gfc + M.fifo_base;
+    big.fcap = M.fifo_cap;
+    big.hz = B.ghz + M.base;
+    big.hc = B.ghc + M.base;
+    big.hcap = static_cast<std::uint32_t>(static_cast<std::int64_t>(M.nr) * M.nc);
+    std::uint32_t stamp_id = 0;
+    int w = 0;
+    while (w < G.ncut)
+    {
+        int nx;
+        if (B.status[cb + w] != kWinOk)
+        {
+            // a replay that overflows may have written some raised cells
+            // already; the one that completes writes every one of them again
+            mid.stamp_id = ++stamp_id;
+            WinResult r = win_replay(G, w, mid, 0);
+            if (r.status != kWinOk)
+            {
+                big.stamp_id = ++stamp_id;
+                r = win_replay(G, w, big, 0);
+            }
+            if (r.status != kWinOk)
+            {
+                if (lane == 0) atomicExch(&B.u[5], 1u);
+                return;
+            }
+            nx = r.next;
+            if (lane == 0) B.chain[cb + w] = 2;
+        }
+        else
+        {
+            nx = B.next[cb + w];
+            if (lane == 0) B.chain[cb + w] = 1;
+        }
+        __syncwarp();
+        if (nx <= w)  // a window always ends above its start
+        {
+            if (lane == 0) atomicExch(&B.u[5], 2u);
+            return;
+        }
+        w = nx;
+    }
+}
+
+// 7. Staged raised cells of the chain windows into F, one warp per window.
+__global__ void ex_commit(const ExMember* __restrict__ mem, std::int64_t N, float* __restrict__ F, ExBuffers B)
+{
+    LSDTT_COUNT();
+    const int lane = threadIdx.x & 31;
+    const std::int64_t warps = static_cast<std::int64_t>(gridDim.x) * (blockDim.x >> 5);
+    const std::int64_t total = static_cast<std::int64_t>(B.u[0]);
+    for (std::int64_t k = (static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+         k < total && k < N; k += warps)
+    {
+        if (B.chain[k] != 1) continue;
+        float* Fm = F + mem[B.cut_member[k]].base;
+        const std::uint32_t o = B.off[k], c = B.cnt[k];
+        for (std::uint32_t t = lane; t < c; t += 32) Fm[B.pool_c[o + t]] = B.pool_v[o + t];
+    }
+}
+
+constexpr int kExA_FQ = 128, kExA_DH = 256, kExA_HS = 1024, kExA_OC = 256;
+constexpr int kExB_FQ = 1024, kExB_DH = 4096, kExB_HS = 8192, kExB_OC = 4096;
+constexpr std::size_t kExSmemA = 8 * kExA_FQ + 8 * kExA_DH + 4 * kExA_HS + 8 * kExA_OC;
+constexpr std::size_t kExSmemB = 8 * kExB_FQ + 8 * kExB_DH + 4 * kExB_HS + 8 * kExB_OC;
+constexpr int kExC_FQ = 4096, kExC_DH = 20480;
+constexpr std::size_t kExSmemC = 8 * kExC_FQ + 8 * kExC_DH;
+
+// Opt the larger replay sizes into their shared memory (current device).
+inline cudaError_t ex_setup()
+{
+    cudaError_t e = cudaFuncSetAttribute(ex_windows<kExB_FQ, kExB_DH, kExB_HS, kExB_OC>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kExSmemB));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(ex_chain<kExC_FQ, kExC_DH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(kExSmemC));
+    return e;
+}
+
+// Enqueue the whole exact fill on st. On entry F holds the value-ordered
+// estimate for the members that are on; on return (in stream order) their
+// fill in the reference's order. `ws` holds the buffers carved by ex_carve
+// and room for the sort and scan scratch. `mbits` = bits of the member index
+// (0 for one member). Failures of the replays are left in B.u[5].
+inline cudaError_t ex_run(const ExMember* mem, const std::uint16_t* blk_member, std::int64_t N, int M, int mbits,
+                          const float* z, const std::uint8_t* kind, const float* F0, float* F, const ExBuffers& B,
+                          Scratch& ws, int sms, cudaStream_t st)
+{
+    const unsigned nb = static_cast<unsigned>(N / 256);
+    cudaError_t e = cudaMemsetAsync(B.u, 0, 16 * sizeof(unsigned), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(B.pool_used, 0, sizeof(unsigned long long), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(B.nsorted, 0, sizeof(std::int64_t) * M, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(B.ncut, 0, sizeof(int) * M, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(B.diff, 0, sizeof(int) * (static_cast<std::size_t>(N) + 1), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(B.stamp, 0, sizeof(std::uint32_t) * static_cast<std::size_t>(N), st);
+    if (e != cudaSuccess) return e;
+    ex_prep<<<nb, 256, 0, st>>>(mem, blk_member, N, z, kind, F0, B);
+    // distinct pour levels (the cell keys stay in key0/val0 meanwhile)
+    const int bits = 32 + mbits;
+    int r = radix_sort_pairs(B.pkey, B.ordL, B.key1, B.val1, N, bits, ws, st, &e);
+    if (e != cudaSuccess) return e;
+    const std::uint64_t* lk = r ? B.key1 : B.pkey;
+    std::uint32_t* flag = reinterpret_cast<std::uint32_t*>(B.ordF0);
+    std::uint32_t* pos = reinterpret_cast<std::uint32_t*>(B.ordMnb);
+    ex_level_flags<<<nb, 256, 0, st>>>(lk, N, flag);
+    e = exclusive_scan<std::uint32_t, std::uint32_t>(flag, N, pos, B.u, ws, st);
+    if (e != cudaSuccess) return e;
+    ex_level_scatter<<<nb, 256, 0, st>>>(lk, N, flag, pos, B);
+    e = exclusive_scan<int, int>(B.ncut, M, B.cut_base, static_cast<int*>(nullptr), ws, st);
+    if (e != cudaSuccess) return e;
+    // candidate starts
+    ex_cover<<<nb, 256, 0, st>>>(mem, blk_member, N, z, kind, F0, F, B);
+    e = exclusive_scan<int, int>(B.diff, N, B.excl, static_cast<int*>(nullptr), ws, st);
+    if (e != cudaSuccess) return e;
+    ex_candidates<<<nb, 256, 0, st>>>(N, B);
+    // the valid cells of each member by (F0, index)
+    r = radix_sort_pairs(B.key0, B.val0, B.key1, B.val1, N, bits, ws, st, &e);
+    if (e != cudaSuccess) return e;
+    ex_gather<<<nb, 256, 0, st>>>(mem, blk_member, N, r ? B.val1 : B.val0, F0, B);
+    ex_base<<<nb, 256, 0, st>>>(mem, blk_member, N, z, kind, F);
+    // replays: small shared-memory size, then the larger one for overflows
+    ex_windows<kExA_FQ, kExA_DH, kExA_HS, kExA_OC><<<sms * 16, 32, kExSmemA, st>>>(
+        mem, z, kind, F0, B, B.wl, B.u + 1, B.u + 2, static_cast<unsigned long long>(N), 16ull * kExA_HS);
+    ex_overflow_list<<<nb, 256, 0, st>>>(N, B);
+    ex_windows<kExB_FQ, kExB_DH, kExB_HS, kExB_OC><<<sms * 2, 32, kExSmemB, st>>>(
+        mem, z, kind, F0, B, B.wl2, B.u + 3, B.u + 4, static_cast<unsigned long long>(N), 16ull * kExB_HS);
+    ex_chain<kExC_FQ, kExC_DH><<<M, 32, kExSmemC, st>>>(mem, z, kind, F0, F, B);
+    ex_commit<<<static_cast<unsigned>(std::max<std::int64_t>(1, std::min<std::int64_t>(N / 8, sms * 64))), 256, 0,
+                st>>>(mem, N, F, B);
+    return cudaGetLastError();
+}
+
+}  // namespace
+}  // namespace lsdtt_gb300

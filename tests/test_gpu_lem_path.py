@@ -1,12 +1,9 @@
 """GPU fill, stream power, hillslope, LEM step and host routing against the
 CPU oracle.
 
-Bars: stream power and every integer output bit-exact; hillslope elevations
-within 1e-5 relative of the FP64 restatement (PCG to a 1e-8 relative
-residual); the fill's raised/unraised partition exact, with the count of
-raised cells whose value differs from the reference reported (the GPU fill
-orders raised cells by value where the reference orders flats breadth-first;
-see lsdtt_gb300/csrc/fill.cu)."""
+Bars: the fill, stream power and every integer output bit-exact;
+hillslope elevations within 1e-5 relative of the FP64 restatement (PCG to a
+1e-8 relative residual)."""
 import numpy as np
 import pytest
 
@@ -23,14 +20,7 @@ def _cfg1(port, n=512):
     return z, np.ones_like(z, np.uint8)
 
 
-# Share of cells whose filled value differs from the reference (value-
-# ordered GPU flood vs the reference's global FIFO order), bounded just above
-# the measured 1.9% and 30%: regression guards, not targets (the target is
-# zero; see lsdtt_gb300/csrc/fill.cu for why the order cannot be emulated).
-FILL_MISMATCH_BOUND = {"noise_tilt_512": 0.021, "fractal_pits_512": 0.31}
-
-
-def test_fill_properties_and_reported_mismatch(port):
+def test_fill_properties_and_bitwise(port):
     import lsdtt_gb300 as G
     report = {}
     for name, (z, m, cell, bc) in {
@@ -57,9 +47,9 @@ def test_fill_properties_and_reported_mismatch(port):
         report[name] = dict(cells=int(diff.sum()), frac=float(diff.mean()), raised_ref=int(raised_ref.sum()),
                             raised_status_differs=int((raised_ref != raised_gpu).sum()),
                             max_abs=float(np.max(np.abs(got - want))))
-    print("fill mismatch vs reference:", report)
+    print("fill vs reference:", report)
     for name, r in report.items():
-        assert r["frac"] <= FILL_MISMATCH_BOUND[name], (name, r)
+        assert r["cells"] == 0, (name, r)
 
 
 def test_fill_zero_slope_is_exact(port):
@@ -190,10 +180,9 @@ def test_hillslope_linear_general_entry_matches_linear_entry(port):
 def test_periodic_fill_against_oracle(port, bc, shape):
     """The periodic fill (fill_pits with a 'p' pair: the priority flood with
     the seam joined, raster_flow_preprocessing_cpu.cpp:744-757) against the
-    oracle: bit-exact at min_slope 0 on grids whose periodic axis has an odd
-    number of 32-cell tiles (the third tile colour) or a partial last tile;
-    at 1e-4 the differing cells are counted and bounded like the other
-    epsilon fills."""
+    oracle, bit-exact at min_slope 0 and 1e-4, on grids whose periodic axis
+    has an odd number of 32-cell tiles (the third tile colour) or a partial
+    last tile."""
     import lsdtt_gb300 as G
     z = surfaces.add_pits(surfaces.fractal(shape[0], shape[1], 200.0, 17), 40, 17)
     m = np.ones_like(z, np.uint8)
@@ -205,4 +194,4 @@ def test_periodic_fill_against_oracle(port, bc, shape):
     diff = got.view(np.uint32) != want.view(np.uint32)
     print(f"periodic fill {bc} {shape}: epsilon 1e-4, {int(diff.sum())} of {int((want != z).sum())} raised cells "
           f"differ")
-    assert diff.mean() <= FILL_MISMATCH_BOUND["fractal_pits_512"]
+    assert not diff.any()
