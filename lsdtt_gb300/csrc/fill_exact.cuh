@@ -22,6 +22,7 @@
 
 #include "common.cuh"
 #include "engine.cuh"
+#include "fill_sweep.cuh"
 #include "fill_window.cuh"
 #include "prims.cuh"
 
@@ -43,10 +44,10 @@ struct ExMember
 // Device buffers of the exact fill for N packed cells and M members.
 struct ExBuffers
 {
-    float* mnb;
+    float4 *rec, *ordRec;  // per cell and per sorted position (WinGrid)
     std::uint64_t *key0, *key1, *pkey;
-    std::uint32_t *val0, *val1, *ordL;
-    float *ordF0, *ordMnb, *cuts;
+    std::uint32_t *val0, *val1;
+    float* cuts;
     std::int32_t* cut_member;
     std::uint8_t *cand, *status, *chain;
     std::int32_t* next;
@@ -57,6 +58,8 @@ struct ExBuffers
     float* pool_v;
     float *gfv, *ghz;
     std::uint32_t *gfc, *ghc, *stamp;
+    SweepBufs sw;           // the block replay's scratch (global cell indices; offset per member)
+    std::uint32_t* sw_ctr;  // [M] stamp counters of the block replay
     std::int64_t* nsorted;  // [M]
     int *ncut, *cut_base;   // [M], [M + 1]
     unsigned* u;            // [0] total cuts, [1] nwl, [2] work, [3] nwl2, [4] work2, [5] error
@@ -72,8 +75,12 @@ inline std::size_t ex_bytes(std::int64_t N, int M, std::int64_t fifo_total)
     const std::size_t n = static_cast<std::size_t>(N) + 1, m = static_cast<std::size_t>(M) + 1;
     const std::size_t tiles = static_cast<std::size_t>((N + kSortTile - 1) / kSortTile) + 2;
     std::size_t b = 0;
-    for (std::size_t w : {4, 8, 8, 8, 4, 4, 4, 4, 4, 4, 4, 1, 1, 1, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4})
+    for (std::size_t w : {16, 16, 8, 8, 8, 4, 4, 4, 4, 1, 1, 1, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4})
         b += ex_round(w * n);
+    // block replay: cst, ev_st, ev_hi, ev_val, mk_c, mk_t, te_st, te_hi,
+    // te_lo, te_val, te_k, la, lb, lc, lt, dc, dc2, dk, dk2
+    for (std::size_t w : {4, 4, 8, 4, 4, 4, 4, 8, 4, 4, 1, 4, 4, 4, 4, 4, 4, 4, 4}) b += ex_round(w * n);
+    b += ex_round(4 * m);
     b += 2 * ex_round(4 * static_cast<std::size_t>(fifo_total) + 4);
     b += ex_round(8 * m) + 2 * ex_round(4 * m) + ex_round(64) + ex_round(8);
     b += tiles * 256 * 4 * 2 + tiles * 64 + (256 << 10);  // sort / scan scratch
@@ -84,15 +91,13 @@ inline std::size_t ex_bytes(std::int64_t N, int M, std::int64_t fifo_total)
 inline bool ex_carve(Scratch& ws, std::int64_t N, int M, std::int64_t fifo_total, ExBuffers& B)
 {
     const std::size_t n = static_cast<std::size_t>(N) + 1, m = static_cast<std::size_t>(M) + 1;
-    B.mnb = ws.take<float>(n);
+    B.rec = ws.take<float4>(n);
+    B.ordRec = ws.take<float4>(n);
     B.key0 = ws.take<std::uint64_t>(n);
     B.key1 = ws.take<std::uint64_t>(n);
     B.pkey = ws.take<std::uint64_t>(n);
     B.val0 = ws.take<std::uint32_t>(n);
     B.val1 = ws.take<std::uint32_t>(n);
-    B.ordL = ws.take<std::uint32_t>(n);
-    B.ordF0 = ws.take<float>(n);
-    B.ordMnb = ws.take<float>(n);
     B.cuts = ws.take<float>(n);
     B.cut_member = ws.take<std::int32_t>(n);
     B.cand = ws.take<std::uint8_t>(n);
@@ -112,6 +117,26 @@ inline bool ex_carve(Scratch& ws, std::int64_t N, int M, std::int64_t fifo_total
     B.stamp = ws.take<std::uint32_t>(n);
     B.gfv = ws.take<float>(static_cast<std::size_t>(fifo_total) + 1);
     B.gfc = ws.take<std::uint32_t>(static_cast<std::size_t>(fifo_total) + 1);
+    B.sw.cst = ws.take<std::uint32_t>(n);
+    B.sw.ev_st = ws.take<std::uint32_t>(n);
+    B.sw.ev_hi = ws.take<std::uint64_t>(n);
+    B.sw.ev_val = ws.take<float>(n);
+    B.sw.mk_c = ws.take<std::uint32_t>(n);
+    B.sw.mk_t = ws.take<std::uint32_t>(n);
+    B.sw.te_st = ws.take<std::uint32_t>(n);
+    B.sw.te_hi = ws.take<std::uint64_t>(n);
+    B.sw.te_lo = ws.take<std::uint32_t>(n);
+    B.sw.te_val = ws.take<float>(n);
+    B.sw.te_k = ws.take<std::uint8_t>(n);
+    B.sw.la = ws.take<std::uint32_t>(n);
+    B.sw.lb = ws.take<std::uint32_t>(n);
+    B.sw.lc = ws.take<std::uint32_t>(n);
+    B.sw.lt = ws.take<std::uint32_t>(n);
+    B.sw.dc = ws.take<std::uint32_t>(n);
+    B.sw.dc2 = ws.take<std::uint32_t>(n);
+    B.sw.dk = ws.take<float>(n);
+    B.sw.dk2 = ws.take<float>(n);
+    B.sw_ctr = ws.take<std::uint32_t>(m);
     B.nsorted = ws.take<std::int64_t>(m);
     B.ncut = ws.take<int>(m);
     B.cut_base = ws.take<int>(m);
@@ -124,13 +149,12 @@ __device__ __forceinline__ WinGrid ex_member_grid(const ExMember& M, int m, cons
                                                   const float* F0, const ExBuffers& B)
 {
     const int cb = B.cut_base[m];
-    return WinGrid{M.nr, M.nc, M.per_ns != 0, M.per_ew != 0, M.L, M.Ld, M.eps, z + M.base, F0 + M.base,
-                   B.mnb + M.base, kind + M.base, B.ordL + M.base, B.ordF0 + M.base, B.ordMnb + M.base,
+    return WinGrid{M.nr, M.nc, M.per_ns != 0, M.per_ew != 0, M.L, M.Ld, M.eps, B.rec + M.base, B.ordRec + M.base,
                    B.nsorted[m], B.cuts + cb, B.cand + cb, B.ncut[m]};
 }
 
-// 1. Per cell: the smallest F0 among valid neighbours (-inf for seeds, +inf
-// for cells never queued), the cell sort key (member, F0; 2^32-1 puts
+// 1. Per cell: the replay record {z, F0, smallest F0 among valid neighbours
+// (-inf for seeds), valid}, the cell sort key (member, F0; 2^32-1 puts
 // invalid and NaN cells last in their member) and the pour-level key.
 // 256-thread blocks over the packed cells (a block never spans two members).
 __global__ void ex_prep(const ExMember* __restrict__ mem, const std::uint16_t* __restrict__ blk_member,
@@ -156,7 +180,7 @@ __global__ void ex_prep(const ExMember* __restrict__ mem, const std::uint16_t* _
         std::uint32_t plev = 0xffffffffu;
         if (!valid)
         {
-            B.mnb[i] = INFINITY;
+            B.rec[i] = make_float4(0.0f, 0.0f, INFINITY, 0.0f);
             B.key0[i] = hi | 0xffffffffull;
         }
         else
@@ -178,7 +202,7 @@ __global__ void ex_prep(const ExMember* __restrict__ mem, const std::uint16_t* _
                 mn = fminf(mn, fj);
                 if (zi <= f && zj == fj && fj == f) pour = true;
             }
-            B.mnb[i] = (kind[i] == 2) ? -INFINITY : mn;
+            B.rec[i] = make_float4(zi, f, (kind[i] == 2) ? -INFINITY : mn, 1.0f);
             if (pour) plev = float_order_key(f);
         }
         B.pkey[i] = hi | plev;
@@ -252,11 +276,10 @@ __global__ void ex_candidates(std::int64_t N, ExBuffers B)
     if (c) B.wl[atomicAdd(&B.u[1], 1u)] = static_cast<std::int32_t>(k);
 }
 
-// 4. Sorted-order copies: member-local cell, F0 and mnb per sorted position
-// (a member's sorted cells occupy its own packed range).
+// 4. Sorted-order records {F0, mnb, member-local cell, 0} per sorted
+// position (a member's sorted cells occupy its own packed range).
 __global__ void ex_gather(const ExMember* __restrict__ mem, const std::uint16_t* __restrict__ blk_member,
-                          std::int64_t N, const std::uint32_t* __restrict__ ord, const float* __restrict__ F0,
-                          ExBuffers B)
+                          std::int64_t N, const std::uint32_t* __restrict__ ord, ExBuffers B)
 {
     LSDTT_COUNT();
     const std::int64_t p = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -264,9 +287,8 @@ __global__ void ex_gather(const ExMember* __restrict__ mem, const std::uint16_t*
     const ExMember M = mem[m];
     if (p >= N || p - M.base >= B.nsorted[m]) return;
     const std::uint32_t c = ord[p];
-    B.ordL[p] = static_cast<std::uint32_t>(c - M.base);
-    B.ordF0[p] = F0[c];
-    B.ordMnb[p] = B.mnb[c];
+    const float4 q = B.rec[c];
+    B.ordRec[p] = make_float4(q.y, q.z, __uint_as_float(static_cast<std::uint32_t>(c - M.base)), 0.0f);
 }
 
 // F before the windows write their raised cells: every valid cell at its own
@@ -354,27 +376,37 @@ __global__ void ex_overflow_list(std::int64_t N, ExBuffers B)
     if (B.status[g] == kWinOverflow) B.wl2[atomicAdd(&B.u[3], 1u)] = g;
 }
 
-// 6. The chain of each member, one warp per member (block m): from the
-// lowest cut each window names the next valid start. A window on the chain
-// that neither shared-memory size held is replayed here: first with its FIFO
-// and heap in this block's shared memory (FQ_C, DH_C) and seen cells marked
-// by per-cell stamps, then, if that too overflows, with everything in global
-// memory; either way writing its raised cells straight into F. u[5] records
-// a failure (1: a global replay outgrew its arrays; 2: the chain did not
-// advance).
+// 6. The chain of each member, one block of kSwThreads per member (block m):
+// from the lowest cut each window names the next valid start. A window on
+// the chain that neither shared-memory size held is replayed here by the
+// whole block, one FIFO sweep at a time (fill_sweep.cuh); a sweep whose FIFO
+// outgrows the block's shared memory sends the window to the sequential
+// rules, run by warp 0 with the heap (DH_C) and FIFO (FQ_C) in the same
+// shared memory, or past that in global memory. Either way the window's
+// raised cells go straight into F. u[5] records a failure (1: a global
+// replay outgrew its arrays; 2: the chain did not advance).
 template <int FQ_C, int DH_C>
-__global__ void __launch_bounds__(32) ex_chain(const ExMember* __restrict__ mem, const float* __restrict__ z,
-                                               const std::uint8_t* __restrict__ kind, const float* __restrict__ F0,
-                                               float* __restrict__ F, ExBuffers B)
+__global__ void __launch_bounds__(kSwThreads) ex_chain(const ExMember* __restrict__ mem, const float* __restrict__ z,
+                                                       const std::uint8_t* __restrict__ kind,
+                                                       const float* __restrict__ F0, float* __restrict__ F,
+                                                       ExBuffers B)
 {
     LSDTT_COUNT();
     extern __shared__ __align__(16) unsigned char ex_csmem[];
-    const int lane = threadIdx.x & 31;
+    const int tid = threadIdx.x, lane = tid & 31;
     const int m = blockIdx.x;
     const ExMember M = mem[m];
     if (!M.on) return;
     const WinGrid G = ex_member_grid(M, m, z, kind, F0, B);
     const int cb = B.cut_base[m];
+    SweepShared& sh = *reinterpret_cast<SweepShared*>(ex_csmem);
+    SweepBufs sb = B.sw;
+    {
+        const std::int64_t o = M.base;
+        sb.cst += o; sb.ev_st += o; sb.ev_hi += o; sb.ev_val += o; sb.mk_c += o; sb.mk_t += o; sb.te_st += o;
+        sb.te_hi += o; sb.te_lo += o; sb.te_val += o; sb.te_k += o; sb.la += o; sb.lb += o; sb.lc += o;
+        sb.lt += o; sb.dc += o; sb.dc2 += o; sb.dk += o; sb.dk2 += o;
+    }
     WinStore mid{};
     mid.fv = reinterpret_cast<float*>(ex_csmem);
     mid.fc = reinterpret_cast<std::uint32_t*>(mid.fv + FQ_C);
@@ -391,43 +423,67 @@ __global__ void __launch_bounds__(32) ex_chain(const ExMember* __restrict__ mem,
     big.hz = B.ghz + M.base;
     big.hc = B.ghc + M.base;
     big.hcap = static_cast<std::uint32_t>(static_cast<std::int64_t>(M.nr) * M.nc);
-    std::uint32_t stamp_id = 0;
+    __shared__ std::uint32_t s_ctr;
+    __shared__ int s_nx, s_fail;
+    if (tid == 0)
+    {
+        s_ctr = B.sw_ctr[m];
+        s_fail = 0;
+    }
+    __syncthreads();
     int w = 0;
     while (w < G.ncut)
     {
         int nx;
         if (B.status[cb + w] != kWinOk)
         {
-            // a replay that overflows may have written some raised cells
-            // already; the one that completes writes every one of them again
-            mid.stamp_id = ++stamp_id;
-            WinResult r = win_replay(G, w, mid, 0);
-            if (r.status != kWinOk)
+            int sn = G.ncut;
+            const int rs = win_sweep_replay(G, w, sb, F + M.base, &s_ctr, sh, &sn);
+            if (rs == kWinOk)
+                nx = sn;
+            else
             {
-                big.stamp_id = ++stamp_id;
-                r = win_replay(G, w, big, 0);
+                // the sequential rules, by warp 0 (the same shared memory)
+                if (tid < 32)
+                {
+                    // seen-set stamps unique per window and attempt
+                    mid.stamp_id = 2u * static_cast<std::uint32_t>(w) + 1u;
+                    WinResult r = win_replay(G, w, mid, 0);
+                    if (r.status != kWinOk)
+                    {
+                        big.stamp_id = 2u * static_cast<std::uint32_t>(w) + 2u;
+                        r = win_replay(G, w, big, 0);
+                    }
+                    if (lane == 0)
+                    {
+                        s_nx = r.next;
+                        s_fail = r.status != kWinOk ? 1 : 0;
+                    }
+                }
+                __syncthreads();
+                if (s_fail)
+                {
+                    if (tid == 0) atomicExch(&B.u[5], 1u);
+                    return;
+                }
+                nx = s_nx;
             }
-            if (r.status != kWinOk)
-            {
-                if (lane == 0) atomicExch(&B.u[5], 1u);
-                return;
-            }
-            nx = r.next;
-            if (lane == 0) B.chain[cb + w] = 2;
+            if (tid == 0) B.chain[cb + w] = 2;
         }
         else
         {
             nx = B.next[cb + w];
-            if (lane == 0) B.chain[cb + w] = 1;
+            if (tid == 0) B.chain[cb + w] = 1;
         }
-        __syncwarp();
+        __syncthreads();
         if (nx <= w)  // a window always ends above its start
         {
-            if (lane == 0) atomicExch(&B.u[5], 2u);
+            if (tid == 0) atomicExch(&B.u[5], 2u);
             return;
         }
         w = nx;
     }
+    if (tid == 0) B.sw_ctr[m] = s_ctr;
 }
 
 // 7. Staged raised cells of the chain windows into F, one warp per window.
@@ -452,7 +508,8 @@ constexpr int kExB_FQ = 1024, kExB_DH = 4096, kExB_HS = 8192, kExB_OC = 4096;
 constexpr std::size_t kExSmemA = 8 * kExA_FQ + 8 * kExA_DH + 4 * kExA_HS + 8 * kExA_OC;
 constexpr std::size_t kExSmemB = 8 * kExB_FQ + 8 * kExB_DH + 4 * kExB_HS + 8 * kExB_OC;
 constexpr int kExC_FQ = 4096, kExC_DH = 20480;
-constexpr std::size_t kExSmemC = 8 * kExC_FQ + 8 * kExC_DH;
+constexpr std::size_t kExSmemC =
+    (8 * kExC_FQ + 8 * kExC_DH) > sizeof(SweepShared) ? (8 * kExC_FQ + 8 * kExC_DH) : sizeof(SweepShared);
 
 // Opt the larger replay sizes into their shared memory (current device).
 inline cudaError_t ex_setup()
@@ -481,15 +538,21 @@ inline cudaError_t ex_run(const ExMember* mem, const std::uint16_t* blk_member, 
     if (e == cudaSuccess) e = cudaMemsetAsync(B.ncut, 0, sizeof(int) * M, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(B.diff, 0, sizeof(int) * (static_cast<std::size_t>(N) + 1), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(B.stamp, 0, sizeof(std::uint32_t) * static_cast<std::size_t>(N), st);
+    // the block replay's stamps and counters start from zero on every run
+    for (std::uint32_t* a : {B.sw.cst, B.sw.ev_st, B.sw.mk_c, B.sw.mk_t, B.sw.te_st})
+        if (e == cudaSuccess) e = cudaMemsetAsync(a, 0, sizeof(std::uint32_t) * static_cast<std::size_t>(N), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(B.sw_ctr, 0, sizeof(std::uint32_t) * M, st);
     if (e != cudaSuccess) return e;
     ex_prep<<<nb, 256, 0, st>>>(mem, blk_member, N, z, kind, F0, B);
     // distinct pour levels (the cell keys stay in key0/val0 meanwhile)
     const int bits = 32 + mbits;
-    int r = radix_sort_pairs(B.pkey, B.ordL, B.key1, B.val1, N, bits, ws, st, &e);
+    // (the values carried by that sort are not used; wl2, off and cnt are
+    // free until the replays)
+    int r = radix_sort_pairs(B.pkey, reinterpret_cast<std::uint32_t*>(B.wl2), B.key1, B.val1, N, bits, ws, st, &e);
     if (e != cudaSuccess) return e;
     const std::uint64_t* lk = r ? B.key1 : B.pkey;
-    std::uint32_t* flag = reinterpret_cast<std::uint32_t*>(B.ordF0);
-    std::uint32_t* pos = reinterpret_cast<std::uint32_t*>(B.ordMnb);
+    std::uint32_t* flag = B.off;
+    std::uint32_t* pos = B.cnt;
     ex_level_flags<<<nb, 256, 0, st>>>(lk, N, flag);
     e = exclusive_scan<std::uint32_t, std::uint32_t>(flag, N, pos, B.u, ws, st);
     if (e != cudaSuccess) return e;
@@ -504,7 +567,7 @@ inline cudaError_t ex_run(const ExMember* mem, const std::uint16_t* blk_member, 
     // the valid cells of each member by (F0, index)
     r = radix_sort_pairs(B.key0, B.val0, B.key1, B.val1, N, bits, ws, st, &e);
     if (e != cudaSuccess) return e;
-    ex_gather<<<nb, 256, 0, st>>>(mem, blk_member, N, r ? B.val1 : B.val0, F0, B);
+    ex_gather<<<nb, 256, 0, st>>>(mem, blk_member, N, r ? B.val1 : B.val0, B);
     ex_base<<<nb, 256, 0, st>>>(mem, blk_member, N, z, kind, F);
     // replays: small shared-memory size, then the larger one for overflows
     ex_windows<kExA_FQ, kExA_DH, kExA_HS, kExA_OC><<<sms * 16, 32, kExSmemA, st>>>(
@@ -512,7 +575,7 @@ inline cudaError_t ex_run(const ExMember* mem, const std::uint16_t* blk_member, 
     ex_overflow_list<<<nb, 256, 0, st>>>(N, B);
     ex_windows<kExB_FQ, kExB_DH, kExB_HS, kExB_OC><<<sms * 2, 32, kExSmemB, st>>>(
         mem, z, kind, F0, B, B.wl2, B.u + 3, B.u + 4, static_cast<unsigned long long>(N), 16ull * kExB_HS);
-    ex_chain<kExC_FQ, kExC_DH><<<M, 32, kExSmemC, st>>>(mem, z, kind, F0, F, B);
+    ex_chain<kExC_FQ, kExC_DH><<<M, kSwThreads, kExSmemC, st>>>(mem, z, kind, F0, F, B);
     ex_commit<<<static_cast<unsigned>(std::max<std::int64_t>(1, std::min<std::int64_t>(N / 8, sms * 64))), 256, 0,
                 st>>>(mem, N, F, B);
     return cudaGetLastError();

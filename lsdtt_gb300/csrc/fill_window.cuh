@@ -70,33 +70,32 @@ __host__ __device__ __forceinline__ float float_from_order_key(std::uint32_t k)
 }
 
 // One grid (or one ensemble member) as the window replay sees it; every
-// pointer and cell index is member-local.
+// pointer and cell index is member-local. Per cell one 16-byte record
+// {z, F0 (epsilon-0 fill), mnb (min F0 over valid neighbours; -inf for
+// seeds, +inf for cells never queued), class (0 invalid or NaN, 1 valid)};
+// per sorted position {F0, mnb, cell, -} over the valid cells by
+// (F0, index): one load gives a replay all it needs of a cell.
 struct WinGrid
 {
     int nr, nc;
     bool per_ns, per_ew;
     float L, Ld, eps;
-    const float* z;
-    const float* F0;            // epsilon-0 fill
-    const float* mnb;           // min F0 over valid neighbours; -inf for seeds
-    const std::uint8_t* kind;   // 0 invalid, 1 free, 2 seed or NaN
-    const std::uint32_t* ord;   // valid non-NaN cells by (F0, index)
-    const float* ordF0;         // F0 in that order
-    const float* ordMnb;        // mnb in that order
+    const float4* rec;
+    const float4* ordRec;
     std::int64_t nsorted;
     const float* cuts;          // sorted distinct pour levels
     const std::uint8_t* cand;   // candidate window start per cut
     int ncut;
 };
 
-// first k in [0, n) with a[k] >= v (n if none)
-__device__ __forceinline__ std::int64_t win_lower_bound(const float* a, std::int64_t n, float v)
+// first sorted position with F0 >= v (n if none)
+__device__ __forceinline__ std::int64_t win_lower_bound(const float4* a, std::int64_t n, float v)
 {
     std::int64_t lo = 0, hi = n;
     while (lo < hi)
     {
         const std::int64_t mid = (lo + hi) >> 1;
-        if (a[mid] < v) lo = mid + 1;
+        if (a[mid].x < v) lo = mid + 1;
         else hi = mid;
     }
     return lo;
@@ -192,17 +191,11 @@ __device__ __forceinline__ std::uint32_t win_hash(std::uint32_t x, std::uint32_t
     return (x * 2654435761u) & mask;
 }
 
-// Insert `cell` into the seen set; false if it was there already (or the set
-// is full: *full is set).
+// Insert `cell` into the shared-memory seen set; false if it was there
+// already (or the set is full: *full is set).
 __device__ __forceinline__ bool win_seen_insert(const WinStore& s, std::uint32_t cell, std::uint32_t* count,
                                                 bool* full)
 {
-    if (s.stamp)
-    {
-        if (s.stamp[cell] == s.stamp_id) return false;
-        s.stamp[cell] = s.stamp_id;
-        return true;
-    }
     const std::uint32_t mask = s.hscap - 1;
     std::uint32_t h = win_hash(cell, mask);
     for (std::uint32_t probe = 0; probe < s.hscap; ++probe)
@@ -247,7 +240,11 @@ __device__ WinResult win_replay(const WinGrid& G, int w, const WinStore& s, std:
     if (s.hs)
         for (std::uint32_t k = lane; k < s.hscap; k += 32) s.hs[k] = kWinNone;
     __syncwarp();
-    std::int64_t p = win_lower_bound(G.ordF0, G.nsorted, S);
+    std::int64_t p = win_lower_bound(G.ordRec, G.nsorted, S);
+    bool rescan = true;  // the list head below is stale
+    bool have_l = false;
+    float lz = INFINITY;
+    std::uint32_t lc = kWinNone;
     std::uint32_t head = 0, tail = 0, hsize = 0, nout = 0;
     float V = S;
     int cnext = w + 1;  // first cut > V
@@ -256,27 +253,35 @@ __device__ WinResult win_replay(const WinGrid& G, int w, const WinStore& s, std:
     const std::uint32_t fmask = s.fcap - 1;
     for (;;)
     {
-        // the list head: next sorted cell queued at the window start
-        while (p < G.nsorted)
+        // the list head: next sorted cell queued at the window start (kept
+        // in registers until the list is popped)
+        if (rescan)
         {
-            const std::int64_t q = p + lane;
-            const bool ok = q < G.nsorted && G.ordMnb[q] < S;
-            const unsigned b = __ballot_sync(0xffffffffu, ok);
-            if (b)
+            have_l = false;
+            while (p < G.nsorted)
             {
-                p += __ffs(b) - 1;
-                break;
+                const std::int64_t q = p + lane;
+                float4 o = make_float4(0.0f, INFINITY, 0.0f, 0.0f);
+                if (q < G.nsorted) o = G.ordRec[q];
+                const unsigned b = __ballot_sync(0xffffffffu, o.y < S);
+                if (b)
+                {
+                    const int k = __ffs(b) - 1;
+                    p += k;
+                    lz = __shfl_sync(0xffffffffu, o.x, k);
+                    lc = __float_as_uint(__shfl_sync(0xffffffffu, o.z, k));
+                    have_l = true;
+                    break;
+                }
+                p += 32;
             }
-            p += 32;
-        }
-        if (p > G.nsorted) p = G.nsorted;
-        const bool have_l = p < G.nsorted;
-        float lz = INFINITY;
-        std::uint32_t lc = kWinNone;
-        if (have_l)
-        {
-            lz = G.ordF0[p];
-            lc = G.ord[p];
+            if (p > G.nsorted) p = G.nsorted;
+            if (!have_l)
+            {
+                lz = INFINITY;
+                lc = kWinNone;
+            }
+            rescan = false;
         }
         // heap minimum (list head or discovered heap top)
         float hmz = lz;
@@ -354,7 +359,10 @@ __device__ WinResult win_replay(const WinGrid& G, int w, const WinStore& s, std:
                 s.out_F[cur_c] = cur_v;
         }
         else if (src == 0)
+        {
             ++p;
+            rescan = true;
+        }
         else
         {
             if (lane == 0) win_heap_pop(s, hsize);
@@ -377,19 +385,19 @@ __device__ WinResult win_replay(const WinGrid& G, int w, const WinStore& s, std:
         std::uint32_t j = kWinNone;
         bool fresh = false;
         float zj = 0.0f;
+        std::uint32_t sv = 0;  // the cell's stamp (large tier), loaded beside its record
         if (lane < 8)
         {
             int rr, cc;
             if (fill_nb(G.nr, G.nc, G.per_ns, G.per_ew, r, c, lane, rr, cc))
             {
                 const std::uint32_t jj = static_cast<std::uint32_t>(rr) * G.nc + cc;
-                if (G.kind[jj] != 0)
-                {
-                    zj = G.z[jj];
-                    // open: not popped before the window (F0 >= S), not
-                    // queued at its start (mnb >= S)
-                    if (!isnan(zj) && G.F0[jj] >= S && !(G.mnb[jj] < S)) j = jj;
-                }
+                const float4 q = G.rec[jj];
+                if (s.stamp) sv = s.stamp[jj];
+                zj = q.x;
+                // open: valid, not popped before the window (F0 >= S), not
+                // queued at its start (mnb >= S)
+                if (q.w != 0.0f && q.y >= S && !(q.z < S)) j = jj;
             }
         }
         // a neighbour reached twice through a periodic wrap counts once
@@ -398,7 +406,16 @@ __device__ WinResult win_replay(const WinGrid& G, int w, const WinStore& s, std:
             const std::uint32_t other = __shfl_sync(0xffffffffu, j, k);
             if (lane > k && j != kWinNone && other == j) j = kWinNone;
         }
-        if (j != kWinNone) fresh = win_seen_insert(s, j, &sh_seen_count[wib], &sh_full[wib]);
+        if (j != kWinNone)
+        {
+            if (s.stamp)
+            {
+                fresh = sv != s.stamp_id;
+                if (fresh) s.stamp[j] = s.stamp_id;
+            }
+            else
+                fresh = win_seen_insert(s, j, &sh_seen_count[wib], &sh_full[wib]);
+        }
         __syncwarp();
         if (sh_full[wib])
         {

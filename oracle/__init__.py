@@ -69,6 +69,24 @@ class _Lib:
             raise OracleError(err.value.decode())
         return out
 
+    def fill_pits_index_ties(self, z, mask, cell, bc="oooo", min_slope=1e-4, nodata=-9999.0):
+        """The priority flood with heap entries of equal value taken in
+        (row, col) order (the oracle only; the reference's heap orders them
+        by its layout). The GPU fill follows this rule."""
+        z = np.ascontiguousarray(z, dtype=np.float32)
+        mask = np.ascontiguousarray(mask, dtype=np.uint8)
+        nr, nc = z.shape
+        out = np.empty_like(z)
+        err = ctypes.create_string_buffer(1024)
+        f = self.fn("fill_pits_index_ties")
+        f.restype = ctypes.c_int
+        rc = f(_p(z, _c_f32), _p(mask, _c_u8), ctypes.c_int(nr), ctypes.c_int(nc),
+               ctypes.c_double(cell), ctypes.c_double(nodata), bc.encode(),
+               ctypes.c_float(min_slope), _p(out, _c_f32), err, ctypes.c_int(1024))
+        if rc != 0:
+            raise OracleError(err.value.decode())
+        return out
+
     # --------------------------------------------------------------- D8 engine
     def flowinfo(self, z, mask, cell, bc="oooo", interior_nodata_is_outlet=True,
                  allow_pits_as_outlets=False, build_topo=True, build_sv=True,

@@ -74,9 +74,18 @@ struct Node
 // with a comparator that looks at zeta alone (:55-62): ties fall wherever
 // libstdc++'s push_heap/pop_heap leave them, and the restatement performs the
 // same push/pop sequence, so it leaves them in the same places.
+//
+// With index_ties, equal keys are ordered by (row, col) instead: the rule the
+// GPU fill uses (a parallel fill cannot reproduce a binary heap's layout).
+// That variant is a test instrument, not a restatement of the reference.
 struct NodeGreater
 {
-    bool operator()(const Node& a, const Node& b) const { return a.zeta > b.zeta; }
+    bool index_ties = false;
+    bool operator()(const Node& a, const Node& b) const
+    {
+        if (a.zeta != b.zeta || !index_ties) return a.zeta > b.zeta;
+        return a.row != b.row ? a.row > b.row : a.col > b.col;
+    }
 };
 using Heap = std::priority_queue<Node, std::vector<Node>, NodeGreater>;
 
@@ -90,9 +99,11 @@ struct FillTrace
 };
 
 void priority_flood(std::vector<float>& dem, std::vector<int>& idx, int nr, int nc,
-                    float L, float min_slope, bool per_ns, bool per_ew, FillTrace tr)
+                    float L, float min_slope, bool per_ns, bool per_ew, FillTrace tr, bool index_ties = false)
 {
-    Heap pq;
+    NodeGreater cmp;
+    cmp.index_ties = index_ties;
+    Heap pq(cmp);
 
     // Seeding (:518-589): every non-nodata cell on a non-periodic raster edge,
     // plus cells with an in-bounds nodata neighbour when the interior has any
@@ -799,9 +810,9 @@ extern "C" {
 // equal to its reconstruction backend (docs/design_and_algorithms/
 // flow_routing.md:603-620).
 // ---------------------------------------------------------------------------
-int oracle_fill_pits_traced(const float* z, const std::uint8_t* mask, int nr, int nc, double cell, double nodata,
-                            const char* bc, float min_slope, float* out, std::int64_t* discoverer,
-                            std::int64_t* order, std::uint8_t* via_fifo, char* err, int errlen)
+int oracle_fill_pits_traced_ties(const float* z, const std::uint8_t* mask, int nr, int nc, double cell, double nodata,
+                                 const char* bc, float min_slope, float* out, std::int64_t* discoverer,
+                                 std::int64_t* order, std::uint8_t* via_fifo, int index_ties, char* err, int errlen)
 {
     try
     {
@@ -829,11 +840,20 @@ int oracle_fill_pits_traced(const float* z, const std::uint8_t* mask, int nr, in
         FillTrace tr{discoverer, order, via_fifo};
         if (discoverer) std::fill(discoverer, discoverer + n, static_cast<std::int64_t>(-2));
         if (order) std::fill(order, order + n, static_cast<std::int64_t>(-1));
-        priority_flood(dem, idx, nr, nc, static_cast<float>(cell), min_slope > 0.0f ? min_slope : 0.0f, per_ns, per_ew, tr);
+        priority_flood(dem, idx, nr, nc, static_cast<float>(cell), min_slope > 0.0f ? min_slope : 0.0f, per_ns, per_ew, tr,
+                       index_ties != 0);
         std::memcpy(out, dem.data(), sizeof(float) * n);
         return 0;
     }
     catch (const std::exception& e) { put_err(err, errlen, e.what()); return 1; }
+}
+
+int oracle_fill_pits_traced(const float* z, const std::uint8_t* mask, int nr, int nc, double cell, double nodata,
+                            const char* bc, float min_slope, float* out, std::int64_t* discoverer,
+                            std::int64_t* order, std::uint8_t* via_fifo, char* err, int errlen)
+{
+    return oracle_fill_pits_traced_ties(z, mask, nr, nc, cell, nodata, bc, min_slope, out, discoverer, order, via_fifo,
+                                        0, err, errlen);
 }
 
 int oracle_fill_pits(const float* z, const std::uint8_t* mask, int nr, int nc, double cell, double nodata,
@@ -841,6 +861,14 @@ int oracle_fill_pits(const float* z, const std::uint8_t* mask, int nr, int nc, d
 {
     return oracle_fill_pits_traced(z, mask, nr, nc, cell, nodata, bc, min_slope, out, nullptr, nullptr, nullptr, err,
                                    errlen);
+}
+
+// The fill with heap ties taken in (row, col) order (NodeGreater).
+int oracle_fill_pits_index_ties(const float* z, const std::uint8_t* mask, int nr, int nc, double cell, double nodata,
+                                const char* bc, float min_slope, float* out, char* err, int errlen)
+{
+    return oracle_fill_pits_traced_ties(z, mask, nr, nc, cell, nodata, bc, min_slope, out, nullptr, nullptr, nullptr,
+                                        1, err, errlen);
 }
 
 // ---------------------------------------------------------------------------

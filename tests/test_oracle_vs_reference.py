@@ -133,3 +133,17 @@ def test_dinf_port_equals_reference(port, ref):
         for n_exp in (1.0, 1.5, 2.0):
             assert _bits_equal(port.dinf_stream_power(f, m, cell, bc, 2e-5, 0.45, n_exp, 500.0),
                                ref.dinf_stream_power(f, m, cell, bc, 2e-5, 0.45, n_exp, 500.0)), (name, n_exp)
+
+
+def test_index_tie_variant_only_changes_ties(port):
+    """The oracle's (row, col) heap-tie variant (the GPU fill's rule) equals
+    the restatement of the reference wherever no two heap entries of equal
+    value compete: on surfaces with continuous random elevations."""
+    from tests import surfaces
+    one = lambda z: np.ones_like(z, np.uint8)  # noqa: E731
+    for z, cell, bc in [(port.noise_tilt_surface(256, 256, 30.0, 1, 0.0, 1.0, "nnon", 0.001), 30.0, "nnon"),
+                        (surfaces.fractal_pits(256), 10.0, "oooo"),
+                        (surfaces.add_pits(surfaces.fractal(96, 112, 150.0, 7), 20, 6), 10.0, "popo")]:
+        a = port.fill_pits(z, one(z), cell, bc, 1e-4)
+        b = port.fill_pits_index_ties(z, one(z), cell, bc, 1e-4)
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
