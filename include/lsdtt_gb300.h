@@ -107,9 +107,11 @@ int lsdtt_gpu_fill_pits(const lsdtt_gpu_grid* grid, const float* z_dev, const ui
  * memory -- a host framework that has reserved the device's memory for its
  * own allocator, or a latency-critical loop where a growing or failing
  * stream-ordered allocation is unacceptable. Its working memory is one
- * fixed array inside the library (16 MiB + 64 KiB, held on every device
- * that loads the library), so grids are limited to about 4096 x 4096 cells;
- * larger grids return LSDTT_GPU_EINVAL. Same results as
+ * fixed array inside the library (64 MiB + 64 KiB, held on every device
+ * that loads the library), so grids are limited to about 8192 x 8192 cells
+ * at min_slope <= 0 and, because the raised cells' reference order needs
+ * about 190 bytes a cell of replay buffers, about 590 x 590 cells at
+ * min_slope > 0; larger grids return LSDTT_GPU_EINVAL. Same results as
  * lsdtt_gpu_fill_pits. The first call on a device looks up the array's
  * device address: make it before any stream capture. All calls share the
  * array, so calls that overlap on the GPU race; order them on one stream. */

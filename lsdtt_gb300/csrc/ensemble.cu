@@ -2733,7 +2733,21 @@ int lsdtt_gpu_ensemble_create(const lsdtt_gpu_member* members, int32_t n_members
         return cuda_fail(e, who);
     }
     cudaMemcpyAsync(E->d_pm, E->pm.data(), sizeof(PackedMember) * n_members, cudaMemcpyHostToDevice, st);
-    if (E->d_exm) cudaMemcpyAsync(E->d_exm, exm.data(), sizeof(ExMember) * n_members, cudaMemcpyHostToDevice, st);
+    std::vector<std::int32_t> chain_order(static_cast<std::size_t>(n_members));
+    if (E->d_exm)
+    {
+        cudaMemcpyAsync(E->d_exm, exm.data(), sizeof(ExMember) * n_members, cudaMemcpyHostToDevice, st);
+        // the exact fill's chain blocks, largest members first (their long
+        // episodes set the fill's time; the rest finish around them)
+        for (int k = 0; k < n_members; ++k) chain_order[static_cast<std::size_t>(k)] = k;
+        std::stable_sort(chain_order.begin(), chain_order.end(), [&](std::int32_t a, std::int32_t b) {
+            const PackedMember &A = E->pm[static_cast<std::size_t>(a)], &Bm = E->pm[static_cast<std::size_t>(b)];
+            return static_cast<std::int64_t>(A.nr) * A.nc > static_cast<std::int64_t>(Bm.nr) * Bm.nc;
+        });
+        cudaMemcpyAsync(E->exB.chain_order, chain_order.data(), sizeof(std::int32_t) * n_members,
+                        cudaMemcpyHostToDevice, st);
+        cudaStreamSynchronize(st);  // chain_order is a local vector
+    }
     cudaMemcpyAsync(E->d_prm, E->prm_h.data(), sizeof(EnsParams) * n_members, cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(E->blk_member, blk.data(), sizeof(std::uint16_t) * blk.size(), cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(E->tile_member, tm.data(), sizeof(std::uint16_t) * tm.size(), cudaMemcpyHostToDevice, st);

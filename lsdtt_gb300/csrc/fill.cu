@@ -227,11 +227,22 @@ cudaError_t relax_fill(int nr, int nc, bool per_ns, bool per_ew, float L, float 
     return e;
 }
 
+// Bytes the exact-fill stages need for one nr x nc grid (beyond F0).
+std::size_t exact_single_bytes(std::int64_t n)
+{
+    const std::int64_t N = (n + 255) / 256 * 256;
+    std::int64_t fcap = 2;
+    while (fcap < n) fcap <<= 1;
+    return ex_round(sizeof(ExMember)) + ex_round(sizeof(std::uint16_t) * static_cast<std::size_t>(N / 256)) +
+           ex_bytes(N, 1, fcap);
+}
+
 // The fill in the reference's order for one grid: the exact-fill stages with
-// a single member. F holds the epsilon relaxation on entry.
-cudaError_t exact_fill_single(int nr, int nc, bool per_ns, bool per_ew, float L, float Ld, float eps, float nodata,
-                              const float* z, const std::uint8_t* kind, const float* F0, float* F, cudaStream_t st,
-                              unsigned* failure)
+// a single member, in the caller's buffer `buf` of exact_single_bytes(n)
+// bytes. F holds the epsilon relaxation on entry. Allocates nothing.
+cudaError_t exact_fill_single_in(int nr, int nc, bool per_ns, bool per_ew, float L, float Ld, float eps, float nodata,
+                                 const float* z, const std::uint8_t* kind, const float* F0, float* F, char* buf,
+                                 cudaStream_t st, unsigned* failure)
 {
     *failure = 0;
     const std::int64_t n = static_cast<std::int64_t>(nr) * nc;
@@ -252,17 +263,18 @@ cudaError_t exact_fill_single(int nr, int nc, bool per_ns, bool per_ew, float L,
     hm.per_ew = per_ew ? 1 : 0;
     hm.on = 1;
     const std::size_t meta = ex_round(sizeof(ExMember)) + ex_round(sizeof(std::uint16_t) * static_cast<std::size_t>(N / 256));
-    const std::size_t bytes = meta + ex_bytes(N, 1, fcap);
-    char* buf = nullptr;
-    cudaError_t e = cudaMallocAsync(&buf, bytes, st);
-    if (e != cudaSuccess) return e;
+    const std::size_t bytes = exact_single_bytes(n);
     ExMember* mem = reinterpret_cast<ExMember*>(buf);
     std::uint16_t* blk = reinterpret_cast<std::uint16_t*>(buf + ex_round(sizeof(ExMember)));
     Scratch ws{buf + meta, bytes - meta, 0};
     ExBuffers B{};
+    cudaError_t e = cudaSuccess;
     if (!ex_carve(ws, N, 1, fcap, B)) e = cudaErrorMemoryAllocation;
+    // the member table travels by a kernel argument-free path: a host-to-
+    // device copy from pageable memory is synchronous and allocates nothing
     if (e == cudaSuccess) e = cudaMemcpyAsync(mem, &hm, sizeof(ExMember), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(blk, 0, sizeof(std::uint16_t) * static_cast<std::size_t>(N / 256), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(B.chain_order, 0, sizeof(std::int32_t), st);
     if (e == cudaSuccess) e = ex_setup();
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
@@ -272,6 +284,19 @@ cudaError_t exact_fill_single(int nr, int nc, bool per_ns, bool per_ew, float L,
     if (e == cudaSuccess) e = cudaMemcpyAsync(hu, B.u, sizeof(hu), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e == cudaSuccess) *failure = hu[5];
+    return e;
+}
+
+// The same with its buffer allocated (stream-ordered) and released here.
+cudaError_t exact_fill_single(int nr, int nc, bool per_ns, bool per_ew, float L, float Ld, float eps, float nodata,
+                              const float* z, const std::uint8_t* kind, const float* F0, float* F, cudaStream_t st,
+                              unsigned* failure)
+{
+    *failure = 0;
+    char* buf = nullptr;
+    cudaError_t e = cudaMallocAsync(&buf, exact_single_bytes(static_cast<std::int64_t>(nr) * nc), st);
+    if (e != cudaSuccess) return e;
+    e = exact_fill_single_in(nr, nc, per_ns, per_ew, L, Ld, eps, nodata, z, kind, F0, F, buf, st, failure);
     cudaFreeAsync(buf, st);
     return e;
 }
@@ -368,14 +393,18 @@ LSDTT_DEFINE_LAUNCH_READER(fill)
 // budgets every byte itself, or a latency-critical loop where a
 // cudaMallocAsync that has to grow its pool (or fails when the pool is
 // exhausted) is not acceptable. For them this entry point takes its working
-// memory -- the per-cell state plane, the two per-tile activity planes and
-// the convergence flags -- from one fixed array that lives in this file:
+// memory -- the per-cell state plane, the two per-tile activity planes, the
+// convergence flags and, with min_slope > 0, the epsilon-0 fill and the
+// buffers of the window replays that put the raised cells in the
+// reference's order -- from one fixed array that lives in this file:
 //
 //   * The array is a file-scope __device__ variable of kFillNoAllocBytes
-//     (16 MiB + 64 KiB), allocated when the library is loaded and held by
+//     (64 MiB + 64 KiB), allocated when the library is loaded and held by
 //     every GPU that loads it until the process exits.
-//   * It fits grids of up to about 16.7 million cells (4096 x 4096); larger
-//     grids are rejected with LSDTT_GPU_EINVAL before any work is queued.
+//   * With min_slope <= 0 it fits grids of up to about 67 million cells
+//     (8192 x 8192); with min_slope > 0 the replays need about 190 bytes a
+//     cell, so up to about 350,000 cells (590 x 590). Larger grids are
+//     rejected with LSDTT_GPU_EINVAL before any work is queued.
 //   * Host code cannot use the array's name as a device address, so the
 //     first call in each CUDA context looks the address up with
 //     cudaGetSymbolAddress (with that device current) and caches it under
@@ -389,7 +418,7 @@ LSDTT_DEFINE_LAUNCH_READER(fill)
 //     them on one stream or otherwise ordered.
 // The caller still provides the input and output buffers.
 // ---------------------------------------------------------------------------
-static constexpr std::size_t kFillNoAllocBytes = (std::size_t(16) << 20) + (std::size_t(64) << 10);
+static constexpr std::size_t kFillNoAllocBytes = (std::size_t(64) << 20) + (std::size_t(64) << 10);
 static __device__ __align__(256) unsigned char g_fill_noalloc_scratch[kFillNoAllocBytes];
 
 static std::mutex g_fill_noalloc_mu;
@@ -453,16 +482,21 @@ extern "C" int lsdtt_gpu_fill_pits_noalloc(const lsdtt_gpu_grid* grid, const flo
     const int nr = grid->n_rows, nc = grid->n_cols;
     const std::int64_t n = static_cast<std::int64_t>(nr) * nc;
     const std::int64_t ntiles = static_cast<std::int64_t>((nc + kT - 1) / kT) * ((nr + kT - 1) / kT);
+    const float eps = min_slope > 0.0f ? min_slope : 0.0f;
     // Layout inside the fixed array: flags (256 B), two activity planes
-    // (rounded to 256 B), then the per-cell state plane.
+    // (rounded to 256 B), the per-cell state plane, then with min_slope > 0
+    // the epsilon-0 fill and the window replays' buffers.
     const std::size_t dirty_bytes = (static_cast<std::size_t>(2 * ntiles) + 255) & ~std::size_t(255);
-    const std::size_t need = 256 + dirty_bytes + static_cast<std::size_t>(n);
+    const std::size_t kind_bytes = (static_cast<std::size_t>(n) + 255) & ~std::size_t(255);
+    const std::size_t f0_bytes = eps > 0.0f ? (sizeof(float) * static_cast<std::size_t>(n) + 255) & ~std::size_t(255) : 0;
+    const std::size_t need = 256 + dirty_bytes + kind_bytes + f0_bytes + (eps > 0.0f ? exact_single_bytes(n) : 0);
     if (need > kFillNoAllocBytes)
         return fail(LSDTT_GPU_EINVAL, "lsdtt_gpu_fill_pits_noalloc: a " + std::to_string(nr) + " x " +
                                           std::to_string(nc) + " grid needs " + std::to_string(need) +
                                           " bytes of scratch but the fixed scratch holds " +
                                           std::to_string(kFillNoAllocBytes) +
-                                          " (about 4096 x 4096 cells); use lsdtt_gpu_fill_pits");
+                                          " (about 8192 x 8192 cells at min_slope 0, 590 x 590 above); use "
+                                          "lsdtt_gpu_fill_pits");
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return cuda_fail(e, "lsdtt_gpu_fill_pits_noalloc");
@@ -489,41 +523,61 @@ extern "C" int lsdtt_gpu_fill_pits_noalloc(const lsdtt_gpu_grid* grid, const flo
         base = g_fill_noalloc_addr[dev];
     }
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    int* flags = static_cast<int*>(base);  // [0] interior nodata, [1] changed
-    std::uint8_t* dirty = static_cast<std::uint8_t*>(base) + 256;
-    std::uint8_t* kind = static_cast<std::uint8_t*>(base) + 256 + dirty_bytes;
-    // The previous call's contents are stale: reset flags and activity.
-    cudaMemsetAsync(flags, 0, sizeof(int) * 2, st);
-    cudaMemsetAsync(dirty, 1, static_cast<std::size_t>(2 * ntiles), st);
-    fill_interior_nodata<<<grid_blocks(n, 256), 256, 0, st>>>(nr, nc, z_dev, mask_dev, grid->no_data_value, flags);
-    fill_init<<<grid_blocks(n, 256), 256, 0, st>>>(nr, nc, per_ns, per_ew, z_dev, mask_dev, grid->no_data_value, flags,
-                                                  out_dev, kind);
+    char* cbase = static_cast<char*>(base);
+    int* flags = reinterpret_cast<int*>(cbase);  // [0] interior nodata, [1] changed
+    std::uint8_t* dirty = reinterpret_cast<std::uint8_t*>(cbase + 256);
+    std::uint8_t* kind = reinterpret_cast<std::uint8_t*>(cbase + 256 + dirty_bytes);
+    float* F0 = eps > 0.0f ? reinterpret_cast<float*>(cbase + 256 + dirty_bytes + kind_bytes) : nullptr;
+    char* exbuf = cbase + 256 + dirty_bytes + kind_bytes + f0_bytes;
     const float L = static_cast<float>(grid->cell_size);
     const float Ld = L * static_cast<float>(1.4142135623730950488);
-    const float eps = min_slope > 0.0f ? min_slope : 0.0f;
     const dim3 block(32, 8);
     const dim3 tiles((nc + kT - 1) / kT, (nr + kT - 1) / kT);
     const int kCheckEvery = 4;
     const long max_pass = 4L * (nr + nc) + 64;
-    long pass = 0;
-    int changed = 0;  // pageable host word: the read-back allocates nothing
-    for (;;)
-    {
-        cudaMemsetAsync(flags + 1, 0, sizeof(int), st);
-        const unsigned colours = fill_colour_mask(static_cast<int>(tiles.x), static_cast<int>(tiles.y), per_ns, per_ew);
-        for (int k = 0; k < kCheckEvery; ++k, ++pass)
-            for (int c = 0; c < kFillColours; ++c)
-            {
-                if (!((colours >> c) & 1u)) continue;
-                fill_relax<<<tiles, block, 0, st>>>(nr, nc, per_ns, per_ew, L, Ld, eps, z_dev, kind, out_dev,
-                                                    flags + 1, dirty + (pass & 1) * ntiles,
-                                                    dirty + ((pass + 1) & 1) * ntiles, c);
-            }
-        e = cudaMemcpyAsync(&changed, flags + 1, sizeof(int), cudaMemcpyDeviceToHost, st);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-        if (e != cudaSuccess) return cuda_fail(e, "lsdtt_gpu_fill_pits_noalloc");
-        if (changed == 0) break;
-        if (pass > max_pass) return fail(LSDTT_GPU_ETIMEOUT, "lsdtt_gpu_fill_pits_noalloc: relaxation did not converge");
-    }
+    // one relaxation with raise step `step` into F; the previous call's
+    // contents of the array are stale, so flags and activity are reset
+    auto relax = [&](float step, float* F) -> int {
+        cudaMemsetAsync(flags, 0, sizeof(int) * 2, st);
+        cudaMemsetAsync(dirty, 1, static_cast<std::size_t>(2 * ntiles), st);
+        fill_interior_nodata<<<grid_blocks(n, 256), 256, 0, st>>>(nr, nc, z_dev, mask_dev, grid->no_data_value, flags);
+        fill_init<<<grid_blocks(n, 256), 256, 0, st>>>(nr, nc, per_ns, per_ew, z_dev, mask_dev, grid->no_data_value,
+                                                      flags, F, kind);
+        long pass = 0;
+        int changed = 0;  // pageable host word: the read-back allocates nothing
+        for (;;)
+        {
+            cudaMemsetAsync(flags + 1, 0, sizeof(int), st);
+            const unsigned colours =
+                fill_colour_mask(static_cast<int>(tiles.x), static_cast<int>(tiles.y), per_ns, per_ew);
+            for (int k = 0; k < kCheckEvery; ++k, ++pass)
+                for (int c = 0; c < kFillColours; ++c)
+                {
+                    if (!((colours >> c) & 1u)) continue;
+                    fill_relax<<<tiles, block, 0, st>>>(nr, nc, per_ns, per_ew, L, Ld, step, z_dev, kind, F,
+                                                        flags + 1, dirty + (pass & 1) * ntiles,
+                                                        dirty + ((pass + 1) & 1) * ntiles, c);
+                }
+            cudaError_t re = cudaMemcpyAsync(&changed, flags + 1, sizeof(int), cudaMemcpyDeviceToHost, st);
+            if (re == cudaSuccess) re = cudaStreamSynchronize(st);
+            if (re != cudaSuccess) return cuda_fail(re, "lsdtt_gpu_fill_pits_noalloc");
+            if (changed == 0) return LSDTT_GPU_OK;
+            if (pass > max_pass)
+                return fail(LSDTT_GPU_ETIMEOUT, "lsdtt_gpu_fill_pits_noalloc: relaxation did not converge");
+        }
+    };
+    int s = relax(eps, out_dev);
+    if (s != LSDTT_GPU_OK || eps <= 0.0f) return s;
+    // min_slope > 0: the epsilon-0 fill, then the raised cells in the
+    // reference's order (the replays' buffers carved from the same array)
+    s = relax(0.0f, F0);
+    if (s != LSDTT_GPU_OK) return s;
+    unsigned failure = 0;
+    e = exact_fill_single_in(nr, nc, per_ns, per_ew, L, Ld, eps, static_cast<float>(grid->no_data_value), z_dev, kind,
+                             F0, out_dev, exbuf, st, &failure);
+    if (e != cudaSuccess) return cuda_fail(e, "lsdtt_gpu_fill_pits_noalloc");
+    if (failure)
+        return fail(LSDTT_GPU_EOVERFLOW, failure == 1 ? "lsdtt_gpu_fill_pits_noalloc: a fill window outgrew its arrays"
+                                                      : "lsdtt_gpu_fill_pits_noalloc: the fill window chain did not advance");
     return LSDTT_GPU_OK;
 }

@@ -60,6 +60,7 @@ struct ExBuffers
     std::uint32_t *gfc, *ghc, *stamp;
     SweepBufs sw;           // the block replay's scratch (global cell indices; offset per member)
     std::uint32_t* sw_ctr;  // [M] stamp counters of the block replay
+    std::int32_t* chain_order;  // [M] member of each chain block (largest members first)
     std::int64_t* nsorted;  // [M]
     int *ncut, *cut_base;   // [M], [M + 1]
     unsigned* u;            // [0] total cuts, [1] nwl, [2] work, [3] nwl2, [4] work2, [5] error
@@ -77,9 +78,9 @@ inline std::size_t ex_bytes(std::int64_t N, int M, std::int64_t fifo_total)
     std::size_t b = 0;
     for (std::size_t w : {16, 16, 8, 8, 8, 4, 4, 4, 4, 1, 1, 1, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4})
         b += ex_round(w * n);
-    // block replay: cst, ev_st, ev_hi, ev_val, mk_c, mk_t, te_st, te_hi,
-    // te_lo, te_val, te_k, la, lb, lc, lt, dc, dc2, dk, dk2
-    for (std::size_t w : {4, 4, 8, 4, 4, 4, 4, 8, 4, 4, 1, 4, 4, 4, 4, 4, 4, 4, 4}) b += ex_round(w * n);
+    // block replay: cst, ev, te, te_st, te_k, mk_c, dc, dc2, dk, dk2, fc, fc2, fk, fk2
+    for (std::size_t w : {4, 16, 16, 4, 1, 4, 4, 4, 4, 4, 4, 4, 4, 4}) b += ex_round(w * n);
+    b += ex_round(4 * m);  // chain order
     b += ex_round(4 * m);
     b += 2 * ex_round(4 * static_cast<std::size_t>(fifo_total) + 4);
     b += ex_round(8 * m) + 2 * ex_round(4 * m) + ex_round(64) + ex_round(8);
@@ -118,24 +119,20 @@ inline bool ex_carve(Scratch& ws, std::int64_t N, int M, std::int64_t fifo_total
     B.gfv = ws.take<float>(static_cast<std::size_t>(fifo_total) + 1);
     B.gfc = ws.take<std::uint32_t>(static_cast<std::size_t>(fifo_total) + 1);
     B.sw.cst = ws.take<std::uint32_t>(n);
-    B.sw.ev_st = ws.take<std::uint32_t>(n);
-    B.sw.ev_hi = ws.take<std::uint64_t>(n);
-    B.sw.ev_val = ws.take<float>(n);
-    B.sw.mk_c = ws.take<std::uint32_t>(n);
-    B.sw.mk_t = ws.take<std::uint32_t>(n);
+    B.sw.ev = ws.take<SwEv>(n);
+    B.sw.te = ws.take<SwTe>(n);
     B.sw.te_st = ws.take<std::uint32_t>(n);
-    B.sw.te_hi = ws.take<std::uint64_t>(n);
-    B.sw.te_lo = ws.take<std::uint32_t>(n);
-    B.sw.te_val = ws.take<float>(n);
     B.sw.te_k = ws.take<std::uint8_t>(n);
-    B.sw.la = ws.take<std::uint32_t>(n);
-    B.sw.lb = ws.take<std::uint32_t>(n);
-    B.sw.lc = ws.take<std::uint32_t>(n);
-    B.sw.lt = ws.take<std::uint32_t>(n);
+    B.sw.mk_c = ws.take<std::uint32_t>(n);
     B.sw.dc = ws.take<std::uint32_t>(n);
     B.sw.dc2 = ws.take<std::uint32_t>(n);
     B.sw.dk = ws.take<float>(n);
     B.sw.dk2 = ws.take<float>(n);
+    B.sw.fc = ws.take<std::uint32_t>(n);
+    B.sw.fc2 = ws.take<std::uint32_t>(n);
+    B.sw.fk = ws.take<float>(n);
+    B.sw.fk2 = ws.take<float>(n);
+    B.chain_order = ws.take<std::int32_t>(m);
     B.sw_ctr = ws.take<std::uint32_t>(m);
     B.nsorted = ws.take<std::int64_t>(m);
     B.ncut = ws.take<int>(m);
@@ -394,7 +391,7 @@ __global__ void __launch_bounds__(kSwThreads) ex_chain(const ExMember* __restric
     LSDTT_COUNT();
     extern __shared__ __align__(16) unsigned char ex_csmem[];
     const int tid = threadIdx.x, lane = tid & 31;
-    const int m = blockIdx.x;
+    const int m = B.chain_order[blockIdx.x];
     const ExMember M = mem[m];
     if (!M.on) return;
     const WinGrid G = ex_member_grid(M, m, z, kind, F0, B);
@@ -403,9 +400,20 @@ __global__ void __launch_bounds__(kSwThreads) ex_chain(const ExMember* __restric
     SweepBufs sb = B.sw;
     {
         const std::int64_t o = M.base;
-        sb.cst += o; sb.ev_st += o; sb.ev_hi += o; sb.ev_val += o; sb.mk_c += o; sb.mk_t += o; sb.te_st += o;
-        sb.te_hi += o; sb.te_lo += o; sb.te_val += o; sb.te_k += o; sb.la += o; sb.lb += o; sb.lc += o;
-        sb.lt += o; sb.dc += o; sb.dc2 += o; sb.dk += o; sb.dk2 += o;
+        sb.cst += o;
+        sb.ev += o;
+        sb.te += o;
+        sb.te_st += o;
+        sb.te_k += o;
+        sb.mk_c += o;
+        sb.dc += o;
+        sb.dc2 += o;
+        sb.dk += o;
+        sb.dk2 += o;
+        sb.fc += o;
+        sb.fc2 += o;
+        sb.fk += o;
+        sb.fk2 += o;
     }
     WinStore mid{};
     mid.fv = reinterpret_cast<float*>(ex_csmem);
@@ -507,7 +515,7 @@ constexpr int kExA_FQ = 128, kExA_DH = 256, kExA_HS = 1024, kExA_OC = 256;
 constexpr int kExB_FQ = 1024, kExB_DH = 4096, kExB_HS = 8192, kExB_OC = 4096;
 constexpr std::size_t kExSmemA = 8 * kExA_FQ + 8 * kExA_DH + 4 * kExA_HS + 8 * kExA_OC;
 constexpr std::size_t kExSmemB = 8 * kExB_FQ + 8 * kExB_DH + 4 * kExB_HS + 8 * kExB_OC;
-constexpr int kExC_FQ = 4096, kExC_DH = 20480;
+constexpr int kExC_FQ = 2048, kExC_DH = 4096;
 constexpr std::size_t kExSmemC =
     (8 * kExC_FQ + 8 * kExC_DH) > sizeof(SweepShared) ? (8 * kExC_FQ + 8 * kExC_DH) : sizeof(SweepShared);
 
@@ -539,8 +547,9 @@ inline cudaError_t ex_run(const ExMember* mem, const std::uint16_t* blk_member, 
     if (e == cudaSuccess) e = cudaMemsetAsync(B.diff, 0, sizeof(int) * (static_cast<std::size_t>(N) + 1), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(B.stamp, 0, sizeof(std::uint32_t) * static_cast<std::size_t>(N), st);
     // the block replay's stamps and counters start from zero on every run
-    for (std::uint32_t* a : {B.sw.cst, B.sw.ev_st, B.sw.mk_c, B.sw.mk_t, B.sw.te_st})
+    for (std::uint32_t* a : {B.sw.cst, B.sw.mk_c, B.sw.te_st})
         if (e == cudaSuccess) e = cudaMemsetAsync(a, 0, sizeof(std::uint32_t) * static_cast<std::size_t>(N), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(B.sw.ev, 0, sizeof(SwEv) * static_cast<std::size_t>(N), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(B.sw_ctr, 0, sizeof(std::uint32_t) * M, st);
     if (e != cudaSuccess) return e;
     ex_prep<<<nb, 256, 0, st>>>(mem, blk_member, N, z, kind, F0, B);

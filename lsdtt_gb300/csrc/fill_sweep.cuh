@@ -15,10 +15,14 @@
 // sweep's FIFO, ordered by (T of the discoverer, direction)) when it is not
 // above the discoverer's value, and otherwise queued as a heap cell (a pop
 // of this sweep if its gap exists). Those rules define every T of the sweep
-// as a fixed point, found by re-evaluating the cells next to changed pops
-// until nothing changes (a changed pop can only move the cells next to it).
-// Between sweeps and when the FIFO runs empty the block falls back to the
-// sequential rules of win_replay (one pop at a time).
+// as a fixed point, found in rounds: each round re-evaluates the cells next
+// to the pops that changed in the previous one (a changed pop can only move
+// the cells next to it). Between sweeps, when the FIFO runs empty, the block
+// takes single heap pops by the sequential rules of win_replay.
+//
+// The replay is latency-bound (one sweep after another), so each round costs
+// a few dependent loads: one 16-byte event record per cell, the round's
+// lists in shared memory, every neighbour's record loaded at once.
 #pragma once
 
 #include <cstdint>
@@ -30,30 +34,42 @@ namespace lsdtt_gb300
 namespace
 {
 
-constexpr int kSwThreads = 256;
-constexpr int kSwFQ = 2048;  // FIFO entries per sweep held in shared memory
+constexpr int kSwThreads = 512;
+constexpr int kSwFQ = 1024;  // FIFO entries of one sweep
+constexpr int kSwL = 2048;   // entries of each per-sweep list (changed pops, discovered cells)
+
+// A cell's pop in the current sweep: valid when st is the sweep's id.
+struct __align__(16) SwEv
+{
+    std::uint64_t hi;  // (gap << 33) | (kind << 32) | value key; kind 1 = FIFO entry
+    std::uint32_t st;
+    float val;
+};
+
+// A cell's discoverer in the current sweep (valid when te_st is the sweep's id).
+struct __align__(16) SwTe
+{
+    std::uint64_t hi;   // discoverer's T
+    std::uint32_t lo;   // its tie word (its cell for heap pops, 0 for FIFO entries)
+    float val;          // its value
+};
 
 // Per-member scratch of the block replay (member-local, one entry per cell
 // unless stated). Stamps make every array valid without clearing: a value
-// counts only when it carries the current window's, sweep's or round's id.
+// counts only when it carries the current window's or sweep's id.
 struct SweepBufs
 {
     std::uint32_t* cst;      // (window id << 2) | 1 heap, 2 FIFO, 3 popped
-    std::uint32_t* ev_st;    // sweep id of the cell's pop in this sweep
-    std::uint64_t* ev_hi;    // (gap << 33) | (kind << 32) | value key
-    float* ev_val;
-    std::uint32_t* mk_c;     // round id: listed as a candidate this round
-    std::uint32_t* mk_t;     // sweep id: discovered (tentatively) in this sweep
-    std::uint32_t* te_st;    // sweep id: tentative discoverer below is valid
-    std::uint64_t* te_hi;    // discoverer's T (hi word)
-    std::uint32_t* te_lo;    //   and tie word (its cell for heap pops, 0 for FIFO)
-    float* te_val;           //   and value
-    std::uint8_t* te_k;      //   and direction
-    std::uint32_t *la, *lb;  // changed-cell lists
-    std::uint32_t* lc;       // candidates of a round
-    std::uint32_t* lt;       // cells discovered in this sweep
-    std::uint32_t *dc, *dc2; // heap cells discovered earlier, not popped (two buffers)
-    float *dk, *dk2;         //   and their values
+    SwEv* ev;
+    SwTe* te;
+    std::uint32_t* te_st;    // sweep id: the discoverer in te is valid
+    std::uint8_t* te_k;      // direction from the discoverer
+    std::uint32_t* mk_c;     // round id: re-evaluated in this round (one thread per cell);
+                             // a value at or below the sweep's id: not yet in this sweep
+    std::uint32_t *dc, *dc2; // heap cells discovered earlier, not popped, with a value
+    float *dk, *dk2;         //   below the threshold T ("near", two buffers)
+    std::uint32_t *fc, *fc2; // the same at or above T ("far", two buffers): not scanned
+    float *fk, *fk2;         //   by a sweep until its FIFO values reach T
 };
 
 struct SweepShared
@@ -66,9 +82,11 @@ struct SweepShared
     std::uint64_t nhi[kSwFQ];
     std::uint32_t nlo[kSwFQ];
     std::uint8_t nk[kSwFQ];
+    std::uint32_t la[kSwL], lb[kSwL], lt[kSwL];
     std::uint32_t cnt[8];
     float red_v[kSwThreads / 32];
     std::uint32_t red_i[kSwThreads / 32];
+    std::uint32_t red_s[kSwThreads / 32];
     std::int64_t red_p;
 };
 
@@ -77,27 +95,35 @@ __device__ __forceinline__ std::uint64_t sw_hi(std::uint32_t g, std::uint32_t ki
     return (static_cast<std::uint64_t>(g) << 33) | (static_cast<std::uint64_t>(kind) << 32) | float_order_key(key);
 }
 
+// FIFOs up to this length are searched entry by entry; longer ones through
+// the next-greater table ng
+constexpr std::uint32_t kSwScan = 64;
+
 // first FIFO index >= g0 (1-based) whose value exceeds key; m + 1 if none
 __device__ __forceinline__ std::uint32_t sw_ng(const SweepShared& sh, std::uint32_t m, std::uint32_t g0, float key)
 {
     std::uint32_t g = g0;
-    while (g <= m && !(sh.fv[g - 1] > key)) g = sh.ng[g];
+    if (m <= kSwScan)
+        while (g <= m && !(sh.fv[g - 1] > key)) ++g;
+    else
+        while (g <= m && !(sh.fv[g - 1] > key)) g = sh.ng[g];
     return g;
 }
 
 // Block replay of window w (every thread of a kSwThreads block calls it).
 // *ctr is the member's id counter (stamps), advanced here. Returns kWinOk
-// with *next set, or kWinOverflow (a sweep's FIFO above kSwFQ, or no fixed
-// point within its round limit) -- then nothing of the window is final and
-// the caller replays it by the sequential rules.
+// with *next set, or kWinOverflow (a sweep's FIFO or lists above their
+// shared-memory size, or no fixed point within its round limit) -- then
+// nothing of the window is final and the caller replays it by the
+// sequential rules.
 __device__ int win_sweep_replay(const WinGrid& G, int w, const SweepBufs& B, float* out_F, std::uint32_t* ctr,
                                 SweepShared& sh, int* next)
 {
     const int tid = threadIdx.x;
     const float S = G.cuts[w];
-    __shared__ std::uint32_t s_ctr, s_m, s_nd, s_win, s_sweep, s_round, s_status;
+    __shared__ std::uint32_t s_ctr, s_m, s_nd, s_nf, s_win, s_sweep, s_status, s_last_move;
     __shared__ std::int64_t s_p;
-    __shared__ float s_V, s_Vmax;
+    __shared__ float s_V, s_Vmax, s_T, s_D;
     __shared__ int s_cnext, s_next, s_stop;
     if (tid == 0)
     {
@@ -108,32 +134,47 @@ __device__ int win_sweep_replay(const WinGrid& G, int w, const SweepBufs& B, flo
         s_cnext = w + 1;
         s_m = 0;
         s_nd = 0;
+        s_nf = 0;
+        // near/far threshold: four diagonal raise steps above the start
+        // (adapted as the window goes)
+        s_D = fmaxf(4.0f * G.eps * G.Ld, 1e-6f * fabsf(S) + 1e-30f);
+        s_T = S + s_D;
+        s_last_move = 0;
         s_status = kWinOk;
         s_next = G.ncut;
         s_stop = 0;
     }
     __syncthreads();
     const std::uint32_t win = s_win;
-    auto open_cell = [&](std::uint32_t j, float4& q) -> bool {
-        q = G.rec[j];
-        return q.w != 0.0f && q.y >= S && !(q.z < S) && (B.cst[j] >> 2) != win;
+    // not queued yet: valid, not popped before the window, not queued at its
+    // start, not queued by this window
+    auto open_cell = [&](std::uint32_t j, float& zj) -> bool {
+        const float4 q = G.rec[j];
+        const std::uint32_t c = B.cst[j];
+        zj = q.x;
+        return q.w != 0.0f && q.y >= S && !(q.z < S) && (c >> 2) != win;
     };
     std::uint32_t* dc = B.dc;
     std::uint32_t* dc2 = B.dc2;
     float* dk = B.dk;
     float* dk2 = B.dk2;
+    std::uint32_t* fcl = B.fc;
+    std::uint32_t* fcl2 = B.fc2;
+    float* fkl = B.fk;
+    float* fkl2 = B.fk2;
     for (;;)
     {
         if (s_m == 0)
         {
             // ---- FIFO empty: one heap pop by the sequential rules ----
-            // the list head (thread 0) and the least discovered heap cell
             if (tid == 0)
             {
                 std::int64_t p = s_p;
                 while (p < G.nsorted && !(G.ordRec[p].y < S)) ++p;
                 s_p = p;
             }
+            // the least discovered heap cell
+            // (slots of the far list are numbered after the near list's)
             float bz = INFINITY;
             std::uint32_t bi = kWinNone, bslot = kWinNone;
             for (std::uint32_t t = tid; t < s_nd; t += kSwThreads)
@@ -142,6 +183,13 @@ __device__ int win_sweep_replay(const WinGrid& G, int w, const SweepBufs& B, flo
                     bz = dk[t];
                     bi = dc[t];
                     bslot = t;
+                }
+            for (std::uint32_t t = tid; t < s_nf; t += kSwThreads)
+                if (win_key_less(fkl[t], fcl[t], bz, bi))
+                {
+                    bz = fkl[t];
+                    bi = fcl[t];
+                    bslot = s_nd + t;
                 }
             for (int o = 16; o > 0; o >>= 1)
             {
@@ -155,12 +203,11 @@ __device__ int win_sweep_replay(const WinGrid& G, int w, const SweepBufs& B, flo
                     bslot = os;
                 }
             }
-            __shared__ std::uint32_t s_slot[kSwThreads / 32];
             if ((tid & 31) == 0)
             {
                 sh.red_v[tid >> 5] = bz;
                 sh.red_i[tid >> 5] = bi;
-                s_slot[tid >> 5] = bslot;
+                sh.red_s[tid >> 5] = bslot;
             }
             __syncthreads();
             if (tid == 0)
@@ -170,7 +217,7 @@ __device__ int win_sweep_replay(const WinGrid& G, int w, const SweepBufs& B, flo
                     {
                         bz = sh.red_v[k];
                         bi = sh.red_i[k];
-                        bslot = s_slot[k];
+                        bslot = sh.red_s[k];
                     }
                 const bool have_l = s_p < G.nsorted;
                 float hz = INFINITY;
@@ -197,6 +244,17 @@ __device__ int win_sweep_replay(const WinGrid& G, int w, const SweepBufs& B, flo
                 else
                 {
                     const float V = s_V;
+                    // first cut above V (sweeps leave it to this point)
+                    {
+                        int lo = s_cnext, hi = G.ncut;
+                        while (lo < hi)
+                        {
+                            const int mid = (lo + hi) >> 1;
+                            if (G.cuts[mid] <= V) lo = mid + 1;
+                            else hi = mid;
+                        }
+                        s_cnext = lo;
+                    }
                     const int cn = s_cnext;
                     const bool trig = hz <= V && cn > 0 && G.cuts[cn - 1] >= hz;
                     if (!trig && (cn >= G.ncut || G.cand[cn]))
@@ -209,10 +267,18 @@ __device__ int win_sweep_replay(const WinGrid& G, int w, const SweepBufs& B, flo
                         if (from_list) ++s_p;
                         else
                         {
-                            // remove from the discovered heap cells
-                            const std::uint32_t last = --s_nd;
-                            dc[bslot] = dc[last];
-                            dk[bslot] = dk[last];
+                            if (bslot < s_nd)
+                            {
+                                const std::uint32_t last = --s_nd;
+                                dc[bslot] = dc[last];
+                                dk[bslot] = dk[last];
+                            }
+                            else
+                            {
+                                const std::uint32_t fs = bslot - s_nd, last = --s_nf;
+                                fcl[fs] = fcl[last];
+                                fkl[fs] = fkl[last];
+                            }
                             B.cst[hc] = (win << 2) | 3u;
                         }
                         if (hz > s_V)
@@ -228,9 +294,9 @@ __device__ int win_sweep_replay(const WinGrid& G, int w, const SweepBufs& B, flo
                             int rr, cc;
                             if (!fill_nb(G.nr, G.nc, G.per_ns, G.per_ew, r, c, d, rr, cc)) continue;
                             const std::uint32_t j = static_cast<std::uint32_t>(rr) * G.nc + cc;
-                            float4 q;
-                            if (!open_cell(j, q)) continue;
-                            if (q.x <= hz)
+                            float zj;
+                            if (!open_cell(j, zj)) continue;
+                            if (zj <= hz)
                             {
                                 sh.fc[m] = j;
                                 sh.fv[m] = raise_from(hz, G.eps, (d & 1) ? G.Ld : G.L);
@@ -239,9 +305,18 @@ __device__ int win_sweep_replay(const WinGrid& G, int w, const SweepBufs& B, flo
                             }
                             else
                             {
-                                dc[s_nd] = j;
-                                dk[s_nd] = q.x;
-                                ++s_nd;
+                                if (zj < s_T)
+                                {
+                                    dc[s_nd] = j;
+                                    dk[s_nd] = zj;
+                                    ++s_nd;
+                                }
+                                else
+                                {
+                                    fcl[s_nf] = j;
+                                    fkl[s_nf] = zj;
+                                    ++s_nf;
+                                }
                                 B.cst[j] = (win << 2) | 1u;
                             }
                         }
@@ -257,54 +332,181 @@ __device__ int win_sweep_replay(const WinGrid& G, int w, const SweepBufs& B, flo
         const std::uint32_t m = s_m;
         if (tid == 0)
         {
+            // the sweep's id, then ids for its rounds (sweep + 1 .. sweep + 64)
             s_sweep = ++s_ctr;
+            s_ctr += 64;
             // next greater FIFO value after each index (1-based, m + 1: none),
             // built right to left with pointer jumps
-            sh.ng[m + 1] = static_cast<std::uint16_t>(m + 1);
             float vmax = -INFINITY;
-            for (std::uint32_t g = m; g >= 1; --g)
+            if (m > kSwScan)
             {
-                std::uint32_t n = g + 1;
-                while (n <= m && !(sh.fv[n - 1] > sh.fv[g - 1])) n = sh.ng[n];
-                sh.ng[g] = static_cast<std::uint16_t>(n);
-                vmax = fmaxf(vmax, sh.fv[g - 1]);
+                sh.ng[m + 1] = static_cast<std::uint16_t>(m + 1);
+                for (std::uint32_t g = m; g >= 1; --g)
+                {
+                    std::uint32_t n = g + 1;
+                    while (n <= m && !(sh.fv[n - 1] > sh.fv[g - 1])) n = sh.ng[n];
+                    sh.ng[g] = static_cast<std::uint16_t>(n);
+                    vmax = fmaxf(vmax, sh.fv[g - 1]);
+                }
             }
+            else
+                for (std::uint32_t g = 0; g < m; ++g) vmax = fmaxf(vmax, sh.fv[g]);
             s_Vmax = vmax;
-            sh.cnt[0] = 0;  // changed list (la)
-            sh.cnt[1] = 0;  // next changed list (lb)
-            sh.cnt[2] = 0;  // discovered in this sweep (lt)
-            sh.cnt[3] = 0;  // surviving heap cells (dc2)
-            sh.cnt[4] = 0;  // next FIFO
+            // cnt: [0] changed (la), [1] changed next (lb), [2] discovered
+            // (lt), [3] surviving heap cells, [4] next FIFO, [5] overflow
+            for (int k = 0; k < 8; ++k) sh.cnt[k] = 0;
         }
         __syncthreads();
         const std::uint32_t sweep = s_sweep;
         const float Vmax = s_Vmax;
-        // FIFO entries: pops (g, 1)
-        for (std::uint32_t g = tid; g < m; g += kSwThreads)
+        if (Vmax >= s_T)
         {
-            const std::uint32_t c = sh.fc[g];
-            B.ev_st[c] = sweep;
-            B.ev_hi[c] = sw_hi(g + 1, 1, 0.0f);
-            B.ev_val[c] = sh.fv[g];
-            B.la[atomicAdd(&sh.cnt[0], 1u)] = c;
+            // the FIFO reaches the far list: raise T and move the far cells
+            // below it to the near list
+            if (tid == 0)
+            {
+                // T moved again within 4 sweeps: widen the band; not within
+                // 64: narrow it (a sweep's id advances by 65)
+                if (sweep - s_last_move < 4u * 65u) s_D *= 2.0f;
+                else if (sweep - s_last_move > 64u * 65u) s_D *= 0.5f;
+                s_last_move = sweep;
+                s_T = Vmax + s_D;
+                sh.cnt[6] = 0;
+                sh.cnt[7] = 0;
+            }
+            __syncthreads();
+            const float T = s_T;
+            const std::uint32_t nf = s_nf, nd0 = s_nd;
+            for (std::uint32_t t0 = 0; t0 < nf; t0 += kSwThreads)
+            {
+                const std::uint32_t t = t0 + tid;
+                const bool in = t < nf;
+                const std::uint32_t c = in ? fcl[t] : 0u;
+                const float k = in ? fkl[t] : INFINITY;
+                const bool mv = in && k < T, kp = in && !mv;
+                const int lane = tid & 31;
+                unsigned b = __ballot_sync(0xffffffffu, mv);
+                if (b)
+                {
+                    const int lead = __ffs(b) - 1;
+                    std::uint32_t base = 0;
+                    if (lane == lead) base = atomicAdd(&sh.cnt[6], static_cast<std::uint32_t>(__popc(b)));
+                    base = __shfl_sync(0xffffffffu, base, lead);
+                    if (mv)
+                    {
+                        const std::uint32_t k2 = nd0 + base + __popc(b & ((1u << lane) - 1u));
+                        dc[k2] = c;
+                        dk[k2] = k;
+                    }
+                }
+                b = __ballot_sync(0xffffffffu, kp);
+                if (b)
+                {
+                    const int lead = __ffs(b) - 1;
+                    std::uint32_t base = 0;
+                    if (lane == lead) base = atomicAdd(&sh.cnt[7], static_cast<std::uint32_t>(__popc(b)));
+                    base = __shfl_sync(0xffffffffu, base, lead);
+                    if (kp)
+                    {
+                        const std::uint32_t k2 = base + __popc(b & ((1u << lane) - 1u));
+                        fcl2[k2] = c;
+                        fkl2[k2] = k;
+                    }
+                }
+            }
+            __syncthreads();
+            if (tid == 0)
+            {
+                s_nd = nd0 + sh.cnt[6];
+                s_nf = sh.cnt[7];
+                for (int k = 0; k < 8; ++k) sh.cnt[k] = 0;
+            }
+            {
+                std::uint32_t* t1 = fcl;
+                fcl = fcl2;
+                fcl2 = t1;
+                float* t2 = fkl;
+                fkl = fkl2;
+                fkl2 = t2;
+            }
+            __syncthreads();
+        }
+        auto push_list = [&](std::uint32_t* list, int which, std::uint32_t c) {
+            const std::uint32_t k = atomicAdd(&sh.cnt[which], 1u);
+            if (k < static_cast<std::uint32_t>(kSwL)) list[k] = c;
+            else sh.cnt[5] = 1;
+        };
+        // the same for a whole warp at once (lanes with `want`): one atomic
+        auto push_warp = [&](std::uint32_t* list, int which, bool want, std::uint32_t c) {
+            const unsigned b = __ballot_sync(0xffffffffu, want);
+            if (!b) return;
+            const int lane = tid & 31;
+            const int lead = __ffs(b) - 1;
+            std::uint32_t base = 0;
+            if (lane == lead) base = atomicAdd(&sh.cnt[which], static_cast<std::uint32_t>(__popc(b)));
+            base = __shfl_sync(0xffffffffu, base, lead);
+            if (want)
+            {
+                const std::uint32_t k = base + __popc(b & ((1u << lane) - 1u));
+                if (k < static_cast<std::uint32_t>(kSwL)) list[k] = c;
+                else sh.cnt[5] = 1;
+            }
+        };
+        // FIFO entries: pops (g, 1)
+        for (std::uint32_t g0 = 0; g0 < m; g0 += kSwThreads)
+        {
+            const std::uint32_t g = g0 + tid;
+            std::uint32_t c = 0;
+            if (g < m)
+            {
+                c = sh.fc[g];
+                B.ev[c] = SwEv{sw_hi(g + 1, 1, 0.0f), sweep, sh.fv[g]};
+            }
+            push_warp(sh.la, 0, g < m, c);
         }
         // heap cells discovered earlier: those below Vmax pop in this sweep
-        for (std::uint32_t t = tid; t < s_nd; t += kSwThreads)
         {
-            const std::uint32_t c = dc[t];
-            const float k = dk[t];
-            if (k < Vmax)
+            const std::uint32_t nd = s_nd;
+            constexpr int kU = 4;
+            for (std::uint32_t t0 = 0; t0 < nd; t0 += kSwThreads * kU)
             {
-                B.ev_st[c] = sweep;
-                B.ev_hi[c] = sw_hi(sw_ng(sh, m, 1, k), 0, k);
-                B.ev_val[c] = k;
-                B.la[atomicAdd(&sh.cnt[0], 1u)] = c;
-            }
-            else
-            {
-                const std::uint32_t s2 = atomicAdd(&sh.cnt[3], 1u);
-                dc2[s2] = c;
-                dk2[s2] = k;
+                std::uint32_t cs[kU];
+                float ks[kU];
+#pragma unroll
+                for (int u = 0; u < kU; ++u)
+                {
+                    const std::uint32_t t = t0 + u * kSwThreads + tid;
+                    cs[u] = t < nd ? dc[t] : 0u;
+                    ks[u] = t < nd ? dk[t] : INFINITY;
+                }
+#pragma unroll
+                for (int u = 0; u < kU; ++u)
+                {
+                    const bool in = t0 + u * kSwThreads + tid < nd;
+                    const bool pops = in && ks[u] < Vmax;
+                    if (pops)
+                    {
+                        B.ev[cs[u]] = SwEv{sw_hi(sw_ng(sh, m, 1, ks[u]), 0, ks[u]), sweep, ks[u]};
+                        B.cst[cs[u]] = (win << 2) | 3u;
+                    }
+                    push_warp(sh.la, 0, pops, cs[u]);
+                    // survivors: compacted with one atomic per warp
+                    const bool keep = in && !pops;
+                    const unsigned b = __ballot_sync(0xffffffffu, keep);
+                    if (b)
+                    {
+                        const int lane = tid & 31, lead = __ffs(b) - 1;
+                        std::uint32_t base = 0;
+                        if (lane == lead) base = atomicAdd(&sh.cnt[3], static_cast<std::uint32_t>(__popc(b)));
+                        base = __shfl_sync(0xffffffffu, base, lead);
+                        if (keep)
+                        {
+                            const std::uint32_t k2 = base + __popc(b & ((1u << lane) - 1u));
+                            dc2[k2] = cs[u];
+                            dk2[k2] = ks[u];
+                        }
+                    }
+                }
             }
         }
         // list cells below Vmax (the sorted list from s_p on) pop too
@@ -313,19 +515,20 @@ __device__ int win_sweep_replay(const WinGrid& G, int w, const SweepBufs& B, flo
             const std::int64_t p0 = s_p;
             const std::int64_t q = p0 + tid;
             bool past = q >= G.nsorted;
+            bool pops = false;
+            std::uint32_t c = 0;
             if (!past)
             {
                 const float4 o = G.ordRec[q];
                 if (!(o.x < Vmax)) past = true;
                 else if (o.y < S)
                 {
-                    const std::uint32_t c = __float_as_uint(o.z);
-                    B.ev_st[c] = sweep;
-                    B.ev_hi[c] = sw_hi(sw_ng(sh, m, 1, o.x), 0, o.x);
-                    B.ev_val[c] = o.x;
-                    B.la[atomicAdd(&sh.cnt[0], 1u)] = c;
+                    c = __float_as_uint(o.z);
+                    B.ev[c] = SwEv{sw_hi(sw_ng(sh, m, 1, o.x), 0, o.x), sweep, o.x};
+                    pops = true;
                 }
             }
+            push_warp(sh.la, 0, pops, c);
             if (tid == 0) sh.red_p = G.nsorted + 1;
             __syncthreads();
             if (past) atomicMin(reinterpret_cast<unsigned long long*>(&sh.red_p), static_cast<unsigned long long>(q));
@@ -342,93 +545,95 @@ __device__ int win_sweep_replay(const WinGrid& G, int w, const SweepBufs& B, flo
         }
         __syncthreads();
         // rounds: re-evaluate the not-yet-queued cells next to changed pops
-        std::uint32_t* la = B.la;
-        std::uint32_t* lb = B.lb;
+        std::uint32_t* la = sh.la;
+        std::uint32_t* lb = sh.lb;
         int rounds = 0;
         for (;;)
         {
-            const std::uint32_t nch = sh.cnt[0];
-            if (nch == 0) break;
-            if (++rounds > 4096)
+            const std::uint32_t nch = min(sh.cnt[0], static_cast<std::uint32_t>(kSwL));
+            if (nch == 0 || sh.cnt[5]) break;
+            // a sweep settles in two or three rounds; one that has not after
+            // 64 leaves the window to the sequential rules
+            if (++rounds > 64)
             {
-                if (tid == 0) s_status = kWinOverflow;
+                __syncthreads();
+                if (tid == 0) sh.cnt[5] = 1;
+                __syncthreads();
                 break;
             }
-            if (tid == 0)
-            {
-                s_round = ++s_ctr;
-                sh.cnt[5] = 0;  // candidates of this round
-            }
-            __syncthreads();
-            const std::uint32_t round = s_round;
-            // candidates: open neighbours of changed cells, once each
+            const std::uint32_t round = sweep + static_cast<std::uint32_t>(rounds);
             for (std::uint32_t t = tid; t < nch * 8; t += kSwThreads)
             {
                 const std::uint32_t c = la[t >> 3];
-                const int d = static_cast<int>(t & 7);
-                const int r = static_cast<int>(c / static_cast<std::uint32_t>(G.nc));
-                const int cc0 = static_cast<int>(c - static_cast<std::uint32_t>(r) * G.nc);
+                const int dd = static_cast<int>(t & 7);
+                const int r0 = static_cast<int>(c / static_cast<std::uint32_t>(G.nc));
+                const int c0 = static_cast<int>(c - static_cast<std::uint32_t>(r0) * G.nc);
                 int rr, cc;
-                if (!fill_nb(G.nr, G.nc, G.per_ns, G.per_ew, r, cc0, d, rr, cc)) continue;
+                if (!fill_nb(G.nr, G.nc, G.per_ns, G.per_ew, r0, c0, dd, rr, cc)) continue;
                 const std::uint32_t j = static_cast<std::uint32_t>(rr) * G.nc + cc;
-                float4 q;
-                if (!open_cell(j, q)) continue;
-                if (atomicExch(&B.mk_c[j], round) == round) continue;
-                B.lc[atomicAdd(&sh.cnt[5], 1u)] = j;
-            }
-            __syncthreads();
-            const std::uint32_t ncand = sh.cnt[5];
-            if (tid == 0) sh.cnt[1] = 0;
-            __syncthreads();
-            for (std::uint32_t t = tid; t < ncand; t += kSwThreads)
-            {
-                const std::uint32_t j = B.lc[t];
-                const int r = static_cast<int>(j / static_cast<std::uint32_t>(G.nc));
-                const int c = static_cast<int>(j - static_cast<std::uint32_t>(r) * G.nc);
-                // the neighbour that pops first, and its direction towards j
-                std::uint64_t bh = ~0ull;
-                std::uint32_t bl = ~0u, be = kWinNone;
-                int bk = 8;
+                // every load the evaluation needs, issued before any is used:
+                // j's record and state, the records of its eight neighbours
+                std::uint32_t nbs[8];
+#pragma unroll
                 for (int d = 0; d < 8; ++d)
                 {
-                    int rr, cc;
-                    if (!fill_nb(G.nr, G.nc, G.per_ns, G.per_ew, r, c, d, rr, cc)) continue;
-                    const std::uint32_t e = static_cast<std::uint32_t>(rr) * G.nc + cc;
-                    if (B.ev_st[e] != sweep) continue;
-                    const std::uint64_t h = B.ev_hi[e];
-                    const std::uint32_t l = ((h >> 32) & 1u) ? 0u : e;
+                    int r2, c2;
+                    nbs[d] = fill_nb(G.nr, G.nc, G.per_ns, G.per_ew, rr, cc, d, r2, c2)
+                                 ? static_cast<std::uint32_t>(r2) * G.nc + c2
+                                 : kWinNone;
+                }
+                const float4 qj = G.rec[j];
+                const std::uint32_t cj = B.cst[j];
+                SwEv evs[8];
+#pragma unroll
+                for (int d = 0; d < 8; ++d) evs[d] = B.ev[nbs[d] != kWinNone ? nbs[d] : j];
+                const SwEv self = B.ev[j];
+                const float zj = qj.x;
+                if (!(qj.w != 0.0f && qj.y >= S && !(qj.z < S) && (cj >> 2) != win)) continue;
+                // one thread per cell and round: the cell's records have a
+                // single writer within the round (an older mark: first
+                // visit in this sweep, listed for the finalisation)
+                const std::uint32_t prev_mark = atomicExch(&B.mk_c[j], round);
+                if (prev_mark == round) continue;
+                if (prev_mark <= sweep) push_list(sh.lt, 2, j);
+                // the neighbour of j that pops first, and its direction to j
+                std::uint64_t bh = ~0ull;
+                std::uint32_t bl = ~0u;
+                float bval = 0.0f;
+                int bk = 8;
+#pragma unroll
+                for (int d = 0; d < 8; ++d)
+                {
+                    if (nbs[d] == kWinNone || evs[d].st != sweep) continue;
+                    const std::uint64_t h = evs[d].hi;
+                    const std::uint32_t l = ((h >> 32) & 1u) ? 0u : nbs[d];
                     const int k = (d + 4) & 7;
                     if (h < bh || (h == bh && (l < bl || (l == bl && k < bk))))
                     {
                         bh = h;
                         bl = l;
-                        be = e;
                         bk = k;
+                        bval = evs[d].val;
                     }
                 }
-                const bool was_ev = B.ev_st[j] == sweep;
-                if (be == kWinNone)
+                const bool was_ev = self.st == sweep;
+                if (bk == 8)
                 {
                     // no pop next to it any more: not discovered in this sweep
                     B.te_st[j] = 0;
                     if (was_ev)
                     {
-                        B.ev_st[j] = 0;
-                        lb[atomicAdd(&sh.cnt[1], 1u)] = j;
+                        B.ev[j].st = 0;
+                        push_list(lb, 1, j);
                     }
                     continue;
                 }
-                const float dval = B.ev_val[be];
-                B.te_st[j] = sweep;
-                B.te_hi[j] = bh;
-                B.te_lo[j] = bl;
-                B.te_val[j] = dval;
+                B.te[j] = SwTe{bh, bl, bval};
                 B.te_k[j] = static_cast<std::uint8_t>(bk);
-                if (atomicExch(&B.mk_t[j], sweep) != sweep) B.lt[atomicAdd(&sh.cnt[2], 1u)] = j;
-                const float zj = G.rec[j].x;
+                B.te_st[j] = sweep;
                 bool ev = false;
                 std::uint64_t nh = 0;
-                if (!(zj <= dval))
+                if (!(zj <= bval))
                 {
                     const std::uint32_t gd = static_cast<std::uint32_t>(bh >> 33);
                     const std::uint32_t gpush = ((bh >> 32) & 1u) ? gd + 1 : gd;
@@ -441,29 +646,36 @@ __device__ int win_sweep_replay(const WinGrid& G, int w, const SweepBufs& B, flo
                 }
                 if (ev)
                 {
-                    if (!was_ev || B.ev_hi[j] != nh)
+                    if (!was_ev || self.hi != nh)
                     {
-                        B.ev_hi[j] = nh;
-                        B.ev_val[j] = zj;
-                        B.ev_st[j] = sweep;
-                        lb[atomicAdd(&sh.cnt[1], 1u)] = j;
+                        B.ev[j] = SwEv{nh, sweep, zj};
+                        push_list(lb, 1, j);
                     }
                 }
                 else if (was_ev)
                 {
-                    B.ev_st[j] = 0;
-                    lb[atomicAdd(&sh.cnt[1], 1u)] = j;
+                    B.ev[j].st = 0;
+                    push_list(lb, 1, j);
                 }
             }
             __syncthreads();
-            if (tid == 0) sh.cnt[0] = sh.cnt[1];
+            if (tid == 0)
+            {
+                sh.cnt[0] = sh.cnt[1];
+                sh.cnt[1] = 0;
+            }
             std::uint32_t* t = la;
             la = lb;
             lb = t;
             __syncthreads();
         }
         __syncthreads();
-        if (s_status != kWinOk) break;
+        if (sh.cnt[5] || sh.cnt[2] > static_cast<std::uint32_t>(kSwL))
+        {
+            if (tid == 0) s_status = kWinOverflow;
+            __syncthreads();
+            break;
+        }
         // finalize: pops, next FIFO, heap cells
         float vmax_pop = -INFINITY;
         for (std::uint32_t g = tid; g < m; g += kSwThreads)
@@ -473,48 +685,54 @@ __device__ int win_sweep_replay(const WinGrid& G, int w, const SweepBufs& B, flo
             B.cst[c] = (win << 2) | 3u;
             vmax_pop = fmaxf(vmax_pop, sh.fv[g]);
         }
-        // heap pops among the cells queued before the sweep
-        for (std::uint32_t t = tid; t < s_nd; t += kSwThreads)
-            if (dk[t] < Vmax)
-            {
-                B.cst[dc[t]] = (win << 2) | 3u;
-                vmax_pop = fmaxf(vmax_pop, dk[t]);
-            }
         const std::uint32_t nt = sh.cnt[2];
         for (std::uint32_t t = tid; t < nt; t += kSwThreads)
         {
-            const std::uint32_t j = B.lt[t];
-            if (B.te_st[j] != sweep) continue;
+            const std::uint32_t j = sh.lt[t];
+            const std::uint32_t tst = B.te_st[j];
             const float zj = G.rec[j].x;
-            if (B.ev_st[j] == sweep)
+            const SwEv e = B.ev[j];
+            const SwTe d = B.te[j];
+            const int dk_dir = B.te_k[j];
+            if (tst != sweep) continue;
+            if (e.st == sweep)
             {
                 B.cst[j] = (win << 2) | 3u;
                 vmax_pop = fmaxf(vmax_pop, zj);
             }
-            else if (zj <= B.te_val[j])
+            else if (zj <= d.val)
             {
                 const std::uint32_t s2 = atomicAdd(&sh.cnt[4], 1u);
-                if (s2 < kSwFQ)
+                if (s2 < static_cast<std::uint32_t>(kSwFQ))
                 {
-                    const int k = B.te_k[j];
+                    const int k = dk_dir;
                     sh.nc[s2] = j;
-                    sh.nv[s2] = raise_from(B.te_val[j], G.eps, (k & 1) ? G.Ld : G.L);
-                    sh.nhi[s2] = B.te_hi[j];
-                    sh.nlo[s2] = B.te_lo[j];
+                    sh.nv[s2] = raise_from(d.val, G.eps, (k & 1) ? G.Ld : G.L);
+                    sh.nhi[s2] = d.hi;
+                    sh.nlo[s2] = d.lo;
                     sh.nk[s2] = static_cast<std::uint8_t>(k);
                 }
                 B.cst[j] = (win << 2) | 2u;
             }
             else
             {
-                const std::uint32_t s2 = atomicAdd(&sh.cnt[3], 1u);
-                dc2[s2] = j;
-                dk2[s2] = zj;
+                if (zj < s_T)
+                {
+                    const std::uint32_t s2 = atomicAdd(&sh.cnt[3], 1u);
+                    dc2[s2] = j;
+                    dk2[s2] = zj;
+                }
+                else
+                {
+                    const std::uint32_t s2 = s_nf + atomicAdd(&sh.cnt[6], 1u);
+                    fcl[s2] = j;
+                    fkl[s2] = zj;
+                }
                 B.cst[j] = (win << 2) | 1u;
             }
         }
-        // list pops' values: the largest is below Vmax; the sweep's largest
-        // popped value is at least its largest FIFO value, which is Vmax
+        // the largest value popped: the FIFO's (list and earlier heap pops
+        // are below Vmax, the FIFO's largest) or a discovered cell's
         for (int o = 16; o > 0; o >>= 1) vmax_pop = fmaxf(vmax_pop, __shfl_down_sync(0xffffffffu, vmax_pop, o));
         if ((tid & 31) == 0) sh.red_v[tid >> 5] = vmax_pop;
         __syncthreads();
@@ -524,14 +742,43 @@ __device__ int win_sweep_replay(const WinGrid& G, int w, const SweepBufs& B, flo
             float v = s_V;
             for (int k = 0; k < kSwThreads / 32; ++k) v = fmaxf(v, sh.red_v[k]);
             s_V = v;
-            while (s_cnext < G.ncut && G.cuts[s_cnext] <= s_V) ++s_cnext;
             s_nd = sh.cnt[3];
-            if (mn > kSwFQ) s_status = kWinOverflow;
+            s_nf += sh.cnt[6];
+            if (mn > static_cast<std::uint32_t>(kSwFQ)) s_status = kWinOverflow;
         }
         __syncthreads();
         if (s_status != kWinOk) break;
-        // the next FIFO in push order: (discoverer's T, direction); a
-        // rank sort (each entry counts the entries before it)
+        // the next FIFO in push order (discoverer's T, direction): each entry
+        // counts the entries before it (keys are distinct); up to 32 entries
+        // within warp 0 by shuffles
+        if (mn <= 32)
+        {
+            if (tid < 32)
+            {
+                const bool in = static_cast<std::uint32_t>(tid) < mn;
+                const std::uint64_t ah = in ? sh.nhi[tid] : ~0ull;
+                const std::uint32_t al = in ? sh.nlo[tid] : ~0u;
+                const std::uint32_t ak = in ? sh.nk[tid] : 255u;
+                const std::uint32_t ac = in ? sh.nc[tid] : 0u;
+                const float av = in ? sh.nv[tid] : 0.0f;
+                std::uint32_t rank = 0;
+                for (int b = 0; b < 32; ++b)
+                {
+                    const std::uint64_t bh = __shfl_sync(0xffffffffu, ah, b);
+                    const std::uint32_t bl = __shfl_sync(0xffffffffu, al, b);
+                    const std::uint32_t bk = __shfl_sync(0xffffffffu, ak, b);
+                    if (static_cast<std::uint32_t>(b) < mn &&
+                        (bh < ah || (bh == ah && (bl < al || (bl == al && bk < ak)))))
+                        ++rank;
+                }
+                if (in)
+                {
+                    sh.fc[rank] = ac;
+                    sh.fv[rank] = av;
+                }
+            }
+        }
+        else
         for (std::uint32_t a = tid; a < mn; a += kSwThreads)
         {
             const std::uint64_t ah = sh.nhi[a];
@@ -548,7 +795,6 @@ __device__ int win_sweep_replay(const WinGrid& G, int w, const SweepBufs& B, flo
         }
         __syncthreads();
         if (tid == 0) s_m = mn;
-        // swap the heap-cell buffers
         {
             std::uint32_t* t1 = dc;
             dc = dc2;
