@@ -10,11 +10,13 @@
 //      raised in the estimate;
 //   4. the valid cells of each member sorted by (F0, index);
 //   5. every candidate replayed by one warp with its state in shared memory
-//      (two sizes); raised cells staged in a pool;
-//   6. per member, one warp follows the chain of valid windows from the
-//      lowest cut, replaying any window on it that neither size could hold
-//      with its heap and FIFO in a whole block's shared memory, or, past
-//      that, in global memory;
+//      (three sizes, each taking the overflows of the one before); raised
+//      cells staged in a pool;
+//   6. per member, one block follows the chain of valid windows from the
+//      lowest cut; a window on it that no size could hold is replayed by
+//      the whole block one FIFO sweep at a time (fill_sweep.cuh), or, where
+//      a sweep outgrows the block's shared memory, by the sequential rules
+//      with the heap and FIFO in shared and then global memory;
 //   7. the chain's staged cells committed.
 #pragma once
 
@@ -56,14 +58,15 @@ struct ExBuffers
     std::int32_t *wl, *wl2;
     std::uint32_t* pool_c;
     float* pool_v;
-    float *gfv, *ghz;
-    std::uint32_t *gfc, *ghc, *stamp;
+    std::uint64_t *gfq, *ghk;  // the global replay's FIFO and heap (WinStore)
+    std::uint32_t* stamp;
     SweepBufs sw;           // the block replay's scratch (global cell indices; offset per member)
     std::uint32_t* sw_ctr;  // [M] stamp counters of the block replay
     std::int32_t* chain_order;  // [M] member of each chain block (largest members first)
     std::int64_t* nsorted;  // [M]
     int *ncut, *cut_base;   // [M], [M + 1]
-    unsigned* u;            // [0] total cuts, [1] nwl, [2] work, [3] nwl2, [4] work2, [5] error
+    unsigned* u;            // [0] total cuts, [1] nwl, [2] work, [3] nwl2, [4] work2, [5] error,
+                            // [6] nwl3, [7] work3
     unsigned long long* pool_used;
 };
 
@@ -76,13 +79,14 @@ inline std::size_t ex_bytes(std::int64_t N, int M, std::int64_t fifo_total)
     const std::size_t n = static_cast<std::size_t>(N) + 1, m = static_cast<std::size_t>(M) + 1;
     const std::size_t tiles = static_cast<std::size_t>((N + kSortTile - 1) / kSortTile) + 2;
     std::size_t b = 0;
-    for (std::size_t w : {16, 16, 8, 8, 8, 4, 4, 4, 4, 1, 1, 1, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4})
+    for (std::size_t w : {16, 16, 8, 8, 8, 4, 4, 4, 4, 1, 1, 1, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4})
         b += ex_round(w * n);
+    b += ex_round(8 * (n + 2));  // global heap
     // block replay: cst, ev, te, te_st, te_k, mk_c, dc, dc2, dk, dk2, fc, fc2, fk, fk2
     for (std::size_t w : {4, 16, 16, 4, 1, 4, 4, 4, 4, 4, 4, 4, 4, 4}) b += ex_round(w * n);
     b += ex_round(4 * m);  // chain order
     b += ex_round(4 * m);
-    b += 2 * ex_round(4 * static_cast<std::size_t>(fifo_total) + 4);
+    b += ex_round(8 * static_cast<std::size_t>(fifo_total) + 8);
     b += ex_round(8 * m) + 2 * ex_round(4 * m) + ex_round(64) + ex_round(8);
     b += tiles * 256 * 4 * 2 + tiles * 64 + (256 << 10);  // sort / scan scratch
     return b;
@@ -113,11 +117,9 @@ inline bool ex_carve(Scratch& ws, std::int64_t N, int M, std::int64_t fifo_total
     B.wl2 = ws.take<std::int32_t>(n);
     B.pool_c = ws.take<std::uint32_t>(n);
     B.pool_v = ws.take<float>(n);
-    B.ghz = ws.take<float>(n);
-    B.ghc = ws.take<std::uint32_t>(n);
     B.stamp = ws.take<std::uint32_t>(n);
-    B.gfv = ws.take<float>(static_cast<std::size_t>(fifo_total) + 1);
-    B.gfc = ws.take<std::uint32_t>(static_cast<std::size_t>(fifo_total) + 1);
+    B.ghk = ws.take<std::uint64_t>(n + 2);
+    B.gfq = ws.take<std::uint64_t>(static_cast<std::size_t>(fifo_total) + 1);
     B.sw.cst = ws.take<std::uint32_t>(n);
     B.sw.ev = ws.take<SwEv>(n);
     B.sw.te = ws.take<SwTe>(n);
@@ -316,13 +318,11 @@ __global__ void __launch_bounds__(32) ex_windows(const ExMember* __restrict__ me
     LSDTT_COUNT();
     extern __shared__ __align__(16) unsigned char ex_smem[];
     WinStore s{};
-    s.fv = reinterpret_cast<float*>(ex_smem);
-    s.fc = reinterpret_cast<std::uint32_t*>(s.fv + FQ);
+    s.fq = reinterpret_cast<std::uint64_t*>(ex_smem);
     s.fcap = FQ;
-    s.hz = reinterpret_cast<float*>(s.fc + FQ);
-    s.hc = reinterpret_cast<std::uint32_t*>(s.hz + DH);
+    s.hk = s.fq + FQ;
     s.hcap = DH;
-    s.hs = s.hc + DH;
+    s.hs = reinterpret_cast<std::uint32_t*>(s.hk + DH + 2);
     s.hscap = HS;
     s.oc = s.hs + HS;
     s.ov = reinterpret_cast<float*>(s.oc + OC);
@@ -363,19 +363,21 @@ __global__ void __launch_bounds__(32) ex_windows(const ExMember* __restrict__ me
     }
 }
 
-// Windows the first size could not hold, listed for the second.
-__global__ void ex_overflow_list(std::int64_t N, ExBuffers B)
+// Windows of list `src` that one size could not hold, listed for the next.
+__global__ void ex_overflow_list(std::int64_t N, const std::int32_t* __restrict__ src, const unsigned* __restrict__ nsrc,
+                                 std::int32_t* __restrict__ dst, unsigned* __restrict__ ndst,
+                                 const std::uint8_t* __restrict__ status)
 {
     LSDTT_COUNT();
     const std::int64_t t = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (t >= N || t >= static_cast<std::int64_t>(B.u[1])) return;
-    const int g = B.wl[t];
-    if (B.status[g] == kWinOverflow) B.wl2[atomicAdd(&B.u[3], 1u)] = g;
+    if (t >= N || t >= static_cast<std::int64_t>(*nsrc)) return;
+    const int g = src[t];
+    if (status[g] == kWinOverflow) dst[atomicAdd(ndst, 1u)] = g;
 }
 
 // 6. The chain of each member, one block of kSwThreads per member (block m):
 // from the lowest cut each window names the next valid start. A window on
-// the chain that neither shared-memory size held is replayed here by the
+// the chain that no shared-memory size held is replayed here by the
 // whole block, one FIFO sweep at a time (fill_sweep.cuh); a sweep whose FIFO
 // outgrows the block's shared memory sends the window to the sequential
 // rules, run by warp 0 with the heap (DH_C) and FIFO (FQ_C) in the same
@@ -416,20 +418,18 @@ __global__ void __launch_bounds__(kSwThreads) ex_chain(const ExMember* __restric
         sb.fk2 += o;
     }
     WinStore mid{};
-    mid.fv = reinterpret_cast<float*>(ex_csmem);
-    mid.fc = reinterpret_cast<std::uint32_t*>(mid.fv + FQ_C);
+    mid.fq = reinterpret_cast<std::uint64_t*>(ex_csmem);
     mid.fcap = FQ_C;
-    mid.hz = reinterpret_cast<float*>(mid.fc + FQ_C);
-    mid.hc = reinterpret_cast<std::uint32_t*>(mid.hz + DH_C);
+    mid.hk = mid.fq + FQ_C;
     mid.hcap = DH_C;
     mid.stamp = B.stamp + M.base;
     mid.out_F = F + M.base;
     WinStore big = mid;
-    big.fv = B.gfv + M.fifo_base;
-    big.fc = B.gfc + M.fifo_base;
+    big.fq = B.gfq + M.fifo_base;
     big.fcap = M.fifo_cap;
-    big.hz = B.ghz + M.base;
-    big.hc = B.ghc + M.base;
+    // (1-based: index nr*nc lands at most on the next member's unused
+    // entry 0, and the pair load reads one past it)
+    big.hk = B.ghk + M.base;
     big.hcap = static_cast<std::uint32_t>(static_cast<std::int64_t>(M.nr) * M.nc);
     __shared__ std::uint32_t s_ctr;
     __shared__ int s_nx, s_fail;
@@ -512,18 +512,24 @@ __global__ void ex_commit(const ExMember* __restrict__ mem, std::int64_t N, floa
 }
 
 constexpr int kExA_FQ = 128, kExA_DH = 256, kExA_HS = 1024, kExA_OC = 256;
-constexpr int kExB_FQ = 1024, kExB_DH = 4096, kExB_HS = 8192, kExB_OC = 4096;
-constexpr std::size_t kExSmemA = 8 * kExA_FQ + 8 * kExA_DH + 4 * kExA_HS + 8 * kExA_OC;
-constexpr std::size_t kExSmemB = 8 * kExB_FQ + 8 * kExB_DH + 4 * kExB_HS + 8 * kExB_OC;
+// (windows past the small size are heap-bound: their FIFO stays short)
+constexpr int kExM_FQ = 128, kExM_DH = 1024, kExM_HS = 4096, kExM_OC = 512;
+constexpr int kExB_FQ = 128, kExB_DH = 4096, kExB_HS = 8192, kExB_OC = 1024;
+constexpr std::size_t kExSmemA = 8 * kExA_FQ + 8 * (kExA_DH + 2) + 4 * kExA_HS + 8 * kExA_OC;
+constexpr std::size_t kExSmemM = 8 * kExM_FQ + 8 * (kExM_DH + 2) + 4 * kExM_HS + 8 * kExM_OC;
+constexpr std::size_t kExSmemB = 8 * kExB_FQ + 8 * (kExB_DH + 2) + 4 * kExB_HS + 8 * kExB_OC;
 constexpr int kExC_FQ = 2048, kExC_DH = 4096;
 constexpr std::size_t kExSmemC =
-    (8 * kExC_FQ + 8 * kExC_DH) > sizeof(SweepShared) ? (8 * kExC_FQ + 8 * kExC_DH) : sizeof(SweepShared);
+    (8 * kExC_FQ + 8 * (kExC_DH + 2)) > sizeof(SweepShared) ? (8 * kExC_FQ + 8 * (kExC_DH + 2)) : sizeof(SweepShared);
 
 // Opt the larger replay sizes into their shared memory (current device).
 inline cudaError_t ex_setup()
 {
-    cudaError_t e = cudaFuncSetAttribute(ex_windows<kExB_FQ, kExB_DH, kExB_HS, kExB_OC>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kExSmemB));
+    cudaError_t e = cudaFuncSetAttribute(ex_windows<kExM_FQ, kExM_DH, kExM_HS, kExM_OC>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kExSmemM));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(ex_windows<kExB_FQ, kExB_DH, kExB_HS, kExB_OC>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kExSmemB));
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(ex_chain<kExC_FQ, kExC_DH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  static_cast<int>(kExSmemC));
@@ -578,12 +584,17 @@ inline cudaError_t ex_run(const ExMember* mem, const std::uint16_t* blk_member, 
     if (e != cudaSuccess) return e;
     ex_gather<<<nb, 256, 0, st>>>(mem, blk_member, N, r ? B.val1 : B.val0, B);
     ex_base<<<nb, 256, 0, st>>>(mem, blk_member, N, z, kind, F);
-    // replays: small shared-memory size, then the larger one for overflows
-    ex_windows<kExA_FQ, kExA_DH, kExA_HS, kExA_OC><<<sms * 16, 32, kExSmemA, st>>>(
+    // replays: small shared-memory size, then two larger ones for the
+    // overflows of the one before (the sizes trade room for warps per SM:
+    // 20, 7 and 3); wl is free again once the middle size has its list
+    ex_windows<kExA_FQ, kExA_DH, kExA_HS, kExA_OC><<<sms * 20, 32, kExSmemA, st>>>(
         mem, z, kind, F0, B, B.wl, B.u + 1, B.u + 2, static_cast<unsigned long long>(N), 16ull * kExA_HS);
-    ex_overflow_list<<<nb, 256, 0, st>>>(N, B);
-    ex_windows<kExB_FQ, kExB_DH, kExB_HS, kExB_OC><<<sms * 2, 32, kExSmemB, st>>>(
-        mem, z, kind, F0, B, B.wl2, B.u + 3, B.u + 4, static_cast<unsigned long long>(N), 16ull * kExB_HS);
+    ex_overflow_list<<<nb, 256, 0, st>>>(N, B.wl, B.u + 1, B.wl2, B.u + 3, B.status);
+    ex_windows<kExM_FQ, kExM_DH, kExM_HS, kExM_OC><<<sms * 7, 32, kExSmemM, st>>>(
+        mem, z, kind, F0, B, B.wl2, B.u + 3, B.u + 4, static_cast<unsigned long long>(N), 16ull * kExM_HS);
+    ex_overflow_list<<<nb, 256, 0, st>>>(N, B.wl2, B.u + 3, B.wl, B.u + 6, B.status);
+    ex_windows<kExB_FQ, kExB_DH, kExB_HS, kExB_OC><<<sms * 3, 32, kExSmemB, st>>>(
+        mem, z, kind, F0, B, B.wl, B.u + 6, B.u + 7, static_cast<unsigned long long>(N), 16ull * kExB_HS);
     ex_chain<kExC_FQ, kExC_DH><<<M, kSwThreads, kExSmemC, st>>>(mem, z, kind, F0, F, B);
     ex_commit<<<static_cast<unsigned>(std::max<std::int64_t>(1, std::min<std::int64_t>(N / 8, sms * 64))), 256, 0,
                 st>>>(mem, N, F, B);

@@ -121,14 +121,15 @@ __device__ __forceinline__ bool win_key_less(float za, std::uint32_t ia, float z
 
 // Storage of one replay. Small tiers keep everything in shared memory (the
 // seen set as an open-addressing hash); the large tier keeps the FIFO and
-// heap in global memory and marks seen cells with a per-cell stamp.
+// heap in global memory and marks seen cells with a per-cell stamp. FIFO
+// entries are {value bits, cell} and heap entries {order key of the value,
+// cell} in one 64-bit word each, so that one load moves an entry and one
+// compare orders two heap entries by (value, cell).
 struct WinStore
 {
-    float* fv;            // FIFO values (ring)
-    std::uint32_t* fc;    // FIFO cells
+    std::uint64_t* fq;    // FIFO (ring)
     std::uint32_t fcap;   // power of two
-    float* hz;            // heap keys
-    std::uint32_t* hc;    // heap cells
+    std::uint64_t* hk;    // heap, 1-based (hk[1] the minimum); hcap + 2 entries, 16-byte aligned
     std::uint32_t hcap;
     std::uint32_t* hs;    // seen hash (small tiers) or null
     std::uint32_t hscap;  // power of two
@@ -140,50 +141,81 @@ struct WinStore
     float* out_F;         // large tier: the fill itself (member-local)
 };
 
-// Binary heap on (key, cell), one thread.
-__device__ __forceinline__ void win_heap_push(const WinStore& s, std::uint32_t& size, float key, std::uint32_t cell)
+// Heap entry of a cell at value z. Both zeros share one key (they compare
+// equal, so the cell index decides); the value read back is then +0, which
+// no replay can tell from -0: it only compares it and raises from it with a
+// positive minimum slope.
+__device__ __forceinline__ std::uint64_t win_hkey(float z, std::uint32_t cell)
 {
-    std::uint32_t i = size++;
-    while (i > 0)
+    return (static_cast<std::uint64_t>(float_order_key(z == 0.0f ? 0.0f : z)) << 32) | cell;
+}
+
+__device__ __forceinline__ float win_hkey_value(std::uint64_t k)
+{
+    return float_from_order_key(static_cast<std::uint32_t>(k >> 32));
+}
+
+__device__ __forceinline__ std::uint64_t win_fentry(float v, std::uint32_t cell)
+{
+    return (static_cast<std::uint64_t>(__float_as_uint(v)) << 32) | cell;
+}
+
+// Binary heap on the 64-bit keys (distinct: one entry per cell), one
+// thread, 1-based so that the two children of a node share one 16-byte load.
+__device__ __forceinline__ void win_heap_push(const WinStore& s, std::uint32_t& size, std::uint64_t key)
+{
+    std::uint32_t i = ++size;
+    while (i > 1)
     {
-        const std::uint32_t p = (i - 1) >> 1;
-        const float pk = s.hz[p];
-        const std::uint32_t pc = s.hc[p];
-        if (!win_key_less(key, cell, pk, pc)) break;
-        s.hz[i] = pk;
-        s.hc[i] = pc;
+        const std::uint32_t p = i >> 1;
+        const std::uint64_t pk = s.hk[p];
+        if (key >= pk) break;
+        s.hk[i] = pk;
         i = p;
     }
-    s.hz[i] = key;
-    s.hc[i] = cell;
+    s.hk[i] = key;
 }
 
 __device__ __forceinline__ void win_heap_pop(const WinStore& s, std::uint32_t& size)
 {
-    const std::uint32_t n = --size;
+    const std::uint32_t n = --size;  // entries left
     if (n == 0) return;
-    const float key = s.hz[n];
-    const std::uint32_t cell = s.hc[n];
-    std::uint32_t i = 0;
+    const std::uint64_t key = s.hk[n + 1];
+    std::uint32_t i = 1;
     for (;;)
     {
-        std::uint32_t c = 2 * i + 1;
-        if (c >= n) break;
-        float ck = s.hz[c];
-        std::uint32_t cc = s.hc[c];
-        if (c + 1 < n && win_key_less(s.hz[c + 1], s.hc[c + 1], ck, cc))
+        std::uint32_t c = 2 * i;
+        if (c > n) break;
+        const ulonglong2 pr = *reinterpret_cast<const ulonglong2*>(s.hk + c);
+        std::uint64_t ck = pr.x;
+        if (c < n && pr.y < ck)
         {
+            ck = pr.y;
             ++c;
-            ck = s.hz[c];
-            cc = s.hc[c];
         }
-        if (!win_key_less(ck, cc, key, cell)) break;
-        s.hz[i] = ck;
-        s.hc[i] = cc;
+        if (key <= ck) break;
+        s.hk[i] = ck;
         i = c;
     }
-    s.hz[i] = key;
-    s.hc[i] = cell;
+    s.hk[i] = key;
+}
+
+// Row of a cell index (exact: a float estimate corrected by whole rows).
+__device__ __forceinline__ int win_row(std::uint32_t cell, int nc, float inv_nc)
+{
+    int r = __float2int_rz(__uint2float_rz(cell) * inv_nc);
+    int c = static_cast<int>(cell - static_cast<std::uint32_t>(r) * static_cast<std::uint32_t>(nc));
+    while (c < 0)
+    {
+        --r;
+        c += nc;
+    }
+    while (c >= nc)
+    {
+        ++r;
+        c -= nc;
+    }
+    return r;
 }
 
 __device__ __forceinline__ std::uint32_t win_hash(std::uint32_t x, std::uint32_t mask)
@@ -225,9 +257,15 @@ struct WinResult
 // loop iteration takes one entry from the list, the heap or the FIFO or
 // leaves; each cell enters the heap or the FIFO at most once (the seen set),
 // so the replay ends after at most nsorted + (cells seen) iterations.
+//
+// A pop is a chain of dependent steps, so the loop keeps what it can off
+// that chain: the neighbour loads are issued before the heap is repaired,
+// and the cuts around the running maximum and a block of the sorted list sit
+// in registers (one entry per lane).
 __device__ WinResult win_replay(const WinGrid& G, int w, const WinStore& s, std::uint64_t pop_limit)
 {
     const int lane = threadIdx.x & 31;
+    const unsigned full = 0xffffffffu;
     const float S = G.cuts[w];
     __shared__ std::uint32_t sh_seen_count[32];  // one per warp of the block
     __shared__ bool sh_full[32];
@@ -240,7 +278,26 @@ __device__ WinResult win_replay(const WinGrid& G, int w, const WinStore& s, std:
     if (s.hs)
         for (std::uint32_t k = lane; k < s.hscap; k += 32) s.hs[k] = kWinNone;
     __syncwarp();
+    // two directions reach the same cell only through the periodic wrap of
+    // a grid one or two cells across
+    const bool dedupe = (G.per_ns && G.nr <= 2) || (G.per_ew && G.nc <= 2);
+    // cuts cb .. cb+31, one per lane (+inf past the last), with their
+    // candidate flags; cb <= cnext - 1 and cnext - cb <= 31 (or cnext = ncut)
+    int cb = w;
+    float cut_l = INFINITY;
+    bool cand_l = true;
+    if (cb + lane < G.ncut)
+    {
+        cut_l = G.cuts[cb + lane];
+        cand_l = G.cand[cb + lane] != 0;
+    }
+    // the sorted list from lb on, one position per lane; the list head is
+    // the first position >= p queued at the window start (mnb < S)
+    const float4 lsent = make_float4(0.0f, INFINITY, 0.0f, 0.0f);
     std::int64_t p = win_lower_bound(G.ordRec, G.nsorted, S);
+    std::int64_t lb = p;
+    float4 lo = lb + lane < G.nsorted ? G.ordRec[lb + lane] : lsent;
+    const float inv_nc = 1.0f / static_cast<float>(G.nc);
     bool rescan = true;  // the list head below is stale
     bool have_l = false;
     float lz = INFINITY;
@@ -253,29 +310,29 @@ __device__ WinResult win_replay(const WinGrid& G, int w, const WinStore& s, std:
     const std::uint32_t fmask = s.fcap - 1;
     for (;;)
     {
-        // the list head: next sorted cell queued at the window start (kept
-        // in registers until the list is popped)
         if (rescan)
         {
             have_l = false;
-            while (p < G.nsorted)
+            for (;;)
             {
-                const std::int64_t q = p + lane;
-                float4 o = make_float4(0.0f, INFINITY, 0.0f, 0.0f);
-                if (q < G.nsorted) o = G.ordRec[q];
-                const unsigned b = __ballot_sync(0xffffffffu, o.y < S);
+                const unsigned b = __ballot_sync(full, lb + lane >= p && lo.y < S);
                 if (b)
                 {
                     const int k = __ffs(b) - 1;
-                    p += k;
-                    lz = __shfl_sync(0xffffffffu, o.x, k);
-                    lc = __float_as_uint(__shfl_sync(0xffffffffu, o.z, k));
+                    p = lb + k;
+                    lz = __shfl_sync(full, lo.x, k);
+                    lc = __float_as_uint(__shfl_sync(full, lo.z, k));
                     have_l = true;
                     break;
                 }
-                p += 32;
+                if (lb + 32 >= G.nsorted)
+                {
+                    p = G.nsorted;
+                    break;
+                }
+                lb += 32;
+                lo = lb + lane < G.nsorted ? G.ordRec[lb + lane] : lsent;
             }
-            if (p > G.nsorted) p = G.nsorted;
             if (!have_l)
             {
                 lz = INFINITY;
@@ -289,8 +346,9 @@ __device__ WinResult win_replay(const WinGrid& G, int w, const WinStore& s, std:
         bool from_list = have_l;
         if (hsize > 0)
         {
-            const float tz = s.hz[0];
-            const std::uint32_t tc = s.hc[0];
+            const std::uint64_t t = s.hk[1];
+            const float tz = win_hkey_value(t);
+            const std::uint32_t tc = static_cast<std::uint32_t>(t);
             if (!have_l || win_key_less(tz, tc, lz, lc))
             {
                 hmz = tz;
@@ -305,12 +363,13 @@ __device__ WinResult win_replay(const WinGrid& G, int w, const WinStore& s, std:
         std::uint32_t cur_c;
         if (fifo_ne)
         {
-            const float fz = s.fv[head & fmask];
+            const std::uint64_t f = s.fq[head & fmask];
+            const float fz = __uint_as_float(static_cast<std::uint32_t>(f >> 32));
             if (!have_h || fz <= hmz)
             {
                 src = 2;
                 cur_v = fz;
-                cur_c = s.fc[head & fmask];
+                cur_c = static_cast<std::uint32_t>(f);
             }
             else
             {
@@ -327,8 +386,10 @@ __device__ WinResult win_replay(const WinGrid& G, int w, const WinStore& s, std:
                 break;
             }
             // FIFO empty: a pop can start an episode only at a cut in [hmz, V]
-            const bool trig = hmz <= V && cnext > 0 && G.cuts[cnext - 1] >= hmz;
-            if (!trig && (cnext >= G.ncut || G.cand[cnext]))
+            const float cprev = __shfl_sync(full, cut_l, cnext - 1 - cb);
+            const bool candn = __shfl_sync(full, cand_l, cnext - cb);
+            const bool trig = hmz <= V && cprev >= hmz;
+            if (!trig && (cnext >= G.ncut || candn))
             {
                 res.next = cnext;
                 break;
@@ -336,6 +397,23 @@ __device__ WinResult win_replay(const WinGrid& G, int w, const WinStore& s, std:
             src = from_list ? 0 : 1;
             cur_v = hmz;
             cur_c = hmc;
+        }
+        // neighbours, one lane per direction (N, NE, ..., NW): the loads go
+        // out first
+        const int r = win_row(cur_c, G.nc, inv_nc);
+        const int c = static_cast<int>(cur_c - static_cast<std::uint32_t>(r) * G.nc);
+        std::uint32_t j = kWinNone;
+        float4 q = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        std::uint32_t sv = 0;  // the cell's stamp (large tier), loaded beside its record
+        if (lane < 8)
+        {
+            int rr, cc;
+            if (fill_nb(G.nr, G.nc, G.per_ns, G.per_ew, r, c, lane, rr, cc))
+            {
+                j = static_cast<std::uint32_t>(rr) * G.nc + cc;
+                q = G.rec[j];
+                if (s.stamp) sv = s.stamp[j];
+            }
         }
         // take it
         if (src == 2)
@@ -372,40 +450,47 @@ __device__ WinResult win_replay(const WinGrid& G, int w, const WinStore& s, std:
         if (cur_v > V)
         {
             V = cur_v;
-            while (cnext < G.ncut && G.cuts[cnext] <= V) ++cnext;
+            // first cut > V (the cuts are sorted; lanes past the last hold +inf)
+            for (;;)
+            {
+                const unsigned b = __ballot_sync(full, cut_l > V);
+                if (b)
+                {
+                    cnext = min(cb + __ffs(b) - 1, G.ncut);
+                    break;
+                }
+                if (cb + 32 >= G.ncut)
+                {
+                    cnext = G.ncut;
+                    break;
+                }
+                cb += 31;
+                cut_l = INFINITY;
+                cand_l = true;
+                if (cb + lane < G.ncut)
+                {
+                    cut_l = G.cuts[cb + lane];
+                    cand_l = G.cand[cb + lane] != 0;
+                }
+            }
         }
         if (pop_limit && ++pops > pop_limit)
         {
             res.status = kWinOverflow;
             break;
         }
-        // neighbours, one lane per direction (N, NE, ..., NW)
-        const int r = static_cast<int>(cur_c / static_cast<std::uint32_t>(G.nc));
-        const int c = static_cast<int>(cur_c - static_cast<std::uint32_t>(r) * G.nc);
-        std::uint32_t j = kWinNone;
-        bool fresh = false;
-        float zj = 0.0f;
-        std::uint32_t sv = 0;  // the cell's stamp (large tier), loaded beside its record
-        if (lane < 8)
-        {
-            int rr, cc;
-            if (fill_nb(G.nr, G.nc, G.per_ns, G.per_ew, r, c, lane, rr, cc))
-            {
-                const std::uint32_t jj = static_cast<std::uint32_t>(rr) * G.nc + cc;
-                const float4 q = G.rec[jj];
-                if (s.stamp) sv = s.stamp[jj];
-                zj = q.x;
-                // open: valid, not popped before the window (F0 >= S), not
-                // queued at its start (mnb >= S)
-                if (q.w != 0.0f && q.y >= S && !(q.z < S)) j = jj;
-            }
-        }
+        // open: valid, not popped before the window (F0 >= S), not queued
+        // at its start (mnb >= S)
+        if (j != kWinNone && !(q.w != 0.0f && q.y >= S && !(q.z < S))) j = kWinNone;
+        const float zj = q.x;
         // a neighbour reached twice through a periodic wrap counts once
-        for (int k = 0; k < 7; ++k)
-        {
-            const std::uint32_t other = __shfl_sync(0xffffffffu, j, k);
-            if (lane > k && j != kWinNone && other == j) j = kWinNone;
-        }
+        if (dedupe)
+            for (int k = 0; k < 7; ++k)
+            {
+                const std::uint32_t other = __shfl_sync(full, j, k);
+                if (lane > k && j != kWinNone && other == j) j = kWinNone;
+            }
+        bool fresh = false;
         if (j != kWinNone)
         {
             if (s.stamp)
@@ -423,8 +508,8 @@ __device__ WinResult win_replay(const WinGrid& G, int w, const WinStore& s, std:
             break;
         }
         const bool raised = fresh && zj <= cur_v;
-        const unsigned rb = __ballot_sync(0xffffffffu, raised);
-        const unsigned hb = __ballot_sync(0xffffffffu, fresh && !raised);
+        const unsigned rb = __ballot_sync(full, raised);
+        const unsigned hb = __ballot_sync(full, fresh && !raised);
         if (tail - head + __popc(rb) > s.fcap || hsize + __popc(hb) > s.hcap)
         {
             res.status = kWinOverflow;
@@ -434,8 +519,7 @@ __device__ WinResult win_replay(const WinGrid& G, int w, const WinStore& s, std:
         {
             const float nz = raise_from(cur_v, G.eps, (lane & 1) ? G.Ld : G.L);
             const std::uint32_t slot = (tail + __popc(rb & ((1u << lane) - 1u))) & fmask;
-            s.fv[slot] = nz;
-            s.fc[slot] = j;
+            s.fq[slot] = win_fentry(nz, j);
         }
         tail += __popc(rb);
         // heap pushes by lane 0
@@ -444,9 +528,9 @@ __device__ WinResult win_replay(const WinGrid& G, int w, const WinStore& s, std:
         {
             const int k = __ffs(m) - 1;
             m &= m - 1;
-            const float kz = __shfl_sync(0xffffffffu, zj, k);
-            const std::uint32_t kc = __shfl_sync(0xffffffffu, j, k);
-            if (lane == 0) win_heap_push(s, hsize, kz, kc);
+            const float kz = __shfl_sync(full, zj, k);
+            const std::uint32_t kc = __shfl_sync(full, j, k);
+            if (lane == 0) win_heap_push(s, hsize, win_hkey(kz, kc));
             else ++hsize;
         }
         __syncwarp();
