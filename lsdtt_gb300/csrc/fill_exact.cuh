@@ -82,8 +82,9 @@ inline std::size_t ex_bytes(std::int64_t N, int M, std::int64_t fifo_total)
     for (std::size_t w : {16, 16, 8, 8, 8, 4, 4, 4, 4, 1, 1, 1, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4})
         b += ex_round(w * n);
     b += ex_round(8 * (n + 2));  // global heap
-    // block replay: cst, ev, te, te_st, te_k, mk_c, dc, dc2, dk, dk2, fc, fc2, fk, fk2
-    for (std::size_t w : {4, 16, 16, 4, 1, 4, 4, 4, 4, 4, 4, 4, 4, 4}) b += ex_round(w * n);
+    // block replay: cst, ev, te, te_st, te_k, mk_c, dc, dc2, dk, dk2, fc, fc2, fk, fk2,
+    // vc, vc2, vk, vk2
+    for (std::size_t w : {4, 16, 16, 4, 1, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4}) b += ex_round(w * n);
     b += ex_round(4 * m);  // chain order
     b += ex_round(4 * m);
     b += ex_round(8 * static_cast<std::size_t>(fifo_total) + 8);
@@ -134,6 +135,10 @@ inline bool ex_carve(Scratch& ws, std::int64_t N, int M, std::int64_t fifo_total
     B.sw.fc2 = ws.take<std::uint32_t>(n);
     B.sw.fk = ws.take<float>(n);
     B.sw.fk2 = ws.take<float>(n);
+    B.sw.vc = ws.take<std::uint32_t>(n);
+    B.sw.vc2 = ws.take<std::uint32_t>(n);
+    B.sw.vk = ws.take<float>(n);
+    B.sw.vk2 = ws.take<float>(n);
     B.chain_order = ws.take<std::int32_t>(m);
     B.sw_ctr = ws.take<std::uint32_t>(m);
     B.nsorted = ws.take<std::int64_t>(m);
@@ -416,6 +421,10 @@ __global__ void __launch_bounds__(kSwThreads) ex_chain(const ExMember* __restric
         sb.fc2 += o;
         sb.fk += o;
         sb.fk2 += o;
+        sb.vc += o;
+        sb.vc2 += o;
+        sb.vk += o;
+        sb.vk2 += o;
     }
     WinStore mid{};
     mid.fq = reinterpret_cast<std::uint64_t*>(ex_csmem);
@@ -518,7 +527,7 @@ constexpr int kExB_FQ = 128, kExB_DH = 4096, kExB_HS = 8192, kExB_OC = 1024;
 constexpr std::size_t kExSmemA = 8 * kExA_FQ + 8 * (kExA_DH + 2) + 4 * kExA_HS + 8 * kExA_OC;
 constexpr std::size_t kExSmemM = 8 * kExM_FQ + 8 * (kExM_DH + 2) + 4 * kExM_HS + 8 * kExM_OC;
 constexpr std::size_t kExSmemB = 8 * kExB_FQ + 8 * (kExB_DH + 2) + 4 * kExB_HS + 8 * kExB_OC;
-constexpr int kExC_FQ = 2048, kExC_DH = 4096;
+constexpr int kExC_FQ = 2048, kExC_DH = 16384;
 constexpr std::size_t kExSmemC =
     (8 * kExC_FQ + 8 * (kExC_DH + 2)) > sizeof(SweepShared) ? (8 * kExC_FQ + 8 * (kExC_DH + 2)) : sizeof(SweepShared);
 

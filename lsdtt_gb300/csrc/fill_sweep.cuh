@@ -35,8 +35,10 @@ namespace
 {
 
 constexpr int kSwThreads = 512;
-constexpr int kSwFQ = 1024;  // FIFO entries of one sweep
-constexpr int kSwL = 2048;   // entries of each per-sweep list (changed pops, discovered cells)
+// (the chain block has a whole SM to itself: its registers fill it, so the
+// shared memory is sized to hold the widest FIFO generations of large basins)
+constexpr int kSwFQ = 4096;  // FIFO entries of one sweep (a power of two)
+constexpr int kSwL = 4096;   // entries of each per-sweep list (changed pops, discovered cells)
 
 // A cell's pop in the current sweep: valid when st is the sweep's id.
 struct __align__(16) SwEv
@@ -68,8 +70,10 @@ struct SweepBufs
                              // a value at or below the sweep's id: not yet in this sweep
     std::uint32_t *dc, *dc2; // heap cells discovered earlier, not popped, with a value
     float *dk, *dk2;         //   below the threshold T ("near", two buffers)
-    std::uint32_t *fc, *fc2; // the same at or above T ("far", two buffers): not scanned
-    float *fk, *fk2;         //   by a sweep until its FIFO values reach T
+    std::uint32_t *fc, *fc2; // the same at or above T and below U ("far", two buffers):
+    float *fk, *fk2;         //   scanned only when a sweep's FIFO values reach T
+    std::uint32_t *vc, *vc2; // the same at or above U ("very far", two buffers):
+    float *vk, *vk2;         //   scanned only when T reaches U
 };
 
 struct SweepShared
@@ -83,7 +87,7 @@ struct SweepShared
     std::uint32_t nlo[kSwFQ];
     std::uint8_t nk[kSwFQ];
     std::uint32_t la[kSwL], lb[kSwL], lt[kSwL];
-    std::uint32_t cnt[8];
+    std::uint32_t cnt[10];
     float red_v[kSwThreads / 32];
     std::uint32_t red_i[kSwThreads / 32];
     std::uint32_t red_s[kSwThreads / 32];
@@ -121,9 +125,10 @@ __device__ int win_sweep_replay(const WinGrid& G, int w, const SweepBufs& B, flo
 {
     const int tid = threadIdx.x;
     const float S = G.cuts[w];
-    __shared__ std::uint32_t s_ctr, s_m, s_nd, s_nf, s_win, s_sweep, s_status, s_last_move;
+    __shared__ std::uint32_t s_ctr, s_m, s_nd, s_nf, s_nv, s_win, s_sweep, s_status, s_last_move;
     __shared__ std::int64_t s_p;
-    __shared__ float s_V, s_Vmax, s_T, s_D;
+    __shared__ float s_V, s_Vmax, s_T, s_U, s_D;
+    __shared__ int s_rebuild;
     __shared__ int s_cnext, s_next, s_stop;
     if (tid == 0)
     {
@@ -135,10 +140,12 @@ __device__ int win_sweep_replay(const WinGrid& G, int w, const SweepBufs& B, flo
         s_m = 0;
         s_nd = 0;
         s_nf = 0;
+        s_nv = 0;
         // near/far threshold: four diagonal raise steps above the start
-        // (adapted as the window goes)
+        // (adapted as the window goes); far/very-far threshold 16 bands on
         s_D = fmaxf(4.0f * G.eps * G.Ld, 1e-6f * fabsf(S) + 1e-30f);
         s_T = S + s_D;
+        s_U = s_T + 16.0f * s_D;
         s_last_move = 0;
         s_status = kWinOk;
         s_next = G.ncut;
@@ -162,8 +169,23 @@ __device__ int win_sweep_replay(const WinGrid& G, int w, const SweepBufs& B, flo
     std::uint32_t* fcl2 = B.fc2;
     float* fkl = B.fk;
     float* fkl2 = B.fk2;
+    std::uint32_t* vcl = B.vc;
+    std::uint32_t* vcl2 = B.vc2;
+    float* vkl = B.vk;
+    float* vkl2 = B.vk2;
+    // every pass pops at least one cell (a background pop or a sweep's
+    // FIFO), so more passes than cells means the replay has gone wrong: it
+    // is then left to the sequential rules
+    const std::uint64_t pass_cap = static_cast<std::uint64_t>(G.nr) * static_cast<std::uint64_t>(G.nc) + 2;
+    std::uint64_t passes = 0;
     for (;;)
     {
+        if (++passes > pass_cap)
+        {
+            if (tid == 0) s_status = kWinOverflow;
+            __syncthreads();
+            break;
+        }
         if (s_m == 0)
         {
             // ---- FIFO empty: one heap pop by the sequential rules ----
@@ -173,23 +195,20 @@ __device__ int win_sweep_replay(const WinGrid& G, int w, const SweepBufs& B, flo
                 while (p < G.nsorted && !(G.ordRec[p].y < S)) ++p;
                 s_p = p;
             }
-            // the least discovered heap cell
-            // (slots of the far list are numbered after the near list's)
+            // the least discovered heap cell: in the first non-empty list
+            // (every near key is below T <= every far key < U <= every very-far key)
+            const int which = s_nd ? 0 : (s_nf ? 1 : 2);
+            const std::uint32_t* lc = which == 0 ? dc : (which == 1 ? fcl : vcl);
+            const float* lk = which == 0 ? dk : (which == 1 ? fkl : vkl);
+            const std::uint32_t ln = which == 0 ? s_nd : (which == 1 ? s_nf : s_nv);
             float bz = INFINITY;
             std::uint32_t bi = kWinNone, bslot = kWinNone;
-            for (std::uint32_t t = tid; t < s_nd; t += kSwThreads)
-                if (win_key_less(dk[t], dc[t], bz, bi))
+            for (std::uint32_t t = tid; t < ln; t += kSwThreads)
+                if (win_key_less(lk[t], lc[t], bz, bi))
                 {
-                    bz = dk[t];
-                    bi = dc[t];
+                    bz = lk[t];
+                    bi = lc[t];
                     bslot = t;
-                }
-            for (std::uint32_t t = tid; t < s_nf; t += kSwThreads)
-                if (win_key_less(fkl[t], fcl[t], bz, bi))
-                {
-                    bz = fkl[t];
-                    bi = fcl[t];
-                    bslot = s_nd + t;
                 }
             for (int o = 16; o > 0; o >>= 1)
             {
@@ -267,17 +286,23 @@ __device__ int win_sweep_replay(const WinGrid& G, int w, const SweepBufs& B, flo
                         if (from_list) ++s_p;
                         else
                         {
-                            if (bslot < s_nd)
+                            if (which == 0)
                             {
                                 const std::uint32_t last = --s_nd;
                                 dc[bslot] = dc[last];
                                 dk[bslot] = dk[last];
                             }
+                            else if (which == 1)
+                            {
+                                const std::uint32_t last = --s_nf;
+                                fcl[bslot] = fcl[last];
+                                fkl[bslot] = fkl[last];
+                            }
                             else
                             {
-                                const std::uint32_t fs = bslot - s_nd, last = --s_nf;
-                                fcl[fs] = fcl[last];
-                                fkl[fs] = fkl[last];
+                                const std::uint32_t last = --s_nv;
+                                vcl[bslot] = vcl[last];
+                                vkl[bslot] = vkl[last];
                             }
                             B.cst[hc] = (win << 2) | 3u;
                         }
@@ -311,11 +336,17 @@ __device__ int win_sweep_replay(const WinGrid& G, int w, const SweepBufs& B, flo
                                     dk[s_nd] = zj;
                                     ++s_nd;
                                 }
-                                else
+                                else if (zj < s_U)
                                 {
                                     fcl[s_nf] = j;
                                     fkl[s_nf] = zj;
                                     ++s_nf;
+                                }
+                                else
+                                {
+                                    vcl[s_nv] = j;
+                                    vkl[s_nv] = zj;
+                                    ++s_nv;
                                 }
                                 B.cst[j] = (win << 2) | 1u;
                             }
@@ -335,26 +366,47 @@ __device__ int win_sweep_replay(const WinGrid& G, int w, const SweepBufs& B, flo
             // the sweep's id, then ids for its rounds (sweep + 1 .. sweep + 64)
             s_sweep = ++s_ctr;
             s_ctr += 64;
-            // next greater FIFO value after each index (1-based, m + 1: none),
-            // built right to left with pointer jumps
-            float vmax = -INFINITY;
+            // cnt: [0] changed (la), [1] changed next (lb), [2] discovered
+            // (lt), [3] surviving heap cells, [4] next FIFO, [5] overflow,
+            // [6..9] list moves and appends
+            for (int k = 0; k < 10; ++k) sh.cnt[k] = 0;
+        }
+        {
+            // the FIFO's largest value, and the next greater FIFO value after
+            // each index (1-based, m + 1: none): every thread looks up to 32
+            // entries ahead; one thread finishes the rest right to left with
+            // pointer jumps (entries g + 1 .. g + 32 are known not greater)
+            float lv = -INFINITY;
+            for (std::uint32_t g = tid; g < m; g += kSwThreads) lv = fmaxf(lv, sh.fv[g]);
             if (m > kSwScan)
-            {
-                sh.ng[m + 1] = static_cast<std::uint16_t>(m + 1);
-                for (std::uint32_t g = m; g >= 1; --g)
+                for (std::uint32_t g = 1 + tid; g <= m; g += kSwThreads)
                 {
+                    const float v = sh.fv[g - 1];
+                    const std::uint32_t lim = min(m + 1, g + 33);
                     std::uint32_t n = g + 1;
-                    while (n <= m && !(sh.fv[n - 1] > sh.fv[g - 1])) n = sh.ng[n];
-                    sh.ng[g] = static_cast<std::uint16_t>(n);
-                    vmax = fmaxf(vmax, sh.fv[g - 1]);
+                    while (n < lim && !(sh.fv[n - 1] > v)) ++n;
+                    sh.ng[g] = static_cast<std::uint16_t>((n < lim || lim == m + 1) ? n : 0u);
+                }
+            for (int o = 16; o > 0; o >>= 1) lv = fmaxf(lv, __shfl_down_sync(0xffffffffu, lv, o));
+            if ((tid & 31) == 0) sh.red_v[tid >> 5] = lv;
+            __syncthreads();
+            if (tid == 0)
+            {
+                float vmax = -INFINITY;
+                for (int k = 0; k < kSwThreads / 32; ++k) vmax = fmaxf(vmax, sh.red_v[k]);
+                s_Vmax = vmax;
+                if (m > kSwScan)
+                {
+                    sh.ng[m + 1] = static_cast<std::uint16_t>(m + 1);
+                    for (std::uint32_t g = m; g >= 1; --g)
+                        if (sh.ng[g] == 0)
+                        {
+                            std::uint32_t n = g + 33;
+                            while (n <= m && !(sh.fv[n - 1] > sh.fv[g - 1])) n = sh.ng[n];
+                            sh.ng[g] = static_cast<std::uint16_t>(n);
+                        }
                 }
             }
-            else
-                for (std::uint32_t g = 0; g < m; ++g) vmax = fmaxf(vmax, sh.fv[g]);
-            s_Vmax = vmax;
-            // cnt: [0] changed (la), [1] changed next (lb), [2] discovered
-            // (lt), [3] surviving heap cells, [4] next FIFO, [5] overflow
-            for (int k = 0; k < 8; ++k) sh.cnt[k] = 0;
         }
         __syncthreads();
         const std::uint32_t sweep = s_sweep;
@@ -373,8 +425,72 @@ __device__ int win_sweep_replay(const WinGrid& G, int w, const SweepBufs& B, flo
                 s_T = Vmax + s_D;
                 sh.cnt[6] = 0;
                 sh.cnt[7] = 0;
+                sh.cnt[8] = 0;
+                sh.cnt[9] = 0;
+                s_rebuild = s_T >= s_U;
+                if (s_rebuild) s_U = s_T + 16.0f * s_D;
             }
             __syncthreads();
+            if (s_rebuild)
+            {
+                // T reached U: the very-far cells below the new U join the far list
+                const float U = s_U;
+                const std::uint32_t nv = s_nv, nf0 = s_nf;
+                for (std::uint32_t t0 = 0; t0 < nv; t0 += kSwThreads)
+                {
+                    const std::uint32_t t = t0 + tid;
+                    const bool in = t < nv;
+                    const std::uint32_t c = in ? vcl[t] : 0u;
+                    const float k = in ? vkl[t] : INFINITY;
+                    const bool mv = in && k < U, kp = in && !mv;
+                    const int lane = tid & 31;
+                    unsigned b = __ballot_sync(0xffffffffu, mv);
+                    if (b)
+                    {
+                        const int lead = __ffs(b) - 1;
+                        std::uint32_t base = 0;
+                        if (lane == lead) base = atomicAdd(&sh.cnt[8], static_cast<std::uint32_t>(__popc(b)));
+                        base = __shfl_sync(0xffffffffu, base, lead);
+                        if (mv)
+                        {
+                            const std::uint32_t k2 = nf0 + base + __popc(b & ((1u << lane) - 1u));
+                            fcl[k2] = c;
+                            fkl[k2] = k;
+                        }
+                    }
+                    b = __ballot_sync(0xffffffffu, kp);
+                    if (b)
+                    {
+                        const int lead = __ffs(b) - 1;
+                        std::uint32_t base = 0;
+                        if (lane == lead) base = atomicAdd(&sh.cnt[9], static_cast<std::uint32_t>(__popc(b)));
+                        base = __shfl_sync(0xffffffffu, base, lead);
+                        if (kp)
+                        {
+                            const std::uint32_t k2 = base + __popc(b & ((1u << lane) - 1u));
+                            vcl2[k2] = c;
+                            vkl2[k2] = k;
+                        }
+                    }
+                }
+                __syncthreads();
+                if (tid == 0)
+                {
+                    s_nf = nf0 + sh.cnt[8];
+                    s_nv = sh.cnt[9];
+                    sh.cnt[8] = 0;
+                    sh.cnt[9] = 0;
+                }
+                {
+                    std::uint32_t* t1 = vcl;
+                    vcl = vcl2;
+                    vcl2 = t1;
+                    float* t2 = vkl;
+                    vkl = vkl2;
+                    vkl2 = t2;
+                }
+                __syncthreads();
+            }
             const float T = s_T;
             const std::uint32_t nf = s_nf, nd0 = s_nd;
             for (std::uint32_t t0 = 0; t0 < nf; t0 += kSwThreads)
@@ -419,7 +535,7 @@ __device__ int win_sweep_replay(const WinGrid& G, int w, const SweepBufs& B, flo
             {
                 s_nd = nd0 + sh.cnt[6];
                 s_nf = sh.cnt[7];
-                for (int k = 0; k < 8; ++k) sh.cnt[k] = 0;
+                for (int k = 0; k < 10; ++k) sh.cnt[k] = 0;
             }
             {
                 std::uint32_t* t1 = fcl;
@@ -722,11 +838,17 @@ __device__ int win_sweep_replay(const WinGrid& G, int w, const SweepBufs& B, flo
                     dc2[s2] = j;
                     dk2[s2] = zj;
                 }
-                else
+                else if (zj < s_U)
                 {
                     const std::uint32_t s2 = s_nf + atomicAdd(&sh.cnt[6], 1u);
                     fcl[s2] = j;
                     fkl[s2] = zj;
+                }
+                else
+                {
+                    const std::uint32_t s2 = s_nv + atomicAdd(&sh.cnt[8], 1u);
+                    vcl[s2] = j;
+                    vkl[s2] = zj;
                 }
                 B.cst[j] = (win << 2) | 1u;
             }
@@ -744,14 +866,56 @@ __device__ int win_sweep_replay(const WinGrid& G, int w, const SweepBufs& B, flo
             s_V = v;
             s_nd = sh.cnt[3];
             s_nf += sh.cnt[6];
+            s_nv += sh.cnt[8];
             if (mn > static_cast<std::uint32_t>(kSwFQ)) s_status = kWinOverflow;
         }
         __syncthreads();
         if (s_status != kWinOk) break;
         // the next FIFO in push order (discoverer's T, direction): each entry
         // counts the entries before it (keys are distinct); up to 32 entries
-        // within warp 0 by shuffles
-        if (mn <= 32)
+        // within warp 0 by shuffles, past 64 by a bitonic sort of indices
+        // (ng is free until the next sweep builds it)
+        if (mn > 64)
+        {
+            const std::uint32_t P = 1u << (32 - __clz(mn - 1));
+            for (std::uint32_t t = tid; t < P; t += kSwThreads) sh.ng[t] = static_cast<std::uint16_t>(t);
+            __syncthreads();
+            // a after b in push order (indices past mn last)
+            auto after = [&](std::uint32_t a, std::uint32_t b) {
+                if (a >= mn) return b < mn || a > b;
+                if (b >= mn) return false;
+                const std::uint64_t ah = sh.nhi[a], bh = sh.nhi[b];
+                if (ah != bh) return ah > bh;
+                const std::uint32_t al = sh.nlo[a], bl = sh.nlo[b];
+                if (al != bl) return al > bl;
+                return sh.nk[a] > sh.nk[b];
+            };
+            for (std::uint32_t k = 2; k <= P; k <<= 1)
+                for (std::uint32_t j = k >> 1; j > 0; j >>= 1)
+                {
+                    for (std::uint32_t i = tid; i < P; i += kSwThreads)
+                    {
+                        const std::uint32_t l = i ^ j;
+                        if (l > i)
+                        {
+                            const std::uint32_t a = sh.ng[i], b = sh.ng[l];
+                            if (after(a, b) == ((i & k) == 0))
+                            {
+                                sh.ng[i] = static_cast<std::uint16_t>(b);
+                                sh.ng[l] = static_cast<std::uint16_t>(a);
+                            }
+                        }
+                    }
+                    __syncthreads();
+                }
+            for (std::uint32_t r = tid; r < mn; r += kSwThreads)
+            {
+                const std::uint32_t a = sh.ng[r];
+                sh.fc[r] = sh.nc[a];
+                sh.fv[r] = sh.nv[a];
+            }
+        }
+        else if (mn <= 32)
         {
             if (tid < 32)
             {
