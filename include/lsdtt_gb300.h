@@ -110,7 +110,7 @@ int lsdtt_gpu_fill_pits(const lsdtt_gpu_grid* grid, const float* z_dev, const ui
  * fixed array inside the library (64 MiB + 64 KiB, held on every device
  * that loads the library), so grids are limited to about 8192 x 8192 cells
  * at min_slope <= 0 and, because the raised cells' reference order needs
- * about 230 bytes a cell of replay buffers, about 530 x 530 cells at
+ * about 240 bytes a cell of replay buffers, about 520 x 520 cells at
  * min_slope > 0; larger grids return LSDTT_GPU_EINVAL. Same results as
  * lsdtt_gpu_fill_pits. The first call on a device looks up the array's
  * device address: make it before any stream capture. All calls share the

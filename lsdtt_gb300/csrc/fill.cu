@@ -402,8 +402,8 @@ LSDTT_DEFINE_LAUNCH_READER(fill)
 //     (64 MiB + 64 KiB), allocated when the library is loaded and held by
 //     every GPU that loads it until the process exits.
 //   * With min_slope <= 0 it fits grids of up to about 67 million cells
-//     (8192 x 8192); with min_slope > 0 the replays need about 230 bytes a
-//     cell, so up to about 280,000 cells (530 x 530). Larger grids are
+//     (8192 x 8192); with min_slope > 0 the replays need about 240 bytes a
+//     cell, so up to about 270,000 cells (520 x 520). Larger grids are
 //     rejected with LSDTT_GPU_EINVAL before any work is queued.
 //   * Host code cannot use the array's name as a device address, so the
 //     first call in each CUDA context looks the address up with
@@ -495,7 +495,7 @@ extern "C" int lsdtt_gpu_fill_pits_noalloc(const lsdtt_gpu_grid* grid, const flo
                                           std::to_string(nc) + " grid needs " + std::to_string(need) +
                                           " bytes of scratch but the fixed scratch holds " +
                                           std::to_string(kFillNoAllocBytes) +
-                                          " (about 8192 x 8192 cells at min_slope 0, 530 x 530 above); use "
+                                          " (about 8192 x 8192 cells at min_slope 0, 520 x 520 above); use "
                                           "lsdtt_gpu_fill_pits");
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);

@@ -82,9 +82,9 @@ inline std::size_t ex_bytes(std::int64_t N, int M, std::int64_t fifo_total)
     for (std::size_t w : {16, 16, 8, 8, 8, 4, 4, 4, 4, 1, 1, 1, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4})
         b += ex_round(w * n);
     b += ex_round(8 * (n + 2));  // global heap
-    // block replay: cst, ev, te, te_st, te_k, mk_c, dc, dc2, dk, dk2, fc, fc2, fk, fk2,
-    // vc, vc2, vk, vk2
-    for (std::size_t w : {4, 16, 16, 4, 1, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4}) b += ex_round(w * n);
+    // block replay: cst, ev, te, te_st, te_k, mk_c, dc, dc2, dk, dk2, sc, sk
+    for (std::size_t w : {4, 16, 16, 4, 1, 4, 4, 4, 4, 4, 4, 4}) b += ex_round(w * n);
+    b += 2 * ex_round(4 * static_cast<std::size_t>(kSwLv) * n);  // lc, lk
     b += ex_round(4 * m);  // chain order
     b += ex_round(4 * m);
     b += ex_round(8 * static_cast<std::size_t>(fifo_total) + 8);
@@ -131,14 +131,11 @@ inline bool ex_carve(Scratch& ws, std::int64_t N, int M, std::int64_t fifo_total
     B.sw.dc2 = ws.take<std::uint32_t>(n);
     B.sw.dk = ws.take<float>(n);
     B.sw.dk2 = ws.take<float>(n);
-    B.sw.fc = ws.take<std::uint32_t>(n);
-    B.sw.fc2 = ws.take<std::uint32_t>(n);
-    B.sw.fk = ws.take<float>(n);
-    B.sw.fk2 = ws.take<float>(n);
-    B.sw.vc = ws.take<std::uint32_t>(n);
-    B.sw.vc2 = ws.take<std::uint32_t>(n);
-    B.sw.vk = ws.take<float>(n);
-    B.sw.vk2 = ws.take<float>(n);
+    B.sw.sc = ws.take<std::uint32_t>(n);
+    B.sw.sk = ws.take<float>(n);
+    B.sw.lc = ws.take<std::uint32_t>(static_cast<std::size_t>(kSwLv) * n);
+    B.sw.lk = ws.take<float>(static_cast<std::size_t>(kSwLv) * n);
+    B.sw.lstride = n;
     B.chain_order = ws.take<std::int32_t>(m);
     B.sw_ctr = ws.take<std::uint32_t>(m);
     B.nsorted = ws.take<std::int64_t>(m);
@@ -417,14 +414,10 @@ __global__ void __launch_bounds__(kSwThreads) ex_chain(const ExMember* __restric
         sb.dc2 += o;
         sb.dk += o;
         sb.dk2 += o;
-        sb.fc += o;
-        sb.fc2 += o;
-        sb.fk += o;
-        sb.fk2 += o;
-        sb.vc += o;
-        sb.vc2 += o;
-        sb.vk += o;
-        sb.vk2 += o;
+        sb.sc += o;
+        sb.sk += o;
+        sb.lc += o;
+        sb.lk += o;
     }
     WinStore mid{};
     mid.fq = reinterpret_cast<std::uint64_t*>(ex_csmem);

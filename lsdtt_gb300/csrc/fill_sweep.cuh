@@ -39,6 +39,7 @@ constexpr int kSwThreads = 512;
 // shared memory is sized to hold the widest FIFO generations of large basins)
 constexpr int kSwFQ = 4096;  // FIFO entries of one sweep (a power of two)
 constexpr int kSwL = 4096;   // entries of each per-sweep list (changed pops, discovered cells)
+constexpr int kSwLv = 4;     // levels of the heap cells at or above the near threshold
 
 // A cell's pop in the current sweep: valid when st is the sweep's id.
 struct __align__(16) SwEv
@@ -70,10 +71,12 @@ struct SweepBufs
                              // a value at or below the sweep's id: not yet in this sweep
     std::uint32_t *dc, *dc2; // heap cells discovered earlier, not popped, with a value
     float *dk, *dk2;         //   below the threshold T ("near", two buffers)
-    std::uint32_t *fc, *fc2; // the same at or above T and below U ("far", two buffers):
-    float *fk, *fk2;         //   scanned only when a sweep's FIFO values reach T
-    std::uint32_t *vc, *vc2; // the same at or above U ("very far", two buffers):
-    float *vk, *vk2;         //   scanned only when T reaches U
+    std::uint32_t* lc;       // the same at or above T, in kSwLv levels of lstride entries:
+    float* lk;               //   level 0 below Lb[1], level k in [Lb[k], Lb[k+1]), the last
+    std::size_t lstride;     //   unbounded; the bands grow 16-fold, a level is gathered and
+                             //   spread again only when T reaches its lower bound (a radix heap)
+    std::uint32_t* sc;       // spare list the gathering goes through
+    float* sk;
 };
 
 struct SweepShared
@@ -87,7 +90,7 @@ struct SweepShared
     std::uint32_t nlo[kSwFQ];
     std::uint8_t nk[kSwFQ];
     std::uint32_t la[kSwL], lb[kSwL], lt[kSwL];
-    std::uint32_t cnt[10];
+    std::uint32_t cnt[12];
     float red_v[kSwThreads / 32];
     std::uint32_t red_i[kSwThreads / 32];
     std::uint32_t red_s[kSwThreads / 32];
@@ -125,10 +128,12 @@ __device__ int win_sweep_replay(const WinGrid& G, int w, const SweepBufs& B, flo
 {
     const int tid = threadIdx.x;
     const float S = G.cuts[w];
-    __shared__ std::uint32_t s_ctr, s_m, s_nd, s_nf, s_nv, s_win, s_sweep, s_status, s_last_move;
+    __shared__ std::uint32_t s_ctr, s_m, s_nd, s_win, s_sweep, s_status, s_last_move;
+    __shared__ std::uint32_t s_nl[kSwLv];
     __shared__ std::int64_t s_p;
-    __shared__ float s_V, s_Vmax, s_T, s_U, s_D;
-    __shared__ int s_rebuild;
+    __shared__ float s_V, s_Vmax, s_T, s_D;
+    __shared__ float s_Lb[kSwLv];
+    __shared__ int s_j;
     __shared__ int s_cnext, s_next, s_stop;
     if (tid == 0)
     {
@@ -139,13 +144,18 @@ __device__ int win_sweep_replay(const WinGrid& G, int w, const SweepBufs& B, flo
         s_cnext = w + 1;
         s_m = 0;
         s_nd = 0;
-        s_nf = 0;
-        s_nv = 0;
-        // near/far threshold: four diagonal raise steps above the start
-        // (adapted as the window goes); far/very-far threshold 16 bands on
+        // near threshold T: four diagonal raise steps above the start
+        // (adapted as the window goes); level bounds 16, 256, 4096 bands on
         s_D = fmaxf(4.0f * G.eps * G.Ld, 1e-6f * fabsf(S) + 1e-30f);
         s_T = S + s_D;
-        s_U = s_T + 16.0f * s_D;
+        float wb = 16.0f * s_D;
+        s_Lb[0] = s_T;
+        for (int k = 0; k < kSwLv; ++k) s_nl[k] = 0;
+        for (int k = 1; k < kSwLv; ++k)
+        {
+            s_Lb[k] = s_T + wb;
+            wb *= 16.0f;
+        }
         s_last_move = 0;
         s_status = kWinOk;
         s_next = G.ncut;
@@ -165,14 +175,14 @@ __device__ int win_sweep_replay(const WinGrid& G, int w, const SweepBufs& B, flo
     std::uint32_t* dc2 = B.dc2;
     float* dk = B.dk;
     float* dk2 = B.dk2;
-    std::uint32_t* fcl = B.fc;
-    std::uint32_t* fcl2 = B.fc2;
-    float* fkl = B.fk;
-    float* fkl2 = B.fk2;
-    std::uint32_t* vcl = B.vc;
-    std::uint32_t* vcl2 = B.vc2;
-    float* vkl = B.vk;
-    float* vkl2 = B.vk2;
+    // level of a heap cell's key at or above T
+    auto level_of = [&](float key) -> int {
+        int k = 0;
+        while (k + 1 < kSwLv && !(key < s_Lb[k + 1])) ++k;
+        return k;
+    };
+    auto lvc = [&](int k) { return B.lc + static_cast<std::size_t>(k) * B.lstride; };
+    auto lvk = [&](int k) { return B.lk + static_cast<std::size_t>(k) * B.lstride; };
     // every pass pops at least one cell (a background pop or a sweep's
     // FIFO), so more passes than cells means the replay has gone wrong: it
     // is then left to the sequential rules
@@ -196,11 +206,18 @@ __device__ int win_sweep_replay(const WinGrid& G, int w, const SweepBufs& B, flo
                 s_p = p;
             }
             // the least discovered heap cell: in the first non-empty list
-            // (every near key is below T <= every far key < U <= every very-far key)
-            const int which = s_nd ? 0 : (s_nf ? 1 : 2);
-            const std::uint32_t* lc = which == 0 ? dc : (which == 1 ? fcl : vcl);
-            const float* lk = which == 0 ? dk : (which == 1 ? fkl : vkl);
-            const std::uint32_t ln = which == 0 ? s_nd : (which == 1 ? s_nf : s_nv);
+            // (every near key is below T, and every level's keys below the
+            // next level's)
+            int which = -1;
+            if (!s_nd)
+            {
+                which = kSwLv - 1;
+                for (int k = kSwLv - 2; k >= 0; --k)
+                    if (s_nl[k]) which = k;
+            }
+            const std::uint32_t* lc = which < 0 ? dc : lvc(which);
+            const float* lk = which < 0 ? dk : lvk(which);
+            const std::uint32_t ln = which < 0 ? s_nd : s_nl[which];
             float bz = INFINITY;
             std::uint32_t bi = kWinNone, bslot = kWinNone;
             for (std::uint32_t t = tid; t < ln; t += kSwThreads)
@@ -286,23 +303,19 @@ __device__ int win_sweep_replay(const WinGrid& G, int w, const SweepBufs& B, flo
                         if (from_list) ++s_p;
                         else
                         {
-                            if (which == 0)
+                            if (which < 0)
                             {
                                 const std::uint32_t last = --s_nd;
                                 dc[bslot] = dc[last];
                                 dk[bslot] = dk[last];
                             }
-                            else if (which == 1)
-                            {
-                                const std::uint32_t last = --s_nf;
-                                fcl[bslot] = fcl[last];
-                                fkl[bslot] = fkl[last];
-                            }
                             else
                             {
-                                const std::uint32_t last = --s_nv;
-                                vcl[bslot] = vcl[last];
-                                vkl[bslot] = vkl[last];
+                                const std::uint32_t last = --s_nl[which];
+                                std::uint32_t* wc = lvc(which);
+                                float* wk = lvk(which);
+                                wc[bslot] = wc[last];
+                                wk[bslot] = wk[last];
                             }
                             B.cst[hc] = (win << 2) | 3u;
                         }
@@ -336,17 +349,12 @@ __device__ int win_sweep_replay(const WinGrid& G, int w, const SweepBufs& B, flo
                                     dk[s_nd] = zj;
                                     ++s_nd;
                                 }
-                                else if (zj < s_U)
-                                {
-                                    fcl[s_nf] = j;
-                                    fkl[s_nf] = zj;
-                                    ++s_nf;
-                                }
                                 else
                                 {
-                                    vcl[s_nv] = j;
-                                    vkl[s_nv] = zj;
-                                    ++s_nv;
+                                    const int k = level_of(zj);
+                                    lvc(k)[s_nl[k]] = j;
+                                    lvk(k)[s_nl[k]] = zj;
+                                    ++s_nl[k];
                                 }
                                 B.cst[j] = (win << 2) | 1u;
                             }
@@ -368,8 +376,8 @@ __device__ int win_sweep_replay(const WinGrid& G, int w, const SweepBufs& B, flo
             s_ctr += 64;
             // cnt: [0] changed (la), [1] changed next (lb), [2] discovered
             // (lt), [3] surviving heap cells, [4] next FIFO, [5] overflow,
-            // [6..9] list moves and appends
-            for (int k = 0; k < 10; ++k) sh.cnt[k] = 0;
+            // [6..10] moves and appends to the near list and the levels
+            for (int k = 0; k < 12; ++k) sh.cnt[k] = 0;
         }
         {
             // the FIFO's largest value, and the next greater FIFO value after
@@ -413,8 +421,10 @@ __device__ int win_sweep_replay(const WinGrid& G, int w, const SweepBufs& B, flo
         const float Vmax = s_Vmax;
         if (Vmax >= s_T)
         {
-            // the FIFO reaches the far list: raise T and move the far cells
-            // below it to the near list
+            // the FIFO reaches T: raise it; the levels whose lower bound it
+            // has reached (0 .. j) are gathered and spread again, below T to
+            // the near list, the rest under new bounds (kept below level
+            // j + 1's); each cell goes down a level at a time
             if (tid == 0)
             {
                 // T moved again within 4 sweeps: widen the band; not within
@@ -423,127 +433,73 @@ __device__ int win_sweep_replay(const WinGrid& G, int w, const SweepBufs& B, flo
                 else if (sweep - s_last_move > 64u * 65u) s_D *= 0.5f;
                 s_last_move = sweep;
                 s_T = Vmax + s_D;
-                sh.cnt[6] = 0;
-                sh.cnt[7] = 0;
-                sh.cnt[8] = 0;
-                sh.cnt[9] = 0;
-                s_rebuild = s_T >= s_U;
-                if (s_rebuild) s_U = s_T + 16.0f * s_D;
+                s_Lb[0] = s_T;
+                int jl = 0;
+                for (int k = 1; k < kSwLv; ++k)
+                    if (!(s_T < s_Lb[k])) jl = k;
+                if (jl > 0)
+                {
+                    const float cap = jl + 1 < kSwLv ? s_Lb[jl + 1] : INFINITY;
+                    float wb = 16.0f * s_D;
+                    for (int k = 1; k <= jl; ++k)
+                    {
+                        s_Lb[k] = fminf(s_T + wb, cap);
+                        wb *= 16.0f;
+                    }
+                }
+                s_j = jl;
+                for (int k = 6; k < 12; ++k) sh.cnt[k] = 0;
             }
             __syncthreads();
-            if (s_rebuild)
+            const int jl = s_j;
+            std::uint32_t ng_all = 0;
+            for (int k = 0; k <= jl; ++k)
             {
-                // T reached U: the very-far cells below the new U join the far list
-                const float U = s_U;
-                const std::uint32_t nv = s_nv, nf0 = s_nf;
-                for (std::uint32_t t0 = 0; t0 < nv; t0 += kSwThreads)
+                const std::uint32_t nk = s_nl[k];
+                const std::uint32_t* src_c = lvc(k);
+                const float* src_k = lvk(k);
+                for (std::uint32_t t = tid; t < nk; t += kSwThreads)
                 {
-                    const std::uint32_t t = t0 + tid;
-                    const bool in = t < nv;
-                    const std::uint32_t c = in ? vcl[t] : 0u;
-                    const float k = in ? vkl[t] : INFINITY;
-                    const bool mv = in && k < U, kp = in && !mv;
-                    const int lane = tid & 31;
-                    unsigned b = __ballot_sync(0xffffffffu, mv);
-                    if (b)
-                    {
-                        const int lead = __ffs(b) - 1;
-                        std::uint32_t base = 0;
-                        if (lane == lead) base = atomicAdd(&sh.cnt[8], static_cast<std::uint32_t>(__popc(b)));
-                        base = __shfl_sync(0xffffffffu, base, lead);
-                        if (mv)
-                        {
-                            const std::uint32_t k2 = nf0 + base + __popc(b & ((1u << lane) - 1u));
-                            fcl[k2] = c;
-                            fkl[k2] = k;
-                        }
-                    }
-                    b = __ballot_sync(0xffffffffu, kp);
-                    if (b)
-                    {
-                        const int lead = __ffs(b) - 1;
-                        std::uint32_t base = 0;
-                        if (lane == lead) base = atomicAdd(&sh.cnt[9], static_cast<std::uint32_t>(__popc(b)));
-                        base = __shfl_sync(0xffffffffu, base, lead);
-                        if (kp)
-                        {
-                            const std::uint32_t k2 = base + __popc(b & ((1u << lane) - 1u));
-                            vcl2[k2] = c;
-                            vkl2[k2] = k;
-                        }
-                    }
+                    B.sc[ng_all + t] = src_c[t];
+                    B.sk[ng_all + t] = src_k[t];
                 }
-                __syncthreads();
-                if (tid == 0)
-                {
-                    s_nf = nf0 + sh.cnt[8];
-                    s_nv = sh.cnt[9];
-                    sh.cnt[8] = 0;
-                    sh.cnt[9] = 0;
-                }
-                {
-                    std::uint32_t* t1 = vcl;
-                    vcl = vcl2;
-                    vcl2 = t1;
-                    float* t2 = vkl;
-                    vkl = vkl2;
-                    vkl2 = t2;
-                }
-                __syncthreads();
+                ng_all += nk;
             }
+            __syncthreads();
             const float T = s_T;
-            const std::uint32_t nf = s_nf, nd0 = s_nd;
-            for (std::uint32_t t0 = 0; t0 < nf; t0 += kSwThreads)
+            const std::uint32_t nd0 = s_nd;
+            const int lane = tid & 31;
+            auto warp_append = [&](bool want, std::uint32_t* dst_c, float* dst_k, std::uint32_t* ctr, std::uint32_t c,
+                                   float key) {
+                const unsigned b = __ballot_sync(0xffffffffu, want);
+                if (!b) return;
+                const int lead = __ffs(b) - 1;
+                std::uint32_t base = 0;
+                if (lane == lead) base = atomicAdd(ctr, static_cast<std::uint32_t>(__popc(b)));
+                base = __shfl_sync(0xffffffffu, base, lead);
+                if (want)
+                {
+                    const std::uint32_t k2 = base + __popc(b & ((1u << lane) - 1u));
+                    dst_c[k2] = c;
+                    dst_k[k2] = key;
+                }
+            };
+            for (std::uint32_t t0 = 0; t0 < ng_all; t0 += kSwThreads)
             {
                 const std::uint32_t t = t0 + tid;
-                const bool in = t < nf;
-                const std::uint32_t c = in ? fcl[t] : 0u;
-                const float k = in ? fkl[t] : INFINITY;
-                const bool mv = in && k < T, kp = in && !mv;
-                const int lane = tid & 31;
-                unsigned b = __ballot_sync(0xffffffffu, mv);
-                if (b)
-                {
-                    const int lead = __ffs(b) - 1;
-                    std::uint32_t base = 0;
-                    if (lane == lead) base = atomicAdd(&sh.cnt[6], static_cast<std::uint32_t>(__popc(b)));
-                    base = __shfl_sync(0xffffffffu, base, lead);
-                    if (mv)
-                    {
-                        const std::uint32_t k2 = nd0 + base + __popc(b & ((1u << lane) - 1u));
-                        dc[k2] = c;
-                        dk[k2] = k;
-                    }
-                }
-                b = __ballot_sync(0xffffffffu, kp);
-                if (b)
-                {
-                    const int lead = __ffs(b) - 1;
-                    std::uint32_t base = 0;
-                    if (lane == lead) base = atomicAdd(&sh.cnt[7], static_cast<std::uint32_t>(__popc(b)));
-                    base = __shfl_sync(0xffffffffu, base, lead);
-                    if (kp)
-                    {
-                        const std::uint32_t k2 = base + __popc(b & ((1u << lane) - 1u));
-                        fcl2[k2] = c;
-                        fkl2[k2] = k;
-                    }
-                }
+                const bool in = t < ng_all;
+                const std::uint32_t c = in ? B.sc[t] : 0u;
+                const float key = in ? B.sk[t] : INFINITY;
+                const int dest = !in ? -2 : (key < T ? -1 : level_of(key));
+                warp_append(dest == -1, dc + nd0, dk + nd0, &sh.cnt[6], c, key);
+                for (int k = 0; k <= jl; ++k) warp_append(dest == k, lvc(k), lvk(k), &sh.cnt[7 + k], c, key);
             }
             __syncthreads();
             if (tid == 0)
             {
                 s_nd = nd0 + sh.cnt[6];
-                s_nf = sh.cnt[7];
-                for (int k = 0; k < 10; ++k) sh.cnt[k] = 0;
-            }
-            {
-                std::uint32_t* t1 = fcl;
-                fcl = fcl2;
-                fcl2 = t1;
-                float* t2 = fkl;
-                fkl = fkl2;
-                fkl2 = t2;
+                for (int k = 0; k <= jl; ++k) s_nl[k] = sh.cnt[7 + k];
+                for (int k = 0; k < 12; ++k) sh.cnt[k] = 0;
             }
             __syncthreads();
         }
@@ -838,17 +794,12 @@ __device__ int win_sweep_replay(const WinGrid& G, int w, const SweepBufs& B, flo
                     dc2[s2] = j;
                     dk2[s2] = zj;
                 }
-                else if (zj < s_U)
-                {
-                    const std::uint32_t s2 = s_nf + atomicAdd(&sh.cnt[6], 1u);
-                    fcl[s2] = j;
-                    fkl[s2] = zj;
-                }
                 else
                 {
-                    const std::uint32_t s2 = s_nv + atomicAdd(&sh.cnt[8], 1u);
-                    vcl[s2] = j;
-                    vkl[s2] = zj;
+                    const int k = level_of(zj);
+                    const std::uint32_t s2 = s_nl[k] + atomicAdd(&sh.cnt[7 + k], 1u);
+                    lvc(k)[s2] = j;
+                    lvk(k)[s2] = zj;
                 }
                 B.cst[j] = (win << 2) | 1u;
             }
@@ -865,8 +816,7 @@ __device__ int win_sweep_replay(const WinGrid& G, int w, const SweepBufs& B, flo
             for (int k = 0; k < kSwThreads / 32; ++k) v = fmaxf(v, sh.red_v[k]);
             s_V = v;
             s_nd = sh.cnt[3];
-            s_nf += sh.cnt[6];
-            s_nv += sh.cnt[8];
+            for (int k = 0; k < kSwLv; ++k) s_nl[k] += sh.cnt[7 + k];
             if (mn > static_cast<std::uint32_t>(kSwFQ)) s_status = kWinOverflow;
         }
         __syncthreads();
