@@ -448,9 +448,12 @@ def ensemble_reference(args, rank, world):
     return 0
 
 
-# Records that time a stage of several kernels (the s-vector stage), not one
-# kernel: listed, but never the roofline's dominant kernel.
+# Records that time a stage whose kernels are also timed one by one (the
+# s-vector stage): listed, but left out of the step's total and shares.
 ENS_STAGES = ("ens_stack_counts",)
+# Records of several kernels (those stages, and the exact fill's sorts and
+# scans): never the roofline's dominant kernel.
+ENS_MULTI = ENS_STAGES + ("ens_fill_exact_levels", "ens_fill_exact_candidates", "ens_fill_exact_cell_sort")
 
 
 def ensemble_gpu(args, rank, world):
@@ -567,7 +570,8 @@ def ensemble_gpu(args, rank, world):
     if rank == 0:
         peak, peak_kind = peaks()
         single = {k: v for k, v in kernels.items() if k not in ENS_STAGES}
-        dom = max(single.items(), key=lambda kv: kv[1]["ms"]) if single else None
+        one = {k: v for k, v in kernels.items() if k not in ENS_MULTI}
+        dom = max(one.items(), key=lambda kv: kv[1]["ms"]) if one else None
         step_ms = sum(v["ms"] for v in single.values())
         roof = None
         if dom:

@@ -1936,11 +1936,9 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
     {
         e = relax_all(E->zf0, 1, "ens_fill_relax_eps0");
         if (e != cudaSuccess) return e;
-        // Algorithmic bytes: z, F0, F1 4 each in, F 4 out per cell (the
-        // sorts and replays are latency-bound and not counted).
-        LSDTT_TIMED("ens_fill_exact", 16.0 * cells, st,
-                    (e = ex_run(E->d_exm, E->blk_member, N, M, E->ex_mbits, E->z, E->kind, E->zf0, E->zf, E->exB,
-                                E->exws, E->sms, st)));
+        // (each stage is timed inside, as ens_fill_exact_*)
+        e = ex_run(E->d_exm, E->blk_member, N, M, E->ex_mbits, E->z, E->kind, E->zf0, E->zf, E->exB, E->exws, E->sms,
+                   st, true);
         if (e != cudaSuccess) return e;
         ens_flag_copy_u<<<1, 1, 0, st>>>(E->exB.u + 5, E->flags + 8);
     }

@@ -542,11 +542,24 @@ inline cudaError_t ex_setup()
 // estimate for the members that are on; on return (in stream order) their
 // fill in the reference's order. `ws` holds the buffers carved by ex_carve
 // and room for the sort and scan scratch. `mbits` = bits of the member index
-// (0 for one member). Failures of the replays are left in B.u[5].
+// (0 for one member). Failures of the replays are left in B.u[5]. With
+// profiling on, each stage is timed under its name (`ens`: the ensemble's
+// names) with its algorithmic bytes: the records and keys it reads and
+// writes once per cell; the replays count one 16-byte record per cell,
+// though they are bound by the latency of their dependent steps.
 inline cudaError_t ex_run(const ExMember* mem, const std::uint16_t* blk_member, std::int64_t N, int M, int mbits,
                           const float* z, const std::uint8_t* kind, const float* F0, float* F, const ExBuffers& B,
-                          Scratch& ws, int sms, cudaStream_t st)
+                          Scratch& ws, int sms, cudaStream_t st, bool ens = false)
 {
+    static const char* const kNames[2][9] = {
+        {"fill_exact_prep", "fill_exact_levels", "fill_exact_candidates", "fill_exact_cell_sort",
+         "fill_exact_windows_small", "fill_exact_windows_mid", "fill_exact_windows_large", "fill_exact_chain",
+         "fill_exact_commit"},
+        {"ens_fill_exact_prep", "ens_fill_exact_levels", "ens_fill_exact_candidates", "ens_fill_exact_cell_sort",
+         "ens_fill_exact_windows_small", "ens_fill_exact_windows_mid", "ens_fill_exact_windows_large",
+         "ens_fill_exact_chain", "ens_fill_exact_commit"}};
+    const char* const* nm = kNames[ens ? 1 : 0];
+    const double cells = static_cast<double>(N);
     const unsigned nb = static_cast<unsigned>(N / 256);
     cudaError_t e = cudaMemsetAsync(B.u, 0, 16 * sizeof(unsigned), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(B.pool_used, 0, sizeof(unsigned long long), st);
@@ -560,46 +573,70 @@ inline cudaError_t ex_run(const ExMember* mem, const std::uint16_t* blk_member, 
     if (e == cudaSuccess) e = cudaMemsetAsync(B.sw.ev, 0, sizeof(SwEv) * static_cast<std::size_t>(N), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(B.sw_ctr, 0, sizeof(std::uint32_t) * M, st);
     if (e != cudaSuccess) return e;
-    ex_prep<<<nb, 256, 0, st>>>(mem, blk_member, N, z, kind, F0, B);
-    // distinct pour levels (the cell keys stay in key0/val0 meanwhile)
+    // z 4, kind 1, F0 4 in; record 16, keys 8 + 8, value 4 out
+    LSDTT_TIMED(nm[0], 45.0 * cells, st, (ex_prep<<<nb, 256, 0, st>>>(mem, blk_member, N, z, kind, F0, B)));
     const int bits = 32 + mbits;
-    // (the values carried by that sort are not used; wl2, off and cnt are
-    // free until the replays)
-    int r = radix_sort_pairs(B.pkey, reinterpret_cast<std::uint32_t*>(B.wl2), B.key1, B.val1, N, bits, ws, st, &e);
+    // distinct pour levels (the cell keys stay in key0/val0 meanwhile; the
+    // values carried by that sort are not used; wl2, off and cnt are free
+    // until the replays): keys and values in and out
+    auto levels = [&]() -> cudaError_t {
+        cudaError_t le = cudaSuccess;
+        const int r = radix_sort_pairs(B.pkey, reinterpret_cast<std::uint32_t*>(B.wl2), B.key1, B.val1, N, bits, ws,
+                                       st, &le);
+        if (le != cudaSuccess) return le;
+        const std::uint64_t* lk = r ? B.key1 : B.pkey;
+        std::uint32_t* flag = B.off;
+        std::uint32_t* pos = B.cnt;
+        ex_level_flags<<<nb, 256, 0, st>>>(lk, N, flag);
+        le = exclusive_scan<std::uint32_t, std::uint32_t>(flag, N, pos, B.u, ws, st);
+        if (le != cudaSuccess) return le;
+        ex_level_scatter<<<nb, 256, 0, st>>>(lk, N, flag, pos, B);
+        return exclusive_scan<int, int>(B.ncut, M, B.cut_base, static_cast<int*>(nullptr), ws, st);
+    };
+    LSDTT_TIMED(nm[1], 24.0 * cells, st, (e = levels()));
     if (e != cudaSuccess) return e;
-    const std::uint64_t* lk = r ? B.key1 : B.pkey;
-    std::uint32_t* flag = B.off;
-    std::uint32_t* pos = B.cnt;
-    ex_level_flags<<<nb, 256, 0, st>>>(lk, N, flag);
-    e = exclusive_scan<std::uint32_t, std::uint32_t>(flag, N, pos, B.u, ws, st);
+    // candidate starts: record 16 and F 4 in per cell
+    auto candidates = [&]() -> cudaError_t {
+        ex_cover<<<nb, 256, 0, st>>>(mem, blk_member, N, z, kind, F0, F, B);
+        const cudaError_t ce = exclusive_scan<int, int>(B.diff, N, B.excl, static_cast<int*>(nullptr), ws, st);
+        if (ce != cudaSuccess) return ce;
+        ex_candidates<<<nb, 256, 0, st>>>(N, B);
+        return cudaSuccess;
+    };
+    LSDTT_TIMED(nm[2], 20.0 * cells, st, (e = candidates()));
     if (e != cudaSuccess) return e;
-    ex_level_scatter<<<nb, 256, 0, st>>>(lk, N, flag, pos, B);
-    e = exclusive_scan<int, int>(B.ncut, M, B.cut_base, static_cast<int*>(nullptr), ws, st);
+    // the valid cells of each member by (F0, index): keys and values in and
+    // out, the sorted records out
+    auto cell_sort = [&]() -> cudaError_t {
+        cudaError_t ce = cudaSuccess;
+        const int r = radix_sort_pairs(B.key0, B.val0, B.key1, B.val1, N, bits, ws, st, &ce);
+        if (ce != cudaSuccess) return ce;
+        ex_gather<<<nb, 256, 0, st>>>(mem, blk_member, N, r ? B.val1 : B.val0, B);
+        ex_base<<<nb, 256, 0, st>>>(mem, blk_member, N, z, kind, F);
+        return cudaSuccess;
+    };
+    LSDTT_TIMED(nm[3], 40.0 * cells, st, (e = cell_sort()));
     if (e != cudaSuccess) return e;
-    // candidate starts
-    ex_cover<<<nb, 256, 0, st>>>(mem, blk_member, N, z, kind, F0, F, B);
-    e = exclusive_scan<int, int>(B.diff, N, B.excl, static_cast<int*>(nullptr), ws, st);
-    if (e != cudaSuccess) return e;
-    ex_candidates<<<nb, 256, 0, st>>>(N, B);
-    // the valid cells of each member by (F0, index)
-    r = radix_sort_pairs(B.key0, B.val0, B.key1, B.val1, N, bits, ws, st, &e);
-    if (e != cudaSuccess) return e;
-    ex_gather<<<nb, 256, 0, st>>>(mem, blk_member, N, r ? B.val1 : B.val0, B);
-    ex_base<<<nb, 256, 0, st>>>(mem, blk_member, N, z, kind, F);
     // replays: small shared-memory size, then two larger ones for the
     // overflows of the one before (the sizes trade room for warps per SM:
     // 20, 7 and 3); wl is free again once the middle size has its list
-    ex_windows<kExA_FQ, kExA_DH, kExA_HS, kExA_OC><<<sms * 20, 32, kExSmemA, st>>>(
-        mem, z, kind, F0, B, B.wl, B.u + 1, B.u + 2, static_cast<unsigned long long>(N), 16ull * kExA_HS);
-    ex_overflow_list<<<nb, 256, 0, st>>>(N, B.wl, B.u + 1, B.wl2, B.u + 3, B.status);
-    ex_windows<kExM_FQ, kExM_DH, kExM_HS, kExM_OC><<<sms * 7, 32, kExSmemM, st>>>(
-        mem, z, kind, F0, B, B.wl2, B.u + 3, B.u + 4, static_cast<unsigned long long>(N), 16ull * kExM_HS);
-    ex_overflow_list<<<nb, 256, 0, st>>>(N, B.wl2, B.u + 3, B.wl, B.u + 6, B.status);
-    ex_windows<kExB_FQ, kExB_DH, kExB_HS, kExB_OC><<<sms * 3, 32, kExSmemB, st>>>(
-        mem, z, kind, F0, B, B.wl, B.u + 6, B.u + 7, static_cast<unsigned long long>(N), 16ull * kExB_HS);
-    ex_chain<kExC_FQ, kExC_DH><<<M, kSwThreads, kExSmemC, st>>>(mem, z, kind, F0, F, B);
-    ex_commit<<<static_cast<unsigned>(std::max<std::int64_t>(1, std::min<std::int64_t>(N / 8, sms * 64))), 256, 0,
-                st>>>(mem, N, F, B);
+    LSDTT_TIMED(nm[4], 16.0 * cells, st,
+                (ex_windows<kExA_FQ, kExA_DH, kExA_HS, kExA_OC><<<sms * 20, 32, kExSmemA, st>>>(
+                    mem, z, kind, F0, B, B.wl, B.u + 1, B.u + 2, static_cast<unsigned long long>(N), 16ull * kExA_HS)));
+    LSDTT_TIMED(nm[5], 16.0 * cells, st,
+                (ex_overflow_list<<<nb, 256, 0, st>>>(N, B.wl, B.u + 1, B.wl2, B.u + 3, B.status),
+                 ex_windows<kExM_FQ, kExM_DH, kExM_HS, kExM_OC><<<sms * 7, 32, kExSmemM, st>>>(
+                     mem, z, kind, F0, B, B.wl2, B.u + 3, B.u + 4, static_cast<unsigned long long>(N), 16ull * kExM_HS)));
+    LSDTT_TIMED(nm[6], 16.0 * cells, st,
+                (ex_overflow_list<<<nb, 256, 0, st>>>(N, B.wl2, B.u + 3, B.wl, B.u + 6, B.status),
+                 ex_windows<kExB_FQ, kExB_DH, kExB_HS, kExB_OC><<<sms * 3, 32, kExSmemB, st>>>(
+                     mem, z, kind, F0, B, B.wl, B.u + 6, B.u + 7, static_cast<unsigned long long>(N), 16ull * kExB_HS)));
+    LSDTT_TIMED(nm[7], 16.0 * cells, st,
+                (ex_chain<kExC_FQ, kExC_DH><<<M, kSwThreads, kExSmemC, st>>>(mem, z, kind, F0, F, B)));
+    // the staged raised cells: cell 4 + value 4 in, 4 out at most per cell
+    LSDTT_TIMED(nm[8], 12.0 * cells, st,
+                (ex_commit<<<static_cast<unsigned>(std::max<std::int64_t>(1, std::min<std::int64_t>(N / 8, sms * 64))),
+                             256, 0, st>>>(mem, N, F, B)));
     return cudaGetLastError();
 }
 
