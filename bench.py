@@ -281,13 +281,8 @@ def routing_gpu(args, rank, world):
         barrier()
     elapsed = ev0.elapsed_time(ev1) / 1e3
     launches = L.lsdtt_gpu_launch_count() - launches0
-    # Kernel table from the live event pairs.
-    kernels = {}
-    for name in ("fill_relax", "d8_receivers", "d8_donors", "stack_ruler_walk"):
-        t, k, b = ctypes.c_double(), ctypes.c_int64(), ctypes.c_double()
-        G._check(L.lsdtt_gpu_profile_read(name.encode(), ctypes.byref(t), ctypes.byref(k), ctypes.byref(b)))
-        if k.value:
-            kernels[name] = {"ms": t.value, "launches": k.value, "bytes": b.value}
+    # Kernel table from the live event pairs (every record of the timed steps).
+    kernels = profile_table(L)
     L.lsdtt_gpu_profile_enable(0)
     t_max = rank_max(elapsed, dist)
     value = job_rate(n * n, args.steps, t_max, world)
@@ -321,7 +316,10 @@ def routing_gpu(args, rank, world):
 
     if rank == 0:
         peak, peak_kind = peaks()
-        dom = max(kernels.items(), key=lambda kv: kv[1]["ms"]) if kernels else None
+        # the exact fill's sort and scan stages are several kernels each
+        one = {k: v for k, v in kernels.items()
+               if k not in ("fill_exact_levels", "fill_exact_candidates", "fill_exact_cell_sort")}
+        dom = max(one.items(), key=lambda kv: kv[1]["ms"]) if one else None
         roof = None
         if dom:
             name, d = dom
@@ -346,7 +344,9 @@ def routing_gpu(args, rank, world):
                        "l2": "inputs (z 268 MB + mask 67 MB) larger than the 129 MB L2; no flush"},
             "roofline": roof,
             "kernels": {k: {"ms_per_launch": v["ms"] / v["launches"], "launches": v["launches"],
-                            "GBps": v["bytes"] / (v["ms"] / 1e3) / 1e9} for k, v in kernels.items()},
+                            "share": v["ms"] / (elapsed * 1e3),
+                            "GBps": (v["bytes"] / (v["ms"] / 1e3) / 1e9) if v["bytes"] > 0 else None}
+                        for k, v in sorted(kernels.items(), key=lambda kv: -kv[1]["ms"])},
             "cpu_baseline": None if cpu_v is None else {
                 "value": cpu_v, "unit": "cell-steps/s", "cores": os.cpu_count(), "kind": "port",
                 "sample": f"{args.cpu_sample}x{args.cpu_sample} sample of the same surface: fill + D8 + s-vector + "
