@@ -112,8 +112,9 @@ int lsdtt_gpu_fill_pits(const lsdtt_gpu_grid* grid, const float* z_dev, const ui
  * at min_slope <= 0 and, because the raised cells' reference order needs
  * about 240 bytes a cell of replay buffers, about 520 x 520 cells at
  * min_slope > 0; larger grids return LSDTT_GPU_EINVAL. Same results as
- * lsdtt_gpu_fill_pits. The first call on a device looks up the array's
- * device address: make it before any stream capture. All calls share the
+ * lsdtt_gpu_fill_pits. It is never capturable: every call reads flags back
+ * to the host between passes, and a call on a stream that is capturing
+ * returns LSDTT_GPU_EINVAL before it enqueues anything. All calls share the
  * array, so calls that overlap on the GPU race; order them on one stream. */
 int lsdtt_gpu_fill_pits_noalloc(const lsdtt_gpu_grid* grid, const float* z_dev, const uint8_t* mask_dev,
                                 float min_slope, float* filled_dev, void* stream);

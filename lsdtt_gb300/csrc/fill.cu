@@ -464,6 +464,16 @@ extern "C" int lsdtt_gpu_fill_pits_noalloc(const lsdtt_gpu_grid* grid, const flo
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
         return fail(LSDTT_GPU_ENODEV, "lsdtt_gpu_fill_pits_noalloc: no CUDA device");
+    {
+        // every call reads flags back to the host between passes, which a
+        // stream capture cannot hold: refuse before anything is enqueued
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        if (cudaStreamIsCapturing(static_cast<cudaStream_t>(stream), &cs) != cudaSuccess)
+            return fail(LSDTT_GPU_EINVAL, "lsdtt_gpu_fill_pits_noalloc: cannot query the stream's capture state");
+        if (cs != cudaStreamCaptureStatusNone)
+            return fail(LSDTT_GPU_EINVAL, "lsdtt_gpu_fill_pits_noalloc: the stream is capturing; this call waits on "
+                                          "the host between passes and cannot be captured");
+    }
     if (!(grid->n_rows > 0 && grid->n_cols > 0 && grid->cell_size > 0.0))
         return fail(LSDTT_GPU_EINVAL, "lsdtt::fill_pits: invalid raster metadata");
     auto is_p = [&](int i) { return grid->boundary_conditions[i] == 'p' || grid->boundary_conditions[i] == 'P'; };

@@ -224,20 +224,16 @@ __device__ __forceinline__ std::uint32_t win_hash(std::uint32_t x, std::uint32_t
 }
 
 // Insert `cell` into the shared-memory seen set; false if it was there
-// already (or the set is full: *full is set).
-__device__ __forceinline__ bool win_seen_insert(const WinStore& s, std::uint32_t cell, std::uint32_t* count,
-                                                bool* full)
+// already (or every slot was probed: *full is set). The caller counts the
+// insertions warp-wide and keeps the set at most three quarters full.
+__device__ __forceinline__ bool win_seen_insert(const WinStore& s, std::uint32_t cell, bool* full)
 {
     const std::uint32_t mask = s.hscap - 1;
     std::uint32_t h = win_hash(cell, mask);
     for (std::uint32_t probe = 0; probe < s.hscap; ++probe)
     {
         const std::uint32_t prev = atomicCAS(&s.hs[h], kWinNone, cell);
-        if (prev == kWinNone)
-        {
-            if (atomicAdd(count, 1u) + 1 > (s.hscap >> 1) + (s.hscap >> 2)) *full = true;
-            return true;
-        }
+        if (prev == kWinNone) return true;
         if (prev == cell) return false;
         h = (h + 1) & mask;
     }
@@ -267,14 +263,8 @@ __device__ WinResult win_replay(const WinGrid& G, int w, const WinStore& s, std:
     const int lane = threadIdx.x & 31;
     const unsigned full = 0xffffffffu;
     const float S = G.cuts[w];
-    __shared__ std::uint32_t sh_seen_count[32];  // one per warp of the block
-    __shared__ bool sh_full[32];
-    const int wib = threadIdx.x >> 5;
-    if (lane == 0)
-    {
-        sh_seen_count[wib] = 0;
-        sh_full[wib] = false;
-    }
+    std::uint32_t seen = 0;  // cells in the seen set (warp-uniform)
+    const std::uint32_t seen_cap = (s.hscap >> 1) + (s.hscap >> 2);
     if (s.hs)
         for (std::uint32_t k = lane; k < s.hscap; k += 32) s.hs[k] = kWinNone;
     __syncwarp();
@@ -490,7 +480,7 @@ __device__ WinResult win_replay(const WinGrid& G, int w, const WinStore& s, std:
                 const std::uint32_t other = __shfl_sync(full, j, k);
                 if (lane > k && j != kWinNone && other == j) j = kWinNone;
             }
-        bool fresh = false;
+        bool fresh = false, probe_full = false;
         if (j != kWinNone)
         {
             if (s.stamp)
@@ -499,17 +489,20 @@ __device__ WinResult win_replay(const WinGrid& G, int w, const WinStore& s, std:
                 if (fresh) s.stamp[j] = s.stamp_id;
             }
             else
-                fresh = win_seen_insert(s, j, &sh_seen_count[wib], &sh_full[wib]);
-        }
-        __syncwarp();
-        if (sh_full[wib])
-        {
-            res.status = kWinOverflow;
-            break;
+                fresh = win_seen_insert(s, j, &probe_full);
         }
         const bool raised = fresh && zj <= cur_v;
         const unsigned rb = __ballot_sync(full, raised);
         const unsigned hb = __ballot_sync(full, fresh && !raised);
+        if (s.hs)
+        {
+            seen += __popc(rb | hb);
+            if (__any_sync(full, probe_full) || seen > seen_cap)
+            {
+                res.status = kWinOverflow;
+                break;
+            }
+        }
         if (tail - head + __popc(rb) > s.fcap || hsize + __popc(hb) > s.hcap)
         {
             res.status = kWinOverflow;
@@ -522,16 +515,17 @@ __device__ WinResult win_replay(const WinGrid& G, int w, const WinStore& s, std:
             s.fq[slot] = win_fentry(nz, j);
         }
         tail += __popc(rb);
-        // heap pushes by lane 0
+        // heap pushes, each by the lane that found the cell, in lane order
+        // (every lane keeps the heap size)
+        const std::uint64_t my_key = win_hkey(zj, j);
         unsigned m = hb;
         while (m)
         {
             const int k = __ffs(m) - 1;
             m &= m - 1;
-            const float kz = __shfl_sync(full, zj, k);
-            const std::uint32_t kc = __shfl_sync(full, j, k);
-            if (lane == 0) win_heap_push(s, hsize, win_hkey(kz, kc));
+            if (lane == k) win_heap_push(s, hsize, my_key);
             else ++hsize;
+            __syncwarp();
         }
         __syncwarp();
     }

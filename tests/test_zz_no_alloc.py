@@ -7,7 +7,8 @@ scratch array keeps the previous call's contents, so the second call checks
 that everything that must start from a known state is reset), and compared
 with the allocating entry point lsdtt_gpu_fill_pits. Both run the same
 kernels, so the tolerance is zero: identical bits. Also checks that a grid
-larger than the fixed scratch is refused with a clear message.
+larger than the fixed scratch is refused with a clear message, and that a
+call on a capturing stream is refused before it enqueues anything.
 
 Named test_zz_* so pytest collects it after every other test file; it also
 passes on its own in a fresh process.
@@ -73,3 +74,28 @@ def test_noalloc_fill_refuses_grids_beyond_its_scratch():
                                        ctypes.c_void_p(zt.data_ptr()), None)
     assert st == G.EINVAL
     assert b"fixed scratch" in L.lsdtt_gpu_last_error()
+
+
+def test_noalloc_fill_refuses_a_capturing_stream():
+    """The call reads flags back to the host between passes, so it cannot be
+    captured: on a stream that is capturing it returns EINVAL before it
+    enqueues anything, and the capture stays valid."""
+    G, L = _abi()
+    import torch
+    z = surfaces.fractal_pits(128)
+    zt = torch.from_numpy(z).cuda()
+    mt = torch.ones_like(zt, dtype=torch.uint8)
+    out = torch.empty_like(zt)
+    g = G.make_grid(128, 128, 10.0, "oooo")
+    s = torch.cuda.Stream()
+    graph = torch.cuda.CUDAGraph()
+    torch.cuda.synchronize()
+    with torch.cuda.graph(graph, stream=s):
+        st = L.lsdtt_gpu_fill_pits_noalloc(ctypes.byref(g), ctypes.c_void_p(zt.data_ptr()),
+                                           ctypes.c_void_p(mt.data_ptr()), ctypes.c_float(1e-4),
+                                           ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(s.cuda_stream))
+        out.add_(0.0)  # something for the capture to hold
+    assert st == G.EINVAL
+    assert b"capturing" in L.lsdtt_gpu_last_error()
+    graph.replay()
+    torch.cuda.synchronize()
