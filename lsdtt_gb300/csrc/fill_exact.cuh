@@ -10,8 +10,9 @@
 //      raised in the estimate;
 //   4. the valid cells of each member sorted by (F0, index);
 //   5. every candidate replayed by one warp with its state in shared memory
-//      (three sizes, each taking the overflows of the one before); raised
-//      cells staged in a pool;
+//      (three sizes, each taking the overflows of the one before; the two
+//      larger only when the members are fewer than the SMs); raised cells
+//      staged in a pool;
 //   6. per member, one block follows the chain of valid windows from the
 //      lowest cut; a window on it that no size could hold is replayed by
 //      the whole block one FIFO sweep at a time (fill_sweep.cuh), or, where
@@ -619,18 +620,27 @@ inline cudaError_t ex_run(const ExMember* mem, const std::uint16_t* blk_member, 
     if (e != cudaSuccess) return e;
     // replays: small shared-memory size, then two larger ones for the
     // overflows of the one before (the sizes trade room for warps per SM:
-    // 20, 7 and 3); wl is free again once the middle size has its list
+    // 20, 7 and 3); wl is free again once the middle size has its list.
+    // The larger sizes pay only where the chains are few: with a member per
+    // SM or more, the chains' block sweeps replay the windows the small size
+    // could not hold -- only those on a chain, where the larger sizes replay
+    // every such candidate one pop at a time -- and the step is faster
+    // without them (256 members: 358 ms a step with them, 234 ms without;
+    // one 2048 x 2048 grid: 498 ms with them, 779 ms without)
     LSDTT_TIMED(nm[4], 16.0 * cells, st,
                 (ex_windows<kExA_FQ, kExA_DH, kExA_HS, kExA_OC><<<sms * 20, 32, kExSmemA, st>>>(
                     mem, z, kind, F0, B, B.wl, B.u + 1, B.u + 2, static_cast<unsigned long long>(N), 16ull * kExA_HS)));
-    LSDTT_TIMED(nm[5], 16.0 * cells, st,
-                (ex_overflow_list<<<nb, 256, 0, st>>>(N, B.wl, B.u + 1, B.wl2, B.u + 3, B.status),
-                 ex_windows<kExM_FQ, kExM_DH, kExM_HS, kExM_OC><<<sms * 7, 32, kExSmemM, st>>>(
-                     mem, z, kind, F0, B, B.wl2, B.u + 3, B.u + 4, static_cast<unsigned long long>(N), 16ull * kExM_HS)));
-    LSDTT_TIMED(nm[6], 16.0 * cells, st,
-                (ex_overflow_list<<<nb, 256, 0, st>>>(N, B.wl2, B.u + 3, B.wl, B.u + 6, B.status),
-                 ex_windows<kExB_FQ, kExB_DH, kExB_HS, kExB_OC><<<sms * 3, 32, kExSmemB, st>>>(
-                     mem, z, kind, F0, B, B.wl, B.u + 6, B.u + 7, static_cast<unsigned long long>(N), 16ull * kExB_HS)));
+    if (M < sms)
+    {
+        LSDTT_TIMED(nm[5], 16.0 * cells, st,
+                    (ex_overflow_list<<<nb, 256, 0, st>>>(N, B.wl, B.u + 1, B.wl2, B.u + 3, B.status),
+                     ex_windows<kExM_FQ, kExM_DH, kExM_HS, kExM_OC><<<sms * 7, 32, kExSmemM, st>>>(
+                         mem, z, kind, F0, B, B.wl2, B.u + 3, B.u + 4, static_cast<unsigned long long>(N), 16ull * kExM_HS)));
+        LSDTT_TIMED(nm[6], 16.0 * cells, st,
+                    (ex_overflow_list<<<nb, 256, 0, st>>>(N, B.wl2, B.u + 3, B.wl, B.u + 6, B.status),
+                     ex_windows<kExB_FQ, kExB_DH, kExB_HS, kExB_OC><<<sms * 3, 32, kExSmemB, st>>>(
+                         mem, z, kind, F0, B, B.wl, B.u + 6, B.u + 7, static_cast<unsigned long long>(N), 16ull * kExB_HS)));
+    }
     LSDTT_TIMED(nm[7], 16.0 * cells, st,
                 (ex_chain<kExC_FQ, kExC_DH><<<M, kSwThreads, kExSmemC, st>>>(mem, z, kind, F0, F, B)));
     // the staged raised cells: cell 4 + value 4 in, 4 out at most per cell

@@ -63,3 +63,37 @@ def test_fill_epsilon_bitwise(port):
         if nd:
             bad[name] = nd
     assert not bad, bad
+
+
+def test_ensemble_with_a_member_per_sm_fills_like_single_grids():
+    """An ensemble with at least one member per SM leaves the windows the
+    small replay size cannot hold to its chains' block sweeps (fewer members
+    also replay them at two larger sizes): its fill equals the single-grid
+    fill bit for bit on every member, noise-plus-tilt surfaces whose long
+    episodes outgrow the small size, and pitted fractals."""
+    import torch
+    import lsdtt_gb300 as G
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    members = []
+    for k in range(sms + 8):
+        if k % 4 == 3:
+            z = surfaces.fractal_pits(64, seed=100 + k)
+            bc = "oooo"
+        else:
+            z = surfaces.noise_tilt(40 + (k % 7) * 9, 48 + (k % 5) * 11, 30.0, 1000 + k, "nnon", 0.001)
+            bc = "nnon"
+        members.append(dict(z=z, cell_size=30.0 if bc == "nnon" else 10.0, boundary_conditions=bc,
+                            fill_min_slope=1e-4, erodibility=0.0, enable_hillslope=False, uplift_rate=0.0))
+    ens = G.Ensemble(members, use_graph=False)
+    try:
+        ens.step()
+        bad = []
+        for k, s in enumerate(members):
+            got = ens.get(k).cpu().numpy()
+            m = np.ones_like(s["z"], np.uint8)
+            want = G.fill_pits(s["z"], m, s["cell_size"], s["boundary_conditions"], 1e-4).cpu().numpy()
+            if not np.array_equal(got.view(np.uint32), want.view(np.uint32)):
+                bad.append(k)
+        assert not bad, bad
+    finally:
+        ens.close()
