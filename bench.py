@@ -592,7 +592,7 @@ def ensemble_gpu(args, rank, world):
                     "source": "CUDA events around every kernel launch of one profiled (eager) step of the same "
                               "ensemble, run right after the timed region; the dominant kernel is the one with the "
                               "largest total"}
-        # The survey's >= 60% of HBM bar for the D8 receivers and the
+        # The >= 60% of HBM bar for the D8 receivers and the
         # contributing counts (algorithmic bytes per cell: receivers 6 + the
         # exported int64 receiver 8; counts 10).
         bars = {}
