@@ -67,7 +67,7 @@ struct ExBuffers
     std::int64_t* nsorted;  // [M]
     int *ncut, *cut_base;   // [M], [M + 1]
     unsigned* u;            // [0] total cuts, [1] nwl, [2] work, [3] nwl2, [4] work2, [5] error,
-                            // [6] nwl3, [7] work3
+                            // [6] nwl3, [7] work3, [8] pour keys
     unsigned long long* pool_used;
 };
 
@@ -157,7 +157,8 @@ __device__ __forceinline__ WinGrid ex_member_grid(const ExMember& M, int m, cons
 
 // 1. Per cell: the replay record {z, F0, smallest F0 among valid neighbours
 // (-inf for seeds), valid}, the cell sort key (member, F0; 2^32-1 puts
-// invalid and NaN cells last in their member) and the pour-level key.
+// invalid and NaN cells last in their member) and, for a pour cell, the
+// pour-level key (member, F0), appended to a compact list counted in u[8].
 // 256-thread blocks over the packed cells (a block never spans two members).
 __global__ void ex_prep(const ExMember* __restrict__ mem, const std::uint16_t* __restrict__ blk_member,
                         std::int64_t N, const float* __restrict__ z, const std::uint8_t* __restrict__ kind,
@@ -169,7 +170,8 @@ __global__ void ex_prep(const ExMember* __restrict__ mem, const std::uint16_t* _
     const ExMember M = mem[m];
     const std::uint64_t hi = static_cast<std::uint64_t>(m) << 32;
     const std::int64_t local = i - M.base;
-    bool valid = false;
+    bool valid = false, has_pour = false;
+    std::uint64_t pour_key = 0;
     if (i < N)
     {
         B.val0[i] = static_cast<std::uint32_t>(i);
@@ -179,7 +181,6 @@ __global__ void ex_prep(const ExMember* __restrict__ mem, const std::uint16_t* _
             zi = z[i];
             valid = !isnan(zi);
         }
-        std::uint32_t plev = 0xffffffffu;
         if (!valid)
         {
             B.rec[i] = make_float4(0.0f, 0.0f, INFINITY, 0.0f);
@@ -205,9 +206,20 @@ __global__ void ex_prep(const ExMember* __restrict__ mem, const std::uint16_t* _
                 if (zi <= f && zj == fj && fj == f) pour = true;
             }
             B.rec[i] = make_float4(zi, f, (kind[i] == 2) ? -INFINITY : mn, 1.0f);
-            if (pour) plev = float_order_key(f);
+            has_pour = pour;
+            pour_key = hi | float_order_key(f);
         }
-        B.pkey[i] = hi | plev;
+    }
+    // the pour keys, compacted (one atomic per warp); their order is undone
+    // by the sort
+    const unsigned pb = __ballot_sync(0xffffffffu, has_pour);
+    if (pb)
+    {
+        const int lane = threadIdx.x & 31, lead = __ffs(pb) - 1;
+        unsigned base = 0;
+        if (lane == lead) base = atomicAdd(&B.u[8], static_cast<unsigned>(__popc(pb)));
+        base = __shfl_sync(0xffffffffu, base, lead);
+        if (has_pour) B.pkey[base + __popc(pb & ((1u << lane) - 1u))] = pour_key;
     }
     const unsigned b = __ballot_sync(0xffffffffu, valid);
     if ((threadIdx.x & 31) == 0 && b) atomicAdd(reinterpret_cast<unsigned long long*>(&B.nsorted[m]),
@@ -215,13 +227,19 @@ __global__ void ex_prep(const ExMember* __restrict__ mem, const std::uint16_t* _
 }
 
 // 2. First-of-run flags over the sorted pour-level keys, then the levels.
-__global__ void ex_level_flags(const std::uint64_t* __restrict__ key, std::int64_t N, std::uint32_t* __restrict__ flag)
+__global__ void ex_level_flags(const std::uint64_t* __restrict__ key, std::int64_t N,
+                               const unsigned* __restrict__ nkeys, std::uint32_t* __restrict__ flag)
 {
     LSDTT_COUNT();
     const std::int64_t k = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (k >= N) return;
+    if (k >= static_cast<std::int64_t>(*nkeys))
+    {
+        flag[k] = 0u;
+        return;
+    }
     const std::uint64_t v = key[k];
-    flag[k] = ((v & 0xffffffffull) != 0xffffffffull && (k == 0 || key[k - 1] != v)) ? 1u : 0u;
+    flag[k] = (k == 0 || key[k - 1] != v) ? 1u : 0u;
 }
 
 __global__ void ex_level_scatter(const std::uint64_t* __restrict__ key, std::int64_t N,
@@ -577,18 +595,18 @@ inline cudaError_t ex_run(const ExMember* mem, const std::uint16_t* blk_member, 
     // z 4, kind 1, F0 4 in; record 16, keys 8 + 8, value 4 out
     LSDTT_TIMED(nm[0], 45.0 * cells, st, (ex_prep<<<nb, 256, 0, st>>>(mem, blk_member, N, z, kind, F0, B)));
     const int bits = 32 + mbits;
-    // distinct pour levels (the cell keys stay in key0/val0 meanwhile; the
-    // values carried by that sort are not used; wl2, off and cnt are free
-    // until the replays): keys and values in and out
+    // distinct pour levels: the compacted pour keys sorted (the cell keys
+    // stay in key0/val0 meanwhile; the values carried by that sort are not
+    // used; wl2, off and cnt are free until the replays)
     auto levels = [&]() -> cudaError_t {
         cudaError_t le = cudaSuccess;
         const int r = radix_sort_pairs(B.pkey, reinterpret_cast<std::uint32_t*>(B.wl2), B.key1, B.val1, N, bits, ws,
-                                       st, &le);
+                                       st, &le, B.u + 8);
         if (le != cudaSuccess) return le;
         const std::uint64_t* lk = r ? B.key1 : B.pkey;
         std::uint32_t* flag = B.off;
         std::uint32_t* pos = B.cnt;
-        ex_level_flags<<<nb, 256, 0, st>>>(lk, N, flag);
+        ex_level_flags<<<nb, 256, 0, st>>>(lk, N, B.u + 8, flag);
         le = exclusive_scan<std::uint32_t, std::uint32_t>(flag, N, pos, B.u, ws, st);
         if (le != cudaSuccess) return le;
         ex_level_scatter<<<nb, 256, 0, st>>>(lk, N, flag, pos, B);

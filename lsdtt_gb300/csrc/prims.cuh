@@ -149,16 +149,19 @@ inline cudaError_t exclusive_scan(const TIn* in, std::int64_t n, T* out, T* tota
 // ---------------------------------------------------------------------------
 // Stable LSD radix sort of (uint64 key, uint32 value) pairs over the low
 // `bits` bits of the key, 8 bits per pass. Ping-pongs between (k0,v0) and
-// (k1,v1); returns the buffer index (0 or 1) holding the result.
+// (k1,v1); returns the buffer index (0 or 1) holding the result. With a
+// device count `dn`, only the first min(n, *dn) pairs are sorted (the
+// launches stay sized for n; tiles past the count do nothing).
 // ---------------------------------------------------------------------------
 constexpr int kSortThreads = 256;  // 8 warps
 constexpr int kSortWarpItems = 512;  // per warp: 16 rounds of 32
 constexpr int kSortTile = kSortWarpItems * (kSortThreads / 32);  // 4096
 
 static __global__ void radix_hist(const std::uint64_t* __restrict__ keys, std::int64_t n, int shift,
-                           std::uint32_t* __restrict__ hist, int n_tiles)
+                           std::uint32_t* __restrict__ hist, int n_tiles, const unsigned* __restrict__ dn)
 {
     LSDTT_COUNT();
+    if (dn && static_cast<std::int64_t>(*dn) < n) n = static_cast<std::int64_t>(*dn);
     __shared__ std::uint32_t h[256];
     for (int i = threadIdx.x; i < 256; i += blockDim.x) h[i] = 0;
     __syncthreads();
@@ -175,9 +178,11 @@ static __global__ void radix_hist(const std::uint64_t* __restrict__ keys, std::i
 
 static __global__ void radix_scatter(const std::uint64_t* __restrict__ kin, const std::uint32_t* __restrict__ vin,
                               std::int64_t n, int shift, const std::uint32_t* __restrict__ offs, int n_tiles,
-                              std::uint64_t* __restrict__ kout, std::uint32_t* __restrict__ vout)
+                              std::uint64_t* __restrict__ kout, std::uint32_t* __restrict__ vout,
+                              const unsigned* __restrict__ dn)
 {
     LSDTT_COUNT();
+    if (dn && static_cast<std::int64_t>(*dn) < n) n = static_cast<std::int64_t>(*dn);
     __shared__ std::uint32_t wcount[kSortThreads / 32][256];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int i = lane; i < 256; i += 32) wcount[warp][i] = 0;
@@ -232,7 +237,8 @@ static __global__ void radix_scatter(const std::uint64_t* __restrict__ kin, cons
 }
 
 inline int radix_sort_pairs(std::uint64_t* k0, std::uint32_t* v0, std::uint64_t* k1, std::uint32_t* v1,
-                            std::int64_t n, int bits, Scratch& ws, cudaStream_t st, cudaError_t* err)
+                            std::int64_t n, int bits, Scratch& ws, cudaStream_t st, cudaError_t* err,
+                            const unsigned* dn = nullptr)
 {
     *err = cudaSuccess;
     if (n <= 1) return 0;
@@ -248,11 +254,11 @@ inline int radix_sort_pairs(std::uint64_t* k0, std::uint32_t* v0, std::uint64_t*
         std::uint32_t* vi = cur ? v1 : v0;
         std::uint64_t* ko = cur ? k0 : k1;
         std::uint32_t* vo = cur ? v0 : v1;
-        radix_hist<<<tiles, kSortThreads, 0, st>>>(ki, n, shift, hist, tiles);
+        radix_hist<<<tiles, kSortThreads, 0, st>>>(ki, n, shift, hist, tiles, dn);
         *err = exclusive_scan<std::uint32_t, std::uint32_t>(hist, static_cast<std::int64_t>(tiles) * 256, offs,
                                                             static_cast<std::uint32_t*>(nullptr), ws, st);
         if (*err != cudaSuccess) return cur;
-        radix_scatter<<<tiles, kSortThreads, 0, st>>>(ki, vi, n, shift, offs, tiles, ko, vo);
+        radix_scatter<<<tiles, kSortThreads, 0, st>>>(ki, vi, n, shift, offs, tiles, ko, vo, dn);
         cur ^= 1;
     }
     ws.used = mark;
