@@ -7,18 +7,20 @@ bc "nnon"; K log-uniform 1e-6..1e-4, m uniform 0.35..0.6, n from {1, 1.5,
 2}, D log-uniform 1e-3..1e-1 m^2/yr, U log-uniform 1e-4..1e-2 m/yr, dt =
 1000 yr; initial surfaces seeded uniform noise 0-1 m plus a 0.001 tilt
 toward the open south edge. One step advances every member by one LEM step:
-fill_pits(1e-4) -> D8 receivers -> s-vector / contributing counts -> implicit
+fill_pits(1e-4, in the reference's FIFO order, bit for bit) -> D8 receivers
+-> s-vector / contributing counts -> implicit
 stream power (per-node Newton for n != 1) -> linear implicit hillslope by
 Jacobi-PCG to a 1e-8 relative residual -> uplift and boundary restore. The
 metric is member cells advanced per second (cell-steps/s).
 
 The same line reports:
   * plain_gpu: the members stepped one at a time through the single-grid
-    LEM (lsdtt_gpu_lem_step), on a sample of members -- the plain GPU form;
+    LEM (lsdtt_gpu_lem_step), all of them -- the plain GPU form;
   * e2e: the ensemble stepped through the C ABI with the packed surfaces
     uploaded from and downloaded to pinned host memory every step;
-  * roofline: the dominant kernel of a profiled (eager) step of the same
-    ensemble, algorithmic bytes over its CUDA-event time;
+  * kernels / roofline: every kernel (and the exact fill's stages) of a
+    profiled (eager) step of the same ensemble, and the dominant single
+    kernel's algorithmic bytes over its CUDA-event time;
   * cpu_baseline: the C++/numpy restatement of the reference (oracle/) on a
     bounded sample of members, on the host cores.
 
