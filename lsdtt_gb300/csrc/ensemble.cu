@@ -1555,6 +1555,7 @@ struct lsdtt_gpu_ensemble
     ExBuffers exB{};
     int ex_mbits = 0;
     bool ex_any = false;  // some member fills with min_slope > 0
+    int ex_on = 0;        // members that fill with min_slope > 0
     int sms = 152;
     std::uint8_t *mask = nullptr, *kind = nullptr, *bflag = nullptr, *dirty = nullptr, *oflag = nullptr;
     std::int32_t* flist = nullptr;           // [kFillColours][T] active fill tiles of the current pass
@@ -1938,7 +1939,7 @@ cudaError_t run_step(lsdtt_gpu_ensemble* E, cudaStream_t st, bool eager, StepRec
         if (e != cudaSuccess) return e;
         // (each stage is timed inside, as ens_fill_exact_*)
         e = ex_run(E->d_exm, E->blk_member, N, M, E->ex_mbits, E->z, E->kind, E->zf0, E->zf, E->exB, E->exws, E->sms,
-                   st, true);
+                   st, true, E->ex_on);
         if (e != cudaSuccess) return e;
         ens_flag_copy_u<<<1, 1, 0, st>>>(E->exB.u + 5, E->flags + 8);
     }
@@ -2683,7 +2684,11 @@ int lsdtt_gpu_ensemble_create(const lsdtt_gpu_member* members, int32_t n_members
             x.per_ns = q.per_ns;
             x.per_ew = q.per_ew;
             x.on = (q.fill_on && q.fill_eps > 0.0f) ? 1 : 0;
-            if (x.on) E->ex_any = true;
+            if (x.on)
+            {
+                E->ex_any = true;
+                ++E->ex_on;
+            }
             fifo_total += cap;
         }
         while ((1 << E->ex_mbits) < n_members) ++E->ex_mbits;

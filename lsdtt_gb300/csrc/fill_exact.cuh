@@ -11,8 +11,8 @@
 //   4. the valid cells of each member sorted by (F0, index);
 //   5. every candidate replayed by one warp with its state in shared memory
 //      (three sizes, each taking the overflows of the one before; the two
-//      larger only when the members are fewer than the SMs); raised cells
-//      staged in a pool;
+//      larger only when the members that fill are fewer than the SMs);
+//      raised cells staged in a pool;
 //   6. per member, one block follows the chain of valid windows from the
 //      lowest cut; a window on it that no size could hold is replayed by
 //      the whole block one FIFO sweep at a time (fill_sweep.cuh), or, where
@@ -565,11 +565,13 @@ inline cudaError_t ex_setup()
 // profiling on, each stage is timed under its name (`ens`: the ensemble's
 // names) with its algorithmic bytes: the records and keys it reads and
 // writes once per cell; the replays count one 16-byte record per cell,
-// though they are bound by the latency of their dependent steps.
+// though they are bound by the latency of their dependent steps. `n_on` =
+// the members whose fill is on (their chains are the ones that work).
 inline cudaError_t ex_run(const ExMember* mem, const std::uint16_t* blk_member, std::int64_t N, int M, int mbits,
                           const float* z, const std::uint8_t* kind, const float* F0, float* F, const ExBuffers& B,
-                          Scratch& ws, int sms, cudaStream_t st, bool ens = false)
+                          Scratch& ws, int sms, cudaStream_t st, bool ens = false, int n_on = -1)
 {
+    if (n_on < 0) n_on = M;
     static const char* const kNames[2][9] = {
         {"fill_exact_prep", "fill_exact_levels", "fill_exact_candidates", "fill_exact_cell_sort",
          "fill_exact_windows_small", "fill_exact_windows_mid", "fill_exact_windows_large", "fill_exact_chain",
@@ -639,16 +641,16 @@ inline cudaError_t ex_run(const ExMember* mem, const std::uint16_t* blk_member, 
     // replays: small shared-memory size, then two larger ones for the
     // overflows of the one before (the sizes trade room for warps per SM:
     // 20, 7 and 3); wl is free again once the middle size has its list.
-    // The larger sizes pay only where the chains are few: with a member per
-    // SM or more, the chains' block sweeps replay the windows the small size
-    // could not hold -- only those on a chain, where the larger sizes replay
-    // every such candidate one pop at a time -- and the step is faster
-    // without them (256 members: 358 ms a step with them, 234 ms without;
-    // one 2048 x 2048 grid: 498 ms with them, 779 ms without)
+    // The larger sizes pay only where the chains are few: with a filling
+    // member per SM or more, the chains' block sweeps replay the windows the
+    // small size could not hold -- only those on a chain, where the larger
+    // sizes replay every such candidate one pop at a time -- and the step
+    // is faster without them (256 members: 358 ms a step with them, 234 ms
+    // without; one 2048 x 2048 grid: 498 ms with them, 779 ms without)
     LSDTT_TIMED(nm[4], 16.0 * cells, st,
                 (ex_windows<kExA_FQ, kExA_DH, kExA_HS, kExA_OC><<<sms * 20, 32, kExSmemA, st>>>(
                     mem, z, kind, F0, B, B.wl, B.u + 1, B.u + 2, static_cast<unsigned long long>(N), 16ull * kExA_HS)));
-    if (M < sms)
+    if (n_on < sms)
     {
         LSDTT_TIMED(nm[5], 16.0 * cells, st,
                     (ex_overflow_list<<<nb, 256, 0, st>>>(N, B.wl, B.u + 1, B.wl2, B.u + 3, B.status),
