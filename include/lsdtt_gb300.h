@@ -98,7 +98,14 @@ int lsdtt_gpu_selftest_mbarrier_wait(int32_t tries);
  * Replaces fill_pits(const lsdtt_raster_cpu&, float min_slope,
  * const std::string& bc, int n_threads, priority_flood_queue_backend)
  * (src/cpu/lsdtt_raster_flow_preprocessing_cpu.hpp:191-199,
- *  .cpp:727-782). Output cells that are masked or nodata hold no_data_value. */
+ *  .cpp:727-782). Output cells that are masked or nodata hold no_data_value.
+ * The result is the reference's priority flood in its own order (each raised
+ * cell takes its value from its first-popped neighbour, the FIFO front taken
+ * when it is at most the heap top), bit for bit, except that heap entries of
+ * equal value are taken in (row, col) order where the reference's heap
+ * layout decides. Errors: LSDTT_GPU_EINVAL (arguments), LSDTT_GPU_ETIMEOUT
+ * (the relaxation did not converge), LSDTT_GPU_EOVERFLOW (a window replay
+ * outgrew its arrays). */
 int lsdtt_gpu_fill_pits(const lsdtt_gpu_grid* grid, const float* z_dev, const uint8_t* mask_dev,
                         float min_slope, float* filled_dev, void* stream);
 
