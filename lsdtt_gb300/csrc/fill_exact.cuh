@@ -655,11 +655,13 @@ inline cudaError_t ex_run(const ExMember* mem, const std::uint16_t* blk_member, 
         LSDTT_TIMED(nm[5], 16.0 * cells, st,
                     (ex_overflow_list<<<nb, 256, 0, st>>>(N, B.wl, B.u + 1, B.wl2, B.u + 3, B.status),
                      ex_windows<kExM_FQ, kExM_DH, kExM_HS, kExM_OC><<<sms * 7, 32, kExSmemM, st>>>(
-                         mem, z, kind, F0, B, B.wl2, B.u + 3, B.u + 4, static_cast<unsigned long long>(N), 16ull * kExM_HS)));
+                         mem, z, kind, F0, B, B.wl2, B.u + 3, B.u + 4, static_cast<unsigned long long>(N),
+                         16ull * kExM_HS)));
         LSDTT_TIMED(nm[6], 16.0 * cells, st,
                     (ex_overflow_list<<<nb, 256, 0, st>>>(N, B.wl2, B.u + 3, B.wl, B.u + 6, B.status),
                      ex_windows<kExB_FQ, kExB_DH, kExB_HS, kExB_OC><<<sms * 3, 32, kExSmemB, st>>>(
-                         mem, z, kind, F0, B, B.wl, B.u + 6, B.u + 7, static_cast<unsigned long long>(N), 16ull * kExB_HS)));
+                         mem, z, kind, F0, B, B.wl, B.u + 6, B.u + 7, static_cast<unsigned long long>(N),
+                         16ull * kExB_HS)));
     }
     LSDTT_TIMED(nm[7], 16.0 * cells, st,
                 (ex_chain<kExC_FQ, kExC_DH><<<M, kSwThreads, kExSmemC, st>>>(mem, z, kind, F0, F, B)));

@@ -240,7 +240,9 @@ inline raster_grid read_envi(const std::string& data_path, const std::string& hd
     g.meta.n_cols = need_int("samples");
     g.meta.n_rows = need_int("lines");
     const int bands = get("bands") ? std::stoi(*get("bands")) : 1;
-    if (bands != 1) throw std::runtime_error("raster_io: " + data_path + " has " + std::to_string(bands) + " bands; one is supported");
+    if (bands != 1)
+        throw std::runtime_error("raster_io: " + data_path + " has " + std::to_string(bands) +
+                                 " bands; one is supported");
     const std::size_t offset = get("header offset") ? static_cast<std::size_t>(std::stoll(*get("header offset"))) : 0;
     const int type = need_int("data type");
     const bool little = !(get("byte order") && std::stoi(*get("byte order")) == 1);
@@ -291,8 +293,18 @@ inline raster_grid read_gridfloat(const std::string& data_path, const std::strin
         k = lower(k);
         if (k == "ncols") g.meta.n_cols = std::stoi(v);
         else if (k == "nrows") g.meta.n_rows = std::stoi(v);
-        else if (k == "xllcorner" || k == "xllcenter") { xll = std::stod(v); centre_x = k == "xllcenter"; have_x = true; }
-        else if (k == "yllcorner" || k == "yllcenter") { yll = std::stod(v); centre_y = k == "yllcenter"; have_y = true; }
+        else if (k == "xllcorner" || k == "xllcenter")
+        {
+            xll = std::stod(v);
+            centre_x = k == "xllcenter";
+            have_x = true;
+        }
+        else if (k == "yllcorner" || k == "yllcenter")
+        {
+            yll = std::stod(v);
+            centre_y = k == "yllcenter";
+            have_y = true;
+        }
         else if (k == "cellsize") g.meta.cell_size = std::stod(v);
         else if (k == "nodata_value") g.meta.no_data_value = std::stod(v);
         else if (k == "byteorder") little = lower(v) != "msbfirst";
