@@ -1,6 +1,7 @@
 """The GDAL-free raster I/O of the host layer (lsdtt_gb300/host/raster_io.hpp)
 through its command-line driver tests/raster_io_check.cpp, compiled here
-with g++: round trips through both formats it writes (ENVI .bil and ESRI
+with g++, and its Python counterpart (lsdtt_gb300/raster_io.py), held to
+it: round trips through both formats they write (ENVI .bil and ESRI
 GridFloat), headers written by hand in the ways other tools write them
 (big-endian float64 and int16 ENVI bands, a header offset, a reference pixel
 other than the first, a CRS string over several lines, cell-centre corners,
@@ -157,3 +158,59 @@ def test_refusals(rio, tmp_path):
     open(tmp_path / "s.hdr", "w").write("ncols 4\nnrows 4\nxllcorner 0\nyllcorner 0\ncellsize 1\n")
     _, _, _, p = _read(rio, tmp_path / "s.flt", tmp_path)
     assert p.returncode == 3 and "shorter" in p.stderr
+
+
+def _same(py, cpp):
+    """The Python module's (data, mask, RasterMeta) equals the C++ driver's
+    (data, mask, meta dict)."""
+    da, ma, mta = py
+    db, mb, mtb = cpp
+    assert np.array_equal(da.view(np.uint32), db.view(np.uint32))
+    assert np.array_equal(ma, mb)
+    for k in ("n_rows", "n_cols", "x_min", "y_min", "cell_size", "no_data_value", "crs_wkt"):
+        assert getattr(mta, k) == mtb[k], k
+
+
+def test_python_module_matches_the_cpp_header(rio, tmp_path):
+    """lsdtt_gb300.raster_io (numpy) and host/raster_io.hpp read every file
+    of the tests above alike, and each reads what the other writes."""
+    from lsdtt_gb300 import raster_io as R
+    z = _surface(23, 31, 4)
+    wkt = 'PROJCS["x",GEOGCS["y"]]'
+    # C++ writes, Python reads
+    for fmt, name in (("envi", "c.bil"), ("esri", "c.flt")):
+        p = _write(rio, z, tmp_path / name, 1000.5, 2000.25, 5.0, -9999.0, fmt, tmp_path,
+                   wkt if fmt == "envi" else None)
+        assert p.returncode == 0, p.stderr
+        data, mask, meta, p = _read(rio, tmp_path / name, tmp_path)
+        py = R.read_raster(str(tmp_path / name))
+        _same(py, (data, mask, meta))
+    # Python writes, C++ reads
+    for fmt, name in (("envi", "p.bil"), ("esri", "p.flt")):
+        m = R.RasterMeta(23, 31, 1000.5, 2000.25, 5.0, -9999.0, wkt if fmt == "envi" else "")
+        R.write_raster(str(tmp_path / name), z, m, fmt)
+        data, mask, meta, p = _read(rio, tmp_path / name, tmp_path)
+        assert p.returncode == 0, p.stderr
+        _same(R.read_raster(str(tmp_path / name)), (data, mask, meta))
+        want, wmask = _expected(z, -9999.0)
+        assert np.array_equal(data.view(np.uint32), want.view(np.uint32)) and np.array_equal(mask, wmask)
+        assert (meta["x_min"], meta["y_min"], meta["cell_size"], meta["crs_wkt"]) == (1000.5, 2000.25, 5.0, m.crs_wkt)
+    # a foreign ENVI header: big-endian float64 after an offset, reference pixel (2, 3), CRS over two lines
+    zz = _surface(11, 7, 2).astype(np.float64)
+    open(tmp_path / "e.bsq", "wb").write(b"\0" * 16 + zz.astype(">f8").tobytes())
+    open(tmp_path / "e.hdr", "w").write(
+        "ENVI\nsamples = 7\nlines = 11\nbands = 1\nheader offset = 16\ndata type = 5\nbyte order = 1\n"
+        "map info = {UTM, 2, 3, 500030.0, 4200000.0, 30.0, 30.0, 30, North}\n"
+        "coordinate system string = {PROJCS[\"a\",\n GEOGCS[\"b\"]]}\ndata ignore value = -9999\n")
+    data, mask, meta, p = _read(rio, tmp_path / "e.bsq", tmp_path)
+    _same(R.read_raster(str(tmp_path / "e.bsq")), (data, mask, meta))
+    # refusals
+    np.zeros((4, 4), "<f4").tofile(tmp_path / "n.bil")
+    open(tmp_path / "n.hdr", "w").write("ENVI\nsamples = 4\nlines = 4\nbands = 1\ndata type = 4\n"
+                                        "map info = {Arbitrary, 1, 1, 0, 40, 10, 20}\n")
+    with pytest.raises(ValueError, match="non-square"):
+        R.read_raster(str(tmp_path / "n.bil"))
+    np.zeros((3, 4), "<f4").tofile(tmp_path / "s.flt")
+    open(tmp_path / "s.hdr", "w").write("ncols 4\nnrows 4\nxllcorner 0\nyllcorner 0\ncellsize 1\n")
+    with pytest.raises(ValueError, match="shorter"):
+        R.read_raster(str(tmp_path / "s.flt"))
