@@ -6,7 +6,7 @@ one-warp replay) or one FIFO sweep at a time with pop times as a fixed point
 (row, col) heap ties bit for bit, and the two replays agree window by window,
 on the surfaces the GPU tests use (a noise-plus-tilt surface, one long
 episode; pitted fractals, many short ones; periodic axes; a filled surface
-with fresh erosion pits)."""
+with fresh erosion pits; interior nodata holes)."""
 import ctypes
 import os
 import shutil
@@ -32,19 +32,20 @@ def model(tmp_path_factory):
     lib = ctypes.CDLL(so)
     f = lib.window_model_fill
     f.restype = ctypes.c_int
-    f.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float,
-                  ctypes.c_float, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    f.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                  ctypes.c_float, ctypes.c_float, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
     return f
 
 
-def _fill(model, z, bc, cell, eps, mode):
+def _fill(model, z, m, bc, cell, eps, mode):
     z = np.ascontiguousarray(z, np.float32)
+    m = np.ascontiguousarray(m, np.uint8)
     out = np.empty_like(z)
     st = np.zeros(5, np.int64)
     per_ns = bc[0] in "pP"
     per_ew = bc[1] in "pP"
-    rc = model(z.ctypes.data, z.shape[0], z.shape[1], int(per_ns), int(per_ew), cell, eps, mode, out.ctypes.data,
-               st.ctypes.data)
+    rc = model(z.ctypes.data, m.ctypes.data, z.shape[0], z.shape[1], int(per_ns), int(per_ew), cell, eps, mode,
+               out.ctypes.data, st.ctypes.data)
     assert rc == 0, rc
     return out, st
 
@@ -57,26 +58,35 @@ def _cases(port):
     z4 = port.fill_pits(z1, one(z1), 30.0, "nnon", 1e-4)
     rng = np.random.default_rng(21)
     z4 = (z4 - (rng.random(z4.shape) < 0.08) * rng.random(z4.shape).astype(np.float32) * 0.02).astype(np.float32)
-    return [("noise_tilt_96x128", z1, "nnon", 30.0, 1e-4), ("fractal_pits_96", z2, "oooo", 10.0, 1e-4),
-            ("fractal_popo_40x56", z3, "popo", 10.0, 1e-4), ("fractal_opop_40x56", z3, "opop", 10.0, 1e-3),
-            ("lem_like_96x128", z4, "nnon", 30.0, 1e-4)]
+    z5 = surfaces.fractal_pits(80, seed=9)
+    m5 = one(z5)
+    m5[20:31, 10:27] = 0
+    m5[50:53, 40:66] = 0
+    return [("noise_tilt_96x128", z1, one(z1), "nnon", 30.0, 1e-4),
+            ("fractal_pits_96", z2, one(z2), "oooo", 10.0, 1e-4),
+            ("fractal_popo_40x56", z3, one(z3), "popo", 10.0, 1e-4),
+            ("fractal_opop_40x56", z3, one(z3), "opop", 10.0, 1e-3),
+            ("lem_like_96x128", z4, one(z4), "nnon", 30.0, 1e-4),
+            ("fractal_holes_80", z5, m5, "oooo", 10.0, 1e-4)]
 
 
 def test_chained_windows_equal_the_priority_flood(model, port):
-    for name, z, bc, cell, eps in _cases(port):
-        want = port.fill_pits_index_ties(z, np.ones_like(z, np.uint8), cell, bc, eps)
-        got, st = _fill(model, z, bc, cell, eps, 0)
-        nd = int((got.view(np.uint32) != want.view(np.uint32)).sum())
-        print(f"{name}: {int((want != z).sum())} raised cells, {st[0]} cuts, {st[1]} candidates, "
+    for name, z, m, bc, cell, eps in _cases(port):
+        want = port.fill_pits_index_ties(z, m, cell, bc, eps)
+        got, st = _fill(model, z, m, bc, cell, eps, 0)
+        v = m != 0
+        nd = int((got[v].view(np.uint32) != want[v].view(np.uint32)).sum())
+        print(f"{name}: {int(((want != z) & (m != 0)).sum())} raised cells, {st[0]} cuts, {st[1]} candidates, "
               f"{st[2]} windows on the chain; {nd} cells differ")
         assert nd == 0, name
 
 
 def test_sweep_replays_equal_the_sequential_replays(model, port):
-    for name, z, bc, cell, eps in _cases(port):
-        want = port.fill_pits_index_ties(z, np.ones_like(z, np.uint8), cell, bc, eps)
-        got, st = _fill(model, z, bc, cell, eps, 2)
+    for name, z, m, bc, cell, eps in _cases(port):
+        want = port.fill_pits_index_ties(z, m, cell, bc, eps)
+        got, st = _fill(model, z, m, bc, cell, eps, 2)
         assert st[3] == 0, (name, int(st[3]))
-        sw, _ = _fill(model, z, bc, cell, eps, 1)
+        sw, _ = _fill(model, z, m, bc, cell, eps, 1)
         print(f"{name}: {st[4]} sweeps over {st[2]} windows, every window alike")
-        assert np.array_equal(sw.view(np.uint32), want.view(np.uint32)), name
+        v = m != 0
+        assert np.array_equal(sw[v].view(np.uint32), want[v].view(np.uint32)), name

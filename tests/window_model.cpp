@@ -3,10 +3,12 @@
 // windows cut at epsilon-0 pour levels, chained from the lowest cut, each
 // replayed either by the sequential rules (the one-warp replay) or by FIFO
 // sweeps whose pop times are a fixed point (the block replay). Plain
-// containers, no attempt at speed; grids without nodata (seeds are the cells
-// on non-periodic edges). tests/test_window_model.py holds its result to the
-// oracle's priority flood with (row, col) heap ties, bit for bit, and the two
-// replays to each other window by window.
+// containers, no attempt at speed. Seeds as the reference seeds them: the
+// valid cells on non-periodic edges, and, when the interior holds nodata,
+// the valid cells next to a nodata cell; nodata cells are never queued.
+// tests/test_window_model.py holds its result to the oracle's priority flood
+// with (row, col) heap ties, bit for bit, and the two replays to each other
+// window by window.
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
@@ -30,6 +32,9 @@ struct Grid
 {
     int nr, nc;
     bool per_ns, per_ew;
+    const std::uint8_t* valid;  // null: every cell valid
+    std::vector<char> seeds;
+    bool ok(std::size_t i) const { return !valid || valid[i] != 0; }
     bool nb(int r, int c, int d, int& rr, int& cc) const
     {
         rr = r + kDr[d];
@@ -38,9 +43,31 @@ struct Grid
         if (per_ew) { if (cc < 0) cc += nc; else if (cc >= nc) cc -= nc; }
         return rr >= 0 && rr < nr && cc >= 0 && cc < nc;
     }
-    bool seed(int r, int c) const
+    bool seed(int r, int c) const { return seeds[static_cast<std::size_t>(r) * nc + c] != 0; }
+    // the reference's seeding (raster_flow_preprocessing_cpu.cpp:518-589):
+    // valid cells on a non-periodic edge, and next to an in-bounds nodata
+    // cell when the interior holds any nodata
+    void make_seeds()
     {
-        return (!per_ns && (r == 0 || r == nr - 1)) || (!per_ew && (c == 0 || c == nc - 1));
+        seeds.assign(static_cast<std::size_t>(nr) * nc, 0);
+        bool interior = false;
+        for (int r = 1; r < nr - 1 && !interior; ++r)
+            for (int c = 1; c < nc - 1; ++c)
+                if (!ok(static_cast<std::size_t>(r) * nc + c)) { interior = true; break; }
+        for (int r = 0; r < nr; ++r)
+            for (int c = 0; c < nc; ++c)
+            {
+                const std::size_t i = static_cast<std::size_t>(r) * nc + c;
+                if (!ok(i)) continue;
+                bool s = (!per_ns && (r == 0 || r == nr - 1)) || (!per_ew && (c == 0 || c == nc - 1));
+                for (int d = 0; d < 8 && !s && interior; ++d)
+                {
+                    const int rr = r + kDr[d], cc = c + kDc[d];
+                    if (rr >= 0 && rr < nr && cc >= 0 && cc < nc && !ok(static_cast<std::size_t>(rr) * nc + cc))
+                        s = true;
+                }
+                seeds[i] = s ? 1 : 0;
+            }
     }
 };
 
@@ -101,7 +128,7 @@ std::vector<float> flood(const float* z, const Grid& g, float L, float eps, bool
             int rr, cc;
             if (!g.nb(r, c, d, rr, cc)) continue;
             const std::uint32_t j = static_cast<std::uint32_t>(rr * g.nc + cc);
-            if (state[j]) continue;
+            if (state[j] || !g.ok(j)) continue;
             if (F[j] <= cur.z)
             {
                 F[j] = eps > 0.0f ? raise_from(cur.z, eps, (d & 1) ? Ld : L) : cur.z;
@@ -139,6 +166,7 @@ Setup setup(const float* z, const Grid& g, float L, float eps)
         for (int c = 0; c < g.nc; ++c)
         {
             const std::size_t i = static_cast<std::size_t>(r) * g.nc + c;
+            if (!g.ok(i)) continue;  // never queued (mnb stays +inf)
             float m = std::numeric_limits<float>::infinity();
             bool pour = false;
             for (int d = 0; d < 8; ++d)
@@ -146,6 +174,7 @@ Setup setup(const float* z, const Grid& g, float L, float eps)
                 int rr, cc;
                 if (!g.nb(r, c, d, rr, cc)) continue;
                 const std::size_t b = static_cast<std::size_t>(rr) * g.nc + cc;
+                if (!g.ok(b)) continue;
                 m = std::min(m, X.F0[b]);
                 // a pour level: c at or below F0(c), next to b with z(b) = F0(b) = F0(c)
                 if (z[i] <= X.F0[i] && z[b] == X.F0[b] && X.F0[b] == X.F0[i]) pour = true;
@@ -176,8 +205,8 @@ Setup setup(const float* z, const Grid& g, float L, float eps)
         acc += diff[k];
         X.cand[k] = (k == 0 || acc == 0) ? 1 : 0;
     }
-    X.sorted.resize(X.n);
-    for (std::size_t i = 0; i < X.n; ++i) X.sorted[i] = static_cast<std::uint32_t>(i);
+    for (std::size_t i = 0; i < X.n; ++i)
+        if (g.ok(i)) X.sorted.push_back(static_cast<std::uint32_t>(i));
     std::sort(X.sorted.begin(), X.sorted.end(),
               [&](std::uint32_t a, std::uint32_t b) { return key_less({X.F0[a], a}, {X.F0[b], b}); });
     return X;
@@ -217,8 +246,8 @@ struct List
     std::size_t p;
     bool head(Key& k)
     {
-        while (p < X.n && !(X.mnb[X.sorted[p]] < S)) ++p;
-        if (p >= X.n) return false;
+        while (p < X.sorted.size() && !(X.mnb[X.sorted[p]] < S)) ++p;
+        if (p >= X.sorted.size()) return false;
         k = {X.F0[X.sorted[p]], X.sorted[p]};
         return true;
     }
@@ -276,7 +305,7 @@ int replay_sequential(const Setup& X, int w, Outputs& out)
             int rr, cc;
             if (!X.g.nb(r, c, d, rr, cc)) continue;
             const std::uint32_t j = static_cast<std::uint32_t>(rr * X.g.nc + cc);
-            if (X.F0[j] < S || X.mnb[j] < S || !seen.insert(j).second) continue;
+            if (!X.g.ok(j) || X.F0[j] < S || X.mnb[j] < S || !seen.insert(j).second) continue;
             if (X.z[j] <= cur.z) fifo.push_back({raise_from(cur.z, X.eps, (d & 1) ? X.Ld : X.L), j});
             else heap.push({X.z[j], j});
         }
@@ -311,7 +340,7 @@ int replay_sweeps(const Setup& X, int w, Outputs& out, long long* sweeps)
     Front front{X, S, w + 1};
     std::unordered_map<std::uint32_t, int> state;  // 1 heap, 2 FIFO, 3 popped (list cells: by p)
     auto st = [&](std::uint32_t j) { const auto it = state.find(j); return it == state.end() ? 0 : it->second; };
-    auto open = [&](std::uint32_t j) { return X.F0[j] >= S && !(X.mnb[j] < S) && st(j) == 0; };
+    auto open = [&](std::uint32_t j) { return X.g.ok(j) && X.F0[j] >= S && !(X.mnb[j] < S) && st(j) == 0; };
     MinHeap heap;  // discovered heap cells (stale entries skipped by state)
     auto heap_top = [&](Key& k) {
         while (!heap.empty() && st(heap.top().i) != 1) heap.pop();
@@ -488,15 +517,17 @@ int replay_sweeps(const Setup& X, int w, Outputs& out, long long* sweeps)
 
 }  // namespace
 
-// The fill by chained windows. mode 0: sequential replays; 1: sweeps; 2:
-// both, compared window by window (stats[3] counts windows that differ).
+// The fill by chained windows (`valid` null: every cell valid; nodata cells
+// keep their input). mode 0: sequential replays; 1: sweeps; 2: both,
+// compared window by window (stats[3] counts windows that differ).
 // stats: [0] cuts, [1] candidates, [2] windows on the chain, [3] windows
 // whose two replays differ, [4] sweeps. Returns 0, or 1 if a chain did not
 // advance, 2 if a sweep found no fixed point.
-extern "C" int window_model_fill(const float* z, int nr, int nc, int per_ns, int per_ew, float L, float eps, int mode,
-                                 float* out, long long* stats)
+extern "C" int window_model_fill(const float* z, const std::uint8_t* valid, int nr, int nc, int per_ns, int per_ew,
+                                 float L, float eps, int mode, float* out, long long* stats)
 {
-    const Grid g{nr, nc, per_ns != 0, per_ew != 0};
+    Grid g{nr, nc, per_ns != 0, per_ew != 0, valid, {}};
+    g.make_seeds();
     const Setup X = setup(z, g, L, eps);
     std::memcpy(out, z, sizeof(float) * X.n);
     const int ncut = static_cast<int>(X.cuts.size());
